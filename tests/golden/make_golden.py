@@ -1,0 +1,534 @@
+"""
+Generate golden vectors by running the reference (Fractalshades 1.2.1) itself.
+
+The reference cannot run as shipped here: numba, gmpy2 and PIL are absent.
+This script imports it from its source tree with three stand-ins:
+
+* ``numba``: ``njit``/``jit`` become identity decorators, so the reference's
+  hot-path functions run as plain Python, statement for statement;
+* ``fractalshades.numpy_utils.numba_xr``: the four functions the hot path calls
+  (``to_standard``, ``to_Xrange_scalar``, ``extended_abs2``, ``one``) are
+  mapped onto the reference's own host ``Xrange_array`` class
+  (``numpy_utils/xrange.py``), whose arithmetic the numba extension mirrors;
+* ``PIL`` and the Cython module ``mpmath_utils/FP_loop``: unused stubs.  The
+  reference orbit is computed here in mpmath with the recurrence of
+  ``FP_loop.pyx:274-421`` and stored through the reference's own
+  ``save_ref_point`` so that ``get_FP_orbit`` reuses it.
+
+Two lowering rules of numba are applied to the reference modules when they are
+loaded (an AST rewrite, nothing else changes): ``x ** 2`` with a literal
+integer exponent becomes ``x * x`` (numba's static power), and ``abs`` /
+``np.abs`` of a complex scalar becomes the C library's ``hypot(re, im)``
+(numba's complex abs).  Plain CPython would call libm ``pow`` and numpy's vectorised complex
+abs, which are not always correctly rounded and differ from numba in the last
+bit.
+
+Everything else -- pixel grid (``chunk_pixel_pos``), ``get_cycle_indep_args``,
+the derivative paths, ``ref_point_kc``, the BLA tree, ``numba_cycles`` /
+``numba_cycles_perturb(_BS)`` -- is the reference's code.  Python evaluates each
+floating point operation once, in source order, with IEEE rounding, which is
+what the oracle restates (the jitted reference may contract some operations
+into FMAs under ``fastmath=True``).
+
+Usage: python tests/golden/make_golden.py [reference_src_dir]
+Writes tests/golden/*.npz (small fixtures, committed).
+"""
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+import mpmath
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+
+
+# --------------------------------------------------------------------------
+# Stand-ins
+# --------------------------------------------------------------------------
+class _Any:
+    def __init__(self, *a, **k):
+        pass
+
+    def __call__(self, *a, **k):
+        if len(a) == 1 and callable(a[0]) and not k:
+            return a[0]
+        return _Any()
+
+    def __getattr__(self, name):
+        return _Any()
+
+    def __getitem__(self, k):
+        return _Any()
+
+    def __iter__(self):
+        return iter(())
+
+
+def _njit(*a, **k):
+    if len(a) == 1 and callable(a[0]) and not k:
+        return a[0]
+    return lambda f: f
+
+
+class _NumbaLowering(__import__("ast").NodeTransformer):
+    """x ** 2 -> x * x ; abs(z) / np.abs(z) -> _nb_abs(z)."""
+
+    def visit_BinOp(self, node):
+        import ast
+        self.generic_visit(node)
+        if (isinstance(node.op, ast.Pow) and isinstance(node.right, ast.Constant)
+                and node.right.value == 2 and isinstance(node.left, (
+                    ast.Name, ast.Subscript, ast.Attribute))):
+            return ast.copy_location(
+                ast.BinOp(left=node.left, op=ast.Mult(), right=node.left), node)
+        return node
+
+    def visit_Call(self, node):
+        import ast
+        self.generic_visit(node)
+        f = node.func
+        is_abs = isinstance(f, ast.Name) and f.id == "abs"
+        is_npabs = (isinstance(f, ast.Attribute) and f.attr == "abs"
+                    and isinstance(f.value, ast.Name) and f.value.id == "np")
+        if (is_abs or is_npabs) and len(node.args) == 1:
+            node.func = ast.copy_location(ast.Name(id="_nb_abs", ctx=ast.Load()), f)
+        return node
+
+
+def _libm_hypot():
+    import ctypes
+    import ctypes.util
+    libm = ctypes.CDLL(ctypes.util.find_library("m"))
+    libm.hypot.argtypes = [ctypes.c_double, ctypes.c_double]
+    libm.hypot.restype = ctypes.c_double
+    return libm.hypot
+
+
+_HYPOT = _libm_hypot()
+
+
+def _nb_abs(x):
+    # numba lowers abs(complex) to a call of the C library's hypot
+    # (CPython's math.hypot is a different algorithm)
+    if isinstance(x, (complex, np.complexfloating)):
+        return np.float64(_HYPOT(float(x.real), float(x.imag)))
+    if isinstance(x, (float, np.floating, int, np.integer)):
+        return abs(x)
+    return np.abs(x)
+
+
+def _install_lowering_loader():
+    import ast
+    import builtins
+    import importlib.abc
+    import importlib.machinery
+    builtins._nb_abs = _nb_abs
+
+    class Loader(importlib.machinery.SourceFileLoader):
+        def source_to_code(self, data, path, *, _optimize=-1):
+            tree = ast.parse(data, filename=path)
+            tree = ast.fix_missing_locations(_NumbaLowering().visit(tree))
+            return compile(tree, path, "exec", dont_inherit=True)
+
+        def get_code(self, fullname):
+            # never reuse a cached (unrewritten) bytecode file
+            return self.source_to_code(self.get_data(self.path), self.path)
+
+    class Finder(importlib.abc.MetaPathFinder):
+        def find_spec(self, name, path, target=None):
+            if not name.startswith("fractalshades"):
+                return None
+            spec = importlib.machinery.PathFinder.find_spec(name, path)
+            if spec is None or not str(spec.origin).endswith(".py"):
+                return spec
+            spec.loader = Loader(name, spec.origin)
+            return spec
+
+    sys.meta_path.insert(0, Finder())
+
+
+def install_shims():
+    _install_lowering_loader()
+    nb = types.ModuleType("numba")
+    nb.njit = nb.jit = nb.vectorize = nb.guvectorize = _njit
+    nb.complex128, nb.float64, nb.int32, nb.int64 = (
+        np.complex128, np.float64, np.int32, np.int64)
+    nb.bool_ = nb.boolean = np.bool_
+    nb.intp, nb.uint8, nb.int8 = np.intp, np.uint8, np.int8
+    nb.prange = range
+    nb.types = nb.core = nb.extending = nb.np = nb.cpython = _Any()
+    nb.from_dtype = lambda d: d
+    sys.modules["numba"] = nb
+    for sub in ["numba.core", "numba.core.types", "numba.core.cgutils",
+                "numba.extending", "numba.core.errors", "numba.np",
+                "numba.np.numpy_support", "numba.cpython",
+                "numba.cpython.unsafe", "numba.cpython.unsafe.numbers",
+                "numba.typed"]:
+        sys.modules[sub] = _Any()
+    pil = types.ModuleType("PIL")
+    pil.Image = _Any()
+    pil.PngImagePlugin = _Any()
+    sys.modules["PIL"] = pil
+    sys.modules["PIL.PngImagePlugin"] = pil.PngImagePlugin
+    sys.modules["PIL.Image"] = pil.Image
+
+    xrm = types.ModuleType("fractalshades.numpy_utils.numba_xr")
+
+    def _fsx():
+        import fractalshades.numpy_utils.xrange as fsx
+        return fsx
+
+    def to_standard(item):
+        fsx = _fsx()
+        if isinstance(item, fsx.Xrange_array):
+            return item.to_standard()[()]
+        return item
+
+    def to_Xrange_scalar(item):
+        fsx = _fsx()
+        if isinstance(item, fsx.Xrange_array):
+            return item
+        dt = np.complex128 if np.iscomplexobj(item) else np.float64
+        return fsx.Xrange_array(np.asarray(item, dtype=dt))
+
+    def extended_abs2(item):
+        fsx = _fsx()
+        if isinstance(item, fsx.Xrange_array):
+            return item.abs2()
+        return item.real ** 2 + item.imag ** 2
+
+    def one():
+        fsx = _fsx()
+        return fsx.Xrange_array(np.asarray(1., dtype=np.float64))
+
+    xrm.to_standard = to_standard
+    xrm.to_Xrange_scalar = to_Xrange_scalar
+    xrm.extended_abs2 = extended_abs2
+    xrm.one = one
+    sys.modules["fractalshades.numpy_utils.numba_xr"] = xrm
+
+    fp = types.ModuleType("fractalshades.mpmath_utils.FP_loop")
+    mu = types.ModuleType("fractalshades.mpmath_utils")
+    mu.FP_loop = fp
+    mu.__path__ = []
+    sys.modules["fractalshades.mpmath_utils"] = mu
+    sys.modules["fractalshades.mpmath_utils.FP_loop"] = fp
+    sys.path.insert(0, REF_SRC)
+
+
+install_shims()
+import fractalshades as fs                       # noqa: E402
+import fractalshades.models as fsm               # noqa: E402
+import fractalshades.numpy_utils.xrange as fsx   # noqa: E402
+
+
+# --------------------------------------------------------------------------
+# Helpers
+# --------------------------------------------------------------------------
+def mp_orbit(c, max_iter, M, need_xr, ref_orbit_len):
+    """mpmath restatement of FP_loop.pyx:274-421 (orbit stored as float64)."""
+    orbit = np.zeros(ref_orbit_len, dtype=np.complex128)
+    z = mpmath.mpc(0)
+    xr_dict = {}
+    i = 0
+    abs_i = 0.
+    for i in range(1, ref_orbit_len):
+        z = z * z + c
+        x, y = float(z.real), float(z.imag)
+        orbit[i] = complex(x, y)
+        abs_i = np.hypot(x, y)
+        if abs_i > M:
+            break
+        if need_xr and abs_i < fs.settings.xrange_zoom_level:
+            xr_dict[i] = fsx.mpc_to_Xrange(z)
+    if i == ref_orbit_len - 1 and abs_i <= M:
+        i += 1
+    return i, orbit, xr_dict
+
+
+def mp_nucleus(p, dps, seed_frac=0.):
+    """Newton for a period-p nucleus from a start outside the 1/p bulb root."""
+    with mpmath.workdps(dps):
+        th = 2 * mpmath.pi / p
+        c = mpmath.expj(th) / 2 - mpmath.expj(2 * th) / 4
+        c = c * (1 + mpmath.mpf(1) / (p * p) * (1 + seed_frac))
+        for _ in range(200):
+            z = mpmath.mpc(0)
+            d = mpmath.mpc(0)
+            for _k in range(p):
+                d = 2 * z * d + 1
+                z = z * z + c
+            dc = z / d
+            c = c - dc
+            if abs(dc) < mpmath.mpf(10) ** (-dps + 5):
+                break
+        return c
+
+
+def store_orbit(f, ref_point, order, max_iter, M):
+    """Store an orbit where the reference looks for it (perturbation.py:256-274)."""
+    ref_orbit_len = max_iter + 1
+    if order is not None:
+        ref_orbit_len = min(order, ref_orbit_len)
+    i, orbit, xr_dict = mp_orbit(ref_point, max_iter, 2 * M,
+                                 f.xr_detect_activated, ref_orbit_len)
+    init_kwargs = f.init_kwargs
+    del init_kwargs["directory"]
+    FP_params = {
+        "ref_point": ref_point, "dps": mpmath.mp.dps, "order": order,
+        "max_iter": max_iter, "FP_code": f.FP_code, "partials": {},
+        "xr": xr_dict, "div_iter": i, "init_kwargs": init_kwargs,
+        "ref_orbit_len": ref_orbit_len,
+    }
+    f.save_ref_point(FP_params, orbit)
+    return FP_params, orbit
+
+
+def xr_arrays(path):
+    """Split an Xrange_array into (mantissa, exp) numpy arrays."""
+    return np.asarray(path._mantissa), np.asarray(path._exp, dtype=np.int32)
+
+
+def run_tile(f, calc_name):
+    chunk = (0, f.nx, 0, f.ny)
+    (c_pix, Z, U, stop_reason, stop_iter), _ = f.get_cycling_dep_args(
+        calc_name, chunk)
+    cia = f._calc_data[calc_name]["cycle_indep_args"]
+    ret = f.numba_cycle_call((c_pix, Z, U, stop_reason, stop_iter), cia)
+    assert ret == 0
+    return c_pix, Z, U, stop_reason, stop_iter, cia
+
+
+# --------------------------------------------------------------------------
+# Cases
+# --------------------------------------------------------------------------
+def golden_std_m2(out):
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Mandelbrot(d)
+        f.zoom(x=-0.5, y=0., dx=3., nx=48, xy_ratio=4. / 3., theta_deg=0.)
+        f.calc_std_div(calc_name="std", subset=None, max_iter=400,
+                       M_divergence=1000., epsilon_stationnary=0.01)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+        np.savez_compressed(
+            out, pix=c_pix, Z=Z, stop_reason=sr, stop_iter=si,
+            center=np.array([-0.5, 0.]), lin_mat=f.lin_mat, dx=3.,
+            max_iter=400, M=1000., eps=0.01, nx=f.nx, ny=f.ny)
+
+
+def golden_std_bs(out):
+    res = {}
+    for flavor_int, flavor in enumerate(
+            ["Burning ship", "Perpendicular burning ship", "Shark fin",
+             "Celtic", "Buffalo"], start=1):
+        with tempfile.TemporaryDirectory() as d:
+            f = fsm.Burning_ship(d, flavor=flavor)
+            f.zoom(x=-0.5, y=-0.5, dx=3.5, nx=24, xy_ratio=1., theta_deg=0.)
+            f.calc_std_div(calc_name="std", subset=None, max_iter=200,
+                           M_divergence=1000.)
+            c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+            res[f"pix_{flavor_int}"] = c_pix
+            res[f"Z_{flavor_int}"] = Z
+            res[f"stop_reason_{flavor_int}"] = sr
+            res[f"stop_iter_{flavor_int}"] = si
+            res["lin_mat"] = f.lin_mat
+    np.savez_compressed(out, center=np.array([-0.5, -0.5]), dx=3.5,
+                        max_iter=200, M=1000., **res)
+
+
+def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
+                      interior, bla_eps=1e-6, eps_stat=1e-3, M=1000.,
+                      ref_shift=0j, x_offset="0"):
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Perturbation_mandelbrot(d)
+        x = str(mpmath.mpf(x) + mpmath.mpf(x_offset))
+        f.zoom(precision=precision, x=x, y=y, dx=dx, nx=nx, xy_ratio=1.,
+               theta_deg=0., projection=fs.projection.Cartesian())
+        ref_point = mpmath.mpc(x, y) + mpmath.mpc(ref_shift) * mpmath.mpf(dx)
+        f.max_iter = max_iter
+        f.M_divergence = M
+        FP_params, orbit = store_orbit(f, ref_point, order, max_iter, M)
+        f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
+                       M_divergence=M, epsilon_stationnary=eps_stat,
+                       BLA_eps=bla_eps, interior_detect=interior,
+                       calc_dzndc=True)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "pert")
+        (_, _, _, Zn_path, dZndc_path, dZndz_path, has_xr, ref_index_xr,
+         ref_xr, ref_div_iter, ref_order, drift_xr, dx_xr, _proj, lin_mat,
+         lin_scale_xr, kc, M_bla, r_bla, bla_len, stages_bla, _m, _i) = cia
+        xr = f.xr_detect_activated
+        res = dict(
+            pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si,
+            Zn=Zn_path, ref_div_iter=ref_div_iter, ref_order=ref_order,
+            xr_mode=int(xr), lin_mat=lin_mat,
+            dx_m=np.asarray(dx_xr._mantissa)[0],
+            dx_e=np.asarray(dx_xr._exp)[0],
+            drift_m=np.asarray(drift_xr._mantissa)[0],
+            drift_e=np.asarray(drift_xr._exp)[0],
+            kc_m=np.asarray(kc._mantissa)[0], kc_e=np.asarray(kc._exp)[0],
+            max_iter=max_iter, M=M, eps_stat=eps_stat, bla_eps=bla_eps,
+            interior=int(interior), codes=np.array(f.codes[0]),
+            M_bla=M_bla, r_bla=r_bla, stages_bla=stages_bla,
+            xr_idx=ref_index_xr,
+        )
+        m, e = xr_arrays(ref_xr)
+        res["xr_m"], res["xr_e"] = m, e
+        if xr:
+            res["dZndc_m"], res["dZndc_e"] = xr_arrays(dZndc_path)
+            if interior:
+                res["dZndz_m"], res["dZndz_e"] = xr_arrays(dZndz_path)
+        else:
+            res["dZndc"] = dZndc_path
+            if interior:
+                res["dZndz"] = dZndz_path
+        np.savez_compressed(out, **res)
+
+
+def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
+                      bla_eps=1e-6, M=1000.):
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Perturbation_burning_ship(d, flavor=flavor)
+        f.zoom(precision=precision, x=x, y=y, dx=dx, nx=nx, xy_ratio=1.,
+               theta_deg=0., projection=fs.projection.Cartesian())
+        ref_point = mpmath.mpc(x, y)
+        f.max_iter = max_iter
+        f.M_divergence = M
+        flavor_int = fs.models.burning_ship.get_flavor_int(flavor)
+        # BS orbit: perturbation_nonholomorphic_FP_loop (FP_loop.pyx:1828-1979)
+        ref_orbit_len = max_iter + 1
+        orbit = np.zeros(ref_orbit_len, dtype=np.complex128)
+        xn, yn = mpmath.mpf(0), mpmath.mpf(0)
+        a, b = ref_point.real, ref_point.imag
+        it = f.xnyn_iterate
+        i = 0
+        for i in range(1, ref_orbit_len):
+            xn, yn = it(xn, yn, a, b)
+            orbit[i] = complex(float(xn), float(yn))
+            if np.hypot(orbit[i].real, orbit[i].imag) > 2 * M:
+                break
+        if i == ref_orbit_len - 1 and np.hypot(orbit[i].real, orbit[i].imag) <= 2 * M:
+            i += 1
+        init_kwargs = f.init_kwargs
+        del init_kwargs["directory"]
+        FP_params = {"ref_point": ref_point, "dps": mpmath.mp.dps,
+                     "order": None, "max_iter": max_iter, "FP_code": f.FP_code,
+                     "partials": {}, "xr": {}, "div_iter": i,
+                     "init_kwargs": init_kwargs, "ref_orbit_len": ref_orbit_len}
+        f.save_ref_point(FP_params, orbit)
+        f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
+                       M_divergence=M, BLA_eps=bla_eps, calc_hessian=True)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "pert")
+        (_, _, _, Zn_path, dXa, dXb, dYa, dYb, has_xr, ref_index_xr, refx_xr,
+         refy_xr, ref_div_iter, ref_order, driftx_xr, drifty_xr, dx_xr, _p,
+         lin_mat, lin_scale_xr, kc, M_bla, r_bla, bla_len, stages_bla, _m,
+         _i) = cia
+        np.savez_compressed(
+            out, pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si,
+            Zn=Zn_path, dXa=dXa, dXb=dXb, dYa=dYa, dYb=dYb,
+            ref_div_iter=ref_div_iter, ref_order=ref_order,
+            lin_mat=lin_mat, flavor=flavor_int,
+            dx_m=np.asarray(dx_xr._mantissa)[0], dx_e=np.asarray(dx_xr._exp)[0],
+            driftx_m=np.asarray(driftx_xr._mantissa)[0],
+            driftx_e=np.asarray(driftx_xr._exp)[0],
+            drifty_m=np.asarray(drifty_xr._mantissa)[0],
+            drifty_e=np.asarray(drifty_xr._exp)[0],
+            kc_m=np.asarray(kc._mantissa)[0], kc_e=np.asarray(kc._exp)[0],
+            max_iter=max_iter, M=M, bla_eps=bla_eps,
+            M_bla=M_bla, r_bla=r_bla, stages_bla=stages_bla)
+
+
+def golden_xrange(out, seed=100, n=400):
+    """Xrange arithmetic through the reference's host class (numpy_utils/xrange.py),
+    operand generator in the spirit of tests/test_numba_xr.py (seeds 100/800,
+    binary exponents up to +-200)."""
+    rg = np.random.default_rng(seed)
+    am = (rg.random(n) - .5) + 1j * (rg.random(n) - .5)
+    bm = (rg.random(n) - .5) + 1j * (rg.random(n) - .5)
+    ae = rg.integers(-200, 200, n).astype(np.int32)
+    be = rg.integers(-200, 200, n).astype(np.int32)
+    # a few exact zeros and equal exponents (edge cases of _coexp_ufunc)
+    am[:5] = 0.
+    be[5:10] = ae[5:10]
+    A = fsx.Xrange_array(am, ae)
+    B = fsx.Xrange_array(bm, be)
+    S = A + B
+    P = A * B
+    Q = A.abs2()
+    res = dict(am=am, ae=ae, bm=bm, be=be,
+               add=S.to_standard() if False else np.zeros(0),
+               add_m=np.asarray(S._mantissa), add_e=np.asarray(S._exp),
+               mul_m=np.asarray(P._mantissa), mul_e=np.asarray(P._exp),
+               abs2_m=np.asarray(Q._mantissa), abs2_e=np.asarray(Q._exp))
+    # to_standard on values that stay in the double range
+    sm = (rg.random(n) - .5) + 1j * (rg.random(n) - .5)
+    se = rg.integers(-1000, 1000, n).astype(np.int32)
+    res["std_m"], res["std_e"] = sm, se
+    res["std_out"] = fsx.Xrange_array(sm, se).to_standard()
+    np.savez_compressed(out, **res)
+
+
+def main():
+    mpmath.mp.dps = 50
+    golden_xrange(os.path.join(HERE, "xrange_ops.npz"))
+    print("xrange done", flush=True)
+    golden_std_m2(os.path.join(HERE, "std_m2.npz"))
+    print("std_m2 done", flush=True)
+    golden_std_bs(os.path.join(HERE, "std_bs.npz"))
+    print("std_bs done", flush=True)
+
+    # Perturbation M2, standard (FP64) branch, non-cycle reference at the centre
+    mpmath.mp.dps = 30
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_fp64.npz"),
+        x="-0.743643887037151", y="0.131825904205330", dx="2.e-9", nx=20,
+        precision=30, order=None, max_iter=6000, interior=False)
+    print("pert_m2_fp64 done", flush=True)
+
+    # Perturbation M2, cycle reference (period-p nucleus), interior detection
+    p = 29
+    dps = 60
+    mpmath.mp.dps = dps
+    c = mp_nucleus(p, dps)
+    size = mpmath.mpf(1) / (p ** 2 * 40)
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_cycle.npz"),
+        x=str(c.real), y=str(c.imag), dx=str(size * 2), nx=16,
+        precision=dps, order=p, max_iter=3000, interior=True)
+    print("pert_m2_cycle done", flush=True)
+
+    # Perturbation M2, Xrange branch (dx < 1e-300), cycle reference
+    dps = 340
+    mpmath.mp.dps = dps
+    c = mp_nucleus(p, dps)
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_xr.npz"),
+        x=str(c.real), y=str(c.imag), dx="1.e-305", nx=4,
+        precision=dps, order=p, max_iter=600, interior=True)
+    print("pert_m2_xr done", flush=True)
+
+    # Perturbation M2, Xrange branch, escaping non-cycle reference that is
+    # off the image centre (drift), dx < 1e-300
+    mpmath.mp.dps = 340
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_xr_div.npz"),
+        x="-0.743643887037158704752191506114774e0",
+        y="0.131825904205311970493132056385139", dx="3.e-304", nx=5,
+        precision=340, order=None, max_iter=5000, interior=False,
+        ref_shift=0.31 - 0.27j, x_offset="1e-14")
+    print("pert_m2_xr_div done", flush=True)
+
+    # Perturbation Burning Ship (flavors 1 and 4), standard branch, around a
+    # point whose orbit escapes after ~2200 iterations
+    mpmath.mp.dps = 30
+    for fl, flav in ((1, "Burning ship"), (4, "Celtic")):
+        golden_perturb_bs(
+            os.path.join(HERE, f"pert_bs_{fl}.npz"),
+            x="-1.773934837092732", y="-0.00025062656641604286", dx="4.e-6",
+            nx=14, precision=30, max_iter=5000, flavor=flav)
+        print(f"pert_bs_{fl} done", flush=True)
+
+
+if __name__ == "__main__":
+    main()

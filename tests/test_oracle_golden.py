@@ -1,0 +1,195 @@
+"""
+Pin the CPU oracle against golden vectors produced by the reference itself
+(tests/golden/make_golden.py runs Fractalshades' hot-path functions as plain
+Python).  Integer outputs (stop_iter, stop_reason, U) must match exactly;
+floating point outputs are compared bit-for-bit where both sides evaluate the
+same IEEE operations in the same order, else to the stated tolerance.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(G, name + ".npz"), allow_pickle=False)
+
+
+# ---------------------------------------------------------------------------
+def test_xrange_ops_vs_reference_host_class():
+    d = load("xrange_ops")
+    am, ae, bm, be = d["am"], d["ae"], d["bm"], d["be"]
+    sm, se = orc.xr_binop("add", am, ae, bm, be)
+    ref = d["add_m"] * np.exp2(d["add_e"].astype(float))
+    got = sm * np.exp2(se.astype(float))
+    np.testing.assert_allclose(got, ref, rtol=2e-16, atol=0)
+    pm, pe = orc.xr_binop("mul", am, ae, bm, be)
+    np.testing.assert_allclose(pm * np.exp2(pe.astype(float)),
+                               d["mul_m"] * np.exp2(d["mul_e"].astype(float)),
+                               rtol=4e-16, atol=0)
+    qm, qe = orc.xr_binop("abs2", am, ae)
+    np.testing.assert_allclose(qm.real * np.exp2(qe.astype(float)),
+                               d["abs2_m"] * np.exp2(d["abs2_e"].astype(float)),
+                               rtol=4e-16, atol=0)
+    tm, _ = orc.xr_binop("to_standard", d["std_m"], d["std_e"])
+    ok = np.isfinite(d["std_out"])
+    assert np.array_equal(tm[ok], d["std_out"][ok])
+
+
+def test_xrange_to_standard_edges():
+    # underflow to 0, overflow to inf, exact powers of two
+    m = np.array([1 + 1j, 0.75 - 0.5j, 1j, 0.5, 0j])
+    e = np.array([-1080, 1030, -1022, 3, 17], dtype=np.int32)
+    out, _ = orc.xr_binop("to_standard", m, e)
+    assert out[0] == 0
+    assert np.isinf(out[1].real)
+    assert out[2] == 1j * 2.0 ** -1022
+    assert out[3] == 4.0
+    assert out[4] == 0
+
+
+# ---------------------------------------------------------------------------
+def test_std_m2_matches_reference_bit_exact():
+    d = load("std_m2")
+    Z, si, sr = orc.std_m2(d["pix"], complex(*d["center"]), d["lin_mat"],
+                           float(d["dx"]), int(d["max_iter"]), float(d["M"]),
+                           float(d["eps"]))
+    assert np.array_equal(si, d["stop_iter"])
+    assert np.array_equal(sr, d["stop_reason"])
+    assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
+
+
+@pytest.mark.parametrize("flavor", [1, 2, 3, 4, 5])
+def test_std_bs_matches_reference_bit_exact(flavor):
+    d = load("std_bs")
+    Z, si, sr = orc.std_bs(d[f"pix_{flavor}"], complex(*d["center"]), d["lin_mat"],
+                           float(d["dx"]), flavor, int(d["max_iter"]), float(d["M"]))
+    assert np.array_equal(si, d[f"stop_iter_{flavor}"])
+    assert np.array_equal(sr, d[f"stop_reason_{flavor}"])
+    assert np.array_equal(Z.view(np.uint64), d[f"Z_{flavor}"].view(np.uint64))
+
+
+# ---------------------------------------------------------------------------
+def _pm2_inputs(d, recompute_tables):
+    xr = bool(d["xr_mode"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    kw = dict(Zn=d["Zn"], ref_div_iter=int(d["ref_div_iter"]),
+              ref_order=int(d["ref_order"]), lin_mat=d["lin_mat"],
+              dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+              drift_m=complex(d["drift_m"]), drift_e=int(d["drift_e"]),
+              max_iter=int(d["max_iter"]), M=float(d["M"]),
+              eps_stat=float(d["eps_stat"]), xr_mode=xr,
+              interior=bool(d["interior"]), calc_dzndc=True,
+              xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"])
+    if recompute_tables:
+        Mb, rb, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]))
+        kw["bla"] = (Mb, rb, st)
+        kw["dZndc"] = orc.dzndc_path_m2(
+            d["Zn"], kw["ref_div_iter"], kw["ref_order"], xr, kw["dx_m"], kw["dx_e"],
+            d["xr_idx"], d["xr_m"], d["xr_e"])
+        if kw["interior"]:
+            kw["dZndz"] = orc.dzndz_path_m2(d["Zn"], kw["ref_div_iter"], xr,
+                                            d["xr_idx"], d["xr_m"], d["xr_e"])
+    else:
+        kw["bla"] = (d["M_bla"], d["r_bla"], int(d["stages_bla"]))
+        if xr:
+            kw["dZndc"] = (d["dZndc_m"], d["dZndc_e"])
+            if kw["interior"]:
+                kw["dZndz"] = (d["dZndz_m"], d["dZndz_e"])
+        else:
+            kw["dZndc"] = d["dZndc"]
+            if kw["interior"]:
+                kw["dZndz"] = d["dZndz"]
+    return kw
+
+
+def _xr_val(m, e):
+    return m * np.exp2(e.astype(float))
+
+
+@pytest.mark.parametrize("case", ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr",
+                                  "pert_m2_xr_div"])
+def test_orbit_tables_match_reference(case):
+    d = load(case)
+    xr = bool(d["xr_mode"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    Mb, rb, bl, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]))
+    assert st == int(d["stages_bla"])
+    assert np.array_equal(Mb.view(np.uint64), d["M_bla"].view(np.uint64))
+    assert np.array_equal(rb.view(np.uint64), d["r_bla"].view(np.uint64))
+    dz = orc.dzndc_path_m2(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), xr,
+                           float(d["dx_m"]), int(d["dx_e"]), d["xr_idx"], d["xr_m"], d["xr_e"])
+    if xr:
+        np.testing.assert_allclose(_xr_val(*dz) / 2.0 ** 1000,
+                                   _xr_val(d["dZndc_m"], d["dZndc_e"]) / 2.0 ** 1000,
+                                   rtol=1e-15)
+    else:
+        assert np.array_equal(dz.view(np.uint64), d["dZndc"].view(np.uint64))
+    if bool(d["interior"]):
+        dzz = orc.dzndz_path_m2(d["Zn"], int(d["ref_div_iter"]), xr,
+                                d["xr_idx"], d["xr_m"], d["xr_e"])
+        if xr:
+            np.testing.assert_allclose(_xr_val(*dzz), _xr_val(d["dZndz_m"], d["dZndz_e"]),
+                                       rtol=1e-15)
+        else:
+            assert np.array_equal(dzz.view(np.uint64), d["dZndz"].view(np.uint64))
+
+
+@pytest.mark.parametrize("case", ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr",
+                                  "pert_m2_xr_div"])
+@pytest.mark.parametrize("recompute", [False, True])
+def test_perturb_m2_matches_reference(case, recompute):
+    d = load(case)
+    kw = _pm2_inputs(d, recompute)
+    Z, U, sr, si = orc.perturb_m2(d["pix"], **kw)
+    assert np.array_equal(si, d["stop_iter"])
+    assert np.array_equal(sr, d["stop_reason"])
+    assert np.array_equal(U, d["U"])
+    if not kw["xr_mode"]:
+        assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
+    else:
+        np.testing.assert_allclose(Z, d["Z"], rtol=1e-13, atol=0)
+
+
+def test_dzndz_carryover_is_erased_by_first_step():
+    """The reference keeps the Xrange dzndz of the previous pixel in a tile
+    (perturbation.py:1015, 1055-1060); the first full step multiplies it by
+    (Z_0 + dz_0) = 0, so results do not depend on it."""
+    d = load("pert_m2_xr")
+    kw = _pm2_inputs(d, False)
+    a = orc.perturb_m2(d["pix"], carryover=True, **kw)
+    b = orc.perturb_m2(d["pix"], carryover=False, **kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4"])
+def test_perturb_bs_matches_reference(case):
+    d = load(case)
+    fl = int(d["flavor"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    Mb, rb, bl, st = orc.make_bla_bs(d["Zn"], fl, kc, float(d["bla_eps"]))
+    assert st == int(d["stages_bla"])
+    assert np.array_equal(Mb.view(np.uint64), d["M_bla"].view(np.uint64))
+    assert np.array_equal(rb.view(np.uint64), d["r_bla"].view(np.uint64))
+    scale = float(np.ldexp(d["dx_m"], d["dx_e"]))
+    paths = orc.dzndc_path_bs(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), fl, scale)
+    for got, k in zip(paths, ["dXa", "dXb", "dYa", "dYb"]):
+        assert np.array_equal(got.view(np.uint64), d[k].view(np.uint64))
+    Z, U, sr, si = orc.perturb_bs(
+        d["pix"], Zn=d["Zn"], ref_div_iter=int(d["ref_div_iter"]),
+        ref_order=int(d["ref_order"]), lin_mat=d["lin_mat"],
+        dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+        driftx_m=float(d["driftx_m"]), driftx_e=int(d["driftx_e"]),
+        drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]),
+        max_iter=int(d["max_iter"]), M=float(d["M"]), flavor=fl,
+        bla=(Mb, rb, st), dpaths=paths)
+    assert np.array_equal(si, d["stop_iter"])
+    assert np.array_equal(sr, d["stop_reason"])
+    assert np.array_equal(U, d["U"])
+    assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
