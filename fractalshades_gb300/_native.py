@@ -1,0 +1,323 @@
+"""
+ctypes binding of libfsgpu.so (declared in include/fsgpu.h).
+
+The GPU library is the only compute path of this package: there is no CPU
+fallback.  Loading fails with an explicit error when the library has not been
+built (``python -c "import __graft_entry__ as g; g.build()"``) or when no CUDA
+device is visible.
+"""
+import ctypes as ct
+import os
+import threading
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "libfsgpu.so")
+
+FSG_OK = 0
+FSG_INTERRUPTED = 1
+FSG_ERR_ARG = -1
+FSG_ERR_CUDA = -2
+FSG_ERR_NOMEM = -3
+FSG_ERR_NODEV = -4
+
+MODE_FP64 = 0
+MODE_XR64 = 1
+MODE_FE32 = 2
+MODES = {"fp64": MODE_FP64, "xr64": MODE_XR64, "fe32": MODE_FE32}
+
+HOST = 0
+DEVICE = 1
+
+P = ct.c_void_p
+I32, I64, F64 = ct.c_int32, ct.c_int64, ct.c_double
+
+
+class RefDesc(ct.Structure):
+    _fields_ = [
+        ("Zn", P), ("len", I64), ("div_iter", I64), ("order", I64),
+        ("n_xr", I32), ("xr_idx", P), ("xr_m", P), ("xr_e", P),
+        ("flavor", I32), ("xr_paths", I32), ("calc_dzndc", I32), ("calc_dzndz", I32),
+        ("scale_m", F64), ("scale_e", I32), ("bla", I32), ("kc", F64), ("bla_eps", F64),
+    ]
+
+
+class Calc(ct.Structure):
+    _fields_ = [
+        ("max_iter", I64), ("M_divergence", F64), ("epsilon_stationnary", F64),
+        ("mode", I32), ("calc_dzndc", I32), ("interior", I32), ("bla", I32),
+        ("flavor", I32), ("xr_semantics", I32),
+    ]
+
+
+class Tile(ct.Structure):
+    _fields_ = [
+        ("nx", I32), ("ny", I32), ("xs", P), ("ys", P), ("lin_mat", F64 * 4),
+        ("center_re", F64), ("center_im", F64), ("dx", F64),
+        ("dx_m", F64), ("dx_e", I32), ("drift_re", F64), ("drift_im", F64),
+        ("drift_e", I32), ("drifty_m", F64), ("drifty_e", I32), ("ref", P),
+        ("Z", P), ("nZ", I32), ("i_dzndz", I32), ("i_dzndc", I32),
+        ("U", P), ("stop_reason", P), ("stop_iter", P), ("potential", P), ("dem", P),
+    ]
+
+
+class Stats(ct.Structure):
+    _fields_ = [
+        ("kernel_ms", F64), ("pixels", I64), ("pixel_iters", I64),
+        ("full_steps", I64), ("bla_steps", I64), ("rebases", I64),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+#: exported symbols (include/fsgpu.h)
+SYMBOLS = [
+    "fsg_version", "fsg_ctx_create", "fsg_ctx_destroy", "fsg_last_error",
+    "fsg_set_stream", "fsg_sync", "fsg_ref_create", "fsg_ref_destroy",
+    "fsg_ref_info", "fsg_ref_download", "fsg_std_tiles", "fsg_perturb_tiles",
+    "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel",
+]
+
+
+class GPUError(RuntimeError):
+    pass
+
+
+def load():
+    """Load libfsgpu.so and declare its signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise GPUError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c \"import __graft_entry__ as g; g.build()\"` "
+                "(this package has no CPU fallback)")
+        L = ct.CDLL(LIB_PATH)
+        L.fsg_version.restype = ct.c_char_p
+        L.fsg_ctx_create.argtypes = [ct.c_int, ct.POINTER(P)]
+        L.fsg_ctx_destroy.argtypes = [P]
+        L.fsg_last_error.argtypes = [P]
+        L.fsg_last_error.restype = ct.c_char_p
+        L.fsg_set_stream.argtypes = [P, P]
+        L.fsg_sync.argtypes = [P]
+        L.fsg_ref_create.argtypes = [P, ct.POINTER(RefDesc), ct.POINTER(P)]
+        L.fsg_ref_destroy.argtypes = [P, P]
+        L.fsg_ref_info.argtypes = [P, ct.POINTER(I64), ct.POINTER(I64), ct.POINTER(I32)]
+        L.fsg_ref_download.argtypes = [P, P, ct.c_int, P, P]
+        L.fsg_std_tiles.argtypes = [P, ct.POINTER(Calc), ct.POINTER(Tile), I32, I32]
+        L.fsg_perturb_tiles.argtypes = [P, ct.POINTER(Calc), ct.POINTER(Tile), I32, I32]
+        L.fsg_last_stats.argtypes = [P, ct.POINTER(Stats)]
+        L.fsg_cancel.argtypes = [P]
+        L.fsg_clear_cancel.argtypes = [P]
+        _lib = L
+        return L
+
+
+def _p(a):
+    return None if a is None else ct.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One CUDA device context of the library (stream, counters, cancel flag)."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        h = P()
+        rc = self.L.fsg_ctx_create(int(device), ct.byref(h))
+        if rc != FSG_OK:
+            raise GPUError(f"fsg_ctx_create failed with code {rc} "
+                           "(no CUDA device visible?)")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fsg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc, what):
+        if rc == FSG_OK or rc == FSG_INTERRUPTED:
+            return rc
+        msg = self.L.fsg_last_error(self.h).decode()
+        raise GPUError(f"{what} failed (code {rc}): {msg}")
+
+    def set_stream(self, stream_ptr):
+        self.check(self.L.fsg_set_stream(self.h, ct.c_void_p(stream_ptr or 0)), "fsg_set_stream")
+
+    def sync(self):
+        return self.check(self.L.fsg_sync(self.h), "fsg_sync")
+
+    def cancel(self):
+        self.L.fsg_cancel(self.h)
+
+    def clear_cancel(self):
+        self.L.fsg_clear_cancel(self.h)
+
+    def stats(self):
+        s = Stats()
+        self.check(self.L.fsg_last_stats(self.h, ct.byref(s)), "fsg_last_stats")
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    # ------------------------------------------------------------------
+    def std_tiles(self, calc, tiles, where=HOST):
+        arr = (Tile * len(tiles))(*tiles)
+        return self.check(self.L.fsg_std_tiles(self.h, ct.byref(calc), arr, len(tiles), where),
+                          "fsg_std_tiles")
+
+    def perturb_tiles(self, calc, tiles, where=HOST):
+        arr = (Tile * len(tiles))(*tiles)
+        return self.check(self.L.fsg_perturb_tiles(self.h, ct.byref(calc), arr, len(tiles), where),
+                          "fsg_perturb_tiles")
+
+
+class Reference:
+    """A reference orbit resident on the device with its derived tables
+    (derivative paths, BLA tree, fe copies), built by fsg_ref_create."""
+
+    def __init__(self, ctx, Zn, *, div_iter, order, flavor=0, xr_idx=None, xr_m=None,
+                 xr_e=None, xr_paths=False, calc_dzndc=True, calc_dzndz=False,
+                 scale_m=1.0, scale_e=0, bla=True, kc=0.0, bla_eps=1e-6):
+        self.ctx = ctx
+        self.Zn = np.ascontiguousarray(Zn, dtype=np.complex128)
+        n_xr = 0 if xr_idx is None else len(xr_idx)
+        self._keep = [self.Zn]
+        d = RefDesc()
+        d.Zn = _p(self.Zn)
+        d.len = self.Zn.size
+        d.div_iter = int(div_iter)
+        d.order = int(order) if order is not None else 0
+        d.n_xr = n_xr
+        if n_xr:
+            idx = np.ascontiguousarray(xr_idx, dtype=np.int32)
+            m = np.ascontiguousarray(xr_m, dtype=np.complex128 if flavor == 0 else np.float64)
+            e = np.ascontiguousarray(xr_e, dtype=np.int32)
+            self._keep += [idx, m, e]
+            d.xr_idx, d.xr_m, d.xr_e = _p(idx), _p(m), _p(e)
+        d.flavor = int(flavor)
+        d.xr_paths = int(bool(xr_paths))
+        d.calc_dzndc = int(bool(calc_dzndc))
+        d.calc_dzndz = int(bool(calc_dzndz))
+        d.scale_m, d.scale_e = float(scale_m), int(scale_e)
+        d.bla = int(bool(bla))
+        d.kc = float(kc)
+        d.bla_eps = float(bla_eps)
+        h = P()
+        ctx.check(ctx.L.fsg_ref_create(ctx.h, ct.byref(d), ct.byref(h)), "fsg_ref_create")
+        self.h = h
+        self.flavor = flavor
+        self.xr_paths = bool(xr_paths)
+        ln, bl, st = I64(), I64(), I32()
+        ctx.L.fsg_ref_info(h, ct.byref(ln), ct.byref(bl), ct.byref(st))
+        self.len, self.bla_len, self.stages = ln.value, bl.value, st.value
+
+    def free(self):
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
+            self.ctx.L.fsg_ref_destroy(self.ctx.h, self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def download(self, which):
+        """Tables built on the device: 'dzndc', 'dzndz', 'bla', 'bs_paths'."""
+        n = self.len
+        L, c = self.ctx.L, self.ctx
+        if which in ("dzndc", "dzndz"):
+            k = 0 if which == "dzndc" else 1
+            m = np.zeros(n + k, dtype=np.complex128)
+            e = np.zeros(n + k, dtype=np.int32)
+            c.check(L.fsg_ref_download(c.h, self.h, k, _p(m), _p(e)), "fsg_ref_download")
+            return (m, e) if self.xr_paths else m
+        if which == "bla":
+            r = np.zeros(self.bla_len)
+            if self.flavor == 0:
+                M = np.zeros(2 * self.bla_len, dtype=np.complex128)
+            else:
+                M = np.zeros(8 * self.bla_len)
+            c.check(L.fsg_ref_download(c.h, self.h, 2, _p(M), _p(r)), "fsg_ref_download")
+            return M, r
+        if which == "bs_paths":
+            out = np.zeros(4 * n)
+            c.check(L.fsg_ref_download(c.h, self.h, 3, _p(out), None), "fsg_ref_download")
+            return out.reshape(4, n)
+        raise ValueError(which)
+
+
+def make_tile(*, xs, ys, lin_mat, Z, stop_reason, stop_iter, U=None, ref=None,
+              center=0j, dx=0.0, dx_m=0.0, dx_e=0, drift_m=0j, drift_e=0,
+              drifty_m=0.0, drifty_e=0, i_dzndz=-1, i_dzndc=-1, potential=None,
+              dem=None, keep=None):
+    """Fill a Tile from numpy (host) arrays; pointers of device arrays can be
+    given as ints through the *_ptr keywords of make_tile_ptrs."""
+    t = Tile()
+    t.nx, t.ny = len(xs), len(ys)
+    t.xs, t.ys = _p(xs), _p(ys)
+    lm = np.asarray(lin_mat, dtype=np.float64).ravel()
+    for k in range(4):
+        t.lin_mat[k] = lm[k]
+    t.center_re, t.center_im, t.dx = complex(center).real, complex(center).imag, float(dx)
+    t.dx_m, t.dx_e = float(dx_m), int(dx_e)
+    t.drift_re, t.drift_im, t.drift_e = complex(drift_m).real, complex(drift_m).imag, int(drift_e)
+    t.drifty_m, t.drifty_e = float(drifty_m), int(drifty_e)
+    t.ref = ref.h if ref is not None else None
+    t.Z = _p(Z)
+    t.nZ = Z.shape[0]
+    t.i_dzndz, t.i_dzndc = int(i_dzndz), int(i_dzndc)
+    t.U = _p(U)
+    t.stop_reason, t.stop_iter = _p(stop_reason), _p(stop_iter)
+    t.potential, t.dem = _p(potential), _p(dem)
+    if keep is not None:
+        keep.extend([xs, ys, Z, U, stop_reason, stop_iter, potential, dem])
+    return t
+
+
+def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_ptr,
+                   stop_iter_ptr, U_ptr=0, ref=None, center=0j, dx=0.0, dx_m=0.0,
+                   dx_e=0, drift_m=0j, drift_e=0, drifty_m=0.0, drifty_e=0, i_dzndz=-1,
+                   i_dzndc=-1, potential_ptr=0, dem_ptr=0):
+    """Fill a Tile from raw device pointers (ints)."""
+    t = Tile()
+    t.nx, t.ny = int(nx), int(ny)
+    t.xs, t.ys = xs_ptr, ys_ptr
+    lm = np.asarray(lin_mat, dtype=np.float64).ravel()
+    for k in range(4):
+        t.lin_mat[k] = lm[k]
+    t.center_re, t.center_im, t.dx = complex(center).real, complex(center).imag, float(dx)
+    t.dx_m, t.dx_e = float(dx_m), int(dx_e)
+    t.drift_re, t.drift_im, t.drift_e = complex(drift_m).real, complex(drift_m).imag, int(drift_e)
+    t.drifty_m, t.drifty_e = float(drifty_m), int(drifty_e)
+    t.ref = ref.h if ref is not None else None
+    t.Z, t.nZ = Z_ptr, int(nZ)
+    t.i_dzndz, t.i_dzndc = int(i_dzndz), int(i_dzndc)
+    t.U = U_ptr or None
+    t.stop_reason, t.stop_iter = stop_reason_ptr, stop_iter_ptr
+    t.potential, t.dem = potential_ptr or None, dem_ptr or None
+    return t
+
+
+def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
+              calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False):
+    c = Calc()
+    c.max_iter = int(max_iter)
+    c.M_divergence = float(M_divergence)
+    c.epsilon_stationnary = float(epsilon_stationnary)
+    c.mode = MODES[mode] if isinstance(mode, str) else int(mode)
+    c.calc_dzndc = int(bool(calc_dzndc))
+    c.interior = int(bool(interior))
+    c.bla = int(bool(bla))
+    c.flavor = int(flavor)
+    c.xr_semantics = int(bool(xr_semantics))
+    return c

@@ -1,0 +1,594 @@
+// fsg_abi.cu -- the extern "C" boundary declared in include/fsgpu.h.
+//
+// Owns the CUDA context state (stream, work counter, statistics, cancel flag),
+// the device copies of reference orbits with their derived tables, and the
+// launch of the iteration kernels over batches of tiles.  No C++ exception
+// crosses the boundary: every entry point returns a status code.
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fsg_internal.cuh"
+#include "../../include/fsgpu.h"
+
+#define FSG_VERSION "fractalshades_gb300 0.1.0 (sm_103a)"
+
+// launchers of fsg_ref.cu
+void fsg_build_paths_m2(const RefDev *Rd, double2 *dzndc, double2 *dzndc_xm, int *dzndc_xe,
+                        double2 *dzndz, double2 *dzndz_xm, int *dzndz_xe, int xr_mode,
+                        int want_dzndc, int want_dzndz, double scale_m, int scale_e,
+                        cudaStream_t s);
+void fsg_build_paths_bs(const RefDev *Rd, double *dXa, double *dXb, double *dYa, double *dYb,
+                        double scale, cudaStream_t s);
+void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *Mbs, double *r,
+                   int stages, double kc, double eps, cudaStream_t s);
+void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzndc,
+                         const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
+                         const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
+                         int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
+                         int4 *bla_A, int4 *bla_B, cudaStream_t s);
+
+struct fsg_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    volatile int *cancel_host = nullptr;   // pinned, mapped
+    int *cancel_dev = nullptr;             // device alias of cancel_host
+    int *status_dev = nullptr;
+    unsigned long long *counter_dev = nullptr;
+    unsigned long long *stats_dev = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_desc = nullptr;
+    bool timed = false;
+    int64_t last_pixels = 0;
+    // tile descriptors: pinned staging + device copy
+    TileDev *tiles_host = nullptr; long long *start_host = nullptr;
+    TileDev *tiles_dev = nullptr; long long *start_dev = nullptr;
+    // grow-only device scratch for host-buffer calls
+    char *scratch = nullptr; size_t scratch_size = 0;
+};
+
+struct fsg_ref {
+    RefDev host;            // device pointers, host copy
+    RefDev *dev = nullptr;  // device copy of the descriptor
+    std::vector<void *> allocs;
+    int64_t len = 0;
+    int xr_paths = 0, flavor = 0, has_dzndc = 0, has_dzndz = 0;
+};
+
+namespace {
+
+int set_err(fsg_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_err(fsg_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return FSG_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return set_err(c, e == cudaErrorMemoryAllocation ? FSG_ERR_NOMEM : FSG_ERR_CUDA, m);
+}
+
+#define CK(call, what)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_err(ctx, e_, what); \
+    } while (0)
+
+template <class T>
+int ref_alloc(fsg_ctx *ctx, fsg_ref *r, T **p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc(reference table)");
+    r->allocs.push_back(q);
+    *p = (T *)q;
+    return FSG_OK;
+}
+
+void ref_release(fsg_ref *r) {
+    for (void *p : r->allocs) cudaFree(p);
+    r->allocs.clear();
+    if (r->dev) cudaFree(r->dev);
+    r->dev = nullptr;
+}
+
+int ensure_scratch(fsg_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->scratch_size) return FSG_OK;
+    if (ctx->scratch) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->scratch);
+        ctx->scratch = nullptr; ctx->scratch_size = 0;
+    }
+    size_t sz = bytes + bytes / 4;
+    CK(cudaMalloc((void **)&ctx->scratch, sz), "cudaMalloc(scratch)");
+    ctx->scratch_size = sz;
+    return FSG_OK;
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *calc) {
+    if (t.nx <= 0 || t.ny <= 0) return set_err(ctx, FSG_ERR_ARG, "tile with nx <= 0 or ny <= 0");
+    if (!t.xs || !t.ys || !t.Z || !t.stop_reason || !t.stop_iter)
+        return set_err(ctx, FSG_ERR_ARG, "tile with a NULL input or output pointer");
+    if (perturb && !t.ref) return set_err(ctx, FSG_ERR_ARG, "perturbation tile without reference");
+    if (perturb && t.ref->flavor != calc->flavor)
+        return set_err(ctx, FSG_ERR_ARG, "reference flavor differs from the calculation flavor");
+    if (perturb && calc->flavor == 0) {
+        if (calc->calc_dzndc && !t.ref->has_dzndc)
+            return set_err(ctx, FSG_ERR_ARG, "calc_dzndc requested but the reference has no dZndc path");
+        if (calc->interior && !t.ref->has_dzndz)
+            return set_err(ctx, FSG_ERR_ARG, "interior detection requested but the reference has no dZndz path");
+        if (calc->mode == FSG_MODE_XR64 && !t.ref->xr_paths && (calc->calc_dzndc || calc->interior))
+            return set_err(ctx, FSG_ERR_ARG, "Xrange mode needs Xrange derivative paths");
+        if (calc->mode == FSG_MODE_FP64 && t.ref->xr_paths && (calc->calc_dzndc || calc->interior))
+            return set_err(ctx, FSG_ERR_ARG, "FP64 mode needs standard derivative paths");
+        if (calc->bla && t.ref->host.bla_len <= 0)
+            return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference has no BLA tree");
+    }
+    if (perturb && calc->flavor != 0) {
+        if (calc->mode != FSG_MODE_FP64)
+            return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 only");
+        if (calc->calc_dzndc && !t.ref->has_dzndc)
+            return set_err(ctx, FSG_ERR_ARG, "calc_hessian requested but the reference has no Jacobian paths");
+        if (calc->bla && t.ref->host.bla_len <= 0)
+            return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference has no BLA tree");
+    }
+    int nZ_min = perturb ? (calc->flavor == 0 ? 1 + (calc->interior ? 1 : 0) + (calc->calc_dzndc ? 1 : 0)
+                                              : (calc->calc_dzndc ? 6 : 2))
+                         : (calc->flavor == 0 ? 3 : 6);
+    if (t.nZ < nZ_min) return set_err(ctx, FSG_ERR_ARG, "tile nZ too small for the requested fields");
+    if (perturb && calc->flavor == 0) {
+        if (calc->interior && (t.i_dzndz <= 0 || t.i_dzndz >= t.nZ))
+            return set_err(ctx, FSG_ERR_ARG, "bad i_dzndz");
+        if (calc->calc_dzndc && (t.i_dzndc <= 0 || t.i_dzndc >= t.nZ))
+            return set_err(ctx, FSG_ERR_ARG, "bad i_dzndc");
+    }
+    return FSG_OK;
+}
+
+CalcDev make_calc(const fsg_calc *c) {
+    CalcDev d;
+    d.max_iter = (int)c->max_iter;
+    d.M2 = c->M_divergence * c->M_divergence;
+    d.eps2 = c->epsilon_stationnary * c->epsilon_stationnary;
+    d.logM = log(c->M_divergence);
+    d.mode = c->mode; d.calc_dzndc = c->calc_dzndc; d.interior = c->interior;
+    d.bla = c->bla; d.flavor = c->flavor; d.xrsem = c->xr_semantics;
+    return d;
+}
+
+TileDev make_tile(const fsg_tile &t) {
+    TileDev d;
+    memset(&d, 0, sizeof(d));
+    d.ref = t.ref ? t.ref->dev : nullptr;
+    d.xs = t.xs; d.ys = t.ys; d.nx = t.nx; d.ny = t.ny;
+    for (int k = 0; k < 4; k++) d.lin[k] = t.lin_mat[k];
+    d.cre = t.center_re; d.cim = t.center_im; d.dx = t.dx;
+    d.dx_m = t.dx_m; d.dx_e = t.dx_e;
+    d.drift_re = t.drift_re; d.drift_im = t.drift_im; d.drift_e = t.drift_e;
+    d.drifty_m = t.drifty_m; d.drifty_e = t.drifty_e;
+    d.Z = t.Z; d.nZ = t.nZ; d.i_dzndz = t.i_dzndz; d.i_dzndc = t.i_dzndc;
+    d.U = t.U; d.stop_reason = (signed char *)t.stop_reason; d.stop_iter = t.stop_iter;
+    d.pot = t.potential; d.dem = t.dem;
+    return d;
+}
+
+// Launch the iteration kernel over ntiles device-resident tiles.
+int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int ntiles,
+                 bool perturb) {
+    // the descriptor staging buffer is reused: wait for the previous upload
+    CK(cudaEventSynchronize(ctx->ev_desc), "cudaEventSynchronize(descriptor upload)");
+    long long total = 0;
+    ctx->start_host[0] = 0;
+    for (int i = 0; i < ntiles; i++) {
+        ctx->tiles_host[i] = tiles[i];
+        total += (long long)tiles[i].nx * tiles[i].ny;
+        ctx->start_host[i + 1] = total;
+    }
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->tiles_dev, ctx->tiles_host, sizeof(TileDev) * ntiles,
+                       cudaMemcpyHostToDevice, s), "copy tile descriptors");
+    CK(cudaMemcpyAsync(ctx->start_dev, ctx->start_host, sizeof(long long) * (ntiles + 1),
+                       cudaMemcpyHostToDevice, s), "copy tile offsets");
+    CK(cudaEventRecord(ctx->ev_desc, s), "cudaEventRecord");
+    CK(cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), s), "reset counter");
+    CK(cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), s), "reset stats");
+    CK(cudaMemsetAsync(ctx->status_dev, 0, sizeof(int), s), "reset status");
+    WorkDev W;
+    W.tiles = ctx->tiles_dev; W.start = ctx->start_dev; W.ntiles = ntiles; W.total = total;
+    W.counter = ctx->counter_dev; W.stats = ctx->stats_dev;
+    W.cancel = ctx->cancel_dev; W.status = ctx->status_dev;
+    CalcDev C = make_calc(calc);
+    const int block = 256;
+    int per_sm = 2;
+    int grid = ctx->sm_count * per_sm;
+    long long need = (total + block - 1) / block;
+    if (need < grid) grid = (int)(need > 0 ? need : 1);
+    CK(cudaEventRecord(ctx->ev0, s), "cudaEventRecord");
+    if (!perturb) fsg_launch_std(W, C, grid, block, s);
+    else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
+    else fsg_launch_perturb(W, C, grid, block, s);
+    CK(cudaGetLastError(), "kernel launch");
+    CK(cudaEventRecord(ctx->ev1, s), "cudaEventRecord");
+    ctx->timed = true;
+    ctx->last_pixels = total;
+    return FSG_OK;
+}
+
+int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+              int32_t where, bool perturb) {
+    if (!ctx) return FSG_ERR_ARG;
+    if (!calc || !tiles || ntiles <= 0) return set_err(ctx, FSG_ERR_ARG, "no tiles");
+    if (ntiles > FSG_MAX_TILES_PER_LAUNCH) {
+        // split into several launches of at most FSG_MAX_TILES_PER_LAUNCH tiles
+        for (int32_t i = 0; i < ntiles; i += FSG_MAX_TILES_PER_LAUNCH) {
+            int32_t n = ntiles - i < FSG_MAX_TILES_PER_LAUNCH ? ntiles - i : FSG_MAX_TILES_PER_LAUNCH;
+            int rc = run_tiles(ctx, calc, tiles + i, n, where, perturb);
+            if (rc != FSG_OK) return rc;
+        }
+        return FSG_OK;
+    }
+    if (calc->max_iter <= 0 || calc->max_iter > INT_MAX / 2)
+        return set_err(ctx, FSG_ERR_ARG, "max_iter out of range (1 .. 2^30)");
+    if (calc->flavor < 0 || calc->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
+    if (calc->mode < 0 || calc->mode > 2) return set_err(ctx, FSG_ERR_ARG, "bad mode");
+    for (int32_t i = 0; i < ntiles; i++) {
+        int rc = check_tile(ctx, tiles[i], perturb, calc);
+        if (rc != FSG_OK) return rc;
+    }
+    std::vector<TileDev> td(ntiles);
+    if (where == FSG_DEVICE) {
+        for (int32_t i = 0; i < ntiles; i++) td[i] = make_tile(tiles[i]);
+        return launch_tiles(ctx, calc, td.data(), ntiles, perturb);
+    }
+    if (where != FSG_HOST) return set_err(ctx, FSG_ERR_ARG, "where must be FSG_HOST or FSG_DEVICE");
+    // host buffers: stage in the grow-only device scratch area
+    const size_t zsz = (calc->flavor == 0) ? 16 : 8;
+    size_t bytes = 0;
+    for (int32_t i = 0; i < ntiles; i++) {
+        const fsg_tile &t = tiles[i];
+        size_t np = (size_t)t.nx * t.ny;
+        bytes += align_up(8 * t.nx) + align_up(8 * t.ny) + align_up(zsz * t.nZ * np)
+                 + align_up(4 * np) + align_up(np) + align_up(4 * np);
+        if (t.potential) bytes += align_up(8 * np);
+        if (t.dem) bytes += align_up(8 * np);
+    }
+    int rc = ensure_scratch(ctx, bytes);
+    if (rc != FSG_OK) return rc;
+    char *p = ctx->scratch;
+    cudaStream_t s = ctx->stream;
+    for (int32_t i = 0; i < ntiles; i++) {
+        fsg_tile t = tiles[i];
+        size_t np = (size_t)t.nx * t.ny;
+        double *xs = (double *)p; p += align_up(8 * t.nx);
+        double *ys = (double *)p; p += align_up(8 * t.ny);
+        CK(cudaMemcpyAsync(xs, t.xs, 8 * t.nx, cudaMemcpyHostToDevice, s), "copy xs");
+        CK(cudaMemcpyAsync(ys, t.ys, 8 * t.ny, cudaMemcpyHostToDevice, s), "copy ys");
+        t.xs = xs; t.ys = ys;
+        t.Z = p; p += align_up(zsz * t.nZ * np);
+        // fields the kernel does not produce come back as zeros, like the
+        // caller's freshly allocated arrays (core.py:2070-2073)
+        CK(cudaMemsetAsync(t.Z, 0, zsz * t.nZ * np, s), "zero Z");
+        t.U = tiles[i].U ? (int32_t *)p : nullptr; p += align_up(4 * np);
+        t.stop_reason = (int8_t *)p; p += align_up(np);
+        t.stop_iter = (int32_t *)p; p += align_up(4 * np);
+        if (t.potential) { t.potential = (double *)p; p += align_up(8 * np); }
+        if (t.dem) { t.dem = (double *)p; p += align_up(8 * np); }
+        td[i] = make_tile(t);
+    }
+    rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
+    if (rc != FSG_OK) return rc;
+    for (int32_t i = 0; i < ntiles; i++) {
+        const fsg_tile &t = tiles[i];
+        const TileDev &d = td[i];
+        size_t np = (size_t)t.nx * t.ny;
+        CK(cudaMemcpyAsync(t.Z, d.Z, zsz * t.nZ * np, cudaMemcpyDeviceToHost, s), "copy Z back");
+        if (t.U) CK(cudaMemcpyAsync(t.U, d.U, 4 * np, cudaMemcpyDeviceToHost, s), "copy U back");
+        CK(cudaMemcpyAsync(t.stop_reason, d.stop_reason, np, cudaMemcpyDeviceToHost, s), "copy stop_reason back");
+        CK(cudaMemcpyAsync(t.stop_iter, d.stop_iter, 4 * np, cudaMemcpyDeviceToHost, s), "copy stop_iter back");
+        if (t.potential) CK(cudaMemcpyAsync(t.potential, d.pot, 8 * np, cudaMemcpyDeviceToHost, s), "copy potential back");
+        if (t.dem) CK(cudaMemcpyAsync(t.dem, d.dem, 8 * np, cudaMemcpyDeviceToHost, s), "copy dem back");
+    }
+    return fsg_sync(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fsg_version(void) { return FSG_VERSION; }
+
+int fsg_ctx_create(int device, fsg_ctx **out) {
+    if (!out) return FSG_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return FSG_ERR_NODEV;
+    if (device < 0 || device >= n) return FSG_ERR_ARG;
+    fsg_ctx *ctx = new (std::nothrow) fsg_ctx();
+    if (!ctx) return FSG_ERR_NOMEM;
+    ctx->device = device;
+    int rc = FSG_OK;
+    do {
+        if (cudaSetDevice(device) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+        if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        ctx->stream = ctx->own_stream;
+        int *h = nullptr;
+        if (cudaHostAlloc((void **)&h, sizeof(int), cudaHostAllocMapped) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        *h = 0;
+        ctx->cancel_host = h;
+        if (cudaHostGetDevicePointer((void **)&ctx->cancel_dev, h, 0) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        if (cudaMalloc((void **)&ctx->status_dev, sizeof(int)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaMalloc((void **)&ctx->counter_dev, sizeof(unsigned long long)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaMalloc((void **)&ctx->stats_dev, 4 * sizeof(unsigned long long)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaMalloc((void **)&ctx->tiles_dev, sizeof(TileDev) * FSG_MAX_TILES_PER_LAUNCH) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaMalloc((void **)&ctx->start_dev, sizeof(long long) * (FSG_MAX_TILES_PER_LAUNCH + 1)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaHostAlloc((void **)&ctx->tiles_host, sizeof(TileDev) * FSG_MAX_TILES_PER_LAUNCH, 0) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaHostAlloc((void **)&ctx->start_host, sizeof(long long) * (FSG_MAX_TILES_PER_LAUNCH + 1), 0) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess
+            || cudaEventCreateWithFlags(&ctx->ev_desc, cudaEventDisableTiming) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        cudaEventRecord(ctx->ev_desc, ctx->stream);
+    } while (0);
+    if (rc != FSG_OK) { fsg_ctx_destroy(ctx); return rc; }
+    *out = ctx;
+    return FSG_OK;
+}
+
+int fsg_ctx_destroy(fsg_ctx *ctx) {
+    if (!ctx) return FSG_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->status_dev) cudaFree(ctx->status_dev);
+    if (ctx->counter_dev) cudaFree(ctx->counter_dev);
+    if (ctx->stats_dev) cudaFree(ctx->stats_dev);
+    if (ctx->tiles_dev) cudaFree(ctx->tiles_dev);
+    if (ctx->start_dev) cudaFree(ctx->start_dev);
+    if (ctx->tiles_host) cudaFreeHost(ctx->tiles_host);
+    if (ctx->start_host) cudaFreeHost(ctx->start_host);
+    if (ctx->cancel_host) cudaFreeHost((void *)ctx->cancel_host);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev_desc) cudaEventDestroy(ctx->ev_desc);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return FSG_OK;
+}
+
+const char *fsg_last_error(const fsg_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int fsg_set_stream(fsg_ctx *ctx, void *stream) {
+    if (!ctx) return FSG_ERR_ARG;
+    cudaStreamSynchronize(ctx->stream);
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    cudaEventRecord(ctx->ev_desc, ctx->stream);
+    return FSG_OK;
+}
+
+int fsg_sync(fsg_ctx *ctx) {
+    if (!ctx) return FSG_ERR_ARG;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    int st = 0;
+    CK(cudaMemcpy(&st, ctx->status_dev, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+    return st ? FSG_INTERRUPTED : FSG_OK;
+}
+
+int fsg_cancel(fsg_ctx *ctx) {
+    if (!ctx) return FSG_ERR_ARG;
+    *ctx->cancel_host = 1;
+    return FSG_OK;
+}
+
+int fsg_clear_cancel(fsg_ctx *ctx) {
+    if (!ctx) return FSG_ERR_ARG;
+    *ctx->cancel_host = 0;
+    return FSG_OK;
+}
+
+int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
+    if (!ctx || !d || !out) return set_err(ctx, FSG_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    if (!d->Zn || d->len < 2) return set_err(ctx, FSG_ERR_ARG, "orbit shorter than 2 points");
+    if (d->len >= INT_MAX / 2) return set_err(ctx, FSG_ERR_ARG, "orbit too long");
+    if (d->n_xr < 0 || (d->n_xr > 0 && (!d->xr_idx || !d->xr_m || !d->xr_e)))
+        return set_err(ctx, FSG_ERR_ARG, "bad Xrange side table");
+    if (d->flavor < 0 || d->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
+    if (d->flavor != 0 && d->n_xr > 0)
+        return set_err(ctx, FSG_ERR_ARG, "Burning Ship references with an Xrange side table are not supported");
+    const int len = (int)d->len;
+    // the iteration index w never passes min(order, div_iter) <= len, so every
+    // orbit read stays inside [0, len] (slot len is a zero pad)
+    if ((d->order <= 0 || d->order > d->len) && (d->div_iter > d->len || d->div_iter < 1))
+        return set_err(ctx, FSG_ERR_ARG, "div_iter must be in [1, len] for a non-cycling reference");
+    for (int k = 0; k < d->n_xr; k++) {
+        if (d->xr_idx[k] < 0 || d->xr_idx[k] >= len || (k > 0 && d->xr_idx[k] <= d->xr_idx[k - 1]))
+            return set_err(ctx, FSG_ERR_ARG, "Xrange side-table indices must be increasing and inside the orbit");
+    }
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    fsg_ref *r = new (std::nothrow) fsg_ref();
+    if (!r) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
+    r->len = len; r->flavor = d->flavor; r->xr_paths = d->xr_paths;
+    r->has_dzndc = d->calc_dzndc; r->has_dzndz = (d->flavor == 0) && d->calc_dzndz;
+    RefDev &R = r->host;
+    memset(&R, 0, sizeof(R));
+    R.len = len;
+    R.div_iter = (int)(d->div_iter < (int64_t)INT_MAX ? d->div_iter : INT_MAX);
+    R.order = (d->order > 0 && d->order < (int64_t)INT_MAX) ? (int)d->order : INT_MAX;
+    R.first_invalid = len;
+    if (R.div_iter < R.first_invalid) R.first_invalid = R.div_iter;
+    if (R.order < R.first_invalid) R.first_invalid = R.order;
+    R.flavor = d->flavor;
+    R.n_xr = d->n_xr;
+    cudaStream_t s = ctx->stream;
+    int rc = FSG_OK;
+#define RA(ptr, n) do { rc = ref_alloc(ctx, r, &(ptr), (n)); if (rc != FSG_OK) { ref_release(r); delete r; return rc; } } while (0)
+#define RCK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { ref_release(r); delete r; return cuda_err(ctx, e_, what); } } while (0)
+    double2 *Zn; RA(Zn, len + 1);
+    RCK(cudaMemcpyAsync(Zn, d->Zn, 16 * (size_t)len, cudaMemcpyHostToDevice, s), "upload orbit");
+    RCK(cudaMemsetAsync(Zn + len, 0, 16, s), "pad orbit");
+    R.Zn = Zn;
+    std::vector<int> slot;
+    std::vector<double2> xm;
+    int *xr_slot = nullptr; double2 *xr_m = nullptr; int *xr_e = nullptr;
+    if (d->n_xr > 0) {
+        slot.assign(len + 1, -1);
+        for (int k = 0; k < d->n_xr; k++) slot[d->xr_idx[k]] = k;
+        RA(xr_slot, len + 1); RA(xr_m, d->n_xr); RA(xr_e, d->n_xr);
+        RCK(cudaMemcpy(xr_slot, slot.data(), 4 * (size_t)(len + 1), cudaMemcpyHostToDevice), "upload xr slots");
+        RCK(cudaMemcpy(xr_m, d->xr_m, 16 * (size_t)d->n_xr, cudaMemcpyHostToDevice), "upload xr mantissas");
+        RCK(cudaMemcpy(xr_e, d->xr_e, 4 * (size_t)d->n_xr, cudaMemcpyHostToDevice), "upload xr exponents");
+    }
+    R.xr_slot = xr_slot; R.xr_m = xr_m; R.xr_e = xr_e;
+    // derivative paths
+    double2 *dzndc = nullptr, *dzndc_xm = nullptr, *dzndz = nullptr, *dzndz_xm = nullptr;
+    int *dzndc_xe = nullptr, *dzndz_xe = nullptr;
+    double *dXa = nullptr, *dXb = nullptr, *dYa = nullptr, *dYb = nullptr;
+    if (d->flavor == 0) {
+        if (d->calc_dzndc) {
+            if (d->xr_paths) { RA(dzndc_xm, len + 1); RA(dzndc_xe, len + 1); }
+            else RA(dzndc, len + 1);
+        }
+        if (d->calc_dzndz) {
+            if (d->xr_paths) { RA(dzndz_xm, len + 2); RA(dzndz_xe, len + 2); }
+            else RA(dzndz, len + 2);
+        }
+    } else if (d->calc_dzndc) {
+        RA(dXa, len + 1); RA(dXb, len + 1); RA(dYa, len + 1); RA(dYb, len + 1);
+    }
+    R.dZndc = dzndc; R.dZndc_xm = dzndc_xm; R.dZndc_xe = dzndc_xe;
+    R.dZndz = dzndz; R.dZndz_xm = dzndz_xm; R.dZndz_xe = dzndz_xe;
+    R.dXa = dXa; R.dXb = dXb; R.dYa = dYa; R.dYb = dYb;
+    // BLA
+    int L = len / 8;
+    double2 *Mbla = nullptr; double *Mbs = nullptr, *rbla = nullptr;
+    int stages = (int)ceil(log2((double)len));
+    if (d->bla && L > 0) {
+        if (d->flavor == 0) RA(Mbla, 4 * (size_t)L); else RA(Mbs, 16 * (size_t)L);
+        RA(rbla, 2 * (size_t)L);
+        RCK(cudaMemsetAsync(rbla, 0, 16 * (size_t)L, s), "zero BLA radii");
+        if (Mbla) RCK(cudaMemsetAsync(Mbla, 0, 64 * (size_t)L, s), "zero BLA");
+        if (Mbs) RCK(cudaMemsetAsync(Mbs, 0, 128 * (size_t)L, s), "zero BLA");
+        R.bla_len = 2 * L;
+    }
+    R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.stages = stages;
+    // fe tables (M2)
+    int4 *Zf = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_A = nullptr, *bla_B = nullptr;
+    if (d->flavor == 0) {
+        RA(Zf, len + 1);
+        if (d->calc_dzndc) RA(dzndc_f, len + 1);
+        if (d->calc_dzndz) RA(dzndz_f, len + 2);
+        if (R.bla_len > 0) { RA(bla_A, R.bla_len); RA(bla_B, R.bla_len); }
+    }
+    R.Zf = Zf; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f_A = bla_A; R.bla_f_B = bla_B;
+    RCK(cudaMalloc((void **)&r->dev, sizeof(RefDev)), "cudaMalloc(reference descriptor)");
+    RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
+    // builds
+    if (d->flavor == 0) {
+        fsg_build_paths_m2(r->dev, dzndc, dzndc_xm, dzndc_xe, dzndz, dzndz_xm, dzndz_xe,
+                           d->xr_paths, d->calc_dzndc, d->calc_dzndz, d->scale_m, d->scale_e, s);
+    } else if (d->calc_dzndc) {
+        fsg_build_paths_bs(r->dev, dXa, dXb, dYa, dYb, ldexp(d->scale_m, d->scale_e), s);
+    }
+    if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
+    if (d->flavor == 0)
+        fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
+                            dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_A, bla_B, s);
+    RCK(cudaGetLastError(), "reference table kernels");
+    RCK(cudaStreamSynchronize(s), "reference table build");
+#undef RA
+#undef RCK
+    *out = r;
+    return FSG_OK;
+}
+
+int fsg_ref_destroy(fsg_ctx *ctx, fsg_ref *ref) {
+    if (!ref) return FSG_OK;
+    if (ctx) { cudaSetDevice(ctx->device); cudaStreamSynchronize(ctx->stream); }
+    ref_release(ref);
+    delete ref;
+    return FSG_OK;
+}
+
+int fsg_ref_info(const fsg_ref *ref, int64_t *len, int64_t *bla_len, int32_t *stages) {
+    if (!ref) return FSG_ERR_ARG;
+    if (len) *len = ref->len;
+    if (bla_len) *bla_len = ref->host.bla_len;
+    if (stages) *stages = ref->host.stages;
+    return FSG_OK;
+}
+
+int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0, void *out1) {
+    if (!ctx || !ref || !out0) return set_err(ctx, FSG_ERR_ARG, "NULL argument");
+    const RefDev &R = ref->host;
+    size_t len = (size_t)ref->len;
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    if (which == 0 || which == 1) {
+        size_t n = which == 0 ? len : len + 1;
+        const double2 *sp = which == 0 ? R.dZndc : R.dZndz;
+        const double2 *xm = which == 0 ? R.dZndc_xm : R.dZndz_xm;
+        const int *xe = which == 0 ? R.dZndc_xe : R.dZndz_xe;
+        if (sp) { CK(cudaMemcpy(out0, sp, 16 * n, cudaMemcpyDeviceToHost), "download path"); return FSG_OK; }
+        if (xm && out1) {
+            CK(cudaMemcpy(out0, xm, 16 * n, cudaMemcpyDeviceToHost), "download path");
+            CK(cudaMemcpy(out1, xe, 4 * n, cudaMemcpyDeviceToHost), "download path");
+            return FSG_OK;
+        }
+        return set_err(ctx, FSG_ERR_ARG, "path not built");
+    }
+    if (which == 2) {
+        if (R.bla_len <= 0 || !out1) return set_err(ctx, FSG_ERR_ARG, "no BLA tree");
+        if (R.Mbla) CK(cudaMemcpy(out0, R.Mbla, 32 * (size_t)R.bla_len, cudaMemcpyDeviceToHost), "download BLA");
+        else CK(cudaMemcpy(out0, R.Mbla_bs, 64 * (size_t)R.bla_len, cudaMemcpyDeviceToHost), "download BLA");
+        CK(cudaMemcpy(out1, R.rbla, 8 * (size_t)R.bla_len, cudaMemcpyDeviceToHost), "download BLA radii");
+        return FSG_OK;
+    }
+    if (which == 3) {
+        if (!R.dXa) return set_err(ctx, FSG_ERR_ARG, "no Jacobian paths");
+        double *o = (double *)out0;
+        CK(cudaMemcpy(o, R.dXa, 8 * len, cudaMemcpyDeviceToHost), "download");
+        CK(cudaMemcpy(o + len, R.dXb, 8 * len, cudaMemcpyDeviceToHost), "download");
+        CK(cudaMemcpy(o + 2 * len, R.dYa, 8 * len, cudaMemcpyDeviceToHost), "download");
+        CK(cudaMemcpy(o + 3 * len, R.dYb, 8 * len, cudaMemcpyDeviceToHost), "download");
+        return FSG_OK;
+    }
+    return set_err(ctx, FSG_ERR_ARG, "bad table selector");
+}
+
+int fsg_std_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+                  int32_t where) {
+    if (ctx) cudaSetDevice(ctx->device);
+    return run_tiles(ctx, calc, tiles, ntiles, where, false);
+}
+
+int fsg_perturb_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+                      int32_t where) {
+    if (ctx) cudaSetDevice(ctx->device);
+    return run_tiles(ctx, calc, tiles, ntiles, where, true);
+}
+
+int fsg_last_stats(const fsg_ctx *cctx, fsg_stats *out) {
+    fsg_ctx *ctx = const_cast<fsg_ctx *>(cctx);
+    if (!ctx || !out) return FSG_ERR_ARG;
+    memset(out, 0, sizeof(*out));
+    if (!ctx->timed) return FSG_OK;
+    CK(cudaEventSynchronize(ctx->ev1), "cudaEventSynchronize");
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "cudaEventElapsedTime");
+    unsigned long long st[4];
+    CK(cudaMemcpy(st, ctx->stats_dev, sizeof(st), cudaMemcpyDeviceToHost), "read stats");
+    out->kernel_ms = ms;
+    out->pixels = ctx->last_pixels;
+    out->pixel_iters = (int64_t)st[0];
+    out->full_steps = (int64_t)st[1];
+    out->bla_steps = (int64_t)st[2];
+    out->rebases = (int64_t)st[3];
+    return FSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+// fsg_internal.cuh -- device-side descriptors shared by the kernel translation
+// units and the C-ABI layer.  Everything here lives in device memory.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "fsg_num.cuh"
+
+#define FSG_MAX_TILES_PER_LAUNCH 1024
+#define FSG_STG_COMPRESSED 3          // settings.py:40 BLA_compression
+#define FSG_CANCEL_POLL 65536         // steps between two reads of the cancel flag
+
+// Reference orbit + derived tables (perturbation.py:317-375, 431-562)
+struct RefDev {
+    int len, div_iter, order, first_invalid;   // order clamped to INT32_MAX when none
+    int flavor;                                 // 0 = M2, 1..5 BS
+    int n_xr;
+    const double2 *Zn;          // [len + 1], Zn[len] = 0 (read when w reaches len)
+    const int *xr_slot;         // [len + 1]: -1 or index in the side table
+    const double2 *xr_m;        // [n_xr] Xrange mantissas (M2)
+    const int *xr_e;
+    // derivative paths, standard form
+    const double2 *dZndc;       // [len + 1]
+    const double2 *dZndz;       // [len + 2] (slot len = wrapped value)
+    // derivative paths, Xrange form
+    const double2 *dZndc_xm; const int *dZndc_xe;
+    const double2 *dZndz_xm; const int *dZndz_xe;
+    // BS Jacobian paths
+    const double *dXa, *dXb, *dYa, *dYb;        // [len + 1]
+    // BLA tree (compressed, perturbation.py:1819-1881)
+    const double2 *Mbla;        // M2: [bla_len][2] (A, B)
+    const double *Mbla_bs;      // BS: [bla_len][8]
+    const double *rbla;         // [bla_len]
+    int stages, bla_len;
+    // FE32 tables: int4 {x bits, y bits, exponent, aux}
+    const int4 *Zf;             // [len + 1]; aux = exponent of max(|x|,|y|) or FE_ZERO_E
+    const int4 *dZndc_f;        // [len + 1]
+    const int4 *dZndz_f;        // [len + 2]
+    const int4 *bla_f_A;        // [bla_len] A (x, y, e, r_bits)
+    const int4 *bla_f_B;        // [bla_len] B (x, y, e, r_e)
+};
+
+struct TileDev {
+    const RefDev *ref;
+    const double *xs, *ys;
+    int nx, ny;
+    double lin[4];
+    double cre, cim, dx;                       // standard loop
+    double dx_m; int dx_e;                     // perturbation
+    double drift_re, drift_im; int drift_e;
+    double drifty_m; int drifty_e;
+    void *Z; int nZ, i_dzndz, i_dzndc;
+    int *U; signed char *stop_reason; int *stop_iter;
+    double *pot, *dem;
+};
+
+struct CalcDev {
+    int max_iter;
+    double M2, eps2, logM;
+    int mode, calc_dzndc, interior, bla, flavor, xrsem;
+};
+
+// Work distribution of one launch: a device counter hands out pixel indices
+// of the concatenated tiles.
+struct WorkDev {
+    const TileDev *tiles;
+    const long long *start;          // [ntiles + 1] prefix sums of pixel counts
+    int ntiles;
+    long long total;
+    unsigned long long *counter;
+    unsigned long long *stats;       // [4]: pixel_iters, full_steps, bla_steps, rebases
+    volatile int *cancel;            // mapped host flag
+    int *status;                     // device status word (1 = interrupted)
+};
+
+// Claim the next pixel: returns false when the work is exhausted.
+__device__ __forceinline__ bool fsg_claim(const WorkDev &W, const long long *s_start,
+                                          int &t, long long &ip) {
+    unsigned long long g = atomicAdd(W.counter, 1ULL);
+    if ((long long)g >= W.total) return false;
+    int lo = 0, hi = W.ntiles - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (s_start[mid] <= (long long)g) lo = mid; else hi = mid - 1;
+    }
+    t = lo;
+    ip = (long long)g - s_start[lo];
+    return true;
+}
+
+__device__ __forceinline__ void fsg_load_starts(const WorkDev &W, long long *s_start) {
+    for (int i = threadIdx.x; i <= W.ntiles; i += blockDim.x) s_start[i] = W.start[i];
+    __syncthreads();
+}
+
+// Warp-reduced statistics (one atomic per warp per counter)
+__device__ __forceinline__ void fsg_flush_stats(const WorkDev &W, unsigned long long a,
+                                                unsigned long long b, unsigned long long c,
+                                                unsigned long long d) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+        d += __shfl_down_sync(0xffffffffu, d, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&W.stats[0], a); atomicAdd(&W.stats[1], b);
+        atomicAdd(&W.stats[2], c); atomicAdd(&W.stats[3], d);
+    }
+}
+
+// Potential (postproc.py:352-406 with Continuous_iter_pp_infinity :1001-1009,
+// d = 2, a_d = 1) and distance estimate (postproc.py:684-731).
+__device__ __forceinline__ void fsg_epilogue(const TileDev &T, const CalcDev &C, long long ip,
+                                             double2 zn, double absd, int n) {
+    if (T.pot == nullptr && T.dem == nullptr) return;
+    double az = hypot(zn.x, zn.y);
+    if (T.pot) {
+        double nu_frac = -(log(log(az) / C.logM) / 0.6931471805599453);
+        double x = -nu_frac;
+        double q = floor(x);
+        T.pot[ip] = ((double)n - q) - (x - q);
+    }
+    if (T.dem) T.dem[ip] = az * log(az) / absd;
+}
+
+// Kernel launchers (one per translation unit)
+void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);
+void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);
+void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
+                             cudaStream_t s);
+// Reference tables
+struct RefHost;   // defined in fsg_ref.cu

@@ -1,0 +1,236 @@
+// fsg_num.cuh -- device arithmetic for the escape-time kernels.
+//
+//   * complex double helpers with the operation order of numba / CPython
+//     complex128 ((a+bi)(c+di) = (ac-bd) + (ad+bc)i, a float is promoted to
+//     complex(x, 0) before a complex product);
+//   * xc: the "Xrange" extended-exponent complex of the reference
+//     (numpy_utils/numba_xr.py): complex128 mantissa + int32 exponent shared by
+//     both parts, lazy renormalisation when the unbiased exponent of a part
+//     leaves [-100, 100];
+//   * fe: the FP32-mantissa / int32-exponent complex used by the fast kernels,
+//     normalised so that max(|x|, |y|) is in [1, 2) (zero carries FE_ZERO_E).
+//
+// The translation units that must reproduce the reference's rounding are
+// compiled with -fmad=false, so every double operation below rounds once.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define FSG_DEV __device__ __forceinline__
+
+// ---------------------------------------------------------------------------
+// complex128
+// ---------------------------------------------------------------------------
+FSG_DEV double2 cx(double re, double im) { return make_double2(re, im); }
+FSG_DEV double2 cadd(double2 a, double2 b) { return cx(a.x + b.x, a.y + b.y); }
+FSG_DEV double2 cmul(double2 a, double2 b) {
+    return cx(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// float * complex: promote the float to complex(x, 0.) first
+FSG_DEV double2 rmul(double s, double2 b) { return cmul(cx(s, 0.), b); }
+FSG_DEV double2 caddr(double2 a, double s) { return cx(a.x + s, a.y + 0.); }
+
+// ---------------------------------------------------------------------------
+// Xrange complex (reference semantics, numba_xr.py)
+// ---------------------------------------------------------------------------
+struct xc { double re, im; int e; };
+struct xf { double m; int e; };
+
+FSG_DEV xc xc_make(double re, double im, int e) { xc r; r.re = re; r.im = im; r.e = e; return r; }
+FSG_DEV xc xc_zero() { return xc_make(0., 0., 0); }
+
+// numba_xr.py _frexp: rewrite the biased exponent to 1023, m in [1, 2)
+FSG_DEV double xr_frexp(double m, int &e) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(m);
+    e = (int)((b >> 52) & 0x7ff) - 0x3ff;
+    return __longlong_as_double((long long)((b & 0x8000000000000000ULL) + (0x3ffULL << 52)
+                                            + (b & 0xfffffffffffffULL)));
+}
+FSG_DEV double xr_norm_real(double m, int exp, int &eo) {
+    if (m == 0.) { eo = 0; return m; }
+    int ne; double nm = xr_frexp(m, ne);
+    eo = exp + ne; return nm;
+}
+// numba_xr.py _exp2_shift: add to the biased exponent, clamped at 0
+FSG_DEV double xr_exp2_shift(double m, long long shift) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(m);
+    long long ex = (long long)((b >> 52) & 0x7ff) + shift;
+    if (ex < 0) ex = 0;
+    return __longlong_as_double((long long)((b & 0x8000000000000000ULL)
+                                            + ((unsigned long long)ex << 52)
+                                            + (b & 0xfffffffffffffULL)));
+}
+FSG_DEV bool xr_need_renorm_r(double m) {
+    long long d = (long long)(((unsigned long long)__double_as_longlong(m) >> 52) & 0x7ff) - 1023;
+    return (d < 0 ? -d : d) > 100;
+}
+FSG_DEV bool xr_need_renorm_c(double2 m) { return xr_need_renorm_r(m.x) || xr_need_renorm_r(m.y); }
+
+FSG_DEV void xr_coexp_r(double m0, int e0, double m1, int e1, double &o0, double &o1, int &eo) {
+    long long d = (long long)e0 - (long long)e1;
+    if (m0 == 0.) { eo = e1; }
+    else if (m1 == 0.) { eo = e0; }
+    else if (e1 > e0) { m0 = xr_exp2_shift(m0, d); eo = e1; }
+    else if (e0 > e1) { m1 = xr_exp2_shift(m1, -d); eo = e0; }
+    else { eo = e0; }
+    o0 = m0; o1 = m1;
+}
+FSG_DEV void xr_coexp_c(double2 m0, int e0, double2 m1, int e1, double2 &o0, double2 &o1, int &eo) {
+    long long d = (long long)e0 - (long long)e1;
+    if (m0.x == 0. && m0.y == 0.) { eo = e1; }
+    else if (m1.x == 0. && m1.y == 0.) { eo = e0; }
+    else if (e1 > e0) { m0 = cx(xr_exp2_shift(m0.x, d), xr_exp2_shift(m0.y, d)); eo = e1; }
+    else if (e0 > e1) { m1 = cx(xr_exp2_shift(m1.x, -d), xr_exp2_shift(m1.y, -d)); eo = e0; }
+    else { eo = e0; }
+    o0 = m0; o1 = m1;
+}
+FSG_DEV xc xr_normalize_c(double2 m, int exp) {
+    int ere, eim;
+    double nre = xr_norm_real(m.x, exp, ere), nim = xr_norm_real(m.y, exp, eim);
+    double cr, ci; int ce;
+    xr_coexp_r(nre, ere, nim, eim, cr, ci, ce);
+    return xc_make(cr, ci, ce);
+}
+FSG_DEV xc xr_from(double2 z) { return xr_normalize_c(z, 0); }
+FSG_DEV double2 xm(xc a) { return cx(a.re, a.im); }
+FSG_DEV xc xr_add(xc a, xc b) {
+    double2 o0, o1; int e;
+    xr_coexp_c(xm(a), a.e, xm(b), b.e, o0, o1, e);
+    double2 s = cadd(o0, o1);
+    return xc_make(s.x, s.y, e);
+}
+FSG_DEV xc xr_add_s(xc a, double2 z) {
+    xc b = xr_need_renorm_c(z) ? xr_normalize_c(z, 0) : xc_make(z.x, z.y, 0);
+    return xr_add(a, b);
+}
+FSG_DEV xc xr_mul(xc a, xc b) {
+    double2 m = cmul(xm(a), xm(b));
+    int e = (int)((unsigned)a.e + (unsigned)b.e);
+    if (xr_need_renorm_c(m)) return xr_normalize_c(m, e);
+    return xc_make(m.x, m.y, e);
+}
+FSG_DEV xc xr_mul_s(double2 s, xc b) {
+    double2 m = cmul(s, xm(b));
+    if (xr_need_renorm_c(m)) return xr_normalize_c(m, b.e);
+    return xc_make(m.x, m.y, b.e);
+}
+FSG_DEV xc xr_mul_r(double s, xc b) {
+    double2 m = rmul(s, xm(b));
+    if (xr_need_renorm_c(m)) return xr_normalize_c(m, b.e);
+    return xc_make(m.x, m.y, b.e);
+}
+FSG_DEV xc xf_mul_c(xf a, double2 z) {
+    double2 m = rmul(a.m, z);
+    if (xr_need_renorm_c(m)) return xr_normalize_c(m, a.e);
+    return xc_make(m.x, m.y, a.e);
+}
+FSG_DEV xf xr_abs2(xc a) {
+    xf r; r.m = a.re * a.re + a.im * a.im; r.e = (int)((unsigned)a.e + (unsigned)a.e); return r;
+}
+FSG_DEV bool xf_lt_s(xf a, double x) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, x, 0, o0, o1, e); return o0 < o1;
+}
+FSG_DEV bool xf_le(xf a, xf b) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, b.m, b.e, o0, o1, e); return o0 <= o1;
+}
+// ldexp(1., e) for any int e (exact power of two, 0 below 2^-1074, inf above)
+FSG_DEV double pow2d(int e) {
+    if (e > 1023) return __longlong_as_double(0x7ff0000000000000LL);
+    if (e >= -1022) return __longlong_as_double((long long)(e + 1023) << 52);
+    if (e >= -1074) return __longlong_as_double(1LL << (e + 1074));
+    return 0.;
+}
+FSG_DEV double2 xr_to_std(xc a) {
+    int ere, eim;
+    double nre = xr_norm_real(a.re, a.e, ere), nim = xr_norm_real(a.im, a.e, eim);
+    double cr, ci; int ce;
+    xr_coexp_r(nre, ere, nim, eim, cr, ci, ce);
+    return rmul(pow2d(ce), cx(cr, ci));
+}
+// ldexp(m, e) with one rounding (m is in [1, 2) or a small normal number)
+FSG_DEV double ldexp_d(double m, int e) {
+    if (e >= -1022 && e <= 1023) return m * pow2d(e);
+    if (e > 1023) return (m * pow2d(e - 1023)) * pow2d(1023);
+    // subnormal results: scale into range first so only the last product rounds
+    if (e < -2200) return 0. * m;
+    return (m * pow2d(e + 1000)) * pow2d(-1000);
+}
+
+// ---------------------------------------------------------------------------
+// fe: FP32 mantissa + int32 exponent (the fast form)
+// ---------------------------------------------------------------------------
+#define FE_ZERO_E (-(1 << 29))
+struct fe { float x, y; int e; };
+
+FSG_DEV fe fe_make(float x, float y, int e) { fe r; r.x = x; r.y = y; r.e = e; return r; }
+FSG_DEV fe fe_zero() { return fe_make(0.f, 0.f, FE_ZERO_E); }
+// 2^k as a float for k <= 0 (0 below 2^-126)
+FSG_DEV float exp2neg(int k) {
+    k = max(k, -127);
+    return __int_as_float((k + 127) << 23);
+}
+// exponent of max(|x|, |y|) (biased; 0 for zero / subnormal)
+FSG_DEV int fe_bexp(float x, float y) {
+    float a = fmaxf(fabsf(x), fabsf(y));
+    return (__float_as_int(a) >> 23) & 0xff;
+}
+FSG_DEV fe fe_norm(fe a) {
+    int b = fe_bexp(a.x, a.y);
+    if (b == 0) return fe_zero();
+    float s = __int_as_float((254 - b) << 23);   // 2^(127 - b)
+    return fe_make(a.x * s, a.y * s, a.e + (b - 127));
+}
+FSG_DEV fe fe_add(fe a, fe b) {
+    int d = a.e - b.e;
+    if (d >= 0) {
+        float s = exp2neg(-d);
+        return fe_make(fmaf(b.x, s, a.x), fmaf(b.y, s, a.y), a.e);
+    }
+    float s = exp2neg(d);
+    return fe_make(fmaf(a.x, s, b.x), fmaf(a.y, s, b.y), b.e);
+}
+FSG_DEV fe fe_mul(fe a, fe b) {
+    return fe_make(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x, a.e + b.e);
+}
+FSG_DEV fe fe_scale2(fe a, int k) { return fe_make(a.x, a.y, a.e + k); }
+// from a double complex (exact exponent, mantissa rounded to float)
+FSG_DEV fe fe_from_d(double2 z) {
+    double a = fmax(fabs(z.x), fabs(z.y));
+    if (a == 0.) return fe_zero();
+    int e;
+    frexp(a, &e);              // a = f * 2^e, f in [0.5, 1)
+    e -= 1;
+    double s = pow2d(-e);
+    if (e < -1022) s = pow2d(-e - 100) * pow2d(100);
+    return fe_make((float)(z.x * s), (float)(z.y * s), e);
+}
+FSG_DEV fe fe_from_xc(xc v) {
+    fe r = fe_from_d(xm(v));
+    if (r.e != FE_ZERO_E) r.e += v.e;
+    return r;
+}
+// value as a double complex (underflows to 0 like to_standard)
+FSG_DEV double2 fe_to_d(fe a) {
+    if (a.e == FE_ZERO_E || (a.x == 0.f && a.y == 0.f)) return cx(0., 0.);
+    return cx(ldexp_d((double)a.x, a.e), ldexp_d((double)a.y, a.e));
+}
+// value as a float complex (flushes below 2^-126)
+FSG_DEV float2 fe_to_f(fe a) {
+    if (a.e > 0) {
+        float s = __int_as_float((min(a.e, 127) + 127) << 23);
+        return make_float2(a.x * s, a.y * s);
+    }
+    float s = exp2neg(a.e);
+    return make_float2(a.x * s, a.y * s);
+}
+// |a|^2 < t (t a positive double threshold, a normalised or not)
+FSG_DEV bool fe_abs2_lt(fe a, double t) {
+    float m2 = a.x * a.x + a.y * a.y;
+    if (m2 == 0.f) return 0. < t;
+    // compare log2 magnitudes first, exact compare only when close
+    double lhs = (double)m2 * 1.0;
+    int e2 = 2 * a.e;
+    if (e2 < -2000) return true;
+    if (e2 > 2000) return false;
+    return ldexp_d(lhs, e2) < t;
+}

@@ -1,0 +1,123 @@
+// fsg_std.cu -- standard (non-perturbation) escape-time loops, FP64.
+//
+// Power-2 Mandelbrot: core.py:2935-3004 numba_cycles / numba_iterate and
+// models/mandelbrot_M2.py:309-334 iterate_once.  Burning Ship family:
+// core.py:3007-3056 numba_iterate_BS and models/burning_ship.py:350-434.
+// The reference compiles these without fastmath, so this file is built with
+// -fmad=false: each operation rounds once, in the order of the reference.
+#include "fsg_internal.cuh"
+
+__device__ __forceinline__ double sgn(double x) { return x < 0. ? -1. : 1.; }
+
+// core.py:3161-3194 c_from_pix, Cartesian projection
+__device__ __forceinline__ double2 std_c(const TileDev &T, long long ip) {
+    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
+    double px = T.xs[ix], py = T.ys[iy];
+    double x1 = T.lin[0] * px + T.lin[1] * py;
+    double y1 = T.lin[2] * px + T.lin[3] * py;
+    return cadd(cx(T.cre, T.cim), rmul(T.dx, cx(x1, y1)));
+}
+
+__global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
+    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    fsg_load_starts(W, s_start);
+    unsigned long long it_sum = 0, steps = 0;
+    int t; long long ip;
+    while (fsg_claim(W, s_start, t, ip)) {
+        const TileDev &T = W.tiles[t];
+        long long np = (long long)T.nx * T.ny;
+        double2 c = std_c(T, ip);
+        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.);
+        int n = 0; signed char reason = -1;
+        for (;;) {
+            n += 1;
+            if (n >= C.max_iter) { reason = 0; break; }
+            dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);
+            dzndz = cmul(rmul(2., dzndz), zn);
+            zn = cadd(cmul(zn, zn), c);
+            if (n == 1) dzndz = cx(1., 0.);
+            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; break; }
+            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; break; }
+        }
+        double2 *Z = (double2 *)T.Z;
+        Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
+        T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
+        fsg_epilogue(T, C, ip, zn, hypot(dzndc.x, dzndc.y), n);
+        it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+    }
+    fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
+}
+
+__global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
+    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    fsg_load_starts(W, s_start);
+    unsigned long long it_sum = 0, steps = 0;
+    const int flavor = C.flavor;
+    int t; long long ip;
+    while (fsg_claim(W, s_start, t, ip)) {
+        const TileDev &T = W.tiles[t];
+        long long np = (long long)T.nx * T.ny;
+        double2 c = std_c(T, ip);
+        double a = c.x, b = c.y;
+        double X = 0., Y = 0., dXdA = 0., dXdB = 0., dYdA = 0., dYdB = 0.;
+        int n = 0; signed char reason = -1;
+        for (;;) {
+            n += 1;
+            if (n >= C.max_iter) { reason = 0; break; }
+            double nX, nY, nXa, nXb, nYa, nYb;
+            if (flavor == 1) {
+                nX = X * X - Y * Y + a;
+                nY = 2. * fabs(X * Y) - b;
+                nXa = 2. * (X * dXdA - Y * dYdA) + 1.;
+                nXb = 2. * (X * dXdB - Y * dYdB);
+                nYa = 2. * (fabs(X) * sgn(Y) * dYdA + sgn(X) * dXdA * fabs(Y));
+                nYb = 2. * (fabs(X) * sgn(Y) * dYdB + sgn(X) * dXdB * fabs(Y)) - 1.;
+            } else if (flavor == 2) {
+                nX = X * X - Y * Y + a;
+                nY = 2. * X * fabs(Y) - b;
+                nXa = 2. * (X * dXdA - Y * dYdA) + 1.;
+                nXb = 2. * (X * dXdB - Y * dYdB);
+                nYa = 2. * (X * sgn(Y) * dYdA + dXdA * fabs(Y));
+                nYb = 2. * (X * sgn(Y) * dYdB + dXdB * fabs(Y)) - 1.;
+            } else if (flavor == 3) {
+                nX = X * X - Y * fabs(Y) + a;
+                nY = 2. * X * Y - b;
+                nXa = 2. * (X * dXdA - fabs(Y) * dYdA) + 1.;
+                nXb = 2. * (X * dXdB - fabs(Y) * dYdB);
+                nYa = 2. * (dXdA * Y + X * dYdA);
+                nYb = 2. * (dXdB * Y + X * dYdB) - 1.;
+            } else if (flavor == 4) {
+                double q = X * X - Y * Y;
+                nX = fabs(q) + a;
+                nY = 2. * X * Y - b;
+                nXa = 2. * sgn(q) * (X * dXdA - Y * dYdA);
+                nXb = 2. * sgn(q) * (X * dXdB - Y * dYdB);
+                nYa = 2. * (dXdA * Y + X * dYdA);
+                nYb = 2. * (dXdB * Y + X * dYdB) - 1.;
+            } else {
+                double q = X * X - Y * Y;
+                nX = fabs(q) + a;
+                nY = 2. * fabs(X * Y) - b;
+                nXa = 2. * sgn(q) * (X * dXdA - Y * dYdA);
+                nXb = 2. * sgn(q) * (X * dXdB - Y * dYdB);
+                nYa = 2. * (fabs(X) * sgn(Y) * dYdA + sgn(X) * dXdA * fabs(Y));
+                nYb = 2. * (fabs(X) * sgn(Y) * dYdB + sgn(X) * dXdB * fabs(Y)) - 1.;
+            }
+            X = nX; Y = nY; dXdA = nXa; dXdB = nXb; dYdA = nYa; dYdB = nYb;
+            if (X * X + Y * Y > C.M2) { reason = 1; break; }
+        }
+        double *Z = (double *)T.Z;
+        Z[ip] = X; Z[np + ip] = Y; Z[2 * np + ip] = dXdA; Z[3 * np + ip] = dXdB;
+        Z[4 * np + ip] = dYdA; Z[5 * np + ip] = dYdB;
+        T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
+        double absd = 0.5 * (hypot(dXdA + dYdB, dXdB - dYdA) + hypot(dXdA - dYdB, dXdB + dYdA));
+        fsg_epilogue(T, C, ip, cx(X, Y), absd, n);
+        it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+    }
+    fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
+}
+
+void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
+    if (C.flavor == 0) k_std_m2<<<grid, block, 0, s>>>(W, C);
+    else k_std_bs<<<grid, block, 0, s>>>(W, C);
+}

@@ -1,0 +1,158 @@
+/*
+ * fsgpu.h -- C-ABI of the GB300 escape-time / perturbation kernels.
+ *
+ * Drop-in boundary for Fractalshades' per-pixel iteration hot path.  Each entry
+ * point replaces one reference interface (paths relative to src/fractalshades/):
+ *
+ *   fsg_std_tiles      <- Fractal.numba_cycle_call -> numba_cycles
+ *                         (core.py:2022-2027, 2935-3056) for the standard
+ *                         Mandelbrot / Burning Ship loops
+ *   fsg_ref_create     <- PerturbationFractal.get_cycle_indep_args
+ *                         (perturbation.py:431-562): uploads the reference
+ *                         orbit and builds on the GPU the derivative paths
+ *                         (numba_dZndc_path :2282, numba_dZndz_path :2466,
+ *                         numba_dZndc_path_BS :2339) and the BLA tree
+ *                         (numba_make_BLA :1819, numba_make_BLA_BS :1884)
+ *   fsg_perturb_tiles  <- PerturbationFractal.numba_cycle_call ->
+ *                         numba_cycles_perturb(_BS) (perturbation.py:414-428,
+ *                         988-1811), plus the potential / distance estimate of
+ *                         postproc.py:352-406, 684-731, 1001-1009 fused in the
+ *                         kernel epilogue
+ *   fsg_cancel         <- Fractal.raise_interruption (core.py:2011) polled by
+ *                         the kernels like _interrupted (perturbation.py:1042)
+ *
+ * Conventions: plain pointers and sizes only; complex arrays are interleaved
+ * (re, im) doubles (numpy complex128); Z is laid out [nZ][npix], pixels of a
+ * tile in row-major order with x fastest (the ravel of the reference's
+ * meshgrid, core.py:1820).  Every function returns FSG_OK or an error code and
+ * never throws; fsg_last_error() gives the message.
+ */
+#ifndef FSGPU_H
+#define FSGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSG_OK 0
+#define FSG_INTERRUPTED 1      /* USER_INTERRUPTED (perturbation.py:984)      */
+#define FSG_ERR_ARG (-1)
+#define FSG_ERR_CUDA (-2)
+#define FSG_ERR_NOMEM (-3)
+#define FSG_ERR_NODEV (-4)
+
+/* delta arithmetic of the perturbation kernels */
+#define FSG_MODE_FP64 0  /* double deltas: the reference with xr_detect_activated False   */
+#define FSG_MODE_XR64 1  /* Xrange deltas, double mantissa + int32 exponent: the reference
+                            with xr_detect_activated True (dx < settings.xrange_zoom_level) */
+#define FSG_MODE_FE32 2  /* float mantissa + int32 exponent deltas (fast form)           */
+
+/* where the tile buffers live */
+#define FSG_HOST 0       /* host pointers: the library stages the copies            */
+#define FSG_DEVICE 1     /* device pointers: asynchronous on the context stream     */
+
+typedef struct fsg_ctx fsg_ctx;
+typedef struct fsg_ref fsg_ref;
+
+/* Reference orbit and the tables derived from it (perturbation.py:317-375,
+ * 431-562).  All pointers are host pointers. */
+typedef struct {
+    const double *Zn;         /* complex128 [len]: FP64 orbit, Zn[0] = 0        */
+    int64_t len;              /* ref_orbit_len                                   */
+    int64_t div_iter;         /* ref_div_iter (first invalid iteration)          */
+    int64_t order;            /* ref_order (cycle length), <= 0 when none        */
+    int32_t n_xr;             /* sparse Xrange side table (ref_index_xr, ref_xr) */
+    const int32_t *xr_idx;    /* [n_xr], increasing                              */
+    const double *xr_m;       /* M2: complex128 mantissas [n_xr]; BS: [n_xr] x
+                                 then [n_xr] y float64 mantissas                 */
+    const int32_t *xr_e;      /* M2: [n_xr]; BS: [2 * n_xr] (x then y)           */
+    int32_t flavor;           /* 0 = power-2 Mandelbrot, 1..5 Burning Ship       */
+    int32_t xr_paths;         /* derivative paths in Xrange form                 */
+    int32_t calc_dzndc;       /* build dZndc (M2) / the Jacobian paths (BS)      */
+    int32_t calc_dzndz;       /* build dZndz (M2, interior detection)            */
+    double scale_m;           /* dx * projection.scale as a float64 Xrange       */
+    int32_t scale_e;
+    int32_t bla;              /* build the BLA tree                              */
+    double kc;                /* to_standard(kc) (perturbation.py:1830)          */
+    double bla_eps;
+} fsg_ref_desc;
+
+/* Calculation options (the calc_std_div keyword arguments). */
+typedef struct {
+    int64_t max_iter;
+    double M_divergence;
+    double epsilon_stationnary;
+    int32_t mode;             /* FSG_MODE_*                                      */
+    int32_t calc_dzndc;       /* M2: dzndc; BS: calc_hessian                     */
+    int32_t interior;         /* M2 interior_detect (dzndz)                      */
+    int32_t bla;              /* BLA_activated                                   */
+    int32_t flavor;           /* 0 = M2, 1..5 Burning Ship                       */
+    int32_t xr_semantics;     /* FE32 only: follow the Xrange branch's rebase
+                                 confirmation (reference xr_detect_activated)    */
+} fsg_calc;
+
+/* One tile: a rectangle of pixels with its own view and outputs. */
+typedef struct {
+    int32_t nx, ny;
+    const double *xs;         /* [nx] screen fraction per column                 */
+    const double *ys;         /* [ny] screen fraction per row (already negated and
+                                 divided by xy_ratio, core.py:1820-1830)          */
+    double lin_mat[4];        /* rotation / skew (core.py:1470-1484), row-major   */
+    /* standard loop: c = center + dx * lin_mat . pix */
+    double center_re, center_im, dx;
+    /* perturbation: dc = dx_xr * lin_mat . pix + drift_xr */
+    double dx_m; int32_t dx_e;
+    double drift_re, drift_im; int32_t drift_e;   /* M2 complex drift; BS: driftx in
+                                                     drift_re with drift_e      */
+    double drifty_m; int32_t drifty_e;            /* BS: drifty                 */
+    fsg_ref *ref;
+    /* outputs, [nZ][nx*ny] etc.; potential / dem may be NULL */
+    void *Z; int32_t nZ; int32_t i_dzndz; int32_t i_dzndc;
+    int32_t *U; int8_t *stop_reason; int32_t *stop_iter;
+    double *potential; double *dem;
+} fsg_tile;
+
+/* Launch statistics of the last fsg_*_tiles call. */
+typedef struct {
+    double kernel_ms;          /* device time of the iteration kernel            */
+    int64_t pixels;
+    int64_t pixel_iters;       /* sum of stop_iter                               */
+    int64_t full_steps;        /* executed perturbation / standard steps         */
+    int64_t bla_steps;         /* executed BLA steps                             */
+    int64_t rebases;
+} fsg_stats;
+
+const char *fsg_version(void);
+int fsg_ctx_create(int device, fsg_ctx **out);
+int fsg_ctx_destroy(fsg_ctx *ctx);
+const char *fsg_last_error(const fsg_ctx *ctx);
+/* Use an external CUDA stream (cudaStream_t as void*) instead of the
+ * context's own; NULL restores it. */
+int fsg_set_stream(fsg_ctx *ctx, void *stream);
+int fsg_sync(fsg_ctx *ctx);
+
+int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *desc, fsg_ref **out);
+int fsg_ref_destroy(fsg_ctx *ctx, fsg_ref *ref);
+/* Copy tables back to the host (tests).  which: 0 dZndc (complex128 [len]) or
+ * its Xrange form (mantissa complex128 [len] + exp int32 [len]), 1 dZndz
+ * ([len + 1]), 2 BLA (M complex128 [bla_len][2], r float64 [bla_len]),
+ * 3 BS Jacobian paths (4 x float64 [len]).  Sizes via fsg_ref_info. */
+int fsg_ref_info(const fsg_ref *ref, int64_t *len, int64_t *bla_len, int32_t *stages);
+int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0,
+                     void *out1);
+
+int fsg_std_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
+                  int32_t ntiles, int32_t where);
+int fsg_perturb_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
+                      int32_t ntiles, int32_t where);
+int fsg_last_stats(const fsg_ctx *ctx, fsg_stats *out);
+
+int fsg_cancel(fsg_ctx *ctx);
+int fsg_clear_cancel(fsg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSGPU_H */

@@ -1,0 +1,236 @@
+"""
+GPU kernels against the CPU oracle, through the C-ABI (include/fsgpu.h).
+
+Inputs are the golden fixtures (reference orbits, pixel grids) of
+tests/golden/.  The FP64 and Xrange (XR64) kernels reproduce the oracle's
+operation order (-fmad=false): integer outputs must agree on >= 99.99 % of the
+pixels with the rest within 1 iteration, floating outputs within 1e-6
+relative.  The FE32 kernel is held to the same iteration-count criterion.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(G, name + ".npz"), allow_pickle=False)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from fractalshades_gb300 import _native as nat
+    c = nat.Context(0)
+    yield c
+    c.close()
+
+
+def axes(pix, nx):
+    pix = np.asarray(pix)
+    xs = np.ascontiguousarray(pix[:nx].real)
+    ys = np.ascontiguousarray(pix[::nx].imag)
+    ny = ys.size
+    assert np.array_equal(pix, (xs[None, :] + 1j * ys[:, None]).ravel()) or \
+        np.array_equal(pix.real, np.tile(xs, ny))
+    return xs, ys
+
+
+def iter_agree(a, b, frac=0.9999, tol=1):
+    a = np.asarray(a).ravel().astype(np.int64)
+    b = np.asarray(b).ravel().astype(np.int64)
+    same = np.mean(a == b)
+    assert same >= frac, f"only {same:.6f} of the iteration counts agree"
+    assert np.max(np.abs(a - b)) <= tol or same == 1.0 or np.mean(np.abs(a - b) <= tol) >= frac
+
+
+def rel_close(a, b, rtol=1e-6, mask=None):
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    if mask is not None:
+        a, b = a[mask.ravel()], b[mask.ravel()]
+    ok = np.isfinite(a) & np.isfinite(b)
+    assert np.array_equal(np.isfinite(a), np.isfinite(b))
+    err = np.abs(a[ok] - b[ok]) / np.maximum(np.abs(b[ok]), 1e-300)
+    assert err.size == 0 or np.max(err) <= rtol, f"max rel err {np.max(err)}"
+
+
+# ---------------------------------------------------------------------------
+def test_std_m2_bit_exact_vs_oracle(ctx):
+    from fractalshades_gb300 import _native as nat
+    d = load("std_m2")
+    nx = int(d["nx"])
+    xs, ys = axes(d["pix"], nx)
+    n = xs.size * ys.size
+    Z = np.zeros((3, n), dtype=np.complex128)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    pot = np.zeros(n)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, stop_reason=sr, stop_iter=si,
+                      center=complex(*d["center"]), dx=float(d["dx"]), potential=pot)
+    calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                         epsilon_stationnary=float(d["eps"]), flavor=0)
+    ctx.std_tiles(calc, [t])
+    assert np.array_equal(si, d["stop_iter"])
+    assert np.array_equal(sr, d["stop_reason"])
+    assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
+    st = ctx.stats()
+    assert st["pixel_iters"] == int(d["stop_iter"].sum())
+
+
+def test_std_m2_full_config_vs_oracle(ctx):
+    """800 x 600, x=-0.5, dx=3, max_iter 1000, M 1000 (the standard-loop
+    configuration), bit-exact against the oracle."""
+    from fractalshades_gb300 import _native as nat
+    nx, ny = 800, 600
+    kx, ky = 0.5 / (nx - 1), 0.5 / (ny - 1)
+    xs = np.linspace(kx * (-nx + 1), kx * (nx - 1), nx)
+    ys = -np.linspace(ky * (-ny + 1), ky * (ny - 1), ny) / (4. / 3.)
+    pix = (xs[None, :] + 1j * ys[:, None]).ravel()
+    lin = np.array([[1., -0.], [0., 1.]])
+    Zo, sio, sro = orc.std_m2(pix, -0.5 + 0j, lin, 3.0, 1000, 1000., 0.01)
+    n = nx * ny
+    Z = np.zeros((3, n), dtype=np.complex128)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=lin, Z=Z, stop_reason=sr, stop_iter=si,
+                      center=-0.5 + 0j, dx=3.0)
+    ctx.std_tiles(nat.make_calc(max_iter=1000, M_divergence=1000., epsilon_stationnary=0.01), [t])
+    assert np.array_equal(si, sio)
+    assert np.array_equal(sr, sro)
+    assert np.array_equal(Z.view(np.uint64), Zo.view(np.uint64))
+
+
+@pytest.mark.parametrize("flavor", [1, 2, 3, 4, 5])
+def test_std_bs_vs_oracle(ctx, flavor):
+    from fractalshades_gb300 import _native as nat
+    d = load("std_bs")
+    pix = d[f"pix_{flavor}"]
+    nx = int(round(np.sqrt(pix.size)))
+    xs, ys = axes(pix, nx)
+    n = pix.size
+    Z = np.zeros((6, n))
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, stop_reason=sr, stop_iter=si,
+                      center=complex(*d["center"]), dx=float(d["dx"]))
+    ctx.std_tiles(nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                                flavor=flavor), [t])
+    assert np.array_equal(si, d[f"stop_iter_{flavor}"])
+    assert np.array_equal(sr, d[f"stop_reason_{flavor}"])
+    assert np.array_equal(Z.view(np.uint64), d[f"Z_{flavor}"].view(np.uint64))
+
+
+# ---------------------------------------------------------------------------
+def _ref_from_golden(ctx, d, xr_paths):
+    from fractalshades_gb300 import _native as nat
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    return nat.Reference(
+        ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
+        xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"], xr_paths=xr_paths,
+        calc_dzndc=True, calc_dzndz=bool(d["interior"]), scale_m=float(d["dx_m"]),
+        scale_e=int(d["dx_e"]), bla=True, kc=kc, bla_eps=float(d["bla_eps"]))
+
+
+def _run_m2(ctx, d, ref, mode, xr_sem):
+    from fractalshades_gb300 import _native as nat
+    nx = int(round(np.sqrt(d["pix"].size)))
+    xs, ys = axes(d["pix"], nx)
+    n = d["pix"].size
+    interior = bool(d["interior"])
+    nZ = 2 + int(interior)
+    Z = np.zeros((nZ, n), dtype=np.complex128)
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
+                      stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                      drift_m=complex(d["drift_m"]), drift_e=int(d["drift_e"]),
+                      i_dzndz=1 if interior else -1, i_dzndc=nZ - 1)
+    calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                         epsilon_stationnary=float(d["eps_stat"]), mode=mode,
+                         calc_dzndc=True, interior=interior, bla=True,
+                         xr_semantics=xr_sem)
+    ctx.perturb_tiles(calc, [t])
+    return Z, U, sr, si
+
+
+M2_CASES = ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr", "pert_m2_xr_div"]
+
+
+@pytest.mark.parametrize("case", M2_CASES)
+def test_ref_tables_vs_oracle(ctx, case):
+    d = load(case)
+    xr = bool(d["xr_mode"])
+    ref = _ref_from_golden(ctx, d, xr)
+    M, r = ref.download("bla")
+    np.testing.assert_allclose(r, d["r_bla"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(M, d["M_bla"], rtol=1e-14, atol=0)
+    dz = ref.download("dzndc")
+    if xr:
+        got = dz[0] * np.exp2(dz[1].astype(float) + 900.)
+        exp = d["dZndc_m"] * np.exp2(d["dZndc_e"].astype(float) + 900.)
+        np.testing.assert_allclose(got, exp, rtol=1e-15)
+    else:
+        assert np.array_equal(dz.view(np.uint64), d["dZndc"].view(np.uint64))
+
+
+@pytest.mark.parametrize("case", M2_CASES)
+def test_perturb_m2_reference_branch_vs_oracle(ctx, case):
+    """FP64 kernel on the standard-branch cases, XR64 on the Xrange cases."""
+    d = load(case)
+    xr = bool(d["xr_mode"])
+    ref = _ref_from_golden(ctx, d, xr)
+    Z, U, sr, si = _run_m2(ctx, d, ref, "xr64" if xr else "fp64", xr)
+    iter_agree(si, d["stop_iter"])
+    assert np.mean(sr == d["stop_reason"]) >= 0.9999
+    same = (si == d["stop_iter"]).ravel()
+    rel_close(Z[0], d["Z"][0], 1e-6, same)
+    rel_close(Z[-1], d["Z"][-1], 1e-6, same)
+
+
+@pytest.mark.parametrize("case", M2_CASES)
+def test_perturb_m2_fe32_vs_oracle(ctx, case):
+    d = load(case)
+    xr = bool(d["xr_mode"])
+    ref = _ref_from_golden(ctx, d, xr)
+    Z, U, sr, si = _run_m2(ctx, d, ref, "fe32", xr)
+    iter_agree(si, d["stop_iter"], frac=0.99, tol=2)
+    assert np.mean(sr == d["stop_reason"]) >= 0.99
+
+
+@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4"])
+def test_perturb_bs_vs_oracle(ctx, case):
+    from fractalshades_gb300 import _native as nat
+    d = load(case)
+    fl = int(d["flavor"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    ref = nat.Reference(ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
+                        flavor=fl, calc_dzndc=True, scale_m=float(d["dx_m"]),
+                        scale_e=int(d["dx_e"]), bla=True, kc=kc, bla_eps=float(d["bla_eps"]))
+    paths = ref.download("bs_paths")
+    for k, name in enumerate(["dXa", "dXb", "dYa", "dYb"]):
+        assert np.array_equal(paths[k].view(np.uint64), d[name].view(np.uint64))
+    nx = int(round(np.sqrt(d["pix"].size)))
+    xs, ys = axes(d["pix"], nx)
+    n = d["pix"].size
+    Z = np.zeros((6, n))
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
+                      stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                      drift_m=float(d["driftx_m"]), drift_e=int(d["driftx_e"]),
+                      drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]))
+    calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]), flavor=fl,
+                         calc_dzndc=True, bla=True)
+    ctx.perturb_tiles(calc, [t])
+    iter_agree(si, d["stop_iter"])
+    same = (si == d["stop_iter"]).ravel()
+    for k in range(6):
+        rel_close(Z[k], d["Z"][k], 1e-6, same)
