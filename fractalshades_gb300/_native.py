@@ -53,7 +53,7 @@ class Calc(ct.Structure):
 
 class Tile(ct.Structure):
     _fields_ = [
-        ("nx", I32), ("ny", I32), ("xs", P), ("ys", P), ("lin_mat", F64 * 4),
+        ("nx", I32), ("ny", I32), ("xs", P), ("ys", P), ("pix", P), ("lin_mat", F64 * 4),
         ("center_re", F64), ("center_im", F64), ("dx", F64),
         ("dx_m", F64), ("dx_e", I32), ("drift_re", F64), ("drift_im", F64),
         ("drift_e", I32), ("drifty_m", F64), ("drifty_e", I32), ("ref", P),
@@ -256,15 +256,19 @@ class Reference:
         raise ValueError(which)
 
 
-def make_tile(*, xs, ys, lin_mat, Z, stop_reason, stop_iter, U=None, ref=None,
-              center=0j, dx=0.0, dx_m=0.0, dx_e=0, drift_m=0j, drift_e=0,
+def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None, U=None,
+              ref=None, center=0j, dx=0.0, dx_m=0.0, dx_e=0, drift_m=0j, drift_e=0,
               drifty_m=0.0, drifty_e=0, i_dzndz=-1, i_dzndc=-1, potential=None,
               dem=None, keep=None):
-    """Fill a Tile from numpy (host) arrays; pointers of device arrays can be
-    given as ints through the *_ptr keywords of make_tile_ptrs."""
+    """Fill a Tile from numpy (host) arrays: either the axes xs / ys of a
+    rectangle or an explicit complex128 list of pixel positions ``pix``."""
     t = Tile()
-    t.nx, t.ny = len(xs), len(ys)
-    t.xs, t.ys = _p(xs), _p(ys)
+    if pix is not None:
+        t.nx, t.ny = int(pix.size), 1
+        t.pix = _p(pix)
+    else:
+        t.nx, t.ny = len(xs), len(ys)
+        t.xs, t.ys = _p(xs), _p(ys)
     lm = np.asarray(lin_mat, dtype=np.float64).ravel()
     for k in range(4):
         t.lin_mat[k] = lm[k]
@@ -280,7 +284,7 @@ def make_tile(*, xs, ys, lin_mat, Z, stop_reason, stop_iter, U=None, ref=None,
     t.stop_reason, t.stop_iter = _p(stop_reason), _p(stop_iter)
     t.potential, t.dem = _p(potential), _p(dem)
     if keep is not None:
-        keep.extend([xs, ys, Z, U, stop_reason, stop_iter, potential, dem])
+        keep.extend([xs, ys, pix, Z, U, stop_reason, stop_iter, potential, dem])
     return t
 
 

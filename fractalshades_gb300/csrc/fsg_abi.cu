@@ -113,7 +113,7 @@ size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *calc) {
     if (t.nx <= 0 || t.ny <= 0) return set_err(ctx, FSG_ERR_ARG, "tile with nx <= 0 or ny <= 0");
-    if (!t.xs || !t.ys || !t.Z || !t.stop_reason || !t.stop_iter)
+    if ((!t.pix && (!t.xs || !t.ys)) || !t.Z || !t.stop_reason || !t.stop_iter)
         return set_err(ctx, FSG_ERR_ARG, "tile with a NULL input or output pointer");
     if (perturb && !t.ref) return set_err(ctx, FSG_ERR_ARG, "perturbation tile without reference");
     if (perturb && t.ref->flavor != calc->flavor)
@@ -167,6 +167,7 @@ TileDev make_tile(const fsg_tile &t) {
     memset(&d, 0, sizeof(d));
     d.ref = t.ref ? t.ref->dev : nullptr;
     d.xs = t.xs; d.ys = t.ys; d.nx = t.nx; d.ny = t.ny;
+    d.pix = (const double2 *)t.pix;
     for (int k = 0; k < 4; k++) d.lin[k] = t.lin_mat[k];
     d.cre = t.center_re; d.cim = t.center_im; d.dx = t.dx;
     d.dx_m = t.dx_m; d.dx_e = t.dx_e;
@@ -253,7 +254,8 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     for (int32_t i = 0; i < ntiles; i++) {
         const fsg_tile &t = tiles[i];
         size_t np = (size_t)t.nx * t.ny;
-        bytes += align_up(8 * t.nx) + align_up(8 * t.ny) + align_up(zsz * t.nZ * np)
+        bytes += (t.pix ? align_up(16 * np) : align_up(8 * t.nx) + align_up(8 * t.ny))
+                 + align_up(zsz * t.nZ * np)
                  + align_up(4 * np) + align_up(np) + align_up(4 * np);
         if (t.potential) bytes += align_up(8 * np);
         if (t.dem) bytes += align_up(8 * np);
@@ -265,11 +267,17 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     for (int32_t i = 0; i < ntiles; i++) {
         fsg_tile t = tiles[i];
         size_t np = (size_t)t.nx * t.ny;
-        double *xs = (double *)p; p += align_up(8 * t.nx);
-        double *ys = (double *)p; p += align_up(8 * t.ny);
-        CK(cudaMemcpyAsync(xs, t.xs, 8 * t.nx, cudaMemcpyHostToDevice, s), "copy xs");
-        CK(cudaMemcpyAsync(ys, t.ys, 8 * t.ny, cudaMemcpyHostToDevice, s), "copy ys");
-        t.xs = xs; t.ys = ys;
+        if (t.pix) {
+            double *pp = (double *)p; p += align_up(16 * np);
+            CK(cudaMemcpyAsync(pp, t.pix, 16 * np, cudaMemcpyHostToDevice, s), "copy pix");
+            t.pix = pp; t.xs = nullptr; t.ys = nullptr;
+        } else {
+            double *xs = (double *)p; p += align_up(8 * t.nx);
+            double *ys = (double *)p; p += align_up(8 * t.ny);
+            CK(cudaMemcpyAsync(xs, t.xs, 8 * t.nx, cudaMemcpyHostToDevice, s), "copy xs");
+            CK(cudaMemcpyAsync(ys, t.ys, 8 * t.ny, cudaMemcpyHostToDevice, s), "copy ys");
+            t.xs = xs; t.ys = ys;
+        }
         t.Z = p; p += align_up(zsz * t.nZ * np);
         // fields the kernel does not produce come back as zeros, like the
         // caller's freshly allocated arrays (core.py:2070-2073)

@@ -42,6 +42,7 @@ struct RefDev {
 struct TileDev {
     const RefDev *ref;
     const double *xs, *ys;
+    const double2 *pix;                        // optional explicit positions
     int nx, ny;
     double lin[4];
     double cre, cim, dx;                       // standard loop
@@ -121,6 +122,13 @@ __device__ __forceinline__ void fsg_epilogue(const TileDev &T, const CalcDev &C,
         T.pot[ip] = ((double)n - q) - (x - q);
     }
     if (T.dem) T.dem[ip] = az * log(az) / absd;
+}
+
+// Screen position of pixel ip of a tile
+__device__ __forceinline__ double2 fsg_pixel(const TileDev &T, long long ip) {
+    if (T.pix) return __ldg(&T.pix[ip]);
+    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
+    return make_double2(__ldg(&T.xs[ix]), __ldg(&T.ys[iy]));
 }
 
 // Kernel launchers (one per translation unit)

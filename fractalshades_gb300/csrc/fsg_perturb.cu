@@ -47,8 +47,8 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
     const int dzndz_on = C.interior, dzndc_on = C.calc_dzndc;
     const int order = R.order, div_iter = R.div_iter, w_wrapped = R.len;
     // perturbation.py:2214-2230 ref_path_c_from_pix, 2666-2672 lin_proj_impl
-    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
-    double px = __ldg(&T.xs[ix]), py = __ldg(&T.ys[iy]);
+    double2 pp = fsg_pixel(T, ip);
+    double px = pp.x, py = pp.y;
     double x1 = T.lin[0] * px + T.lin[1] * py;
     double y1 = T.lin[2] * px + T.lin[3] * py;
     xf dxr; dxr.m = T.dx_m; dxr.e = T.dx_e;
@@ -337,8 +337,8 @@ __device__ __forceinline__ void pixel_bs(const TileDev &T, const CalcDev &C, lon
     const int flavor = C.flavor, hess = C.calc_dzndc;
     const int order = R.order, div_iter = R.div_iter;
     // perturbation.py:2260-2280 ref_path_c_from_pix_BS through Xrange values
-    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
-    double px = __ldg(&T.xs[ix]), py = __ldg(&T.ys[iy]);
+    double2 pp = fsg_pixel(T, ip);
+    double px = pp.x, py = pp.y;
     double x1 = T.lin[0] * px + T.lin[1] * py;
     double y1 = T.lin[2] * px + T.lin[3] * py;
     xf dxr; dxr.m = T.dx_m; dxr.e = T.dx_e;

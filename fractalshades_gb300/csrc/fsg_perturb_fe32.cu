@@ -63,8 +63,8 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     const int order = R.order, div_iter = R.div_iter, w_wrapped = R.len;
     const float M2f = (float)C.M2;
     // c from the pixel (perturbation.py:2214-2230), kept in fe form
-    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
-    double px = __ldg(&T.xs[ix]), py = __ldg(&T.ys[iy]);
+    double2 pp = fsg_pixel(T, ip);
+    double px = pp.x, py = pp.y;
     double x1 = T.lin[0] * px + T.lin[1] * py;
     double y1 = T.lin[2] * px + T.lin[3] * py;
     xf dxr; dxr.m = T.dx_m; dxr.e = T.dx_e;

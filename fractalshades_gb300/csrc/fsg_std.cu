@@ -11,8 +11,8 @@ __device__ __forceinline__ double sgn(double x) { return x < 0. ? -1. : 1.; }
 
 // core.py:3161-3194 c_from_pix, Cartesian projection
 __device__ __forceinline__ double2 std_c(const TileDev &T, long long ip) {
-    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
-    double px = T.xs[ix], py = T.ys[iy];
+    double2 pp = fsg_pixel(T, ip);
+    double px = pp.x, py = pp.y;
     double x1 = T.lin[0] * px + T.lin[1] * py;
     double y1 = T.lin[2] * px + T.lin[3] * py;
     return cadd(cx(T.cre, T.cim), rmul(T.dx, cx(x1, y1)));

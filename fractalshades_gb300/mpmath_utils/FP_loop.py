@@ -1,0 +1,290 @@
+"""
+Arbitrary-precision host kernels: reference orbit, ball-method period search,
+Newton nucleus search and nucleus size estimate.
+
+Same entry points, arguments and results as the reference's Cython module
+``mpmath_utils/FP_loop.pyx`` (which links MPFR/MPC through gmpy2).  Here the
+arithmetic is binary fixed point on Python integers: a value v is held as the
+integer round(v * 2**F) with F = seed_prec + 64 guard bits, so every operation
+carries an absolute error below 2**-F, which is the accuracy that matters for
+a quadratic iteration started from 0.  Results are returned as mpmath numbers
+or float64 / Xrange arrays exactly like the reference.
+
+The orbit stays on the host and is uploaded once per reference to the GPU.
+"""
+import math
+
+import mpmath
+import numpy as np
+
+from ..numpy_utils.xrange import xr_from_mantissa_exp
+
+# settings.py:14 newton_zoom_level and :22 xrange_zoom_level (FP_loop.pyx:142-143)
+PARTIAL_TSHOLD = 1.e-5
+XR_TSHOLD = 1.e-300
+
+GUARD_BITS = 64
+
+
+# ---------------------------------------------------------------------------
+# fixed point helpers
+# ---------------------------------------------------------------------------
+def _fix(v, F):
+    """round(v * 2**F) for an mpmath number or a decimal string (parsed with
+    F + 16 bits, like mpfr_set_str at the working precision)."""
+    with mpmath.workprec(F + 16):
+        v = mpmath.mpf(v)
+    sign, man, exp, _bc = v._mpf_
+    if sign:
+        man = -man
+    s = exp + F
+    if s >= 0:
+        return man << s
+    # round to nearest
+    return (man + (1 << (-s - 1))) >> (-s)
+
+
+def _to_float(x, F):
+    """float(x * 2**-F), correctly rounded for normal results."""
+    if x == 0:
+        return 0.0
+    b = abs(x).bit_length()
+    if b <= 1000:
+        return math.ldexp(float(x), -F)
+    sh = b - 64
+    return math.ldexp(float(x >> sh), sh - F)
+
+
+def _to_mpf(x, F):
+    return mpmath.mpf((x, -F)) if x else mpmath.mpf(0)
+
+
+def _mantissa_exp(x, F):
+    """(m, e) with x * 2**-F = m * 2**e, m in [0.5, 1) (mpfr_get_d_2exp)."""
+    if x == 0:
+        return 0.0, 0
+    b = abs(x).bit_length()
+    sh = b - 64
+    m = float(x >> sh) if sh > 0 else float(x << -sh)
+    m = math.ldexp(m, -64)          # in [0.5, 1)
+    return m, b - F
+
+
+def _xr_of(zx, zy, F):
+    """Xrange (complex mantissa, shared exponent) of z, as mpc_t_to_Xrange
+    (FP_loop.pyx:424-440) does through Xrange addition."""
+    mx, ex = _mantissa_exp(zx, F)
+    my, ey = _mantissa_exp(zy, F)
+    return xr_from_mantissa_exp(mx, ex, my, ey)
+
+
+def _sq_add(zx, zy, cx, cy, F):
+    """z**2 + c"""
+    return (((zx * zx - zy * zy) >> F) + cx, ((zx * zy) >> (F - 1)) + cy)
+
+
+# ---------------------------------------------------------------------------
+# reference orbit (FP_loop.pyx:274-421)
+# ---------------------------------------------------------------------------
+def perturbation_mandelbrot_FP_loop(orbit, need_Xrange, max_iter, M, seed_x, seed_y,
+                                    seed_prec):
+    """Fill ``orbit`` (complex128 of length max_iter + 1, or its float64 view)
+    with the FP64 values of z_n, z_0 = 0, z_{n+1} = z_n**2 + c.
+
+    Returns (i, partial_dict, xr_dict): the exit index (first invalid
+    iteration), the successive minima of |z_n| below PARTIAL_TSHOLD and the
+    iterations with |z_n| < XR_TSHOLD as Xrange (only if need_Xrange)."""
+    orb = orbit.view(np.complex128) if orbit.dtype != np.complex128 else orbit
+    if orb.shape[0] != max_iter + 1:
+        raise ValueError("orbit length must be max_iter + 1")
+    F = int(seed_prec) + GUARD_BITS
+    cx, cy = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    zx, zy = 0, 0
+    orb[0] = 0.
+    xr_dict = {}
+    partial_dict = {}
+    curr_partial = PARTIAL_TSHOLD
+    curr_partial2 = None
+    i = 0
+    abs_i = 0.
+    for i in range(1, max_iter + 1):
+        zx, zy = _sq_add(zx, zy, cx, cy, F)
+        x, y = _to_float(zx, F), _to_float(zy, F)
+        orb[i] = complex(x, y)
+        abs_i = math.hypot(x, y)
+        if abs_i > M:
+            break
+        if need_Xrange and abs_i < XR_TSHOLD:
+            xr_dict[i] = _xr_of(zx, zy, F)
+        if abs_i <= curr_partial:
+            a2 = zx * zx + zy * zy
+            if curr_partial2 is None or a2 < curr_partial2:
+                partial_dict[i] = _xr_of(zx, zy, F)
+                curr_partial2 = a2
+                curr_partial = abs_i
+    if i == max_iter and abs_i <= M:
+        i += 1
+    return i, partial_dict, xr_dict
+
+
+# ---------------------------------------------------------------------------
+# ball method (FP_loop.pyx:631-760)
+# ---------------------------------------------------------------------------
+def perturbation_mandelbrot_ball_method(seed_x, seed_y, seed_prec, seed_px, maxiter,
+                                        M_divergence):
+    """First i such that |z_i / (dz_i/dc)| < px (a ball of radius px around c
+    maps onto a ball containing 0).  Returns -1 if none up to maxiter."""
+    F = int(seed_prec) + GUARD_BITS
+    cx, cy = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    px = _fix(_dec(seed_px), F)
+    px2 = px * px
+    one = 1 << F
+    zx = zy = 0
+    dx = dy = 0
+    for i in range(1, maxiter + 1):
+        # dzndc <- 2 z dzndc + 1 (iter_deriv_M2 with var_c_z = 0), then z <- z^2 + c
+        dx, dy = ((zx * dx - zy * dy) >> (F - 1)) + one, ((zx * dy + zy * dx) >> (F - 1))
+        zx, zy = _sq_add(zx, zy, cx, cy, F)
+        if math.hypot(_to_float(zx, F), _to_float(zy, F)) > M_divergence:
+            return -1
+        # |z / dzndc| / px < 1  <=>  |z|^2 < px^2 |dzndc|^2
+        z2 = zx * zx + zy * zy
+        d2 = dx * dx + dy * dy
+        if (z2 << (2 * F)) < px2 * d2:
+            return i
+    return -1
+
+
+# ---------------------------------------------------------------------------
+# Newton nucleus search (FP_loop.pyx:900-1116, 1119-1340)
+# ---------------------------------------------------------------------------
+def _cdiv(ax, ay, bx, by, F):
+    """(a / b) in fixed point"""
+    den = bx * bx + by * by
+    if den == 0:
+        raise ZeroDivisionError
+    nx = ax * bx + ay * by
+    ny = ay * bx - ax * by
+    return (nx << F) // den, (ny << F) // den
+
+
+def _cmul(ax, ay, bx, by, F):
+    return (ax * bx - ay * by) >> F, (ax * by + ay * bx) >> F
+
+
+def _find_nucleus(seed_x, seed_y, seed_prec, order, max_newton, seed_eps_cv,
+                  seed_eps_valid, divide_divisors):
+    F = int(seed_prec) + GUARD_BITS
+    cx, cy = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    eps_cv = mpmath.mpf(_dec(seed_eps_cv)) * 64
+    eps_valid = mpmath.mpf(_dec(seed_eps_valid))
+    one = 1 << F
+    order = int(order)
+    newton_cv = False
+    for _ in range(int(max_newton)):
+        zx = zy = 0
+        dx = dy = 0
+        hx, hy = one, 0
+        dhx = dhy = 0
+        for i in range(1, order + 1):
+            dx, dy = ((zx * dx - zy * dy) >> (F - 1)) + one, (zx * dy + zy * dx) >> (F - 1)
+            zx, zy = _sq_add(zx, zy, cx, cy, F)
+            if divide_divisors and i < order and order % i == 0:
+                hx, hy = _cmul(hx, hy, zx, zy, F)
+                qx, qy = _cdiv(dx, dy, zx, zy, F)
+                dhx, dhy = dhx + qx, dhy + qy
+        # f = zr / h ; df = (dzrdc - zr * dh) / h ; step = f / df
+        fx, fy = _cdiv(zx, zy, hx, hy, F)
+        tx, ty = _cmul(zx, zy, dhx, dhy, F)
+        gx, gy = _cdiv(dx - tx, dy - ty, hx, hy, F)
+        sx, sy = _cdiv(fx, fy, gx, gy, F)
+        cx, cy = cx - sx, cy - sy
+        step = mpmath.sqrt(_to_mpf(sx, F) ** 2 + _to_mpf(sy, F) ** 2)
+        if step <= eps_cv:
+            az = mpmath.sqrt(_to_mpf(zx, F) ** 2 + _to_mpf(zy, F) ** 2)
+            newton_cv = az <= eps_valid
+            break
+    if newton_cv:
+        return True, mpmath.mpc(_to_mpf(cx, F), _to_mpf(cy, F))
+    return False, mpmath.mpc("nan", "nan")
+
+
+def perturbation_mandelbrot_find_nucleus(seed_x, seed_y, seed_prec, order, max_newton,
+                                         seed_eps_cv, seed_eps_valid):
+    """Newton for f^order(0) = 0 with division by the roots of the divisor
+    periods (FP_loop.pyx:900-1116).  Returns (newton_cv, c)."""
+    return _find_nucleus(seed_x, seed_y, seed_prec, order, max_newton, seed_eps_cv,
+                         seed_eps_valid, True)
+
+
+def perturbation_mandelbrot_find_any_nucleus(seed_x, seed_y, seed_prec, order, max_newton,
+                                             seed_eps_cv, seed_eps_valid):
+    """Newton for f^order(0) = 0 accepting divisor periods (FP_loop.pyx:1119-1340)."""
+    return _find_nucleus(seed_x, seed_y, seed_prec, order, max_newton, seed_eps_cv,
+                         seed_eps_valid, False)
+
+
+# ---------------------------------------------------------------------------
+# nucleus size estimate (FP_loop.pyx:487-604)
+# ---------------------------------------------------------------------------
+def perturbation_mandelbrot_nucleus_size_estimate(seed_x, seed_y, seed_prec, order):
+    """Size estimate of the hyperbolic component of period ``order`` at c
+    (the renormalisation estimate 1 / (beta * lambda**2) of the reference,
+    with lambda = dz_p/dz and beta = sum_i 1 / prod_{j<=i} dz_j/dz)."""
+    with mpmath.workprec(int(seed_prec)):
+        c = mpmath.mpc(_dec(seed_x), _dec(seed_y))
+        z = mpmath.mpc(0)
+        l = mpmath.mpc(1)
+        b = mpmath.mpc(1)
+        for _ in range(1, int(order)):
+            z = z * z + c
+            l = 2 * z * l
+            b = b + 1 / l
+        size = 1 / (b * l * l)
+        return size
+
+
+def _dec(s):
+    if isinstance(s, (bytes, bytearray)):
+        return s.decode("utf8")
+    return s
+
+
+# ---------------------------------------------------------------------------
+# Burning Ship family orbit (FP_loop.pyx:1828-1979)
+# ---------------------------------------------------------------------------
+def perturbation_nonholomorphic_FP_loop(orbit, need_Xrange, max_iter, M, seed_x, seed_y,
+                                        seed_prec, kind=1):
+    """BS-family orbit (x_{n+1}, y_{n+1}) = f_kind(x_n, y_n) + (a, -b).
+    Returns (i, partial_dict, xr_dict) with the Xrange register holding
+    iterations where |x| or |y| < XR_TSHOLD (only if need_Xrange)."""
+    orb = orbit.view(np.complex128) if orbit.dtype != np.complex128 else orbit
+    F = int(seed_prec) + GUARD_BITS
+    a, b = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    x = y = 0
+    orb[0] = 0.
+    xr_dict = {}
+    i = 0
+    abs_i = 0.
+    for i in range(1, max_iter + 1):
+        x2, y2, xy = (x * x) >> F, (y * y) >> F, (x * y) >> F
+        if kind == 1:
+            x, y = x2 - y2 + a, 2 * abs(xy) - b
+        elif kind == 2:
+            x, y = x2 - y2 + a, 2 * ((x * abs(y)) >> F) - b
+        elif kind == 3:
+            x, y = x2 - ((y * abs(y)) >> F) + a, 2 * xy - b
+        elif kind == 4:
+            x, y = abs(x2 - y2) + a, 2 * xy - b
+        else:
+            x, y = abs(x2 - y2) + a, 2 * abs(xy) - b
+        fx, fy = _to_float(x, F), _to_float(y, F)
+        orb[i] = complex(fx, fy)
+        abs_i = math.hypot(fx, fy)
+        if abs_i > M:
+            break
+        if need_Xrange and (abs(fx) < XR_TSHOLD or abs(fy) < XR_TSHOLD):
+            xr_dict[i] = (_mantissa_exp(x, F), _mantissa_exp(y, F))
+    if i == max_iter and abs_i <= M:
+        i += 1
+    return i, {}, xr_dict

@@ -99,6 +99,10 @@ typedef struct {
     const double *xs;         /* [nx] screen fraction per column                 */
     const double *ys;         /* [ny] screen fraction per row (already negated and
                                  divided by xy_ratio, core.py:1820-1830)          */
+    const double *pix;        /* optional complex128 [nx * ny] explicit pixel
+                                 positions (the reference's c_pix, e.g. a subset
+                                 or a jittered grid); when set, xs / ys are
+                                 ignored and may be NULL                          */
     double lin_mat[4];        /* rotation / skew (core.py:1470-1484), row-major   */
     /* standard loop: c = center + dx * lin_mat . pix */
     double center_re, center_im, dx;

@@ -163,21 +163,43 @@ def _run_m2(ctx, d, ref, mode, xr_sem):
 M2_CASES = ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr", "pert_m2_xr_div"]
 
 
+def _xr_rel(m, e, eref):
+    return m * np.exp2((np.asarray(e, dtype=np.int64) - eref).astype(float))
+
+
 @pytest.mark.parametrize("case", M2_CASES)
 def test_ref_tables_vs_oracle(ctx, case):
+    """BLA tree and derivative paths built on the GPU against the oracle's
+    (same operation order; CUDA's hypot may differ from the C library's by an
+    ulp in the BLA radii)."""
     d = load(case)
     xr = bool(d["xr_mode"])
     ref = _ref_from_golden(ctx, d, xr)
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    Mo, ro, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]))
     M, r = ref.download("bla")
-    np.testing.assert_allclose(r, d["r_bla"], rtol=1e-14, atol=0)
-    np.testing.assert_allclose(M, d["M_bla"], rtol=1e-14, atol=0)
+    assert ref.stages == st
+    np.testing.assert_allclose(r, ro, rtol=1e-14, atol=0)
+    np.testing.assert_allclose(M, Mo, rtol=1e-14, atol=0)
+    dzo = orc.dzndc_path_m2(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), xr,
+                            float(d["dx_m"]), int(d["dx_e"]), d["xr_idx"], d["xr_m"], d["xr_e"])
     dz = ref.download("dzndc")
     if xr:
-        got = dz[0] * np.exp2(dz[1].astype(float) + 900.)
-        exp = d["dZndc_m"] * np.exp2(d["dZndc_e"].astype(float) + 900.)
-        np.testing.assert_allclose(got, exp, rtol=1e-15)
+        eref = int(dzo[1].max())
+        np.testing.assert_allclose(_xr_rel(dz[0], dz[1], eref),
+                                   _xr_rel(dzo[0], dzo[1], eref), rtol=1e-15, atol=0)
     else:
-        assert np.array_equal(dz.view(np.uint64), d["dZndc"].view(np.uint64))
+        assert np.array_equal(dz.view(np.uint64), dzo.view(np.uint64))
+    if bool(d["interior"]):
+        dzzo = orc.dzndz_path_m2(d["Zn"], int(d["ref_div_iter"]), xr, d["xr_idx"],
+                                 d["xr_m"], d["xr_e"])
+        dzz = ref.download("dzndz")
+        if xr:
+            eref = int(dzzo[1].max())
+            np.testing.assert_allclose(_xr_rel(dzz[0], dzz[1], eref),
+                                       _xr_rel(dzzo[0], dzzo[1], eref), rtol=1e-15, atol=0)
+        else:
+            assert np.array_equal(dzz.view(np.uint64), dzzo.view(np.uint64))
 
 
 @pytest.mark.parametrize("case", M2_CASES)
