@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""
+Headline benchmark: pixel-iterations per second of the power-2 Mandelbrot
+perturbation loop at dx = 1e-300, FP32-mantissa + int32-exponent deltas
+versus the FP64 path, with the p50 / p99 latency of a stream of tiles.
+
+Workload (seeded, synthetic): 2048 x 2048 pixels, width 1e-300, centred on
+the nucleus of a period-p component (p ~ U[300, 3000], seed 2) found by
+Newton at 400 digits; reference orbit at 400 digits, max_iter 200000, escape
+radius 1e3, BLA eps 1e-6, outputs iteration count, smoothed potential and the
+dzndc distance estimate.  One step = one launch over the whole image.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+Prints one JSON line.  With torchrun (N > 1) every rank renders its own
+replica of the image (the pixels are independent) and rank 0 prints.
+"""
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pixel-iter/s at 1e-300 zoom, FP32+exp vs FP64 path; p50/p99 tile latency"
+FLOPS_FULL = 35      # M2 perturbation step with dzndc (zn 17 + dzndc 18)
+FLOPS_BLA = 23       # M2 BLA step with dzndc (17 + 6)
+LIN = np.array([[1., -0.], [0., 1.]])
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nx", type=int, default=2048)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0., set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle (C restatement of the reference's loop) on host cores
+# ---------------------------------------------------------------------------
+def cpu_sample(w, target_s=10.0, threads=None):
+    """Time the oracle's Xrange-branch loop (the reference's branch at
+    dx = 1e-300) on a seeded random sample of pixels, on all host cores."""
+    from oracle import oracle as orc
+    threads = threads or os.cpu_count() or 1
+    Mb, rb, _, st = orc.make_bla_m2(w.Zn, w.kc, 1e-6)
+    dz = orc.dzndc_path_m2(w.Zn, w.div_iter, w.order, w.xr_mode, w.dx_m, w.dx_e,
+                           w.xr_idx, w.xr_m, w.xr_e)
+    kw = dict(Zn=w.Zn, ref_div_iter=w.div_iter, ref_order=w.order, lin_mat=LIN,
+              dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e,
+              max_iter=w.max_iter, M=w.M, eps_stat=0., xr_mode=w.xr_mode,
+              bla=(Mb, rb, st), dZndc=dz, xr_idx=w.xr_idx, xr_m=w.xr_m, xr_e=w.xr_e)
+    rng = np.random.default_rng(7)
+
+    def chunk(n):
+        ix = rng.integers(0, w.nx, n)
+        iy = rng.integers(0, w.ny, n)
+        return w.xs[ix] + 1j * w.ys[iy]
+
+    # calibrate on a small chunk, then size the sample to ~target_s
+    t0 = time.perf_counter()
+    _, _, _, si = orc.perturb_m2(chunk(64), **kw)
+    dt = max(time.perf_counter() - t0, 1e-4)
+    per_px = dt / 64
+    n_total = int(max(threads * 64, min(2_000_000, target_s * threads / per_px)))
+    per = max(1, n_total // threads)
+    chunks = [chunk(per) for _ in range(threads)]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(lambda p: orc.perturb_m2(p, **kw)[3], chunks))
+    dt = time.perf_counter() - t0
+    iters = float(sum(r.sum() for r in res))
+    return {"value": iters / dt, "unit": "pixel-iter/s", "cores": threads, "kind": "port",
+            "sample": f"{per * threads} random pixels of the 2048x2048 image "
+                      f"({iters:.3e} pixel-iterations, {dt:.2f} s), Xrange branch, BLA on"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU loop (oracle port; the reference
+    itself needs numba, absent here) on every host core."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from fractalshades_gb300 import synthetic as syn
+    w = syn.config2_workload(nx=args.nx)
+    vals = []
+    for s in range(args.warmup + args.steps):
+        r = cpu_sample(w, target_s=4.0)
+        if s >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pixel-iter/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+i32exp", "data": "synthetic",
+            "config": config_dict(w, args),
+            "cpu_baseline": {"value": v, "unit": "pixel-iter/s", "cores": r["cores"],
+                             "kind": "port", "sample": r["sample"]},
+            "e2e": {"value": v, "unit": "pixel-iter/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_dict(w, args):
+    return {"workload": "perturbation Mandelbrot 2048x2048 at dx=1e-300 on a period-p nucleus",
+            "nx": w.nx, "ny": w.ny, "dx": "1e-300", "period": w.p, "digits": w.dps,
+            "max_iter": w.max_iter, "M_divergence": w.M, "BLA_eps": 1e-6,
+            "outputs": ["stop_iter", "stop_reason", "zn", "dzndc", "potential", "DEM"],
+            "seed": 2, "l2": "flushed between timed steps (256 MB write)"}
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import synthetic as syn
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    w = syn.config2_workload(nx=args.nx)
+    n = w.nx * w.ny
+    ctx = nat.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    peak32 = ctx.peak_tflops(False)
+    peak64 = ctx.peak_tflops(True)
+
+    refs = {}
+    refs["xr"] = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order,
+                               xr_idx=w.xr_idx, xr_m=w.xr_m, xr_e=w.xr_e, xr_paths=True,
+                               calc_dzndc=True, scale_m=w.dx_m, scale_e=w.dx_e, bla=True,
+                               kc=w.kc, bla_eps=1e-6)
+    refs["std"] = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order,
+                                xr_idx=w.xr_idx, xr_m=w.xr_m, xr_e=w.xr_e, xr_paths=False,
+                                calc_dzndc=True, scale_m=w.dx_m, scale_e=w.dx_e, bla=True,
+                                kc=w.kc, bla_eps=1e-6)
+
+    f64 = dict(dtype=torch.float64, device=dev)
+    xs = torch.from_numpy(w.xs).to(dev)
+    ys = torch.from_numpy(w.ys).to(dev)
+    Z = torch.zeros((2, n, 2), **f64)          # complex128 [zn, dzndc]
+    U = torch.zeros(n, dtype=torch.int32, device=dev)
+    sr = torch.zeros(n, dtype=torch.int8, device=dev)
+    si = torch.zeros(n, dtype=torch.int32, device=dev)
+    pot = torch.zeros(n, **f64)
+    dem = torch.zeros(n, **f64)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def tile(ref):
+        return nat.make_tile_ptrs(
+            nx=w.nx, ny=w.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(), lin_mat=LIN,
+            Z_ptr=Z.data_ptr(), nZ=2, stop_reason_ptr=sr.data_ptr(),
+            stop_iter_ptr=si.data_ptr(), U_ptr=U.data_ptr(), ref=ref, dx_m=w.dx_m,
+            dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e, i_dzndc=1,
+            potential_ptr=pot.data_ptr(), dem_ptr=dem.data_ptr())
+
+    def calc(mode):
+        return nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=mode,
+                             calc_dzndc=True, interior=False, bla=True,
+                             xr_semantics=w.xr_mode)
+
+    def timed_steps(mode, ref, k, warm):
+        t, c = tile(ref), calc(mode)
+        for _ in range(warm):
+            ctx.perturb_tiles(c, [t], nat.DEVICE)
+        torch.cuda.synchronize(dev)
+        step_ms, kern_ms, stats = [], [], []
+        if dist:
+            dist.barrier()
+        for _ in range(k):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.perturb_tiles(c, [t], nat.DEVICE)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            st = ctx.stats()
+            kern_ms.append(st["kernel_ms"])
+            stats.append(st)
+        torch.cuda.synchronize(dev)
+        return step_ms, kern_ms, stats
+
+    def snapshot():
+        return (si.cpu().numpy().copy(), sr.cpu().numpy().copy(),
+                pot.cpu().numpy().copy(), dem.cpu().numpy().copy())
+
+    # headline: FP32 + exponent
+    with ClockSampler(local) as clk:
+        step_ms, kern_ms, stats = timed_steps("fe32", refs["xr"], args.steps, args.warmup)
+    fe_out = snapshot()
+    pix_iters = stats[-1]["pixel_iters"]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([total_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_s = float(tt.item())
+    value = pix_iters * args.steps * world / total_s
+    st = stats[-1]
+    flops = st["full_steps"] * FLOPS_FULL + st["bla_steps"] * FLOPS_BLA
+    kms = float(np.mean(kern_ms))
+    achieved = flops / (kms * 1e-3) / 1e12
+
+    # the two FP64 forms of the reference (one or two steps each: slower)
+    k64 = max(1, min(2, args.steps))
+    xr_step, xr_kern, xr_stats = timed_steps("xr64", refs["xr"], k64, 1)
+    xr_out = snapshot()
+    fp_step, fp_kern, fp_stats = timed_steps("fp64", refs["std"], k64, 1)
+    value_xr = xr_stats[-1]["pixel_iters"] / (np.mean(xr_step) / 1e3)
+    value_fp = fp_stats[-1]["pixel_iters"] / (np.mean(fp_step) / 1e3)
+    fl64 = xr_stats[-1]["full_steps"] * FLOPS_FULL + xr_stats[-1]["bla_steps"] * FLOPS_BLA
+    achieved64 = fl64 / (np.mean(xr_kern) * 1e-3) / 1e12
+
+    # accuracy of the FP32 form against the FP64 (Xrange) form, per output
+    def relerr(a, b):
+        m = np.isfinite(a) & np.isfinite(b) & (b != 0)
+        return float(np.max(np.abs(a[m] - b[m]) / np.abs(b[m]))) if m.any() else 0.0
+    accuracy = {
+        "pixels": int(n),
+        "iter_count_differs_frac": float(np.mean(fe_out[0] != xr_out[0])),
+        "iter_count_max_abs_diff": int(np.max(np.abs(fe_out[0].astype(np.int64) - xr_out[0]))),
+        "stop_reason_differs_frac": float(np.mean(fe_out[1] != xr_out[1])),
+        "potential_max_rel_err": relerr(fe_out[2], xr_out[2]),
+        "dem_max_rel_err": relerr(fe_out[3], xr_out[3]),
+    }
+
+    # end to end through the C-ABI with host buffers (pinned), FP32 form
+    h = {}
+    h["Z"] = torch.zeros((2, n, 2), dtype=torch.float64, pin_memory=True).numpy()
+    h["U"] = torch.zeros(n, dtype=torch.int32, pin_memory=True).numpy()
+    h["sr"] = torch.zeros(n, dtype=torch.int8, pin_memory=True).numpy()
+    h["si"] = torch.zeros(n, dtype=torch.int32, pin_memory=True).numpy()
+    h["pot"] = torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
+    h["dem"] = torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
+    hxs = torch.from_numpy(w.xs).pin_memory().numpy()
+    hys = torch.from_numpy(w.ys).pin_memory().numpy()
+    Zc = h["Z"].view(np.complex128).reshape(2, n)
+    ht = nat.make_tile(xs=hxs, ys=hys, lin_mat=LIN, Z=Zc, U=h["U"], stop_reason=h["sr"],
+                       stop_iter=h["si"], ref=refs["xr"], dx_m=w.dx_m, dx_e=w.dx_e,
+                       drift_m=w.drift_m, drift_e=w.drift_e, i_dzndc=1,
+                       potential=h["pot"], dem=h["dem"])
+    hc = calc("fe32")
+    ctx.perturb_tiles(hc, [ht], nat.HOST)
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        ctx.perturb_tiles(hc, [ht], nat.HOST)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_val = int(h["si"].astype(np.int64).sum()) / float(np.mean(e2e_t))
+    d2h = sum(a.nbytes for a in h.values())
+    h2d = hxs.nbytes + hys.nbytes
+
+    # tile latency: a seeded stream of tiles of 256..2048 squared (host buffers)
+    rng = np.random.default_rng(5)
+    lat = []
+    sizes = [256, 512, 1024, 2048]
+    for i in range(24):
+        side = int(rng.choice(sizes))
+        xs_t, ys_t = syn.image_axes(side, side)
+        m = side * side
+        Zt = np.zeros((2, m), dtype=np.complex128)
+        Ut = np.zeros(m, dtype=np.int32)
+        srt = np.zeros(m, dtype=np.int8)
+        sit = np.zeros(m, dtype=np.int32)
+        tt = nat.make_tile(xs=xs_t, ys=ys_t, lin_mat=LIN, Z=Zt, U=Ut, stop_reason=srt,
+                           stop_iter=sit, ref=refs["xr"], dx_m=w.dx_m, dx_e=w.dx_e,
+                           drift_m=w.drift_m, drift_e=w.drift_e, i_dzndc=1)
+        t0 = time.perf_counter()
+        ctx.perturb_tiles(hc, [tt], nat.HOST)
+        lat.append((time.perf_counter() - t0) * 1e3)
+    lat = np.array(lat[2:])
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return 0
+
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu = cpu_sample(w, target_s=10.0)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "pixel-iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32exp",
+        "data": "synthetic", "config": config_dict(w, args),
+        "e2e": {"value": e2e_val, "unit": "pixel-iter/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(args.steps),
+        "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": peak32,
+                     "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,
+                     "traffic": None,
+                     "peak_source": "measured FFMA-chain kernel on this GPU (fsg_peak_flops)",
+                     "flops_per_step": {"full": FLOPS_FULL, "bla": FLOPS_BLA},
+                     "executed_steps": {"full": st["full_steps"], "bla": st["bla_steps"]},
+                     "kernel_ms": kms},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "paths": {
+            "fe32": {"value": value, "kernel_ms": kms},
+            "xr64": {"value": value_xr, "kernel_ms": float(np.mean(xr_kern)),
+                     "fp64_tflops": achieved64, "fp64_peak": peak64},
+            "fp64": {"value": value_fp, "kernel_ms": float(np.mean(fp_kern))},
+            "speedup_fe32_vs_xr64": value / value_xr if value_xr else None,
+            "speedup_fe32_vs_fp64": value / value_fp if value_fp else None,
+        },
+        "accuracy_fe32_vs_xr64": accuracy,
+        "tile_latency_ms": {"p50": float(np.percentile(lat, 50)),
+                            "p99": float(np.percentile(lat, 99)), "tiles": int(lat.size),
+                            "sizes": sizes, "path": "C-ABI host buffers, FP32+exp"},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

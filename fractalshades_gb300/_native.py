@@ -77,7 +77,7 @@ SYMBOLS = [
     "fsg_version", "fsg_ctx_create", "fsg_ctx_destroy", "fsg_last_error",
     "fsg_set_stream", "fsg_sync", "fsg_ref_create", "fsg_ref_destroy",
     "fsg_ref_info", "fsg_ref_download", "fsg_std_tiles", "fsg_perturb_tiles",
-    "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel",
+    "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel", "fsg_peak_flops",
 ]
 
 
@@ -111,6 +111,7 @@ def load():
         L.fsg_std_tiles.argtypes = [P, ct.POINTER(Calc), ct.POINTER(Tile), I32, I32]
         L.fsg_perturb_tiles.argtypes = [P, ct.POINTER(Calc), ct.POINTER(Tile), I32, I32]
         L.fsg_last_stats.argtypes = [P, ct.POINTER(Stats)]
+        L.fsg_peak_flops.argtypes = [P, I32, ct.POINTER(F64)]
         L.fsg_cancel.argtypes = [P]
         L.fsg_clear_cancel.argtypes = [P]
         _lib = L
@@ -162,6 +163,12 @@ class Context:
 
     def clear_cancel(self):
         self.L.fsg_clear_cancel(self.h)
+
+    def peak_tflops(self, fp64=False):
+        """Measured FMA-pipe throughput (TFLOP/s) of this GPU."""
+        v = F64()
+        self.check(self.L.fsg_peak_flops(self.h, int(bool(fp64)), ct.byref(v)), "fsg_peak_flops")
+        return v.value
 
     def stats(self):
         s = Stats()

@@ -28,6 +28,7 @@ SOURCES = {
     "fsg_perturb.cu": ["-fmad=false"],
     "fsg_ref.cu": ["-fmad=false"],
     "fsg_perturb_fe32.cu": [],
+    "fsg_peak.cu": [],
     "fsg_abi.cu": [],
 }
 HEADERS = ["fsg_num.cuh", "fsg_internal.cuh"]

@@ -31,6 +31,8 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
                          int4 *bla_A, int4 *bla_B, cudaStream_t s);
 
+double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
+
 struct fsg_ctx {
     int device = 0;
     int sm_count = 0;
@@ -578,6 +580,31 @@ int fsg_perturb_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
                       int32_t where) {
     if (ctx) cudaSetDevice(ctx->device);
     return run_tiles(ctx, calc, tiles, ntiles, where, true);
+}
+
+int fsg_peak_flops(fsg_ctx *ctx, int32_t fp64, double *tflops) {
+    if (!ctx || !tflops) return FSG_ERR_ARG;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    void *out = nullptr;
+    CK(cudaMalloc(&out, (size_t)ctx->sm_count * 8 * 256 * 8), "cudaMalloc(peak)");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a); cudaEventCreate(&b);
+    double best = 0.;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(a, ctx->stream);
+        double flops = fsg_launch_fma_peak(fp64, ctx->sm_count, out, ctx->stream);
+        cudaEventRecord(b, ctx->stream);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms > 0.f) { double t = flops / (ms * 1e-3) / 1e12; if (t > best) best = t; }
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(a); cudaEventDestroy(b);
+    cudaFree(out);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "peak kernel");
+    *tflops = best;
+    return FSG_OK;
 }
 
 int fsg_last_stats(const fsg_ctx *cctx, fsg_stats *out) {

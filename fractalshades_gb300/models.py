@@ -1,0 +1,342 @@
+"""
+Fractal model classes with the reference's calculation API.
+
+Mandelbrot (models/mandelbrot_M2.py:17-354), Perturbation_mandelbrot
+(:361-877), Burning_ship and Perturbation_burning_ship
+(models/burning_ship.py:126-435, 862-1130).  Each ``calc_std_div`` keeps the
+reference's keyword arguments, codes and defaults; its ``iterate()`` factory
+returns the GPU calculation options instead of a numba closure.
+"""
+import enum
+import typing
+from typing import Optional
+
+import mpmath
+import numpy as np
+
+from . import settings
+from . import utils
+from .core import Fractal
+from .perturbation import PerturbationFractal
+from .gpu import StdSpec, PerturbSpec
+from .mpmath_utils import FP_loop as fsFP
+
+
+def _no_initialize():
+    def impl(*args):
+        return None
+    return impl
+
+
+# ---------------------------------------------------------------------------
+# Mandelbrot, power 2
+# ---------------------------------------------------------------------------
+class Mandelbrot(Fractal):
+
+    def __init__(self, directory: str):
+        """Standard power-2 Mandelbrot set, z_0 = 0, z_{n+1} = z_n^2 + c."""
+        super().__init__(directory)
+        self.potential_kind = "infinity"
+        self.potential_d = 2
+        self.potential_a_d = 1.
+        self.potential_M_cutoff = 1000.
+        self.holomorphic = True
+        self.implements_dzndc = "always"
+        self.implements_interior_detection = "always"
+        self.implements_deepzoom = False
+
+    @utils.calc_options
+    def calc_std_div(self, *,
+                     calc_name: str = "base_calc",
+                     subset=None,
+                     max_iter: int = 10000,
+                     M_divergence: float = 1000.,
+                     epsilon_stationnary: float = 0.01,
+                     calc_d2zndc2: bool = False,
+                     calc_orbit: bool = False,
+                     backshift: int = 0):
+        """Escape-time iterations with dz/dz (interior detection) and dz/dc
+        (mandelbrot_M2.py:61-176).  Exit codes 0 max_iter, 1 divergence,
+        2 stationnary."""
+        if calc_d2zndc2 or calc_orbit:
+            raise NotImplementedError("calc_d2zndc2 / calc_orbit are not computed by the GPU kernels")
+        complex_codes = ["zn", "dzndz", "dzndc"]
+        int_codes = []
+        stop_codes = ["max_iter", "divergence", "stationnary"]
+
+        def set_state():
+            def impl(instance):
+                instance.codes = (complex_codes, int_codes, stop_codes)
+                instance.complex_type = np.complex128
+                instance.potential_M = M_divergence
+                instance.backshift = None
+            return impl
+
+        spec = StdSpec(flavor=0, max_iter=max_iter, M_divergence=M_divergence,
+                       epsilon_stationnary=epsilon_stationnary)
+        return {"set_state": set_state, "initialize": _no_initialize,
+                "iterate": lambda: spec}
+
+
+class Perturbation_mandelbrot(PerturbationFractal):
+
+    def __init__(self, directory: str):
+        """Arbitrary-precision power-2 Mandelbrot set (perturbation, BLA)."""
+        super().__init__(directory)
+        self.potential_kind = "infinity"
+        self.potential_d = 2
+        self.potential_a_d = 1.
+        self.potential_M_cutoff = 1000.
+        self.critical_pt = 0.
+        self.FP_code = "zn"
+        self.holomorphic = True
+        self.implements_dzndc = "user"
+        self.implements_interior_detection = "user"
+        self.implements_deepzoom = True
+
+    def FP_loop(self, NP_orbit, c0):
+        """Full precision orbit, fills NP_orbit in place
+        (mandelbrot_M2.py:408-430)."""
+        max_orbit_iter = NP_orbit.shape[0] - 1
+        return fsFP.perturbation_mandelbrot_FP_loop(
+            NP_orbit.view(dtype=np.float64), self.xr_detect_activated, max_orbit_iter,
+            self.M_divergence * 2, str(c0.real).encode("utf8"),
+            str(c0.imag).encode("utf8"), mpmath.mp.prec)
+
+    @utils.calc_options
+    def calc_std_div(self, *,
+                     calc_name: str,
+                     subset,
+                     max_iter: int,
+                     M_divergence: float,
+                     epsilon_stationnary: float,
+                     BLA_eps: float = 1e-6,
+                     interior_detect: bool = False,
+                     calc_dzndc: bool = True,
+                     calc_orbit: bool = False,
+                     backshift: int = 0):
+        """Perturbation iterations (mandelbrot_M2.py:432-588).  Codes: zn,
+        [dzndz], [dzndc]; int code ref_cycle_iter; exit codes 0 max_iter,
+        1 divergence, 2 stationnary."""
+        if calc_orbit:
+            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        complex_codes = ["zn"]
+        code_int = 0
+        dzndz = dzndc = -1
+        if interior_detect:
+            code_int += 1
+            complex_codes += ["dzndz"]
+            dzndz = code_int
+        if calc_dzndc:
+            code_int += 1
+            complex_codes += ["dzndc"]
+            dzndc = code_int
+        int_codes = ["ref_cycle_iter"]
+        stop_codes = ["max_iter", "divergence", "stationnary"]
+        BLA_activated = (BLA_eps is not None) and (self.dx < settings.newton_zoom_level)
+
+        def set_state():
+            def impl(instance):
+                instance.complex_type = np.complex128
+                instance.potential_M = M_divergence
+                instance.codes = (complex_codes, int_codes, stop_codes)
+                instance.calc_dZndz = interior_detect
+                instance.calc_dZndc = calc_dzndc
+            return impl
+
+        spec = PerturbSpec(flavor=0, max_iter=max_iter, M_divergence=M_divergence,
+                           epsilon_stationnary=epsilon_stationnary, calc_dzndc=calc_dzndc,
+                           interior=interior_detect, bla=BLA_activated,
+                           xr_detect_activated=self.xr_detect_activated,
+                           i_dzndz=dzndz, i_dzndc=dzndc, nZ=len(complex_codes))
+        return {"set_state": set_state, "initialize": _no_initialize,
+                "iterate": lambda: spec}
+
+    # ------------------------------------------------------------------
+    @staticmethod
+    def _ball_method(c, px, maxiter, M_divergence):
+        order = fsFP.perturbation_mandelbrot_ball_method(
+            str(c.real).encode("utf8"), str(c.imag).encode("utf8"), mpmath.mp.prec,
+            str(px).encode("utf8"), maxiter, M_divergence)
+        return None if order == -1 else order
+
+    @staticmethod
+    def find_nucleus(c, order, eps_pixel, max_newton=None, eps_cv=None):
+        if order is None:
+            raise ValueError("order shall be defined for Newton method")
+        seed_prec = mpmath.mp.prec
+        if max_newton is None:
+            max_newton = 80
+        if eps_cv is None:
+            eps_cv = mpmath.mpf(val=(2, -seed_prec))
+        return fsFP.perturbation_mandelbrot_find_nucleus(
+            str(c.real).encode("utf8"), str(c.imag).encode("utf8"), seed_prec, order,
+            max_newton, str(eps_cv).encode("utf8"), str(eps_pixel).encode("utf8"))
+
+    @staticmethod
+    def find_any_nucleus(c, order, eps_pixel, max_newton=None, eps_cv=None):
+        if order is None:
+            raise ValueError("order shall be defined for Newton method")
+        seed_prec = mpmath.mp.prec
+        if max_newton is None:
+            max_newton = 80
+        if eps_cv is None:
+            eps_cv = mpmath.mpf(val=(2, -seed_prec))
+        return fsFP.perturbation_mandelbrot_find_any_nucleus(
+            str(c.real).encode("utf8"), str(c.imag).encode("utf8"), seed_prec, order,
+            max_newton, str(eps_cv).encode("utf8"), str(eps_pixel).encode("utf8"))
+
+    @staticmethod
+    def _nucleus_size_estimate(c0, order):
+        return fsFP.perturbation_mandelbrot_nucleus_size_estimate(
+            str(c0.real).encode("utf8"), str(c0.imag).encode("utf8"), mpmath.mp.prec, order)
+
+
+# ---------------------------------------------------------------------------
+# Burning Ship family
+# ---------------------------------------------------------------------------
+BS_flavor_list = (
+    "Burning ship",
+    "Perpendicular burning ship",
+    "Shark fin",
+    "Celtic",
+    "Buffalo",
+)
+BS_flavor_enum = enum.Enum("BS_flavor_enum", BS_flavor_list, module=__name__)
+
+
+def get_flavor_int(flavor: str):
+    """1-based index of the flavor (burning_ship.py:76-80)."""
+    return getattr(BS_flavor_enum, flavor).value
+
+
+class Burning_ship(Fractal):
+
+    def __init__(self, directory: str,
+                 flavor: typing.Literal[BS_flavor_enum] = "Burning ship"):
+        """Burning Ship and its 'abs variations' (burning_ship.py:126-280):
+        x' = x^2 - y^2 + a, y' = 2|xy| - b and four other flavors."""
+        super().__init__(directory)
+        self.flavor = flavor
+        self.flavor_int = get_flavor_int(flavor)
+        self.potential_kind = "infinity"
+        self.potential_d = 2
+        self.potential_a_d = 1.
+        self.potential_M_cutoff = {"Burning ship": 1000., "Perpendicular burning ship": 1000,
+                                   "Shark fin": 1.e20, "Celtic": 1000., "Buffalo": 1000}[flavor]
+        self.holomorphic = False
+        self.implements_dzndc = "always"
+        self.implements_interior_detection = "no"
+        self.implements_deepzoom = False
+
+    @utils.calc_options
+    def calc_std_div(self, *,
+                     calc_name: str,
+                     subset,
+                     max_iter: int,
+                     M_divergence: float,
+                     calc_orbit: bool = False,
+                     backshift: int = 0):
+        """Escape-time iterations with the Jacobian (burning_ship.py:282-346).
+        Codes xn, yn, dxnda, dxndb, dynda, dyndb (float64)."""
+        if calc_orbit:
+            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        complex_codes = ["xn", "yn", "dxnda", "dxndb", "dynda", "dyndb"]
+        int_codes = []
+        stop_codes = ["max_iter", "divergence", "stationnary"]
+
+        def set_state():
+            def impl(instance):
+                instance.codes = (complex_codes, int_codes, stop_codes)
+                instance.complex_type = np.float64
+                instance.potential_M = M_divergence
+                instance.backshift = None
+            return impl
+
+        spec = StdSpec(flavor=self.flavor_int, max_iter=max_iter, M_divergence=M_divergence)
+        return {"set_state": set_state, "initialize": _no_initialize,
+                "iterate": lambda: spec}
+
+
+class Perturbation_burning_ship(PerturbationFractal):
+
+    def __init__(self, directory: str,
+                 flavor: typing.Literal[BS_flavor_enum] = "Burning ship"):
+        """Arbitrary-precision Burning Ship family (perturbation with sign
+        folding, 8-coefficient BLA)."""
+        super().__init__(directory)
+        self.flavor = flavor
+        self.flavor_int = get_flavor_int(flavor)
+        self.potential_kind = "infinity"
+        self.potential_d = 2
+        self.potential_a_d = 1.
+        self.potential_M_cutoff = 1000.
+        self.critical_pt = 0.
+        self.FP_code = ["xn", "yn"]
+        self.holomorphic = False
+        self.implements_dzndc = "always"
+        self.implements_interior_detection = "no"
+        self.implements_deepzoom = True
+
+    def FP_loop(self, NP_orbit, c0):
+        max_orbit_iter = NP_orbit.shape[0] - 1
+        if self.xr_detect_activated:
+            raise NotImplementedError(
+                "Burning Ship perturbation below dx = 1e-300 (Xrange deltas) is not "
+                "supported by the GPU kernels")
+        return fsFP.perturbation_nonholomorphic_FP_loop(
+            NP_orbit.view(dtype=np.float64), self.xr_detect_activated, max_orbit_iter,
+            self.M_divergence * 2, str(c0.real).encode("utf8"),
+            str(c0.imag).encode("utf8"), mpmath.mp.prec, kind=self.flavor_int)
+
+    @utils.calc_options
+    def calc_std_div(self, *,
+                     calc_name: str,
+                     subset,
+                     max_iter: int,
+                     M_divergence: float,
+                     BLA_eps: float = 1e-6,
+                     calc_hessian: bool = True,
+                     calc_orbit: bool = False,
+                     backshift: int = 0):
+        """Perturbation iterations (burning_ship.py:971-1130).  Codes xn, yn
+        [, dxnda, dxndb, dynda, dyndb]; int code ref_cycle_iter; exit codes
+        0 max_iter, 1 divergence."""
+        if calc_orbit:
+            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        complex_codes = ["xn", "yn"]
+        if calc_hessian:
+            complex_codes += ["dxnda", "dxndb", "dynda", "dyndb"]
+        int_codes = ["ref_cycle_iter"]
+        stop_codes = ["max_iter", "divergence"]
+        BLA_activated = (BLA_eps is not None) and (self.dx < settings.newton_zoom_level)
+
+        def set_state():
+            def impl(instance):
+                instance.complex_type = np.float64
+                instance.potential_M = M_divergence
+                instance.codes = (complex_codes, int_codes, stop_codes)
+                instance.calc_hessian = calc_hessian
+                instance.backshift = None
+            return impl
+
+        spec = PerturbSpec(flavor=self.flavor_int, max_iter=max_iter,
+                           M_divergence=M_divergence, calc_dzndc=calc_hessian,
+                           bla=BLA_activated, xr_detect_activated=False,
+                           nZ=len(complex_codes))
+        return {"set_state": set_state, "initialize": _no_initialize,
+                "iterate": lambda: spec}
+
+    @staticmethod
+    def _ball_method(c, px, maxiter, M_divergence):
+        # the BS ball method (FP_loop.pyx:2357-2563) is not restated: the
+        # reference falls back to the image centre when it fails
+        return None
+
+    @staticmethod
+    def find_nucleus(c, order, eps_pixel, max_newton=None, eps_cv=None):
+        raise NotImplementedError
+
+    @staticmethod
+    def find_any_nucleus(c, order, eps_pixel, max_newton=None, eps_cv=None):
+        return False, c

@@ -172,6 +172,25 @@ def _cmul(ax, ay, bx, by, F):
     return (ax * bx - ay * by) >> F, (ax * by + ay * bx) >> F
 
 
+def _newton_step_float(c, order, divide_divisors, prec):
+    """One Newton step in floating point (mpmath at ``prec`` bits): used when
+    the current c escapes, where fixed point would overflow."""
+    with mpmath.workprec(prec):
+        zr = mpmath.mpc(0)
+        dz = mpmath.mpc(0)
+        h = mpmath.mpc(1)
+        dh = mpmath.mpc(0)
+        for i in range(1, order + 1):
+            dz = 2 * dz * zr + 1
+            zr = zr * zr + c
+            if divide_divisors and i < order and order % i == 0:
+                h *= zr
+                dh += dz / zr
+        f = zr / h
+        df = (dz - zr * dh) / h
+        return f / df, zr
+
+
 def _find_nucleus(seed_x, seed_y, seed_prec, order, max_newton, seed_eps_cv,
                   seed_eps_valid, divide_divisors):
     F = int(seed_prec) + GUARD_BITS
@@ -179,6 +198,7 @@ def _find_nucleus(seed_x, seed_y, seed_prec, order, max_newton, seed_eps_cv,
     eps_cv = mpmath.mpf(_dec(seed_eps_cv)) * 64
     eps_valid = mpmath.mpf(_dec(seed_eps_valid))
     one = 1 << F
+    big = F + 64          # |z| > 2**64: the orbit escapes
     order = int(order)
     newton_cv = False
     for _ in range(int(max_newton)):
@@ -186,13 +206,23 @@ def _find_nucleus(seed_x, seed_y, seed_prec, order, max_newton, seed_eps_cv,
         dx = dy = 0
         hx, hy = one, 0
         dhx = dhy = 0
+        escaped = False
         for i in range(1, order + 1):
             dx, dy = ((zx * dx - zy * dy) >> (F - 1)) + one, (zx * dy + zy * dx) >> (F - 1)
             zx, zy = _sq_add(zx, zy, cx, cy, F)
+            if zx.bit_length() > big or zy.bit_length() > big:
+                escaped = True
+                break
             if divide_divisors and i < order and order % i == 0:
                 hx, hy = _cmul(hx, hy, zx, zy, F)
                 qx, qy = _cdiv(dx, dy, zx, zy, F)
                 dhx, dhy = dhx + qx, dhy + qy
+        if escaped:
+            step_c, zr = _newton_step_float(
+                mpmath.mpc(_to_mpf(cx, F), _to_mpf(cy, F)), order, divide_divisors, F)
+            sx, sy = _fix(step_c.real, F), _fix(step_c.imag, F)
+            cx, cy = cx - sx, cy - sy
+            continue
         # f = zr / h ; df = (dzrdc - zr * dh) / h ; step = f / df
         fx, fy = _cdiv(zx, zy, hx, hy, F)
         tx, ty = _cmul(zx, zy, dhx, dhy, F)

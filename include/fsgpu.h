@@ -153,6 +153,11 @@ int fsg_perturb_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
                       int32_t ntiles, int32_t where);
 int fsg_last_stats(const fsg_ctx *ctx, fsg_stats *out);
 
+/* Measured FMA throughput of this GPU in TFLOP/s (fp64 = 0: FP32 pipe,
+ * 1: FP64 pipe): the roofline denominator of the iteration kernels.  No
+ * counterpart in the reference (a measurement helper). */
+int fsg_peak_flops(fsg_ctx *ctx, int32_t fp64, double *tflops);
+
 int fsg_cancel(fsg_ctx *ctx);
 int fsg_clear_cancel(fsg_ctx *ctx);
 
