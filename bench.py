@@ -193,7 +193,10 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the library launches on it and the CUDA events
+    # that time the steps are recorded on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
 
     w = syn.config2_workload(nx=args.nx)
     n = w.nx * w.ny
@@ -246,6 +249,7 @@ def run_ours(args):
             dist.barrier()
         for _ in range(k):
             flush.fill_(1.0)
+            stream.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)

@@ -289,6 +289,9 @@ def perturbation_nonholomorphic_FP_loop(orbit, need_Xrange, max_iter, M, seed_x,
     Returns (i, partial_dict, xr_dict) with the Xrange register holding
     iterations where |x| or |y| < XR_TSHOLD (only if need_Xrange)."""
     orb = orbit.view(np.complex128) if orbit.dtype != np.complex128 else orbit
+    if int(seed_prec) <= 53:
+        # MPFR at 53 bits, round to nearest, is IEEE double arithmetic
+        return _bs_loop_double(orb, max_iter, M, float(_dec(seed_x)), float(_dec(seed_y)), kind)
     F = int(seed_prec) + GUARD_BITS
     a, b = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
     x = y = 0
@@ -318,3 +321,29 @@ def perturbation_nonholomorphic_FP_loop(orbit, need_Xrange, max_iter, M, seed_x,
     if i == max_iter and abs_i <= M:
         i += 1
     return i, {}, xr_dict
+
+
+def _bs_loop_double(orb, max_iter, M, a, b, kind):
+    """BS-family orbit in IEEE double (the seed_prec <= 53 case)."""
+    x = y = 0.
+    orb[0] = 0.
+    i = 0
+    abs_i = 0.
+    for i in range(1, max_iter + 1):
+        if kind == 1:
+            x, y = x * x - y * y + a, 2. * abs(x * y) - b
+        elif kind == 2:
+            x, y = x * x - y * y + a, 2. * x * abs(y) - b
+        elif kind == 3:
+            x, y = x * x - y * abs(y) + a, 2. * x * y - b
+        elif kind == 4:
+            x, y = abs(x * x - y * y) + a, 2. * x * y - b
+        else:
+            x, y = abs(x * x - y * y) + a, 2. * abs(x * y) - b
+        orb[i] = complex(x, y)
+        abs_i = math.hypot(x, y)
+        if abs_i > M:
+            break
+    if i == max_iter and abs_i <= M:
+        i += 1
+    return i, {}, {}

@@ -133,7 +133,8 @@ int fsg_ctx_create(int device, fsg_ctx **out);
 int fsg_ctx_destroy(fsg_ctx *ctx);
 const char *fsg_last_error(const fsg_ctx *ctx);
 /* Use an external CUDA stream (cudaStream_t as void*) instead of the
- * context's own; NULL restores it. */
+ * context's own; NULL restores the context's own stream (the legacy default
+ * stream cannot be selected). */
 int fsg_set_stream(fsg_ctx *ctx, void *stream);
 int fsg_sync(fsg_ctx *ctx);
 

@@ -469,7 +469,46 @@ def golden_xrange(out, seed=100, n=400):
     np.savez_compressed(out, **res)
 
 
+def golden_flake_orbit(out):
+    """The reference's stored FP64 orbit of the 'flake' point
+    (tests/REFERENCE_DATA/perturb_REF/flake/dev_pt0.ref), first period."""
+    import pickle
+    path = os.path.join(os.path.dirname(REF_SRC), "tests", "REFERENCE_DATA",
+                        "perturb_REF", "flake", "dev_pt0.ref")
+    with open(path, "rb") as f:
+        params = pickle.load(f)
+        orbit = pickle.load(f)[:, 0]
+    rp = params["ref_point"]
+    prec = max(rp.real._mpf_[1].bit_length(), rp.imag._mpf_[1].bit_length())
+    order = int(params["order"])
+    with mpmath.workprec(prec + 64):
+        x = mpmath.nstr(rp.real, int(prec / 3.3) + 20)
+        y = mpmath.nstr(rp.imag, int(prec / 3.3) + 20)
+    np.savez_compressed(out, x=x, y=y, prec=prec, order=order, orbit=orbit[:order + 1])
+
+
+def golden_newton_kat(out):
+    """Newton known answer of the reference's tests/test_FP_loop.py (test_newton):
+    the start point and expected nucleus digits, read from the test source."""
+    import ast
+    path = os.path.join(os.path.dirname(REF_SRC), "tests", "test_FP_loop.py")
+    tree = ast.parse(open(path).read())
+    found = {}
+    for node in ast.walk(tree):
+        if isinstance(node, ast.Assign) and isinstance(node.value, ast.Dict):
+            keys = [k.value for k in node.value.keys if isinstance(k, ast.Constant)]
+            if "x_nucleus" in keys:
+                found = {k.value: v.value for k, v in zip(node.value.keys, node.value.values)
+                         if isinstance(v, ast.Constant)}
+    np.savez_compressed(out, x_start=found["x_start"], y_start=found["y_start"],
+                        order=found["order"], x_nucleus=found["x_nucleus"],
+                        y_nucleus=found["y_nucleus"])
+
+
 def main():
+    golden_flake_orbit(os.path.join(HERE, "flake_orbit.npz"))
+    golden_newton_kat(os.path.join(HERE, "newton_4252.npz"))
+    print("host orbit fixtures done", flush=True)
     mpmath.mp.dps = 50
     golden_xrange(os.path.join(HERE, "xrange_ops.npz"))
     print("xrange done", flush=True)

@@ -1,0 +1,123 @@
+"""
+The host-side mirror of the reference API, without a GPU: decorators, pixel
+grid, codes of the calc_std_div variants, reference-point preparation.
+Same checks as the reference's tests/test_core.py (chunk indexing) and the
+plug-in contract of tests/test_postproc.py (codes, keyword-only options).
+"""
+import mpmath
+import numpy as np
+import pytest
+
+import fractalshades_gb300 as fs
+import fractalshades_gb300.models as fsm
+from fractalshades_gb300 import settings
+
+
+def test_zoom_options_keyword_only_and_stored(tmp_path):
+    f = fsm.Mandelbrot(str(tmp_path))
+    with pytest.raises(TypeError):
+        f.zoom(0.)
+    f.zoom(x=-0.5, y=0.1, dx=3., nx=800, xy_ratio=4. / 3., theta_deg=0.)
+    assert f.zoom_kwargs["nx"] == 800 and f.zoom_kwargs["has_skew"] is False
+    assert f.x == -0.5 and f.ny == 600
+    assert np.array_equal(f.lin_mat, np.array([[1., -0.], [0., 1.]]))
+
+
+def test_calc_options_hook_receives_defaults(tmp_path):
+    seen = {}
+
+    class Probe(fsm.Mandelbrot):
+        def calc_hook(self, calc_callable, calc_kwargs, return_dic):
+            seen["name"] = calc_callable
+            seen["kwargs"] = calc_kwargs
+            seen["ret"] = return_dic
+
+    f = Probe(str(tmp_path))
+    f.zoom(x=-0.5, y=0., dx=3., nx=80, xy_ratio=1., theta_deg=0.)
+    f.calc_std_div(calc_name="c", subset=None, max_iter=100, M_divergence=1000.)
+    assert seen["name"] == "calc_std_div"
+    assert seen["kwargs"]["epsilon_stationnary"] == 0.01
+    assert set(seen["ret"]) == {"set_state", "initialize", "iterate"}
+    with pytest.raises(TypeError):
+        f.calc_std_div("c")
+
+
+@pytest.mark.parametrize("nx,ratio", [(800, 4. / 3.), (451, 1.), (203, 0.7)])
+def test_chunks_and_pixel_grid(tmp_path, nx, ratio):
+    """tests/test_core.py chunk indexing; image_axes reproduces every tile's
+    chunk_pixel_pos (core.py:1767-1830)."""
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=0., y=0., dx=1., nx=nx, xy_ratio=ratio, theta_deg=0.)
+    xs, ys = f.image_axes()
+    for rank, cs in enumerate(f.chunk_slices()):
+        assert f.chunk_rank(cs) == rank
+        assert f.chunk_from_rank(rank) == cs
+        ix, ixx, iy, iyy = cs
+        pix = f.chunk_pixel_pos(cs)
+        assert np.array_equal(pix.real, np.broadcast_to(xs[ix:ixx], pix.shape))
+        assert np.array_equal(pix.imag, np.broadcast_to(ys[iy:iyy, None], pix.shape))
+    assert f.chunks_count == rank + 1
+
+
+def _codes(f, **kw):
+    ret = type(f).calc_std_div.__wrapped__(f, **kw)
+    ns = type("S", (), {})()
+    ret["set_state"]()(ns)
+    return ns.codes, ret["iterate"]()
+
+
+def test_perturbation_codes(tmp_path):
+    f = fsm.Perturbation_mandelbrot(str(tmp_path))
+    f.zoom(precision=30, x="-0.75", y="0.1", dx="1e-10", nx=64, xy_ratio=1., theta_deg=0.)
+    base = dict(calc_name="c", subset=None, max_iter=1000, M_divergence=1000.,
+                epsilon_stationnary=1e-3)
+    codes, spec = _codes(f, **base)
+    assert codes == (["zn", "dzndc"], ["ref_cycle_iter"], ["max_iter", "divergence", "stationnary"])
+    assert spec.i_dzndc == 1 and spec.i_dzndz == -1 and spec.bla
+    codes, spec = _codes(f, interior_detect=True, **base)
+    assert codes[0] == ["zn", "dzndz", "dzndc"] and spec.i_dzndz == 1 and spec.i_dzndc == 2
+    codes, spec = _codes(f, calc_dzndc=False, BLA_eps=None, **base)
+    assert codes[0] == ["zn"] and not spec.bla
+    # precision mode follows the reference's Xrange switch (H1)
+    settings.precision_mode = "auto"
+    assert spec.mode == "fp64"
+    f.zoom(precision=400, x="-0.75", y="0.1", dx="1e-300", nx=64, xy_ratio=1., theta_deg=0.)
+    assert f.xr_detect_activated          # mpf('1e-300') < 1e-300 (float)
+    _, spec = _codes(f, **base)
+    assert spec.mode == "xr64"
+
+
+def test_bs_codes(tmp_path):
+    f = fsm.Perturbation_burning_ship(str(tmp_path), flavor="Celtic")
+    f.zoom(precision=30, x="-1.75", y="-0.03", dx="1e-8", nx=64, xy_ratio=1., theta_deg=0.)
+    codes, spec = _codes(f, calc_name="c", subset=None, max_iter=1000, M_divergence=1000.)
+    assert codes == (["xn", "yn", "dxnda", "dxndb", "dynda", "dyndb"], ["ref_cycle_iter"],
+                     ["max_iter", "divergence"])
+    assert spec.flavor == 4
+
+
+def test_reference_point_search_and_path_data(tmp_path):
+    """get_FP_orbit: ball method -> Newton -> orbit wrapped at the period;
+    get_path_data and ref_point_kc (perturbation.py:166-194, 317-375, 651-854)."""
+    from fractalshades_gb300 import synthetic as syn
+    c = syn.find_nucleus(40, 80)
+    f = fsm.Perturbation_mandelbrot(str(tmp_path))
+    with mpmath.workdps(80):
+        x, y = str(c.real + mpmath.mpf("3e-40")), str(c.imag)
+    # zoom sets mpmath's working precision for the calculations that follow
+    f.zoom(precision=80, x=x, y=y, dx="1e-38", nx=100, xy_ratio=1., theta_deg=0.)
+    f.max_iter = 5000
+    f.M_divergence = 1000.
+    f.get_FP_orbit()
+    assert f.FP_params["order"] == 40
+    assert abs(f.FP_params["ref_point"] - c) < mpmath.mpf("1e-60")
+    (Zn, has_xr, idx, xr, div_iter, order, drift, dx) = f.get_path_data()
+    assert Zn.size == 40 and order == 40 and div_iter == 5001 and not has_xr
+    z = mpmath.mpc(0)
+    for k in range(1, 40):
+        z = z * z + c
+        assert Zn[k] == complex(float(z.real), float(z.imag))
+    kc = f.ref_point_kc().to_standard()
+    assert 1.1 * 0.5 * np.sqrt(2) * 1e-38 < kc < 1.1 * (0.5 * np.sqrt(2) + 0.4) * 1e-38
+    # a second call reuses the stored orbit (ref_point_matching)
+    assert f.ref_point_matching()

@@ -1,0 +1,92 @@
+"""
+Host arbitrary-precision layer (mpmath_utils/FP_loop.py) against the known
+answers of the reference's tests/test_FP_loop.py and its stored FP64 orbits
+(tests/REFERENCE_DATA).  The values below are copied from those tests (they
+are the reference's test vectors, not computed here).
+"""
+import os
+import pickle
+
+import mpmath
+import numpy as np
+import pytest
+
+from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_ball_method_order_4252():
+    """tests/test_FP_loop.py:166-193 of the reference."""
+    x = ("-1.38489865821023436791757551552306535886843948840412919252407990736888"
+         "673896107")
+    y = ("0.02274991237672465768411681642741466833930426052197620974166612959128"
+         "19114324773")
+    order = fsFP.perturbation_mandelbrot_ball_method(
+        x.encode(), y.encode(), int(78 * 3.33), "1.253026641642179625e-70".encode(),
+        100000, 1000.0)
+    assert order == 4252
+
+
+def test_bs_orbit_is_double_recurrence_at_53_bits():
+    """tests/test_FP_loop.py:278-309: at 53 bits the BS orbit is the IEEE
+    double recurrence x' = x^2 - y^2 + a, y' = 2|xy| - b."""
+    x, y = 0.1, 0.1
+    npts = 10
+    orbit = np.empty((npts,), dtype=np.complex128)
+    fsFP.perturbation_nonholomorphic_FP_loop(orbit.view(np.float64), False, npts - 1, 1000.,
+                                             str(x).encode(), str(y).encode(), 53, 1)
+    z = complex(0.)
+    for i in range(10):
+        assert orbit[i] == z
+        nx = z.real ** 2 - z.imag ** 2 + x
+        ny = 2 * np.abs(z.real * z.imag) - y
+        z = nx + 1j * ny
+
+
+def test_orbit_matches_reference_stored_orbit():
+    """The reference stores (tests/REFERENCE_DATA/perturb_REF/flake/dev_pt0.ref)
+    an FP64 orbit of its 668-bit reference point, period 7884.  The host loop
+    reproduces it bit-for-bit over the whole period (at the period the orbit
+    returns to ~0, a value made of rounding noise)."""
+    fx = os.path.join(HERE, "golden", "flake_orbit.npz")
+    d = np.load(fx)
+    order = int(d["order"])
+    orbit = np.zeros(order + 1, dtype=np.complex128)
+    i, _, _ = fsFP.perturbation_mandelbrot_FP_loop(
+        orbit, False, order, 1e6, str(d["x"]), str(d["y"]), int(d["prec"]))
+    assert i == order + 1
+    assert np.array_equal(orbit[:order].view(np.uint64), d["orbit"][:order].view(np.uint64))
+
+
+def test_newton_nucleus_and_size():
+    """Newton with divisor deflation lands on a nucleus whose orbit returns to
+    0 at the period; the ball method confirms the period."""
+    from fractalshades_gb300 import synthetic as syn
+    c = syn.find_nucleus(37, 60)
+    with mpmath.workdps(60):
+        z = mpmath.mpc(0)
+        for _ in range(37):
+            z = z * z + c
+        assert abs(z) < mpmath.mpf(10) ** -25
+        size = fsFP.perturbation_mandelbrot_nucleus_size_estimate(
+            str(c.real), str(c.imag), mpmath.mp.prec, 37)
+        assert 0 < abs(size) < 1e-3
+
+
+@pytest.mark.slow
+def test_newton_4252_reference_digits():
+    """tests/test_FP_loop.py:231-272: Newton from a 80-digit start at order
+    4252 and 11622-bit precision agrees with the reference's ~3500-digit
+    nucleus.  Expected digits stored in tests/golden/newton_4252.npz."""
+    d = np.load(os.path.join(HERE, "golden", "newton_4252.npz"))
+    precision = int(3522 * 3.3)
+    eps = mpmath.mpf(val=(2, -precision))
+    eps_pix = mpmath.mpf(val=(2, -int(84 * 3.3)))
+    with mpmath.workprec(precision):
+        ok, val = fsFP.perturbation_mandelbrot_find_nucleus(
+            str(d["x_start"]).encode(), str(d["y_start"]).encode(), precision, 4252, 80,
+            str(eps).encode(), str(eps_pix).encode())
+    assert ok
+    with mpmath.workprec(precision - 10):
+        assert mpmath.almosteq(mpmath.mpf(str(d["x_nucleus"])), val.real)
