@@ -21,6 +21,8 @@ FSG_ERR_ARG = -1
 FSG_ERR_CUDA = -2
 FSG_ERR_NOMEM = -3
 FSG_ERR_NODEV = -4
+FSG_ERR_LIMIT = -5
+FSG_NOALLOC_MAX_TILES = 64
 
 MODE_FP64 = 0
 MODE_XR64 = 1
@@ -78,6 +80,7 @@ SYMBOLS = [
     "fsg_set_stream", "fsg_sync", "fsg_ref_create", "fsg_ref_destroy",
     "fsg_ref_info", "fsg_ref_download", "fsg_std_tiles", "fsg_perturb_tiles",
     "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel", "fsg_peak_flops",
+    "fsg_std_tiles_noalloc",
 ]
 
 

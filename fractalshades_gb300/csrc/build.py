@@ -29,6 +29,7 @@ SOURCES = {
     "fsg_ref.cu": ["-fmad=false"],
     "fsg_perturb_fe32.cu": [],
     "fsg_peak.cu": [],
+    "fsg_noalloc.cu": [],
     "fsg_abi.cu": [],
 }
 HEADERS = ["fsg_num.cuh", "fsg_internal.cuh"]

@@ -42,6 +42,7 @@ extern "C" {
 #define FSG_ERR_CUDA (-2)
 #define FSG_ERR_NOMEM (-3)
 #define FSG_ERR_NODEV (-4)
+#define FSG_ERR_LIMIT (-5)     /* a size beyond a stated maximum              */
 
 /* delta arithmetic of the perturbation kernels */
 #define FSG_MODE_FP64 0  /* double deltas: the reference with xr_detect_activated False   */
@@ -161,6 +162,28 @@ int fsg_peak_flops(fsg_ctx *ctx, int32_t fp64, double *tflops);
 
 int fsg_cancel(fsg_ctx *ctx);
 int fsg_clear_cancel(fsg_ctx *ctx);
+
+/* Allocation-free variant of fsg_std_tiles.  It has no counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc -- their device
+ * memory is reserved up front by another allocator, or they cannot afford the
+ * device synchronisation that cudaMalloc / cudaFree imply inside a frame loop.
+ * It needs no context and allocates nothing: every pointer of every tile
+ * (xs / ys or pix, Z, stop_reason, stop_iter, optional potential / dem) is a
+ * device pointer, and the launch's work counter, statistics and tile
+ * descriptors live in a file-scope __device__ array of the library, one per
+ * device, held until the process exits.
+ *   - at most FSG_NOALLOC_MAX_TILES tiles per call, else FSG_ERR_LIMIT;
+ *   - asynchronous on `stream` (NULL: the legacy default stream); results are
+ *     valid once the stream has completed;
+ *   - every call shares the array (the counter and statistics are cleared at
+ *     the start of each call): calls whose launches overlap on the GPU, from
+ *     other streams or host threads, race on it;
+ *   - the first call on a device resolves the array's address with that device
+ *     current; make that first call before any stream capture;
+ *   - not cancellable (fsg_cancel does not apply). */
+#define FSG_NOALLOC_MAX_TILES 64
+int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+                          void *stream);
 
 #ifdef __cplusplus
 }
