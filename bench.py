@@ -43,7 +43,39 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nx", type=int, default=2048)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--serving-requests", type=int, default=2000,
+                    help="requests of the serving stream (0: skip)")
     return ap.parse_args()
+
+
+def serving_leg(n_requests, device):
+    """The serving stream: Poisson arrivals at 200/s, tiles of 256..2048
+    squared, widths log-uniform in [1e-1000, 1e-10] around 8 seeded period-p
+    nuclei (1100 digits), max_iter 2e5, FP32+exp deltas, 120 GB HBM budget."""
+    from fractalshades_gb300 import serving as srv
+    rng = np.random.default_rng(5)
+    periods = [int(p) for p in rng.integers(300, 3001, 8)]
+    t0 = time.perf_counter()
+    centers = [srv.make_center(p, 1100, 200000) for p in periods]
+    setup_s = time.perf_counter() - t0
+    reqs = srv.request_stream(centers, n_requests, rate=200.0, seed=5)
+    server = srv.TileServer(centers, hbm_budget=120 * 2 ** 30, n_slots=3,
+                            max_batch_pixels=8 * 2 ** 20, mode="fe32", device=device)
+    t0 = time.perf_counter()
+    try:
+        done = server.run(reqs, realtime=True, timeout=600)
+    finally:
+        wall = time.perf_counter() - t0
+        server.close()
+    lat = np.array([(r.done - r.arrival) * 1e3 for r in done])
+    iters = float(sum(r.pixel_iters for r in done))
+    return {"requests": len(done), "rate_per_s": 200.0, "wall_s": wall,
+            "pixel_iter_per_s": iters / wall, "latency_ms": {
+                "p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                "max": float(lat.max())},
+            "slots": 3, "hbm_budget_gb": 120, "peak_reserved_gb": server.max_reserved / 2 ** 30,
+            "centers": periods, "center_setup_s": setup_s,
+            "sides": [256, 512, 1024, 2048], "widths": "1e-1000 .. 1e-10 log-uniform"}
 
 
 # ---------------------------------------------------------------------------
@@ -352,6 +384,10 @@ def run_ours(args):
         lat.append((time.perf_counter() - t0) * 1e3)
     lat = np.array(lat[2:])
 
+    serving = None
+    if args.serving_requests > 0 and rank == 0:
+        serving = serving_leg(args.serving_requests, local)
+
     if rank != 0:
         if dist:
             dist.barrier()
@@ -388,6 +424,7 @@ def run_ours(args):
             "speedup_fe32_vs_fp64": value / value_fp if value_fp else None,
         },
         "accuracy_fe32_vs_xr64": accuracy,
+        "serving": serving,
         "tile_latency_ms": {"p50": float(np.percentile(lat, 50)),
                             "p99": float(np.percentile(lat, 99)), "tiles": int(lat.size),
                             "sizes": sizes, "path": "C-ABI host buffers, FP32+exp"},

@@ -25,6 +25,7 @@ void fsg_build_paths_bs(const RefDev *Rd, double *dXa, double *dXb, double *dYa,
                         double scale, cudaStream_t s);
 void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *Mbs, double *r,
                    int stages, double kc, double eps, cudaStream_t s);
+void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, cudaStream_t s);
 void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzndc,
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
@@ -208,10 +209,7 @@ int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int n
     W.cancel = ctx->cancel_dev; W.status = ctx->status_dev;
     CalcDev C = make_calc(calc);
     const int block = 256;
-    int per_sm = 2;
-    int grid = ctx->sm_count * per_sm;
-    long long need = (total + block - 1) / block;
-    if (need < grid) grid = (int)(need > 0 ? need : 1);
+    const int grid = 0;   // one persistent wave at the kernel's occupancy limit
     CK(cudaEventRecord(ctx->ev0, s), "cudaEventRecord");
     if (!perturb) fsg_launch_std(W, C, grid, block, s);
     else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
@@ -488,14 +486,16 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     }
     R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.stages = stages;
     // fe tables (M2)
-    int4 *Zf = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_A = nullptr, *bla_B = nullptr;
+    int4 *Zf = nullptr, *Zp = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_A = nullptr,
+         *bla_B = nullptr;
     if (d->flavor == 0) {
         RA(Zf, len + 1);
+        RA(Zp, len + 1);
         if (d->calc_dzndc) RA(dzndc_f, len + 1);
         if (d->calc_dzndz) RA(dzndz_f, len + 2);
         if (R.bla_len > 0) { RA(bla_A, R.bla_len); RA(bla_B, R.bla_len); }
     }
-    R.Zf = Zf; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f_A = bla_A; R.bla_f_B = bla_B;
+    R.Zf = Zf; R.Zp = Zp; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f_A = bla_A; R.bla_f_B = bla_B;
     RCK(cudaMalloc((void **)&r->dev, sizeof(RefDev)), "cudaMalloc(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     // builds
@@ -506,9 +506,11 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
         fsg_build_paths_bs(r->dev, dXa, dXb, dYa, dYb, ldexp(d->scale_m, d->scale_e), s);
     }
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
-    if (d->flavor == 0)
+    if (d->flavor == 0) {
         fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
                             dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_A, bla_B, s);
+        fsg_build_plain_orbit(r->dev, len, Zf, Zp, s);
+    }
     RCK(cudaGetLastError(), "reference table kernels");
     RCK(cudaStreamSynchronize(s), "reference table build");
 #undef RA

@@ -33,6 +33,8 @@ struct RefDev {
     int stages, bla_len;
     // FE32 tables: int4 {x bits, y bits, exponent, aux}
     const int4 *Zf;             // [len + 1]; aux = exponent of max(|x|,|y|) or FE_ZERO_E
+    const int4 *Zp;             // [len + 1] plain floats {x bits, y bits, exponent of
+                                // max(|x|,|y|) or FE_ZERO_E when below 2^-100, 0}
     const int4 *dZndc_f;        // [len + 1]
     const int4 *dZndz_f;        // [len + 2]
     const int4 *bla_f_A;        // [bla_len] A (x, y, e, r_bits)
@@ -131,7 +133,24 @@ __device__ __forceinline__ double2 fsg_pixel(const TileDev &T, long long ip) {
     return make_double2(__ldg(&T.xs[ix]), __ldg(&T.ys[iy]));
 }
 
-// Kernel launchers (one per translation unit)
+// Persistent grid for a kernel: every SM filled to its occupancy limit,
+// capped by the number of blocks the work needs.  grid > 0 is kept as given.
+template <class K>
+inline int fsg_auto_grid(K kernel, int grid, int block, long long total) {
+    if (grid > 0) return grid;
+    int dev = 0, sms = 1, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess || per < 1)
+        per = 1;
+    long long need = (total + block - 1) / block;
+    long long g = (long long)sms * per;
+    if (need < g) g = need > 0 ? need : 1;
+    return (int)g;
+}
+
+// Kernel launchers (one per translation unit); grid 0 = one persistent wave
+// at full occupancy
 void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);
 void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,

@@ -426,7 +426,10 @@ __global__ void __launch_bounds__(256) k_perturb_bs(WorkDev W, CalcDev C) {
 }
 
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    if (C.flavor != 0) k_perturb_bs<<<grid, block, 0, s>>>(W, C);
-    else if (C.mode == 1) k_perturb_m2<true><<<grid, block, 0, s>>>(W, C);
-    else k_perturb_m2<false><<<grid, block, 0, s>>>(W, C);
+    if (C.flavor != 0)
+        k_perturb_bs<<<fsg_auto_grid(k_perturb_bs, grid, block, W.total), block, 0, s>>>(W, C);
+    else if (C.mode == 1)
+        k_perturb_m2<true><<<fsg_auto_grid(k_perturb_m2<true>, grid, block, W.total), block, 0, s>>>(W, C);
+    else
+        k_perturb_m2<false><<<fsg_auto_grid(k_perturb_m2<false>, grid, block, W.total), block, 0, s>>>(W, C);
 }

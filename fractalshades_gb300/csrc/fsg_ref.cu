@@ -246,6 +246,22 @@ __global__ void k_fe_orbit(const RefDev *Rp, int4 *Zf) {
     Zf[i] = pack_fe(v);
 }
 
+// plain-float copy of the orbit for the fast steps; values below 2^-100 are
+// flagged (exponent FE_ZERO_E) so that the kernel takes its exact path there
+__global__ void k_plain_orbit(const RefDev *Rp, const int4 *Zf, int4 *Zp) {
+    const RefDev &R = *Rp;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > R.len) return;
+    int4 f = Zf[i];
+    if (f.z == FE_ZERO_E || f.z < -100) {
+        Zp[i] = make_int4(0, 0, FE_ZERO_E, 0);
+        return;
+    }
+    float s = __int_as_float((f.z + 127) << 23);   // 2^e, e in [-100, 127]
+    float x = __int_as_float(f.x) * s, y = __int_as_float(f.y) * s;
+    Zp[i] = make_int4(__float_as_int(x), __float_as_int(y), f.z, 0);
+}
+
 __global__ void k_fe_path(const double2 *std_p, const double2 *xm, const int *xe, int n,
                           int4 *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,6 +316,11 @@ void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *M
             k_bla_level_bs<<<(n + tb - 1) / tb, tb, 0, s>>>(Mbs, r, L, stg, kc, eps);
         }
     }
+}
+
+void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, cudaStream_t s) {
+    int tb = 256;
+    k_plain_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf, Zp);
 }
 
 void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzndc,

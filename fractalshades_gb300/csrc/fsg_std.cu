@@ -118,6 +118,6 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
 }
 
 void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    if (C.flavor == 0) k_std_m2<<<grid, block, 0, s>>>(W, C);
-    else k_std_bs<<<grid, block, 0, s>>>(W, C);
+    if (C.flavor == 0) k_std_m2<<<fsg_auto_grid(k_std_m2, grid, block, W.total), block, 0, s>>>(W, C);
+    else k_std_bs<<<fsg_auto_grid(k_std_bs, grid, block, W.total), block, 0, s>>>(W, C);
 }
