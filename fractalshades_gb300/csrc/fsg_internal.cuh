@@ -33,12 +33,14 @@ struct RefDev {
     int stages, bla_len;
     // FE32 tables: int4 {x bits, y bits, exponent, aux}
     const int4 *Zf;             // [len + 1]; aux = exponent of max(|x|,|y|) or FE_ZERO_E
-    const int4 *Zp;             // [len + 1] plain floats {x bits, y bits, exponent of
-                                // max(|x|,|y|) or FE_ZERO_E when below 2^-100, 0}
+    const int4 *Zp;             // [len + 1] plain floats {2 Z.x bits, 2 Z.y bits,
+                                // (exponent of max(|Z.x|,|Z.y|)) - 26 or FE_ZERO_E
+                                // outside [2^-100, 2^100], 1 if Z is exactly 0}
     const int4 *dZndc_f;        // [len + 1]
     const int4 *dZndz_f;        // [len + 2]
-    const int4 *bla_f_A;        // [bla_len] A (x, y, e, r_bits)
-    const int4 *bla_f_B;        // [bla_len] B (x, y, e, r_e)
+    const int4 *bla_f;          // [2 bla_len] per entry i: [2i] = {r mantissa bits,
+                                // r exponent, A exponent, B exponent},
+                                // [2i + 1] = {A.x, A.y, B.x, B.y} float bits
 };
 
 struct TileDev {

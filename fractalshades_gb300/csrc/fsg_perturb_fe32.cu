@@ -111,26 +111,78 @@ __device__ __forceinline__ void store_fe(float &x, float &y, int &e, fe d) {
     else { x = d.x; y = d.y; e = d.e; }
 }
 
-__device__ __forceinline__ int bla_lookup_fast(const RefDev &R, const Lane &s, int L, int w,
-                                               int &ib) {
-    int it = w >> FSG_STG_COMPRESSED;
-    int stages = FSG_STG_COMPRESSED;
-    for (int k = FSG_STG_COMPRESSED; k < R.stages; k++) {
-        stages = k;
-        if (it & 1) break;
-        it >>= 1;
+// biased exponent of max(|ux|, |uy|) (0 for 0 and subnormals)
+__device__ __forceinline__ int mag_b(const Lane &s) {
+    return __float_as_int(fmaxf(fabsf(s.ux), fabsf(s.uy))) >> 23;
+}
+
+// One fast step at orbit index w, Zc = {2 Z_w, limit, flags}:
+//   u' = 2 Z u + cu,   v' = 2 (Z v + 2^kd D u),  kd = De + E - F
+// (D = dZndc_w, zero right after a dynamic rebase).  v = 0 is held with
+// F = FE_ZERO_E, which sends kd above 100 and rescales v onto the new term.
+__device__ __forceinline__ void fast_step(Lane &s, int4 Zc, const int4 *__restrict__ Zp,
+                                          const int4 *__restrict__ dZndc_f, int w, bool dyn) {
+    const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);   // 2 Z
+    if (dZndc_f) {
+        int4 Dv = __ldg(&dZndc_f[w]);
+        const float dx = dyn ? 0.f : __int_as_float(Dv.x), dy = dyn ? 0.f : __int_as_float(Dv.y);
+        const int De = dyn ? FE_ZERO_E : Dv.z;
+        int kd = De + s.E - s.F;
+        if (kd > 100) {
+            int Fn = De + s.E - 30;
+            float sc = p2f(s.F - Fn);
+            s.vx *= sc; s.vy *= sc; s.F = Fn; kd = 30;
+        }
+        // 2^(kd + 1), 0 below 2^-126 (kd <= 100 here)
+        const float sk = __int_as_float((max(kd + 1, -127) + 127) << 23);
+        const float ax = (dx * s.ux - dy * s.uy) * sk, ay = (dx * s.uy + dy * s.ux) * sk;
+        const float vx = fmaf(Zx, s.vx, fmaf(-Zy, s.vy, ax));
+        const float vy = fmaf(Zx, s.vy, fmaf(Zy, s.vx, ay));
+        s.vx = vx; s.vy = vy;
+        renorm_v(s.vx, s.vy, s.F);
     }
-    int invalid_step = R.first_invalid - w;
-    for (int stg = stages; stg >= FSG_STG_COMPRESSED; stg--) {
-        int step = 1 << stg;
-        if (step >= invalid_step) continue;
-        int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
-        float rm = __int_as_float(__ldg(&R.bla_f_A[idx].w));
-        int re = __ldg(&R.bla_f_B[idx].w);
-        bool ok = (L == FE_ZERO_E) ? (re != FE_ZERO_E) : lt_r(s.ux, s.uy, s.E, L, rm, re);
-        if (ok) { ib = idx; return step; }
+    const float nx = fmaf(Zx, s.ux, fmaf(-Zy, s.uy, s.cux));
+    const float ny = fmaf(Zx, s.uy, fmaf(Zy, s.ux, s.cuy));
+    s.ux = nx; s.uy = ny;
+}
+
+// |dz| < r for the BLA entry whose header is H = {r mantissa bits, r exponent,
+// A exponent, B exponent}; L = magnitude exponent of dz (FE_ZERO_E for 0:
+// valid iff r > 0, the reference's 0 < r)
+__device__ __forceinline__ bool bla_ok(const Lane &s, int L, int4 H) {
+    return (L == FE_ZERO_E) ? (H.y != FE_ZERO_E)
+                            : lt_r(s.ux, s.uy, s.E, L, __int_as_float(H.x), H.y);
+}
+
+// ref_BLA_get (perturbation.py:2116-2170): the largest stage from
+// 3 + ctz(w >> 3) (capped at stages - 1) down to 3 whose step is below
+// first_invalid - w and whose radius admits dz.  Radii of one start index
+// never grow with the stage (a parent's r is min(r of its first child, ...),
+// :2023-2024), so when stage 3 refuses, every stage does: the search tests
+// the top stage, then stage 3, then the ones between.
+__device__ __forceinline__ int bla_find(const RefDev &R, const int4 *__restrict__ T,
+                                        const Lane &s, int L, int w, int &ib, int4 &H) {
+    const int inv = R.first_invalid - w;
+    if (inv <= 8) return 0;
+    const int it = w >> FSG_STG_COMPRESSED;
+    int top = R.stages - 1;
+    if (it != 0) top = min(top, FSG_STG_COMPRESSED + __ffs(it) - 1);
+    top = min(top, 31 - __clz(inv - 1));         // largest stage with 2^stg < inv
+    if (top < FSG_STG_COMPRESSED) return 0;
+    const int i0 = 2 * it;
+    int idx = i0 + (1 << (top - FSG_STG_COMPRESSED)) - 1;
+    H = __ldg(&T[2 * idx]);
+    if (bla_ok(s, L, H)) { ib = idx; return 1 << top; }
+    if (top == FSG_STG_COMPRESSED) return 0;
+    int4 H3 = __ldg(&T[2 * i0]);
+    if (!bla_ok(s, L, H3)) return 0;
+    for (int stg = top - 1; stg > FSG_STG_COMPRESSED; stg--) {
+        idx = i0 + (1 << (stg - FSG_STG_COMPRESSED)) - 1;
+        H = __ldg(&T[2 * idx]);
+        if (bla_ok(s, L, H)) { ib = idx; return 1 << stg; }
     }
-    return 0;
+    H = H3; ib = i0;
+    return 1 << FSG_STG_COMPRESSED;
 }
 
 __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, long long ip,
@@ -140,7 +192,11 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     const long long np = (long long)T.nx * T.ny;
     const int dzndz_on = C.interior, dzndc_on = C.calc_dzndc, xrsem = C.xrsem;
     const int order = R.order, div_iter = R.div_iter, w_wrapped = R.len;
-    const float M2f = (float)C.M2;
+    // escape test on the table's 2 Z: |2 Z|^2 > 4 M^2
+    const float M2f = (float)C.M2, M2f4 = 4.f * M2f;
+    const int4 *__restrict__ Zp = R.Zp;
+    const int4 *__restrict__ dZndc_f = R.dZndc_f;
+    const int4 *__restrict__ bla_f = R.bla_f;
     // c from the pixel (perturbation.py:2214-2230) in Xrange, then fe
     double2 pp = fsg_pixel(T, ip);
     double x1 = T.lin[0] * pp.x + T.lin[1] * pp.y;
@@ -164,77 +220,76 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     for (;;) {
         // ---------------- BLA step (perturbation.py:1121-1154) -------------
         if (C.bla && (w & 7) == 0) {
-            int ib;
-            int L = mag_u(s);
-            int step = bla_lookup_fast(R, s, L, w, ib);
+            int ib; int4 H;
+            const int bu = mag_b(s);
+            const int L = (bu == 0) ? FE_ZERO_E : s.E + bu - 127;
+            const int step = bla_find(R, bla_f, s, L, w, ib, H);
             if (step != 0) {
-                int4 Av = __ldg(&R.bla_f_A[ib]), Bv = __ldg(&R.bla_f_B[ib]);
-                float Ax = __int_as_float(Av.x), Ay = __int_as_float(Av.y);
-                float Bx = __int_as_float(Bv.x), By = __int_as_float(Bv.y);
-                // dz' = A dz + B dc, on the scale of the larger term
-                int ea = (L == FE_ZERO_E) ? FE_ZERO_E : L + Av.z;
-                int eb = dc_zero ? FE_ZERO_E : Ec + Bv.z;
-                int En = max(ea, eb);
-                if (En == FE_ZERO_E) En = Ec;
-                float sa = p2f(s.E + Av.z - En), sb = p2f(Ec + Bv.z - En);
-                float bx = Bx * cmx - By * cmy, by = Bx * cmy + By * cmx;
-                float nx = (Ax * s.ux - Ay * s.uy) * sa + bx * sb;
-                float ny = (Ax * s.uy + Ay * s.ux) * sa + by * sb;
-                s.ux = nx; s.uy = ny; s.E = max(En, Ec - 100);
-                if (s.E != En) { float sc = p2f(En - s.E); s.ux *= sc; s.uy *= sc; }
+                const int4 P = __ldg(&bla_f[2 * ib + 1]);
+                const float Ax = __int_as_float(P.x), Ay = __int_as_float(P.y);
+                const float Bx = __int_as_float(P.z), By = __int_as_float(P.w);
+                // dz' = A dz + B dc on the exponent En = max(E + Ae, Ec + Be - 60,
+                // Ec - 100): A dz scaled by 2^(E + Ae - En) <= 1, B dc by
+                // 2^(Ec + Be - En) <= 2^60 (terms below 2^-127 of the scale vanish)
+                const int Ea = s.E + H.z, Eb = Ec + H.w;
+                const int En = max(max(Ea, Eb - 60), Ec - 100);
+                const float sa = __int_as_float((max(Ea - En, -127) + 127) << 23);
+                const float sb = __int_as_float((max(Eb - En, -127) + 127) << 23);
+                const float bx = (Bx * cmx - By * cmy) * sb, by = (Bx * cmy + By * cmx) * sb;
+                const float nx = fmaf(Ax * s.ux - Ay * s.uy, sa, bx);
+                const float ny = fmaf(Ax * s.uy + Ay * s.ux, sa, by);
+                s.ux = nx; s.uy = ny; s.E = En;
                 set_cu(s, cmx, cmy, Ec);
-                renorm_u(s, cmx, cmy, Ec);
+                if ((unsigned)(mag_b(s) - 97) > 60u) renorm_u(s, cmx, cmy, Ec);
                 if (dzndc_on) {
                     float vx = Ax * s.vx - Ay * s.vy, vy = Ax * s.vy + Ay * s.vx;
-                    s.vx = vx; s.vy = vy; s.F += Av.z;
+                    s.vx = vx; s.vy = vy; s.F += H.z;
                     renorm_v(s.vx, s.vy, s.F);
                 }
                 if (dzndz_on) {
                     float qx = Ax * s.qx - Ay * s.qy, qy = Ax * s.qy + Ay * s.qx;
-                    s.qx = qx; s.qy = qy; s.G += Av.z;
+                    s.qx = qx; s.qy = qy; s.G += H.z;
                     renorm_v(s.qx, s.qy, s.G);
                 }
                 n += step;
-                w = (w + step) % order;
-                Zc = __ldg(&R.Zp[w]);
+                w += step;               // step < first_invalid - w <= order - w: no wrap
+                Zc = __ldg(&Zp[w]);
                 nbla++;
                 continue;
             }
         }
         // ---------------- full step (perturbation.py:1158-1214) ------------
-        n += 1;
-        nfull++;
-        const int Ldz = mag_u(s);
-        if (!dzndz_on && Zc.z != FE_ZERO_E && Zc.z >= Ldz + 26) {
-            // fast step: |dz| < 2^-26 |Z|
-            float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
-            if (dzndc_on) {
-                float dx = 0.f, dy = 0.f; int De = 0;
-                if (!dyn) {
-                    int4 Dv = __ldg(&R.dZndc_f[w]);
-                    dx = __int_as_float(Dv.x); dy = __int_as_float(Dv.y); De = Dv.z;
-                    if (De == FE_ZERO_E) { dx = 0.f; dy = 0.f; De = 0; }
-                }
-                bool dzero = (dx == 0.f && dy == 0.f) || Ldz == FE_ZERO_E;
-                if (s.vx == 0.f && s.vy == 0.f) s.F = dzero ? 0 : De + s.E;
-                int kd = De + s.E - s.F;
-                if (!dzero && kd > 100) {          // the D dz term dominates: rescale v
-                    int Fn = De + s.E - 30;
-                    float sc = p2f(s.F - Fn);
-                    s.vx *= sc; s.vy *= sc; s.F = Fn; kd = 30;
-                }
-                float sk = dzero ? 0.f : p2f(kd);
-                float ax = dx * s.ux - dy * s.uy, ay = dx * s.uy + dy * s.ux;
-                float vx = 2.f * (Zx * s.vx - Zy * s.vy + sk * ax);
-                float vy = 2.f * (Zx * s.vy + Zy * s.vx + sk * ay);
-                s.vx = vx; s.vy = vy;
-                renorm_v(s.vx, s.vy, s.F);
+        // (u = 0 counts as 2^(E - 127): the limit FE_ZERO_E of a zero or
+        // out-of-range orbit value never passes)
+        if (!dzndz_on && Zc.z >= s.E + mag_b(s) - 127) {
+            // run of fast steps (|dz| < 2^-26 |Z| at each), up to the next
+            // event that needs the general tests: a BLA attempt (w % 8 == 0),
+            // max_iter, the reference's divergence rebase, the orbit's wrap
+            int k = order - w;
+            if (C.bla) k = min(k, 8 - (w & 7));
+            k = min(k, max(div_iter - 1 - w, 1));
+            k = max(min(k, C.max_iter - n), 1);
+            int j = 0;
+            bool esc = false;
+            for (;;) {
+                fast_step(s, Zc, Zp, dzndc_on ? dZndc_f : nullptr, w, dyn);
+                j++; w++;
+                if (j == k) break;
+                Zc = __ldg(&Zp[w]);
+                int b = mag_b(s);
+                if ((unsigned)(b - 97) > 60u) { renorm_u(s, cmx, cmy, Ec); b = mag_b(s); }
+                if (Zc.z < s.E + b - 127) break;           // next step is not fast
+                float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
+                if (Zx * Zx + Zy * Zy > M2f4) { esc = true; break; }
+                dyn = false;
             }
-            float nx = 2.f * (Zx * s.ux - Zy * s.uy) + s.cux;
-            float ny = 2.f * (Zx * s.uy + Zy * s.ux) + s.cuy;
-            s.ux = nx; s.uy = ny;
             renorm_u(s, cmx, cmy, Ec);
+            n += j; nfull += j;
+            if (esc) { stop = 1; break; }
+            if (w >= order) w = 0;
         } else {
+            n += 1;
+            nfull++;
             // exact step in fe arithmetic
             fe Zw = ld_fe(R.Zf, w);
             fe dz = as_fe(s.ux, s.uy, s.E);
@@ -252,9 +307,9 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             }
             dz = fe_norm(fe_add(fe_mul(dz, fe_add(dz, fe_scale2(Zw, 1))), dcf));
             from_fe_u(s, dz, cmx, cmy, Ec);
+            w += 1;
+            if (w >= order) w = 0;       // w < order before the increment
         }
-        w += 1;
-        if (w >= order) w = w % order;
         // ---------------- max_iter (:1218-1220) ----------------------------
         if (n >= C.max_iter) { stop = 0; break; }
         // ---------------- interior detection (:1224-1246) ------------------
@@ -263,12 +318,11 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             fe ZdZ = fe_add(as_fe(s.qx, s.qy, s.G), ld_fe(R.dZndz_f, k));
             if (fe_abs2_lt(ZdZ, C.eps2)) { stop = 2; break; }
         }
-        Zc = __ldg(&R.Zp[w]);
-        const int Ln = mag_u(s);
-        if (Zc.z != FE_ZERO_E && Zc.z >= Ln + 26 && w < div_iter - 1) {
+        Zc = __ldg(&Zp[w]);
+        if (Zc.z >= s.E + mag_b(s) - 127 && w < div_iter - 1) {
             // fast tests: |dz| < 2^-26 |Z_next|, no rebase possible
             float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
-            if (Zx * Zx + Zy * Zy > M2f) { stop = 1; break; }
+            if (Zx * Zx + Zy * Zy > M2f4) { stop = 1; break; }
             dyn = false;
             continue;
         }
@@ -294,7 +348,26 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             Zc = __ldg(&R.Zp[0]);
             continue;
         }
-        // dynamic rebase: integer pre-rejection, then the double-range test
+        // dynamic rebase.  Z_next exactly 0 (the critical point, flagged in
+        // the table): the componentwise test |dz| <= |dz| and the Xrange
+        // confirmation are true, and dz is unchanged by the rebase.
+        if (Zc.w & 1) {
+            dyn = true;
+            if (dzndc_on)
+                store_fe(s.vx, s.vy, s.F,
+                         fe_norm(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w))));
+            if (dzndz_on) {
+                if (!nullify)
+                    store_fe(s.qx, s.qy, s.G,
+                             fe_norm(fe_add(as_fe(s.qx, s.qy, s.G),
+                                            ld_fe(R.dZndz_f, (n == order) ? w_wrapped : w))));
+                nullify = true;
+            }
+            w = 0; nreb++;
+            Zc = __ldg(&R.Zp[0]);
+            continue;
+        }
+        // integer pre-rejection, then the double-range test
         dyn = false;
         if (Zn.e < dz.e + 2) {
             double2 dd = fe_to_d(dz);
@@ -348,7 +421,10 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     itsum += (unsigned long long)n;
 }
 
-__global__ void __launch_bounds__(256) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
+// 128-thread blocks, 7 per SM: 72 registers a thread without spills, 28 warps
+// an SM (the register file's limit at 72)
+#define FE32_BLOCK 128
+__global__ void __launch_bounds__(FE32_BLOCK, 7) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
@@ -361,7 +437,8 @@ __global__ void __launch_bounds__(256) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }
 
-void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
+void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int /*block*/,
                              cudaStream_t s) {
-    k_perturb_m2_fe32<<<fsg_auto_grid(k_perturb_m2_fe32, grid, block, W.total), block, 0, s>>>(W, C);
+    k_perturb_m2_fe32<<<fsg_auto_grid(k_perturb_m2_fe32, grid, FE32_BLOCK, W.total), FE32_BLOCK, 0,
+                        s>>>(W, C);
 }

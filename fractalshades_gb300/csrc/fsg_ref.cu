@@ -246,20 +246,25 @@ __global__ void k_fe_orbit(const RefDev *Rp, int4 *Zf) {
     Zf[i] = pack_fe(v);
 }
 
-// plain-float copy of the orbit for the fast steps; values below 2^-100 are
-// flagged (exponent FE_ZERO_E) so that the kernel takes its exact path there
+// plain-float copy of 2 Z for the fast steps, with the fast-step limit (the
+// exponent of max(|Z.x|, |Z.y|) minus 26); values below 2^-100 or above 2^100
+// get FE_ZERO_E so that the kernel takes its exact path there, and exact zeros
+// are flagged (w = 1)
 __global__ void k_plain_orbit(const RefDev *Rp, const int4 *Zf, int4 *Zp) {
     const RefDev &R = *Rp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i > R.len) return;
     int4 f = Zf[i];
-    if (f.z == FE_ZERO_E || f.z < -100) {
-        Zp[i] = make_int4(0, 0, FE_ZERO_E, 0);
+    if (f.z == FE_ZERO_E || f.z < -100 || f.z > 100) {
+        // flag 1: the orbit value is exactly 0 (no Xrange entry either)
+        bool zero = (f.z == FE_ZERO_E) && R.Zn[i].x == 0. && R.Zn[i].y == 0.
+                    && !(R.n_xr && i < R.len && R.xr_slot[i] >= 0);
+        Zp[i] = make_int4(0, 0, FE_ZERO_E, zero ? 1 : 0);
         return;
     }
-    float s = __int_as_float((f.z + 127) << 23);   // 2^e, e in [-100, 127]
+    float s = __int_as_float((f.z + 128) << 23);   // 2^(e + 1), e in [-100, 100]
     float x = __int_as_float(f.x) * s, y = __int_as_float(f.y) * s;
-    Zp[i] = make_int4(__float_as_int(x), __float_as_int(y), f.z, 0);
+    Zp[i] = make_int4(__float_as_int(x), __float_as_int(y), f.z - 26, 0);
 }
 
 __global__ void k_fe_path(const double2 *std_p, const double2 *xm, const int *xe, int n,
@@ -270,14 +275,15 @@ __global__ void k_fe_path(const double2 *std_p, const double2 *xm, const int *xe
     out[i] = pack_fe(v);
 }
 
-__global__ void k_fe_bla(const double2 *M, const double *r, int n, int4 *A, int4 *B) {
+__global__ void k_fe_bla(const double2 *M, const double *r, int n, int4 *F) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     fe a = fe_norm(fe_from_d(M[2 * i])), b = fe_norm(fe_from_d(M[2 * i + 1]));
     // r as (mantissa in [1, 2), exponent); r = 0 -> exponent FE_ZERO_E
     fe rf = fe_norm(fe_from_d(cx(r[i], 0.)));
-    A[i] = make_int4(__float_as_int(a.x), __float_as_int(a.y), a.e, __float_as_int(rf.x));
-    B[i] = make_int4(__float_as_int(b.x), __float_as_int(b.y), b.e, rf.e);
+    F[2 * i] = make_int4(__float_as_int(rf.x), rf.e, a.e, b.e);
+    F[2 * i + 1] = make_int4(__float_as_int(a.x), __float_as_int(a.y), __float_as_int(b.x),
+                             __float_as_int(b.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -327,10 +333,10 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
-                         int4 *bla_A, int4 *bla_B, cudaStream_t s) {
+                         int4 *bla_f, cudaStream_t s) {
     int tb = 256;
     k_fe_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (dzndc_f) k_fe_path<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dzndc, dzndc_xm, dzndc_xe, len + 1, dzndc_f);
     if (dzndz_f) k_fe_path<<<(len + 2 + tb - 1) / tb, tb, 0, s>>>(dzndz, dzndz_xm, dzndz_xe, len + 2, dzndz_f);
-    if (bla_A && bla_len > 0) k_fe_bla<<<(bla_len + tb - 1) / tb, tb, 0, s>>>(Mbla, rbla, bla_len, bla_A, bla_B);
+    if (bla_f && bla_len > 0) k_fe_bla<<<(bla_len + tb - 1) / tb, tb, 0, s>>>(Mbla, rbla, bla_len, bla_f);
 }
