@@ -30,7 +30,8 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
-                         int4 *bla_f, cudaStream_t s);
+                         int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                         cudaStream_t s);
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
@@ -486,15 +487,23 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     }
     R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.stages = stages;
     // fe tables (M2)
-    int4 *Zf = nullptr, *Zp = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_f = nullptr;
+    int4 *Zf = nullptr, *Zp = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_f = nullptr,
+         *bla_first = nullptr;
+    int *bla_first_step = nullptr;
+    const int bla_nit = (len >> 3) + 1;
     if (d->flavor == 0) {
         RA(Zf, len + 1);
         RA(Zp, len + 1);
         if (d->calc_dzndc) RA(dzndc_f, len + 1);
         if (d->calc_dzndz) RA(dzndz_f, len + 2);
-        if (R.bla_len > 0) RA(bla_f, 2 * (size_t)R.bla_len);
+        if (R.bla_len > 0) {
+            RA(bla_f, 2 * (size_t)R.bla_len);
+            RA(bla_first, 2 * (size_t)bla_nit);
+            RA(bla_first_step, (size_t)bla_nit);
+        }
     }
     R.Zf = Zf; R.Zp = Zp; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f = bla_f;
+    R.bla_first = bla_first; R.bla_first_step = bla_first_step; R.bla_nit = bla_nit;
     RCK(cudaMalloc((void **)&r->dev, sizeof(RefDev)), "cudaMalloc(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     // builds
@@ -507,7 +516,8 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
     if (d->flavor == 0) {
         fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
-                            dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_f, s);
+                            dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_f, bla_nit, bla_first,
+                            bla_first_step, s);
         fsg_build_plain_orbit(r->dev, len, Zf, Zp, s);
     }
     RCK(cudaGetLastError(), "reference table kernels");

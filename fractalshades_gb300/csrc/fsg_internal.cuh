@@ -41,6 +41,10 @@ struct RefDev {
     const int4 *bla_f;          // [2 bla_len] per entry i: [2i] = {r mantissa bits,
                                 // r exponent, A exponent, B exponent},
                                 // [2i + 1] = {A.x, A.y, B.x, B.y} float bits
+    const int4 *bla_first;      // [2 bla_nit] per start index it = w / 8, the first
+                                // stage ref_BLA_get tries there: its bla_f record
+    const int *bla_first_step;  // [bla_nit] that stage's step, 0 when none is tried
+    int bla_nit;                // (len >> 3) + 1
 };
 
 struct TileDev {

@@ -19,9 +19,9 @@
 //     form: the componentwise rebase test on the double values (with
 //     to_standard()'s underflow), then -- following the Xrange branch -- the
 //     extended |Z + dz|^2 <= |dz|^2 confirmation.
-// The BLA validity test |dz| < r compares exponents first and mantissas only
-// on near ties, which is exact with respect to the reference's comparison of
-// to_standard(dz) (it underflows to 0 only below every r > 0).
+// The BLA validity test |dz| < r is |u|^2 < r^2 2^(-2E) in FP32 with the
+// exponent gap clamped (to_standard(dz), which the reference compares, is 0
+// only below every r > 0).
 #include "fsg_internal.cuh"
 
 // 2^k as a float for k in [-126, 127]; 0 below; k > 127 is clamped (callers
@@ -36,20 +36,6 @@ __device__ __forceinline__ int fexp(float m) { return ((__float_as_int(m) >> 23)
 __device__ __forceinline__ fe ld_fe(const int4 *p, int i) {
     int4 v = __ldg(&p[i]);
     return fe_make(__int_as_float(v.x), __int_as_float(v.y), v.z);
-}
-
-// |dz| < r for dz = u 2^E with magnitude exponent L (of max(|ux|, |uy|) 2^E),
-// r given as (mantissa in [1, 2), exponent)
-__device__ __forceinline__ bool lt_r(float ux, float uy, int E, int L, float rm, int re) {
-    int k = re - L;
-    if (k >= 2) return true;
-    if (k <= -2) return false;
-    // compare u^2 2^(2E) against rm^2 2^(2 re): scale u by 2^-(L - E)
-    float s = p2f(E - L);
-    float x = ux * s, y = uy * s;
-    float r2 = rm * rm;
-    r2 = (k == 1) ? r2 * 4.f : ((k == -1) ? r2 * 0.25f : r2);
-    return x * x + y * y < r2;
 }
 
 struct Lane {
@@ -97,6 +83,7 @@ __device__ __forceinline__ int mag_u(const Lane &s) {
 __device__ __forceinline__ fe as_fe(float x, float y, int e) {
     return (x == 0.f && y == 0.f) ? fe_zero() : fe_norm(fe_make(x, y, e));
 }
+// dz from an fe value (cu is set when a fast run starts)
 __device__ __forceinline__ void from_fe_u(Lane &s, fe d, float cmx, float cmy, int Ec) {
     if (d.e == FE_ZERO_E || (d.x == 0.f && d.y == 0.f)) { s.ux = 0.f; s.uy = 0.f; s.E = Ec; }
     else {
@@ -104,7 +91,6 @@ __device__ __forceinline__ void from_fe_u(Lane &s, fe d, float cmx, float cmy, i
         float sc = p2f(d.e - s.E);
         s.ux = d.x * sc; s.uy = d.y * sc;
     }
-    set_cu(s, cmx, cmy, Ec);
 }
 __device__ __forceinline__ void store_fe(float &x, float &y, int &e, fe d) {
     if (d.e == FE_ZERO_E || (d.x == 0.f && d.y == 0.f)) { x = 0.f; y = 0.f; e = FE_ZERO_E; }
@@ -116,28 +102,26 @@ __device__ __forceinline__ int mag_b(const Lane &s) {
     return __float_as_int(fmaxf(fabsf(s.ux), fabsf(s.uy))) >> 23;
 }
 
-// One fast step at orbit index w, Zc = {2 Z_w, limit, flags}:
-//   u' = 2 Z u + cu,   v' = 2 (Z v + 2^kd D u),  kd = De + E - F
-// (D = dZndc_w, zero right after a dynamic rebase).  v = 0 is held with
-// F = FE_ZERO_E, which sends kd above 100 and rescales v onto the new term.
-__device__ __forceinline__ void fast_step(Lane &s, int4 Zc, const int4 *__restrict__ Zp,
-                                          const int4 *__restrict__ dZndc_f, int w, bool dyn) {
+// One fast step, Zc = {2 Z_w, limit, flags}, Dv = dZndc_w as {x, y, e} (e =
+// FE_ZERO_E for 0, and right after a dynamic rebase):
+//   u' = 2 Z u + cu,   v' = 2 (Z v + 2^kd D u),  kd = De + E - F.
+// v = 0 is held with F = FE_ZERO_E, which sends kd above 100 and rescales v
+// onto the new term.
+__device__ __forceinline__ void fast_step(Lane &s, int4 Zc, int4 Dv, bool dzndc_on) {
     const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);   // 2 Z
-    if (dZndc_f) {
-        int4 Dv = __ldg(&dZndc_f[w]);
-        const float dx = dyn ? 0.f : __int_as_float(Dv.x), dy = dyn ? 0.f : __int_as_float(Dv.y);
-        const int De = dyn ? FE_ZERO_E : Dv.z;
-        int kd = De + s.E - s.F;
+    if (dzndc_on) {
+        const float dx = __int_as_float(Dv.x), dy = __int_as_float(Dv.y);
+        int kd = Dv.z + s.E - s.F;
         if (kd > 100) {
-            int Fn = De + s.E - 30;
+            int Fn = Dv.z + s.E - 30;
             float sc = p2f(s.F - Fn);
             s.vx *= sc; s.vy *= sc; s.F = Fn; kd = 30;
         }
         // 2^(kd + 1), 0 below 2^-126 (kd <= 100 here)
         const float sk = __int_as_float((max(kd + 1, -127) + 127) << 23);
-        const float ax = (dx * s.ux - dy * s.uy) * sk, ay = (dx * s.uy + dy * s.ux) * sk;
-        const float vx = fmaf(Zx, s.vx, fmaf(-Zy, s.vy, ax));
-        const float vy = fmaf(Zx, s.vy, fmaf(Zy, s.vx, ay));
+        const float dxs = dx * sk, dys = dy * sk;
+        const float vx = fmaf(Zx, s.vx, fmaf(-Zy, s.vy, fmaf(dxs, s.ux, -dys * s.uy)));
+        const float vy = fmaf(Zx, s.vy, fmaf(Zy, s.vx, fmaf(dxs, s.uy, dys * s.ux)));
         s.vx = vx; s.vy = vy;
         renorm_v(s.vx, s.vy, s.F);
     }
@@ -147,42 +131,59 @@ __device__ __forceinline__ void fast_step(Lane &s, int4 Zc, const int4 *__restri
 }
 
 // |dz| < r for the BLA entry whose header is H = {r mantissa bits, r exponent,
-// A exponent, B exponent}; L = magnitude exponent of dz (FE_ZERO_E for 0:
-// valid iff r > 0, the reference's 0 < r)
-__device__ __forceinline__ bool bla_ok(const Lane &s, int L, int4 H) {
-    return (L == FE_ZERO_E) ? (H.y != FE_ZERO_E)
-                            : lt_r(s.ux, s.uy, s.E, L, __int_as_float(H.x), H.y);
+// A exponent, B exponent}, as |u|^2 < rm^2 2^(2 (re - E)).  u is normalised
+// (|u| in [2^-30, 2^31) or 0), so exponent gaps beyond +-126 are decided by
+// the clamp alone; r = 0 (rm = 0) admits nothing, dz = 0 any r > 0 -- the
+// reference's strict 0 < r.
+__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H) {
+    const int d = min(max(2 * (H.y - s.E), -126), 126);
+    const float rm = __int_as_float(H.x);
+    return fmaf(s.ux, s.ux, s.uy * s.uy) < (rm * rm) * __int_as_float((d + 127) << 23);
 }
 
 // ref_BLA_get (perturbation.py:2116-2170): the largest stage from
 // 3 + ctz(w >> 3) (capped at stages - 1) down to 3 whose step is below
-// first_invalid - w and whose radius admits dz.  Radii of one start index
-// never grow with the stage (a parent's r is min(r of its first child, ...),
-// :2023-2024), so when stage 3 refuses, every stage does: the search tests
-// the top stage, then stage 3, then the ones between.
-__device__ __forceinline__ int bla_find(const RefDev &R, const int4 *__restrict__ T,
-                                        const Lane &s, int L, int w, int &ib, int4 &H) {
-    const int inv = R.first_invalid - w;
-    if (inv <= 8) return 0;
+// first_invalid - w and whose radius admits dz.  The first candidate of each
+// start index (header, payload and step) is tabulated when the reference is
+// built.  Radii of one start index never grow with the stage (a parent's r is
+// min(r of its first child, ...), :2023-2024), so when stage 3 refuses, every
+// stage does: after the first candidate the search tests stage 3, then the
+// stages between.
+__device__ __forceinline__ int bla_find(const int4 *__restrict__ T, const int4 *__restrict__ FF,
+                                        const int *__restrict__ FS, const Lane &s, int w,
+                                        int4 &H, int4 &P) {
     const int it = w >> FSG_STG_COMPRESSED;
-    int top = R.stages - 1;
-    if (it != 0) top = min(top, FSG_STG_COMPRESSED + __ffs(it) - 1);
-    top = min(top, 31 - __clz(inv - 1));         // largest stage with 2^stg < inv
-    if (top < FSG_STG_COMPRESSED) return 0;
+    const int st = __ldg(&FS[it]);
+    H = __ldg(&FF[2 * it]);
+    P = __ldg(&FF[2 * it + 1]);
+    if (st == 0) return 0;
+    if (bla_ok(s, H)) return st;
+    if (st == 8) return 0;
     const int i0 = 2 * it;
-    int idx = i0 + (1 << (top - FSG_STG_COMPRESSED)) - 1;
-    H = __ldg(&T[2 * idx]);
-    if (bla_ok(s, L, H)) { ib = idx; return 1 << top; }
-    if (top == FSG_STG_COMPRESSED) return 0;
-    int4 H3 = __ldg(&T[2 * i0]);
-    if (!bla_ok(s, L, H3)) return 0;
-    for (int stg = top - 1; stg > FSG_STG_COMPRESSED; stg--) {
-        idx = i0 + (1 << (stg - FSG_STG_COMPRESSED)) - 1;
+    const int4 H3 = __ldg(&T[2 * i0]);
+    if (!bla_ok(s, H3)) return 0;
+    for (int stg = 30 - __clz(st); stg > FSG_STG_COMPRESSED; stg--) {
+        const int idx = i0 + (1 << (stg - FSG_STG_COMPRESSED)) - 1;
         H = __ldg(&T[2 * idx]);
-        if (bla_ok(s, L, H)) { ib = idx; return 1 << stg; }
+        if (bla_ok(s, H)) { P = __ldg(&T[2 * idx + 1]); return 1 << stg; }
     }
-    H = H3; ib = i0;
+    H = H3; P = __ldg(&T[2 * i0 + 1]);
     return 1 << FSG_STG_COMPRESSED;
+}
+
+// rebase bookkeeping shared by the three rebase kinds: dzndc += dZndc_w,
+// dzndz += dZndz_w (wrapped slot at n = order) unless nullified
+__device__ __forceinline__ void rebase_derivs(Lane &s, const RefDev &R, int w, int n, int order,
+                                              bool dzndc_on, bool dzndz_on, bool &nullify) {
+    if (dzndc_on)
+        store_fe(s.vx, s.vy, s.F, fe_norm(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w))));
+    if (dzndz_on) {
+        if (!nullify)
+            store_fe(s.qx, s.qy, s.G,
+                     fe_norm(fe_add(as_fe(s.qx, s.qy, s.G),
+                                    ld_fe(R.dZndz_f, (n == order) ? R.len : w))));
+        nullify = true;
+    }
 }
 
 __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, long long ip,
@@ -190,13 +191,17 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
                                            unsigned long long &nreb, unsigned long long &itsum) {
     const RefDev &R = *T.ref;
     const long long np = (long long)T.nx * T.ny;
-    const int dzndz_on = C.interior, dzndc_on = C.calc_dzndc, xrsem = C.xrsem;
-    const int order = R.order, div_iter = R.div_iter, w_wrapped = R.len;
+    const bool dzndz_on = C.interior, dzndc_on = C.calc_dzndc;
+    const int xrsem = C.xrsem, max_iter = C.max_iter;
+    const int order = R.order, div_iter = R.div_iter, first_invalid = R.first_invalid;
+    const bool bla_on = C.bla && R.bla_first != nullptr;
     // escape test on the table's 2 Z: |2 Z|^2 > 4 M^2
     const float M2f = (float)C.M2, M2f4 = 4.f * M2f;
     const int4 *__restrict__ Zp = R.Zp;
     const int4 *__restrict__ dZndc_f = R.dZndc_f;
     const int4 *__restrict__ bla_f = R.bla_f;
+    const int4 *__restrict__ bla_first = R.bla_first;
+    const int *__restrict__ bla_first_step = R.bla_first_step;
     // c from the pixel (perturbation.py:2214-2230) in Xrange, then fe
     double2 pp = fsg_pixel(T, ip);
     double x1 = T.lin[0] * pp.x + T.lin[1] * pp.y;
@@ -212,20 +217,19 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     s.ux = 0.f; s.uy = 0.f; s.E = Ec;
     s.vx = 0.f; s.vy = 0.f; s.F = FE_ZERO_E;
     s.qx = 0.f; s.qy = 0.f; s.G = FE_ZERO_E;
-    set_cu(s, cmx, cmy, Ec);
+    s.cux = cmx; s.cuy = cmy;
     int w = 0, n = 0; signed char stop = -1;
     bool nullify = false, dyn = true;
-    int4 Zc = __ldg(&R.Zp[0]);
+    int4 Zc = __ldg(&Zp[0]);
 
     for (;;) {
         // ---------------- BLA step (perturbation.py:1121-1154) -------------
-        if (C.bla && (w & 7) == 0) {
-            int ib; int4 H;
-            const int bu = mag_b(s);
-            const int L = (bu == 0) ? FE_ZERO_E : s.E + bu - 127;
-            const int step = bla_find(R, bla_f, s, L, w, ib, H);
+        // (w < first_invalid here: w = 0, or the tests that let the loop
+        // continue saw w < div_iter - 1, or a BLA jump stopped short of it)
+        if (bla_on && (w & 7) == 0 && w < first_invalid) {
+            int4 H, P;
+            const int step = bla_find(bla_f, bla_first, bla_first_step, s, w, H, P);
             if (step != 0) {
-                const int4 P = __ldg(&bla_f[2 * ib + 1]);
                 const float Ax = __int_as_float(P.x), Ay = __int_as_float(P.y);
                 const float Bx = __int_as_float(P.z), By = __int_as_float(P.w);
                 // dz' = A dz + B dc on the exponent En = max(E + Ae, Ec + Be - 60,
@@ -239,7 +243,6 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
                 const float nx = fmaf(Ax * s.ux - Ay * s.uy, sa, bx);
                 const float ny = fmaf(Ax * s.uy + Ay * s.ux, sa, by);
                 s.ux = nx; s.uy = ny; s.E = En;
-                set_cu(s, cmx, cmy, Ec);
                 if ((unsigned)(mag_b(s) - 97) > 60u) renorm_u(s, cmx, cmy, Ec);
                 if (dzndc_on) {
                     float vx = Ax * s.vx - Ay * s.vy, vy = Ax * s.vy + Ay * s.vx;
@@ -266,20 +269,27 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             // event that needs the general tests: a BLA attempt (w % 8 == 0),
             // max_iter, the reference's divergence rebase, the orbit's wrap
             int k = order - w;
-            if (C.bla) k = min(k, 8 - (w & 7));
+            if (bla_on) k = min(k, 8 - (w & 7));
             k = min(k, max(div_iter - 1 - w, 1));
-            k = max(min(k, C.max_iter - n), 1);
+            k = max(min(k, max_iter - n), 1);
+            set_cu(s, cmx, cmy, Ec);
+            int4 Dv = make_int4(0, 0, FE_ZERO_E, 0);
+            if (dzndc_on && !dyn) Dv = __ldg(&dZndc_f[w]);
             int j = 0;
             bool esc = false;
             for (;;) {
-                fast_step(s, Zc, Zp, dzndc_on ? dZndc_f : nullptr, w, dyn);
+                // next entries (w + 1 <= order <= len, inside both tables)
+                const int4 Zn = __ldg(&Zp[w + 1]);
+                int4 Dn = Dv;
+                if (dzndc_on) Dn = __ldg(&dZndc_f[w + 1]);
+                fast_step(s, Zc, Dv, dzndc_on);
                 j++; w++;
                 if (j == k) break;
-                Zc = __ldg(&Zp[w]);
+                Zc = Zn; Dv = Dn;
                 int b = mag_b(s);
                 if ((unsigned)(b - 97) > 60u) { renorm_u(s, cmx, cmy, Ec); b = mag_b(s); }
                 if (Zc.z < s.E + b - 127) break;           // next step is not fast
-                float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
+                const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
                 if (Zx * Zx + Zy * Zy > M2f4) { esc = true; break; }
                 dyn = false;
             }
@@ -290,41 +300,66 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
         } else {
             n += 1;
             nfull++;
-            // exact step in fe arithmetic
-            fe Zw = ld_fe(R.Zf, w);
             fe dz = as_fe(s.ux, s.uy, s.E);
-            if (dzndc_on) {
-                fe D = dyn ? fe_zero() : ld_fe(R.dZndc_f, w);
-                fe d = as_fe(s.vx, s.vy, s.F);
-                store_fe(s.vx, s.vy, s.F,
-                         fe_norm(fe_scale2(fe_add(fe_mul(fe_add(Zw, dz), d), fe_mul(D, dz)), 1)));
+            if ((Zc.w & 1) && !dzndz_on) {
+                // Z_w = 0: dz' = dz^2 + dc, dzndc' = 2 dz (dzndc + D)
+                if (dzndc_on) {
+                    fe t = as_fe(s.vx, s.vy, s.F);
+                    if (!dyn) t = fe_add(t, ld_fe(dZndc_f, w));
+                    store_fe(s.vx, s.vy, s.F, fe_norm(fe_scale2(fe_mul(dz, t), 1)));
+                }
+                dz = fe_norm(fe_add(fe_mul(dz, dz), dcf));
+            } else {
+                // exact step in fe arithmetic
+                fe Zw = ld_fe(R.Zf, w);
+                if (dzndc_on) {
+                    fe D = dyn ? fe_zero() : ld_fe(dZndc_f, w);
+                    fe d = as_fe(s.vx, s.vy, s.F);
+                    store_fe(s.vx, s.vy, s.F,
+                             fe_norm(fe_scale2(fe_add(fe_mul(fe_add(Zw, dz), d), fe_mul(D, dz)), 1)));
+                }
+                if (dzndz_on) {
+                    fe D = ld_fe(R.dZndz_f, nullify ? 0 : w);
+                    fe q = as_fe(s.qx, s.qy, s.G);
+                    store_fe(s.qx, s.qy, s.G,
+                             fe_norm(fe_scale2(fe_add(fe_mul(fe_add(Zw, dz), q), fe_mul(D, dz)), 1)));
+                }
+                dz = fe_norm(fe_add(fe_mul(dz, fe_add(dz, fe_scale2(Zw, 1))), dcf));
             }
-            if (dzndz_on) {
-                fe D = ld_fe(R.dZndz_f, nullify ? 0 : w);
-                fe q = as_fe(s.qx, s.qy, s.G);
-                store_fe(s.qx, s.qy, s.G,
-                         fe_norm(fe_scale2(fe_add(fe_mul(fe_add(Zw, dz), q), fe_mul(D, dz)), 1)));
-            }
-            dz = fe_norm(fe_add(fe_mul(dz, fe_add(dz, fe_scale2(Zw, 1))), dcf));
             from_fe_u(s, dz, cmx, cmy, Ec);
             w += 1;
             if (w >= order) w = 0;       // w < order before the increment
         }
         // ---------------- max_iter (:1218-1220) ----------------------------
-        if (n >= C.max_iter) { stop = 0; break; }
+        if (n >= max_iter) { stop = 0; break; }
         // ---------------- interior detection (:1224-1246) ------------------
         if (dzndz_on) {
-            int k = nullify ? 0 : ((n == order) ? w_wrapped : w);
+            int k = nullify ? 0 : ((n == order) ? R.len : w);
             fe ZdZ = fe_add(as_fe(s.qx, s.qy, s.G), ld_fe(R.dZndz_f, k));
             if (fe_abs2_lt(ZdZ, C.eps2)) { stop = 2; break; }
         }
         Zc = __ldg(&Zp[w]);
-        if (Zc.z >= s.E + mag_b(s) - 127 && w < div_iter - 1) {
-            // fast tests: |dz| < 2^-26 |Z_next|, no rebase possible
-            float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
-            if (Zx * Zx + Zy * Zy > M2f4) { stop = 1; break; }
-            dyn = false;
-            continue;
+        if (w < div_iter - 1) {
+            if (Zc.z >= s.E + mag_b(s) - 127) {
+                // fast tests: |dz| < 2^-26 |Z_next|, no rebase possible
+                const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
+                if (Zx * Zx + Zy * Zy > M2f4) { stop = 1; break; }
+                dyn = false;
+                continue;
+            }
+            if (Zc.w & 1) {
+                // Z_w exactly 0 (the critical point, flagged in the table):
+                // ZZ = dz escapes iff |dz|^2 > M^2; otherwise the
+                // componentwise test |dz| <= |dz| and the Xrange confirmation
+                // hold, and the dynamic rebase leaves dz unchanged
+                const float2 df = fe_to_f(as_fe(s.ux, s.uy, s.E));
+                if (df.x * df.x + df.y * df.y > M2f) { stop = 1; break; }
+                dyn = true;
+                rebase_derivs(s, R, w, n, order, dzndc_on, dzndz_on, nullify);
+                w = 0; nreb++;
+                Zc = __ldg(&Zp[0]);
+                continue;
+            }
         }
         // ---------------- exact tests ---------------------------------------
         fe Zn = ld_fe(R.Zf, w);
@@ -334,40 +369,12 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
         if (XX * XX + YY * YY > M2f) { stop = 1; break; }
         if (w >= div_iter - 1) {        // rebase when the reference diverges
             from_fe_u(s, fe_norm(fe_add(Zn, dz)), cmx, cmy, Ec);
-            if (dzndc_on)
-                store_fe(s.vx, s.vy, s.F,
-                         fe_norm(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w))));
-            if (dzndz_on) {
-                if (!nullify)
-                    store_fe(s.qx, s.qy, s.G,
-                             fe_norm(fe_add(as_fe(s.qx, s.qy, s.G),
-                                            ld_fe(R.dZndz_f, (n == order) ? w_wrapped : w))));
-                nullify = true;
-            }
+            rebase_derivs(s, R, w, n, order, dzndc_on, dzndz_on, nullify);
             w = 0; nreb++;
-            Zc = __ldg(&R.Zp[0]);
+            Zc = __ldg(&Zp[0]);
             continue;
         }
-        // dynamic rebase.  Z_next exactly 0 (the critical point, flagged in
-        // the table): the componentwise test |dz| <= |dz| and the Xrange
-        // confirmation are true, and dz is unchanged by the rebase.
-        if (Zc.w & 1) {
-            dyn = true;
-            if (dzndc_on)
-                store_fe(s.vx, s.vy, s.F,
-                         fe_norm(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w))));
-            if (dzndz_on) {
-                if (!nullify)
-                    store_fe(s.qx, s.qy, s.G,
-                             fe_norm(fe_add(as_fe(s.qx, s.qy, s.G),
-                                            ld_fe(R.dZndz_f, (n == order) ? w_wrapped : w))));
-                nullify = true;
-            }
-            w = 0; nreb++;
-            Zc = __ldg(&R.Zp[0]);
-            continue;
-        }
-        // integer pre-rejection, then the double-range test
+        // dynamic rebase: integer pre-rejection, then the double-range test
         dyn = false;
         if (Zn.e < dz.e + 2) {
             double2 dd = fe_to_d(dz);
@@ -388,18 +395,9 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
                 }
                 if (ok) {
                     from_fe_u(s, fe_norm(ZZ), cmx, cmy, Ec);
-                    if (dzndc_on)
-                        store_fe(s.vx, s.vy, s.F,
-                                 fe_norm(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w))));
-                    if (dzndz_on) {
-                        if (!nullify)
-                            store_fe(s.qx, s.qy, s.G,
-                                     fe_norm(fe_add(as_fe(s.qx, s.qy, s.G),
-                                                    ld_fe(R.dZndz_f, (n == order) ? w_wrapped : w))));
-                        nullify = true;
-                    }
+                    rebase_derivs(s, R, w, n, order, dzndc_on, dzndz_on, nullify);
                     w = 0; nreb++;
-                    Zc = __ldg(&R.Zp[0]);
+                    Zc = __ldg(&Zp[0]);
                     continue;
                 }
             }

@@ -286,6 +286,30 @@ __global__ void k_fe_bla(const double2 *M, const double *r, int n, int4 *F) {
                              __float_as_int(b.y));
 }
 
+// the first stage ref_BLA_get (perturbation.py:2116-2170) tries at each start
+// index it = w / 8: 3 + ctz(it) capped at stages - 1 (stages - 1 for it = 0),
+// lowered to the largest stage whose step is below first_invalid - w; its
+// bla_f record is copied beside it so that the kernel's first test needs one
+// load
+__global__ void k_fe_bla_first(const RefDev *Rp, const int4 *F, int nit, int4 *FF, int *FS) {
+    const RefDev &R = *Rp;
+    int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nit) return;
+    const int inv = R.first_invalid - (it << 3);
+    int4 h = make_int4(0, FE_ZERO_E, 0, 0), p = make_int4(0, 0, 0, 0);
+    int step = 0;
+    if (inv > 8 && R.stages - 1 >= 3) {
+        int top = R.stages - 1;
+        if (it != 0) top = min(top, 3 + __ffs(it) - 1);
+        top = min(top, 31 - __clz(inv - 1));
+        if (top >= 3) {
+            const int idx = 2 * it + (1 << (top - 3)) - 1;
+            if (idx < R.bla_len) { h = F[2 * idx]; p = F[2 * idx + 1]; step = 1 << top; }
+        }
+    }
+    FF[2 * it] = h; FF[2 * it + 1] = p; FS[it] = step;
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the C-ABI layer)
 // ---------------------------------------------------------------------------
@@ -333,10 +357,15 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
-                         int4 *bla_f, cudaStream_t s) {
+                         int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                         cudaStream_t s) {
     int tb = 256;
     k_fe_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (dzndc_f) k_fe_path<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dzndc, dzndc_xm, dzndc_xe, len + 1, dzndc_f);
     if (dzndz_f) k_fe_path<<<(len + 2 + tb - 1) / tb, tb, 0, s>>>(dzndz, dzndz_xm, dzndz_xe, len + 2, dzndz_f);
-    if (bla_f && bla_len > 0) k_fe_bla<<<(bla_len + tb - 1) / tb, tb, 0, s>>>(Mbla, rbla, bla_len, bla_f);
+    if (bla_f && bla_len > 0) {
+        k_fe_bla<<<(bla_len + tb - 1) / tb, tb, 0, s>>>(Mbla, rbla, bla_len, bla_f);
+        k_fe_bla_first<<<(bla_nit + tb - 1) / tb, tb, 0, s>>>(Rd, bla_f, bla_nit, bla_first,
+                                                              bla_first_step);
+    }
 }
