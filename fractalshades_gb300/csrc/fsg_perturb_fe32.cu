@@ -102,32 +102,40 @@ __device__ __forceinline__ int mag_b(const Lane &s) {
     return __float_as_int(fmaxf(fabsf(s.ux), fabsf(s.uy))) >> 23;
 }
 
-// One fast step, Zc = {2 Z_w, limit, flags}, Dv = dZndc_w as {x, y, e} (e =
-// FE_ZERO_E for 0, and right after a dynamic rebase):
-//   u' = 2 Z u + cu,   v' = 2 (Z v + 2^kd D u),  kd = De + E - F.
-// v = 0 is held with F = FE_ZERO_E, which sends kd above 100 and rescales v
-// onto the new term.
-__device__ __forceinline__ void fast_step(Lane &s, int4 Zc, int4 Dv, bool dzndc_on) {
-    const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);   // 2 Z
-    if (dzndc_on) {
-        const float dx = __int_as_float(Dv.x), dy = __int_as_float(Dv.y);
-        int kd = Dv.z + s.E - s.F;
-        if (kd > 100) {
-            int Fn = Dv.z + s.E - 30;
-            float sc = p2f(s.F - Fn);
-            s.vx *= sc; s.vy *= sc; s.F = Fn; kd = 30;
-        }
-        // 2^(kd + 1), 0 below 2^-126 (kd <= 100 here)
-        const float sk = __int_as_float((max(kd + 1, -127) + 127) << 23);
-        const float dxs = dx * sk, dys = dy * sk;
-        const float vx = fmaf(Zx, s.vx, fmaf(-Zy, s.vy, fmaf(dxs, s.ux, -dys * s.uy)));
-        const float vy = fmaf(Zx, s.vy, fmaf(Zy, s.vx, fmaf(dxs, s.uy, dys * s.ux)));
-        s.vx = vx; s.vy = vy;
-        renorm_v(s.vx, s.vy, s.F);
+// Fast update of a derivative delta d = x 2^e against the reference
+// derivative Dv = {x, y, e} (e = FE_ZERO_E for 0, and for dzndc right after
+// a dynamic rebase), 2 Z = (Zx, Zy):
+//   d' = 2 (Z d + D dz)  as  x' = 2Z x + 2^(kd+1) D u,  kd = De + E - e
+// (the dz d term is below FP32 resolution when |dz| < 2^-26 |Z|).  d = 0 is
+// held with e = FE_ZERO_E, which sends kd above 100 and rescales d onto the
+// new term.
+__device__ __forceinline__ void deriv_fast(float &x, float &y, int &e, int4 Dv, float Zx, float Zy,
+                                           const Lane &s) {
+    const float dx = __int_as_float(Dv.x), dy = __int_as_float(Dv.y);
+    int kd = Dv.z + s.E - e;
+    if (kd > 100) {
+        int en = Dv.z + s.E - 30;
+        float sc = p2f(e - en);
+        x *= sc; y *= sc; e = en; kd = 30;
     }
-    const float nx = fmaf(Zx, s.ux, fmaf(-Zy, s.uy, s.cux));
-    const float ny = fmaf(Zx, s.uy, fmaf(Zy, s.ux, s.cuy));
-    s.ux = nx; s.uy = ny;
+    // 2^(kd + 1), 0 below 2^-126 (kd <= 100 here)
+    const float sk = __int_as_float((max(kd + 1, -127) + 127) << 23);
+    const float dxs = dx * sk, dys = dy * sk;
+    const float nx = fmaf(Zx, x, fmaf(-Zy, y, fmaf(dxs, s.ux, -dys * s.uy)));
+    const float ny = fmaf(Zx, y, fmaf(Zy, x, fmaf(dxs, s.uy, dys * s.ux)));
+    x = nx; y = ny;
+    renorm_v(x, y, e);
+}
+
+// |q 2^G + Q|^2 < eps^2 (eps2 a normal float): both terms aligned on the
+// larger exponent e, then compared against eps^2 2^(-2e) with the gap clamped
+__device__ __forceinline__ bool stationary_fast(float qx, float qy, int G, int4 Q, float eps2) {
+    const int e = max(G, Q.z);
+    const float a = __int_as_float((max(G - e, -127) + 127) << 23);
+    const float b = __int_as_float((max(Q.z - e, -127) + 127) << 23);
+    const float x = fmaf(qx, a, __int_as_float(Q.x) * b), y = fmaf(qy, a, __int_as_float(Q.y) * b);
+    const int d = min(max(-2 * e, -126), 126);
+    return fmaf(x, x, y * y) < eps2 * __int_as_float((d + 127) << 23);
 }
 
 // |dz| < r for the BLA entry whose header is H = {r mantissa bits, r exponent,
@@ -186,12 +194,16 @@ __device__ __forceinline__ void rebase_derivs(Lane &s, const RefDev &R, int w, i
     }
 }
 
+template <bool INTERIOR>
 __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, long long ip,
                                            unsigned long long &nfull, unsigned long long &nbla,
                                            unsigned long long &nreb, unsigned long long &itsum) {
     const RefDev &R = *T.ref;
     const long long np = (long long)T.nx * T.ny;
-    const bool dzndz_on = C.interior, dzndc_on = C.calc_dzndc;
+    const bool dzndz_on = INTERIOR, dzndc_on = C.calc_dzndc;
+    // the fast interior test needs eps^2 as a normal float
+    const float eps2f = (float)C.eps2;
+    const bool eps_fast = C.eps2 >= 1e-30 && C.eps2 <= 1e30;
     const int xrsem = C.xrsem, max_iter = C.max_iter;
     const int order = R.order, div_iter = R.div_iter, first_invalid = R.first_invalid;
     const bool bla_on = C.bla && R.bla_first != nullptr;
@@ -199,6 +211,7 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     const float M2f = (float)C.M2, M2f4 = 4.f * M2f;
     const int4 *__restrict__ Zp = R.Zp;
     const int4 *__restrict__ dZndc_f = R.dZndc_f;
+    const int4 *__restrict__ dZndz_f = R.dZndz_f;
     const int4 *__restrict__ bla_f = R.bla_f;
     const int4 *__restrict__ bla_first = R.bla_first;
     const int *__restrict__ bla_first_step = R.bla_first_step;
@@ -264,7 +277,7 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
         // ---------------- full step (perturbation.py:1158-1214) ------------
         // (u = 0 counts as 2^(E - 127): the limit FE_ZERO_E of a zero or
         // out-of-range orbit value never passes)
-        if (!dzndz_on && Zc.z >= s.E + mag_b(s) - 127) {
+        if (Zc.z >= s.E + mag_b(s) - 127) {
             // run of fast steps (|dz| < 2^-26 |Z| at each), up to the next
             // event that needs the general tests: a BLA attempt (w % 8 == 0),
             // max_iter, the reference's divergence rebase, the orbit's wrap
@@ -275,26 +288,49 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             set_cu(s, cmx, cmy, Ec);
             int4 Dv = make_int4(0, 0, FE_ZERO_E, 0);
             if (dzndc_on && !dyn) Dv = __ldg(&dZndc_f[w]);
+            // dzndz: the reference derivative is dZndz_0 once nullified, else
+            // dZndz_w (n = order, the wrapped slot, is a wrap: an event)
+            int4 Q0 = Dv, Qv = Dv;
+            if (INTERIOR) {
+                Q0 = __ldg(&dZndz_f[0]);
+                Qv = nullify ? Q0 : __ldg(&dZndz_f[w]);
+            }
             int j = 0;
-            bool esc = false;
+            bool esc = false, stat = false;
             for (;;) {
-                // next entries (w + 1 <= order <= len, inside both tables)
+                // next entries (w + 1 <= order <= len, inside the tables)
                 const int4 Zn = __ldg(&Zp[w + 1]);
-                int4 Dn = Dv;
+                int4 Dn = Dv, Qn = Qv;
                 if (dzndc_on) Dn = __ldg(&dZndc_f[w + 1]);
-                fast_step(s, Zc, Dv, dzndc_on);
+                if (INTERIOR) Qn = nullify ? Q0 : __ldg(&dZndz_f[w + 1]);
+                const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);   // 2 Z
+                if (dzndc_on) deriv_fast(s.vx, s.vy, s.F, Dv, Zx, Zy, s);
+                if (INTERIOR) deriv_fast(s.qx, s.qy, s.G, Qv, Zx, Zy, s);
+                const float nx = fmaf(Zx, s.ux, fmaf(-Zy, s.uy, s.cux));
+                const float ny = fmaf(Zx, s.uy, fmaf(Zy, s.ux, s.cuy));
+                s.ux = nx; s.uy = ny;
                 j++; w++;
                 if (j == k) break;
-                Zc = Zn; Dv = Dn;
+                Zc = Zn; Dv = Dn; Qv = Qn;
+                if (INTERIOR) {
+                    // (:1224-1246) against the next reference derivative
+                    bool st = eps_fast ? stationary_fast(s.qx, s.qy, s.G, Qn, eps2f)
+                                       : fe_abs2_lt(fe_add(as_fe(s.qx, s.qy, s.G),
+                                                           fe_make(__int_as_float(Qn.x),
+                                                                   __int_as_float(Qn.y), Qn.z)),
+                                                    C.eps2);
+                    if (st) { stat = true; break; }
+                }
                 int b = mag_b(s);
                 if ((unsigned)(b - 97) > 60u) { renorm_u(s, cmx, cmy, Ec); b = mag_b(s); }
                 if (Zc.z < s.E + b - 127) break;           // next step is not fast
-                const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);
-                if (Zx * Zx + Zy * Zy > M2f4) { esc = true; break; }
+                const float Zx2 = __int_as_float(Zc.x), Zy2 = __int_as_float(Zc.y);
+                if (Zx2 * Zx2 + Zy2 * Zy2 > M2f4) { esc = true; break; }
                 dyn = false;
             }
             renorm_u(s, cmx, cmy, Ec);
             n += j; nfull += j;
+            if (stat) { stop = 2; break; }
             if (esc) { stop = 1; break; }
             if (w >= order) w = 0;
         } else {
@@ -420,9 +456,11 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
 }
 
 // 128-thread blocks, 7 per SM: 72 registers a thread without spills, 28 warps
-// an SM (the register file's limit at 72)
+// an SM (the register file's limit at 72); with interior detection 6 per SM
+// (80 registers)
 #define FE32_BLOCK 128
-__global__ void __launch_bounds__(FE32_BLOCK, 7) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
+template <bool INTERIOR>
+__global__ void __launch_bounds__(FE32_BLOCK, INTERIOR ? 6 : 7) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
@@ -430,13 +468,17 @@ __global__ void __launch_bounds__(FE32_BLOCK, 7) k_perturb_m2_fe32(WorkDev W, Ca
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
-        pixel_fe32(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        pixel_fe32<INTERIOR>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
     }
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }
 
 void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int /*block*/,
                              cudaStream_t s) {
-    k_perturb_m2_fe32<<<fsg_auto_grid(k_perturb_m2_fe32, grid, FE32_BLOCK, W.total), FE32_BLOCK, 0,
-                        s>>>(W, C);
+    if (C.interior)
+        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, FE32_BLOCK, W.total),
+                                  FE32_BLOCK, 0, s>>>(W, C);
+    else
+        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, FE32_BLOCK, W.total),
+                                   FE32_BLOCK, 0, s>>>(W, C);
 }

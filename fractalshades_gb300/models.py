@@ -188,8 +188,12 @@ class Perturbation_mandelbrot(PerturbationFractal):
 
     @staticmethod
     def _nucleus_size_estimate(c0, order):
-        return fsFP.perturbation_mandelbrot_nucleus_size_estimate(
-            str(c0.real).encode("utf8"), str(c0.imag).encode("utf8"), mpmath.mp.prec, order)
+        """(nucleus_size, julia_size) of the period-``order`` component at c0,
+        julia_size = nucleus_size ** 0.75 (mandelbrot_M2.py:717-760)."""
+        nucleus_size = abs(fsFP.perturbation_mandelbrot_nucleus_size_estimate(
+            str(c0.real).encode("utf8"), str(c0.imag).encode("utf8"), mpmath.mp.prec, order))
+        sqrt = mpmath.sqrt(nucleus_size)
+        return nucleus_size, mpmath.sqrt(sqrt) * sqrt
 
 
 # ---------------------------------------------------------------------------
@@ -327,16 +331,38 @@ class Perturbation_burning_ship(PerturbationFractal):
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 
-    @staticmethod
-    def _ball_method(c, px, maxiter, M_divergence):
-        # the BS ball method (FP_loop.pyx:2357-2563) is not restated: the
-        # reference falls back to the image centre when it fails
-        return None
+    # Newton search & related (burning_ship.py:1168-1290)
+    def _ball_method(self, c, px, maxiter, M_divergence):
+        """Order-1 ball method on the 2 x 2 Jacobian (FP_loop.pyx:2357-2440)."""
+        order = fsFP.perturbation_nonholomorphic_ball_method(
+            str(c.real).encode("utf8"), str(c.imag).encode("utf8"), mpmath.mp.prec,
+            str(px).encode("utf8"), maxiter, M_divergence, kind=self.flavor_int)
+        return None if order == -1 else order
 
     @staticmethod
     def find_nucleus(c, order, eps_pixel, max_newton=None, eps_cv=None):
-        raise NotImplementedError
+        raise NotImplementedError("Divide by undesired roots technique "
+                                  "not implemented for burning ship")
 
-    @staticmethod
-    def find_any_nucleus(c, order, eps_pixel, max_newton=None, eps_cv=None):
-        return False, c
+    def find_any_nucleus(self, c, order, eps_pixel, max_newton=None, eps_cv=None):
+        """Newton search for f^order(0) = 0, divisor periods accepted
+        (FP_loop.pyx:2564-2720)."""
+        if order is None:
+            raise ValueError("order shall be defined for Newton method")
+        seed_prec = mpmath.mp.prec
+        if max_newton is None:
+            max_newton = 80
+        if eps_cv is None:
+            eps_cv = mpmath.mpf(val=(2, -seed_prec))
+        return fsFP.perturbation_nonholomorphic_find_any_nucleus(
+            str(c.real).encode("utf8"), str(c.imag).encode("utf8"), seed_prec, order,
+            max_newton, str(eps_cv).encode("utf8"), str(eps_pixel).encode("utf8"),
+            kind=self.flavor_int)
+
+    def _nucleus_size_estimate(self, c0, order):
+        """(nucleus_size, julia_size, skew) (FP_loop.pyx:1982-2100)."""
+        nucleus_size, skew = fsFP.perturbation_nonholomorphic_nucleus_size_estimate(
+            str(c0.real).encode("utf8"), str(c0.imag).encode("utf8"), mpmath.mp.prec, order,
+            kind=self.flavor_int)
+        sqrt = mpmath.sqrt(nucleus_size)
+        return nucleus_size, mpmath.sqrt(sqrt) * sqrt, skew

@@ -347,3 +347,212 @@ def _bs_loop_double(orb, max_iter, M, a, b, kind):
     if i == max_iter and abs_i <= M:
         i += 1
     return i, {}, {}
+
+
+# ---------------------------------------------------------------------------
+# Burning Ship family: ball method, Newton search and size estimate
+# (FP_loop.pyx:1343-1827 iterations, Jacobians, matsolve; 1982-2100 size
+# estimate; 2357-2440 ball method; 2564-2720 Newton).  The same arithmetic
+# serves fixed-point integers (mul = product >> F) and mpmath numbers.
+# ---------------------------------------------------------------------------
+def _sgn(v):
+    """sign() of FP_loop.pyx:1778-1784: +1 for v >= 0, else -1"""
+    return 1 if v >= 0 else -1
+
+
+def _bs_iter(kind, x, y, a, b, mul):
+    """One iteration of flavor ``kind`` (FP_loop.pyx:1358-1455):
+    1 BS       x' = x^2 - y^2 + a,     y' = 2 |x y| - b
+    2 pBS      x' = x^2 - y^2 + a,     y' = 2 x |y| - b
+    3 shark    x' = x^2 - y |y| + a,   y' = 2 x y - b
+    4 celtic   x' = |x^2 - y^2| + a,   y' = 2 x y - b
+    5 buffalo  x' = |x^2 - y^2| + a,   y' = 2 |x y| - b"""
+    x2, y2 = mul(x, x), mul(y, y)
+    if kind == 1:
+        xy = mul(x, y)
+        return x2 - y2 + a, 2 * abs(xy) - b
+    if kind == 2:
+        return x2 - y2 + a, 2 * mul(x, abs(y)) - b
+    if kind == 3:
+        return x2 - mul(abs(y), y) + a, 2 * mul(x, y) - b
+    if kind == 4:
+        return abs(x2 - y2) + a, 2 * mul(x, y) - b
+    if kind == 5:
+        return abs(x2 - y2) + a, 2 * abs(mul(x, y)) - b
+    raise NotImplementedError(kind)
+
+
+def _bs_jac(kind, x, y, J, mul, one, var_c):
+    """Jacobian recurrence of flavor ``kind`` at the point (x, y)
+    (FP_loop.pyx:1458-1743).  J = (dxdu, dxdv, dydu, dydv); with var_c the
+    derivatives are taken w.r.t. c = a + i b and pick up +1 on dxda and -1 on
+    dydb (the -b of the y update)."""
+    jxx, jxy, jyx, jyy = J
+    if kind in (1, 2, 5):
+        sy = _sgn(y)
+        ay = abs(y)
+        if kind == 2:
+            cx_, cy_ = x * sy, ay              # dyn/d. = 2 (x sgn(y) dy + |y| dx)
+        else:
+            cx_, cy_ = abs(x) * sy, ay * _sgn(x)
+    if kind in (4, 5):
+        s = _sgn(mul(x, x) - mul(y, y))
+    else:
+        s = 1
+    if kind == 3:
+        ay = abs(y)
+        txx, txy = mul(x, jxx) - mul(ay, jyx), mul(x, jxy) - mul(ay, jyy)
+        tyx, tyy = mul(x, jyx) + mul(y, jxx), mul(x, jyy) + mul(y, jxy)
+    elif kind == 4:
+        txx, txy = s * (mul(x, jxx) - mul(y, jyx)), s * (mul(x, jxy) - mul(y, jyy))
+        tyx, tyy = mul(x, jyx) + mul(y, jxx), mul(x, jyy) + mul(y, jxy)
+    else:
+        txx, txy = s * (mul(x, jxx) - mul(y, jyx)), s * (mul(x, jxy) - mul(y, jyy))
+        tyx = mul(cx_, jyx) + mul(cy_, jxx)
+        tyy = mul(cx_, jyy) + mul(cy_, jxy)
+    J = [2 * txx, 2 * txy, 2 * tyx, 2 * tyy]
+    if var_c:
+        J[0] += one
+        J[3] -= one
+    return tuple(J)
+
+
+def _bs_escaped(x, y, F):
+    return x.bit_length() > F + 64 or y.bit_length() > F + 64
+
+
+def perturbation_nonholomorphic_ball_method(seed_x, seed_y, seed_prec, seed_px, maxiter,
+                                            M_divergence, kind=1):
+    """First i for which the ball of radius px around c maps onto a ball that
+    contains 0 to first order: (rx, ry) = J^-1 (x_i, y_i) / px with |rx| < 1,
+    |ry| < 1 and hypot(rx, ry) < 1, J the Jacobian w.r.t. c
+    (FP_loop.pyx:2357-2440).  -1 if the orbit escapes M_divergence or no
+    such i <= maxiter exists."""
+    F = int(seed_prec) + GUARD_BITS
+    a, b = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    px = _fix(_dec(seed_px), F)
+    one = 1 << F
+
+    def mul(u, v):
+        return (u * v) >> F
+
+    x = y = 0
+    J = (0, 0, 0, 0)
+    for i in range(1, int(maxiter) + 1):
+        J = _bs_jac(kind, x, y, J, mul, one, True)
+        x, y = _bs_iter(kind, x, y, a, b, mul)
+        if math.hypot(_to_float(x, F), _to_float(y, F)) > M_divergence:
+            return -1
+        jxx, jxy, jyx, jyy = J
+        det = jxx * jyy - jyx * jxy                   # scale 2^(2F)
+        if det == 0:
+            continue                                  # MPFR: inf / nan, no cycle
+        nx = jyy * x - jxy * y                        # (J^-1 X) * det, scale 2^(2F)
+        ny = jxx * y - jyx * x
+        lim = abs(det) * px                           # scale 2^(3F)
+        if abs(nx) << F < lim and abs(ny) << F < lim:
+            if (nx * nx + ny * ny) << (2 * F) < lim * lim:
+                return i
+    return -1
+
+
+def _bs_newton_step_float(a, b, order, kind, prec):
+    """One Newton step in mpmath at ``prec`` bits, for an orbit that escapes
+    (where fixed point would overflow): returns (da, db, x_order, y_order)."""
+    with mpmath.workprec(prec):
+        one = mpmath.mpf(1)
+        x = y = mpmath.mpf(0)
+        J = (x, x, x, x)
+        for _ in range(int(order)):
+            J = _bs_jac(kind, x, y, J, lambda u, v: u * v, one, True)
+            x, y = _bs_iter(kind, x, y, a, b, lambda u, v: u * v)
+        jxx, jxy, jyx, jyy = J
+        det = jxx * jyy - jyx * jxy
+        return (jyy * x - jxy * y) / det, (jxx * y - jyx * x) / det, x, y
+
+
+def perturbation_nonholomorphic_find_any_nucleus(seed_x, seed_y, seed_prec, order, max_newton,
+                                                 seed_eps_cv, seed_eps_valid, kind=1):
+    """Newton search for c with f_c^order(0) = 0 on the 2 x 2 Jacobian,
+    divisor periods accepted (FP_loop.pyx:2564-2720).  Converged when the
+    step is below 64 eps_cv; valid when |(x, y)_order| <= eps_valid.
+    Returns (newton_cv, c) with c an mpmath mpc (nan when not converged)."""
+    F = int(seed_prec) + GUARD_BITS
+    a, b = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    eps_cv = mpmath.mpf(_dec(seed_eps_cv)) * 64
+    eps_valid = mpmath.mpf(_dec(seed_eps_valid))
+    one = 1 << F
+
+    def mul(u, v):
+        return (u * v) >> F
+
+    newton_cv = False
+    for _ in range(int(max_newton)):
+        x = y = 0
+        J = (0, 0, 0, 0)
+        escaped = False
+        for _i in range(int(order)):
+            J = _bs_jac(kind, x, y, J, mul, one, True)
+            x, y = _bs_iter(kind, x, y, a, b, mul)
+            if _bs_escaped(x, y, F):
+                escaped = True
+                break
+        if escaped:
+            da, db, xo, yo = _bs_newton_step_float(_to_mpf(a, F), _to_mpf(b, F), order, kind, F)
+            sa, sb = _fix(da, F), _fix(db, F)
+            a, b = a - sa, b - sb
+            continue
+        jxx, jxy, jyx, jyy = J
+        det = (jxx * jyy - jyx * jxy) >> F
+        if det == 0:
+            break
+        sa = (jyy * x - jxy * y) // det                # scale 2^F
+        sb = (jxx * y - jyx * x) // det
+        a, b = a - sa, b - sb
+        step = mpmath.sqrt(_to_mpf(sa, F) ** 2 + _to_mpf(sb, F) ** 2)
+        if step <= eps_cv:
+            az = mpmath.sqrt(_to_mpf(x, F) ** 2 + _to_mpf(y, F) ** 2)
+            newton_cv = az <= eps_valid
+            break
+    if newton_cv:
+        with mpmath.workprec(int(seed_prec)):
+            return True, mpmath.mpc(_to_mpf(a, F), _to_mpf(b, F))
+    return False, mpmath.mpc("nan", "nan")
+
+
+def perturbation_nonholomorphic_nucleus_size_estimate(seed_x, seed_y, seed_prec, order, kind=1):
+    """Size estimate of the period-``order`` component at c and its skew
+    matrix (FP_loop.pyx:1982-2100): with L_i the Jacobian of z_i w.r.t. z_1
+    (taken after each iteration) and beta = I + sum_i L_i^-1,
+    size = |det(L)^2 det(beta)|^(-1/2) and skew = beta / sqrt(det beta),
+    returned as [[b_yy, b_xy], [b_yx, b_xx]]."""
+    with mpmath.workprec(int(seed_prec)):
+        a, b = mpmath.mpf(_dec(seed_x)), mpmath.mpf(_dec(seed_y))
+        one, zero = mpmath.mpf(1), mpmath.mpf(0)
+
+        def mul(u, v):
+            return u * v
+
+        x = y = zero
+        J = (one, zero, zero, one)
+        bxx, bxy, byx, byy = one, zero, zero, one
+        for _ in range(1, int(order)):
+            x, y = _bs_iter(kind, x, y, a, b, mul)
+            J = _bs_jac(kind, x, y, J, mul, one, False)
+            jxx, jxy, jyx, jyy = J
+            inv = 1 / (jxx * jyy - jyx * jxy)
+            bxx += inv * jyy
+            bxy -= inv * jxy
+            byx -= inv * jyx
+            byy += inv * jxx
+        jxx, jxy, jyx, jyy = J
+        d = (jxx * jyy - jyx * jxy) ** 2
+        det_b = bxx * byy - byx * bxy
+        size = 1 / mpmath.sqrt(abs(det_b * d))
+        if det_b > 0:
+            s = 1 / mpmath.sqrt(det_b)
+            skew = np.array(((float(byy * s), float(bxy * s)),
+                             (float(byx * s), float(bxx * s))), dtype=np.float64)
+        else:
+            skew = np.full((2, 2), np.nan)
+        return size, skew

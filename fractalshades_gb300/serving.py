@@ -67,7 +67,7 @@ class Request:
 
 
 def make_center(p, dps, max_iter):
-    c = syn.find_nucleus(p, dps)
+    c = syn.nucleus(p, dps)
     w = syn.prepare_m2(p=p, dps=dps, dx="1e-10", nx=2, max_iter=max_iter, center=c)
     return Center(c=c, p=p, dps=dps, Zn=w.Zn, xr_idx=w.xr_idx, xr_m=w.xr_m, xr_e=w.xr_e)
 

@@ -13,6 +13,8 @@ divisor periods); the ball method confirms the period.
 orbit with its Xrange side table, kc, and the pixel axes of the image.
 """
 import dataclasses
+import json
+import os
 
 import mpmath
 import numpy as np
@@ -46,6 +48,27 @@ def find_nucleus(p, dps):
         if order != p:
             raise RuntimeError(f"ball method found period {order}, expected {p}")
         return c
+
+
+NUCLEI_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "nuclei.json")
+_nuclei = None
+
+
+def nucleus(p, dps):
+    """``find_nucleus(p, dps)``, read from data/nuclei.json when that file
+    holds it (written by data/make_nuclei.py with the same search)."""
+    global _nuclei
+    if _nuclei is None:
+        try:
+            with open(NUCLEI_FILE) as f:
+                _nuclei = json.load(f)
+        except (OSError, ValueError):
+            _nuclei = {}
+    rec = _nuclei.get(f"{p}:{dps}")
+    if rec is None:
+        return find_nucleus(p, dps)
+    with mpmath.workdps(dps):
+        return mpmath.mpc(mpmath.mpf(rec[0]), mpmath.mpf(rec[1]))
 
 
 @dataclasses.dataclass
@@ -98,7 +121,7 @@ def prepare_m2(*, p, dps, dx, nx, ny=None, max_iter, M=1000., center=None, offse
     dx).  The reference point is the nucleus; the orbit wraps at p."""
     ny = ny or nx
     with mpmath.workdps(dps):
-        c = center if center is not None else find_nucleus(p, dps)
+        c = center if center is not None else nucleus(p, dps)
         dxm = mpmath.mpf(dx)
         view = c + mpmath.mpc(offset[0], offset[1]) * dxm
         prec = mpmath.mp.prec
@@ -136,3 +159,111 @@ def config2_workload(seed=2, nx=2048, max_iter=200000):
     rng = np.random.default_rng(seed)
     p = int(rng.integers(300, 3001))
     return prepare_m2(p=p, dps=400, dx="1e-300", nx=nx, max_iter=max_iter, M=1000.)
+
+
+# ---------------------------------------------------------------------------
+# the other measured configurations
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class StdWorkload:
+    nx: int
+    ny: int
+    center: complex
+    dx: float
+    max_iter: int
+    M: float
+    eps: float
+    xs: np.ndarray
+    ys: np.ndarray
+
+
+def config1_workload():
+    """Standard power-2 Mandelbrot: 800 x 600 (xy_ratio 4/3) centred on
+    -0.5, width 3, max_iter 1000, escape radius 1e3, stationarity eps 0.01."""
+    nx, ny = 800, 600
+    xs, ys = image_axes(nx, ny, nx / ny)
+    return StdWorkload(nx=nx, ny=ny, center=-0.5 + 0j, dx=3.0, max_iter=1000, M=1000.,
+                       eps=0.01, xs=xs, ys=ys)
+
+
+def config3_workload(seed=3, nx=4096, max_iter=1000000):
+    """4096 x 4096 at dx = 1e-1000 on a period-p nucleus, p ~ U[2000, 20000],
+    1100 digits, max_iter 1e6, interior detection (eps 1e-3)."""
+    rng = np.random.default_rng(seed)
+    p = int(rng.integers(2000, 20001))
+    return prepare_m2(p=p, dps=1100, dx="1e-1000", nx=nx, max_iter=max_iter, M=1000.)
+
+
+@dataclasses.dataclass
+class BSTile:
+    side: int
+    dx: object              # mpmath mpf
+    seed_point: tuple       # (x0, y0) floats drawn
+    order: object           # period found by the ball method + Newton, or None
+    Zn: np.ndarray          # complex128 (x + i y) [len]
+    div_iter: int
+    ref_order: int
+    dx_m: float
+    dx_e: int
+    driftx_m: float
+    driftx_e: int
+    drifty_m: float
+    drifty_e: int
+    kc: float
+    xs: np.ndarray
+    ys: np.ndarray
+
+
+def bs_center(rng, dps, kind=1, radius="1e-3", tries=64, max_iter=50000):
+    """A Burning Ship view centre: seeded points x ~ U[-1.8, -1.7],
+    y ~ U[-0.1, 0], the first whose order-1 ball of ``radius`` finds a period
+    (FP_loop.pyx:2357-2440), refined by Newton (FP_loop.pyx:2564-2720); the
+    last raw point when no draw finds one (the reference's fallback,
+    perturbation.py:747-751)."""
+    with mpmath.workdps(dps):
+        prec = mpmath.mp.prec
+        for _ in range(tries):
+            x0, y0 = -1.8 + 0.1 * rng.random(), -0.1 * rng.random()
+            order = fsFP.perturbation_nonholomorphic_ball_method(
+                repr(x0), repr(y0), prec, radius, max_iter, 1e5, kind)
+            if order <= 0:
+                continue
+            ok, c = fsFP.perturbation_nonholomorphic_find_any_nucleus(
+                repr(x0), repr(y0), prec, order, 80, str(mpmath.mpf(val=(2, -prec))),
+                str(mpmath.mpf(10) ** (-(dps // 2))), kind)
+            if ok:
+                return (x0, y0), c, order
+        return (x0, y0), mpmath.mpc(x0, y0), None
+
+
+def config4_workload(seed=4, n_tiles=64, max_iter=50000, M=1000., kind=1, dps=250):
+    """64 Burning Ship tiles, side round(exp(U[ln 256, ln 2048])), width
+    10^U[-200, -30], each on its own centre (``bs_center``) with its own
+    250-digit reference orbit; max_iter 5e4, escape radius 1e3."""
+    rng = np.random.default_rng(seed)
+    tiles = []
+    for _ in range(n_tiles):
+        side = int(round(np.exp(rng.uniform(np.log(256), np.log(2048)))))
+        width_exp = rng.uniform(-200, -30)
+        seed_pt, c, order = bs_center(rng, dps, kind)
+        with mpmath.workdps(dps):
+            dxm = mpmath.mpf(10) ** mpmath.mpf(width_exp)
+            prec = mpmath.mp.prec
+            ref_len = min(order, max_iter + 1) if order else max_iter + 1
+            orb = np.empty(max_iter + 1 if not order else ref_len, dtype=np.complex128)
+            i, _, _ = fsFP.perturbation_nonholomorphic_FP_loop(
+                orb.view(np.float64), False, orb.size - 1, 2 * M, str(c.real), str(c.imag),
+                prec, kind)
+            div_iter = max_iter + 1 if order else i
+            Zn = orb[:ref_len] if order else orb[:min(i + 1, orb.size)]
+            dx_xr = fsx.mpf_to_Xrange(dxm)
+            half = mpmath.mpf(0.5) * dxm
+            kc = mpmath.sqrt(2) * half * mpmath.mpf(1.1)
+            kc_xr = fsx.mpf_to_Xrange(kc)
+        xs, ys = image_axes(side, side)
+        tiles.append(BSTile(
+            side=side, dx=dxm, seed_point=seed_pt, order=order, Zn=np.ascontiguousarray(Zn),
+            div_iter=int(div_iter), ref_order=int(order) if order else (1 << 62),
+            dx_m=dx_xr.m, dx_e=dx_xr.e, driftx_m=0., driftx_e=0, drifty_m=0., drifty_e=0,
+            kc=kc_xr.to_standard(), xs=xs, ys=ys))
+    return tiles

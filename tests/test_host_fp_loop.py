@@ -90,3 +90,66 @@ def test_newton_4252_reference_digits():
     assert ok
     with mpmath.workprec(precision - 10):
         assert mpmath.almosteq(mpmath.mpf(str(d["x_nucleus"])), val.real)
+
+
+BS_KATS = [("-1.7545128115395", "0.0015894811966473", "0.01"),
+           ("0.88410156557344", "1.5218981991448", "0.012")]
+
+
+@pytest.mark.parametrize("x, y, px", BS_KATS)
+def test_bs_ball_method_order_3(x, y, px):
+    """tests/test_FP_loop.py:311-341 of the reference: period 3 at both seeds
+    (53 bits, px 0.01, maxiter 100, M 1000)."""
+    order = fsFP.perturbation_nonholomorphic_ball_method(
+        x.encode(), y.encode(), 53, b"0.01", 100, 1000., 1)
+    assert order == 3
+
+
+def _bs_orbit(c, n, kind=1):
+    x = y = mpmath.mpf(0)
+    for _ in range(n):
+        x, y = fsFP._bs_iter(kind, x, y, c.real, c.imag, lambda u, v: u * v)
+    return x, y
+
+
+@pytest.mark.parametrize("x, y, px", BS_KATS)
+def test_bs_newton_period_3(x, y, px):
+    """tests/test_FP_loop.py:343-382: Newton from the same seeds converges
+    (53 bits, 40 steps); the point found is periodic, z_3 = 0."""
+    eps_cv = mpmath.mpf(val=(2, -53))
+    ok, c = fsFP.perturbation_nonholomorphic_find_any_nucleus(
+        x.encode(), y.encode(), 53, 3, 40, str(eps_cv).encode(), px.encode(), 1)
+    assert ok
+    with mpmath.workprec(200):
+        zx, zy = _bs_orbit(c, 3)
+        assert abs(zx) < 1e-12 and abs(zy) < 1e-12
+    size, skew = fsFP.perturbation_nonholomorphic_nucleus_size_estimate(
+        str(c.real).encode(), str(c.imag).encode(), 53, 3, 1)
+    assert 1e-3 < float(size) < 1.
+    assert np.all(np.isfinite(skew))
+
+
+@pytest.mark.parametrize("kind", [1, 2, 3, 4, 5])
+def test_bs_newton_deep_every_flavor(kind):
+    """At 300 bits the Newton search converges to a point whose period-p
+    orbit returns to 0 to the working precision, for every flavor (p from the
+    ball method around a seeded point)."""
+    rng = np.random.default_rng(kind)
+    with mpmath.workprec(300):
+        found = False
+        for _ in range(40):
+            c0 = mpmath.mpc(-2 + 2.5 * rng.random(), -1.5 + 2 * rng.random())
+            order = fsFP.perturbation_nonholomorphic_ball_method(
+                str(c0.real).encode(), str(c0.imag).encode(), 300, b"0.05", 200, 1e5, kind)
+            if order < 2 or order > 60:
+                continue
+            ok, c = fsFP.perturbation_nonholomorphic_find_any_nucleus(
+                str(c0.real).encode(), str(c0.imag).encode(), 300, order, 80,
+                str(mpmath.mpf(val=(2, -300))).encode(), b"1e-60", kind)
+            if not ok:
+                continue
+            zx, zy = _bs_orbit(c, order, kind)
+            assert abs(zx) < 1e-60 and abs(zy) < 1e-60
+            found = True
+            break
+        assert found
