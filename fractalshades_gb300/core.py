@@ -9,12 +9,21 @@ point -- which here launches the GPU kernel instead of a numba loop.
 
 Where the reference runs one numba call per 200 x 200 tile on a thread pool
 (mthreading.py:48-68), ``calc_raw`` launches all tiles of the image in one
-persistent GPU launch and keeps the raw arrays in memory.
+persistent GPU launch.  The raw arrays are then written to the reference's
+on-disk layout (core.py:2125-2510): ``data/<calc>_{Z,U,stop_reason,
+stop_iter}.arr`` npy-format memory maps in chunk-compressed order, the
+``data/<calc>.report`` chunk table and the ``data/<calc>.fingerprint``
+pickle, so that stored results are found again (and only missing tiles
+recomputed) exactly as the reference does.
 """
 import copy
 import inspect
 import logging
+import os
+import pickle
 import types
+
+from numpy.lib.format import open_memmap
 
 import numpy as np
 
@@ -151,6 +160,15 @@ class Fractal:
         return (ix, min(ix + cs, self.nx), iy, min(iy + cs, self.ny))
 
     def pts_count(self, calc_name=None, chunk_slice=None):
+        """Compressed 1-d points of the calculation (of one chunk, or all):
+        the subset's true entries when there is a subset (core.py:1743-1765)."""
+        subset = None
+        if calc_name is not None and calc_name in getattr(self, "_calc_data", {}):
+            subset = self._calc_data[calc_name]["state"].subset
+        if subset is not None:
+            if chunk_slice is None:
+                return int(sum(np.count_nonzero(subset[cs]) for cs in self.chunk_slices()))
+            return int(np.count_nonzero(subset[chunk_slice]))
         if chunk_slice is None:
             return self.nx * self.ny
         ix, ixx, iy, iyy = chunk_slice
@@ -255,6 +273,21 @@ class Fractal:
         }
         state.fingerprint = {k: self._calc_data[calc_name][k] for k in (
             "calc_class", "calc_callable", "calc_kwargs", "zoom_kwargs", "init_kwargs")}
+        # stored results: reuse them when the fingerprint matches and every
+        # file is there, else start a new set (core.py:1976-2009)
+        if self.res_available(calc_name):
+            try:
+                self.get_report_memmap(calc_name, mode="r+")
+                for key in self.SAVE_ARRS:
+                    self.get_data_memmap(calc_name, key, mode="r+")
+                if state.subset is not None:
+                    self.get_data_memmap(calc_name, "subset", mode="r+")
+                self._calc_data[calc_name]["need_new_mmap"] = False
+            except FileNotFoundError:
+                self._calc_data[calc_name]["need_new_mmap"] = True
+        else:
+            self._calc_data[calc_name]["need_new_mmap"] = True
+            self.save_fingerprint(calc_name, state.fingerprint)
 
     @staticmethod
     def saved_codes(codes):
@@ -326,29 +359,88 @@ class Fractal:
     # whole image
     # ------------------------------------------------------------------
     def calc_raw(self, calc_name, tile_validator=None):
-        """Compute every tile of the image in one GPU launch; the raw arrays
-        are kept in memory, in image layout (ny, nx) per field."""
+        """Compute the image and store its raw arrays (core.py:2724-2737).
+
+        Without a subset every tile of the image is computed in one GPU launch
+        (kept in memory in image layout (ny, nx) for ``get_raw``) and written
+        to the memory maps; with a subset, or when stored results exist, only
+        the tiles whose report entry is not done are computed, one launch per
+        tile as the reference's compute_rawdata_dev (core.py:2518-2554)."""
         if self.is_interrupted():
             return None
-        cia = self._calc_data[calc_name]["cycle_indep_args"]
-        state = self._calc_data[calc_name]["state"]
-        if state.subset is not None:
-            raise NotImplementedError("calc_raw with a subset: use compute_tile")
-        xs, ys = self.image_axes()
-        res = gpu.run_image(self, xs, ys, cia)
-        if res is None:
-            return None
-        self._calc_data[calc_name]["raw"] = res
-        return res
+        data = self._calc_data[calc_name]
+        if data["need_new_mmap"]:
+            self.init_report_mmap(calc_name)
+            self.init_data_mmaps(calc_name)
+            data["need_new_mmap"] = False
+        state = data["state"]
+        todo = [cs for cs in self.chunk_slices()
+                if (tile_validator is None or tile_validator(cs))
+                and not self.res_available(calc_name, cs)]
+        if not todo:
+            return data.get("raw")
+        if state.subset is None and len(todo) == self.chunks_count:
+            xs, ys = self.image_axes()
+            res = gpu.run_image(self, xs, ys, data["cycle_indep_args"])
+            if res is None:
+                return None
+            data["raw"] = res
+            self._store_image(calc_name, res)
+            return res
+        for cs in todo:
+            out = self.compute_tile(calc_name, cs)
+            if out is None:
+                return None
+            (_c_pix, Z, U, stop_reason, stop_iter), _subset = out
+            self.update_report_mmap(calc_name, cs, stop_reason)
+            self.update_data_mmaps(calc_name, cs, Z, U, stop_reason, stop_iter)
+        data["raw"] = None
+        return None
+
+    def _store_image(self, calc_name, res):
+        """Whole-image raw arrays (image layout) -> per-chunk compressed
+        memory maps, every chunk marked done."""
+        ny, nx = self.ny, self.nx
+        Z = res["Z"].reshape(res["Z"].shape[0], ny, nx)
+        U = res["U"].reshape(res["U"].shape[0], ny, nx)
+        sr = res["stop_reason"].reshape(1, ny, nx)
+        si = res["stop_iter"].reshape(1, ny, nx)
+        for cs in self.chunk_slices():
+            ix, ixx, iy, iyy = cs
+            sl = (slice(None), slice(iy, iyy), slice(ix, ixx))
+            m = (ixx - ix) * (iyy - iy)
+            self.update_data_mmaps(calc_name, cs, Z[sl].reshape(-1, m), U[sl].reshape(-1, m),
+                                   sr[sl].reshape(1, m), si[sl].reshape(1, m))
+            self.update_report_mmap(calc_name, cs, None)
 
     def get_raw(self, calc_name, key):
-        """A raw field of the last calc_raw, in image layout (ny, nx):
-        a complex code (e.g. "zn"), an int code, "stop_reason" or "stop_iter"."""
-        raw = self._calc_data[calc_name]["raw"]
-        if raw is None:
-            raise RuntimeError(f"calc_raw has not been run for {calc_name}")
+        """A raw field in image layout (ny, nx): a complex code (e.g. "zn"),
+        an int code, "stop_reason" or "stop_iter" -- from the last calc_raw,
+        else reassembled from the stored memory maps ("potential" and "dem"
+        exist only after a calc_raw of this session)."""
+        raw = self._calc_data[calc_name].get("raw")
         complex_codes, int_codes, _ = self.codes
         ny, nx = self.ny, self.nx
+        if raw is None:
+            if key in ("potential", "dem"):
+                raise RuntimeError(f"calc_raw has not been run for {calc_name}")
+            if self._calc_data[calc_name]["state"].subset is not None:
+                raise NotImplementedError("image layout of a subset calculation")
+            if key in complex_codes:
+                arr_key, row = "Z", self._calc_data[calc_name]["saved_codes"][0].index(key)
+            elif key in int_codes:
+                arr_key, row = "U", self._calc_data[calc_name]["saved_codes"][1].index(key)
+            elif key in ("stop_reason", "stop_iter"):
+                arr_key, row = key, 0
+            else:
+                raise KeyError(key)
+            mmap = self.get_data_memmap(calc_name, arr_key, mode="r")
+            img = np.empty((ny, nx), dtype=mmap.dtype)
+            for rank, cs in enumerate(self.chunk_slices()):
+                ix, ixx, iy, iyy = cs
+                beg, end = self.compressed_beg_end(calc_name, self.chunk_rank(cs))
+                img[iy:iyy, ix:ixx] = np.asarray(mmap[row, beg:end]).reshape(iyy - iy, ixx - ix)
+            return img
         if key in complex_codes:
             return raw["Z"][complex_codes.index(key)].reshape(ny, nx)
         if key in int_codes:
@@ -356,6 +448,188 @@ class Fractal:
         if key in ("stop_reason", "stop_iter", "potential", "dem"):
             return raw[key].reshape(ny, nx)
         raise KeyError(key)
+
+    # ------------------------------------------------------------------
+    # raw-array storage (core.py:2125-2510)
+    # ------------------------------------------------------------------
+    def fingerprint_path(self, calc_name):
+        return os.path.join(self.directory, "data", calc_name + ".fingerprint")
+
+    def save_fingerprint(self, calc_name, fingerprint):
+        path = self.fingerprint_path(calc_name)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "wb+") as f:
+            pickle.dump(fingerprint, f, pickle.HIGHEST_PROTOCOL)
+
+    def reload_fingerprint(self, calc_name):
+        with open(self.fingerprint_path(calc_name), "rb") as f:
+            return pickle.load(f)
+
+    def fingerprint_matching(self, calc_name, test_fingerprint, log=False):
+        """Every flattened key of the current fingerprint equals the stored
+        one (core.py:1851-1881)."""
+        flat = utils.dic_flatten(test_fingerprint)
+        expected = utils.dic_flatten(self._calc_data[calc_name]["state"].fingerprint)
+        for key, val in expected.items():
+            if key not in flat:
+                return False
+            try:
+                same = flat[key] == val
+                if isinstance(same, np.ndarray):
+                    same = bool(same.all()) and np.shape(flat[key]) == np.shape(val)
+            except Exception:      # noqa: BLE001 -- incomparable values differ
+                same = False
+            if not same:
+                if log:
+                    logger.debug(f"Parameter mismatch: {key}, {flat[key]} --> {val}")
+                return False
+        return True
+
+    def res_available(self, calc_name, chunk_slice=None):
+        """Fingerprint match (chunk_slice None), or the chunk's report entry
+        is done (core.py:1883-1915)."""
+        try:
+            fingerprint = self.reload_fingerprint(calc_name)
+        except (IOError, EOFError, pickle.UnpicklingError):
+            return False
+        if not self.fingerprint_matching(calc_name, fingerprint, chunk_slice is None):
+            return False
+        if chunk_slice is None:
+            return True
+        try:
+            report = self.reload_report(calc_name, chunk_slice)
+        except (IOError, ValueError):
+            return False
+        return report["done"] > 0
+
+    def report_path(self, calc_name):
+        return os.path.join(self.directory, "data", calc_name + ".report")
+
+    def init_report_mmap(self, calc_name):
+        """int32 [chunks_count, (chunk1d_begin, chunk1d_end, chunk_pts, done)]
+        (core.py:2173-2209)."""
+        items = self.REPORT_ITEMS
+        path = self.report_path(calc_name)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        mmap = open_memmap(filename=path, mode="w+", dtype=np.dtype(np.int32),
+                           shape=(self.chunks_count, len(items)), fortran_order=False,
+                           version=None)
+        mmap[:, items.index("done")] = 0
+        pts = np.array([self.pts_count(calc_name, cs) for cs in self.chunk_slices()],
+                       dtype=np.int32)
+        cum = np.zeros(self.chunks_count + 1, dtype=np.int32)
+        np.cumsum(pts, out=cum[1:])
+        mmap[:, items.index("chunk_pts")] = pts
+        mmap[:, items.index("chunk1d_begin")] = cum[:-1]
+        mmap[:, items.index("chunk1d_end")] = cum[1:]
+        mmap.flush()
+        del mmap
+
+    def get_report_memmap(self, calc_name, mode="r+"):
+        return open_memmap(filename=self.report_path(calc_name), mode=mode)
+
+    def update_report_mmap(self, calc_name, chunk_slice, stop_reason):
+        mmap = self.get_report_memmap(calc_name, mode="r+")
+        mmap[self.chunk_rank(chunk_slice), self.REPORT_ITEMS.index("done")] = 1
+        mmap.flush()
+        del mmap
+
+    def reload_report(self, calc_name, chunk_slice):
+        """The chunk's report entry as a dict, or (items, full report) when
+        chunk_slice is None (core.py:2253-2271)."""
+        mmap = self.get_report_memmap(calc_name, mode="r")
+        items = self.REPORT_ITEMS
+        if chunk_slice is None:
+            return items, np.array(mmap)
+        rank = self.chunk_rank(chunk_slice)
+        return dict(zip(items, (int(mmap[rank, items.index(it)]) for it in items)))
+
+    def compressed_beg_end(self, calc_name, rank):
+        mmap = self.get_report_memmap(calc_name, mode="r")
+        items = self.REPORT_ITEMS
+        return (int(mmap[rank, items.index("chunk1d_begin")]),
+                int(mmap[rank, items.index("chunk1d_end")]))
+
+    def uncompressed_beg_end(self, rank):
+        """Span of the chunk in the (full-size) subset mask, chunks in rank
+        order (core.py:1700-1727)."""
+        arr = np.zeros(self.chunks_count + 1, dtype=np.int64)
+        for i, (ix, ixx, iy, iyy) in enumerate(self.chunk_slices()):
+            arr[i + 1] = arr[i] + (ixx - ix) * (iyy - iy)
+        return int(arr[rank]), int(arr[rank + 1])
+
+    def data_path(self, calc_name):
+        keys = ["subset"] + self.SAVE_ARRS
+        return {k: os.path.join(self.directory, "data", f"{calc_name}_{k}.arr") for k in keys}
+
+    def init_data_mmaps(self, calc_name):
+        """Z [n_Z, pts], U [n_U, pts], stop_reason / stop_iter [1, pts] with
+        the stored codes only, and the subset mask (core.py:2362-2430)."""
+        state = self._calc_data[calc_name]["state"]
+        f_complex, f_int, _stop = self._calc_data[calc_name]["saved_codes"]
+        pts = self.pts_count(calc_name)
+        dtypes = {"Z": self.complex_type, "U": self.int_type,
+                  "stop_reason": self.termination_type, "stop_iter": self.int_type}
+        dims = {"Z": (len(f_complex), pts), "U": (len(f_int), pts),
+                "stop_reason": (1, pts), "stop_iter": (1, pts)}
+        paths = self.data_path(calc_name)
+        os.makedirs(os.path.dirname(paths["Z"]), exist_ok=True)
+        for key in self.SAVE_ARRS:
+            mmap = open_memmap(filename=paths[key], mode="w+", dtype=np.dtype(dtypes[key]),
+                               shape=dims[key], fortran_order=False, version=None)
+            del mmap
+        if state.subset is not None:
+            mmap = open_memmap(filename=paths["subset"], mode="w+", dtype=bool,
+                               shape=(self.ny * self.nx,), fortran_order=False, version=None)
+            for rank, cs in enumerate(self.chunk_slices()):
+                beg, end = self.uncompressed_beg_end(rank)
+                mmap[beg:end] = np.ravel(state.subset[cs])
+            del mmap
+
+    def get_data_memmap(self, calc_name, key, mode="r+"):
+        return open_memmap(filename=self.data_path(calc_name)[key], mode=mode)
+
+    def update_data_mmaps(self, calc_name, chunk_slice, Z, U, stop_reason, stop_iter):
+        """The chunk's columns [beg, end) of each stored array; codes starting
+        with '_' are not stored (core.py:2441-2473)."""
+        state = self._calc_data[calc_name]["state"]
+        complex_codes, int_codes, _ = state.codes
+        f_complex, f_int, _ = self._calc_data[calc_name]["saved_codes"]
+        rank = self.chunk_rank(chunk_slice)
+        beg, end = self.compressed_beg_end(calc_name, rank)
+        rows = {"Z": [complex_codes.index(c) for c in f_complex],
+                "U": [int_codes.index(c) for c in f_int],
+                "stop_reason": [0], "stop_iter": [0]}
+        arrs = {"Z": Z, "U": U, "stop_reason": stop_reason, "stop_iter": stop_iter}
+        for key in self.SAVE_ARRS:
+            mmap = self.get_data_memmap(calc_name, key, mode="r+")
+            for field, src in enumerate(rows[key]):
+                mmap[field, beg:end] = arrs[key][src, :]
+            mmap.flush()
+            del mmap
+
+    def reload_data(self, chunk_slice, calc_name):
+        """(subset, c_pix, Z, U, stop_reason, stop_iter) of a chunk from the
+        memory maps (core.py:2476-2510)."""
+        rank = self.chunk_rank(chunk_slice)
+        beg, end = self.compressed_beg_end(calc_name, rank)
+        arr = {}
+        for key in self.SAVE_ARRS:
+            mmap = self.get_data_memmap(calc_name, key, mode="r")
+            arr[key] = np.array(mmap[:, beg:end])
+            del mmap
+        subset = self._calc_data[calc_name]["state"].subset
+        if subset is not None:
+            ub, ue = self.uncompressed_beg_end(rank)
+            mmap = self.get_data_memmap(calc_name, "subset", mode="r")
+            arr["subset"] = np.array(mmap[ub:ue])
+            del mmap
+        else:
+            arr["subset"] = None
+        c_pix = np.ravel(self.chunk_pixel_pos(chunk_slice, jitter=False, supersampling=None))
+        if arr["subset"] is not None:
+            c_pix = c_pix[arr["subset"]]
+        return arr["subset"], c_pix, arr["Z"], arr["U"], arr["stop_reason"], arr["stop_iter"]
 
     def get_std_cpt(self, c_pix):
         """c = center + dx * lin_mat . pix (core.py:2781-2794)."""

@@ -88,7 +88,17 @@ def xr_table(xr_dict):
     """Sparse side table of an orbit (perturbation.py:317-375 get_path_data):
     sorted indices, complex mantissas and exponents."""
     keys = sorted(xr_dict.keys())
+    vals = [_as_scalar(xr_dict[k]) for k in keys]
     idx = np.array(keys, dtype=np.int32)
-    m = np.array([complex(xr_dict[k].m) for k in keys], dtype=np.complex128)
-    e = np.array([xr_dict[k].e for k in keys], dtype=np.int32)
+    m = np.array([complex(v.m) for v in vals], dtype=np.complex128)
+    e = np.array([v.e for v in vals], dtype=np.int32)
     return idx, m, e
+
+
+def _as_scalar(v):
+    """XrScalar of an XrScalar or of a (mantissa, exp) record array (the
+    reference's Xrange values read from its pickles)."""
+    if isinstance(v, XrScalar):
+        return v
+    rec = np.asarray(v).reshape(-1)[0]
+    return XrScalar(rec["mantissa"].item(), int(rec["exp"]))

@@ -33,6 +33,18 @@ def mpc_lin_proj_impl_noscale(lin_mat, x, y):
     return mpmath.mpc(x1, y1)
 
 
+class _XrangeArrayCompat(np.ndarray):
+    """Stands for the reference's Xrange_array (numpy_utils/xrange.py:65) when
+    its pickles are read: the record array (mantissa, exp) it is made of."""
+
+
+class _RefPointUnpickler(pickle.Unpickler):
+    def find_class(self, module, name):
+        if module == "fractalshades.numpy_utils.xrange" and name == "Xrange_array":
+            return _XrangeArrayCompat
+        return super().find_class(module, name)
+
+
 class PerturbationFractal(Fractal):
 
     def __init__(self, directory):
@@ -101,11 +113,14 @@ class PerturbationFractal(Fractal):
             pickle.dump(Zn_path, tmpfile, pickle.HIGHEST_PROTOCOL)
 
     def reload_ref_point(self, scan_only=False):
+        """(FP_params, Zn_path) from data/ref_pt.dat -- also a file written by
+        the reference, whose Xrange values unpickle as (mantissa, exp)
+        record arrays (perturbation.py:276-289)."""
         with open(self.ref_point_file(), 'rb') as tmpfile:
-            FP_params = pickle.load(tmpfile)
+            FP_params = _RefPointUnpickler(tmpfile).load()
             if scan_only:
                 return FP_params
-            Zn_path = pickle.load(tmpfile)
+            Zn_path = _RefPointUnpickler(tmpfile).load()
         return FP_params, Zn_path
 
     @property

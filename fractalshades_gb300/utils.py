@@ -18,6 +18,19 @@ def mkdir_p(path):
             raise
 
 
+def dic_flatten(nested_dic, key_prefix="", sep="@"):
+    """Flatten nested dicts: dic[k1]...[kn] becomes flat[k1@...@kn]
+    (utils.py:32-45 of the reference)."""
+    res = dict()
+    if isinstance(nested_dic, dict):
+        for key, val in nested_dic.items():
+            pre = "" if key_prefix == "" else key_prefix + sep
+            res.update(dic_flatten(val, pre + key, sep))
+    else:
+        res[key_prefix] = nested_dic
+    return res
+
+
 def _store_kwargs(identifier):
     """Decorator for the zoom method: keyword-only call; every argument
     (defaults applied) becomes an instance attribute and the dict is kept as

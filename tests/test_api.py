@@ -121,3 +121,98 @@ def test_reference_point_search_and_path_data(tmp_path):
     assert 1.1 * 0.5 * np.sqrt(2) * 1e-38 < kc < 1.1 * (0.5 * np.sqrt(2) + 0.4) * 1e-38
     # a second call reuses the stored orbit (ref_point_matching)
     assert f.ref_point_matching()
+
+
+def _std_fractal(path, max_iter=100):
+    f = fsm.Mandelbrot(str(path))
+    f.zoom(x=-0.5, y=0.1, dx=3., nx=450, xy_ratio=1.5, theta_deg=0.)
+    f.calc_std_div(calc_name="c", subset=None, max_iter=max_iter, M_divergence=1000.)
+    return f
+
+
+def test_raw_storage_layout_and_reuse(tmp_path):
+    """The reference's on-disk layout (core.py:2125-2510): npy memory maps
+    data/<calc>_<key>.arr in chunk-compressed order (chunks by rank, pixels of
+    a chunk row-major, x fastest), the .report chunk table and the
+    .fingerprint pickle; a second instance with the same parameters finds the
+    stored results, another max_iter does not."""
+    f = _std_fractal(tmp_path)
+    data = f._calc_data["c"]
+    assert data["need_new_mmap"]
+    f.init_report_mmap("c")
+    f.init_data_mmaps("c")
+    data["need_new_mmap"] = False
+    ny, nx = f.ny, f.nx
+    n = nx * ny
+    rng = np.random.default_rng(0)
+    nZ, nU = len(f.codes[0]), len(f.codes[1])
+    Z = rng.random((nZ, n)) + 1j * rng.random((nZ, n))
+    U = rng.integers(0, 50, (nU, n)).astype(np.int32)
+    sr = rng.integers(-1, 3, n).astype(np.int8)
+    si = rng.integers(0, 100, n).astype(np.int32)
+    f._store_image("c", {"Z": Z, "U": U, "stop_reason": sr, "stop_iter": si})
+    for cs in f.chunk_slices():
+        subset, c_pix, Zc, Uc, src, sic = f.reload_data(cs, "c")
+        ix, ixx, iy, iyy = cs
+        m = (ixx - ix) * (iyy - iy)
+        assert subset is None
+        assert np.array_equal(Zc, Z.reshape(nZ, ny, nx)[:, iy:iyy, ix:ixx].reshape(nZ, m))
+        assert np.array_equal(sic[0], si.reshape(ny, nx)[iy:iyy, ix:ixx].ravel())
+        assert np.array_equal(src[0], sr.reshape(ny, nx)[iy:iyy, ix:ixx].ravel())
+        assert np.array_equal(c_pix, np.ravel(f.chunk_pixel_pos(cs)))
+    arr = np.load(str(tmp_path / "data" / "c_Z.arr"), mmap_mode="r")
+    assert arr.shape == (nZ, n) and arr.dtype == np.complex128
+    items, report = f.reload_report("c", None)
+    assert items == ["chunk1d_begin", "chunk1d_end", "chunk_pts", "done"]
+    assert report[-1, 1] == n and np.all(report[:, 3] == 1)
+
+    g = _std_fractal(tmp_path)
+    assert not g._calc_data["c"]["need_new_mmap"]
+    assert all(g.res_available("c", cs) for cs in g.chunk_slices())
+    assert g.calc_raw("c") is None            # every tile done: nothing launched
+    assert np.array_equal(g.get_raw("c", "stop_iter"), si.reshape(ny, nx))
+    assert np.array_equal(g.get_raw("c", "zn"), Z[f.codes[0].index("zn")].reshape(ny, nx))
+
+    h = _std_fractal(tmp_path, max_iter=200)
+    assert h._calc_data["c"]["need_new_mmap"]         # calc_raw starts a new set
+    assert h.reload_fingerprint("c")["calc_kwargs"]["max_iter"] == 200
+    h.init_report_mmap("c")
+    assert not h.res_available("c", next(h.chunk_slices()))
+
+
+def test_reads_reference_written_ref_pt(tmp_path, monkeypatch):
+    """data/ref_pt.dat as the reference writes it (perturbation.py:256-274:
+    FP_params then Zn_path, Xrange values pickled as its Xrange_array record
+    arrays) is read back, and its Xrange side table feeds get_path_data."""
+    import pickle
+    import sys
+    import types
+    from fractalshades_gb300.numpy_utils import xrange as fsx
+
+    class Xrange_array(np.ndarray):
+        pass
+    Xrange_array.__module__ = "fractalshades.numpy_utils.xrange"
+    Xrange_array.__qualname__ = "Xrange_array"
+    for name in ("fractalshades", "fractalshades.numpy_utils", "fractalshades.numpy_utils.xrange"):
+        monkeypatch.setitem(sys.modules, name, types.ModuleType(name))
+    sys.modules["fractalshades.numpy_utils.xrange"].Xrange_array = Xrange_array
+    rec = np.zeros((1,), dtype=fsx.get_xr_dtype(np.complex128))
+    rec["mantissa"], rec["exp"] = 0.75 - 0.5j, -1200
+    xr_val = rec.view(Xrange_array)
+    with mpmath.workdps(30):
+        FP_params = {"ref_point": mpmath.mpc("-1.75", "0.01"), "dps": 30, "order": 7,
+                     "max_iter": 100, "FP_code": ["zn"], "partials": {}, "xr": {3: xr_val},
+                     "div_iter": 101, "ref_orbit_len": 7, "init_kwargs": {}}
+    Zn = (np.arange(7) * (0.1 + 0.2j)).astype(np.complex128)
+    (tmp_path / "data").mkdir()
+    with open(tmp_path / "data" / "ref_pt.dat", "wb") as fh:
+        pickle.dump(FP_params, fh, pickle.HIGHEST_PROTOCOL)
+        pickle.dump(Zn, fh, pickle.HIGHEST_PROTOCOL)
+    for name in ("fractalshades", "fractalshades.numpy_utils", "fractalshades.numpy_utils.xrange"):
+        monkeypatch.delitem(sys.modules, name)
+
+    f = fsm.Perturbation_mandelbrot(str(tmp_path))
+    params, path = f.reload_ref_point()
+    assert params["order"] == 7 and np.array_equal(path, Zn)
+    idx, m, e = fsx.xr_table(params["xr"])
+    assert idx.tolist() == [3] and m[0] == 0.75 - 0.5j and e[0] == -1200
