@@ -64,7 +64,8 @@ def serving_leg(n_requests, device):
     setup_s = time.perf_counter() - t0
     reqs = srv.request_stream(centers, n_requests, rate=200.0, seed=5)
     server = srv.TileServer(centers, hbm_budget=120 * 2 ** 30, n_slots=3,
-                            max_batch_pixels=8 * 2 ** 20, mode="fe32", device=device)
+                            max_batch_pixels=8 * 2 ** 20, mode="fe32", device=device,
+                            keep_results=False)
     t0 = time.perf_counter()
     try:
         done = server.run(reqs, realtime=True, timeout=600)
@@ -74,6 +75,9 @@ def serving_leg(n_requests, device):
     lat = np.array([(r.done - r.arrival) * 1e3 for r in done])
     iters = float(sum(r.pixel_iters for r in done))
     return {"requests": len(done), "rate_per_s": 200.0, "wall_s": wall,
+            "arrival_span_s": float(max(r.arrival for r in done) - t0),
+            "pixel_iters": iters, "results_to_host_gb": float(
+                sum(r.side ** 2 for r in done) * srv.BYTES_PER_PIXEL / 1e9),
             "pixel_iter_per_s": iters / wall, "latency_ms": {
                 "p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                 "max": float(lat.max())},

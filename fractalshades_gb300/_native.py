@@ -61,6 +61,7 @@ class Tile(ct.Structure):
         ("drift_e", I32), ("drifty_m", F64), ("drifty_e", I32), ("ref", P),
         ("Z", P), ("nZ", I32), ("i_dzndz", I32), ("i_dzndc", I32),
         ("U", P), ("stop_reason", P), ("stop_iter", P), ("potential", P), ("dem", P),
+        ("dzndc_scale_e", I32),
     ]
 
 
@@ -80,7 +81,7 @@ SYMBOLS = [
     "fsg_set_stream", "fsg_sync", "fsg_ref_create", "fsg_ref_destroy",
     "fsg_ref_info", "fsg_ref_download", "fsg_std_tiles", "fsg_perturb_tiles",
     "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel", "fsg_peak_flops",
-    "fsg_std_tiles_noalloc",
+    "fsg_std_tiles_noalloc", "fsg_ref_derive_bla",
 ]
 
 
@@ -109,6 +110,7 @@ def load():
         L.fsg_sync.argtypes = [P]
         L.fsg_ref_create.argtypes = [P, ct.POINTER(RefDesc), ct.POINTER(P)]
         L.fsg_ref_destroy.argtypes = [P, P]
+        L.fsg_ref_derive_bla.argtypes = [P, P, ct.c_double, ct.c_double, ct.POINTER(P)]
         L.fsg_ref_info.argtypes = [P, ct.POINTER(I64), ct.POINTER(I64), ct.POINTER(I32)]
         L.fsg_ref_download.argtypes = [P, P, ct.c_int, P, P]
         L.fsg_std_tiles.argtypes = [P, ct.POINTER(Calc), ct.POINTER(Tile), I32, I32]
@@ -230,10 +232,27 @@ class Reference:
         ctx.L.fsg_ref_info(h, ct.byref(ln), ct.byref(bl), ct.byref(st))
         self.len, self.bla_len, self.stages = ln.value, bl.value, st.value
 
+    def derive_bla(self, kc, bla_eps=1e-6, ctx=None):
+        """A Reference that shares this one's orbit and derivative tables and
+        owns a BLA tree built for ``kc`` (fsg_ref_derive_bla).  It keeps this
+        reference alive."""
+        ctx = ctx or self.ctx
+        h = P()
+        ctx.check(ctx.L.fsg_ref_derive_bla(ctx.h, self.h, float(kc), float(bla_eps), ct.byref(h)),
+                  "fsg_ref_derive_bla")
+        r = Reference.__new__(Reference)
+        r.ctx, r.h, r._base, r._keep = ctx, h, self, []
+        r.Zn, r.flavor, r.xr_paths = self.Zn, self.flavor, self.xr_paths
+        ln, bl, st = I64(), I64(), I32()
+        ctx.L.fsg_ref_info(h, ct.byref(ln), ct.byref(bl), ct.byref(st))
+        r.len, r.bla_len, r.stages = ln.value, bl.value, st.value
+        return r
+
     def free(self):
         if getattr(self, "h", None) and getattr(self.ctx, "h", None):
-            self.ctx.L.fsg_ref_destroy(self.ctx.h, self.h)
+            self.ctx.check(self.ctx.L.fsg_ref_destroy(self.ctx.h, self.h), "fsg_ref_destroy")
         self.h = None
+        self._base = None
 
     def __del__(self):
         try:
@@ -269,7 +288,7 @@ class Reference:
 def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None, U=None,
               ref=None, center=0j, dx=0.0, dx_m=0.0, dx_e=0, drift_m=0j, drift_e=0,
               drifty_m=0.0, drifty_e=0, i_dzndz=-1, i_dzndc=-1, potential=None,
-              dem=None, keep=None):
+              dem=None, keep=None, dzndc_scale_e=0):
     """Fill a Tile from numpy (host) arrays: either the axes xs / ys of a
     rectangle or an explicit complex128 list of pixel positions ``pix``."""
     t = Tile()
@@ -293,6 +312,7 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
     t.U = _p(U)
     t.stop_reason, t.stop_iter = _p(stop_reason), _p(stop_iter)
     t.potential, t.dem = _p(potential), _p(dem)
+    t.dzndc_scale_e = int(dzndc_scale_e)
     if keep is not None:
         keep.extend([xs, ys, pix, Z, U, stop_reason, stop_iter, potential, dem])
     return t
@@ -301,7 +321,7 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
 def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_ptr,
                    stop_iter_ptr, U_ptr=0, ref=None, center=0j, dx=0.0, dx_m=0.0,
                    dx_e=0, drift_m=0j, drift_e=0, drifty_m=0.0, drifty_e=0, i_dzndz=-1,
-                   i_dzndc=-1, potential_ptr=0, dem_ptr=0):
+                   i_dzndc=-1, potential_ptr=0, dem_ptr=0, dzndc_scale_e=0):
     """Fill a Tile from raw device pointers (ints)."""
     t = Tile()
     t.nx, t.ny = int(nx), int(ny)
@@ -319,6 +339,7 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
     t.U = U_ptr or None
     t.stop_reason, t.stop_iter = stop_reason_ptr, stop_iter_ptr
     t.potential, t.dem = potential_ptr or None, dem_ptr or None
+    t.dzndc_scale_e = int(dzndc_scale_e)
     return t
 
 

@@ -32,6 +32,9 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
                          int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
                          cudaStream_t s);
+void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
+                      int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                      cudaStream_t s);
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
@@ -59,9 +62,13 @@ struct fsg_ctx {
 struct fsg_ref {
     RefDev host;            // device pointers, host copy
     RefDev *dev = nullptr;  // device copy of the descriptor
-    std::vector<void *> allocs;
+    std::vector<void *> allocs;   // stream-ordered allocations (cudaMallocAsync)
     int64_t len = 0;
     int xr_paths = 0, flavor = 0, has_dzndc = 0, has_dzndz = 0;
+    fsg_ref *base = nullptr;      // fsg_ref_derive_bla: owner of the shared tables
+    int derived = 0;              // live references derived from this one
+    cudaEvent_t ready = nullptr;  // derived references: recorded after the BLA build;
+                                  // launches and downloads wait for it
 };
 
 namespace {
@@ -86,17 +93,18 @@ int cuda_err(fsg_ctx *c, cudaError_t e, const char *what) {
 template <class T>
 int ref_alloc(fsg_ctx *ctx, fsg_ref *r, T **p, size_t n) {
     void *q = nullptr;
-    cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
+    // stream-ordered: no device-wide synchronisation while other streams run
+    cudaError_t e = cudaMallocAsync(&q, n * sizeof(T) + 16, ctx->stream);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc(reference table)");
     r->allocs.push_back(q);
     *p = (T *)q;
     return FSG_OK;
 }
 
-void ref_release(fsg_ref *r) {
-    for (void *p : r->allocs) cudaFree(p);
+void ref_release(fsg_ref *r, cudaStream_t s) {
+    for (void *p : r->allocs) cudaFreeAsync(p, s);
     r->allocs.clear();
-    if (r->dev) cudaFree(r->dev);
+    if (r->dev) cudaFreeAsync(r->dev, s);
     r->dev = nullptr;
 }
 
@@ -134,6 +142,10 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
         if (calc->bla && t.ref->host.bla_len <= 0)
             return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference has no BLA tree");
     }
+    if (t.dzndc_scale_e != 0 && (!perturb || calc->flavor != 0))
+        return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e applies to the power-2 Mandelbrot perturbation only");
+    if (t.dzndc_scale_e < -100000 || t.dzndc_scale_e > 100000)
+        return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e out of range");
     if (perturb && calc->flavor != 0) {
         if (calc->mode != FSG_MODE_FP64)
             return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 only");
@@ -180,6 +192,7 @@ TileDev make_tile(const fsg_tile &t) {
     d.Z = t.Z; d.nZ = t.nZ; d.i_dzndz = t.i_dzndz; d.i_dzndc = t.i_dzndc;
     d.U = t.U; d.stop_reason = (signed char *)t.stop_reason; d.stop_iter = t.stop_iter;
     d.pot = t.potential; d.dem = t.dem;
+    d.dzs = t.dzndc_scale_e;
     return d;
 }
 
@@ -242,6 +255,13 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     for (int32_t i = 0; i < ntiles; i++) {
         int rc = check_tile(ctx, tiles[i], perturb, calc);
         if (rc != FSG_OK) return rc;
+    }
+    // tables of derived references may still be building on another stream:
+    // the launch stream waits for them on the device
+    for (int32_t i = 0; i < ntiles; i++) {
+        fsg_ref *r = tiles[i].ref;
+        if (r && r->ready && (i == 0 || tiles[i - 1].ref != r))
+            CK(cudaStreamWaitEvent(ctx->stream, r->ready, 0), "cudaStreamWaitEvent(reference)");
     }
     std::vector<TileDev> td(ntiles);
     if (where == FSG_DEVICE) {
@@ -436,8 +456,8 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     R.n_xr = d->n_xr;
     cudaStream_t s = ctx->stream;
     int rc = FSG_OK;
-#define RA(ptr, n) do { rc = ref_alloc(ctx, r, &(ptr), (n)); if (rc != FSG_OK) { ref_release(r); delete r; return rc; } } while (0)
-#define RCK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { ref_release(r); delete r; return cuda_err(ctx, e_, what); } } while (0)
+#define RA(ptr, n) do { rc = ref_alloc(ctx, r, &(ptr), (n)); if (rc != FSG_OK) { ref_release(r, s); delete r; return rc; } } while (0)
+#define RCK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { ref_release(r, s); delete r; return cuda_err(ctx, e_, what); } } while (0)
     double2 *Zn; RA(Zn, len + 1);
     RCK(cudaMemcpyAsync(Zn, d->Zn, 16 * (size_t)len, cudaMemcpyHostToDevice, s), "upload orbit");
     RCK(cudaMemsetAsync(Zn + len, 0, 16, s), "pad orbit");
@@ -449,9 +469,10 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
         slot.assign(len + 1, -1);
         for (int k = 0; k < d->n_xr; k++) slot[d->xr_idx[k]] = k;
         RA(xr_slot, len + 1); RA(xr_m, d->n_xr); RA(xr_e, d->n_xr);
-        RCK(cudaMemcpy(xr_slot, slot.data(), 4 * (size_t)(len + 1), cudaMemcpyHostToDevice), "upload xr slots");
-        RCK(cudaMemcpy(xr_m, d->xr_m, 16 * (size_t)d->n_xr, cudaMemcpyHostToDevice), "upload xr mantissas");
-        RCK(cudaMemcpy(xr_e, d->xr_e, 4 * (size_t)d->n_xr, cudaMemcpyHostToDevice), "upload xr exponents");
+        // stream-ordered like the allocations (pageable sources: staged before return)
+        RCK(cudaMemcpyAsync(xr_slot, slot.data(), 4 * (size_t)(len + 1), cudaMemcpyHostToDevice, s), "upload xr slots");
+        RCK(cudaMemcpyAsync(xr_m, d->xr_m, 16 * (size_t)d->n_xr, cudaMemcpyHostToDevice, s), "upload xr mantissas");
+        RCK(cudaMemcpyAsync(xr_e, d->xr_e, 4 * (size_t)d->n_xr, cudaMemcpyHostToDevice, s), "upload xr exponents");
     }
     R.xr_slot = xr_slot; R.xr_m = xr_m; R.xr_e = xr_e;
     // derivative paths
@@ -504,7 +525,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     }
     R.Zf = Zf; R.Zp = Zp; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f = bla_f;
     R.bla_first = bla_first; R.bla_first_step = bla_first_step; R.bla_nit = bla_nit;
-    RCK(cudaMalloc((void **)&r->dev, sizeof(RefDev)), "cudaMalloc(reference descriptor)");
+    RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     // builds
     if (d->flavor == 0) {
@@ -530,9 +551,71 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
 
 int fsg_ref_destroy(fsg_ctx *ctx, fsg_ref *ref) {
     if (!ref) return FSG_OK;
-    if (ctx) { cudaSetDevice(ctx->device); cudaStreamSynchronize(ctx->stream); }
-    ref_release(ref);
+    if (ref->derived > 0)
+        return set_err(ctx, FSG_ERR_ARG, "reference still has derived references");
+    cudaStream_t s = nullptr;
+    if (ctx) { cudaSetDevice(ctx->device); cudaStreamSynchronize(ctx->stream); s = ctx->stream; }
+    if (ref->ready) { cudaEventSynchronize(ref->ready); cudaEventDestroy(ref->ready); }
+    ref_release(ref, s);
+    if (ref->base) ref->base->derived--;
     delete ref;
+    if (s) cudaStreamSynchronize(s);
+    return FSG_OK;
+}
+
+int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, fsg_ref **out) {
+    if (!ctx || !base || !out) return set_err(ctx, FSG_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    if (base->base) return set_err(ctx, FSG_ERR_ARG, "derive from the reference that owns the orbit");
+    if (!(kc >= 0.) || !(bla_eps >= 0.)) return set_err(ctx, FSG_ERR_ARG, "bad kc or BLA eps");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    fsg_ref *r = new (std::nothrow) fsg_ref();
+    if (!r) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
+    r->len = base->len; r->flavor = base->flavor; r->xr_paths = base->xr_paths;
+    r->has_dzndc = base->has_dzndc; r->has_dzndz = base->has_dzndz;
+    r->base = base;
+    RefDev &R = r->host;
+    R = base->host;                  // shares the orbit, side table, paths, fe orbit
+    const int len = (int)base->len;
+    const int L = len / 8;
+    cudaStream_t s = ctx->stream;
+    int rc = FSG_OK;
+#define RA(ptr, n) do { rc = ref_alloc(ctx, r, &(ptr), (n)); if (rc != FSG_OK) { ref_release(r, s); delete r; return rc; } } while (0)
+#define RCK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { ref_release(r, s); delete r; return cuda_err(ctx, e_, what); } } while (0)
+    double2 *Mbla = nullptr; double *Mbs = nullptr, *rbla = nullptr;
+    int4 *bla_f = nullptr, *bla_first = nullptr; int *bla_first_step = nullptr;
+    R.bla_len = 0;
+    if (L > 0) {
+        if (R.flavor == 0) RA(Mbla, 4 * (size_t)L); else RA(Mbs, 16 * (size_t)L);
+        RA(rbla, 2 * (size_t)L);
+        RCK(cudaMemsetAsync(rbla, 0, 16 * (size_t)L, s), "zero BLA radii");
+        if (Mbla) RCK(cudaMemsetAsync(Mbla, 0, 64 * (size_t)L, s), "zero BLA");
+        if (Mbs) RCK(cudaMemsetAsync(Mbs, 0, 128 * (size_t)L, s), "zero BLA");
+        R.bla_len = 2 * L;
+        if (R.flavor == 0) {
+            RA(bla_f, 2 * (size_t)R.bla_len);
+            RA(bla_first, 2 * (size_t)R.bla_nit);
+            RA(bla_first_step, (size_t)R.bla_nit);
+        }
+    }
+    R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla;
+    R.bla_f = bla_f; R.bla_first = bla_first; R.bla_first_step = bla_first_step;
+    RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
+    RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
+    if (R.bla_len > 0) {
+        fsg_build_bla(r->dev, R.flavor, len, Mbla, Mbs, rbla, R.stages, kc, bla_eps, s);
+        if (R.flavor == 0)
+            fsg_build_fe_bla(r->dev, Mbla, rbla, R.bla_len, bla_f, R.bla_nit, bla_first,
+                             bla_first_step, s);
+    }
+    RCK(cudaGetLastError(), "BLA kernels");
+    // no host wait: launches and downloads that use r wait for this event
+    RCK(cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming), "cudaEventCreate");
+    RCK(cudaEventRecord(r->ready, s), "cudaEventRecord(reference)");
+#undef RA
+#undef RCK
+    base->derived++;
+    *out = r;
     return FSG_OK;
 }
 
@@ -549,6 +632,8 @@ int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0, vo
     const RefDev &R = ref->host;
     size_t len = (size_t)ref->len;
     CK(cudaStreamSynchronize(ctx->stream), "sync");
+    if (ref->ready) CK(cudaEventSynchronize(ref->ready), "sync reference build");
+    if (ref->base && ref->base->ready) CK(cudaEventSynchronize(ref->base->ready), "sync reference build");
     if (which == 0 || which == 1) {
         size_t n = which == 0 ? len : len + 1;
         const double2 *sp = which == 0 ? R.dZndc : R.dZndz;

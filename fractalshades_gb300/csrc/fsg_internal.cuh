@@ -60,6 +60,7 @@ struct TileDev {
     void *Z; int nZ, i_dzndz, i_dzndc;
     int *U; signed char *stop_reason; int *stop_iter;
     double *pot, *dem;
+    int dzs;                                   // dzndc scale 2^dzs over the reference's
 };
 
 struct CalcDev {

@@ -197,13 +197,21 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         }
     }
     // end of iterations :1375-1385
+    // dzndc in the tile's unit: the reference's scale times 2^dzs
     if (XR) {
         zn = cadd(xr_to_std(xzn), __ldg(&R.Zn[w]));
-        if (dzndc_on) dzndc = xr_to_std(xr_add(xdzndc, ldx(R.dZndc_xm, R.dZndc_xe, w)));
+        if (dzndc_on) {
+            xc t = xr_add(xdzndc, ldx(R.dZndc_xm, R.dZndc_xe, w));
+            t.e += T.dzs;
+            dzndc = xr_to_std(t);
+        }
         dzndz = cx(0., 0.);   // the Xrange branch never writes back Z[dzndz]
     } else {
         zn = cadd(zn, __ldg(&R.Zn[w]));
-        if (dzndc_on) dzndc = cadd(dzndc, __ldg(&R.dZndc[w]));
+        if (dzndc_on) {
+            dzndc = cadd(dzndc, __ldg(&R.dZndc[w]));
+            if (T.dzs != 0) dzndc = cx(ldexp_d(dzndc.x, T.dzs), ldexp_d(dzndc.y, T.dzs));
+        }
     }
     double2 *Z = (double2 *)T.Z;
     Z[ip] = zn;

@@ -443,7 +443,8 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     fe dzf = as_fe(s.ux, s.uy, s.E);
     double2 zn = cadd(fe_to_d(dzf), __ldg(&R.Zn[w]));
     double2 dzc = cx(0., 0.);
-    if (dzndc_on) dzc = fe_to_d(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w)));
+    // dzndc in the tile's unit: the reference's scale times 2^dzs
+    if (dzndc_on) dzc = fe_to_d(fe_scale2(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w)), T.dzs));
     double2 *Z = (double2 *)T.Z;
     Z[ip] = zn;
     if (dzndz_on) Z[T.i_dzndz * np + ip] = xrsem ? cx(0., 0.) : fe_to_d(as_fe(s.qx, s.qy, s.G));

@@ -353,6 +353,10 @@ void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, 
     k_plain_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf, Zp);
 }
 
+void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
+                      int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                      cudaStream_t s);
+
 void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzndc,
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
@@ -363,6 +367,13 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
     k_fe_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (dzndc_f) k_fe_path<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dzndc, dzndc_xm, dzndc_xe, len + 1, dzndc_f);
     if (dzndz_f) k_fe_path<<<(len + 2 + tb - 1) / tb, tb, 0, s>>>(dzndz, dzndz_xm, dzndz_xe, len + 2, dzndz_f);
+    fsg_build_fe_bla(Rd, Mbla, rbla, bla_len, bla_f, bla_nit, bla_first, bla_first_step, s);
+}
+
+void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
+                      int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                      cudaStream_t s) {
+    int tb = 256;
     if (bla_f && bla_len > 0) {
         k_fe_bla<<<(bla_len + tb - 1) / tb, tb, 0, s>>>(Mbla, rbla, bla_len, bla_f);
         k_fe_bla_first<<<(bla_nit + tb - 1) / tb, tb, 0, s>>>(Rd, bla_f, bla_nit, bla_first,

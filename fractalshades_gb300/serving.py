@@ -9,13 +9,19 @@ free up, and run concurrently on the device (continuous batching).
 * Admission: a request is admitted when a slot is free and its output buffers
   plus any new reference tables fit in the HBM budget still unreserved;
   memory is released when its results have been copied back.
-* Reference cache: the orbit of a centre does not depend on the view; the
-  derivative paths scale with dx and the BLA radii depend on kc.  A reference
-  is built per (centre, floor(log2 dx), Xrange branch) with the derivative
-  scale 2^floor(log2 dx) and kc rounded up to a power of two (smaller, still
-  valid, BLA radii); the dzndc output is rescaled by dx / 2^floor(log2 dx).
-  Every request of a bucket uses the same tables whether it runs alone or in
-  a mix, so its result does not depend on what else is on the GPU.
+* Reference cache: the orbit of a centre does not depend on the view, the
+  derivative paths scale linearly with dx and only the BLA radii depend on
+  kc.  One base reference per (centre, Xrange branch, max_iter) holds the
+  orbit and the derivative paths at unit scale; each tile sets its dzndc
+  scale 2^(e - 1) (dx = m 2^e, m in [0.5, 1)) with fsg_tile.dzndc_scale_e and
+  the output is rescaled by dx / 2^(e - 1).  BLA trees are derived from the
+  base (fsg_ref_derive_bla) per kc bucket: kc rounded up to 2^(8 ceil(e/8))
+  (smaller, still valid, radii), or 0 below the double range -- where the
+  reference's own kc, to_standard(kc), is 0 too.  Every request of a bucket
+  uses the same tables whether it runs alone or in a mix, so its result does
+  not depend on what else is on the GPU.
+* References are built on a context of their own (its own stream) with
+  stream-ordered allocation, so a build does not wait for running tiles.
 * Latency of a request = arrival -> results on the host.
 
 The reference has no serving mode; this replaces its interactive GUI loop
@@ -90,7 +96,7 @@ class TileServer:
 
     def __init__(self, centers, *, hbm_budget=120 * 2 ** 30, n_slots=3,
                  max_batch_pixels=8 * 2 ** 20, mode="fe32", M=1000., bla_eps=1e-6,
-                 device=0):
+                 device=0, keep_results=True):
         import torch
         self.torch = torch
         self.device = torch.device("cuda", device)
@@ -102,11 +108,21 @@ class TileServer:
         self.bla_eps = bla_eps
         self.max_batch_pixels = int(max_batch_pixels)
         self.slots = [_Slot(torch, self.device, i) for i in range(n_slots)]
-        self.cache = collections.OrderedDict()   # key -> (Reference, bytes)
+        # reference builds on a high-priority stream of their own: their
+        # kernels are scheduled first as SMs free up, and launches wait for
+        # them on the device (fsg_ref_derive_bla does not block the host)
+        self.builder = nat.Context(self.device.index or 0)
+        self.builder_stream = torch.cuda.Stream(self.device, priority=-1)
+        self.builder.set_stream(self.builder_stream.cuda_stream)
+        self.bases = {}                          # (centre, xr, max_iter) -> (Reference, bytes)
+        self.cache = collections.OrderedDict()   # + kc bucket -> (derived Reference, bytes)
         self.cache_bytes = 0
         self.pending = collections.deque()
         self.done = []
         self.max_reserved = 0
+        # False: results reach the host (pinned buffers) and are dropped once
+        # counted, so that the pinned pool is recycled (load tests)
+        self.keep_results = keep_results
 
     # ------------------------------------------------------------------
     def _view(self, req):
@@ -124,23 +140,38 @@ class TileServer:
         # dx = m 2^e with m in [0.5, 1): bucket scale 2^(e - 1)
         return dx_xr, drift, kc_xr, xr
 
+    @staticmethod
+    def kc_bucket(kc_xr):
+        """kc rounded up to 2^(8 ceil(e / 8)) (kc = m 2^e, m in [0.5, 1)),
+        0 below the smallest double (the reference's to_standard(kc))."""
+        if kc_xr.e < -1074 or kc_xr.m == 0:
+            return 0.0
+        e8 = 8 * -(-kc_xr.e // 8)
+        return math.ldexp(1.0, min(e8, 1023))
+
+    def _base(self, req, xr):
+        key = (req.center, xr, req.max_iter)
+        if key not in self.bases:
+            cen = self.centers[req.center]
+            ref = nat.Reference(self.builder, cen.Zn, div_iter=req.max_iter + 1, order=cen.p,
+                                xr_idx=cen.xr_idx if cen.xr_idx.size else None,
+                                xr_m=cen.xr_m if cen.xr_idx.size else None,
+                                xr_e=cen.xr_e if cen.xr_idx.size else None,
+                                xr_paths=xr, calc_dzndc=True, scale_m=0.5, scale_e=1,
+                                bla=False)
+            nbytes = ref.len * (16 * 6 + 64)
+            self.bases[key] = (ref, nbytes)
+            self.cache_bytes += nbytes
+        return self.bases[key][0]
+
     def _reference(self, req, dx_xr, kc_xr, xr):
-        key = (req.center, dx_xr.e, xr, req.max_iter)
+        kc_b = self.kc_bucket(kc_xr)
+        key = (req.center, xr, req.max_iter, kc_b)
         if key in self.cache:
             self.cache.move_to_end(key)
             return self.cache[key][0], 0
-        cen = self.centers[req.center]
-        # kc rounded up to a power of two: every request of the bucket shares it
-        kc_b = math.ldexp(1.0, kc_xr.e) if kc_xr.e > -1074 else 5e-324
-        if kc_xr.e < -1074:
-            kc_b = 0.0
-        ref = nat.Reference(self.slots[0].ctx, cen.Zn, div_iter=req.max_iter + 1, order=cen.p,
-                            xr_idx=cen.xr_idx if cen.xr_idx.size else None,
-                            xr_m=cen.xr_m if cen.xr_idx.size else None,
-                            xr_e=cen.xr_e if cen.xr_idx.size else None,
-                            xr_paths=xr, calc_dzndc=True, scale_m=0.5, scale_e=dx_xr.e,
-                            bla=True, kc=kc_b, bla_eps=self.bla_eps)
-        nbytes = ref.len * (16 * 6 + 64) + ref.bla_len * 80
+        ref = self._base(req, xr).derive_bla(kc_b, self.bla_eps, ctx=self.builder)
+        nbytes = ref.bla_len * 112
         self.cache[key] = (ref, nbytes)
         self.cache_bytes += nbytes
         return ref, nbytes
@@ -182,7 +213,8 @@ class TileServer:
                 stop_reason_ptr=b["sr"].data_ptr(), stop_iter_ptr=b["si"].data_ptr(),
                 U_ptr=b["U"].data_ptr(), ref=req._ref, dx_m=dx_xr.m, dx_e=dx_xr.e,
                 drift_m=drift.m, drift_e=drift.e, i_dzndc=1,
-                potential_ptr=b["pot"].data_ptr(), dem_ptr=b["dem"].data_ptr())
+                potential_ptr=b["pot"].data_ptr(), dem_ptr=b["dem"].data_ptr(),
+                dzndc_scale_e=dx_xr.e - 1)
             tiles.append(t)
         calc = nat.make_calc(max_iter=batch[0].max_iter, M_divergence=self.M, mode=self.mode,
                              calc_dzndc=True, interior=False, bla=True,
@@ -190,8 +222,19 @@ class TileServer:
         slot.ctx.perturb_tiles(calc, tiles, nat.DEVICE)
         with torch.cuda.stream(slot.stream):
             for req in batch:
-                req._host = {k: v.to("cpu", non_blocking=True) for k, v in req._bufs.items()
-                             if k not in ("xs", "ys")}
+                b = req._bufs
+                # dzndc was computed with the bucket scale 2^(e - 1): rescale to
+                # dx on the device, then copy into pinned host memory
+                ratio = 2.0 * req._view[0].m
+                b["Z"][1].mul_(ratio)
+                b["dem"].div_(ratio)
+                req._host = {}
+                for k, v in b.items():
+                    if k in ("xs", "ys"):
+                        continue
+                    h = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+                    h.copy_(v, non_blocking=True)
+                    req._host[k] = h
             slot.event = torch.cuda.Event()
             slot.event.record(slot.stream)
         slot.busy = True
@@ -201,16 +244,13 @@ class TileServer:
         now = time.perf_counter()
         for req in slot.batch:
             h = req._host
-            dx_xr = req._view[0]
-            # dzndc was computed with the bucket scale 2^(e - 1): rescale to dx
-            ratio = 2.0 * dx_xr.m
-            Z = h["Z"].numpy().view(np.complex128).reshape(2, -1).copy()
-            Z[1] *= ratio
-            dem = h["dem"].numpy() / ratio
-            req.result = {"Z": Z, "U": h["U"].numpy(), "stop_reason": h["sr"].numpy(),
-                          "stop_iter": h["si"].numpy(), "potential": h["pot"].numpy(),
-                          "dem": dem}
-            req.pixel_iters = int(req.result["stop_iter"].astype(np.int64).sum())
+            si = h["si"].numpy()
+            req.pixel_iters = int(si.sum(dtype=np.int64))
+            if self.keep_results:
+                req.result = {"Z": h["Z"].numpy().view(np.complex128).reshape(2, -1),
+                              "U": h["U"].numpy(), "stop_reason": h["sr"].numpy(),
+                              "stop_iter": si, "potential": h["pot"].numpy(),
+                              "dem": h["dem"].numpy()}
             req.done = now
             self.reserved -= req._bytes
             del req._bufs, req._host
@@ -290,8 +330,12 @@ class TileServer:
         for _, (ref, _) in self.cache.items():
             ref.free()
         self.cache.clear()
+        for _, (ref, _) in self.bases.items():
+            ref.free()
+        self.bases.clear()
         for s in self.slots:
             s.ctx.close()
+        self.builder.close()
 
 
 def request_stream(centers, n, rate, seed, sides=(256, 512, 1024, 2048),

@@ -117,6 +117,14 @@ typedef struct {
     void *Z; int32_t nZ; int32_t i_dzndz; int32_t i_dzndc;
     int32_t *U; int8_t *stop_reason; int32_t *stop_iter;
     double *potential; double *dem;
+    /* power-2 Mandelbrot perturbation: the tile's dzndc unit is the
+       reference's derivative scale times 2^dzndc_scale_e (the derivative
+       recurrence is linear in its scale, so one reference serves views of
+       every width: the outputs dzndc and DEM are scaled exactly); 0 for the
+       reference's own scale.  Must be 0 for the Burning Ship and the
+       standard loop.  No counterpart in the reference (one scale per
+       reference, perturbation.py:461-468). */
+    int32_t dzndc_scale_e;
 } fsg_tile;
 
 /* Launch statistics of the last fsg_*_tiles call. */
@@ -141,6 +149,20 @@ int fsg_sync(fsg_ctx *ctx);
 
 int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *desc, fsg_ref **out);
 int fsg_ref_destroy(fsg_ctx *ctx, fsg_ref *ref);
+
+/* A reference that shares the orbit, the Xrange side table, the derivative
+   paths and their FP32 copies of `base` and owns a BLA tree of its own, built
+   for kc / bla_eps: views of one centre at other widths need another kc (the
+   BLA radii depend on it, nothing else does; the derivative scale is set per
+   tile with fsg_tile.dzndc_scale_e).  FSG_ERR_ARG when base is itself derived;
+   fsg_ref_destroy refuses a base while references derived from it live.
+   Returns without waiting for the build: the BLA kernels run on ctx's stream
+   and every later launch (on any context) or download that uses the derived
+   reference waits for them on the device.
+   No counterpart in the reference (one BLA tree per calculation,
+   perturbation.py:1819-1881). */
+int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps,
+                       fsg_ref **out);
 /* Copy tables back to the host (tests).  which: 0 dZndc (complex128 [len]) or
  * its Xrange form (mantissa complex128 [len] + exp int32 [len]), 1 dZndz
  * ([len + 1]), 2 BLA (M complex128 [bla_len][2], r float64 [bla_len]),

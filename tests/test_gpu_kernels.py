@@ -290,3 +290,54 @@ def test_perturb_bs_vs_oracle(ctx, case):
     same = (si == d["stop_iter"]).ravel()
     for k in range(6):
         rel_close(Z[k], d["Z"][k], 1e-6, same)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fe32"])
+def test_dzndc_scale_and_derived_bla(ctx, mode):
+    """fsg_tile.dzndc_scale_e = k on a reference of derivative scale 2^s gives
+    the outputs of a reference of scale 2^(s+k) (the derivative recurrence is
+    linear in its scale; power-of-two scaling is exact), and a BLA tree
+    derived with fsg_ref_derive_bla equals the one of a fresh reference."""
+    from fractalshades_gb300 import _native as nat
+    d = load("pert_m2_fp64")
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+
+    def ref(scale_e, kc_=kc, bla=True):
+        return nat.Reference(ctx, d["Zn"], div_iter=int(d["ref_div_iter"]),
+                             order=int(d["ref_order"]), calc_dzndc=True,
+                             scale_m=float(d["dx_m"]), scale_e=int(d["dx_e"]) + scale_e,
+                             bla=bla, kc=kc_, bla_eps=float(d["bla_eps"]))
+
+    def run(r, k):
+        nx = int(round(np.sqrt(d["pix"].size)))
+        xs, ys = axes(d["pix"], nx)
+        n = d["pix"].size
+        Z = np.zeros((2, n), dtype=np.complex128)
+        sr = -np.ones((1, n), dtype=np.int8)
+        si = np.zeros((1, n), dtype=np.int32)
+        dem = np.zeros(n)
+        pot = np.zeros(n)
+        t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, stop_reason=sr,
+                          stop_iter=si, ref=r, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                          drift_m=complex(d["drift_m"]), drift_e=int(d["drift_e"]),
+                          i_dzndc=1, potential=pot, dem=dem, dzndc_scale_e=k)
+        ctx.perturb_tiles(nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                                        mode=mode, calc_dzndc=True, bla=True), [t])
+        return Z, si, dem
+
+    Za, sia, dema = run(ref(7), 0)
+    Zb, sib, demb = run(ref(0), 7)
+    assert np.array_equal(sia, sib)
+    assert np.array_equal(Za.view(np.uint64), Zb.view(np.uint64))
+    assert np.array_equal(dema.view(np.uint64), demb.view(np.uint64))
+    base = ref(0, bla=False)
+    kc2 = kc * 4.
+    derived = base.derive_bla(kc2, float(d["bla_eps"]))
+    Zc, sic, _ = run(derived, 7)
+    Zd, sid, _ = run(ref(0, kc_=kc2), 7)
+    assert np.array_equal(sic, sid)
+    assert np.array_equal(Zc.view(np.uint64), Zd.view(np.uint64))
+    with pytest.raises(nat.GPUError):
+        base.free()                 # a base outlives the references derived from it
+    derived.free()
+    base.free()
