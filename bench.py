@@ -196,9 +196,14 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter):
                                      U_ptr=U.data_ptr(), ref=r, dx_m=t.dx_m, dx_e=t.dx_e,
                                      drift_m=t.driftx_m, drift_e=t.driftx_e,
                                      drifty_m=t.drifty_m, drifty_e=t.drifty_e))
-    c4 = nat.make_calc(max_iter=bs_max_iter, M_divergence=1000., flavor=1, calc_dzndc=True,
-                       bla=True)
-    k4, st4 = timed(lambda: ctx.perturb_tiles(c4, ts, nat.DEVICE), 1, 1)
+    def c4(mode):
+        return nat.make_calc(max_iter=bs_max_iter, M_divergence=1000., flavor=1,
+                             calc_dzndc=True, bla=True, mode=mode)
+    si4 = keep[4::6]
+    k4f, st4f = timed(lambda: ctx.perturb_tiles(c4("fe32"), ts, nat.DEVICE), 1, 1)
+    si_fe = np.concatenate([t.cpu().numpy() for t in si4])
+    k4, st4 = timed(lambda: ctx.perturb_tiles(c4("fp64"), ts, nat.DEVICE), 1, 0)
+    si_64 = np.concatenate([t.cpu().numpy() for t in si4])
     out["burning_ship_64_tiles"] = {
         "workload": f"Burning Ship, 64 tiles of side 256..2048 (log-uniform), widths 1e-200..1e-30, "
                     f"centres from the BS ball method + Newton at 250 digits, max_iter {bs_max_iter}, "
@@ -206,7 +211,10 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter):
         "pixels": int(sum(t.side ** 2 for t in tiles4)), "pixel_iters": int(st4["pixel_iters"]),
         "periods": sorted({t.order for t in tiles4 if t.order}),
         "kernel_ms": k4, "value": st4["pixel_iters"] / (k4 * 1e-3), "unit": "pixel-iter/s",
-        "dtype": "f64"}
+        "dtype": "f64",
+        "fe32": {"kernel_ms": k4f, "value": st4f["pixel_iters"] / (k4f * 1e-3),
+                 "speedup_vs_fp64": (st4f["pixel_iters"] / k4f) / (st4["pixel_iters"] / k4),
+                 "iter_count_differs_frac": float(np.mean(si_fe != si_64))}}
     for r in refs4:
         r.free()
     return out

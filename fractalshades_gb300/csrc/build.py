@@ -28,11 +28,12 @@ SOURCES = {
     "fsg_perturb.cu": ["-fmad=false"],
     "fsg_ref.cu": ["-fmad=false"],
     "fsg_perturb_fe32.cu": [],
+    "fsg_perturb_bs32.cu": [],
     "fsg_peak.cu": [],
     "fsg_noalloc.cu": [],
     "fsg_abi.cu": [],
 }
-HEADERS = ["fsg_num.cuh", "fsg_internal.cuh"]
+HEADERS = ["fsg_num.cuh", "fsg_internal.cuh", "fsg_bs.cuh"]
 
 
 def nvcc():

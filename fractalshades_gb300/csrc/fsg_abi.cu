@@ -147,8 +147,8 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
     if (t.dzndc_scale_e < -100000 || t.dzndc_scale_e > 100000)
         return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e out of range");
     if (perturb && calc->flavor != 0) {
-        if (calc->mode != FSG_MODE_FP64)
-            return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 only");
+        if (calc->mode == FSG_MODE_XR64)
+            return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 and FSG_MODE_FE32");
         if (calc->calc_dzndc && !t.ref->has_dzndc)
             return set_err(ctx, FSG_ERR_ARG, "calc_hessian requested but the reference has no Jacobian paths");
         if (calc->bla && t.ref->host.bla_len <= 0)
@@ -227,6 +227,7 @@ int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int n
     CK(cudaEventRecord(ctx->ev0, s), "cudaEventRecord");
     if (!perturb) fsg_launch_std(W, C, grid, block, s);
     else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
+    else if (calc->mode == FSG_MODE_FE32) fsg_launch_perturb_bs_fe32(W, C, grid, block, s);
     else fsg_launch_perturb(W, C, grid, block, s);
     CK(cudaGetLastError(), "kernel launch");
     CK(cudaEventRecord(ctx->ev1, s), "cudaEventRecord");

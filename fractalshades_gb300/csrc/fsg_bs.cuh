@@ -1,0 +1,330 @@
+// fsg_bs.cuh -- the Burning Ship family perturbation loop, templated on the
+// real type of the deltas:
+//   * double -- the reference's standard branch (instantiated in
+//     fsg_perturb.cu, compiled without FMA contraction: one rounding per
+//     operation in the order of the reference source);
+//   * fr -- FP32 mantissa + int32 exponent (instantiated in fsg_perturb_bs32.cu):
+//     no underflow at any depth and FP32-pipe arithmetic instead of GB300's
+//     slow FP64 pipe; results within FP32 rounding of the double form.
+// perturbation.py:1406-1811 (numba_cycles_perturb_BS, numba_iterate_BS,
+// apply_BLA_BS, apply_BLA_deriv_BS) with the closures of
+// models/burning_ship.py:19-60 (diffabs and its derivatives), 535-619
+// (_p_iter_zn) and 622-859 (_p_iter_hessian).
+#pragma once
+#include "fsg_internal.cuh"
+
+// perturbation.py:2116-2170 ref_BLA_get: returns the step (0 if none) and the
+// table index of the accepted entry.
+__device__ __forceinline__ int bla_lookup(const RefDev &R, double abs_zn, int w, int &ib) {
+    int it = w >> FSG_STG_COMPRESSED;
+    int stages = FSG_STG_COMPRESSED;
+    for (int s = FSG_STG_COMPRESSED; s < R.stages; s++) {
+        stages = s;
+        if (it & 1) break;
+        it >>= 1;
+    }
+    int invalid_step = R.first_invalid - w;
+    for (int stg = stages; stg >= FSG_STG_COMPRESSED; stg--) {
+        int step = 1 << stg;
+        if (step >= invalid_step) continue;
+        int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
+        if (abs_zn < __ldg(&R.rbla[idx])) { ib = idx; return step; }
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// fr: a real m * 2^e with an FP32 mantissa, |m| in [1, 2), or m = 0 (e =
+// FR_ZERO_E).  Every operation rounds the mantissa once (FP32) and keeps the
+// exponent exact.
+// ---------------------------------------------------------------------------
+struct fr { float m; int e; };
+#define FR_ZERO_E (-(1 << 29))
+
+FSG_DEV fr fr_zero() { fr r; r.m = 0.f; r.e = FR_ZERO_E; return r; }
+// normalise m * 2^e for |m| < 2^126 (0 and subnormal mantissas give 0)
+FSG_DEV fr fr_norm(float m, int e) {
+    const int b = (__float_as_int(m) >> 23) & 0xff;
+    if (b == 0) return fr_zero();
+    fr r; r.m = m * __int_as_float((254 - b) << 23); r.e = e + (b - 127);
+    return r;
+}
+FSG_DEV fr fr_from_d(double x) {
+    const long long bits = __double_as_longlong(x);
+    const int be = (int)((bits >> 52) & 0x7ff);
+    if (be == 0) {
+        if (x == 0.) return fr_zero();
+        int e; double f = frexp(x, &e);            // subnormal double
+        return fr_norm((float)(2. * f), e - 1);
+    }
+    // the mantissa in [1, 2) with the sign of x; its FP32 rounding may give 2
+    const double m = __longlong_as_double((bits & 0x800fffffffffffffLL) | 0x3ff0000000000000LL);
+    return fr_norm((float)m, be - 1023);
+}
+FSG_DEV double fr_to_d(fr a) { return a.m == 0.f ? 0. : ldexp_d((double)a.m, a.e); }
+// 2^k for k in [-60, 0]
+FSG_DEV float fr_p2(int k) { return __int_as_float((k + 127) << 23); }
+
+FSG_DEV fr operator+(fr a, fr b) {
+    if (a.m == 0.f) return b;
+    if (b.m == 0.f) return a;
+    const int d = a.e - b.e;
+    if (d >= 0) return d > 60 ? a : fr_norm(fmaf(b.m, fr_p2(-d), a.m), a.e);
+    return d < -60 ? b : fr_norm(fmaf(a.m, fr_p2(d), b.m), b.e);
+}
+FSG_DEV fr operator-(fr a) { a.m = -a.m; return a; }
+FSG_DEV fr operator-(fr a, fr b) { return a + (-b); }
+FSG_DEV fr operator*(fr a, fr b) {
+    if (a.m == 0.f || b.m == 0.f) return fr_zero();
+    fr r; r.m = a.m * b.m; r.e = a.e + b.e;              // |m| in [1, 4)
+    if (fabsf(r.m) >= 2.f) { r.m *= 0.5f; r.e += 1; }
+    return r;
+}
+FSG_DEV fr operator*(double s, fr b) { return fr_from_d(s) * b; }
+FSG_DEV fr &operator+=(fr &a, fr b) { a = a + b; return a; }
+
+// the operations the loop needs, for both real types
+FSG_DEV double to_d(double x) { return x; }
+FSG_DEV double to_d(fr x) { return fr_to_d(x); }
+template <class T> FSG_DEV T from_d(double x);
+template <> FSG_DEV double from_d<double>(double x) { return x; }
+template <> FSG_DEV fr from_d<fr>(double x) { return fr_from_d(x); }
+// m * 2^e from a mantissa and an exponent (the Xrange form of c)
+template <class T> FSG_DEV T from_me(double m, int e);
+template <> FSG_DEV double from_me<double>(double m, int e) { return ldexp_d(m, e); }
+template <> FSG_DEV fr from_me<fr>(double m, int e) {
+    fr r = fr_from_d(m);
+    if (r.m != 0.f) r.e += e;
+    return r;
+}
+FSG_DEV bool ge0(double x) { return x >= 0.; }
+FSG_DEV bool ge0(fr x) { return x.m >= 0.f; }
+FSG_DEV bool le0(double x) { return x <= 0.; }
+FSG_DEV bool le0(fr x) { return x.m <= 0.f; }
+FSG_DEV double absT(double x) { return fabs(x); }
+FSG_DEV fr absT(fr x) { x.m = fabsf(x.m); return x; }
+// sgn with 0 mapped to +1 (burning_ship.py:12-17)
+FSG_DEV double sgnT(double x) { return x < 0. ? -1. : 1.; }
+FSG_DEV fr sgnT(fr x) { fr r; r.m = x.m < 0.f ? -1.f : 1.f; r.e = 0; return r; }
+// |a| <= |b|
+FSG_DEV bool abs_le(double a, double b) { return fabs(a) <= fabs(b); }
+FSG_DEV bool abs_le(fr a, fr b) {
+    if (a.m == 0.f) return true;
+    if (b.m == 0.f) return false;
+    return a.e != b.e ? a.e < b.e : fabsf(a.m) <= fabsf(b.m);
+}
+
+// burning_ship.py:19-60 diffabs(X, x) = |X + x| - |X| and its derivatives
+template <class T> FSG_DEV T diffabs(T X, T x) {
+    if (ge0(X)) { if (ge0(X + x)) return 1. * x; else return -(2. * X + x); }
+    else { if (le0(X + x)) return -x; else return (2. * X + x); }
+}
+template <class T> FSG_DEV T ddiffabsdX(T X, T x) {
+    if (ge0(X)) { if (ge0(X + x)) return from_d<T>(0.); else return from_d<T>(-2.); }
+    else { if (le0(X + x)) return from_d<T>(0.); else return from_d<T>(2.); }
+}
+template <class T> FSG_DEV T ddiffabsdx(T X, T x) {
+    if (ge0(X)) { if (ge0(X + x)) return from_d<T>(1.); else return from_d<T>(-1.); }
+    else { if (le0(X + x)) return from_d<T>(-1.); else return from_d<T>(1.); }
+}
+
+// burning_ship.py:535-619 _p_iter_zn
+template <class T>
+FSG_DEV void bs_zn(int flavor, T &xn, T &yn, T X, T Y, T a, T b) {
+    T nx, ny;
+    if (flavor == 1) {
+        T ref_xyn = X * Y;
+        nx = xn * (xn + 2. * X) - yn * (yn + 2. * Y) + a;
+        ny = 2. * diffabs(ref_xyn, xn * yn + xn * Y + yn * X) - b;
+    } else if (flavor == 2) {
+        nx = xn * (xn + 2. * X) - yn * (yn + 2. * Y) + a;
+        ny = 2. * (X * diffabs(Y, yn) + xn * absT(Y + yn)) - b;
+    } else if (flavor == 3) {
+        nx = xn * (xn + 2. * X) - Y * diffabs(Y, yn) - yn * absT(Y + yn) + a;
+        ny = 2. * (X * yn + Y * xn + xn * yn) - b;
+    } else if (flavor == 4) {
+        T q = X * X - Y * Y;
+        nx = diffabs(q, xn * (xn + 2. * X) - yn * (yn + 2. * Y)) + a;
+        ny = 2. * (X * yn + Y * xn + xn * yn) - b;
+    } else {
+        T ref_xyn = X * Y, q = X * X - Y * Y;
+        nx = diffabs(q, xn * (xn + 2. * X) - yn * (yn + 2. * Y)) + a;
+        ny = 2. * diffabs(ref_xyn, xn * yn + xn * Y + yn * X) - b;
+    }
+    xn = nx; yn = ny;
+}
+
+// burning_ship.py:622-859 _p_iter_hessian, h = (dxnda, dxndb, dynda, dyndb)
+template <class T>
+FSG_DEV void bs_hess(int flavor, T h[4], T xn, T yn, T X, T Y, T Xa, T Xb, T Ya, T Yb) {
+    T xa = h[0], xb = h[1], ya = h[2], yb = h[3];
+    T nxa, nxb, nya, nyb;
+    if (flavor == 1 || flavor == 5) {
+        T opX = X * Y;
+        T dXa = Xa * Y + X * Ya, dXb = Xb * Y + X * Yb;
+        T opx = xn * yn + xn * Y + yn * X;
+        T dxa = xa * yn + xn * ya + xa * Y + xn * Ya + ya * X + yn * Xa;
+        T dxb = xb * yn + xn * yb + xb * Y + xn * Yb + yb * X + yn * Xb;
+        T dX = ddiffabsdX(opX, opx), dx = ddiffabsdx(opX, opx);
+        nya = 2. * (dX * dXa + dx * dxa);
+        nyb = 2. * (dX * dXb + dx * dxb);
+        if (flavor == 1) {
+            nxa = 2. * ((X + xn) * xa + Xa * xn) - 2. * ((Y + yn) * ya + Ya * yn);
+            nxb = 2. * ((X + xn) * xb + Xb * xn) - 2. * ((Y + yn) * yb + Yb * yn);
+        } else {
+            T opX2 = X * X - Y * Y;
+            T dXa2 = 2. * (X * Xa - Y * Ya), dXb2 = 2. * (X * Xb - Y * Yb);
+            T opx2 = xn * (xn + 2. * X) - yn * (yn + 2. * Y);
+            T dxa2 = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - ya * (yn + 2. * Y) - yn * (ya + 2. * Ya);
+            T dxb2 = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - yb * (yn + 2. * Y) - yn * (yb + 2. * Yb);
+            T dX2 = ddiffabsdX(opX2, opx2), dx2 = ddiffabsdx(opX2, opx2);
+            nxa = dX2 * dXa2 + dx2 * dxa2;
+            nxb = dX2 * dXb2 + dx2 * dxb2;
+        }
+    } else if (flavor == 2) {
+        T da = diffabs(Y, yn), dX = ddiffabsdX(Y, yn), dx = ddiffabsdx(Y, yn);
+        T Yy = Y + yn, ab = absT(Yy), sg = sgnT(Yy);
+        nxa = 2. * (((X + xn) * xa + Xa * xn) - ((Y + yn) * ya + Ya * yn));
+        nxb = 2. * (((X + xn) * xb + Xb * xn) - ((Y + yn) * yb + Yb * yn));
+        nya = 2. * (Xa * da + X * (dX * Ya + dx * ya) + xa * ab + xn * sg * (Ya + ya));
+        nyb = 2. * (Xb * da + X * (dX * Yb + dx * yb) + xb * ab + xn * sg * (Yb + yb));
+    } else if (flavor == 3) {
+        T da = diffabs(Y, yn), dX = ddiffabsdX(Y, yn), dx = ddiffabsdx(Y, yn);
+        T Yy = Y + yn, ab = absT(Yy), sg = sgnT(Yy);
+        nxa = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - Ya * da - Y * (Ya * dX + ya * dx)
+              - ya * ab - yn * sg * (Ya + ya);
+        nxb = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - Yb * da - Y * (Yb * dX + yb * dx)
+              - yb * ab - yn * sg * (Yb + yb);
+        nya = 2. * (Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
+        nyb = 2. * (Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
+    } else {
+        T opX = X * X - Y * Y;
+        T dXa = 2. * (X * Xa - Y * Ya), dXb = 2. * (X * Xb - Y * Yb);
+        T opx = xn * (xn + 2. * X) - yn * (yn + 2. * Y);
+        T dxa = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - ya * (yn + 2. * Y) - yn * (ya + 2. * Ya);
+        T dxb = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - yb * (yn + 2. * Y) - yn * (yb + 2. * Yb);
+        T dX = ddiffabsdX(opX, opx), dx = ddiffabsdx(opX, opx);
+        nxa = dX * dXa + dx * dxa;
+        nxb = dX * dXb + dx * dxb;
+        nya = 2. * (Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
+        nyb = 2. * (Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
+    }
+    h[0] = nxa; h[1] = nxb; h[2] = nya; h[3] = nyb;
+}
+
+template <class T>
+FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
+                      unsigned long long &nfull, unsigned long long &nbla,
+                      unsigned long long &nreb, unsigned long long &itsum) {
+    const TileDev &Tl = T_;
+    const RefDev &R = *Tl.ref;
+    const long long np = (long long)Tl.nx * Tl.ny;
+    const int flavor = C.flavor, hess = C.calc_dzndc;
+    const int order = R.order, div_iter = R.div_iter;
+    // perturbation.py:2260-2280 ref_path_c_from_pix_BS through Xrange values
+    double2 pp = fsg_pixel(Tl, ip);
+    double px = pp.x, py = pp.y;
+    double x1 = Tl.lin[0] * px + Tl.lin[1] * py;
+    double y1 = Tl.lin[2] * px + Tl.lin[3] * py;
+    xf dxr; dxr.m = Tl.dx_m; dxr.e = Tl.dx_e;
+    xc c_xr = xf_mul_c(dxr, cx(x1, y1));
+    double ar, br; int ae, be;
+    xr_coexp_r(c_xr.re, c_xr.e, Tl.drift_re, Tl.drift_e, ar, br, ae);
+    const T a = from_me<T>(ar + br, ae);
+    xr_coexp_r(c_xr.im, c_xr.e, Tl.drifty_m, Tl.drifty_e, ar, br, be);
+    const T b = from_me<T>(ar + br, be);
+
+    T xn = from_d<T>(0.), yn = from_d<T>(0.);
+    T h[4] = {from_d<T>(0.), from_d<T>(0.), from_d<T>(0.), from_d<T>(0.)};
+    int w = 0, n = 0; signed char stop = -1; bool dyn = true;
+    for (;;) {
+        if (C.bla && (w & 7) == 0) {
+            int ib;
+            // the reference compares the double value of |dz| (0 when it
+            // underflows, perturbation.py:1123-1135)
+            int step = bla_lookup(R, hypot(to_d(xn), to_d(yn)), w, ib);
+            if (step != 0) {
+                const double *M = R.Mbla_bs + 8 * ib;
+                T M0 = from_d<T>(__ldg(M)), M1 = from_d<T>(__ldg(M + 1));
+                T M2 = from_d<T>(__ldg(M + 2)), M3 = from_d<T>(__ldg(M + 3));
+                n += step; w = (w + step) % order;
+                T nx = M0 * xn + M1 * yn + from_d<T>(__ldg(M + 4)) * a + from_d<T>(__ldg(M + 5)) * b;
+                T ny = M2 * xn + M3 * yn + from_d<T>(__ldg(M + 6)) * a + from_d<T>(__ldg(M + 7)) * b;
+                xn = nx; yn = ny;
+                if (hess) {
+                    T xa = M0 * h[0] + M1 * h[2], xb = M0 * h[1] + M1 * h[3];
+                    T ya = M2 * h[0] + M3 * h[2], yb = M2 * h[1] + M3 * h[3];
+                    h[0] = xa; h[1] = xb; h[2] = ya; h[3] = yb;
+                }
+                nbla++;
+                continue;
+            }
+        }
+        n += 1;
+        nfull++;
+        double2 Zr = __ldg(&R.Zn[w]);
+        const T X = from_d<T>(Zr.x), Y = from_d<T>(Zr.y);
+        if (hess) {
+            T Xa = from_d<T>(0.), Xb = from_d<T>(0.), Ya = from_d<T>(0.), Yb = from_d<T>(0.);
+            if (!dyn) {
+                Xa = from_d<T>(__ldg(&R.dXa[w])); Xb = from_d<T>(__ldg(&R.dXb[w]));
+                Ya = from_d<T>(__ldg(&R.dYa[w])); Yb = from_d<T>(__ldg(&R.dYb[w]));
+            }
+            bs_hess<T>(flavor, h, xn, yn, X, Y, Xa, Xb, Ya, Yb);
+        }
+        bs_zn<T>(flavor, xn, yn, X, Y, a, b);
+        if (n >= C.max_iter) { stop = 0; break; }
+        w += 1;
+        if (w >= order) w = w % order;
+        double2 Zs = __ldg(&R.Zn[w]);
+        T XX = xn + from_d<T>(Zs.x), YY = yn + from_d<T>(Zs.y);
+        const double XXd = to_d(XX), YYd = to_d(YY);
+        if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
+        if (w >= div_iter - 1) {
+            xn = XX; yn = YY;
+            if (hess) {
+                h[0] += from_d<T>(__ldg(&R.dXa[w])); h[1] += from_d<T>(__ldg(&R.dXb[w]));
+                h[2] += from_d<T>(__ldg(&R.dYa[w])); h[3] += from_d<T>(__ldg(&R.dYb[w]));
+            }
+            w = 0; nreb++; continue;
+        }
+        dyn = abs_le(XX, xn) && abs_le(YY, yn);
+        if (dyn) {
+            xn = XX; yn = YY;
+            if (hess) {
+                h[0] += from_d<T>(__ldg(&R.dXa[w])); h[1] += from_d<T>(__ldg(&R.dXb[w]));
+                h[2] += from_d<T>(__ldg(&R.dYa[w])); h[3] += from_d<T>(__ldg(&R.dYb[w]));
+            }
+            w = 0; nreb++; continue;
+        }
+    }
+    double2 Zr = __ldg(&R.Zn[w]);
+    const double xo = to_d(xn + from_d<T>(Zr.x)), yo = to_d(yn + from_d<T>(Zr.y));
+    double hd[4] = {0., 0., 0., 0.};
+    if (hess) {
+        hd[0] = to_d(h[0] + from_d<T>(__ldg(&R.dXa[w]))); hd[1] = to_d(h[1] + from_d<T>(__ldg(&R.dXb[w])));
+        hd[2] = to_d(h[2] + from_d<T>(__ldg(&R.dYa[w]))); hd[3] = to_d(h[3] + from_d<T>(__ldg(&R.dYb[w])));
+    }
+    double *Z = (double *)Tl.Z;
+    Z[ip] = xo; Z[np + ip] = yo;
+    if (hess) { Z[2 * np + ip] = hd[0]; Z[3 * np + ip] = hd[1]; Z[4 * np + ip] = hd[2]; Z[5 * np + ip] = hd[3]; }
+    if (Tl.U) Tl.U[ip] = w;
+    Tl.stop_iter[ip] = n; Tl.stop_reason[ip] = stop;
+    double absd = 0.5 * (hypot(hd[0] + hd[3], hd[1] - hd[2]) + hypot(hd[0] - hd[3], hd[1] + hd[2]));
+    fsg_epilogue(Tl, C, ip, cx(xo, yo), absd, n);
+    itsum += (unsigned long long)n;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_perturb_bs(WorkDev W, CalcDev C) {
+    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    fsg_load_starts(W, s_start);
+    unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
+    int t; long long ip;
+    while (true) {
+        if (*W.cancel) { *W.status = 1; break; }
+        if (!fsg_claim(W, s_start, t, ip)) break;
+        pixel_bs<T>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+    }
+    fsg_flush_stats(W, itsum, nfull, nbla, nreb);
+}

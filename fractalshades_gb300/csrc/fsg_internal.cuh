@@ -160,6 +160,8 @@ inline int fsg_auto_grid(K kernel, int grid, int block, long long total) {
 // at full occupancy
 void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);
+void fsg_launch_perturb_bs_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
+                                cudaStream_t s);
 void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
                              cudaStream_t s);
 // Reference tables

@@ -13,25 +13,7 @@
 // the next pixel from the launch's work counter as soon as it finishes.
 #include "fsg_internal.cuh"
 
-// perturbation.py:2116-2170 ref_BLA_get: returns the step (0 if none) and the
-// table index of the accepted entry.
-__device__ __forceinline__ int bla_lookup(const RefDev &R, double abs_zn, int w, int &ib) {
-    int it = w >> FSG_STG_COMPRESSED;
-    int stages = FSG_STG_COMPRESSED;
-    for (int s = FSG_STG_COMPRESSED; s < R.stages; s++) {
-        stages = s;
-        if (it & 1) break;
-        it >>= 1;
-    }
-    int invalid_step = R.first_invalid - w;
-    for (int stg = stages; stg >= FSG_STG_COMPRESSED; stg--) {
-        int step = 1 << stg;
-        if (step >= invalid_step) continue;
-        int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
-        if (abs_zn < __ldg(&R.rbla[idx])) { ib = idx; return step; }
-    }
-    return 0;
-}
+#include "fsg_bs.cuh"
 
 __device__ __forceinline__ xc ldx(const double2 *m, const int *e, int i) {
     double2 v = __ldg(&m[i]);
@@ -238,204 +220,14 @@ __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }
 
-// ---------------------------------------------------------------------------
-// Burning Ship family, double deltas
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double sgnd(double x) { return x < 0. ? -1. : 1.; }
-__device__ __forceinline__ double diffabs(double X, double x) {
-    if (X >= 0.) { if ((X + x) >= 0.) return 1. * x; else return -(2. * X + x); }
-    else { if ((X + x) <= 0.) return -x; else return (2. * X + x); }
-}
-__device__ __forceinline__ double ddiffabsdX(double X, double x) {
-    if (X >= 0.) { if ((X + x) >= 0.) return 0.; else return -2.; }
-    else { if ((X + x) <= 0.) return 0.; else return 2.; }
-}
-__device__ __forceinline__ double ddiffabsdx(double X, double x) {
-    if (X >= 0.) { if ((X + x) >= 0.) return 1.; else return -1.; }
-    else { if ((X + x) <= 0.) return -1.; else return 1.; }
-}
-
-__device__ __forceinline__ void bs_zn(int flavor, double &xn, double &yn, double X, double Y,
-                                      double a, double b) {
-    double nx, ny;
-    if (flavor == 1) {
-        double ref_xyn = X * Y;
-        nx = xn * (xn + 2. * X) - yn * (yn + 2. * Y) + a;
-        ny = 2. * diffabs(ref_xyn, xn * yn + xn * Y + yn * X) - b;
-    } else if (flavor == 2) {
-        nx = xn * (xn + 2. * X) - yn * (yn + 2. * Y) + a;
-        ny = 2. * (X * diffabs(Y, yn) + xn * fabs(Y + yn)) - b;
-    } else if (flavor == 3) {
-        nx = xn * (xn + 2. * X) - Y * diffabs(Y, yn) - yn * fabs(Y + yn) + a;
-        ny = 2. * (X * yn + Y * xn + xn * yn) - b;
-    } else if (flavor == 4) {
-        double q = X * X - Y * Y;
-        nx = diffabs(q, xn * (xn + 2. * X) - yn * (yn + 2. * Y)) + a;
-        ny = 2. * (X * yn + Y * xn + xn * yn) - b;
-    } else {
-        double ref_xyn = X * Y, q = X * X - Y * Y;
-        nx = diffabs(q, xn * (xn + 2. * X) - yn * (yn + 2. * Y)) + a;
-        ny = 2. * diffabs(ref_xyn, xn * yn + xn * Y + yn * X) - b;
-    }
-    xn = nx; yn = ny;
-}
-
-__device__ __forceinline__ void bs_hess(int flavor, double h[4], double xn, double yn, double X,
-                                        double Y, double Xa, double Xb, double Ya, double Yb) {
-    double xa = h[0], xb = h[1], ya = h[2], yb = h[3];
-    double nxa, nxb, nya, nyb;
-    if (flavor == 1 || flavor == 5) {
-        double opX = X * Y;
-        double dXa = Xa * Y + X * Ya, dXb = Xb * Y + X * Yb;
-        double opx = xn * yn + xn * Y + yn * X;
-        double dxa = xa * yn + xn * ya + xa * Y + xn * Ya + ya * X + yn * Xa;
-        double dxb = xb * yn + xn * yb + xb * Y + xn * Yb + yb * X + yn * Xb;
-        double dX = ddiffabsdX(opX, opx), dx = ddiffabsdx(opX, opx);
-        nya = 2. * (dX * dXa + dx * dxa);
-        nyb = 2. * (dX * dXb + dx * dxb);
-        if (flavor == 1) {
-            nxa = 2. * ((X + xn) * xa + Xa * xn) - 2. * ((Y + yn) * ya + Ya * yn);
-            nxb = 2. * ((X + xn) * xb + Xb * xn) - 2. * ((Y + yn) * yb + Yb * yn);
-        } else {
-            double opX2 = X * X - Y * Y;
-            double dXa2 = 2. * (X * Xa - Y * Ya), dXb2 = 2. * (X * Xb - Y * Yb);
-            double opx2 = xn * (xn + 2. * X) - yn * (yn + 2. * Y);
-            double dxa2 = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - ya * (yn + 2. * Y) - yn * (ya + 2. * Ya);
-            double dxb2 = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - yb * (yn + 2. * Y) - yn * (yb + 2. * Yb);
-            double dX2 = ddiffabsdX(opX2, opx2), dx2 = ddiffabsdx(opX2, opx2);
-            nxa = dX2 * dXa2 + dx2 * dxa2;
-            nxb = dX2 * dXb2 + dx2 * dxb2;
-        }
-    } else if (flavor == 2) {
-        double da = diffabs(Y, yn), dX = ddiffabsdX(Y, yn), dx = ddiffabsdx(Y, yn);
-        double Yy = Y + yn, ab = fabs(Yy), sg = sgnd(Yy);
-        nxa = 2. * (((X + xn) * xa + Xa * xn) - ((Y + yn) * ya + Ya * yn));
-        nxb = 2. * (((X + xn) * xb + Xb * xn) - ((Y + yn) * yb + Yb * yn));
-        nya = 2. * (Xa * da + X * (dX * Ya + dx * ya) + xa * ab + xn * sg * (Ya + ya));
-        nyb = 2. * (Xb * da + X * (dX * Yb + dx * yb) + xb * ab + xn * sg * (Yb + yb));
-    } else if (flavor == 3) {
-        double da = diffabs(Y, yn), dX = ddiffabsdX(Y, yn), dx = ddiffabsdx(Y, yn);
-        double Yy = Y + yn, ab = fabs(Yy), sg = sgnd(Yy);
-        nxa = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - Ya * da - Y * (Ya * dX + ya * dx)
-              - ya * ab - yn * sg * (Ya + ya);
-        nxb = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - Yb * da - Y * (Yb * dX + yb * dx)
-              - yb * ab - yn * sg * (Yb + yb);
-        nya = 2. * (Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
-        nyb = 2. * (Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
-    } else {
-        double opX = X * X - Y * Y;
-        double dXa = 2. * (X * Xa - Y * Ya), dXb = 2. * (X * Xb - Y * Yb);
-        double opx = xn * (xn + 2. * X) - yn * (yn + 2. * Y);
-        double dxa = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - ya * (yn + 2. * Y) - yn * (ya + 2. * Ya);
-        double dxb = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - yb * (yn + 2. * Y) - yn * (yb + 2. * Yb);
-        double dX = ddiffabsdX(opX, opx), dx = ddiffabsdx(opX, opx);
-        nxa = dX * dXa + dx * dxa;
-        nxb = dX * dXb + dx * dxb;
-        nya = 2. * (Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
-        nyb = 2. * (Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
-    }
-    h[0] = nxa; h[1] = nxb; h[2] = nya; h[3] = nyb;
-}
-
-__device__ __forceinline__ void pixel_bs(const TileDev &T, const CalcDev &C, long long ip,
-                                         unsigned long long &nfull, unsigned long long &nbla,
-                                         unsigned long long &nreb, unsigned long long &itsum) {
-    const RefDev &R = *T.ref;
-    const long long np = (long long)T.nx * T.ny;
-    const int flavor = C.flavor, hess = C.calc_dzndc;
-    const int order = R.order, div_iter = R.div_iter;
-    // perturbation.py:2260-2280 ref_path_c_from_pix_BS through Xrange values
-    double2 pp = fsg_pixel(T, ip);
-    double px = pp.x, py = pp.y;
-    double x1 = T.lin[0] * px + T.lin[1] * py;
-    double y1 = T.lin[2] * px + T.lin[3] * py;
-    xf dxr; dxr.m = T.dx_m; dxr.e = T.dx_e;
-    xc c_xr = xf_mul_c(dxr, cx(x1, y1));
-    double ar, br; int ae, be;
-    xr_coexp_r(c_xr.re, c_xr.e, T.drift_re, T.drift_e, ar, br, ae);
-    double a = ldexp_d(ar + br, ae);
-    xr_coexp_r(c_xr.im, c_xr.e, T.drifty_m, T.drifty_e, ar, br, be);
-    double b = ldexp_d(ar + br, be);
-
-    double xn = 0., yn = 0.;
-    double h[4] = {0., 0., 0., 0.};
-    int w = 0, n = 0; signed char stop = -1; bool dyn = true;
-    for (;;) {
-        if (C.bla && (w & 7) == 0) {
-            int ib;
-            int step = bla_lookup(R, hypot(xn, yn), w, ib);
-            if (step != 0) {
-                const double *M = R.Mbla_bs + 8 * ib;
-                double M0 = __ldg(M), M1 = __ldg(M + 1), M2 = __ldg(M + 2), M3 = __ldg(M + 3);
-                n += step; w = (w + step) % order;
-                double nx = M0 * xn + M1 * yn + __ldg(M + 4) * a + __ldg(M + 5) * b;
-                double ny = M2 * xn + M3 * yn + __ldg(M + 6) * a + __ldg(M + 7) * b;
-                xn = nx; yn = ny;
-                if (hess) {
-                    double xa = M0 * h[0] + M1 * h[2], xb = M0 * h[1] + M1 * h[3];
-                    double ya = M2 * h[0] + M3 * h[2], yb = M2 * h[1] + M3 * h[3];
-                    h[0] = xa; h[1] = xb; h[2] = ya; h[3] = yb;
-                }
-                nbla++;
-                continue;
-            }
-        }
-        n += 1;
-        nfull++;
-        double2 Zr = __ldg(&R.Zn[w]);
-        if (hess) {
-            double Xa = 0., Xb = 0., Ya = 0., Yb = 0.;
-            if (!dyn) { Xa = __ldg(&R.dXa[w]); Xb = __ldg(&R.dXb[w]); Ya = __ldg(&R.dYa[w]); Yb = __ldg(&R.dYb[w]); }
-            bs_hess(flavor, h, xn, yn, Zr.x, Zr.y, Xa, Xb, Ya, Yb);
-        }
-        bs_zn(flavor, xn, yn, Zr.x, Zr.y, a, b);
-        if (n >= C.max_iter) { stop = 0; break; }
-        w += 1;
-        if (w >= order) w = w % order;
-        double2 Zs = __ldg(&R.Zn[w]);
-        double XX = xn + Zs.x, YY = yn + Zs.y;
-        if (XX * XX + YY * YY > C.M2) { stop = 1; break; }
-        if (w >= div_iter - 1) {
-            xn = XX; yn = YY;
-            if (hess) { h[0] += __ldg(&R.dXa[w]); h[1] += __ldg(&R.dXb[w]); h[2] += __ldg(&R.dYa[w]); h[3] += __ldg(&R.dYb[w]); }
-            w = 0; nreb++; continue;
-        }
-        dyn = (fabs(XX) <= fabs(xn)) && (fabs(YY) <= fabs(yn));
-        if (dyn) {
-            xn = XX; yn = YY;
-            if (hess) { h[0] += __ldg(&R.dXa[w]); h[1] += __ldg(&R.dXb[w]); h[2] += __ldg(&R.dYa[w]); h[3] += __ldg(&R.dYb[w]); }
-            w = 0; nreb++; continue;
-        }
-    }
-    double2 Zr = __ldg(&R.Zn[w]);
-    xn += Zr.x; yn += Zr.y;
-    if (hess) { h[0] += __ldg(&R.dXa[w]); h[1] += __ldg(&R.dXb[w]); h[2] += __ldg(&R.dYa[w]); h[3] += __ldg(&R.dYb[w]); }
-    double *Z = (double *)T.Z;
-    Z[ip] = xn; Z[np + ip] = yn;
-    if (hess) { Z[2 * np + ip] = h[0]; Z[3 * np + ip] = h[1]; Z[4 * np + ip] = h[2]; Z[5 * np + ip] = h[3]; }
-    if (T.U) T.U[ip] = w;
-    T.stop_iter[ip] = n; T.stop_reason[ip] = stop;
-    double absd = 0.5 * (hypot(h[0] + h[3], h[1] - h[2]) + hypot(h[0] - h[3], h[1] + h[2]));
-    fsg_epilogue(T, C, ip, cx(xn, yn), absd, n);
-    itsum += (unsigned long long)n;
-}
-
-__global__ void __launch_bounds__(256) k_perturb_bs(WorkDev W, CalcDev C) {
-    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
-    fsg_load_starts(W, s_start);
-    unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
-    int t; long long ip;
-    while (true) {
-        if (*W.cancel) { *W.status = 1; break; }
-        if (!fsg_claim(W, s_start, t, ip)) break;
-        pixel_bs(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
-    }
-    fsg_flush_stats(W, itsum, nfull, nbla, nreb);
-}
+// Burning Ship family, double deltas: fsg_bs.cuh instantiated on double
+// (compiled here, without FMA contraction)
+template __global__ void k_perturb_bs<double>(WorkDev W, CalcDev C);
 
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
     if (C.flavor != 0)
-        k_perturb_bs<<<fsg_auto_grid(k_perturb_bs, grid, block, W.total), block, 0, s>>>(W, C);
+        k_perturb_bs<double><<<fsg_auto_grid(k_perturb_bs<double>, grid, block, W.total), block, 0,
+                               s>>>(W, C);
     else if (C.mode == 1)
         k_perturb_m2<true><<<fsg_auto_grid(k_perturb_m2<true>, grid, block, W.total), block, 0, s>>>(W, C);
     else

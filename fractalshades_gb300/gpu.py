@@ -82,7 +82,7 @@ class PerturbSpec:
         m = settings.precision_mode
         if m == "auto":
             return "xr64" if self.xr_detect_activated else "fp64"
-        if self.flavor != 0 and m != "fp64":
+        if self.flavor != 0 and m == "xr64":
             return "fp64"
         return m
 

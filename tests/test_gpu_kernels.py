@@ -260,6 +260,52 @@ def test_perturb_m2_fe32_vs_oracle(ctx, case):
     assert np.mean(sr == d["stop_reason"]) >= floor
 
 
+def _run_bs(ctx, d, mode):
+    from fractalshades_gb300 import _native as nat
+    fl = int(d["flavor"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    ref = nat.Reference(ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
+                        flavor=fl, calc_dzndc=True, scale_m=float(d["dx_m"]),
+                        scale_e=int(d["dx_e"]), bla=True, kc=kc, bla_eps=float(d["bla_eps"]))
+    nx = int(round(np.sqrt(d["pix"].size)))
+    xs, ys = axes(d["pix"], nx)
+    n = d["pix"].size
+    Z = np.zeros((6, n))
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
+                      stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                      drift_m=float(d["driftx_m"]), drift_e=int(d["driftx_e"]),
+                      drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]))
+    calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]), flavor=fl,
+                         calc_dzndc=True, bla=True, mode=mode)
+    ctx.perturb_tiles(calc, [t])
+    return Z, sr, si
+
+
+@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4"])
+def test_perturb_bs_fe32_vs_oracle(ctx, case):
+    """Burning Ship with FP32-mantissa + int32-exponent deltas: iteration
+    counts agree with the FP64 oracle on >= 99 % of the pixels (the loop, its
+    sign tests and the BLA are the reference's; only the arithmetic differs)."""
+    d = load(case)
+    Z, sr, si = _run_bs(ctx, d, "fe32")
+    agree = float(np.mean(si == d["stop_iter"]))
+    assert agree >= 0.99, agree
+    assert np.mean(sr == d["stop_reason"]) >= 0.99
+    # z at the last iteration: the FP32 rounding of dz (2^-24 relative) is
+    # amplified by the orbit's derivative on the way out (these pixels escape
+    # after ~2200 iterations near the boundary).  Measured on pert_bs_1,
+    # relative to |z|: median 1.2e-4, 90th percentile 4.5e-3, worst 7e-2
+    same = (si == d["stop_iter"]).ravel()
+    z = Z[0][same] + 1j * Z[1][same]
+    zo = d["Z"][0].ravel()[same] + 1j * d["Z"][1].ravel()[same]
+    err = np.abs(z - zo) / np.abs(zo)              # relative to |z|
+    assert np.median(err) <= 1e-3, np.median(err)
+    assert np.percentile(err, 90) <= 2e-2 and np.max(err) <= 0.2, (np.percentile(err, 90), err.max())
+
+
 @pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4"])
 def test_perturb_bs_vs_oracle(ctx, case):
     from fractalshades_gb300 import _native as nat
