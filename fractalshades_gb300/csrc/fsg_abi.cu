@@ -35,6 +35,9 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
 void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
                       int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
                       cudaStream_t s);
+void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
+                     const double *dYa, const double *dYb, int4 *hf, cudaStream_t s);
+void fsg_build_bs_fr_bla(const double *Mbs, int bla_len, int4 *blaf, cudaStream_t s);
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
@@ -142,8 +145,8 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
         if (calc->bla && t.ref->host.bla_len <= 0)
             return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference has no BLA tree");
     }
-    if (t.dzndc_scale_e != 0 && (!perturb || calc->flavor != 0))
-        return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e applies to the power-2 Mandelbrot perturbation only");
+    if (t.dzndc_scale_e != 0 && !perturb)
+        return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e applies to the perturbation loops only");
     if (t.dzndc_scale_e < -100000 || t.dzndc_scale_e > 100000)
         return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e out of range");
     if (perturb && calc->flavor != 0) {
@@ -429,8 +432,6 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (d->n_xr < 0 || (d->n_xr > 0 && (!d->xr_idx || !d->xr_m || !d->xr_e)))
         return set_err(ctx, FSG_ERR_ARG, "bad Xrange side table");
     if (d->flavor < 0 || d->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
-    if (d->flavor != 0 && d->n_xr > 0)
-        return set_err(ctx, FSG_ERR_ARG, "Burning Ship references with an Xrange side table are not supported");
     const int len = (int)d->len;
     // the iteration index w never passes min(order, div_iter) <= len, so every
     // orbit read stays inside [0, len] (slot len is a zero pad)
@@ -469,11 +470,13 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (d->n_xr > 0) {
         slot.assign(len + 1, -1);
         for (int k = 0; k < d->n_xr; k++) slot[d->xr_idx[k]] = k;
-        RA(xr_slot, len + 1); RA(xr_m, d->n_xr); RA(xr_e, d->n_xr);
+        // BS: one exponent per coordinate
+        const int ne = d->flavor == 0 ? d->n_xr : 2 * d->n_xr;
+        RA(xr_slot, len + 1); RA(xr_m, d->n_xr); RA(xr_e, ne);
         // stream-ordered like the allocations (pageable sources: staged before return)
         RCK(cudaMemcpyAsync(xr_slot, slot.data(), 4 * (size_t)(len + 1), cudaMemcpyHostToDevice, s), "upload xr slots");
         RCK(cudaMemcpyAsync(xr_m, d->xr_m, 16 * (size_t)d->n_xr, cudaMemcpyHostToDevice, s), "upload xr mantissas");
-        RCK(cudaMemcpyAsync(xr_e, d->xr_e, 4 * (size_t)d->n_xr, cudaMemcpyHostToDevice, s), "upload xr exponents");
+        RCK(cudaMemcpyAsync(xr_e, d->xr_e, 4 * (size_t)ne, cudaMemcpyHostToDevice, s), "upload xr exponents");
     }
     R.xr_slot = xr_slot; R.xr_m = xr_m; R.xr_e = xr_e;
     // derivative paths
@@ -526,6 +529,14 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     }
     R.Zf = Zf; R.Zp = Zp; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f = bla_f;
     R.bla_first = bla_first; R.bla_first_step = bla_first_step; R.bla_nit = bla_nit;
+    // FP32+exp tables (Burning Ship)
+    int4 *bs_Zf = nullptr, *bs_hf = nullptr, *bs_blaf = nullptr;
+    if (d->flavor != 0) {
+        RA(bs_Zf, len + 1);
+        if (d->calc_dzndc) RA(bs_hf, 2 * (size_t)(len + 1));
+        if (R.bla_len > 0) RA(bs_blaf, 4 * (size_t)R.bla_len);
+    }
+    R.bs_Zf = bs_Zf; R.bs_hf = bs_hf; R.bs_blaf = bs_blaf;
     RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     // builds
@@ -536,6 +547,10 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
         fsg_build_paths_bs(r->dev, dXa, dXb, dYa, dYb, ldexp(d->scale_m, d->scale_e), s);
     }
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
+    if (d->flavor != 0) {
+        fsg_build_bs_fr(r->dev, len, bs_Zf, dXa, dXb, dYa, dYb, bs_hf, s);
+        fsg_build_bs_fr_bla(Mbs, R.bla_len, bs_blaf, s);
+    }
     if (d->flavor == 0) {
         fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
                             dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_f, bla_nit, bla_first,
@@ -599,7 +614,9 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
             RA(bla_first_step, (size_t)R.bla_nit);
         }
     }
-    R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla;
+    int4 *bs_blaf = nullptr;
+    if (R.flavor != 0 && R.bla_len > 0) RA(bs_blaf, 4 * (size_t)R.bla_len);
+    R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.bs_blaf = bs_blaf;
     R.bla_f = bla_f; R.bla_first = bla_first; R.bla_first_step = bla_first_step;
     RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
@@ -608,6 +625,8 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
         if (R.flavor == 0)
             fsg_build_fe_bla(r->dev, Mbla, rbla, R.bla_len, bla_f, R.bla_nit, bla_first,
                              bla_first_step, s);
+        else
+            fsg_build_bs_fr_bla(Mbs, R.bla_len, bs_blaf, s);
     }
     RCK(cudaGetLastError(), "BLA kernels");
     // no host wait: launches and downloads that use r wait for this event

@@ -114,6 +114,44 @@ FSG_DEV bool abs_le(fr a, fr b) {
     return a.e != b.e ? a.e < b.e : fabsf(a.m) <= fabsf(b.m);
 }
 
+// v * 2^k (k = 0: v)
+FSG_DEV double scale2(double v, int k) { return k == 0 ? v : ldexp_d(v, k); }
+FSG_DEV fr scale2(fr v, int k) { if (v.m != 0.f) v.e += k; return v; }
+
+// Reads of the reference's tables in the loop's real type: the double
+// tables themselves, or their fr copies (orbit values from the Xrange side
+// table where the orbit holds one)
+template <class T> struct BSRef;
+template <> struct BSRef<double> {
+    static FSG_DEV void orbit(const RefDev &R, int w, double &X, double &Y) {
+        double2 z = __ldg(&R.Zn[w]); X = z.x; Y = z.y;
+    }
+    static FSG_DEV void hess(const RefDev &R, int w, double &a, double &b, double &c, double &d) {
+        a = __ldg(&R.dXa[w]); b = __ldg(&R.dXb[w]); c = __ldg(&R.dYa[w]); d = __ldg(&R.dYb[w]);
+    }
+    static FSG_DEV void bla(const RefDev &R, int ib, double M[8]) {
+        const double *p = R.Mbla_bs + 8 * ib;
+        for (int k = 0; k < 8; k++) M[k] = __ldg(p + k);
+    }
+};
+template <> struct BSRef<fr> {
+    static FSG_DEV fr lo(int4 v) { fr r; r.m = __int_as_float(v.x); r.e = v.y; return r; }
+    static FSG_DEV fr hi(int4 v) { fr r; r.m = __int_as_float(v.z); r.e = v.w; return r; }
+    static FSG_DEV void orbit(const RefDev &R, int w, fr &X, fr &Y) {
+        int4 v = __ldg(&R.bs_Zf[w]); X = lo(v); Y = hi(v);
+    }
+    static FSG_DEV void hess(const RefDev &R, int w, fr &a, fr &b, fr &c, fr &d) {
+        int4 p = __ldg(&R.bs_hf[2 * w]), q = __ldg(&R.bs_hf[2 * w + 1]);
+        a = lo(p); b = hi(p); c = lo(q); d = hi(q);
+    }
+    static FSG_DEV void bla(const RefDev &R, int ib, fr M[8]) {
+        for (int k = 0; k < 4; k++) {
+            int4 v = __ldg(&R.bs_blaf[4 * ib + k]);
+            M[2 * k] = lo(v); M[2 * k + 1] = hi(v);
+        }
+    }
+};
+
 // burning_ship.py:19-60 diffabs(X, x) = |X + x| - |X| and its derivatives
 template <class T> FSG_DEV T diffabs(T X, T x) {
     if (ge0(X)) { if (ge0(X + x)) return 1. * x; else return -(2. * X + x); }
@@ -244,16 +282,15 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             // underflows, perturbation.py:1123-1135)
             int step = bla_lookup(R, hypot(to_d(xn), to_d(yn)), w, ib);
             if (step != 0) {
-                const double *M = R.Mbla_bs + 8 * ib;
-                T M0 = from_d<T>(__ldg(M)), M1 = from_d<T>(__ldg(M + 1));
-                T M2 = from_d<T>(__ldg(M + 2)), M3 = from_d<T>(__ldg(M + 3));
+                T M[8];
+                BSRef<T>::bla(R, ib, M);
                 n += step; w = (w + step) % order;
-                T nx = M0 * xn + M1 * yn + from_d<T>(__ldg(M + 4)) * a + from_d<T>(__ldg(M + 5)) * b;
-                T ny = M2 * xn + M3 * yn + from_d<T>(__ldg(M + 6)) * a + from_d<T>(__ldg(M + 7)) * b;
+                T nx = M[0] * xn + M[1] * yn + M[4] * a + M[5] * b;
+                T ny = M[2] * xn + M[3] * yn + M[6] * a + M[7] * b;
                 xn = nx; yn = ny;
                 if (hess) {
-                    T xa = M0 * h[0] + M1 * h[2], xb = M0 * h[1] + M1 * h[3];
-                    T ya = M2 * h[0] + M3 * h[2], yb = M2 * h[1] + M3 * h[3];
+                    T xa = M[0] * h[0] + M[1] * h[2], xb = M[0] * h[1] + M[1] * h[3];
+                    T ya = M[2] * h[0] + M[3] * h[2], yb = M[2] * h[1] + M[3] * h[3];
                     h[0] = xa; h[1] = xb; h[2] = ya; h[3] = yb;
                 }
                 nbla++;
@@ -262,29 +299,28 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         }
         n += 1;
         nfull++;
-        double2 Zr = __ldg(&R.Zn[w]);
-        const T X = from_d<T>(Zr.x), Y = from_d<T>(Zr.y);
+        T X, Y;
+        BSRef<T>::orbit(R, w, X, Y);
         if (hess) {
             T Xa = from_d<T>(0.), Xb = from_d<T>(0.), Ya = from_d<T>(0.), Yb = from_d<T>(0.);
-            if (!dyn) {
-                Xa = from_d<T>(__ldg(&R.dXa[w])); Xb = from_d<T>(__ldg(&R.dXb[w]));
-                Ya = from_d<T>(__ldg(&R.dYa[w])); Yb = from_d<T>(__ldg(&R.dYb[w]));
-            }
+            if (!dyn) BSRef<T>::hess(R, w, Xa, Xb, Ya, Yb);
             bs_hess<T>(flavor, h, xn, yn, X, Y, Xa, Xb, Ya, Yb);
         }
         bs_zn<T>(flavor, xn, yn, X, Y, a, b);
         if (n >= C.max_iter) { stop = 0; break; }
         w += 1;
         if (w >= order) w = w % order;
-        double2 Zs = __ldg(&R.Zn[w]);
-        T XX = xn + from_d<T>(Zs.x), YY = yn + from_d<T>(Zs.y);
+        T Xs, Ys;
+        BSRef<T>::orbit(R, w, Xs, Ys);
+        T XX = xn + Xs, YY = yn + Ys;
         const double XXd = to_d(XX), YYd = to_d(YY);
         if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
         if (w >= div_iter - 1) {
             xn = XX; yn = YY;
             if (hess) {
-                h[0] += from_d<T>(__ldg(&R.dXa[w])); h[1] += from_d<T>(__ldg(&R.dXb[w]));
-                h[2] += from_d<T>(__ldg(&R.dYa[w])); h[3] += from_d<T>(__ldg(&R.dYb[w]));
+                T Ha, Hb, Hc, Hd;
+                BSRef<T>::hess(R, w, Ha, Hb, Hc, Hd);
+                h[0] += Ha; h[1] += Hb; h[2] += Hc; h[3] += Hd;
             }
             w = 0; nreb++; continue;
         }
@@ -292,18 +328,23 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         if (dyn) {
             xn = XX; yn = YY;
             if (hess) {
-                h[0] += from_d<T>(__ldg(&R.dXa[w])); h[1] += from_d<T>(__ldg(&R.dXb[w]));
-                h[2] += from_d<T>(__ldg(&R.dYa[w])); h[3] += from_d<T>(__ldg(&R.dYb[w]));
+                T Ha, Hb, Hc, Hd;
+                BSRef<T>::hess(R, w, Ha, Hb, Hc, Hd);
+                h[0] += Ha; h[1] += Hb; h[2] += Hc; h[3] += Hd;
             }
             w = 0; nreb++; continue;
         }
     }
-    double2 Zr = __ldg(&R.Zn[w]);
-    const double xo = to_d(xn + from_d<T>(Zr.x)), yo = to_d(yn + from_d<T>(Zr.y));
+    T Xe, Ye;
+    BSRef<T>::orbit(R, w, Xe, Ye);
+    const double xo = to_d(xn + Xe), yo = to_d(yn + Ye);
     double hd[4] = {0., 0., 0., 0.};
     if (hess) {
-        hd[0] = to_d(h[0] + from_d<T>(__ldg(&R.dXa[w]))); hd[1] = to_d(h[1] + from_d<T>(__ldg(&R.dXb[w])));
-        hd[2] = to_d(h[2] + from_d<T>(__ldg(&R.dYa[w]))); hd[3] = to_d(h[3] + from_d<T>(__ldg(&R.dYb[w])));
+        // the Hessian in the tile's unit: the reference's scale times 2^dzs
+        T Ha, Hb, Hc, Hd;
+        BSRef<T>::hess(R, w, Ha, Hb, Hc, Hd);
+        hd[0] = to_d(scale2(h[0] + Ha, Tl.dzs)); hd[1] = to_d(scale2(h[1] + Hb, Tl.dzs));
+        hd[2] = to_d(scale2(h[2] + Hc, Tl.dzs)); hd[3] = to_d(scale2(h[3] + Hd, Tl.dzs));
     }
     double *Z = (double *)Tl.Z;
     Z[ip] = xo; Z[np + ip] = yo;

@@ -16,8 +16,9 @@ struct RefDev {
     int n_xr;
     const double2 *Zn;          // [len + 1], Zn[len] = 0 (read when w reaches len)
     const int *xr_slot;         // [len + 1]: -1 or index in the side table
-    const double2 *xr_m;        // [n_xr] Xrange mantissas (M2)
-    const int *xr_e;
+    const double2 *xr_m;        // [n_xr] Xrange mantissas (M2: complex; BS: as doubles,
+                                // [n_xr] x then [n_xr] y)
+    const int *xr_e;            // [n_xr] (M2) or [2 n_xr] x then y (BS) exponents
     // derivative paths, standard form
     const double2 *dZndc;       // [len + 1]
     const double2 *dZndz;       // [len + 2] (slot len = wrapped value)
@@ -45,6 +46,10 @@ struct RefDev {
                                 // stage ref_BLA_get tries there: its bla_f record
     const int *bla_first_step;  // [bla_nit] that stage's step, 0 when none is tried
     int bla_nit;                // (len >> 3) + 1
+    // Burning Ship FP32+exp tables: reals as {mantissa bits, exponent} pairs
+    const int4 *bs_Zf;          // [len + 1] {X, Y} (Xrange side-table values where present)
+    const int4 *bs_hf;          // [2 (len + 1)] {dXa, dXb}, {dYa, dYb}
+    const int4 *bs_blaf;        // [4 bla_len] the 8 BLA coefficients, two per int4
 };
 
 struct TileDev {

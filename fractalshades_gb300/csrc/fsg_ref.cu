@@ -13,6 +13,7 @@
 //   * the fe (FP32 mantissa + int32 exponent) copies used by the fast kernel.
 // Built with -fmad=false like the loops that consume these tables.
 #include "fsg_internal.cuh"
+#include "fsg_bs.cuh"
 
 // ---------------------------------------------------------------------------
 // derivative paths
@@ -308,6 +309,60 @@ __global__ void k_fe_bla_first(const RefDev *Rp, const int4 *F, int nit, int4 *F
         }
     }
     FF[2 * it] = h; FF[2 * it + 1] = p; FS[it] = step;
+}
+
+// ---------------------------------------------------------------------------
+// Burning Ship FP32+exp tables (fr pairs, fsg_bs.cuh)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int2 fr_pack(fr v) { return make_int2(__float_as_int(v.m), v.e); }
+__device__ __forceinline__ fr fr_of_xr(double m, int e) {
+    fr r = fr_from_d(m);
+    if (r.m != 0.f) r.e += e;
+    return r;
+}
+// orbit values, from the Xrange side table where the orbit holds one
+// (values below the double range, FP_loop.pyx:1828-1979)
+__global__ void k_bs_fr_orbit(const RefDev *Rp, int4 *out) {
+    const RefDev &R = *Rp;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > R.len) return;
+    fr x, y;
+    int s = (R.n_xr > 0 && i < R.len) ? R.xr_slot[i] : -1;
+    if (s >= 0) {
+        // planar layout: x mantissas / exponents, then y
+        const double *m = (const double *)R.xr_m;
+        x = fr_of_xr(m[s], R.xr_e[s]);
+        y = fr_of_xr(m[R.n_xr + s], R.xr_e[R.n_xr + s]);
+    }
+    else { x = fr_from_d(R.Zn[i].x); y = fr_from_d(R.Zn[i].y); }
+    int2 a = fr_pack(x), b = fr_pack(y);
+    out[i] = make_int4(a.x, a.y, b.x, b.y);
+}
+__global__ void k_bs_fr_paths(const double *dXa, const double *dXb, const double *dYa,
+                              const double *dYb, int n, int4 *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int2 a = fr_pack(fr_from_d(dXa[i])), b = fr_pack(fr_from_d(dXb[i]));
+    int2 c = fr_pack(fr_from_d(dYa[i])), d = fr_pack(fr_from_d(dYb[i]));
+    out[2 * i] = make_int4(a.x, a.y, b.x, b.y);
+    out[2 * i + 1] = make_int4(c.x, c.y, d.x, d.y);
+}
+__global__ void k_bs_fr_bla(const double *M, int n, int4 *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * n) return;
+    int2 a = fr_pack(fr_from_d(M[2 * i])), b = fr_pack(fr_from_d(M[2 * i + 1]));
+    out[i] = make_int4(a.x, a.y, b.x, b.y);
+}
+
+void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
+                     const double *dYa, const double *dYb, int4 *hf, cudaStream_t s) {
+    int tb = 256;
+    k_bs_fr_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
+    if (hf) k_bs_fr_paths<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dXa, dXb, dYa, dYb, len + 1, hf);
+}
+void fsg_build_bs_fr_bla(const double *Mbs, int bla_len, int4 *blaf, cudaStream_t s) {
+    int tb = 256;
+    if (blaf && bla_len > 0) k_bs_fr_bla<<<(4 * bla_len + tb - 1) / tb, tb, 0, s>>>(Mbs, bla_len, blaf);
 }
 
 // ---------------------------------------------------------------------------

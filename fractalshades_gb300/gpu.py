@@ -80,10 +80,17 @@ class PerturbSpec:
     @property
     def mode(self):
         m = settings.precision_mode
+        if self.flavor != 0:
+            # Burning Ship: no Xrange kernel; below the double range the
+            # FP32 + exponent form is the one without underflow
+            if self.xr_detect_activated:
+                if m in ("fp64", "xr64"):
+                    raise ValueError("Burning Ship below dx = 1e-300 runs with "
+                                     "precision_mode 'auto' or 'fe32'")
+                return "fe32"
+            return "fp64" if m in ("auto", "xr64") else m
         if m == "auto":
             return "xr64" if self.xr_detect_activated else "fp64"
-        if self.flavor != 0 and m == "xr64":
-            return "fp64"
         return m
 
     def calc(self):
@@ -123,7 +130,8 @@ def _tile_for(fractal_args, spec, pix=None, xs=None, ys=None, Z=None, U=None, sr
     ref = fractal_args["ref"]
     kw = dict(lin_mat=fractal_args["lin_mat"], Z=Z, U=U, stop_reason=sr, stop_iter=si,
               ref=ref, dx_m=fractal_args["dx_m"], dx_e=fractal_args["dx_e"],
-              i_dzndz=spec.i_dzndz, i_dzndc=spec.i_dzndc, potential=pot, dem=dem)
+              i_dzndz=spec.i_dzndz, i_dzndc=spec.i_dzndc, potential=pot, dem=dem,
+              dzndc_scale_e=fractal_args.get("dzndc_scale_e", 0))
     if spec.flavor == 0:
         kw.update(drift_m=fractal_args["drift_m"], drift_e=fractal_args["drift_e"])
     else:

@@ -284,10 +284,6 @@ class Perturbation_burning_ship(PerturbationFractal):
 
     def FP_loop(self, NP_orbit, c0):
         max_orbit_iter = NP_orbit.shape[0] - 1
-        if self.xr_detect_activated:
-            raise NotImplementedError(
-                "Burning Ship perturbation below dx = 1e-300 (Xrange deltas) is not "
-                "supported by the GPU kernels")
         return fsFP.perturbation_nonholomorphic_FP_loop(
             NP_orbit.view(dtype=np.float64), self.xr_detect_activated, max_orbit_iter,
             self.M_divergence * 2, str(c0.real).encode("utf8"),
@@ -326,7 +322,7 @@ class Perturbation_burning_ship(PerturbationFractal):
 
         spec = PerturbSpec(flavor=self.flavor_int, max_iter=max_iter,
                            M_divergence=M_divergence, calc_dzndc=calc_hessian,
-                           bla=BLA_activated, xr_detect_activated=False,
+                           bla=BLA_activated, xr_detect_activated=self.xr_detect_activated,
                            nZ=len(complex_codes))
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}

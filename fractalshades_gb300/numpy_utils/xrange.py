@@ -102,3 +102,23 @@ def _as_scalar(v):
         return v
     rec = np.asarray(v).reshape(-1)[0]
     return XrScalar(rec["mantissa"].item(), int(rec["exp"]))
+
+
+def xr_table_xy(xr_dict):
+    """Burning Ship side table: indices and planar (x then y) mantissas and
+    exponents of the register {i: (x, y)} -- x, y given as (mantissa, exp)
+    pairs or as the reference's Xrange records."""
+    keys = sorted(xr_dict)
+    n = len(keys)
+    idx = np.array(keys, dtype=np.int32)
+    m = np.zeros(2 * n, dtype=np.float64)
+    e = np.zeros(2 * n, dtype=np.int32)
+    for k, key in enumerate(keys):
+        for j, v in enumerate(xr_dict[key]):
+            if isinstance(v, tuple):
+                mv, ev = float(v[0]), int(v[1])
+            else:
+                sc = _as_scalar(v)
+                mv, ev = float(np.real(sc.m)), int(sc.e)
+            m[j * n + k], e[j * n + k] = mv, ev
+    return idx, m, e

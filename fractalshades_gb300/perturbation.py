@@ -278,7 +278,8 @@ class PerturbationFractal(Fractal):
         refp = FP_params["ref_point"]
         driftx_xr = fsx.mpf_to_Xrange(self.x - refp.real)
         drifty_xr = fsx.mpf_to_Xrange(self.y - refp.imag)
-        return (Zn_path, has_xr, np.zeros(0, np.int32), None, ref_div_iter, ref_order,
+        idx, m, e = fsx.xr_table_xy(ref_xr_python)
+        return (Zn_path, has_xr, idx, (m, e), ref_div_iter, ref_order,
                 driftx_xr, drifty_xr, dx_xr)
 
     @staticmethod
@@ -314,6 +315,12 @@ class PerturbationFractal(Fractal):
                 "the reference calculation precicion.")
         bla_eps = self.BLA_eps
         xr = self.xr_detect_activated
+        # Burning Ship below the double range: the Jacobian paths at the
+        # scale m (dx = m 2^e), the tiles add 2^e (fsg_tile.dzndc_scale_e)
+        dzndc_scale_e = 0
+        if xr and not holomorphic:
+            scale = fsx.XrScalar(dx_xr.m, 0)
+            dzndc_scale_e = dx_xr.e
         ref = nat.Reference(
             gpu.context(), Zn_path, div_iter=ref_div_iter,
             order=(ref_order if ref_order < (1 << 62) else None),
@@ -327,7 +334,8 @@ class PerturbationFractal(Fractal):
         args = {"holomorphic": holomorphic, "spec": iterate, "ref": ref,
                 "lin_mat": self.lin_mat, "dx_m": dx_xr.m, "dx_e": dx_xr.e,
                 "interrupted": self._interrupted, "kc": kc,
-                "ref_div_iter": ref_div_iter, "ref_order": ref_order, "has_xr": has_xr}
+                "ref_div_iter": ref_div_iter, "ref_order": ref_order, "has_xr": has_xr,
+                "dzndc_scale_e": dzndc_scale_e}
         if holomorphic:
             args.update(drift_m=drift_xr.m, drift_e=drift_xr.e)
         else:

@@ -117,11 +117,12 @@ typedef struct {
     void *Z; int32_t nZ; int32_t i_dzndz; int32_t i_dzndc;
     int32_t *U; int8_t *stop_reason; int32_t *stop_iter;
     double *potential; double *dem;
-    /* power-2 Mandelbrot perturbation: the tile's dzndc unit is the
-       reference's derivative scale times 2^dzndc_scale_e (the derivative
-       recurrence is linear in its scale, so one reference serves views of
-       every width: the outputs dzndc and DEM are scaled exactly); 0 for the
-       reference's own scale.  Must be 0 for the Burning Ship and the
+    /* perturbation: the tile's derivative unit (M2 dzndc, BS Hessian) is
+       the reference's derivative scale times 2^dzndc_scale_e (the
+       derivative recurrences are linear in their scale, so one reference
+       serves views of every width, and a reference of unit scale serves
+       widths below the double range: the derivative outputs and DEM are
+       scaled exactly); 0 for the reference's own scale.  Must be 0 for the
        standard loop.  No counterpart in the reference (one scale per
        reference, perturbation.py:461-468). */
     int32_t dzndc_scale_e;
