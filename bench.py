@@ -220,6 +220,18 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter):
     return out
 
 
+def traffic_per_launch(nx):
+    """DRAM bytes of one FE32 launch from the committed ncu capture
+    (profiles/dram_fe32_config2_2048.md), for the 2048² workload it was
+    measured on; None for another size."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_fe32_config2_2048.json")) as f:
+            rec = json.load(f)
+    except (OSError, ValueError):
+        return None
+    return int(rec["bytes_per_launch"]) if nx == 2048 else None
+
+
 class ClockSampler:
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -551,7 +563,7 @@ def run_ours(args):
         "gpu_launches": int(args.steps),
         "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": peak32,
                      "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,
-                     "traffic": None,
+                     "traffic": traffic_per_launch(args.nx),
                      "peak_source": "measured FFMA-chain kernel on this GPU (fsg_peak_flops)",
                      "flops_per_step": {"full": FLOPS_FULL, "bla": FLOPS_BLA},
                      "executed_steps": {"full": st["full_steps"], "bla": st["bla_steps"]},
