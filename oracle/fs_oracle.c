@@ -265,6 +265,126 @@ EXPORT int orc_std_m2(int64_t npts, const double *pix, double cx, double cy,
 /* models/burning_ship.py:12-17 sgn (0 maps to +1) */
 static inline double sgn(double x) { return x < 0. ? -1. : 1.; }
 
+/* ------------------------------------------------------------------------- */
+/* Power-n Mandelbrot (models/mandelbrot_Mn.py).  nexp = 0 selects the power-2 */
+/* model's own closures (models/mandelbrot_M2.py), nexp >= 2 the Mn ones.      */
+/* ------------------------------------------------------------------------- */
+/* integer power of a complex as numpy's npy_cpow does for |n| < 100 (the
+ * reference's `zn ** deg_m1` on complex128 values): n = 1, 2, 3 directly,
+ * else binary powering from 1 */
+static inline cplx mn_ipow(cplx a, int n) {
+    if (n == 1) return a;
+    if (n == 2) return cmul(a, a);
+    if (n == 3) return cmul(a, cmul(a, a));
+    cplx aa = C(1., 0.), p = a;
+    int mask = 1;
+    for (;;) {
+        if (n & mask) aa = cmul(aa, p);
+        mask <<= 1;
+        if (n < mask || mask <= 0) break;
+        p = cmul(p, p);
+    }
+    return aa;
+}
+/* mandelbrot_Mn.py:645-652 dfdz = n z^(n-1) (products from z), M2: 2 z */
+static inline cplx mn_dfdz_c(int nexp, cplx z) {
+    if (nexp == 0) return rmul(2., z);
+    cplx t = z;
+    for (int k = 2; k < nexp; k++) t = cmul(t, z);
+    return rmul((double)nexp, t);
+}
+/* binomial coefficients C(n, k) as float64 (mandelbrot_Mn.py:636-640) */
+static inline void mn_binom(int n, double *Cb) {
+    for (int k = 0; k <= n; k++) {
+        double v = 1.;
+        for (int j = 1; j <= k; j++) v = v * (double)(n - k + j) / (double)j;
+        Cb[k] = v;
+    }
+}
+/* mandelbrot_Mn.py:660-672 p_iter_zn */
+static inline cplx mn_p_zn(int n, const double *Cb, cplx z, cplx ref, cplx c) {
+    cplx tmp = cmul(z, cadd(z, rmul(Cb[1], ref)));
+    cplx pk = ref;
+    for (int k = 2; k < n; k++) { pk = cmul(pk, ref); tmp = cmul(z, cadd(tmp, rmul(Cb[k], pk))); }
+    return cadd(tmp, c);
+}
+/* mandelbrot_Mn.py:674-733 p_iter_dzndz / p_iter_dzndc (same expansion) */
+static inline cplx mn_p_deriv(int n, const double *Cb, cplx z, cplx d, cplx ref, cplx rd) {
+    cplx mul = cadd(z, rmul(Cb[1], ref));
+    cplx tmp = cmul(z, mul);
+    cplx dt = cadd(cmul(d, mul), cmul(z, cadd(d, rmul(Cb[1], rd))));
+    cplx pk = ref;
+    for (int k = 2; k < n; k++) {
+        cplx dpk = cmul(rmul((double)k, pk), rd);
+        pk = cmul(pk, ref);
+        mul = cadd(tmp, rmul(Cb[k], pk));
+        dt = cadd(cmul(d, mul), cmul(z, cadd(dt, rmul(Cb[k], dpk))));
+        tmp = cmul(z, mul);
+    }
+    return dt;
+}
+
+/* the same closures on Xrange values (the reference's Xrange branch) */
+static inline xc mn_dfdz_x(int nexp, xc z) {
+    if (nexp == 0) return xr_mul_r(2., z);
+    xc t = z;
+    for (int k = 2; k < nexp; k++) t = xr_mul(t, z);
+    return xr_mul_r((double)nexp, t);
+}
+static inline xc mn_p_zn_x(int n, const double *Cb, xc z, xc ref, xc c) {
+    xc tmp = xr_mul(z, xr_add(z, xr_mul_r(Cb[1], ref)));
+    xc pk = ref;
+    for (int k = 2; k < n; k++) { pk = xr_mul(pk, ref); tmp = xr_mul(z, xr_add(tmp, xr_mul_r(Cb[k], pk))); }
+    return xr_add(tmp, c);
+}
+static inline xc mn_p_deriv_x(int n, const double *Cb, xc z, xc d, xc ref, xc rd) {
+    xc mul = xr_add(z, xr_mul_r(Cb[1], ref));
+    xc tmp = xr_mul(z, mul);
+    xc dt = xr_add(xr_mul(d, mul), xr_mul(z, xr_add(d, xr_mul_r(Cb[1], rd))));
+    xc pk = ref;
+    for (int k = 2; k < n; k++) {
+        xc dpk = xr_mul(xr_mul_r((double)k, pk), rd);
+        pk = xr_mul(pk, ref);
+        mul = xr_add(tmp, xr_mul_r(Cb[k], pk));
+        dt = xr_add(xr_mul(d, mul), xr_mul(z, xr_add(dt, xr_mul_r(Cb[k], dpk))));
+        tmp = xr_mul(z, mul);
+    }
+    return dt;
+}
+
+/*
+ * Standard power-n Mandelbrot: core.py:2935-3004 numba_cycles / numba_iterate
+ * with models/mandelbrot_Mn.py:317-355 iterate_once (calc_d2zndc2 False).
+ */
+EXPORT int orc_std_mn(int64_t npts, const double *pix, double cx, double cy,
+                      const double *lin_mat, double dx, int64_t max_iter,
+                      double M2, double eps2, int32_t nexp, double *Z, int32_t *stop_iter,
+                      int8_t *stop_reason) {
+    cplx *Zc = (cplx *)Z;
+    const double deg = (double)nexp;
+    for (int64_t i = 0; i < npts; i++) {
+        cplx c = c_from_pix(C(pix[2 * i], pix[2 * i + 1]), lin_mat, dx, C(cx, cy));
+        cplx zn = Zc[i], dzndz = Zc[npts + i], dzndc = Zc[2 * npts + i];
+        int64_t n = 0; int8_t reason = -1;
+        for (;;) {
+            n += 1;
+            if (n >= max_iter) { reason = 0; break; }
+            cplx zm1 = mn_ipow(zn, nexp - 1);
+            cplx zm = cmul(zm1, zn);
+            dzndc = caddr(cmul(rmul(deg, dzndc), zm1), 1.);
+            dzndz = cmul(rmul(deg, dzndz), zm1);
+            zn = cadd(zm, c);
+            if (n == 1) dzndz = C(1., 0.);
+            if (zn.re * zn.re + zn.im * zn.im > M2) { reason = 1; break; }
+            if (dzndz.re * dzndz.re + dzndz.im * dzndz.im < eps2) { reason = 2; break; }
+        }
+        Zc[i] = zn; Zc[npts + i] = dzndz; Zc[2 * npts + i] = dzndc;
+        stop_iter[i] = (int32_t)n; stop_reason[i] = reason;
+    }
+    return 0;
+}
+
+
 /*
  * Standard Burning Ship family: core.py:3007-3056 numba_iterate_BS,
  * models/burning_ship.py:350-423 iterate_once (flavors 1..5).
@@ -374,7 +494,7 @@ static void combine_bla(cplx *M, double *r, double kc, int stg, int64_t len, dou
  * r [2L] with L = len // 8.  Returns stages.
  */
 EXPORT int32_t orc_make_bla_m2(const double *Zn, int64_t len, double kc, double eps,
-                               double *M_out, double *r_out) {
+                               double *M_out, double *r_out, int32_t nexp) {
     const int64_t kcomp = 1 << STG_COMPRESSED;
     int64_t L = len / kcomp;
     cplx *M = (cplx *)M_out;
@@ -385,7 +505,7 @@ EXPORT int32_t orc_make_bla_m2(const double *Zn, int64_t len, double kc, double 
         memset(tM, 0, sizeof(tM)); memset(tr, 0, sizeof(tr));
         for (int64_t j = 0; j < kcomp; j++) {
             cplx z = C(Zn[2 * (i * kcomp + j)], Zn[2 * (i * kcomp + j) + 1]);
-            tM[2 * (2 * j)] = rmul(2., z);
+            tM[2 * (2 * j)] = mn_dfdz_c(nexp, z);
             tM[2 * (2 * j) + 1] = C(1., 0.);
             tr[2 * j] = eps * hypot(tM[2 * (2 * j)].re, tM[2 * (2 * j)].im);
         }
@@ -512,7 +632,8 @@ EXPORT void orc_dzndc_path_m2(const double *Zn, int64_t len, int64_t ref_div_ite
                               int32_t n_xr, const int32_t *xr_idx, const double *xr_re,
                               const double *xr_im, const int32_t *xr_e,
                               double scale_m, int32_t scale_e,
-                              double *out_std, double *out_re, double *out_im, int32_t *out_e) {
+                              double *out_std, double *out_re, double *out_im, int32_t *out_e,
+                              int32_t nexp) {
     int64_t valid = len < ref_div_iter ? len : ref_div_iter;
     xr_table t = {n_xr, xr_idx, xr_re, xr_im, xr_e};
     int has_xr = n_xr > 0;
@@ -524,7 +645,7 @@ EXPORT void orc_dzndc_path_m2(const double *Zn, int64_t len, int64_t ref_div_ite
             xc zx; cplx zs = C(Zn[2 * (i - 1)], Zn[2 * (i - 1) + 1]);
             if (!(has_xr && xr_lookup(&t, i - 1, &zx))) zx = xr_from_c(zs);
             xc prev = {out_re[i - 1], out_im[i - 1], out_e[i - 1]};
-            xc v = xr_add_xf(xr_mul(xr_mul_r(2., zx), prev), scale);
+            xc v = xr_add_xf(xr_mul(mn_dfdz_x(nexp, zx), prev), scale);
             out_re[i] = v.re; out_im[i] = v.im; out_e[i] = v.e;
         }
         i -= 1;
@@ -532,7 +653,7 @@ EXPORT void orc_dzndc_path_m2(const double *Zn, int64_t len, int64_t ref_div_ite
             /* the wrapped value uses the standard orbit value (perturbation.py:2320) */
             cplx zs = C(Zn[2 * i], Zn[2 * i + 1]);
             xc prev = {out_re[i], out_im[i], out_e[i]};
-            xc v = xr_add_xf(xr_mul_s(rmul(2., zs), prev), scale);
+            xc v = xr_add_xf(xr_mul_s(mn_dfdz_c(nexp, zs), prev), scale);
             out_re[0] = v.re; out_im[0] = v.im; out_e[0] = v.e;
         }
     } else {
@@ -540,10 +661,10 @@ EXPORT void orc_dzndc_path_m2(const double *Zn, int64_t len, int64_t ref_div_ite
         cplx *o = (cplx *)out_std;
         for (int64_t k = 0; k < len; k++) o[k] = C(0., 0.);
         for (i = 1; i < valid; i++)
-            o[i] = caddr(cmul(rmul(2., C(Zn[2 * (i - 1)], Zn[2 * (i - 1) + 1])), o[i - 1]), scale);
+            o[i] = caddr(cmul(mn_dfdz_c(nexp, C(Zn[2 * (i - 1)], Zn[2 * (i - 1) + 1])), o[i - 1]), scale);
         i -= 1;
         if (i == ref_order - 1)
-            o[0] = caddr(cmul(rmul(2., C(Zn[2 * i], Zn[2 * i + 1])), o[i]), scale);
+            o[0] = caddr(cmul(mn_dfdz_c(nexp, C(Zn[2 * i], Zn[2 * i + 1])), o[i]), scale);
     }
 }
 
@@ -551,7 +672,8 @@ EXPORT void orc_dzndc_path_m2(const double *Zn, int64_t len, int64_t ref_div_ite
 EXPORT void orc_dzndz_path_m2(const double *Zn, int64_t len, int64_t ref_div_iter,
                               int32_t xr_mode, int32_t n_xr, const int32_t *xr_idx,
                               const double *xr_re, const double *xr_im, const int32_t *xr_e,
-                              double *out_std, double *out_re, double *out_im, int32_t *out_e) {
+                              double *out_std, double *out_re, double *out_im, int32_t *out_e,
+                              int32_t nexp) {
     int64_t valid = len < ref_div_iter ? len : ref_div_iter;
     xr_table t = {n_xr, xr_idx, xr_re, xr_im, xr_e};
     int has_xr = n_xr > 0;
@@ -563,23 +685,23 @@ EXPORT void orc_dzndz_path_m2(const double *Zn, int64_t len, int64_t ref_div_ite
             xc zx; cplx zs = C(Zn[2 * (i - 1)], Zn[2 * (i - 1) + 1]);
             if (!(has_xr && xr_lookup(&t, i - 1, &zx))) zx = xr_from_c(zs);
             xc prev = {out_re[i - 1], out_im[i - 1], out_e[i - 1]};
-            xc v = xr_mul(xr_mul_r(2., zx), prev);
+            xc v = xr_mul(mn_dfdz_x(nexp, zx), prev);
             out_re[i] = v.re; out_im[i] = v.im; out_e[i] = v.e;
         }
         i -= 1;
         xc zx; cplx zs = C(Zn[2 * i], Zn[2 * i + 1]);
         if (!(has_xr && xr_lookup(&t, i, &zx))) zx = xr_from_c(zs);
         xc prev = {out_re[i], out_im[i], out_e[i]};
-        xc v = xr_mul(xr_mul_r(2., zx), prev);
+        xc v = xr_mul(mn_dfdz_x(nexp, zx), prev);
         out_re[len] = v.re; out_im[len] = v.im; out_e[len] = v.e;
     } else {
         cplx *o = (cplx *)out_std;
         for (int64_t k = 0; k <= len; k++) o[k] = C(0., 0.);
         o[1] = C(1., 0.);
         for (i = 2; i < valid; i++)
-            o[i] = cmul(rmul(2., C(Zn[2 * (i - 1)], Zn[2 * (i - 1) + 1])), o[i - 1]);
+            o[i] = cmul(mn_dfdz_c(nexp, C(Zn[2 * (i - 1)], Zn[2 * (i - 1) + 1])), o[i - 1]);
         i -= 1;
-        o[len] = cmul(rmul(2., C(Zn[2 * i], Zn[2 * i + 1])), o[i]);
+        o[len] = cmul(mn_dfdz_c(nexp, C(Zn[2 * i], Zn[2 * i + 1])), o[i]);
     }
 }
 
@@ -626,6 +748,8 @@ typedef struct {
     int32_t i_dzndz; int32_t i_dzndc; int32_t dzndz_carryover;
     /* pixel mapping (perturbation.py:2214-2230, 2666-2672) */
     double lin_mat[4]; double dx_m; int32_t dx_e; double drift_re; double drift_im; int32_t drift_e;
+    /* 0: power-2 model (mandelbrot_M2.py closures); n >= 2: power-n (mandelbrot_Mn.py) */
+    int32_t nexp;
 } orc_pm2_args;
 
 static inline cplx path_c(const double *p, int64_t i) { return C(p[2 * i], p[2 * i + 1]); }
@@ -657,7 +781,9 @@ EXPORT int orc_perturb_m2(const orc_pm2_args *P, int64_t npts, const double *pix
     int64_t first_invalid = plen;
     if (div_iter < first_invalid) first_invalid = div_iter;
     if (order < first_invalid) first_invalid = order;
-
+    const int nexp = P->nexp;
+    double Cb[64];
+    if (nexp) mn_binom(nexp, Cb);
     for (int64_t ip = 0; ip < npts; ip++) {
         xc c_xr = pm_c_from_pix(C(pix[2 * ip], pix[2 * ip + 1]), P->lin_mat, dxr, drift);
         cplx c = xr_to_std(c_xr);
@@ -701,28 +827,34 @@ EXPORT int orc_perturb_m2(const orc_pm2_args *P, int64_t npts, const double *pix
             if (calc_dzndc) {
                 if (xr) {
                     xc rd = dyn ? xzero : path_x(P->dZndc_re, P->dZndc_im, P->dZndc_e, w);
-                    Zx[dzndc] = xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, Zx[zn]), Zx[dzndc]), xr_mul(rd, Zx[zn])));
+                    Zx[dzndc] = nexp ? mn_p_deriv_x(nexp, Cb, Zx[zn], Zx[dzndc], ref_zn_xr, rd)
+                                     : xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, Zx[zn]), Zx[dzndc]), xr_mul(rd, Zx[zn])));
                 } else {
                     cplx rd = path_c(P->dZndc, w);
                     if (dyn) rd = C(0., 0.);
-                    Z[dzndc] = rmul(2., cadd(cmul(cadd(ref_zn, Z[zn]), Z[dzndc]), cmul(rd, Z[zn])));
+                    Z[dzndc] = nexp ? mn_p_deriv(nexp, Cb, Z[zn], Z[dzndc], ref_zn, rd)
+                                    : rmul(2., cadd(cmul(cadd(ref_zn, Z[zn]), Z[dzndc]), cmul(rd, Z[zn])));
                 }
             }
             if (calc_dzndz) {
                 int64_t k = nullify ? 0 : w;
                 if (xr) {
                     xc rd = path_x(P->dZndz_re, P->dZndz_im, P->dZndz_e, k);
-                    Zx[dzndz] = xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, Zx[zn]), Zx[dzndz]), xr_mul(rd, Zx[zn])));
+                    Zx[dzndz] = nexp ? mn_p_deriv_x(nexp, Cb, Zx[zn], Zx[dzndz], ref_zn_xr, rd)
+                                     : xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, Zx[zn]), Zx[dzndz]), xr_mul(rd, Zx[zn])));
                 } else {
                     cplx rd = path_c(P->dZndz, k);
-                    Z[dzndz] = rmul(2., cadd(cmul(cadd(ref_zn, Z[zn]), Z[dzndz]), cmul(rd, Z[zn])));
+                    Z[dzndz] = nexp ? mn_p_deriv(nexp, Cb, Z[zn], Z[dzndz], ref_zn, rd)
+                                    : rmul(2., cadd(cmul(cadd(ref_zn, Z[zn]), Z[dzndz]), cmul(rd, Z[zn])));
                 }
             }
             if (xr) {
-                Zx[zn] = xr_add(xr_mul(Zx[zn], xr_add(Zx[zn], xr_mul_r(2., ref_zn_xr))), c_xr);
+                Zx[zn] = nexp ? mn_p_zn_x(nexp, Cb, Zx[zn], ref_zn_xr, c_xr)
+                              : xr_add(xr_mul(Zx[zn], xr_add(Zx[zn], xr_mul_r(2., ref_zn_xr))), c_xr);
                 Z[zn] = xr_to_std(Zx[zn]);
             } else {
-                Z[zn] = cadd(cmul(Z[zn], cadd(Z[zn], rmul(2., ref_zn))), c);
+                Z[zn] = nexp ? mn_p_zn(nexp, Cb, Z[zn], ref_zn, c)
+                             : cadd(cmul(Z[zn], cadd(Z[zn], rmul(2., ref_zn))), c);
             }
             w += 1;
             if (w >= order) w = w % order;

@@ -49,7 +49,7 @@ class PM2Args(ct.Structure):
         ("max_iter", I64), ("M2", F64), ("eps2", F64), ("xr_mode", I32),
         ("i_dzndz", I32), ("i_dzndc", I32), ("dzndz_carryover", I32),
         ("lin_mat", F64 * 4), ("dx_m", F64), ("dx_e", I32),
-        ("drift_re", F64), ("drift_im", F64), ("drift_e", I32),
+        ("drift_re", F64), ("drift_im", F64), ("drift_e", I32), ("nexp", I32),
     ]
 
 
@@ -72,13 +72,15 @@ def _declare(L):
     L.orc_std_bs.restype = ct.c_int
     L.orc_stages_bla.argtypes = [I64]
     L.orc_stages_bla.restype = I32
-    L.orc_make_bla_m2.argtypes = [P, I64, F64, F64, P, P]
+    L.orc_make_bla_m2.argtypes = [P, I64, F64, F64, P, P, I32]
     L.orc_make_bla_m2.restype = I32
     L.orc_make_bla_bs.argtypes = [P, I64, I32, F64, F64, P, P]
     L.orc_make_bla_bs.restype = I32
     L.orc_dzndc_path_m2.argtypes = [P, I64, I64, I64, I32, I32, P, P, P, P,
-                                    F64, I32, P, P, P, P]
-    L.orc_dzndz_path_m2.argtypes = [P, I64, I64, I32, I32, P, P, P, P, P, P, P, P]
+                                    F64, I32, P, P, P, P, I32]
+    L.orc_dzndz_path_m2.argtypes = [P, I64, I64, I32, I32, P, P, P, P, P, P, P, P, I32]
+    L.orc_std_mn.argtypes = [I64, P, F64, F64, P, F64, I64, F64, F64, I32, P, P, P]
+    L.orc_std_mn.restype = ct.c_int
     L.orc_dzndc_path_bs.argtypes = [P, I64, I64, I64, I32, F64, P, P, P, P]
     L.orc_perturb_m2.argtypes = [ct.POINTER(PM2Args), I64, P, P, I32, P, P, P]
     L.orc_perturb_m2.restype = ct.c_int
@@ -137,6 +139,19 @@ def std_m2(pix, center, lin_mat, dx, max_iter, M, eps):
     return Z, si, sr
 
 
+def std_mn(pix, center, lin_mat, dx, max_iter, M, eps, nexp):
+    """Standard power-n Mandelbrot (models/mandelbrot_Mn.py:317-355)."""
+    pix = _c(pix, np.complex128)
+    n = pix.size
+    Z = np.zeros((3, n), dtype=np.complex128)
+    si = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    lm = _c(lin_mat, np.float64).ravel()
+    lib().orc_std_mn(n, _p(pix), center.real, center.imag, _p(lm), dx,
+                     max_iter, M * M, eps * eps, int(nexp), _p(Z), _p(si), _p(sr))
+    return Z, si, sr
+
+
 def std_bs(pix, center, lin_mat, dx, flavor, max_iter, M):
     pix = _c(pix, np.complex128)
     n = pix.size
@@ -152,12 +167,13 @@ def std_bs(pix, center, lin_mat, dx, flavor, max_iter, M):
 # ---------------------------------------------------------------------------
 # Orbit-derived tables
 # ---------------------------------------------------------------------------
-def make_bla_m2(Zn, kc, eps):
+def make_bla_m2(Zn, kc, eps, nexp=0):
+    """nexp 0: the power-2 model (dfdz = 2 z); n >= 2: power n (n z^(n-1))."""
     Zn = _c(Zn, np.complex128)
     L = Zn.size // 8
     M = np.zeros(2 * L * 2, dtype=np.complex128)
     r = np.zeros(2 * L, dtype=np.float64)
-    st = lib().orc_make_bla_m2(_p(Zn), Zn.size, kc, eps, _p(M), _p(r))
+    st = lib().orc_make_bla_m2(_p(Zn), Zn.size, kc, eps, _p(M), _p(r), int(nexp))
     return M, r, 2 * L, st
 
 
@@ -178,7 +194,7 @@ def _xr_table(xr_idx, xr_m, xr_e):
 
 
 def dzndc_path_m2(Zn, ref_div_iter, ref_order, xr_mode, scale_m, scale_e,
-                  xr_idx=None, xr_m=None, xr_e=None):
+                  xr_idx=None, xr_m=None, xr_e=None, nexp=0):
     Zn = _c(Zn, np.complex128)
     n = Zn.size
     idx, re, im, e = _xr_table(xr_idx, xr_m, xr_e)
@@ -187,13 +203,13 @@ def dzndc_path_m2(Zn, ref_div_iter, ref_order, xr_mode, scale_m, scale_e,
     oe = np.zeros(n, dtype=np.int32)
     lib().orc_dzndc_path_m2(_p(Zn), n, ref_div_iter, ref_order, int(xr_mode),
                             idx.size, _p(idx), _p(re), _p(im), _p(e),
-                            scale_m, scale_e, _p(std), _p(ore), _p(oim), _p(oe))
+                            scale_m, scale_e, _p(std), _p(ore), _p(oim), _p(oe), int(nexp))
     if xr_mode:
         return _cx(ore, oim), oe
     return std
 
 
-def dzndz_path_m2(Zn, ref_div_iter, xr_mode, xr_idx=None, xr_m=None, xr_e=None):
+def dzndz_path_m2(Zn, ref_div_iter, xr_mode, xr_idx=None, xr_m=None, xr_e=None, nexp=0):
     Zn = _c(Zn, np.complex128)
     n = Zn.size
     idx, re, im, e = _xr_table(xr_idx, xr_m, xr_e)
@@ -202,7 +218,7 @@ def dzndz_path_m2(Zn, ref_div_iter, xr_mode, xr_idx=None, xr_m=None, xr_e=None):
     oe = np.zeros(n + 1, dtype=np.int32)
     lib().orc_dzndz_path_m2(_p(Zn), n, ref_div_iter, int(xr_mode), idx.size,
                             _p(idx), _p(re), _p(im), _p(e), _p(std), _p(ore),
-                            _p(oim), _p(oe))
+                            _p(oim), _p(oe), int(nexp))
     if xr_mode:
         return _cx(ore, oim), oe
     return std
@@ -224,7 +240,7 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
                drift_m, drift_e, max_iter, M, eps_stat, xr_mode,
                calc_dzndc=True, interior=False, bla=None, dZndc=None,
                dZndz=None, xr_idx=None, xr_m=None, xr_e=None,
-               carryover=False, Z0=None):
+               carryover=False, Z0=None, nexp=0):
     """bla: (M_bla complex flat, r_bla, stages) or None.  dZndc / dZndz are
     complex arrays (standard form) or (mantissa, exp) tuples (Xrange form)."""
     pix = _c(pix, np.complex128)
@@ -275,6 +291,7 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
         a.lin_mat[k] = lm[k]
     a.dx_m, a.dx_e = float(dx_m), int(dx_e)
     a.drift_re, a.drift_im, a.drift_e = float(np.real(drift_m)), float(np.imag(drift_m)), int(drift_e)
+    a.nexp = int(nexp)
     nZ = len(codes)
     Z = np.zeros((nZ, n), dtype=np.complex128) if Z0 is None else _c(Z0, np.complex128).copy()
     U = np.zeros((1, n), dtype=np.int32)

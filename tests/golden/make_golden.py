@@ -249,6 +249,44 @@ def mp_orbit(c, max_iter, M, need_xr, ref_orbit_len):
     return i, orbit, xr_dict
 
 
+def mp_orbit_n(c, nexp, max_iter, M, need_xr, ref_orbit_len):
+    """mp_orbit for z^n + c (FP_loop.pyx:255-421, mpc_pow_ui)."""
+    orbit = np.zeros(ref_orbit_len, dtype=np.complex128)
+    z = mpmath.mpc(0)
+    xr_dict = {}
+    i = 0
+    abs_i = 0.
+    for i in range(1, ref_orbit_len):
+        z = z ** nexp + c
+        x, y = float(z.real), float(z.imag)
+        orbit[i] = complex(x, y)
+        abs_i = np.hypot(x, y)
+        if abs_i > M:
+            break
+        if need_xr and abs_i < fs.settings.xrange_zoom_level:
+            xr_dict[i] = fsx.mpc_to_Xrange(z)
+    if i == ref_orbit_len - 1 and abs_i <= M:
+        i += 1
+    return i, orbit, xr_dict
+
+
+def mp_nucleus_n(nexp, p, dps, c0):
+    """Newton for f^p(0) = 0 with f = z^n + c, from c0."""
+    with mpmath.workdps(dps):
+        c = mpmath.mpc(c0)
+        for _ in range(200):
+            z = mpmath.mpc(0)
+            d = mpmath.mpc(0)
+            for _k in range(p):
+                d = nexp * z ** (nexp - 1) * d + 1
+                z = z ** nexp + c
+            dc = z / d
+            c = c - dc
+            if abs(dc) < mpmath.mpf(10) ** (-dps + 5):
+                break
+        return c
+
+
 def mp_nucleus(p, dps, seed_frac=0.):
     """Newton for a period-p nucleus from a start outside the 1/p bulb root."""
     with mpmath.workdps(dps):
@@ -275,6 +313,25 @@ def store_orbit(f, ref_point, order, max_iter, M):
         ref_orbit_len = min(order, ref_orbit_len)
     i, orbit, xr_dict = mp_orbit(ref_point, max_iter, 2 * M,
                                  f.xr_detect_activated, ref_orbit_len)
+    init_kwargs = f.init_kwargs
+    del init_kwargs["directory"]
+    FP_params = {
+        "ref_point": ref_point, "dps": mpmath.mp.dps, "order": order,
+        "max_iter": max_iter, "FP_code": f.FP_code, "partials": {},
+        "xr": xr_dict, "div_iter": i, "init_kwargs": init_kwargs,
+        "ref_orbit_len": ref_orbit_len,
+    }
+    f.save_ref_point(FP_params, orbit)
+    return FP_params, orbit
+
+
+def store_orbit_n(f, nexp, ref_point, order, max_iter, M):
+    """store_orbit for z^n + c."""
+    ref_orbit_len = max_iter + 1
+    if order is not None:
+        ref_orbit_len = min(order, ref_orbit_len)
+    i, orbit, xr_dict = mp_orbit_n(ref_point, nexp, max_iter, 2 * M,
+                                   f.xr_detect_activated, ref_orbit_len)
     init_kwargs = f.init_kwargs
     del init_kwargs["directory"]
     FP_params = {
@@ -361,6 +418,72 @@ def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
         xr = f.xr_detect_activated
         res = dict(
             pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si,
+            Zn=Zn_path, ref_div_iter=ref_div_iter, ref_order=ref_order,
+            xr_mode=int(xr), lin_mat=lin_mat,
+            dx_m=np.asarray(dx_xr._mantissa)[0],
+            dx_e=np.asarray(dx_xr._exp)[0],
+            drift_m=np.asarray(drift_xr._mantissa)[0],
+            drift_e=np.asarray(drift_xr._exp)[0],
+            kc_m=np.asarray(kc._mantissa)[0], kc_e=np.asarray(kc._exp)[0],
+            max_iter=max_iter, M=M, eps_stat=eps_stat, bla_eps=bla_eps,
+            interior=int(interior), codes=np.array(f.codes[0]),
+            M_bla=M_bla, r_bla=r_bla, stages_bla=stages_bla,
+            xr_idx=ref_index_xr,
+        )
+        m, e = xr_arrays(ref_xr)
+        res["xr_m"], res["xr_e"] = m, e
+        if xr:
+            res["dZndc_m"], res["dZndc_e"] = xr_arrays(dZndc_path)
+            if interior:
+                res["dZndz_m"], res["dZndz_e"] = xr_arrays(dZndz_path)
+        else:
+            res["dZndc"] = dZndc_path
+            if interior:
+                res["dZndz"] = dZndz_path
+        np.savez_compressed(out, **res)
+
+
+def golden_std_mn(out):
+    """Standard power-n Mandelbrot (models/mandelbrot_Mn.py:20-176), n = 3, 4."""
+    res = {}
+    for nexp in (3, 4):
+        with tempfile.TemporaryDirectory() as d:
+            f = fsm.Mandelbrot_N(d, exponent=nexp)
+            f.zoom(x=0., y=0., dx=3., nx=40, xy_ratio=1., theta_deg=0.)
+            f.calc_std_div(calc_name="std", subset=None, max_iter=300,
+                           M_divergence=1000., epsilon_stationnary=0.01)
+            c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+            res[f"pix_{nexp}"] = c_pix
+            res[f"Z_{nexp}"] = Z
+            res[f"stop_reason_{nexp}"] = sr
+            res[f"stop_iter_{nexp}"] = si
+            res["lin_mat"] = f.lin_mat
+    np.savez_compressed(out, center=np.array([0., 0.]), dx=3., max_iter=300, M=1000.,
+                        eps=0.01, **res)
+
+
+def golden_perturb_mn(out, *, nexp, x, y, dx, nx, precision, order, max_iter,
+                      interior, bla_eps=1e-6, eps_stat=1e-3, M=1000., ref_shift=0j):
+    """Perturbation power-n Mandelbrot (models/mandelbrot_Mn.py:387-740)."""
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Perturbation_mandelbrot_N(d, exponent=nexp)
+        f.zoom(precision=precision, x=x, y=y, dx=dx, nx=nx, xy_ratio=1.,
+               theta_deg=0., projection=fs.projection.Cartesian())
+        ref_point = mpmath.mpc(x, y) + mpmath.mpc(ref_shift) * mpmath.mpf(dx)
+        f.max_iter = max_iter
+        f.M_divergence = M
+        store_orbit_n(f, nexp, ref_point, order, max_iter, M)
+        f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
+                       M_divergence=M, epsilon_stationnary=eps_stat,
+                       BLA_eps=bla_eps, interior_detect=interior,
+                       calc_dzndc=True)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "pert")
+        (_, _, _, Zn_path, dZndc_path, dZndz_path, has_xr, ref_index_xr,
+         ref_xr, ref_div_iter, ref_order, drift_xr, dx_xr, _proj, lin_mat,
+         lin_scale_xr, kc, M_bla, r_bla, bla_len, stages_bla, _m, _i) = cia
+        xr = f.xr_detect_activated
+        res = dict(
+            pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si, nexp=nexp,
             Zn=Zn_path, ref_div_iter=ref_div_iter, ref_order=ref_order,
             xr_mode=int(xr), lin_mat=lin_mat,
             dx_m=np.asarray(dx_xr._mantissa)[0],
@@ -558,6 +681,12 @@ def main():
         ref_shift=0.31 - 0.27j, x_offset="1e-14")
     print("pert_m2_xr_div done", flush=True)
 
+    # Power-n Mandelbrot, standard loop (n = 3, 4)
+    mpmath.mp.dps = 50
+    golden_std_mn(os.path.join(HERE, "std_mn.npz"))
+    print("std_mn done", flush=True)
+    mn_cases()
+
     # Perturbation Burning Ship (flavors 1 and 4), standard branch, around a
     # point whose orbit escapes after ~2200 iterations
     mpmath.mp.dps = 30
@@ -569,5 +698,41 @@ def main():
         print(f"pert_bs_{fl} done", flush=True)
 
 
+def mn_cases():
+    """Perturbation power-n Mandelbrot: n = 3 around a period-10 nucleus with
+    interior detection (standard branch); n = 3 with an off-centre escaping
+    reference (rebases); n = 4 in the Xrange branch (dx < 1e-300)."""
+    # nuclei found by an order-1 ball (radius 1e-3) around seeded points and
+    # Newton on that period (periods 10: the reference's BLA lookup needs an
+    # orbit of at least 9 points, perturbation.py:2138-2149)
+    dps = 60
+    mpmath.mp.dps = dps
+    c3 = mp_nucleus_n(3, 10, dps, mpmath.mpc("0.64287667998175895118", "0.25145447487965245909"))
+    golden_perturb_mn(
+        os.path.join(HERE, "pert_mn3_cycle.npz"), nexp=3,
+        x=str(c3.real), y=str(c3.imag), dx="2.5e-4", nx=16,
+        precision=dps, order=10, max_iter=3000, interior=True)
+    print("pert_mn3_cycle done", flush=True)
+    mpmath.mp.dps = 30
+    golden_perturb_mn(
+        os.path.join(HERE, "pert_mn3_div.npz"), nexp=3,
+        x=str(c3.real + mpmath.mpf("0.004")), y=str(c3.imag), dx="2.e-3", nx=16,
+        precision=30, order=None, max_iter=3000, interior=False, ref_shift=0.21 - 0.13j)
+    print("pert_mn3_div done", flush=True)
+    dps = 340
+    mpmath.mp.dps = dps
+    c4 = mp_nucleus_n(4, 10, dps, mpmath.mpc("-0.51534888699245770184", "0.46481172994907691405"))
+    golden_perturb_mn(
+        os.path.join(HERE, "pert_mn4_xr.npz"), nexp=4,
+        x=str(c4.real), y=str(c4.imag), dx="1.e-305", nx=4,
+        precision=dps, order=10, max_iter=600, interior=True)
+    print("pert_mn4_xr done", flush=True)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 2 and sys.argv[2] == "mn":
+        mpmath.mp.dps = 50
+        golden_std_mn(os.path.join(HERE, "std_mn.npz"))
+        mn_cases()
+    else:
+        main()

@@ -63,6 +63,19 @@ def test_std_m2_matches_reference_bit_exact():
     assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
 
 
+@pytest.mark.parametrize("nexp", [3, 4])
+def test_std_mn_matches_reference_bit_exact(nexp):
+    """Standard power-n loop (models/mandelbrot_Mn.py:317-355); the fixture's
+    `zn ** (n - 1)` ran as numpy's complex integer power."""
+    d = load("std_mn")
+    Z, si, sr = orc.std_mn(d[f"pix_{nexp}"], complex(*d["center"]), d["lin_mat"],
+                           float(d["dx"]), int(d["max_iter"]), float(d["M"]),
+                           float(d["eps"]), nexp)
+    assert np.array_equal(si, d[f"stop_iter_{nexp}"])
+    assert np.array_equal(sr, d[f"stop_reason_{nexp}"])
+    assert np.array_equal(Z.view(np.uint64), d[f"Z_{nexp}"].view(np.uint64))
+
+
 @pytest.mark.parametrize("flavor", [1, 2, 3, 4, 5])
 def test_std_bs_matches_reference_bit_exact(flavor):
     d = load("std_bs")
@@ -74,6 +87,11 @@ def test_std_bs_matches_reference_bit_exact(flavor):
 
 
 # ---------------------------------------------------------------------------
+def _nexp(d):
+    """0 for the power-2 model, n for the power-n model's fixtures."""
+    return int(d["nexp"]) if "nexp" in d.files else 0
+
+
 def _pm2_inputs(d, recompute_tables):
     xr = bool(d["xr_mode"])
     kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
@@ -84,16 +102,16 @@ def _pm2_inputs(d, recompute_tables):
               max_iter=int(d["max_iter"]), M=float(d["M"]),
               eps_stat=float(d["eps_stat"]), xr_mode=xr,
               interior=bool(d["interior"]), calc_dzndc=True,
-              xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"])
+              xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"], nexp=_nexp(d))
     if recompute_tables:
-        Mb, rb, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]))
+        Mb, rb, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]), _nexp(d))
         kw["bla"] = (Mb, rb, st)
         kw["dZndc"] = orc.dzndc_path_m2(
             d["Zn"], kw["ref_div_iter"], kw["ref_order"], xr, kw["dx_m"], kw["dx_e"],
-            d["xr_idx"], d["xr_m"], d["xr_e"])
+            d["xr_idx"], d["xr_m"], d["xr_e"], nexp=_nexp(d))
         if kw["interior"]:
             kw["dZndz"] = orc.dzndz_path_m2(d["Zn"], kw["ref_div_iter"], xr,
-                                            d["xr_idx"], d["xr_m"], d["xr_e"])
+                                            d["xr_idx"], d["xr_m"], d["xr_e"], nexp=_nexp(d))
     else:
         kw["bla"] = (d["M_bla"], d["r_bla"], int(d["stages_bla"]))
         if xr:
@@ -116,18 +134,22 @@ def _xr_val(m, e, e_ref=None):
     return m * np.exp2((e - e_ref).astype(float))
 
 
-@pytest.mark.parametrize("case", ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr",
-                                  "pert_m2_xr_div"])
+PERT_CASES = ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr", "pert_m2_xr_div",
+              "pert_mn3_cycle", "pert_mn3_div", "pert_mn4_xr"]
+
+
+@pytest.mark.parametrize("case", PERT_CASES)
 def test_orbit_tables_match_reference(case):
     d = load(case)
     xr = bool(d["xr_mode"])
     kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
-    Mb, rb, bl, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]))
+    Mb, rb, bl, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]), _nexp(d))
     assert st == int(d["stages_bla"])
     assert np.array_equal(Mb.view(np.uint64), d["M_bla"].view(np.uint64))
     assert np.array_equal(rb.view(np.uint64), d["r_bla"].view(np.uint64))
     dz = orc.dzndc_path_m2(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), xr,
-                           float(d["dx_m"]), int(d["dx_e"]), d["xr_idx"], d["xr_m"], d["xr_e"])
+                           float(d["dx_m"]), int(d["dx_e"]), d["xr_idx"], d["xr_m"], d["xr_e"],
+                           nexp=_nexp(d))
     if xr:
         # the golden Xrange paths come from the reference's numpy Xrange_array
         # class, whose rounding differs from numba_xr in the last bits
@@ -139,7 +161,7 @@ def test_orbit_tables_match_reference(case):
         assert np.array_equal(dz.view(np.uint64), d["dZndc"].view(np.uint64))
     if bool(d["interior"]):
         dzz = orc.dzndz_path_m2(d["Zn"], int(d["ref_div_iter"]), xr,
-                                d["xr_idx"], d["xr_m"], d["xr_e"])
+                                d["xr_idx"], d["xr_m"], d["xr_e"], nexp=_nexp(d))
         if xr:
             eref = int(d["dZndz_e"].max())
             np.testing.assert_allclose(_xr_val(dzz[0], dzz[1], eref),
@@ -149,8 +171,7 @@ def test_orbit_tables_match_reference(case):
             assert np.array_equal(dzz.view(np.uint64), d["dZndz"].view(np.uint64))
 
 
-@pytest.mark.parametrize("case", ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr",
-                                  "pert_m2_xr_div"])
+@pytest.mark.parametrize("case", PERT_CASES)
 @pytest.mark.parametrize("recompute", [False, True])
 def test_perturb_m2_matches_reference(case, recompute):
     d = load(case)
