@@ -23,6 +23,7 @@ FSG_ERR_NOMEM = -3
 FSG_ERR_NODEV = -4
 FSG_ERR_LIMIT = -5
 FSG_NOALLOC_MAX_TILES = 64
+FSG_MN_MAX_EXP = 32
 
 MODE_FP64 = 0
 MODE_XR64 = 1
@@ -42,6 +43,7 @@ class RefDesc(ct.Structure):
         ("n_xr", I32), ("xr_idx", P), ("xr_m", P), ("xr_e", P),
         ("flavor", I32), ("xr_paths", I32), ("calc_dzndc", I32), ("calc_dzndz", I32),
         ("scale_m", F64), ("scale_e", I32), ("bla", I32), ("kc", F64), ("bla_eps", F64),
+        ("nexp", I32),
     ]
 
 
@@ -49,7 +51,7 @@ class Calc(ct.Structure):
     _fields_ = [
         ("max_iter", I64), ("M_divergence", F64), ("epsilon_stationnary", F64),
         ("mode", I32), ("calc_dzndc", I32), ("interior", I32), ("bla", I32),
-        ("flavor", I32), ("xr_semantics", I32),
+        ("flavor", I32), ("xr_semantics", I32), ("nexp", I32),
     ]
 
 
@@ -198,7 +200,7 @@ class Reference:
 
     def __init__(self, ctx, Zn, *, div_iter, order, flavor=0, xr_idx=None, xr_m=None,
                  xr_e=None, xr_paths=False, calc_dzndc=True, calc_dzndz=False,
-                 scale_m=1.0, scale_e=0, bla=True, kc=0.0, bla_eps=1e-6):
+                 scale_m=1.0, scale_e=0, bla=True, kc=0.0, bla_eps=1e-6, nexp=0):
         self.ctx = ctx
         self.Zn = np.ascontiguousarray(Zn, dtype=np.complex128)
         n_xr = 0 if xr_idx is None else len(xr_idx)
@@ -223,10 +225,12 @@ class Reference:
         d.bla = int(bool(bla))
         d.kc = float(kc)
         d.bla_eps = float(bla_eps)
+        d.nexp = int(nexp)
         h = P()
         ctx.check(ctx.L.fsg_ref_create(ctx.h, ct.byref(d), ct.byref(h)), "fsg_ref_create")
         self.h = h
         self.flavor = flavor
+        self.nexp = int(nexp)
         self.xr_paths = bool(xr_paths)
         ln, bl, st = I64(), I64(), I32()
         ctx.L.fsg_ref_info(h, ct.byref(ln), ct.byref(bl), ct.byref(st))
@@ -242,7 +246,7 @@ class Reference:
                   "fsg_ref_derive_bla")
         r = Reference.__new__(Reference)
         r.ctx, r.h, r._base, r._keep = ctx, h, self, []
-        r.Zn, r.flavor, r.xr_paths = self.Zn, self.flavor, self.xr_paths
+        r.Zn, r.flavor, r.xr_paths, r.nexp = self.Zn, self.flavor, self.xr_paths, self.nexp
         ln, bl, st = I64(), I64(), I32()
         ctx.L.fsg_ref_info(h, ct.byref(ln), ct.byref(bl), ct.byref(st))
         r.len, r.bla_len, r.stages = ln.value, bl.value, st.value
@@ -344,7 +348,8 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
 
 
 def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
-              calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False):
+              calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False,
+              nexp=0):
     c = Calc()
     c.max_iter = int(max_iter)
     c.M_divergence = float(M_divergence)
@@ -355,4 +360,5 @@ def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
     c.bla = int(bool(bla))
     c.flavor = int(flavor)
     c.xr_semantics = int(bool(xr_semantics))
+    c.nexp = int(nexp)
     return c

@@ -33,7 +33,7 @@ SOURCES = {
     "fsg_noalloc.cu": [],
     "fsg_abi.cu": [],
 }
-HEADERS = ["fsg_num.cuh", "fsg_internal.cuh", "fsg_bs.cuh"]
+HEADERS = ["fsg_num.cuh", "fsg_internal.cuh", "fsg_bs.cuh", "fsg_mn.cuh"]
 
 
 def nvcc():

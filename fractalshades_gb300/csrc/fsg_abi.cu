@@ -68,6 +68,7 @@ struct fsg_ref {
     std::vector<void *> allocs;   // stream-ordered allocations (cudaMallocAsync)
     int64_t len = 0;
     int xr_paths = 0, flavor = 0, has_dzndc = 0, has_dzndz = 0;
+    int nexp = 0;                 // 0: power-2 model, n: power-n model
     fsg_ref *base = nullptr;      // fsg_ref_derive_bla: owner of the shared tables
     int derived = 0;              // live references derived from this one
     cudaEvent_t ready = nullptr;  // derived references: recorded after the BLA build;
@@ -133,6 +134,8 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
     if (perturb && !t.ref) return set_err(ctx, FSG_ERR_ARG, "perturbation tile without reference");
     if (perturb && t.ref->flavor != calc->flavor)
         return set_err(ctx, FSG_ERR_ARG, "reference flavor differs from the calculation flavor");
+    if (perturb && t.ref->nexp != calc->nexp)
+        return set_err(ctx, FSG_ERR_ARG, "reference exponent (nexp) differs from the calculation's");
     if (perturb && calc->flavor == 0) {
         if (calc->calc_dzndc && !t.ref->has_dzndc)
             return set_err(ctx, FSG_ERR_ARG, "calc_dzndc requested but the reference has no dZndc path");
@@ -170,6 +173,14 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
     return FSG_OK;
 }
 
+int check_nexp(fsg_ctx *ctx, int flavor, int nexp) {
+    if (nexp == 0) return FSG_OK;
+    if (flavor != 0) return set_err(ctx, FSG_ERR_ARG, "nexp applies to flavor 0 (Mandelbrot) only");
+    if (nexp < 2) return set_err(ctx, FSG_ERR_ARG, "nexp must be 0 or an exponent >= 2");
+    if (nexp > FSG_MN_MAX_EXP) return set_err(ctx, FSG_ERR_LIMIT, "nexp above FSG_MN_MAX_EXP");
+    return FSG_OK;
+}
+
 CalcDev make_calc(const fsg_calc *c) {
     CalcDev d;
     d.max_iter = (int)c->max_iter;
@@ -178,6 +189,8 @@ CalcDev make_calc(const fsg_calc *c) {
     d.logM = log(c->M_divergence);
     d.mode = c->mode; d.calc_dzndc = c->calc_dzndc; d.interior = c->interior;
     d.bla = c->bla; d.flavor = c->flavor; d.xrsem = c->xr_semantics;
+    d.nexp = c->nexp;
+    d.logd = log(c->nexp ? (double)c->nexp : 2.);
     return d;
 }
 
@@ -256,6 +269,12 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         return set_err(ctx, FSG_ERR_ARG, "max_iter out of range (1 .. 2^30)");
     if (calc->flavor < 0 || calc->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
     if (calc->mode < 0 || calc->mode > 2) return set_err(ctx, FSG_ERR_ARG, "bad mode");
+    {
+        int rc = check_nexp(ctx, calc->flavor, calc->nexp);
+        if (rc != FSG_OK) return rc;
+    }
+    if (perturb && calc->nexp != 0 && calc->mode == FSG_MODE_FE32)
+        return set_err(ctx, FSG_ERR_ARG, "the power-n model runs in FSG_MODE_FP64 or FSG_MODE_XR64");
     for (int32_t i = 0; i < ntiles; i++) {
         int rc = check_tile(ctx, tiles[i], perturb, calc);
         if (rc != FSG_OK) return rc;
@@ -432,6 +451,10 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (d->n_xr < 0 || (d->n_xr > 0 && (!d->xr_idx || !d->xr_m || !d->xr_e)))
         return set_err(ctx, FSG_ERR_ARG, "bad Xrange side table");
     if (d->flavor < 0 || d->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
+    {
+        int rc = check_nexp(ctx, d->flavor, d->nexp);
+        if (rc != FSG_OK) return rc;
+    }
     const int len = (int)d->len;
     // the iteration index w never passes min(order, div_iter) <= len, so every
     // orbit read stays inside [0, len] (slot len is a zero pad)
@@ -456,6 +479,14 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (R.order < R.first_invalid) R.first_invalid = R.order;
     R.flavor = d->flavor;
     R.n_xr = d->n_xr;
+    // binomial coefficients C(n, k) as float64, exact for n <= FSG_MN_MAX_EXP
+    // (mandelbrot_Mn.py:636-640 math.comb)
+    r->nexp = R.nexp = d->nexp;
+    for (int k = 0; k <= d->nexp; k++) {
+        unsigned long long v = 1;
+        for (int j = 1; j <= k; j++) v = v * (unsigned long long)(d->nexp - k + j) / (unsigned long long)j;
+        R.binom[k] = (double)v;
+    }
     cudaStream_t s = ctx->stream;
     int rc = FSG_OK;
 #define RA(ptr, n) do { rc = ref_alloc(ctx, r, &(ptr), (n)); if (rc != FSG_OK) { ref_release(r, s); delete r; return rc; } } while (0)
@@ -516,7 +547,8 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
          *bla_first = nullptr;
     int *bla_first_step = nullptr;
     const int bla_nit = (len >> 3) + 1;
-    if (d->flavor == 0) {
+    const bool fe_tables = d->flavor == 0 && d->nexp == 0;   // FE32 is the power-2 form
+    if (fe_tables) {
         RA(Zf, len + 1);
         RA(Zp, len + 1);
         if (d->calc_dzndc) RA(dzndc_f, len + 1);
@@ -551,7 +583,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
         fsg_build_bs_fr(r->dev, len, bs_Zf, dXa, dXb, dYa, dYb, bs_hf, s);
         fsg_build_bs_fr_bla(Mbs, R.bla_len, bs_blaf, s);
     }
-    if (d->flavor == 0) {
+    if (fe_tables) {
         fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
                             dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_f, bla_nit, bla_first,
                             bla_first_step, s);
@@ -589,6 +621,7 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
     if (!r) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
     r->len = base->len; r->flavor = base->flavor; r->xr_paths = base->xr_paths;
     r->has_dzndc = base->has_dzndc; r->has_dzndz = base->has_dzndz;
+    r->nexp = base->nexp;
     r->base = base;
     RefDev &R = r->host;
     R = base->host;                  // shares the orbit, side table, paths, fe orbit
@@ -608,7 +641,7 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
         if (Mbla) RCK(cudaMemsetAsync(Mbla, 0, 64 * (size_t)L, s), "zero BLA");
         if (Mbs) RCK(cudaMemsetAsync(Mbs, 0, 128 * (size_t)L, s), "zero BLA");
         R.bla_len = 2 * L;
-        if (R.flavor == 0) {
+        if (R.flavor == 0 && R.nexp == 0) {
             RA(bla_f, 2 * (size_t)R.bla_len);
             RA(bla_first, 2 * (size_t)R.bla_nit);
             RA(bla_first_step, (size_t)R.bla_nit);
@@ -622,10 +655,10 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     if (R.bla_len > 0) {
         fsg_build_bla(r->dev, R.flavor, len, Mbla, Mbs, rbla, R.stages, kc, bla_eps, s);
-        if (R.flavor == 0)
+        if (R.flavor == 0 && R.nexp == 0)
             fsg_build_fe_bla(r->dev, Mbla, rbla, R.bla_len, bla_f, R.bla_nit, bla_first,
                              bla_first_step, s);
-        else
+        else if (R.flavor != 0)
             fsg_build_bs_fr_bla(Mbs, R.bla_len, bs_blaf, s);
     }
     RCK(cudaGetLastError(), "BLA kernels");

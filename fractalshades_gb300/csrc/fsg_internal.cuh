@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "fsg_num.cuh"
+#include "fsg_mn.cuh"
 
 #define FSG_MAX_TILES_PER_LAUNCH 1024
 #define FSG_STG_COMPRESSED 3          // settings.py:40 BLA_compression
@@ -13,6 +14,8 @@
 struct RefDev {
     int len, div_iter, order, first_invalid;   // order clamped to INT32_MAX when none
     int flavor;                                 // 0 = M2, 1..5 BS
+    int nexp;                                   // 0: power-2 closures; n: power-n model
+    double binom[FSG_MN_MAX_EXP + 1];           // C(nexp, k) as float64
     int n_xr;
     const double2 *Zn;          // [len + 1], Zn[len] = 0 (read when w reaches len)
     const int *xr_slot;         // [len + 1]: -1 or index in the side table
@@ -72,6 +75,8 @@ struct CalcDev {
     int max_iter;
     double M2, eps2, logM;
     int mode, calc_dzndc, interior, bla, flavor, xrsem;
+    int nexp;                                  // 0: power-2 model; n: power-n model
+    double logd;                               // log of the degree (potential)
 };
 
 // Work distribution of one launch: a device counter hands out pixel indices
@@ -124,13 +129,13 @@ __device__ __forceinline__ void fsg_flush_stats(const WorkDev &W, unsigned long 
 }
 
 // Potential (postproc.py:352-406 with Continuous_iter_pp_infinity :1001-1009,
-// d = 2, a_d = 1) and distance estimate (postproc.py:684-731).
+// d = the degree, a_d = 1) and distance estimate (postproc.py:684-731).
 __device__ __forceinline__ void fsg_epilogue(const TileDev &T, const CalcDev &C, long long ip,
                                              double2 zn, double absd, int n) {
     if (T.pot == nullptr && T.dem == nullptr) return;
     double az = hypot(zn.x, zn.y);
     if (T.pot) {
-        double nu_frac = -(log(log(az) / C.logM) / 0.6931471805599453);
+        double nu_frac = -(log(log(az) / C.logM) / C.logd);
         double x = -nu_frac;
         double q = floor(x);
         T.pot[ip] = ((double)n - q) - (x - q);

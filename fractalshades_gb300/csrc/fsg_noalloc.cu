@@ -70,6 +70,8 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     if (ntiles > FSG_NOALLOC_MAX_TILES) return FSG_ERR_LIMIT;
     if (calc->max_iter <= 0 || calc->max_iter > (1 << 30)) return FSG_ERR_ARG;
     if (calc->flavor < 0 || calc->flavor > 5) return FSG_ERR_ARG;
+    if (calc->nexp != 0 && (calc->flavor != 0 || calc->nexp < 2)) return FSG_ERR_ARG;
+    if (calc->nexp > FSG_MN_MAX_EXP) return FSG_ERR_LIMIT;
     const int nZ_min = calc->flavor == 0 ? 3 : 6;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return FSG_ERR_NODEV;
@@ -115,6 +117,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     C.logM = log(calc->M_divergence);
     C.mode = FSG_MODE_FP64; C.calc_dzndc = 1; C.interior = 0; C.bla = 0;
     C.flavor = calc->flavor; C.xrsem = 0;
+    C.nexp = calc->nexp; C.logd = log(calc->nexp ? (double)calc->nexp : 2.);
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
         return FSG_ERR_CUDA;

@@ -2,7 +2,8 @@
 //
 // Power-2 Mandelbrot: perturbation.py:988-1400 (numba_cycles_perturb,
 // numba_initialize, numba_iterate) with the closures of
-// models/mandelbrot_M2.py:591-627.  XR = false is the branch with
+// models/mandelbrot_M2.py:591-627 (MN = false) or, for the power-n model,
+// models/mandelbrot_Mn.py:626-733 (MN = true, fsg_mn.cuh).  XR = false is the branch with
 // xr_detect_activated False (double deltas), XR = true the Xrange branch
 // (double mantissa + int32 exponent, numba_xr.py semantics).
 // Burning Ship family: perturbation.py:1406-1811 with the closures of
@@ -20,7 +21,7 @@ __device__ __forceinline__ xc ldx(const double2 *m, const int *e, int i) {
     return xc_make(v.x, v.y, __ldg(&e[i]));
 }
 
-template <bool XR>
+template <bool XR, bool MN>
 __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, long long ip,
                                          unsigned long long &nfull, unsigned long long &nbla,
                                          unsigned long long &nreb, unsigned long long &itsum) {
@@ -28,6 +29,8 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
     const long long np = (long long)T.nx * T.ny;
     const int dzndz_on = C.interior, dzndc_on = C.calc_dzndc;
     const int order = R.order, div_iter = R.div_iter, w_wrapped = R.len;
+    const int nexp = R.nexp;
+    const double *Cb = R.binom;
     // perturbation.py:2214-2230 ref_path_c_from_pix, 2666-2672 lin_proj_impl
     double2 pp = fsg_pixel(T, ip);
     double px = pp.x, py = pp.y;
@@ -80,27 +83,32 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         if (dzndc_on) {
             if (XR) {
                 xc rd = dyn ? xzero : ldx(R.dZndc_xm, R.dZndc_xe, w);
-                xdzndc = xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndc), xr_mul(rd, xzn)));
+                xdzndc = MN ? mn_p_deriv_x(nexp, Cb, xzn, xdzndc, ref_zn_xr, rd)
+                            : xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndc), xr_mul(rd, xzn)));
             } else {
                 double2 rd = dyn ? cx(0., 0.) : __ldg(&R.dZndc[w]);
-                dzndc = rmul(2., cadd(cmul(cadd(ref_zn, zn), dzndc), cmul(rd, zn)));
+                dzndc = MN ? mn_p_deriv(nexp, Cb, zn, dzndc, ref_zn, rd)
+                           : rmul(2., cadd(cmul(cadd(ref_zn, zn), dzndc), cmul(rd, zn)));
             }
         }
         if (dzndz_on) {
             int k = nullify ? 0 : w;
             if (XR) {
                 xc rd = ldx(R.dZndz_xm, R.dZndz_xe, k);
-                xdzndz = xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndz), xr_mul(rd, xzn)));
+                xdzndz = MN ? mn_p_deriv_x(nexp, Cb, xzn, xdzndz, ref_zn_xr, rd)
+                            : xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndz), xr_mul(rd, xzn)));
             } else {
                 double2 rd = __ldg(&R.dZndz[k]);
-                dzndz = rmul(2., cadd(cmul(cadd(ref_zn, zn), dzndz), cmul(rd, zn)));
+                dzndz = MN ? mn_p_deriv(nexp, Cb, zn, dzndz, ref_zn, rd)
+                           : rmul(2., cadd(cmul(cadd(ref_zn, zn), dzndz), cmul(rd, zn)));
             }
         }
         if (XR) {
-            xzn = xr_add(xr_mul(xzn, xr_add(xzn, xr_mul_r(2., ref_zn_xr))), c_xr);
+            xzn = MN ? mn_p_zn_x(nexp, Cb, xzn, ref_zn_xr, c_xr)
+                     : xr_add(xr_mul(xzn, xr_add(xzn, xr_mul_r(2., ref_zn_xr))), c_xr);
             zn = xr_to_std(xzn);
         } else {
-            zn = cadd(cmul(zn, cadd(zn, rmul(2., ref_zn))), c);
+            zn = MN ? mn_p_zn(nexp, Cb, zn, ref_zn, c) : cadd(cmul(zn, cadd(zn, rmul(2., ref_zn))), c);
         }
         w += 1;
         if (w >= order) w = w % order;
@@ -206,7 +214,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
     itsum += (unsigned long long)n;
 }
 
-template <bool XR>
+template <bool XR, bool MN>
 __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
@@ -215,7 +223,7 @@ __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
-        pixel_m2<XR>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        pixel_m2<XR, MN>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
     }
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }
@@ -228,8 +236,16 @@ void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block,
     if (C.flavor != 0)
         k_perturb_bs<double><<<fsg_auto_grid(k_perturb_bs<double>, grid, block, W.total), block, 0,
                                s>>>(W, C);
+    else if (C.nexp != 0 && C.mode == 1)
+        k_perturb_m2<true, true><<<fsg_auto_grid(k_perturb_m2<true, true>, grid, block, W.total),
+                                   block, 0, s>>>(W, C);
+    else if (C.nexp != 0)
+        k_perturb_m2<false, true><<<fsg_auto_grid(k_perturb_m2<false, true>, grid, block, W.total),
+                                    block, 0, s>>>(W, C);
     else if (C.mode == 1)
-        k_perturb_m2<true><<<fsg_auto_grid(k_perturb_m2<true>, grid, block, W.total), block, 0, s>>>(W, C);
+        k_perturb_m2<true, false><<<fsg_auto_grid(k_perturb_m2<true, false>, grid, block, W.total),
+                                    block, 0, s>>>(W, C);
     else
-        k_perturb_m2<false><<<fsg_auto_grid(k_perturb_m2<false>, grid, block, W.total), block, 0, s>>>(W, C);
+        k_perturb_m2<false, false><<<fsg_auto_grid(k_perturb_m2<false, false>, grid, block, W.total),
+                                     block, 0, s>>>(W, C);
 }

@@ -1,6 +1,8 @@
 // fsg_ref.cu -- tables derived from the reference orbit, built on the GPU.
 //
 //   * derivative paths: numba_dZndc_path (perturbation.py:2282-2336),
+//     with df/dz = 2 z (power-2 model) or n z^(n-1) (power-n model,
+//     models/mandelbrot_Mn.py:645-652),
 //     numba_dZndz_path (:2466-2516), numba_dZndc_path_BS + incr_deriv_ref_BS
 //     (:2339-2463).  These are first-order linear recurrences evaluated in
 //     the reference's order by one thread (they are O(len) and run once per
@@ -39,20 +41,21 @@ __global__ void k_dzndc_m2(const RefDev *Rp, double2 *out_std, double2 *out_xm, 
         for (i = 1; i < valid; i++) {
             xc zx = orbit_xr(R, i - 1);
             xc prev = xc_make(out_xm[i - 1].x, out_xm[i - 1].y, out_xe[i - 1]);
-            xc v = xr_add(xr_mul(xr_mul_r(2., zx), prev), xc_make(scale_m, 0., scale_e));
+            xc v = xr_add(xr_mul(mn_dfdz_x(R.nexp, zx), prev), xc_make(scale_m, 0., scale_e));
             out_xm[i] = cx(v.re, v.im); out_xe[i] = v.e;
         }
         i -= 1;
         if (i == R.order - 1) {
             xc prev = xc_make(out_xm[i].x, out_xm[i].y, out_xe[i]);
-            xc v = xr_add(xr_mul_s(rmul(2., R.Zn[i]), prev), xc_make(scale_m, 0., scale_e));
+            xc v = xr_add(xr_mul_s(mn_dfdz(R.nexp, R.Zn[i]), prev), xc_make(scale_m, 0., scale_e));
             out_xm[0] = cx(v.re, v.im); out_xe[0] = v.e;
         }
     } else {
         double scale = ldexp_d(scale_m, scale_e);
-        for (i = 1; i < valid; i++) out_std[i] = caddr(cmul(rmul(2., R.Zn[i - 1]), out_std[i - 1]), scale);
+        for (i = 1; i < valid; i++)
+            out_std[i] = caddr(cmul(mn_dfdz(R.nexp, R.Zn[i - 1]), out_std[i - 1]), scale);
         i -= 1;
-        if (i == R.order - 1) out_std[0] = caddr(cmul(rmul(2., R.Zn[i]), out_std[i]), scale);
+        if (i == R.order - 1) out_std[0] = caddr(cmul(mn_dfdz(R.nexp, R.Zn[i]), out_std[i]), scale);
     }
 }
 
@@ -70,18 +73,18 @@ __global__ void k_dzndz_m2(const RefDev *Rp, double2 *out_std, double2 *out_xm, 
         out_xm[1] = cx(1., 0.); out_xe[1] = 0;
         for (i = 2; i < valid; i++) {
             xc prev = xc_make(out_xm[i - 1].x, out_xm[i - 1].y, out_xe[i - 1]);
-            xc v = xr_mul(xr_mul_r(2., orbit_xr(R, i - 1)), prev);
+            xc v = xr_mul(mn_dfdz_x(R.nexp, orbit_xr(R, i - 1)), prev);
             out_xm[i] = cx(v.re, v.im); out_xe[i] = v.e;
         }
         i -= 1;
         xc prev = xc_make(out_xm[i].x, out_xm[i].y, out_xe[i]);
-        xc v = xr_mul(xr_mul_r(2., orbit_xr(R, i)), prev);
+        xc v = xr_mul(mn_dfdz_x(R.nexp, orbit_xr(R, i)), prev);
         out_xm[len] = cx(v.re, v.im); out_xe[len] = v.e;
     } else {
         out_std[1] = cx(1., 0.);
-        for (i = 2; i < valid; i++) out_std[i] = cmul(rmul(2., R.Zn[i - 1]), out_std[i - 1]);
+        for (i = 2; i < valid; i++) out_std[i] = cmul(mn_dfdz(R.nexp, R.Zn[i - 1]), out_std[i - 1]);
         i -= 1;
-        out_std[len] = cmul(rmul(2., R.Zn[i]), out_std[i]);
+        out_std[len] = cmul(mn_dfdz(R.nexp, R.Zn[i]), out_std[i]);
     }
 }
 
@@ -150,7 +153,7 @@ __global__ void k_bla_leaf_m2(const RefDev *Rp, double2 *M, double *r, int L, do
     double2 tM[32]; double tr[16];
     for (int j = 0; j < 16; j++) { tM[2 * j] = cx(0., 0.); tM[2 * j + 1] = cx(0., 0.); tr[j] = 0.; }
     for (int j = 0; j < 8; j++) {
-        double2 A = rmul(2., R.Zn[8 * i + j]);
+        double2 A = mn_dfdz(R.nexp, R.Zn[8 * i + j]);
         tM[4 * j] = A; tM[4 * j + 1] = cx(1., 0.);
         tr[2 * j] = eps * hypot(A.x, A.y);
     }

@@ -1,7 +1,8 @@
 // fsg_std.cu -- standard (non-perturbation) escape-time loops, FP64.
 //
 // Power-2 Mandelbrot: core.py:2935-3004 numba_cycles / numba_iterate and
-// models/mandelbrot_M2.py:309-334 iterate_once.  Burning Ship family:
+// models/mandelbrot_M2.py:309-334 iterate_once; power-n Mandelbrot:
+// models/mandelbrot_Mn.py:317-355.  Burning Ship family:
 // core.py:3007-3056 numba_iterate_BS and models/burning_ship.py:350-434.
 // The reference compiles these without fastmath, so this file is built with
 // -fmad=false: each operation rounds once, in the order of the reference.
@@ -35,6 +36,42 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
             dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);
             dzndz = cmul(rmul(2., dzndz), zn);
             zn = cadd(cmul(zn, zn), c);
+            if (n == 1) dzndz = cx(1., 0.);
+            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; break; }
+            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; break; }
+        }
+        double2 *Z = (double2 *)T.Z;
+        Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
+        T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
+        fsg_epilogue(T, C, ip, zn, hypot(dzndc.x, dzndc.y), n);
+        it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+    }
+    fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
+}
+
+// Power-n Mandelbrot: models/mandelbrot_Mn.py:317-355 iterate_once
+// (calc_d2zndc2 False): z^(n-1) once per step, z^n = z^(n-1) z.
+__global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
+    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    fsg_load_starts(W, s_start);
+    unsigned long long it_sum = 0, steps = 0;
+    const int nexp = C.nexp;
+    const double deg = (double)nexp;
+    int t; long long ip;
+    while (fsg_claim(W, s_start, t, ip)) {
+        const TileDev &T = W.tiles[t];
+        long long np = (long long)T.nx * T.ny;
+        double2 c = std_c(T, ip);
+        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.);
+        int n = 0; signed char reason = -1;
+        for (;;) {
+            n += 1;
+            if (n >= C.max_iter) { reason = 0; break; }
+            double2 zm1 = mn_ipow(zn, nexp - 1);
+            double2 zm = cmul(zm1, zn);
+            dzndc = caddr(cmul(rmul(deg, dzndc), zm1), 1.);
+            dzndz = cmul(rmul(deg, dzndz), zm1);
+            zn = cadd(zm, c);
             if (n == 1) dzndz = cx(1., 0.);
             if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; break; }
             if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; break; }
@@ -118,6 +155,8 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
 }
 
 void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    if (C.flavor == 0) k_std_m2<<<fsg_auto_grid(k_std_m2, grid, block, W.total), block, 0, s>>>(W, C);
+    if (C.flavor == 0 && C.nexp != 0)
+        k_std_mn<<<fsg_auto_grid(k_std_mn, grid, block, W.total), block, 0, s>>>(W, C);
+    else if (C.flavor == 0) k_std_m2<<<fsg_auto_grid(k_std_m2, grid, block, W.total), block, 0, s>>>(W, C);
     else k_std_bs<<<fsg_auto_grid(k_std_bs, grid, block, W.total), block, 0, s>>>(W, C);
 }

@@ -43,16 +43,17 @@ def clear_cancel():
 class StdSpec:
     """Options of a standard (non-perturbation) calculation."""
 
-    def __init__(self, *, flavor, max_iter, M_divergence, epsilon_stationnary=0.):
+    def __init__(self, *, flavor, max_iter, M_divergence, epsilon_stationnary=0., nexp=0):
         self.flavor = int(flavor)
         self.max_iter = int(max_iter)
         self.M_divergence = float(M_divergence)
         self.epsilon_stationnary = float(epsilon_stationnary)
+        self.nexp = int(nexp)     # 0: power-2 model, n: power-n model
 
     def calc(self):
         return nat.make_calc(max_iter=self.max_iter, M_divergence=self.M_divergence,
                              epsilon_stationnary=self.epsilon_stationnary,
-                             flavor=self.flavor)
+                             flavor=self.flavor, nexp=self.nexp)
 
     @property
     def nZ(self):
@@ -64,7 +65,7 @@ class PerturbSpec:
 
     def __init__(self, *, flavor, max_iter, M_divergence, epsilon_stationnary=0.,
                  calc_dzndc=True, interior=False, bla=True, xr_detect_activated=False,
-                 i_dzndz=-1, i_dzndc=-1, nZ=1):
+                 i_dzndz=-1, i_dzndc=-1, nZ=1, nexp=0):
         self.flavor = int(flavor)
         self.max_iter = int(max_iter)
         self.M_divergence = float(M_divergence)
@@ -76,10 +77,19 @@ class PerturbSpec:
         self.i_dzndz = int(i_dzndz)
         self.i_dzndc = int(i_dzndc)
         self.nZ = int(nZ)
+        self.nexp = int(nexp)     # 0: power-2 model, n: power-n model
 
     @property
     def mode(self):
         m = settings.precision_mode
+        if self.nexp != 0:
+            # power-n model: the reference's two delta forms (no FE32 kernel)
+            if m == "fe32":
+                raise ValueError("the power-n model runs with precision_mode 'auto', "
+                                 "'fp64' or 'xr64'")
+            if m == "auto":
+                return "xr64" if self.xr_detect_activated else "fp64"
+            return m
         if self.flavor != 0:
             # Burning Ship: no Xrange kernel; below the double range the
             # FP32 + exponent form is the one without underflow
@@ -98,7 +108,7 @@ class PerturbSpec:
                              epsilon_stationnary=self.epsilon_stationnary, mode=self.mode,
                              calc_dzndc=self.calc_dzndc, interior=self.interior,
                              bla=self.bla, flavor=self.flavor,
-                             xr_semantics=self.xr_detect_activated)
+                             xr_semantics=self.xr_detect_activated, nexp=self.nexp)
 
 
 def _check_rc(rc):

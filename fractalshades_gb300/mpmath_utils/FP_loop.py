@@ -274,6 +274,183 @@ def perturbation_mandelbrot_nucleus_size_estimate(seed_x, seed_y, seed_prec, ord
         return size
 
 
+# ---------------------------------------------------------------------------
+# power-n Mandelbrot, z -> z^n + c (FP_loop.pyx:167-235, 255-421, 472-604,
+# 618-760, 1139-1340): mpc_pow_ui for z^n and n dzdc z^(n-1) (+ 1) for the
+# derivative; exponent 2 runs the power-2 functions above.
+# ---------------------------------------------------------------------------
+def _pow_fix(zx, zy, n, F):
+    """z**n in fixed point (binary powering), n >= 1"""
+    rx, ry = None, None
+    px, py = zx, zy
+    while True:
+        if n & 1:
+            if rx is None:
+                rx, ry = px, py
+            else:
+                rx, ry = _cmul(rx, ry, px, py, F)
+        n >>= 1
+        if not n:
+            return rx, ry
+        px, py = _cmul(px, py, px, py, F)
+
+
+def _check_exponent(exponent):
+    exponent = int(exponent)
+    if exponent < 2:
+        raise NotImplementedError(exponent)
+    return exponent
+
+
+def perturbation_mandelbrotN_FP_loop(orbit, need_Xrange, max_iter, exponent, M, seed_x,
+                                     seed_y, seed_prec):
+    """Orbit of z_{n+1} = z_n**exponent + c, z_0 = 0 (FP_loop.pyx:255-421):
+    same outputs as perturbation_mandelbrot_FP_loop."""
+    n = _check_exponent(exponent)
+    if n == 2:
+        return perturbation_mandelbrot_FP_loop(orbit, need_Xrange, max_iter, M, seed_x, seed_y,
+                                               seed_prec)
+    orb = orbit.view(np.complex128) if orbit.dtype != np.complex128 else orbit
+    if orb.shape[0] != max_iter + 1:
+        raise ValueError("orbit length must be max_iter + 1")
+    F = int(seed_prec) + GUARD_BITS
+    cx, cy = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    zx, zy = 0, 0
+    orb[0] = 0.
+    xr_dict = {}
+    partial_dict = {}
+    curr_partial = PARTIAL_TSHOLD
+    curr_partial2 = None
+    i = 0
+    abs_i = 0.
+    for i in range(1, max_iter + 1):
+        px, py = _pow_fix(zx, zy, n, F)
+        zx, zy = px + cx, py + cy
+        x, y = _to_float(zx, F), _to_float(zy, F)
+        orb[i] = complex(x, y)
+        abs_i = math.hypot(x, y)
+        if abs_i > M:
+            break
+        if need_Xrange and abs_i < XR_TSHOLD:
+            xr_dict[i] = _xr_of(zx, zy, F)
+        if abs_i <= curr_partial:
+            a2 = zx * zx + zy * zy
+            if curr_partial2 is None or a2 < curr_partial2:
+                partial_dict[i] = _xr_of(zx, zy, F)
+                curr_partial2 = a2
+                curr_partial = abs_i
+    if i == max_iter and abs_i <= M:
+        i += 1
+    return i, partial_dict, xr_dict
+
+
+def perturbation_mandelbrotN_ball_method(seed_x, seed_y, seed_prec, seed_px, exponent, maxiter,
+                                         M_divergence):
+    """First i with |z_i / (dz_i/dc)| < px for z -> z**exponent + c
+    (FP_loop.pyx:618-760), -1 if none up to maxiter."""
+    n = _check_exponent(exponent)
+    F = int(seed_prec) + GUARD_BITS
+    cx, cy = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    px = _fix(_dec(seed_px), F)
+    px2 = px * px
+    one = 1 << F
+    zx = zy = 0
+    dx = dy = 0
+    for i in range(1, maxiter + 1):
+        # dzndc <- n dzndc z^(n-1) + 1 with the current z, then z <- z^n + c
+        wx, wy = _pow_fix(zx, zy, n - 1, F)
+        tx, ty = _cmul(dx, dy, wx, wy, F)
+        dx, dy = n * tx + one, n * ty
+        zx, zy = _cmul(wx, wy, zx, zy, F)
+        zx, zy = zx + cx, zy + cy
+        if math.hypot(_to_float(zx, F), _to_float(zy, F)) > M_divergence:
+            return -1
+        z2 = zx * zx + zy * zy
+        d2 = dx * dx + dy * dy
+        if (z2 << (2 * F)) < px2 * d2:
+            return i
+    return -1
+
+
+def _newton_step_float_n(c, order, n, prec):
+    """Newton step c -> c - z_order / (dz_order/dc) in floating point
+    (mpmath at ``prec`` bits), for orbits that leave the fixed-point range."""
+    with mpmath.workprec(prec):
+        zr = mpmath.mpc(0)
+        dz = mpmath.mpc(0)
+        for _ in range(1, order + 1):
+            dz = n * dz * zr ** (n - 1) + 1
+            zr = zr ** n + c
+        return zr / dz, zr
+
+
+def perturbation_mandelbrotN_find_any_nucleus(seed_x, seed_y, seed_prec, exponent, order,
+                                              max_newton, seed_eps_cv, seed_eps_valid):
+    """Newton for f^order(0) = 0, f = z**exponent + c, divisor periods
+    accepted (FP_loop.pyx:1139-1340).  Returns (newton_cv, c)."""
+    n = _check_exponent(exponent)
+    if n == 2:
+        return perturbation_mandelbrot_find_any_nucleus(seed_x, seed_y, seed_prec, order,
+                                                        max_newton, seed_eps_cv, seed_eps_valid)
+    F = int(seed_prec) + GUARD_BITS
+    cx, cy = _fix(_dec(seed_x), F), _fix(_dec(seed_y), F)
+    eps_cv = mpmath.mpf(_dec(seed_eps_cv)) * 64
+    eps_valid = mpmath.mpf(_dec(seed_eps_valid))
+    one = 1 << F
+    big = F + 64
+    order = int(order)
+    newton_cv = False
+    for _ in range(int(max_newton)):
+        zx = zy = 0
+        dx = dy = 0
+        escaped = False
+        for i in range(1, order + 1):
+            wx, wy = _pow_fix(zx, zy, n - 1, F)
+            tx, ty = _cmul(dx, dy, wx, wy, F)
+            dx, dy = n * tx + one, n * ty
+            zx, zy = _cmul(wx, wy, zx, zy, F)
+            zx, zy = zx + cx, zy + cy
+            if zx.bit_length() > big or zy.bit_length() > big:
+                escaped = True
+                break
+        if escaped:
+            step_c, _zr = _newton_step_float_n(
+                mpmath.mpc(_to_mpf(cx, F), _to_mpf(cy, F)), order, n, F)
+            sx, sy = _fix(step_c.real, F), _fix(step_c.imag, F)
+            cx, cy = cx - sx, cy - sy
+            continue
+        sx, sy = _cdiv(zx, zy, dx, dy, F)
+        cx, cy = cx - sx, cy - sy
+        step = mpmath.sqrt(_to_mpf(sx, F) ** 2 + _to_mpf(sy, F) ** 2)
+        if step <= eps_cv:
+            az = mpmath.sqrt(_to_mpf(zx, F) ** 2 + _to_mpf(zy, F) ** 2)
+            newton_cv = az <= eps_valid
+            break
+    if newton_cv:
+        return True, mpmath.mpc(_to_mpf(cx, F), _to_mpf(cy, F))
+    return False, mpmath.mpc("nan", "nan")
+
+
+def perturbation_mandelbrotN_nucleus_size_estimate(seed_x, seed_y, seed_prec, exponent, order):
+    """Size estimate of the period-``order`` component of z -> z**n + c
+    (FP_loop.pyx:472-604): with l = dz_i/dz_1 and b = 1 + sum_i 1 / l,
+    size = 1 / (b * l**(n / (n - 1))) (principal power; l**2 for n = 2)."""
+    n = _check_exponent(exponent)
+    if n == 2:
+        return perturbation_mandelbrot_nucleus_size_estimate(seed_x, seed_y, seed_prec, order)
+    with mpmath.workprec(int(seed_prec)):
+        c = mpmath.mpc(_dec(seed_x), _dec(seed_y))
+        z = mpmath.mpc(0)
+        l = mpmath.mpc(1)
+        b = mpmath.mpc(1)
+        for _ in range(1, int(order)):
+            z = z ** n + c
+            l = n * l * z ** (n - 1)
+            b = b + 1 / l
+        # the exponent n / (n - 1) is a double in the reference (mpc_pow_d)
+        return 1 / (b * l ** mpmath.mpf(n / (n - 1.)))
+
+
 def _dec(s):
     if isinstance(s, (bytes, bytearray)):
         return s.decode("utf8")

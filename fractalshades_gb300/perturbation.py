@@ -47,6 +47,9 @@ class _RefPointUnpickler(pickle.Unpickler):
 
 class PerturbationFractal(Fractal):
 
+    #: 0 for the power-2 closures, n for the power-n model (z -> z^n + c)
+    nexp = 0
+
     def __init__(self, directory):
         """Base class for escape-time fractals computed by perturbation
         around an arbitrary-precision reference orbit (z_0 = 0,
@@ -330,7 +333,8 @@ class PerturbationFractal(Fractal):
             xr_paths=xr and holomorphic, calc_dzndc=calc_deriv_c,
             calc_dzndz=calc_dZndz, scale_m=scale.m, scale_e=scale.e,
             bla=bla_eps is not None, kc=kc.to_standard(),
-            bla_eps=bla_eps if bla_eps is not None else 0.)
+            bla_eps=bla_eps if bla_eps is not None else 0.,
+            nexp=self.nexp if holomorphic else 0)
         args = {"holomorphic": holomorphic, "spec": iterate, "ref": ref,
                 "lin_mat": self.lin_mat, "dx_m": dx_xr.m, "dx_e": dx_xr.e,
                 "interrupted": self._interrupted, "kc": kc,

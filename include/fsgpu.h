@@ -50,6 +50,8 @@ extern "C" {
                             with xr_detect_activated True (dx < settings.xrange_zoom_level) */
 #define FSG_MODE_FE32 2  /* float mantissa + int32 exponent deltas (fast form)           */
 
+#define FSG_MN_MAX_EXP 32  /* largest exponent of the power-n model                      */
+
 /* where the tile buffers live */
 #define FSG_HOST 0       /* host pointers: the library stages the copies            */
 #define FSG_DEVICE 1     /* device pointers: asynchronous on the context stream     */
@@ -78,6 +80,11 @@ typedef struct {
     int32_t bla;              /* build the BLA tree                              */
     double kc;                /* to_standard(kc) (perturbation.py:1830)          */
     double bla_eps;
+    int32_t nexp;             /* flavor 0 only: 0 = the power-2 model
+                                 (models/mandelbrot_M2.py), n in 2 ..
+                                 FSG_MN_MAX_EXP = the power-n model
+                                 (models/mandelbrot_Mn.py, exponent n): the
+                                 paths and BLA use df/dz = n z^(n-1)         */
 } fsg_ref_desc;
 
 /* Calculation options (the calc_std_div keyword arguments). */
@@ -92,6 +99,13 @@ typedef struct {
     int32_t flavor;           /* 0 = M2, 1..5 Burning Ship                       */
     int32_t xr_semantics;     /* FE32 only: follow the Xrange branch's rebase
                                  confirmation (reference xr_detect_activated)    */
+    int32_t nexp;             /* flavor 0 only: 0 = power-2 model, n in 2 ..
+                                 FSG_MN_MAX_EXP = power-n model (standard loop
+                                 of models/mandelbrot_Mn.py:317-355, perturbation
+                                 closures :626-733, potential with d = n); a
+                                 perturbation tile's reference must have been
+                                 created with the same nexp.  FP64 and XR64
+                                 only (FSG_MODE_FE32 is the power-2 form)     */
 } fsg_calc;
 
 /* One tile: a rectangle of pixels with its own view and outputs. */

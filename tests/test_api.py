@@ -216,3 +216,38 @@ def test_reads_reference_written_ref_pt(tmp_path, monkeypatch):
     assert params["order"] == 7 and np.array_equal(path, Zn)
     idx, m, e = fsx.xr_table(params["xr"])
     assert idx.tolist() == [3] and m[0] == 0.75 - 0.5j and e[0] == -1200
+
+
+def test_power_n_models(tmp_path):
+    """Mandelbrot_N / Perturbation_mandelbrot_N (models/mandelbrot_Mn.py):
+    codes, the exponent carried to the GPU options, FP32 refused, the
+    reference's find_nucleus refusal and the Julia size exponent."""
+    f = fsm.Mandelbrot_N(str(tmp_path / "std"), 5)
+    f.zoom(x=0., y=0., dx=3., nx=64, xy_ratio=1., theta_deg=0.)
+    codes, spec = _codes(f, calc_name="c", subset=None, max_iter=100, M_divergence=1000.,
+                         epsilon_stationnary=1e-3)
+    assert codes[0] == ["zn", "dzndz", "dzndc"] and spec.nexp == 5
+    assert spec.calc().nexp == 5
+    g = fsm.Perturbation_mandelbrot_N(str(tmp_path / "pert"), 3)
+    assert g.init_kwargs == {"directory": str(tmp_path / "pert"), "exponent": 3}
+    g.zoom(precision=30, x="0.6428766799817589", y="0.2514544748796524", dx="1e-10", nx=64,
+           xy_ratio=1., theta_deg=0.)
+    base = dict(calc_name="c", subset=None, max_iter=1000, M_divergence=1000.,
+                epsilon_stationnary=1e-3)
+    codes, spec = _codes(g, interior_detect=True, **base)
+    assert codes[0] == ["zn", "dzndz", "dzndc"] and spec.nexp == 3
+    settings.precision_mode = "auto"
+    assert spec.mode == "fp64" and spec.calc().nexp == 3
+    settings.precision_mode = "fe32"
+    try:
+        with pytest.raises(ValueError):
+            spec.mode
+    finally:
+        settings.precision_mode = "auto"
+    with pytest.raises(NotImplementedError):
+        g.find_nucleus(g.x + 1j * g.y, 10, 1e-12)
+    c0 = mpmath.mpc("0.64287667998175895118", "0.25145447487965245909")
+    size, julia = g._nucleus_size_estimate(c0, 10)
+    assert abs(julia - size ** (8. / 9.)) < 1e-12 * julia
+    with pytest.raises(ValueError):
+        fsm.Perturbation_mandelbrot_N(str(tmp_path / "bad"), 1)

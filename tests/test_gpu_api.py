@@ -109,3 +109,66 @@ def test_burning_ship_below_double_range(tmp_path):
         a = out["1e-310"][k] / 1e-310 * 1e-250       # per unit of c, both
         b = out["1e-250"][k]
         np.testing.assert_allclose(a, b, rtol=1e-3)
+
+
+@pytest.mark.parametrize("nexp,x,y,dx", [
+    # z^3 + c: the edge of the period-10 component, where the ball method
+    # finds a period-70 nucleus; the view holds escaping, stationary and
+    # max_iter pixels
+    (3, "0.64289167998175895118", "0.25147047487965245909", "8e-6"),
+    # z^4 + c: the period-10 nucleus at 1e-305 (Xrange branch, interior)
+    (4, "-0.51534888699245770184", "0.46481172994907691405", "1e-305"),
+])
+def test_power_n_calc_raw_vs_oracle(tmp_path, nexp, x, y, dx):
+    """Perturbation_mandelbrot_N end to end: ball method and Newton on the
+    host, reference tables and the power-n loop on the GPU (FP64 at 8e-6,
+    the Xrange branch at 1e-305), against the oracle run on the same orbit;
+    Mandelbrot_N's standard loop bit-exact against the oracle."""
+    import fractalshades_gb300.models as fsm
+    from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
+    if float(dx) < 1e-300:
+        # centre on the nucleus to 340 digits (Newton from the 20-digit seed)
+        with mpmath.workdps(340):
+            ok, nuc = fsFP.perturbation_mandelbrotN_find_any_nucleus(
+                x.encode(), y.encode(), mpmath.mp.prec, nexp, 10, 80,
+                str(mpmath.mpf(2) ** -mpmath.mp.prec).encode(), b"1e-300")
+            assert ok
+            x, y = mpmath.nstr(nuc.real, 340), mpmath.nstr(nuc.imag, 340)
+    f = fsm.Perturbation_mandelbrot_N(str(tmp_path / "pert"), nexp)
+    f.zoom(precision=340, x=x, y=y, dx=dx, nx=48, xy_ratio=1., theta_deg=0.)
+    f.calc_std_div(calc_name="mn", subset=None, max_iter=5000, M_divergence=1000.,
+                   epsilon_stationnary=1e-3, BLA_eps=1e-6, interior_detect=True,
+                   calc_dzndc=True)
+    f.calc_raw("mn")
+    assert f.FP_params["order"] == (70 if nexp == 3 else 10)
+    xr = f.xr_detect_activated
+    assert xr == (dx == "1e-305")
+    si = f.get_raw("mn", "stop_iter").ravel()
+    (Zn, has_xr, idx, xrt, div_iter, order, drift, dxx) = f.get_path_data()
+    kc = f.ref_point_kc().to_standard()
+    Mb, rb, _, st = orc.make_bla_m2(Zn, kc, 1e-6, nexp)
+    xi, xm, xe = (idx, xrt[0], xrt[1]) if has_xr else (None, None, None)
+    dz = orc.dzndc_path_m2(Zn, div_iter, order, xr, dxx.m, dxx.e, xi, xm, xe, nexp=nexp)
+    dzz = orc.dzndz_path_m2(Zn, div_iter, xr, xi, xm, xe, nexp=nexp)
+    xs, ys = f.image_axes()
+    pix = (xs[None, :] + 1j * ys[:, None]).ravel()
+    Zo, Uo, sro, sio = orc.perturb_m2(
+        pix, Zn=Zn, ref_div_iter=div_iter, ref_order=order, lin_mat=f.lin_mat, dx_m=dxx.m,
+        dx_e=dxx.e, drift_m=complex(drift.m), drift_e=drift.e, max_iter=5000, M=1000.,
+        eps_stat=1e-3, xr_mode=xr, interior=True, bla=(Mb, rb, st), dZndc=dz, dZndz=dzz,
+        xr_idx=xi, xr_m=xm, xr_e=xe, nexp=nexp)
+    agree = float(np.mean(si == sio.ravel()))
+    assert agree >= 0.9999, agree
+    assert np.mean(f.get_raw("mn", "stop_reason").ravel() == sro.ravel()) >= 0.9999
+
+    g = fsm.Mandelbrot_N(str(tmp_path / "std"), nexp)
+    g.zoom(x=0., y=0., dx=3., nx=200, xy_ratio=1., theta_deg=0.)
+    g.calc_std_div(calc_name="s", subset=None, max_iter=300, M_divergence=1000.,
+                   epsilon_stationnary=0.01)
+    g.calc_raw("s")
+    xs, ys = g.image_axes()
+    pix = (xs[None, :] + 1j * ys[:, None]).ravel()
+    Zs, sis, srs = orc.std_mn(pix, 0j, g.lin_mat, 3.0, 300, 1000., 0.01, nexp)
+    assert np.array_equal(g.get_raw("s", "stop_iter").ravel(), sis.ravel())
+    zn = g.get_raw("s", "zn").ravel()
+    assert np.array_equal(zn.view(np.uint64), Zs[0].view(np.uint64))

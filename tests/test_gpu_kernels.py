@@ -126,7 +126,40 @@ def test_std_bs_vs_oracle(ctx, flavor):
     assert np.array_equal(Z.view(np.uint64), d[f"Z_{flavor}"].view(np.uint64))
 
 
+@pytest.mark.parametrize("nexp", [3, 4])
+def test_std_mn_bit_exact_vs_golden(ctx, nexp):
+    """Power-n standard loop against the reference's own outputs."""
+    from fractalshades_gb300 import _native as nat
+    d = load("std_mn")
+    pix = d[f"pix_{nexp}"]
+    nx = int(round(np.sqrt(pix.size)))
+    xs, ys = axes(pix, nx)
+    n = pix.size
+    Z = np.zeros((3, n), dtype=np.complex128)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    pot = np.zeros(n)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, stop_reason=sr, stop_iter=si,
+                      center=complex(*d["center"]), dx=float(d["dx"]), potential=pot)
+    calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                         epsilon_stationnary=float(d["eps"]), flavor=0, nexp=nexp)
+    ctx.std_tiles(calc, [t])
+    assert np.array_equal(si, d[f"stop_iter_{nexp}"])
+    assert np.array_equal(sr, d[f"stop_reason_{nexp}"])
+    assert np.array_equal(Z.view(np.uint64), d[f"Z_{nexp}"].view(np.uint64))
+    # potential with d = n (postproc.py:1001-1009)
+    esc = (sr[0] == 1)
+    az = np.abs(Z[0][esc])
+    nu = -(np.log(np.log(az) / np.log(float(d["M"]))) / np.log(nexp))
+    q = np.floor(-nu)
+    np.testing.assert_allclose(pot[esc], (si[0][esc] - q) - (-nu - q), rtol=1e-12)
+
+
 # ---------------------------------------------------------------------------
+def _nexp(d):
+    return int(d["nexp"]) if "nexp" in d.files else 0
+
+
 def _ref_from_golden(ctx, d, xr_paths):
     from fractalshades_gb300 import _native as nat
     kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
@@ -134,7 +167,8 @@ def _ref_from_golden(ctx, d, xr_paths):
         ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
         xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"], xr_paths=xr_paths,
         calc_dzndc=True, calc_dzndz=bool(d["interior"]), scale_m=float(d["dx_m"]),
-        scale_e=int(d["dx_e"]), bla=True, kc=kc, bla_eps=float(d["bla_eps"]))
+        scale_e=int(d["dx_e"]), bla=True, kc=kc, bla_eps=float(d["bla_eps"]),
+        nexp=_nexp(d))
 
 
 def _run_m2(ctx, d, ref, mode, xr_sem):
@@ -155,19 +189,22 @@ def _run_m2(ctx, d, ref, mode, xr_sem):
     calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
                          epsilon_stationnary=float(d["eps_stat"]), mode=mode,
                          calc_dzndc=True, interior=interior, bla=True,
-                         xr_semantics=xr_sem)
+                         xr_semantics=xr_sem, nexp=_nexp(d))
     ctx.perturb_tiles(calc, [t])
     return Z, U, sr, si
 
 
 M2_CASES = ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr", "pert_m2_xr_div"]
+# power-n model: period-10 nuclei of z^3 + c (interior and escaping views)
+# and of z^4 + c at dx = 1e-305 (Xrange branch)
+MN_CASES = ["pert_mn3_cycle", "pert_mn3_div", "pert_mn4_xr"]
 
 
 def _xr_rel(m, e, eref):
     return m * np.exp2((np.asarray(e, dtype=np.int64) - eref).astype(float))
 
 
-@pytest.mark.parametrize("case", M2_CASES)
+@pytest.mark.parametrize("case", M2_CASES + MN_CASES)
 def test_ref_tables_vs_oracle(ctx, case):
     """BLA tree and derivative paths built on the GPU against the oracle's
     (same operation order; CUDA's hypot may differ from the C library's by an
@@ -176,13 +213,14 @@ def test_ref_tables_vs_oracle(ctx, case):
     xr = bool(d["xr_mode"])
     ref = _ref_from_golden(ctx, d, xr)
     kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
-    Mo, ro, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]))
+    Mo, ro, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]), _nexp(d))
     M, r = ref.download("bla")
     assert ref.stages == st
     np.testing.assert_allclose(r, ro, rtol=1e-14, atol=0)
     np.testing.assert_allclose(M, Mo, rtol=1e-14, atol=0)
     dzo = orc.dzndc_path_m2(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), xr,
-                            float(d["dx_m"]), int(d["dx_e"]), d["xr_idx"], d["xr_m"], d["xr_e"])
+                            float(d["dx_m"]), int(d["dx_e"]), d["xr_idx"], d["xr_m"], d["xr_e"],
+                            nexp=_nexp(d))
     dz = ref.download("dzndc")
     if xr:
         eref = int(dzo[1].max())
@@ -192,7 +230,7 @@ def test_ref_tables_vs_oracle(ctx, case):
         assert np.array_equal(dz.view(np.uint64), dzo.view(np.uint64))
     if bool(d["interior"]):
         dzzo = orc.dzndz_path_m2(d["Zn"], int(d["ref_div_iter"]), xr, d["xr_idx"],
-                                 d["xr_m"], d["xr_e"])
+                                 d["xr_m"], d["xr_e"], nexp=_nexp(d))
         dzz = ref.download("dzndz")
         if xr:
             eref = int(dzzo[1].max())
@@ -202,7 +240,7 @@ def test_ref_tables_vs_oracle(ctx, case):
             assert np.array_equal(dzz.view(np.uint64), dzzo.view(np.uint64))
 
 
-@pytest.mark.parametrize("case", M2_CASES)
+@pytest.mark.parametrize("case", M2_CASES + MN_CASES)
 def test_perturb_m2_reference_branch_vs_oracle(ctx, case):
     """FP64 kernel on the standard-branch cases, XR64 on the Xrange cases."""
     d = load(case)
@@ -387,3 +425,25 @@ def test_dzndc_scale_and_derived_bla(ctx, mode):
         base.free()                 # a base outlives the references derived from it
     derived.free()
     base.free()
+
+
+def test_power_n_rejects_fe32_and_mismatched_exponent(ctx):
+    """The power-n model runs in FP64 / XR64; a reference built for one
+    exponent serves no calculation of another."""
+    from fractalshades_gb300 import _native as nat
+    d = load("pert_mn3_div")
+    ref = _ref_from_golden(ctx, d, False)
+    with pytest.raises(RuntimeError):
+        _run_m2(ctx, d, ref, "fe32", False)
+    nx = int(round(np.sqrt(d["pix"].size)))
+    xs, ys = axes(d["pix"], nx)
+    n = d["pix"].size
+    Z = np.zeros((2, n), dtype=np.complex128)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, stop_reason=sr, stop_iter=si,
+                      ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                      drift_m=complex(d["drift_m"]), drift_e=int(d["drift_e"]), i_dzndc=1)
+    for k in (0, 4):
+        with pytest.raises(RuntimeError):
+            ctx.perturb_tiles(nat.make_calc(max_iter=100, M_divergence=1e3, nexp=k), [t])

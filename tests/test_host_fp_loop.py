@@ -153,3 +153,65 @@ def test_bs_newton_deep_every_flavor(kind):
             found = True
             break
         assert found
+
+
+# ---------------------------------------------------------------------------
+# power-n Mandelbrot (FP_loop.pyx:255-421, 472-604, 618-760, 1139-1340)
+# ---------------------------------------------------------------------------
+# period-10 nuclei of z^3 + c and z^4 + c to 20 digits (the seeds of the
+# power-n golden vectors)
+MN_NUCLEI = {3: ("0.64287667998175895118", "0.25145447487965245909"),
+             4: ("-0.51534888699245770184", "0.46481172994907691405")}
+
+
+@pytest.mark.parametrize("n", [3, 4])
+def test_power_n_orbit_and_partials(n):
+    mpmath.mp.dps = 40
+    x, y = MN_NUCLEI[n]
+    c = mpmath.mpc(x, y)
+    orb = np.zeros(61, dtype=np.complex128)
+    i, partials, xr = fsFP.perturbation_mandelbrotN_FP_loop(
+        orb, True, 60, n, 2000., x.encode(), y.encode(), mpmath.mp.prec)
+    assert i == 61 and not xr
+    z = mpmath.mpc(0)
+    for k in range(1, 61):
+        z = z ** n + c
+        assert orb[k] == complex(float(z.real), float(z.imag))
+    # successive minima of |z_k| below 1e-5: the first return at the period
+    assert list(partials)[0] == 10 and all(k % 10 == 0 for k in partials)
+
+
+@pytest.mark.parametrize("n", [3, 4])
+def test_power_n_ball_newton_size(n):
+    mpmath.mp.dps = 40
+    x, y = MN_NUCLEI[n]
+    c = mpmath.mpc(x, y)
+    prec = mpmath.mp.prec
+    order = fsFP.perturbation_mandelbrotN_ball_method(
+        x.encode(), y.encode(), prec, b"1e-7", n, 10000, 1e5)
+    assert order == 10
+    seed = c + mpmath.mpf("1e-9")
+    ok, nucleus = fsFP.perturbation_mandelbrotN_find_any_nucleus(
+        str(seed.real).encode(), str(seed.imag).encode(), prec, n, 10, 80,
+        str(mpmath.mpf(2) ** -prec).encode(), b"1e-20")
+    assert ok and abs(nucleus - c) < mpmath.mpf("1e-19")
+    z = mpmath.mpc(0)
+    for _ in range(10):
+        z = z ** n + nucleus
+    assert abs(z) < mpmath.mpf("1e-30")
+    size = abs(fsFP.perturbation_mandelbrotN_nucleus_size_estimate(
+        str(nucleus.real).encode(), str(nucleus.imag).encode(), prec, n, 10))
+    # the component's size: at c + size / 4 along any direction the cycle
+    # stays attracting (|d z_10 / d z_0| < 1 at the 10-cycle)
+    assert mpmath.mpf("1e-7") < size < mpmath.mpf("1e-2")
+
+
+def test_power_2_delegates_to_power_2_functions():
+    mpmath.mp.dps = 30
+    a = np.zeros(41, dtype=np.complex128)
+    b = np.zeros(41, dtype=np.complex128)
+    ra = fsFP.perturbation_mandelbrotN_FP_loop(a, False, 40, 2, 1e3, b"-0.1", b"0.65", 100)
+    rb = fsFP.perturbation_mandelbrot_FP_loop(b, False, 40, 1e3, b"-0.1", b"0.65", 100)
+    assert ra[0] == rb[0] and np.array_equal(a, b)
+    with pytest.raises(NotImplementedError):
+        fsFP.perturbation_mandelbrotN_FP_loop(a, False, 40, 1, 1e3, b"0", b"0", 100)
