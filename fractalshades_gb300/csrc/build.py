@@ -1,7 +1,8 @@
 """
 Build libfsgpu.so (the CUDA kernels and the C-ABI of include/fsgpu.h) for
-sm_103a with nvcc, in-tree: objects in fractalshades_gb300/_build/, the shared
-library in fractalshades_gb300/_lib/.
+sm_103a with nvcc, and libfsghost.so (the arbitrary-precision host side of
+include/fsghost.h, g++ against the system MPFR / MPC / GMP), in-tree: objects
+in fractalshades_gb300/_build/, the shared libraries in fractalshades_gb300/_lib/.
 
 The translation units that reproduce the reference's rounding are compiled
 with -fmad=false (no contraction of a*b+c into an FMA); the FP32 fast kernel
@@ -19,6 +20,13 @@ ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libfsgpu.so")
+HOST_LIB = os.path.join(LIBDIR, "libfsghost.so")
+HOST_SRC = os.path.join(HERE, "host", "fsg_host.cpp")
+HOST_DEPS = [HOST_SRC, os.path.join(HERE, "host", "fsg_mp.h"),
+             os.path.join(ROOT, "include", "fsghost.h")]
+# runtime sonames of the libraries the reference's Cython module links
+# (FP_loop.pyx); no development headers are needed (host/fsg_mp.h)
+HOST_LIBS = ["-l:libmpc.so.3", "-l:libmpfr.so.6", "-l:libgmp.so.10"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -50,7 +58,25 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def build_host(verbose=False):
+    """libfsghost.so: g++ -O2, no architecture-specific flags (x86_64 and
+    aarch64 give the same results: MPFR's arithmetic is exact-rounded)."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    if not _stale(HOST_LIB, HOST_DEPS):
+        return HOST_LIB
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-o", HOST_LIB, HOST_SRC,
+           "-Wl,--no-undefined"] + HOST_LIBS
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout + r.stderr)
+    return HOST_LIB
+
+
 def build(verbose=False, ptxas_info=False):
+    build_host(verbose)
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     hdrs = [os.path.join(HERE, h) for h in HEADERS] + [os.path.join(ROOT, "include", "fsgpu.h")]

@@ -74,3 +74,25 @@ def test_null_arguments_are_rejected(lib):
     assert lib.fsg_perturb_tiles(None, None, None, 0, 0) < 0
     lib.fsg_last_error.restype = ct.c_char_p
     assert lib.fsg_last_error(None) == b"no context"
+
+
+# ---------------------------------------------------------------------------
+# the arbitrary-precision host library (include/fsghost.h)
+# ---------------------------------------------------------------------------
+HOST_HEADER = os.path.join(ROOT, "include", "fsghost.h")
+
+
+def host_declared_functions():
+    src = open(HOST_HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fsh_\w+)\s*\(", src)))
+
+
+def test_host_library_exports_and_binding_cover_the_header():
+    from fractalshades_gb300.csrc import build as nb
+    from fractalshades_gb300 import _host
+    hl = ct.CDLL(nb.build_host())
+    names = host_declared_functions()
+    assert "fsh_orbit_mn" in names and "fsh_nucleus_m2" in names
+    assert not [n for n in names if not hasattr(hl, n)]
+    assert sorted(_host.SYMBOLS) == names

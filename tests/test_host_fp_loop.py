@@ -1,8 +1,10 @@
 """
-Host arbitrary-precision layer (mpmath_utils/FP_loop.py) against the known
-answers of the reference's tests/test_FP_loop.py and its stored FP64 orbits
-(tests/REFERENCE_DATA).  The values below are copied from those tests (they
-are the reference's test vectors, not computed here).
+Host arbitrary-precision layer (mpmath_utils/FP_loop.py over libfsghost.so,
+MPFR / MPC) against the known answers of the reference's
+tests/test_FP_loop.py and its stored FP64 orbits (tests/REFERENCE_DATA), and
+against the independent fixed-point restatement oracle/fp_loop_fixed.py.  The
+known-answer values are copied from the reference's tests (they are its test
+vectors, not computed here).
 """
 import os
 import pickle
@@ -12,6 +14,7 @@ import numpy as np
 import pytest
 
 from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
+from oracle import fp_loop_fixed as fixed
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -108,7 +111,7 @@ def test_bs_ball_method_order_3(x, y, px):
 def _bs_orbit(c, n, kind=1):
     x = y = mpmath.mpf(0)
     for _ in range(n):
-        x, y = fsFP._bs_iter(kind, x, y, c.real, c.imag, lambda u, v: u * v)
+        x, y = fixed._bs_iter(kind, x, y, c.real, c.imag, lambda u, v: u * v)
     return x, y
 
 
@@ -215,3 +218,104 @@ def test_power_2_delegates_to_power_2_functions():
     assert ra[0] == rb[0] and np.array_equal(a, b)
     with pytest.raises(NotImplementedError):
         fsFP.perturbation_mandelbrotN_FP_loop(a, False, 40, 1, 1e3, b"0", b"0", 100)
+
+
+# ---------------------------------------------------------------------------
+# the MPFR library against the fixed-point restatement and exact iteration
+# ---------------------------------------------------------------------------
+def _seeded_nucleus_400():
+    from fractalshades_gb300 import synthetic as syn
+    mpmath.mp.dps = 400
+    return syn.nucleus(2562, 400)
+
+
+def test_native_m2_orbit_registers_and_period_vs_fixed_point():
+    """Period-2562 nucleus at 400 digits: the orbit (every double), the exit
+    index and both registers equal the fixed-point restatement's, whose
+    values are correctly rounded from 64 guard bits; the ball method finds
+    the period in both."""
+    c = _seeded_nucleus_400()
+    prec = mpmath.mp.prec
+    sx, sy = str(c.real).encode(), str(c.imag).encode()
+    a = np.zeros(2563, dtype=np.complex128)
+    b = np.zeros(2563, dtype=np.complex128)
+    ra = fsFP.perturbation_mandelbrot_FP_loop(a, True, 2562, 2000., sx, sy, prec)
+    rb = fixed.perturbation_mandelbrot_FP_loop(b, True, 2562, 2000., sx, sy, prec)
+    assert ra[0] == rb[0] == 2563
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert sorted(ra[1]) == sorted(rb[1]) and sorted(ra[2]) == sorted(rb[2])
+    for reg_a, reg_b in ((ra[1], rb[1]), (ra[2], rb[2])):
+        for k in reg_a:
+            if k < 2562:
+                assert reg_a[k] == reg_b[k]
+            else:
+                # z_p of a 400-digit nucleus: rounding noise of either method
+                for r in (reg_a[k], reg_b[k]):
+                    assert r.e < -1200
+    px = b"1e-300"
+    assert fsFP.perturbation_mandelbrot_ball_method(sx, sy, prec, px, 3000, 1e5) == 2562
+    assert fixed.perturbation_mandelbrot_ball_method(sx, sy, prec, px, 3000, 1e5) == 2562
+
+
+def test_native_m2_newton_and_size_vs_fixed_point():
+    c = _seeded_nucleus_400()
+    prec = mpmath.mp.prec
+    seed = c + mpmath.mpf("1e-200")
+    eps = str(mpmath.mpf(2) ** -prec).encode()
+    args = (str(seed.real).encode(), str(seed.imag).encode(), prec, 2562, 80, eps, b"1e-300")
+    ok_a, ca = fsFP.perturbation_mandelbrot_find_nucleus(*args)
+    ok_b, cb = fixed.perturbation_mandelbrot_find_nucleus(*args)
+    assert ok_a and ok_b
+    assert abs(ca - c) < mpmath.mpf(10) ** -395 and abs(ca - cb) < mpmath.mpf(10) ** -395
+    sa = fsFP.perturbation_mandelbrot_nucleus_size_estimate(
+        str(c.real).encode(), str(c.imag).encode(), prec, 2562)
+    sb = fixed.perturbation_mandelbrot_nucleus_size_estimate(
+        str(c.real).encode(), str(c.imag).encode(), prec, 2562)
+    assert abs(sa - sb) < 1e-15 * abs(sb)
+
+
+@pytest.mark.parametrize("kind", [1, 2, 3, 4, 5])
+def test_native_bs_orbit_vs_fixed_point_and_exact(kind):
+    """Burning Ship family at 300 bits: the orbit doubles equal the fixed-
+    point restatement's and the correctly rounded values of a 600-bit
+    iteration; the Xrange register records the coordinates below 1e-300."""
+    with mpmath.workprec(300):
+        a0, b0 = mpmath.mpf("-1.7545128115395"), mpmath.mpf("0.0015894811966473")
+        sx, sy = str(a0).encode(), str(b0).encode()
+    n = 400
+    o = np.zeros(n + 1, dtype=np.complex128)
+    f = np.zeros(n + 1, dtype=np.complex128)
+    ia, pa, xa = fsFP.perturbation_nonholomorphic_FP_loop(o, True, n, 1e3, sx, sy, 300, kind)
+    ib, _, _ = fixed.perturbation_nonholomorphic_FP_loop(f, True, n, 1e3, sx, sy, 300, kind)
+    assert ia == ib
+    assert np.array_equal(o[:ia].view(np.uint64), f[:ia].view(np.uint64))
+    with mpmath.workprec(600):
+        x = y = mpmath.mpf(0)
+        a, b = mpmath.mpf(sx.decode()), mpmath.mpf(sy.decode())
+        for k in range(1, min(ia, n) + 1):
+            x, y = fixed._bs_iter(kind, x, y, a, b, lambda u, v: u * v)
+            assert o[k] == complex(float(x), float(y)), (kind, k)
+    assert all(k % 1 == 0 for k in pa)
+    for k, ((mx, ex), (my, ey)) in xa.items():
+        assert min(abs(o[k].real), abs(o[k].imag)) < 1e-300
+
+
+def test_native_mn_matches_fixed_point():
+    mpmath.mp.dps = 60
+    x, y = MN_NUCLEI[3]
+    a = np.zeros(301, dtype=np.complex128)
+    b = np.zeros(301, dtype=np.complex128)
+    ra = fsFP.perturbation_mandelbrotN_FP_loop(a, False, 300, 3, 1e3, x.encode(), y.encode(),
+                                               mpmath.mp.prec)
+    rb = fixed.perturbation_mandelbrotN_FP_loop(b, False, 300, 3, 1e3, x.encode(), y.encode(),
+                                                mpmath.mp.prec)
+    assert ra[0] == rb[0] and np.array_equal(a, b) and sorted(ra[1]) == sorted(rb[1])
+
+
+def test_host_errors_are_reported():
+    from fractalshades_gb300 import _host
+    o = np.zeros(11, dtype=np.complex128)
+    with pytest.raises(_host.HostError):
+        fsFP.perturbation_mandelbrot_FP_loop(o, False, 10, 1e3, b"not-a-number", b"0", 100)
+    with pytest.raises(ValueError):
+        fsFP.perturbation_mandelbrot_FP_loop(o, False, 20, 1e3, b"0", b"0", 100)
