@@ -237,26 +237,69 @@ static inline cplx c_from_pix(cplx pix, const double *lin_mat, double dx, cplx c
  * core.py:2965-3004 numba_iterate, models/mandelbrot_M2.py:309-334 iterate_once.
  * Z codes: zn = 0, dzndz = 1, dzndc = 2 (mandelbrot_M2.py:107-111).
  */
+/* Orbit snapshots of calc_orbit (core.py:2965-3004 numba_iterate,
+ * perturbation.py:1096-1101, 1265-1273, 1389-1396): every time n // backshift
+ * grows, the two last snapshots shift; at exit the older one is iterated
+ * forward to iteration n - backshift. */
+typedef struct { int64_t div_shift, i1, i2; cplx z1, z2; } orbit_snap;
+static inline void snap_init(orbit_snap *s, cplx z0) {
+    s->div_shift = 0; s->i1 = 0; s->i2 = 0; s->z1 = z0; s->z2 = z0;
+}
+static inline void snap_take(orbit_snap *s, int64_t n, int64_t backshift, cplx z) {
+    int64_t div = n / backshift;
+    if (div > s->div_shift) { s->div_shift = div; s->i2 = s->i1; s->z2 = s->z1; s->i1 = n; s->z1 = z; }
+}
+
+/* Burning Ship maps, models/burning_ship.py:82-123 BS_iterate (xn ** 2 as
+ * xn * xn, the lowering numba applies) */
+static inline void bs_iterate(int flavor, double X, double Y, double a, double b,
+                              double *nX, double *nY) {
+    switch (flavor) {
+    case 1: *nX = X * X - Y * Y + a; *nY = 2. * fabs(X * Y) - b; break;
+    case 2: *nX = X * X - Y * Y + a; *nY = 2. * X * fabs(Y) - b; break;
+    case 3: *nX = X * X - Y * fabs(Y) + a; *nY = 2. * X * Y - b; break;
+    case 4: *nX = fabs(X * X - Y * Y) + a; *nY = 2. * X * Y - b; break;
+    default: *nX = fabs(X * X - Y * Y) + a; *nY = 2. * fabs(X * Y) - b; break;
+    }
+}
+
 EXPORT int orc_std_m2(int64_t npts, const double *pix, double cx, double cy,
                       const double *lin_mat, double dx, int64_t max_iter,
                       double M2, double eps2, double *Z, int32_t *stop_iter,
-                      int8_t *stop_reason) {
+                      int8_t *stop_reason, int32_t nZ, int32_t calc_d2, int32_t backshift) {
+    /* Z rows: zn, dzndz, dzndc, [d2zndc2], [zn_orbit] (mandelbrot_M2.py:107-124) */
     cplx *Zc = (cplx *)Z;
+    const int64_t i_d2 = 3, i_orb = 3 + (calc_d2 ? 1 : 0);
     for (int64_t i = 0; i < npts; i++) {
         cplx c = c_from_pix(C(pix[2 * i], pix[2 * i + 1]), lin_mat, dx, C(cx, cy));
         cplx zn = Zc[i], dzndz = Zc[npts + i], dzndc = Zc[2 * npts + i];
+        cplx d2 = calc_d2 ? Zc[i_d2 * npts + i] : C(0., 0.);
+        orbit_snap S; snap_init(&S, zn);
         int64_t n = 0; int8_t reason = -1;
         for (;;) {
             n += 1;
-            if (n >= max_iter) { reason = 0; break; }                         /* :312-314 */
+            int ret = 1;
+            if (n >= max_iter) { reason = 0; goto snap; }                    /* :312-314 */
+            if (calc_d2)                                                      /* :316-317 */
+                d2 = rmul(2., cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
             dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);                     /* :319 */
             dzndz = cmul(rmul(2., dzndz), zn);                                /* :320 */
             zn = cadd(cmul(zn, zn), c);                                       /* :321 */
             if (n == 1) dzndz = C(1., 0.);                                    /* :323-324 */
-            if (zn.re * zn.re + zn.im * zn.im > M2) { reason = 1; break; }   /* :326-328 */
-            if (dzndz.re * dzndz.re + dzndz.im * dzndz.im < eps2) { reason = 2; break; }
+            if (zn.re * zn.re + zn.im * zn.im > M2) { reason = 1; goto snap; } /* :326-328 */
+            if (dzndz.re * dzndz.re + dzndz.im * dzndz.im < eps2) { reason = 2; goto snap; }
+            ret = 0;
+        snap:
+            if (backshift > 0) snap_take(&S, n, backshift, zn);               /* core.py:2984-2991 */
+            if (ret) break;
         }
         Zc[i] = zn; Zc[npts + i] = dzndz; Zc[2 * npts + i] = dzndc;
+        if (calc_d2) Zc[i_d2 * npts + i] = d2;
+        if (backshift > 0 && i_orb < nZ) {                                    /* core.py:2996-3001 */
+            cplx zo = S.z2;
+            while (S.i2 < n - backshift) { zo = cadd(cmul(zo, zo), c); S.i2 += 1; }
+            Zc[i_orb * npts + i] = zo;
+        }
         stop_iter[i] = (int32_t)n; stop_reason[i] = reason;
     }
     return 0;
@@ -359,26 +402,52 @@ static inline xc mn_p_deriv_x(int n, const double *Cb, xc z, xc d, xc ref, xc rd
 EXPORT int orc_std_mn(int64_t npts, const double *pix, double cx, double cy,
                       const double *lin_mat, double dx, int64_t max_iter,
                       double M2, double eps2, int32_t nexp, double *Z, int32_t *stop_iter,
-                      int8_t *stop_reason) {
+                      int8_t *stop_reason, int32_t nZ, int32_t calc_d2, int32_t backshift) {
+    /* Z rows: zn, dzndz, dzndc, [d2zndc2], [zn_orbit] (mandelbrot_Mn.py:104-124) */
     cplx *Zc = (cplx *)Z;
     const double deg = (double)nexp;
+    const int64_t i_d2 = 3, i_orb = 3 + (calc_d2 ? 1 : 0);
     for (int64_t i = 0; i < npts; i++) {
         cplx c = c_from_pix(C(pix[2 * i], pix[2 * i + 1]), lin_mat, dx, C(cx, cy));
         cplx zn = Zc[i], dzndz = Zc[npts + i], dzndc = Zc[2 * npts + i];
+        cplx d2 = calc_d2 ? Zc[i_d2 * npts + i] : C(0., 0.);
+        orbit_snap S; snap_init(&S, zn);
         int64_t n = 0; int8_t reason = -1;
         for (;;) {
             n += 1;
-            if (n >= max_iter) { reason = 0; break; }
-            cplx zm1 = mn_ipow(zn, nexp - 1);
-            cplx zm = cmul(zm1, zn);
+            int ret = 1;
+            if (n >= max_iter) { reason = 0; goto snap; }
+            cplx zm1, zm;
+            if (calc_d2) {                                  /* mandelbrot_Mn.py:325-333 */
+                cplx zm2 = mn_ipow(zn, nexp - 2);
+                zm1 = cmul(zm2, zn);
+                zm = cmul(zm1, zn);
+                /* the reference multiplies by dzndz here, not by dzndc */
+                d2 = rmul(deg, cadd(cmul(d2, zm1),
+                                    cmul(cmul(rmul((double)(nexp - 1), dzndz), dzndc), zm2)));
+            } else {
+                zm1 = mn_ipow(zn, nexp - 1);
+                zm = cmul(zm1, zn);
+            }
             dzndc = caddr(cmul(rmul(deg, dzndc), zm1), 1.);
             dzndz = cmul(rmul(deg, dzndz), zm1);
             zn = cadd(zm, c);
             if (n == 1) dzndz = C(1., 0.);
-            if (zn.re * zn.re + zn.im * zn.im > M2) { reason = 1; break; }
-            if (dzndz.re * dzndz.re + dzndz.im * dzndz.im < eps2) { reason = 2; break; }
+            if (zn.re * zn.re + zn.im * zn.im > M2) { reason = 1; goto snap; }
+            if (dzndz.re * dzndz.re + dzndz.im * dzndz.im < eps2) { reason = 2; goto snap; }
+            ret = 0;
+        snap:
+            if (backshift > 0) snap_take(&S, n, backshift, zn);
+            if (ret) break;
         }
         Zc[i] = zn; Zc[npts + i] = dzndz; Zc[2 * npts + i] = dzndc;
+        if (calc_d2) Zc[i_d2 * npts + i] = d2;
+        if (backshift > 0 && i_orb < nZ) {
+            /* Mn_iterate (mandelbrot_Mn.py:13-17): zn ** n + c */
+            cplx zo = S.z2;
+            while (S.i2 < n - backshift) { zo = cadd(mn_ipow(zo, nexp), c); S.i2 += 1; }
+            Zc[i_orb * npts + i] = zo;
+        }
         stop_iter[i] = (int32_t)n; stop_reason[i] = reason;
     }
     return 0;
@@ -393,17 +462,24 @@ EXPORT int orc_std_mn(int64_t npts, const double *pix, double cx, double cy,
 EXPORT int orc_std_bs(int64_t npts, const double *pix, double cx, double cy,
                       const double *lin_mat, double dx, int32_t flavor,
                       int64_t max_iter, double M2, double *Z, int32_t *stop_iter,
-                      int8_t *stop_reason) {
+                      int8_t *stop_reason, int32_t nZ, int32_t backshift) {
+    /* Z rows: xn, yn, dxnda, dxndb, dynda, dyndb, [xn_orbit, yn_orbit]
+     * (burning_ship.py:264-289); orbit snapshots core.py:3016-3047 */
     for (int64_t i = 0; i < npts; i++) {
         cplx c = c_from_pix(C(pix[2 * i], pix[2 * i + 1]), lin_mat, dx, C(cx, cy));
         double a = c.re, b = c.im;
         double X = Z[i], Y = Z[npts + i];
         double dXdA = Z[2 * npts + i], dXdB = Z[3 * npts + i];
         double dYdA = Z[4 * npts + i], dYdB = Z[5 * npts + i];
+        orbit_snap S; snap_init(&S, C(X, Y));
         int64_t n = 0; int8_t reason = -1;
         for (;;) {
             n += 1;
-            if (n >= max_iter) { reason = 0; break; }
+            if (n >= max_iter) {
+                reason = 0;
+                if (backshift > 0) snap_take(&S, n, backshift, C(X, Y));
+                break;
+            }
             double nX, nY, ndXdA, ndXdB, ndYdA, ndYdB;
             switch (flavor) {
             case 1: /* burning_ship.py:383-390 */
@@ -450,10 +526,21 @@ EXPORT int orc_std_bs(int64_t npts, const double *pix, double cx, double cy,
             } break;
             }
             X = nX; Y = nY; dXdA = ndXdA; dXdB = ndXdB; dYdA = ndYdA; dYdB = ndYdB;
-            if (X * X + Y * Y > M2) { reason = 1; break; }                  /* :431-433 */
+            int esc = X * X + Y * Y > M2;                                   /* :431-433 */
+            if (backshift > 0) snap_take(&S, n, backshift, C(X, Y));
+            if (esc) { reason = 1; break; }
         }
         Z[i] = X; Z[npts + i] = Y; Z[2 * npts + i] = dXdA; Z[3 * npts + i] = dXdB;
         Z[4 * npts + i] = dYdA; Z[5 * npts + i] = dYdB;
+        if (backshift > 0 && nZ >= 8) {
+            double xo = S.z2.re, yo = S.z2.im;
+            while (S.i2 < n - backshift) {
+                double nx_, ny_;
+                bs_iterate(flavor, xo, yo, a, b, &nx_, &ny_);
+                xo = nx_; yo = ny_; S.i2 += 1;
+            }
+            Z[6 * npts + i] = xo; Z[7 * npts + i] = yo;
+        }
         stop_iter[i] = (int32_t)n; stop_reason[i] = reason;
     }
     return 0;
@@ -750,6 +837,8 @@ typedef struct {
     double lin_mat[4]; double dx_m; int32_t dx_e; double drift_re; double drift_im; int32_t drift_e;
     /* 0: power-2 model (mandelbrot_M2.py closures); n >= 2: power-n (mandelbrot_Mn.py) */
     int32_t nexp;
+    /* calc_orbit: snapshots every backshift iterations (0: off) into row i_znorbit */
+    int32_t backshift; int32_t i_znorbit;
 } orc_pm2_args;
 
 static inline cplx path_c(const double *p, int64_t i) { return C(p[2 * i], p[2 * i + 1]); }
@@ -796,6 +885,7 @@ EXPORT int orc_perturb_m2(const orc_pm2_args *P, int64_t npts, const double *pix
 
         int64_t w = 0, n = 0; int8_t stop = -1;
         int nullify = 0; int64_t w_wrapped = plen;   /* len(dZndz_path) - 1 */
+        orbit_snap S; snap_init(&S, Z[zn]);          /* :1096-1101 */
         int dyn = 1;
         for (;;) {
             /* BLA step :1121-1154 */
@@ -879,6 +969,7 @@ EXPORT int orc_perturb_m2(const orc_pm2_args *P, int64_t npts, const double *pix
             if (xr && has_xr) next_is_xr = xr_lookup(&T, w, &ref_next_xr);
             cplx ZZ = cadd(Z[zn], ref_next);
             double sq = ZZ.re * ZZ.re + ZZ.im * ZZ.im;
+            if (P->backshift > 0) snap_take(&S, n, P->backshift, ZZ);       /* :1265-1273 */
             if (sq > P->M2) { stop = 1; break; }
             /* rebase when the reference diverges :1283-1313 */
             if (w >= div_iter - 1) {
@@ -943,6 +1034,15 @@ EXPORT int orc_perturb_m2(const orc_pm2_args *P, int64_t npts, const double *pix
         } else {
             Z[zn] = cadd(Z[zn], path_c(P->Zn, w));
             if (calc_dzndc) Z[dzndc] = cadd(Z[dzndc], path_c(P->dZndc, w));
+        }
+        if (P->backshift > 0 && P->i_znorbit >= 0) {                          /* :1389-1396 */
+            cplx CC = cadd(c, path_c(P->Zn, 1));
+            cplx zo = S.z2;
+            while (S.i2 < n - P->backshift) {
+                zo = nexp ? cadd(mn_ipow(zo, nexp), CC) : cadd(cmul(zo, zo), CC);
+                S.i2 += 1;
+            }
+            Z[P->i_znorbit] = zo;
         }
         for (int k = 0; k < nZ; k++) Zc[k * npts + ip] = Z[k];
         stop_iter[ip] = (int32_t)n; stop_reason[ip] = stop;
@@ -1080,6 +1180,9 @@ typedef struct {
     int64_t max_iter; double M2; int32_t flavor; int32_t calc_hessian;
     double lin_mat[4]; double dx_m; int32_t dx_e; double driftx_m; int32_t driftx_e;
     double drifty_m; int32_t drifty_e;
+    /* calc_orbit: snapshots every backshift iterations (0: off) into rows
+     * i_xnorbit, i_xnorbit + 1 */
+    int32_t backshift; int32_t i_xnorbit;
 } orc_pbs_args;
 
 EXPORT int orc_perturb_bs(const orc_pbs_args *P, int64_t npts, const double *pix,
@@ -1104,6 +1207,7 @@ EXPORT int orc_perturb_bs(const orc_pbs_args *P, int64_t npts, const double *pix
         double h[4] = {0., 0., 0., 0.};
         if (hess) for (int k = 0; k < 4; k++) h[k] = Zout[(2 + k) * npts + ip];
         int64_t w = 0, n = 0; int8_t stop = -1; int dyn = 1;
+        orbit_snap S; snap_init(&S, C(xn, yn));      /* perturbation.py:1501-1508 */
         for (;;) {
             if (P->bla_on && (w & 7) == 0) {
                 int64_t ib;
@@ -1134,7 +1238,9 @@ EXPORT int orc_perturb_bs(const orc_pbs_args *P, int64_t npts, const double *pix
             w += 1;
             if (w >= order) w = w % order;
             double XX = xn + P->Zn[2 * w], YY = yn + P->Zn[2 * w + 1];
-            if (XX * XX + YY * YY > P->M2) { stop = 1; break; }
+            double sq = XX * XX + YY * YY;
+            if (P->backshift > 0) snap_take(&S, n, P->backshift, C(XX, YY));  /* :1641-1651 */
+            if (sq > P->M2) { stop = 1; break; }
             if (w >= div_iter - 1) {
                 xn = XX; yn = YY;
                 if (hess) { h[0] += P->dXa[w]; h[1] += P->dXb[w]; h[2] += P->dYa[w]; h[3] += P->dYb[w]; }
@@ -1152,6 +1258,18 @@ EXPORT int orc_perturb_bs(const orc_pbs_args *P, int64_t npts, const double *pix
         if (hess) { h[0] += P->dXa[w]; h[1] += P->dXb[w]; h[2] += P->dYa[w]; h[3] += P->dYb[w]; }
         Zout[ip] = xn; Zout[npts + ip] = yn;
         if (hess) for (int k = 0; k < 4; k++) Zout[(2 + k) * npts + ip] = h[k];
+        if (P->backshift > 0 && P->i_xnorbit >= 0) {                          /* :1778-1787 */
+            /* AA, BB as the reference forms them: b + Im(Z_1) with Im(Z_1) = -b_ref,
+             * so BB = b - b_ref rather than the pixel's b + b_ref */
+            double AA = a + P->Zn[2], BB = b + P->Zn[3];
+            double xo = S.z2.re, yo = S.z2.im;
+            while (S.i2 < n - P->backshift) {
+                double nx_, ny_;
+                bs_iterate(P->flavor, xo, yo, AA, BB, &nx_, &ny_);
+                xo = nx_; yo = ny_; S.i2 += 1;
+            }
+            Zout[P->i_xnorbit * npts + ip] = xo; Zout[(P->i_xnorbit + 1) * npts + ip] = yo;
+        }
         stop_iter[ip] = (int32_t)n; stop_reason[ip] = stop;
     }
     return 0;

@@ -50,6 +50,7 @@ class PM2Args(ct.Structure):
         ("i_dzndz", I32), ("i_dzndc", I32), ("dzndz_carryover", I32),
         ("lin_mat", F64 * 4), ("dx_m", F64), ("dx_e", I32),
         ("drift_re", F64), ("drift_im", F64), ("drift_e", I32), ("nexp", I32),
+        ("backshift", I32), ("i_znorbit", I32),
     ]
 
 
@@ -61,14 +62,15 @@ class PBSArgs(ct.Structure):
         ("max_iter", I64), ("M2", F64), ("flavor", I32), ("calc_hessian", I32),
         ("lin_mat", F64 * 4), ("dx_m", F64), ("dx_e", I32),
         ("driftx_m", F64), ("driftx_e", I32), ("drifty_m", F64), ("drifty_e", I32),
+        ("backshift", I32), ("i_xnorbit", I32),
     ]
 
 
 def _declare(L):
     L.orc_xr_binop.argtypes = [ct.c_int, I64] + [P] * 9
-    L.orc_std_m2.argtypes = [I64, P, F64, F64, P, F64, I64, F64, F64, P, P, P]
+    L.orc_std_m2.argtypes = [I64, P, F64, F64, P, F64, I64, F64, F64, P, P, P, I32, I32, I32]
     L.orc_std_m2.restype = ct.c_int
-    L.orc_std_bs.argtypes = [I64, P, F64, F64, P, F64, I32, I64, F64, P, P, P]
+    L.orc_std_bs.argtypes = [I64, P, F64, F64, P, F64, I32, I64, F64, P, P, P, I32, I32]
     L.orc_std_bs.restype = ct.c_int
     L.orc_stages_bla.argtypes = [I64]
     L.orc_stages_bla.restype = I32
@@ -79,7 +81,8 @@ def _declare(L):
     L.orc_dzndc_path_m2.argtypes = [P, I64, I64, I64, I32, I32, P, P, P, P,
                                     F64, I32, P, P, P, P, I32]
     L.orc_dzndz_path_m2.argtypes = [P, I64, I64, I32, I32, P, P, P, P, P, P, P, P, I32]
-    L.orc_std_mn.argtypes = [I64, P, F64, F64, P, F64, I64, F64, F64, I32, P, P, P]
+    L.orc_std_mn.argtypes = [I64, P, F64, F64, P, F64, I64, F64, F64, I32, P, P, P, I32, I32,
+                             I32]
     L.orc_std_mn.restype = ct.c_int
     L.orc_dzndc_path_bs.argtypes = [P, I64, I64, I64, I32, F64, P, P, P, P]
     L.orc_perturb_m2.argtypes = [ct.POINTER(PM2Args), I64, P, P, I32, P, P, P]
@@ -127,40 +130,50 @@ def _cx(re, im):
 # ---------------------------------------------------------------------------
 # Standard loops
 # ---------------------------------------------------------------------------
-def std_m2(pix, center, lin_mat, dx, max_iter, M, eps):
+def std_m2(pix, center, lin_mat, dx, max_iter, M, eps, calc_d2zndc2=False, backshift=0):
+    """Standard power-2 loop; Z rows zn, dzndz, dzndc, [d2zndc2], [zn_orbit]
+    (zn_orbit when backshift > 0, the reference's calc_orbit)."""
     pix = _c(pix, np.complex128)
     n = pix.size
-    Z = np.zeros((3, n), dtype=np.complex128)
+    nZ = 3 + int(bool(calc_d2zndc2)) + int(backshift > 0)
+    Z = np.zeros((nZ, n), dtype=np.complex128)
     si = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
     lm = _c(lin_mat, np.float64).ravel()
     lib().orc_std_m2(n, _p(pix), center.real, center.imag, _p(lm), dx,
-                     max_iter, M * M, eps * eps, _p(Z), _p(si), _p(sr))
+                     max_iter, M * M, eps * eps, _p(Z), _p(si), _p(sr), nZ,
+                     int(bool(calc_d2zndc2)), int(backshift))
     return Z, si, sr
 
 
-def std_mn(pix, center, lin_mat, dx, max_iter, M, eps, nexp):
-    """Standard power-n Mandelbrot (models/mandelbrot_Mn.py:317-355)."""
+def std_mn(pix, center, lin_mat, dx, max_iter, M, eps, nexp, calc_d2zndc2=False, backshift=0):
+    """Standard power-n Mandelbrot (models/mandelbrot_Mn.py:317-355); rows as
+    std_m2."""
     pix = _c(pix, np.complex128)
     n = pix.size
-    Z = np.zeros((3, n), dtype=np.complex128)
+    nZ = 3 + int(bool(calc_d2zndc2)) + int(backshift > 0)
+    Z = np.zeros((nZ, n), dtype=np.complex128)
     si = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
     lm = _c(lin_mat, np.float64).ravel()
     lib().orc_std_mn(n, _p(pix), center.real, center.imag, _p(lm), dx,
-                     max_iter, M * M, eps * eps, int(nexp), _p(Z), _p(si), _p(sr))
+                     max_iter, M * M, eps * eps, int(nexp), _p(Z), _p(si), _p(sr), nZ,
+                     int(bool(calc_d2zndc2)), int(backshift))
     return Z, si, sr
 
 
-def std_bs(pix, center, lin_mat, dx, flavor, max_iter, M):
+def std_bs(pix, center, lin_mat, dx, flavor, max_iter, M, backshift=0):
+    """Standard Burning Ship loop; rows xn, yn, dxnda, dxndb, dynda, dyndb,
+    [xn_orbit, yn_orbit]."""
     pix = _c(pix, np.complex128)
     n = pix.size
-    Z = np.zeros((6, n), dtype=np.float64)
+    nZ = 8 if backshift > 0 else 6
+    Z = np.zeros((nZ, n), dtype=np.float64)
     si = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
     lm = _c(lin_mat, np.float64).ravel()
     lib().orc_std_bs(n, _p(pix), center.real, center.imag, _p(lm), dx, flavor,
-                     max_iter, M * M, _p(Z), _p(si), _p(sr))
+                     max_iter, M * M, _p(Z), _p(si), _p(sr), nZ, int(backshift))
     return Z, si, sr
 
 
@@ -240,7 +253,7 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
                drift_m, drift_e, max_iter, M, eps_stat, xr_mode,
                calc_dzndc=True, interior=False, bla=None, dZndc=None,
                dZndz=None, xr_idx=None, xr_m=None, xr_e=None,
-               carryover=False, Z0=None, nexp=0):
+               carryover=False, Z0=None, nexp=0, backshift=0):
     """bla: (M_bla complex flat, r_bla, stages) or None.  dZndc / dZndz are
     complex arrays (standard form) or (mantissa, exp) tuples (Xrange form)."""
     pix = _c(pix, np.complex128)
@@ -292,6 +305,10 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
     a.dx_m, a.dx_e = float(dx_m), int(dx_e)
     a.drift_re, a.drift_im, a.drift_e = float(np.real(drift_m)), float(np.imag(drift_m)), int(drift_e)
     a.nexp = int(nexp)
+    if backshift > 0:
+        codes.append("zn_orbit")
+    a.backshift = int(backshift)
+    a.i_znorbit = codes.index("zn_orbit") if backshift > 0 else -1
     nZ = len(codes)
     Z = np.zeros((nZ, n), dtype=np.complex128) if Z0 is None else _c(Z0, np.complex128).copy()
     U = np.zeros((1, n), dtype=np.int32)
@@ -303,7 +320,7 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
 
 def perturb_bs(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
                driftx_m, driftx_e, drifty_m, drifty_e, max_iter, M, flavor,
-               calc_hessian=True, bla=None, dpaths=None):
+               calc_hessian=True, bla=None, dpaths=None, backshift=0):
     pix = _c(pix, np.complex128)
     n = pix.size
     Zn = _c(Zn, np.complex128)
@@ -329,6 +346,9 @@ def perturb_bs(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
     a.driftx_m, a.driftx_e = float(driftx_m), int(driftx_e)
     a.drifty_m, a.drifty_e = float(drifty_m), int(drifty_e)
     nZ = 6 if calc_hessian else 2
+    a.backshift = int(backshift)
+    a.i_xnorbit = nZ if backshift > 0 else -1
+    nZ += 2 if backshift > 0 else 0
     Z = np.zeros((nZ, n), dtype=np.float64)
     U = np.zeros((1, n), dtype=np.int32)
     si = np.zeros((1, n), dtype=np.int32)

@@ -397,7 +397,7 @@ def golden_std_bs(out):
 
 def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
                       interior, bla_eps=1e-6, eps_stat=1e-3, M=1000.,
-                      ref_shift=0j, x_offset="0"):
+                      ref_shift=0j, x_offset="0", backshift=0):
     with tempfile.TemporaryDirectory() as d:
         f = fsm.Perturbation_mandelbrot(d)
         x = str(mpmath.mpf(x) + mpmath.mpf(x_offset))
@@ -410,14 +410,14 @@ def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
         f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
                        M_divergence=M, epsilon_stationnary=eps_stat,
                        BLA_eps=bla_eps, interior_detect=interior,
-                       calc_dzndc=True)
+                       calc_dzndc=True, calc_orbit=backshift > 0, backshift=backshift)
         c_pix, Z, U, sr, si, cia = run_tile(f, "pert")
         (_, _, _, Zn_path, dZndc_path, dZndz_path, has_xr, ref_index_xr,
          ref_xr, ref_div_iter, ref_order, drift_xr, dx_xr, _proj, lin_mat,
          lin_scale_xr, kc, M_bla, r_bla, bla_len, stages_bla, _m, _i) = cia
         xr = f.xr_detect_activated
         res = dict(
-            pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si,
+            pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si, backshift=backshift,
             Zn=Zn_path, ref_div_iter=ref_div_iter, ref_order=ref_order,
             xr_mode=int(xr), lin_mat=lin_mat,
             dx_m=np.asarray(dx_xr._mantissa)[0],
@@ -463,7 +463,8 @@ def golden_std_mn(out):
 
 
 def golden_perturb_mn(out, *, nexp, x, y, dx, nx, precision, order, max_iter,
-                      interior, bla_eps=1e-6, eps_stat=1e-3, M=1000., ref_shift=0j):
+                      interior, bla_eps=1e-6, eps_stat=1e-3, M=1000., ref_shift=0j,
+                      backshift=0):
     """Perturbation power-n Mandelbrot (models/mandelbrot_Mn.py:387-740)."""
     with tempfile.TemporaryDirectory() as d:
         f = fsm.Perturbation_mandelbrot_N(d, exponent=nexp)
@@ -476,7 +477,7 @@ def golden_perturb_mn(out, *, nexp, x, y, dx, nx, precision, order, max_iter,
         f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
                        M_divergence=M, epsilon_stationnary=eps_stat,
                        BLA_eps=bla_eps, interior_detect=interior,
-                       calc_dzndc=True)
+                       calc_dzndc=True, calc_orbit=backshift > 0, backshift=backshift)
         c_pix, Z, U, sr, si, cia = run_tile(f, "pert")
         (_, _, _, Zn_path, dZndc_path, dZndz_path, has_xr, ref_index_xr,
          ref_xr, ref_div_iter, ref_order, drift_xr, dx_xr, _proj, lin_mat,
@@ -484,6 +485,7 @@ def golden_perturb_mn(out, *, nexp, x, y, dx, nx, precision, order, max_iter,
         xr = f.xr_detect_activated
         res = dict(
             pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si, nexp=nexp,
+            backshift=backshift,
             Zn=Zn_path, ref_div_iter=ref_div_iter, ref_order=ref_order,
             xr_mode=int(xr), lin_mat=lin_mat,
             dx_m=np.asarray(dx_xr._mantissa)[0],
@@ -510,7 +512,7 @@ def golden_perturb_mn(out, *, nexp, x, y, dx, nx, precision, order, max_iter,
 
 
 def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
-                      bla_eps=1e-6, M=1000.):
+                      bla_eps=1e-6, M=1000., backshift=0):
     with tempfile.TemporaryDirectory() as d:
         f = fsm.Perturbation_burning_ship(d, flavor=flavor)
         f.zoom(precision=precision, x=x, y=y, dx=dx, nx=nx, xy_ratio=1.,
@@ -541,7 +543,8 @@ def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
                      "init_kwargs": init_kwargs, "ref_orbit_len": ref_orbit_len}
         f.save_ref_point(FP_params, orbit)
         f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
-                       M_divergence=M, BLA_eps=bla_eps, calc_hessian=True)
+                       M_divergence=M, BLA_eps=bla_eps, calc_hessian=True,
+                       calc_orbit=backshift > 0, backshift=backshift)
         c_pix, Z, U, sr, si, cia = run_tile(f, "pert")
         (_, _, _, Zn_path, dXa, dXb, dYa, dYb, has_xr, ref_index_xr, refx_xr,
          refy_xr, ref_div_iter, ref_order, driftx_xr, drifty_xr, dx_xr, _p,
@@ -558,8 +561,80 @@ def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
             drifty_m=np.asarray(drifty_xr._mantissa)[0],
             drifty_e=np.asarray(drifty_xr._exp)[0],
             kc_m=np.asarray(kc._mantissa)[0], kc_e=np.asarray(kc._exp)[0],
-            max_iter=max_iter, M=M, bla_eps=bla_eps,
+            max_iter=max_iter, M=M, bla_eps=bla_eps, backshift=backshift,
             M_bla=M_bla, r_bla=r_bla, stages_bla=stages_bla)
+
+
+def golden_std_opts(out):
+    """Standard loops with the optional outputs: d2zndc2 (Milnor) and the
+    orbit point n - backshift (calc_orbit) for the power-2 and power-3
+    models, the orbit point for Burning Ship flavors 1 and 4."""
+    res = {}
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Mandelbrot(d)
+        f.zoom(x=-0.5, y=0., dx=3., nx=32, xy_ratio=1., theta_deg=0.)
+        f.calc_std_div(calc_name="std", subset=None, max_iter=400, M_divergence=1000.,
+                       epsilon_stationnary=0.01, calc_d2zndc2=True, calc_orbit=True,
+                       backshift=3)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+        res.update(pix_m2=c_pix, Z_m2=Z, stop_reason_m2=sr, stop_iter_m2=si,
+                   codes_m2=np.array(f.codes[0]), lin_mat=f.lin_mat)
+    for nexp in (2, 3):
+        with tempfile.TemporaryDirectory() as d:
+            f = fsm.Mandelbrot_N(d, exponent=nexp)
+            f.zoom(x=0., y=0., dx=3., nx=32, xy_ratio=1., theta_deg=0.)
+            f.calc_std_div(calc_name="std", subset=None, max_iter=300, M_divergence=1000.,
+                           epsilon_stationnary=0.01, calc_d2zndc2=True, calc_orbit=True,
+                           backshift=4)
+            c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+            res.update({f"pix_mn{nexp}": c_pix, f"Z_mn{nexp}": Z,
+                        f"stop_reason_mn{nexp}": sr, f"stop_iter_mn{nexp}": si})
+    for flavor_int, flavor in ((1, "Burning ship"), (4, "Celtic")):
+        with tempfile.TemporaryDirectory() as d:
+            f = fsm.Burning_ship(d, flavor=flavor)
+            f.zoom(x=-0.5, y=-0.5, dx=3.5, nx=24, xy_ratio=1., theta_deg=0.)
+            f.calc_std_div(calc_name="std", subset=None, max_iter=200, M_divergence=1000.,
+                           calc_orbit=True, backshift=3)
+            c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+            res.update({f"pix_bs{flavor_int}": c_pix, f"Z_bs{flavor_int}": Z,
+                        f"stop_reason_bs{flavor_int}": sr, f"stop_iter_bs{flavor_int}": si})
+    np.savez_compressed(out, **res)
+
+
+def opts_cases():
+    """The calc_orbit / calc_d2zndc2 options of the standard and perturbation
+    loops."""
+    mpmath.mp.dps = 50
+    golden_std_opts(os.path.join(HERE, "std_opts.npz"))
+    print("std_opts done", flush=True)
+    mpmath.mp.dps = 30
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_orbit.npz"),
+        x="-0.743643887037151", y="0.131825904205330", dx="2.e-9", nx=12,
+        precision=30, order=None, max_iter=6000, interior=False, backshift=5)
+    print("pert_m2_orbit done", flush=True)
+    mpmath.mp.dps = 340
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_xr_orbit.npz"),
+        x="-0.743643887037158704752191506114774e0",
+        y="0.131825904205311970493132056385139", dx="3.e-304", nx=4,
+        precision=340, order=None, max_iter=5000, interior=False,
+        ref_shift=0.31 - 0.27j, x_offset="1e-14", backshift=7)
+    print("pert_m2_xr_orbit done", flush=True)
+    mpmath.mp.dps = 60
+    c3 = mp_nucleus_n(3, 10, 60, mpmath.mpc("0.64287667998175895118", "0.25145447487965245909"))
+    mpmath.mp.dps = 30
+    golden_perturb_mn(
+        os.path.join(HERE, "pert_mn3_orbit.npz"), nexp=3,
+        x=str(c3.real + mpmath.mpf("0.004")), y=str(c3.imag), dx="2.e-3", nx=12,
+        precision=30, order=None, max_iter=3000, interior=False, ref_shift=0.21 - 0.13j,
+        backshift=4)
+    print("pert_mn3_orbit done", flush=True)
+    golden_perturb_bs(
+        os.path.join(HERE, "pert_bs_orbit.npz"),
+        x="-1.773934837092732", y="-0.00025062656641604286", dx="4.e-6",
+        nx=10, precision=30, max_iter=5000, flavor="Burning ship", backshift=6)
+    print("pert_bs_orbit done", flush=True)
 
 
 def golden_xrange(out, seed=100, n=400):
@@ -730,7 +805,9 @@ def mn_cases():
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "mn":
+    if len(sys.argv) > 2 and sys.argv[2] == "opts":
+        opts_cases()
+    elif len(sys.argv) > 2 and sys.argv[2] == "mn":
         mpmath.mp.dps = 50
         golden_std_mn(os.path.join(HERE, "std_mn.npz"))
         mn_cases()

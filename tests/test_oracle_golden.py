@@ -63,6 +63,30 @@ def test_std_m2_matches_reference_bit_exact():
     assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
 
 
+def test_std_options_match_reference_bit_exact():
+    """calc_d2zndc2 and calc_orbit (backshift 3 / 4) of the standard loops:
+    power 2 (mandelbrot_M2.py:316-317, core.py:2965-3004), power 2 and 3 of
+    Mandelbrot_N (mandelbrot_Mn.py:325-333, whose d2zndc2 recurrence uses
+    dzndz) and Burning Ship flavors 1, 4 (core.py:3007-3056)."""
+    d = load("std_opts")
+    lin = d["lin_mat"]
+    Z, si, sr = orc.std_m2(d["pix_m2"], -0.5 + 0j, lin, 3., 400, 1000., 0.01,
+                           calc_d2zndc2=True, backshift=3)
+    assert list(d["codes_m2"]) == ["zn", "dzndz", "dzndc", "d2zndc2", "zn_orbit"]
+    assert np.array_equal(si, d["stop_iter_m2"]) and np.array_equal(sr, d["stop_reason_m2"])
+    assert np.array_equal(Z.view(np.uint64), d["Z_m2"].view(np.uint64))
+    for nexp in (2, 3):
+        Z, si, sr = orc.std_mn(d[f"pix_mn{nexp}"], 0j, lin, 3., 300, 1000., 0.01, nexp,
+                               calc_d2zndc2=True, backshift=4)
+        assert np.array_equal(si, d[f"stop_iter_mn{nexp}"])
+        assert np.array_equal(Z.view(np.uint64), d[f"Z_mn{nexp}"].view(np.uint64)), nexp
+    for fl in (1, 4):
+        Z, si, sr = orc.std_bs(d[f"pix_bs{fl}"], -0.5 - 0.5j, lin, 3.5, fl, 200, 1000.,
+                               backshift=3)
+        assert np.array_equal(si, d[f"stop_iter_bs{fl}"])
+        assert np.array_equal(Z.view(np.uint64), d[f"Z_bs{fl}"].view(np.uint64)), fl
+
+
 @pytest.mark.parametrize("nexp", [3, 4])
 def test_std_mn_matches_reference_bit_exact(nexp):
     """Standard power-n loop (models/mandelbrot_Mn.py:317-355); the fixture's
@@ -92,6 +116,11 @@ def _nexp(d):
     return int(d["nexp"]) if "nexp" in d.files else 0
 
 
+def _backshift(d):
+    """calc_orbit fixtures store the backshift (0: no orbit output)."""
+    return int(d["backshift"]) if "backshift" in d.files else 0
+
+
 def _pm2_inputs(d, recompute_tables):
     xr = bool(d["xr_mode"])
     kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
@@ -102,7 +131,8 @@ def _pm2_inputs(d, recompute_tables):
               max_iter=int(d["max_iter"]), M=float(d["M"]),
               eps_stat=float(d["eps_stat"]), xr_mode=xr,
               interior=bool(d["interior"]), calc_dzndc=True,
-              xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"], nexp=_nexp(d))
+              xr_idx=d["xr_idx"], xr_m=d["xr_m"], xr_e=d["xr_e"], nexp=_nexp(d),
+              backshift=_backshift(d))
     if recompute_tables:
         Mb, rb, _, st = orc.make_bla_m2(d["Zn"], kc, float(d["bla_eps"]), _nexp(d))
         kw["bla"] = (Mb, rb, st)
@@ -135,7 +165,8 @@ def _xr_val(m, e, e_ref=None):
 
 
 PERT_CASES = ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr", "pert_m2_xr_div",
-              "pert_mn3_cycle", "pert_mn3_div", "pert_mn4_xr"]
+              "pert_mn3_cycle", "pert_mn3_div", "pert_mn4_xr",
+              "pert_m2_orbit", "pert_m2_xr_orbit", "pert_mn3_orbit"]
 
 
 @pytest.mark.parametrize("case", PERT_CASES)
@@ -199,7 +230,7 @@ def test_dzndz_carryover_is_erased_by_first_step():
 
 
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4"])
+@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4", "pert_bs_orbit"])
 def test_perturb_bs_matches_reference(case):
     d = load(case)
     fl = int(d["flavor"])
@@ -219,7 +250,7 @@ def test_perturb_bs_matches_reference(case):
         driftx_m=float(d["driftx_m"]), driftx_e=int(d["driftx_e"]),
         drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]),
         max_iter=int(d["max_iter"]), M=float(d["M"]), flavor=fl,
-        bla=(Mb, rb, st), dpaths=paths)
+        bla=(Mb, rb, st), dpaths=paths, backshift=_backshift(d))
     assert np.array_equal(si, d["stop_iter"])
     assert np.array_equal(sr, d["stop_reason"])
     assert np.array_equal(U, d["U"])
