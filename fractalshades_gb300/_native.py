@@ -52,6 +52,7 @@ class Calc(ct.Structure):
         ("max_iter", I64), ("M_divergence", F64), ("epsilon_stationnary", F64),
         ("mode", I32), ("calc_dzndc", I32), ("interior", I32), ("bla", I32),
         ("flavor", I32), ("xr_semantics", I32), ("nexp", I32),
+        ("backshift", I32), ("calc_d2zndc2", I32),
     ]
 
 
@@ -63,7 +64,7 @@ class Tile(ct.Structure):
         ("drift_e", I32), ("drifty_m", F64), ("drifty_e", I32), ("ref", P),
         ("Z", P), ("nZ", I32), ("i_dzndz", I32), ("i_dzndc", I32),
         ("U", P), ("stop_reason", P), ("stop_iter", P), ("potential", P), ("dem", P),
-        ("dzndc_scale_e", I32),
+        ("dzndc_scale_e", I32), ("i_znorbit", I32),
     ]
 
 
@@ -292,7 +293,7 @@ class Reference:
 def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None, U=None,
               ref=None, center=0j, dx=0.0, dx_m=0.0, dx_e=0, drift_m=0j, drift_e=0,
               drifty_m=0.0, drifty_e=0, i_dzndz=-1, i_dzndc=-1, potential=None,
-              dem=None, keep=None, dzndc_scale_e=0):
+              dem=None, keep=None, dzndc_scale_e=0, i_znorbit=0):
     """Fill a Tile from numpy (host) arrays: either the axes xs / ys of a
     rectangle or an explicit complex128 list of pixel positions ``pix``."""
     t = Tile()
@@ -317,6 +318,7 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
     t.stop_reason, t.stop_iter = _p(stop_reason), _p(stop_iter)
     t.potential, t.dem = _p(potential), _p(dem)
     t.dzndc_scale_e = int(dzndc_scale_e)
+    t.i_znorbit = int(i_znorbit)
     if keep is not None:
         keep.extend([xs, ys, pix, Z, U, stop_reason, stop_iter, potential, dem])
     return t
@@ -325,7 +327,7 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
 def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_ptr,
                    stop_iter_ptr, U_ptr=0, ref=None, center=0j, dx=0.0, dx_m=0.0,
                    dx_e=0, drift_m=0j, drift_e=0, drifty_m=0.0, drifty_e=0, i_dzndz=-1,
-                   i_dzndc=-1, potential_ptr=0, dem_ptr=0, dzndc_scale_e=0):
+                   i_dzndc=-1, potential_ptr=0, dem_ptr=0, dzndc_scale_e=0, i_znorbit=0):
     """Fill a Tile from raw device pointers (ints)."""
     t = Tile()
     t.nx, t.ny = int(nx), int(ny)
@@ -344,12 +346,13 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
     t.stop_reason, t.stop_iter = stop_reason_ptr, stop_iter_ptr
     t.potential, t.dem = potential_ptr or None, dem_ptr or None
     t.dzndc_scale_e = int(dzndc_scale_e)
+    t.i_znorbit = int(i_znorbit)
     return t
 
 
 def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
               calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False,
-              nexp=0):
+              nexp=0, backshift=0, calc_d2zndc2=False):
     c = Calc()
     c.max_iter = int(max_iter)
     c.M_divergence = float(M_divergence)
@@ -361,4 +364,6 @@ def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
     c.flavor = int(flavor)
     c.xr_semantics = int(bool(xr_semantics))
     c.nexp = int(nexp)
+    c.backshift = int(backshift)
+    c.calc_d2zndc2 = int(bool(calc_d2zndc2))
     return c

@@ -162,8 +162,15 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
     }
     int nZ_min = perturb ? (calc->flavor == 0 ? 1 + (calc->interior ? 1 : 0) + (calc->calc_dzndc ? 1 : 0)
                                               : (calc->calc_dzndc ? 6 : 2))
-                         : (calc->flavor == 0 ? 3 : 6);
+                         : (calc->flavor == 0 ? 3 + (calc->calc_d2zndc2 ? 1 : 0) : 6);
     if (t.nZ < nZ_min) return set_err(ctx, FSG_ERR_ARG, "tile nZ too small for the requested fields");
+    if (calc->backshift > 0) {
+        // the orbit row(s) come after the fields above (complex zn_orbit, or
+        // the real xn_orbit, yn_orbit pair of the Burning Ship family)
+        const int rows = calc->flavor == 0 ? 1 : 2;
+        if (t.i_znorbit < nZ_min || t.i_znorbit + rows > t.nZ)
+            return set_err(ctx, FSG_ERR_ARG, "bad i_znorbit for calc_orbit");
+    }
     if (perturb && calc->flavor == 0) {
         if (calc->interior && (t.i_dzndz <= 0 || t.i_dzndz >= t.nZ))
             return set_err(ctx, FSG_ERR_ARG, "bad i_dzndz");
@@ -191,6 +198,8 @@ CalcDev make_calc(const fsg_calc *c) {
     d.bla = c->bla; d.flavor = c->flavor; d.xrsem = c->xr_semantics;
     d.nexp = c->nexp;
     d.logd = log(c->nexp ? (double)c->nexp : 2.);
+    d.backshift = c->backshift;
+    d.d2 = c->calc_d2zndc2;
     return d;
 }
 
@@ -209,6 +218,7 @@ TileDev make_tile(const fsg_tile &t) {
     d.U = t.U; d.stop_reason = (signed char *)t.stop_reason; d.stop_iter = t.stop_iter;
     d.pot = t.potential; d.dem = t.dem;
     d.dzs = t.dzndc_scale_e;
+    d.i_orb = t.i_znorbit;
     return d;
 }
 
@@ -275,6 +285,11 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     }
     if (perturb && calc->nexp != 0 && calc->mode == FSG_MODE_FE32)
         return set_err(ctx, FSG_ERR_ARG, "the power-n model runs in FSG_MODE_FP64 or FSG_MODE_XR64");
+    if (calc->backshift < 0) return set_err(ctx, FSG_ERR_ARG, "backshift must be >= 0");
+    if (calc->backshift > 0 && perturb && calc->mode == FSG_MODE_FE32)
+        return set_err(ctx, FSG_ERR_ARG, "calc_orbit runs in FSG_MODE_FP64 or FSG_MODE_XR64");
+    if (calc->calc_d2zndc2 && (perturb || calc->flavor != 0))
+        return set_err(ctx, FSG_ERR_ARG, "calc_d2zndc2 applies to the standard Mandelbrot loops");
     for (int32_t i = 0; i < ntiles; i++) {
         int rc = check_tile(ctx, tiles[i], perturb, calc);
         if (rc != FSG_OK) return rc;

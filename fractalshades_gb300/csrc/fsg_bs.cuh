@@ -250,6 +250,9 @@ FSG_DEV void bs_hess(int flavor, T h[4], T xn, T yn, T X, T Y, T Xa, T Xb, T Ya,
     h[0] = nxa; h[1] = nxb; h[2] = nya; h[3] = nyb;
 }
 
+template <class T> struct IsDouble { static constexpr bool value = false; };
+template <> struct IsDouble<double> { static constexpr bool value = true; };
+
 template <class T>
 FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                       unsigned long long &nfull, unsigned long long &nbla,
@@ -275,6 +278,12 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     T xn = from_d<T>(0.), yn = from_d<T>(0.);
     T h[4] = {from_d<T>(0.), from_d<T>(0.), from_d<T>(0.), from_d<T>(0.)};
     int w = 0, n = 0; signed char stop = -1; bool dyn = true;
+    // calc_orbit snapshots (perturbation.py:1501-1508), FP64 form only: the
+    // FP32 + exponent instantiation compiles without them
+    constexpr bool ORB_FORM = IsDouble<T>::value;
+    const int bs = ORB_FORM ? C.backshift : 0;
+    OrbitSnap<double2> S;
+    S.init(bs, cx(0., 0.));
     for (;;) {
         if (C.bla && (w & 7) == 0) {
             int ib;
@@ -314,6 +323,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         BSRef<T>::orbit(R, w, Xs, Ys);
         T XX = xn + Xs, YY = yn + Ys;
         const double XXd = to_d(XX), YYd = to_d(YY);
+        if (bs > 0) S.take(n, bs, cx(XXd, YYd));                 // :1641-1651
         if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
         if (w >= div_iter - 1) {
             xn = XX; yn = YY;
@@ -347,6 +357,20 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         hd[2] = to_d(scale2(h[2] + Hc, Tl.dzs)); hd[3] = to_d(scale2(h[3] + Hd, Tl.dzs));
     }
     double *Z = (double *)Tl.Z;
+    if (bs > 0) {
+        // :1778-1787: the reference replays with AA = a + Re(Z_1) and
+        // BB = b + Im(Z_1) = b - b_ref (kept as is)
+        const double2 Z1 = __ldg(&R.Zn[1]);
+        const double AA = to_d(a) + Z1.x, BB = to_d(b) + Z1.y;
+        double xr = S.z2.x, yr = S.z2.y;
+        for (int i2 = S.i2; i2 < n - bs; i2++) {
+            double nx_, ny_;
+            bs_map(flavor, xr, yr, AA, BB, nx_, ny_);
+            xr = nx_; yr = ny_;
+        }
+        Z[(long long)Tl.i_orb * np + ip] = xr;
+        Z[(long long)(Tl.i_orb + 1) * np + ip] = yr;
+    }
     Z[ip] = xo; Z[np + ip] = yo;
     if (hess) { Z[2 * np + ip] = hd[0]; Z[3 * np + ip] = hd[1]; Z[4 * np + ip] = hd[2]; Z[5 * np + ip] = hd[3]; }
     if (Tl.U) Tl.U[ip] = w;

@@ -69,6 +69,37 @@ struct TileDev {
     int *U; signed char *stop_reason; int *stop_iter;
     double *pot, *dem;
     int dzs;                                   // dzndc scale 2^dzs over the reference's
+    int i_orb;                                 // Z row of the orbit point
+};
+
+// The Burning Ship map of flavor 1..5 (burning_ship.py:82-123 BS_iterate,
+// x ** 2 as x * x): the orbit replay of calc_orbit
+__device__ __forceinline__ void bs_map(int flavor, double X, double Y, double a, double b,
+                                       double &nX, double &nY) {
+    if (flavor == 1) { nX = X * X - Y * Y + a; nY = 2. * fabs(X * Y) - b; }
+    else if (flavor == 2) { nX = X * X - Y * Y + a; nY = 2. * X * fabs(Y) - b; }
+    else if (flavor == 3) { nX = X * X - Y * fabs(Y) + a; nY = 2. * X * Y - b; }
+    else if (flavor == 4) { nX = fabs(X * X - Y * Y) + a; nY = 2. * X * Y - b; }
+    else { nX = fabs(X * X - Y * Y) + a; nY = 2. * fabs(X * Y) - b; }
+}
+
+// Orbit snapshots of calc_orbit (core.py:2965-3004, perturbation.py:1096-1101,
+// 1265-1273): when n // backshift grows, the last two snapshots shift; at
+// exit the older one is iterated forward to n - backshift.  "n // backshift
+// grew" is tested as n >= next (no division per step).
+template <class V>
+struct OrbitSnap {
+    int next, i1, i2;
+    V z1, z2;
+    __device__ __forceinline__ void init(int backshift, V z0) {
+        next = backshift; i1 = 0; i2 = 0; z1 = z0; z2 = z0;
+    }
+    __device__ __forceinline__ void take(int n, int backshift, V z) {
+        if (n >= next) {
+            next = (n / backshift + 1) * backshift;
+            i2 = i1; z2 = z1; i1 = n; z1 = z;
+        }
+    }
 };
 
 struct CalcDev {
@@ -77,6 +108,8 @@ struct CalcDev {
     int mode, calc_dzndc, interior, bla, flavor, xrsem;
     int nexp;                                  // 0: power-2 model; n: power-n model
     double logd;                               // log of the degree (potential)
+    int backshift;                             // > 0: orbit point n - backshift
+    int d2;                                    // standard loop: d2zndc2 in row 3
 };
 
 // Work distribution of one launch: a device counter hands out pixel indices

@@ -72,6 +72,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     if (calc->flavor < 0 || calc->flavor > 5) return FSG_ERR_ARG;
     if (calc->nexp != 0 && (calc->flavor != 0 || calc->nexp < 2)) return FSG_ERR_ARG;
     if (calc->nexp > FSG_MN_MAX_EXP) return FSG_ERR_LIMIT;
+    if (calc->backshift != 0 || calc->calc_d2zndc2 != 0) return FSG_ERR_ARG;  // fsg_std_tiles
     const int nZ_min = calc->flavor == 0 ? 3 : 6;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return FSG_ERR_NODEV;
@@ -118,6 +119,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     C.mode = FSG_MODE_FP64; C.calc_dzndc = 1; C.interior = 0; C.bla = 0;
     C.flavor = calc->flavor; C.xrsem = 0;
     C.nexp = calc->nexp; C.logd = log(calc->nexp ? (double)calc->nexp : 2.);
+    C.backshift = 0; C.d2 = 0;
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
         return FSG_ERR_CUDA;

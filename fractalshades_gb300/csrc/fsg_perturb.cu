@@ -21,7 +21,7 @@ __device__ __forceinline__ xc ldx(const double2 *m, const int *e, int i) {
     return xc_make(v.x, v.y, __ldg(&e[i]));
 }
 
-template <bool XR, bool MN>
+template <bool XR, bool MN, bool ORB>
 __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, long long ip,
                                          unsigned long long &nfull, unsigned long long &nbla,
                                          unsigned long long &nreb, unsigned long long &itsum) {
@@ -47,6 +47,10 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
     int w = 0, n = 0; signed char stop = -1;
     bool nullify = false, dyn = true;
     const xc xzero = xc_zero();
+    // calc_orbit snapshots :1096-1101
+    const int bs = ORB ? C.backshift : 0;
+    OrbitSnap<double2> S;
+    if (ORB) S.init(bs, zn);
 
     for (;;) {
         // BLA step :1121-1154
@@ -130,6 +134,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         // divergence :1252-1279
         double2 ref_next = __ldg(&R.Zn[w]);
         double2 ZZ = cadd(zn, ref_next);
+        if (ORB) S.take(n, bs, ZZ);                                   // :1265-1273
         if (ZZ.x * ZZ.x + ZZ.y * ZZ.y > C.M2) { stop = 1; break; }
         // rebase when the reference diverges :1283-1313
         if (w >= div_iter - 1) {
@@ -204,6 +209,14 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         }
     }
     double2 *Z = (double2 *)T.Z;
+    if (ORB) {
+        // :1389-1396, the orbit point n - backshift from the full c
+        double2 CC = cadd(c, __ldg(&R.Zn[1]));
+        double2 zo = S.z2;
+        for (int i2 = S.i2; i2 < n - bs; i2++)
+            zo = MN ? cadd(mn_ipow(zo, nexp), CC) : cadd(cmul(zo, zo), CC);
+        Z[(long long)T.i_orb * np + ip] = zo;
+    }
     Z[ip] = zn;
     if (dzndz_on) Z[T.i_dzndz * np + ip] = dzndz;
     if (dzndc_on) Z[T.i_dzndc * np + ip] = dzndc;
@@ -214,7 +227,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
     itsum += (unsigned long long)n;
 }
 
-template <bool XR, bool MN>
+template <bool XR, bool MN, bool ORB>
 __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
@@ -223,7 +236,7 @@ __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
-        pixel_m2<XR, MN>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        pixel_m2<XR, MN, ORB>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
     }
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }
@@ -232,20 +245,27 @@ __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
 // (compiled here, without FMA contraction)
 template __global__ void k_perturb_bs<double>(WorkDev W, CalcDev C);
 
+template <bool XR, bool MN, bool ORB>
+static void launch_m2(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
+    k_perturb_m2<XR, MN, ORB><<<fsg_auto_grid(k_perturb_m2<XR, MN, ORB>, grid, block, W.total),
+                                block, 0, s>>>(W, C);
+}
+
+template <bool ORB>
+static void launch_m2_orb(const WorkDev &W, const CalcDev &C, int grid, int block,
+                          cudaStream_t s) {
+    if (C.nexp != 0 && C.mode == 1) launch_m2<true, true, ORB>(W, C, grid, block, s);
+    else if (C.nexp != 0) launch_m2<false, true, ORB>(W, C, grid, block, s);
+    else if (C.mode == 1) launch_m2<true, false, ORB>(W, C, grid, block, s);
+    else launch_m2<false, false, ORB>(W, C, grid, block, s);
+}
+
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
     if (C.flavor != 0)
         k_perturb_bs<double><<<fsg_auto_grid(k_perturb_bs<double>, grid, block, W.total), block, 0,
                                s>>>(W, C);
-    else if (C.nexp != 0 && C.mode == 1)
-        k_perturb_m2<true, true><<<fsg_auto_grid(k_perturb_m2<true, true>, grid, block, W.total),
-                                   block, 0, s>>>(W, C);
-    else if (C.nexp != 0)
-        k_perturb_m2<false, true><<<fsg_auto_grid(k_perturb_m2<false, true>, grid, block, W.total),
-                                    block, 0, s>>>(W, C);
-    else if (C.mode == 1)
-        k_perturb_m2<true, false><<<fsg_auto_grid(k_perturb_m2<true, false>, grid, block, W.total),
-                                    block, 0, s>>>(W, C);
+    else if (C.backshift > 0)
+        launch_m2_orb<true>(W, C, grid, block, s);
     else
-        k_perturb_m2<false, false><<<fsg_auto_grid(k_perturb_m2<false, false>, grid, block, W.total),
-                                     block, 0, s>>>(W, C);
+        launch_m2_orb<false>(W, C, grid, block, s);
 }

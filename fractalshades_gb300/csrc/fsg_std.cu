@@ -19,29 +19,48 @@ __device__ __forceinline__ double2 std_c(const TileDev &T, long long ip) {
     return cadd(cx(T.cre, T.cim), rmul(T.dx, cx(x1, y1)));
 }
 
+// OPT: the optional outputs d2zndc2 (mandelbrot_M2.py:316-317) and the orbit
+// point n - backshift (core.py:2965-3004)
+template <bool OPT>
 __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long it_sum = 0, steps = 0;
+    const int bs = OPT ? C.backshift : 0;
+    const bool d2_on = OPT && C.d2;
     int t; long long ip;
     while (fsg_claim(W, s_start, t, ip)) {
         const TileDev &T = W.tiles[t];
         long long np = (long long)T.nx * T.ny;
         double2 c = std_c(T, ip);
-        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.);
+        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.), d2 = cx(0., 0.);
+        OrbitSnap<double2> S;
+        if (OPT) S.init(bs, zn);
         int n = 0; signed char reason = -1;
         for (;;) {
             n += 1;
-            if (n >= C.max_iter) { reason = 0; break; }
+            bool stop = true;
+            if (n >= C.max_iter) { reason = 0; goto snap; }
+            if (d2_on) d2 = rmul(2., cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
             dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);
             dzndz = cmul(rmul(2., dzndz), zn);
             zn = cadd(cmul(zn, zn), c);
             if (n == 1) dzndz = cx(1., 0.);
-            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; break; }
-            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; break; }
+            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; goto snap; }
+            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; goto snap; }
+            stop = false;
+        snap:
+            if (OPT && bs > 0) S.take(n, bs, zn);
+            if (stop) break;
         }
         double2 *Z = (double2 *)T.Z;
         Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
+        if (d2_on) Z[3 * np + ip] = d2;
+        if (OPT && bs > 0) {
+            double2 zo = S.z2;
+            for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(cmul(zo, zo), c);   // M2_iterate
+            Z[(long long)T.i_orb * np + ip] = zo;
+        }
         T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
         fsg_epilogue(T, C, ip, zn, hypot(dzndc.x, dzndc.y), n);
         it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
@@ -51,33 +70,60 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
 
 // Power-n Mandelbrot: models/mandelbrot_Mn.py:317-355 iterate_once
 // (calc_d2zndc2 False): z^(n-1) once per step, z^n = z^(n-1) z.
+template <bool OPT>
 __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long it_sum = 0, steps = 0;
     const int nexp = C.nexp;
     const double deg = (double)nexp;
+    const int bs = OPT ? C.backshift : 0;
+    const bool d2_on = OPT && C.d2;
     int t; long long ip;
     while (fsg_claim(W, s_start, t, ip)) {
         const TileDev &T = W.tiles[t];
         long long np = (long long)T.nx * T.ny;
         double2 c = std_c(T, ip);
-        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.);
+        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.), d2 = cx(0., 0.);
+        OrbitSnap<double2> S;
+        if (OPT) S.init(bs, zn);
         int n = 0; signed char reason = -1;
         for (;;) {
             n += 1;
-            if (n >= C.max_iter) { reason = 0; break; }
-            double2 zm1 = mn_ipow(zn, nexp - 1);
-            double2 zm = cmul(zm1, zn);
+            bool stop = true;
+            double2 zm1, zm;
+            if (n >= C.max_iter) { reason = 0; goto snap; }
+            if (d2_on) {
+                // mandelbrot_Mn.py:325-333; the reference's recurrence
+                // multiplies by dzndz where d/dc of n z^(n-1) dzndc has dzndc
+                double2 zm2 = mn_ipow(zn, nexp - 2);
+                zm1 = cmul(zm2, zn);
+                zm = cmul(zm1, zn);
+                d2 = rmul(deg, cadd(cmul(d2, zm1),
+                                    cmul(cmul(rmul((double)(nexp - 1), dzndz), dzndc), zm2)));
+            } else {
+                zm1 = mn_ipow(zn, nexp - 1);
+                zm = cmul(zm1, zn);
+            }
             dzndc = caddr(cmul(rmul(deg, dzndc), zm1), 1.);
             dzndz = cmul(rmul(deg, dzndz), zm1);
             zn = cadd(zm, c);
             if (n == 1) dzndz = cx(1., 0.);
-            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; break; }
-            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; break; }
+            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; goto snap; }
+            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; goto snap; }
+            stop = false;
+        snap:
+            if (OPT && bs > 0) S.take(n, bs, zn);
+            if (stop) break;
         }
         double2 *Z = (double2 *)T.Z;
         Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
+        if (d2_on) Z[3 * np + ip] = d2;
+        if (OPT && bs > 0) {
+            double2 zo = S.z2;
+            for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(mn_ipow(zo, nexp), c);   // Mn_iterate
+            Z[(long long)T.i_orb * np + ip] = zo;
+        }
         T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
         fsg_epilogue(T, C, ip, zn, hypot(dzndc.x, dzndc.y), n);
         it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
@@ -85,11 +131,14 @@ __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
     fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
 }
 
+// OPT: the orbit point n - backshift (core.py:3007-3056)
+template <bool OPT>
 __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long it_sum = 0, steps = 0;
     const int flavor = C.flavor;
+    const int bs = OPT ? C.backshift : 0;
     int t; long long ip;
     while (fsg_claim(W, s_start, t, ip)) {
         const TileDev &T = W.tiles[t];
@@ -97,10 +146,16 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
         double2 c = std_c(T, ip);
         double a = c.x, b = c.y;
         double X = 0., Y = 0., dXdA = 0., dXdB = 0., dYdA = 0., dYdB = 0.;
+        OrbitSnap<double2> S;
+        if (OPT) S.init(bs, cx(0., 0.));
         int n = 0; signed char reason = -1;
         for (;;) {
             n += 1;
-            if (n >= C.max_iter) { reason = 0; break; }
+            if (n >= C.max_iter) {
+                reason = 0;
+                if (OPT && bs > 0) S.take(n, bs, cx(X, Y));
+                break;
+            }
             double nX, nY, nXa, nXb, nYa, nYb;
             if (flavor == 1) {
                 nX = X * X - Y * Y + a;
@@ -141,11 +196,23 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
                 nYb = 2. * (fabs(X) * sgn(Y) * dYdB + sgn(X) * dXdB * fabs(Y)) - 1.;
             }
             X = nX; Y = nY; dXdA = nXa; dXdB = nXb; dYdA = nYa; dYdB = nYb;
-            if (X * X + Y * Y > C.M2) { reason = 1; break; }
+            bool esc = X * X + Y * Y > C.M2;
+            if (OPT && bs > 0) S.take(n, bs, cx(X, Y));
+            if (esc) { reason = 1; break; }
         }
         double *Z = (double *)T.Z;
         Z[ip] = X; Z[np + ip] = Y; Z[2 * np + ip] = dXdA; Z[3 * np + ip] = dXdB;
         Z[4 * np + ip] = dYdA; Z[5 * np + ip] = dYdB;
+        if (OPT && bs > 0) {
+            double xo = S.z2.x, yo = S.z2.y;
+            for (int i2 = S.i2; i2 < n - bs; i2++) {
+                double nx_, ny_;
+                bs_map(flavor, xo, yo, a, b, nx_, ny_);
+                xo = nx_; yo = ny_;
+            }
+            Z[(long long)T.i_orb * np + ip] = xo;
+            Z[(long long)(T.i_orb + 1) * np + ip] = yo;
+        }
         T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
         double absd = 0.5 * (hypot(dXdA + dYdB, dXdB - dYdA) + hypot(dXdA - dYdB, dXdB + dYdA));
         fsg_epilogue(T, C, ip, cx(X, Y), absd, n);
@@ -154,9 +221,17 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
     fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
 }
 
-void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
+template <bool OPT>
+static void launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
     if (C.flavor == 0 && C.nexp != 0)
-        k_std_mn<<<fsg_auto_grid(k_std_mn, grid, block, W.total), block, 0, s>>>(W, C);
-    else if (C.flavor == 0) k_std_m2<<<fsg_auto_grid(k_std_m2, grid, block, W.total), block, 0, s>>>(W, C);
-    else k_std_bs<<<fsg_auto_grid(k_std_bs, grid, block, W.total), block, 0, s>>>(W, C);
+        k_std_mn<OPT><<<fsg_auto_grid(k_std_mn<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+    else if (C.flavor == 0)
+        k_std_m2<OPT><<<fsg_auto_grid(k_std_m2<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+    else
+        k_std_bs<OPT><<<fsg_auto_grid(k_std_bs<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+}
+
+void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
+    if (C.backshift > 0 || C.d2) launch_std<true>(W, C, grid, block, s);
+    else launch_std<false>(W, C, grid, block, s);
 }

@@ -43,21 +43,35 @@ def clear_cancel():
 class StdSpec:
     """Options of a standard (non-perturbation) calculation."""
 
-    def __init__(self, *, flavor, max_iter, M_divergence, epsilon_stationnary=0., nexp=0):
+    def __init__(self, *, flavor, max_iter, M_divergence, epsilon_stationnary=0., nexp=0,
+                 calc_d2zndc2=False, backshift=0):
         self.flavor = int(flavor)
         self.max_iter = int(max_iter)
         self.M_divergence = float(M_divergence)
         self.epsilon_stationnary = float(epsilon_stationnary)
         self.nexp = int(nexp)     # 0: power-2 model, n: power-n model
+        self.calc_d2zndc2 = bool(calc_d2zndc2)
+        self.backshift = int(backshift)   # > 0: calc_orbit
 
     def calc(self):
         return nat.make_calc(max_iter=self.max_iter, M_divergence=self.M_divergence,
                              epsilon_stationnary=self.epsilon_stationnary,
-                             flavor=self.flavor, nexp=self.nexp)
+                             flavor=self.flavor, nexp=self.nexp,
+                             calc_d2zndc2=self.calc_d2zndc2, backshift=self.backshift)
+
+    @property
+    def i_znorbit(self):
+        """Z row of zn_orbit (xn_orbit for the Burning Ship family), after the
+        reference's other codes (mandelbrot_M2.py:107-124, burning_ship.py:264-280)"""
+        if self.flavor != 0:
+            return 6
+        return 3 + int(self.calc_d2zndc2)
 
     @property
     def nZ(self):
-        return 3 if self.flavor == 0 else 6
+        if self.flavor != 0:
+            return 6 + (2 if self.backshift > 0 else 0)
+        return 3 + int(self.calc_d2zndc2) + int(self.backshift > 0)
 
 
 class PerturbSpec:
@@ -65,7 +79,7 @@ class PerturbSpec:
 
     def __init__(self, *, flavor, max_iter, M_divergence, epsilon_stationnary=0.,
                  calc_dzndc=True, interior=False, bla=True, xr_detect_activated=False,
-                 i_dzndz=-1, i_dzndc=-1, nZ=1, nexp=0):
+                 i_dzndz=-1, i_dzndc=-1, nZ=1, nexp=0, backshift=0, i_znorbit=0):
         self.flavor = int(flavor)
         self.max_iter = int(max_iter)
         self.M_divergence = float(M_divergence)
@@ -78,10 +92,17 @@ class PerturbSpec:
         self.i_dzndc = int(i_dzndc)
         self.nZ = int(nZ)
         self.nexp = int(nexp)     # 0: power-2 model, n: power-n model
+        self.backshift = int(backshift)   # > 0: calc_orbit, orbit row(s) at i_znorbit
+        self.i_znorbit = int(i_znorbit)
 
     @property
     def mode(self):
         m = settings.precision_mode
+        if self.backshift > 0:
+            # the orbit snapshots are kept by the reference's two delta forms
+            if m == "fe32" or (self.flavor != 0 and self.xr_detect_activated):
+                raise ValueError("calc_orbit runs in the FP64 / Xrange forms: precision_mode "
+                                 "'auto', 'fp64' or 'xr64' (Burning Ship: above dx = 1e-300)")
         if self.nexp != 0:
             # power-n model: the reference's two delta forms (no FE32 kernel)
             if m == "fe32":
@@ -108,7 +129,8 @@ class PerturbSpec:
                              epsilon_stationnary=self.epsilon_stationnary, mode=self.mode,
                              calc_dzndc=self.calc_dzndc, interior=self.interior,
                              bla=self.bla, flavor=self.flavor,
-                             xr_semantics=self.xr_detect_activated, nexp=self.nexp)
+                             xr_semantics=self.xr_detect_activated, nexp=self.nexp,
+                             backshift=self.backshift)
 
 
 def _check_rc(rc):
@@ -128,7 +150,7 @@ def run_std_pixels(cycle_dep_args, cycle_indep_args):
     pix = np.ascontiguousarray(c_pix, dtype=np.complex128)
     Zw = Z if Z.flags.c_contiguous else np.ascontiguousarray(Z)
     t = nat.make_tile(pix=pix, lin_mat=lin_mat, Z=Zw, stop_reason=stop_reason,
-                      stop_iter=stop_iter, center=center, dx=dx)
+                      stop_iter=stop_iter, center=center, dx=dx, i_znorbit=spec.i_znorbit)
     rc = ctx.std_tiles(spec.calc(), [t], nat.HOST)
     if Zw is not Z:
         Z[...] = Zw
@@ -141,7 +163,7 @@ def _tile_for(fractal_args, spec, pix=None, xs=None, ys=None, Z=None, U=None, sr
     kw = dict(lin_mat=fractal_args["lin_mat"], Z=Z, U=U, stop_reason=sr, stop_iter=si,
               ref=ref, dx_m=fractal_args["dx_m"], dx_e=fractal_args["dx_e"],
               i_dzndz=spec.i_dzndz, i_dzndc=spec.i_dzndc, potential=pot, dem=dem,
-              dzndc_scale_e=fractal_args.get("dzndc_scale_e", 0))
+              dzndc_scale_e=fractal_args.get("dzndc_scale_e", 0), i_znorbit=spec.i_znorbit)
     if spec.flavor == 0:
         kw.update(drift_m=fractal_args["drift_m"], drift_e=fractal_args["drift_e"])
     else:
@@ -198,7 +220,8 @@ def run_image(fractal, xs, ys, cycle_indep_args, potential=True):
     else:
         (_init, spec, center, _proj, lin_mat, dx, interrupted) = cycle_indep_args
         t = nat.make_tile(xs=xs, ys=ys, lin_mat=lin_mat, Z=Z, stop_reason=sr, stop_iter=si,
-                          center=center, dx=dx, potential=pot, dem=dem)
+                          center=center, dx=dx, potential=pot, dem=dem,
+                          i_znorbit=spec.i_znorbit)
         rc = ctx.std_tiles(spec.calc(), [t], nat.HOST)
     if rc == nat.FSG_INTERRUPTED:
         return None

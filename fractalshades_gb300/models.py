@@ -23,6 +23,16 @@ from .gpu import StdSpec, PerturbSpec
 from .mpmath_utils import FP_loop as fsFP
 
 
+def _orbit_backshift(calc_orbit, backshift):
+    """The backshift the kernels use: 0 without calc_orbit (the reference
+    divides by it when the orbit is stored, core.py:2985)."""
+    if not calc_orbit:
+        return 0
+    if int(backshift) <= 0:
+        raise ValueError("calc_orbit needs backshift > 0")
+    return int(backshift)
+
+
 def _no_initialize():
     def impl(*args):
         return None
@@ -59,9 +69,12 @@ class Mandelbrot(Fractal):
         """Escape-time iterations with dz/dz (interior detection) and dz/dc
         (mandelbrot_M2.py:61-176).  Exit codes 0 max_iter, 1 divergence,
         2 stationnary."""
-        if calc_d2zndc2 or calc_orbit:
-            raise NotImplementedError("calc_d2zndc2 / calc_orbit are not computed by the GPU kernels")
+        bs = _orbit_backshift(calc_orbit, backshift)
         complex_codes = ["zn", "dzndz", "dzndc"]
+        if calc_d2zndc2:
+            complex_codes += ["d2zndc2"]
+        if calc_orbit:
+            complex_codes += ["zn_orbit"]
         int_codes = []
         stop_codes = ["max_iter", "divergence", "stationnary"]
 
@@ -70,11 +83,12 @@ class Mandelbrot(Fractal):
                 instance.codes = (complex_codes, int_codes, stop_codes)
                 instance.complex_type = np.complex128
                 instance.potential_M = M_divergence
-                instance.backshift = None
+                instance.backshift = bs if calc_orbit else None
             return impl
 
         spec = StdSpec(flavor=0, max_iter=max_iter, M_divergence=M_divergence,
-                       epsilon_stationnary=epsilon_stationnary)
+                       epsilon_stationnary=epsilon_stationnary, calc_d2zndc2=calc_d2zndc2,
+                       backshift=bs)
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 
@@ -119,11 +133,10 @@ class Perturbation_mandelbrot(PerturbationFractal):
         """Perturbation iterations (mandelbrot_M2.py:432-588).  Codes: zn,
         [dzndz], [dzndc]; int code ref_cycle_iter; exit codes 0 max_iter,
         1 divergence, 2 stationnary."""
-        if calc_orbit:
-            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        bs = _orbit_backshift(calc_orbit, backshift)
         complex_codes = ["zn"]
         code_int = 0
-        dzndz = dzndc = -1
+        dzndz = dzndc = i_znorbit = -1
         if interior_detect:
             code_int += 1
             complex_codes += ["dzndz"]
@@ -132,6 +145,10 @@ class Perturbation_mandelbrot(PerturbationFractal):
             code_int += 1
             complex_codes += ["dzndc"]
             dzndc = code_int
+        if calc_orbit:
+            code_int += 1
+            complex_codes += ["zn_orbit"]
+            i_znorbit = code_int
         int_codes = ["ref_cycle_iter"]
         stop_codes = ["max_iter", "divergence", "stationnary"]
         BLA_activated = (BLA_eps is not None) and (self.dx < settings.newton_zoom_level)
@@ -143,13 +160,17 @@ class Perturbation_mandelbrot(PerturbationFractal):
                 instance.codes = (complex_codes, int_codes, stop_codes)
                 instance.calc_dZndz = interior_detect
                 instance.calc_dZndc = calc_dzndc
+                # the field-lines postproc reads it (the reference's power-2
+                # model leaves it unset, mandelbrot_M2.py:529-539)
+                instance.backshift = bs if calc_orbit else None
             return impl
 
         spec = PerturbSpec(flavor=0, max_iter=max_iter, M_divergence=M_divergence,
                            epsilon_stationnary=epsilon_stationnary, calc_dzndc=calc_dzndc,
                            interior=interior_detect, bla=BLA_activated,
                            xr_detect_activated=self.xr_detect_activated,
-                           i_dzndz=dzndz, i_dzndc=dzndc, nZ=len(complex_codes))
+                           i_dzndz=dzndz, i_dzndc=dzndc, nZ=len(complex_codes),
+                           backshift=bs, i_znorbit=i_znorbit)
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 
@@ -240,9 +261,12 @@ class Mandelbrot_N(Fractal):
         """Escape-time iterations of z^N + c with dz/dz and dz/dc
         (mandelbrot_Mn.py:60-175).  Codes zn, dzndz, dzndc; exit codes
         0 max_iter, 1 divergence, 2 stationnary."""
-        if calc_d2zndc2 or calc_orbit:
-            raise NotImplementedError("calc_d2zndc2 / calc_orbit are not computed by the GPU kernels")
+        bs = _orbit_backshift(calc_orbit, backshift)
         complex_codes = ["zn", "dzndz", "dzndc"]
+        if calc_d2zndc2:
+            complex_codes += ["d2zndc2"]
+        if calc_orbit:
+            complex_codes += ["zn_orbit"]
         int_codes = []
         stop_codes = ["max_iter", "divergence", "stationnary"]
 
@@ -251,11 +275,12 @@ class Mandelbrot_N(Fractal):
                 instance.codes = (complex_codes, int_codes, stop_codes)
                 instance.complex_type = np.complex128
                 instance.potential_M = M_divergence
-                instance.backshift = None
+                instance.backshift = bs if calc_orbit else None
             return impl
 
         spec = StdSpec(flavor=0, max_iter=max_iter, M_divergence=M_divergence,
-                       epsilon_stationnary=epsilon_stationnary, nexp=self.exponent)
+                       epsilon_stationnary=epsilon_stationnary, nexp=self.exponent,
+                       calc_d2zndc2=calc_d2zndc2, backshift=bs)
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 
@@ -304,11 +329,10 @@ class Perturbation_mandelbrot_N(PerturbationFractal):
         """Perturbation iterations for z^N + c (mandelbrot_Mn.py:460-623).
         Codes: zn, [dzndz], [dzndc]; int code ref_cycle_iter; exit codes
         0 max_iter, 1 divergence, 2 stationnary."""
-        if calc_orbit:
-            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        bs = _orbit_backshift(calc_orbit, backshift)
         complex_codes = ["zn"]
         code_int = 0
-        dzndz = dzndc = -1
+        dzndz = dzndc = i_znorbit = -1
         if interior_detect:
             code_int += 1
             complex_codes += ["dzndz"]
@@ -317,6 +341,10 @@ class Perturbation_mandelbrot_N(PerturbationFractal):
             code_int += 1
             complex_codes += ["dzndc"]
             dzndc = code_int
+        if calc_orbit:
+            code_int += 1
+            complex_codes += ["zn_orbit"]
+            i_znorbit = code_int
         int_codes = ["ref_cycle_iter"]
         stop_codes = ["max_iter", "divergence", "stationnary"]
         BLA_activated = (BLA_eps is not None) and (self.dx < settings.newton_zoom_level)
@@ -328,6 +356,9 @@ class Perturbation_mandelbrot_N(PerturbationFractal):
                 instance.codes = (complex_codes, int_codes, stop_codes)
                 instance.calc_dZndz = interior_detect
                 instance.calc_dZndc = calc_dzndc
+                # the field-lines postproc reads it (the reference's power-2
+                # model leaves it unset, mandelbrot_M2.py:529-539)
+                instance.backshift = bs if calc_orbit else None
             return impl
 
         spec = PerturbSpec(flavor=0, max_iter=max_iter, M_divergence=M_divergence,
@@ -335,7 +366,7 @@ class Perturbation_mandelbrot_N(PerturbationFractal):
                            interior=interior_detect, bla=BLA_activated,
                            xr_detect_activated=self.xr_detect_activated,
                            i_dzndz=dzndz, i_dzndc=dzndc, nZ=len(complex_codes),
-                           nexp=self.exponent)
+                           nexp=self.exponent, backshift=bs, i_znorbit=i_znorbit)
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 
@@ -421,9 +452,10 @@ class Burning_ship(Fractal):
                      backshift: int = 0):
         """Escape-time iterations with the Jacobian (burning_ship.py:282-346).
         Codes xn, yn, dxnda, dxndb, dynda, dyndb (float64)."""
-        if calc_orbit:
-            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        bs = _orbit_backshift(calc_orbit, backshift)
         complex_codes = ["xn", "yn", "dxnda", "dxndb", "dynda", "dyndb"]
+        if calc_orbit:
+            complex_codes += ["xn_orbit", "yn_orbit"]
         int_codes = []
         stop_codes = ["max_iter", "divergence", "stationnary"]
 
@@ -432,10 +464,11 @@ class Burning_ship(Fractal):
                 instance.codes = (complex_codes, int_codes, stop_codes)
                 instance.complex_type = np.float64
                 instance.potential_M = M_divergence
-                instance.backshift = None
+                instance.backshift = bs if calc_orbit else None
             return impl
 
-        spec = StdSpec(flavor=self.flavor_int, max_iter=max_iter, M_divergence=M_divergence)
+        spec = StdSpec(flavor=self.flavor_int, max_iter=max_iter, M_divergence=M_divergence,
+                       backshift=bs)
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 
@@ -480,11 +513,14 @@ class Perturbation_burning_ship(PerturbationFractal):
         """Perturbation iterations (burning_ship.py:971-1130).  Codes xn, yn
         [, dxnda, dxndb, dynda, dyndb]; int code ref_cycle_iter; exit codes
         0 max_iter, 1 divergence."""
-        if calc_orbit:
-            raise NotImplementedError("calc_orbit is not computed by the GPU kernels")
+        bs = _orbit_backshift(calc_orbit, backshift)
         complex_codes = ["xn", "yn"]
         if calc_hessian:
             complex_codes += ["dxnda", "dxndb", "dynda", "dyndb"]
+        i_xnorbit = -1
+        if calc_orbit:
+            i_xnorbit = len(complex_codes)
+            complex_codes += ["xn_orbit", "yn_orbit"]
         int_codes = ["ref_cycle_iter"]
         stop_codes = ["max_iter", "divergence"]
         BLA_activated = (BLA_eps is not None) and (self.dx < settings.newton_zoom_level)
@@ -495,13 +531,13 @@ class Perturbation_burning_ship(PerturbationFractal):
                 instance.potential_M = M_divergence
                 instance.codes = (complex_codes, int_codes, stop_codes)
                 instance.calc_hessian = calc_hessian
-                instance.backshift = None
+                instance.backshift = bs if calc_orbit else None
             return impl
 
         spec = PerturbSpec(flavor=self.flavor_int, max_iter=max_iter,
                            M_divergence=M_divergence, calc_dzndc=calc_hessian,
                            bla=BLA_activated, xr_detect_activated=self.xr_detect_activated,
-                           nZ=len(complex_codes))
+                           nZ=len(complex_codes), backshift=bs, i_znorbit=i_xnorbit)
         return {"set_state": set_state, "initialize": _no_initialize,
                 "iterate": lambda: spec}
 

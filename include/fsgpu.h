@@ -106,6 +106,16 @@ typedef struct {
                                  perturbation tile's reference must have been
                                  created with the same nexp.  FP64 and XR64
                                  only (FSG_MODE_FE32 is the power-2 form)     */
+    int32_t backshift;        /* > 0: calc_orbit -- store the orbit point at
+                                 iteration stop_iter - backshift in the tile's
+                                 row i_znorbit (core.py:2965-3056,
+                                 perturbation.py:1096-1101, 1265-1273,
+                                 1389-1396, 1641-1651, 1778-1787); 0: off.
+                                 Standard loops and FP64 / XR64 perturbation  */
+    int32_t calc_d2zndc2;     /* standard power-2 / power-n loops: the second
+                                 derivative d2zndc2 in Z row 3
+                                 (mandelbrot_M2.py:316-317,
+                                 mandelbrot_Mn.py:325-333)                    */
 } fsg_calc;
 
 /* One tile: a rectangle of pixels with its own view and outputs. */
@@ -140,6 +150,9 @@ typedef struct {
        standard loop.  No counterpart in the reference (one scale per
        reference, perturbation.py:461-468). */
     int32_t dzndc_scale_e;
+    /* with fsg_calc.backshift > 0: the Z row of the orbit point (complex
+       zn_orbit; Burning Ship: xn_orbit, then yn_orbit in the next row) */
+    int32_t i_znorbit;
 } fsg_tile;
 
 /* Launch statistics of the last fsg_*_tiles call. */

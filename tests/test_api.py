@@ -251,3 +251,43 @@ def test_power_n_models(tmp_path):
     assert abs(julia - size ** (8. / 9.)) < 1e-12 * julia
     with pytest.raises(ValueError):
         fsm.Perturbation_mandelbrot_N(str(tmp_path / "bad"), 1)
+
+
+def test_orbit_and_d2_options_codes(tmp_path):
+    """calc_orbit / backshift / calc_d2zndc2: the reference's code lists
+    (mandelbrot_M2.py:107-124, 482-506, burning_ship.py:264-280, 1015-1035)
+    and the rows the kernels write."""
+    f = fsm.Mandelbrot(str(tmp_path / "a"))
+    f.zoom(x=-0.5, y=0., dx=3., nx=64, xy_ratio=1., theta_deg=0.)
+    codes, spec = _codes(f, calc_name="c", subset=None, max_iter=100, M_divergence=1000.,
+                         epsilon_stationnary=1e-3, calc_d2zndc2=True, calc_orbit=True,
+                         backshift=3)
+    assert codes[0] == ["zn", "dzndz", "dzndc", "d2zndc2", "zn_orbit"]
+    assert spec.nZ == 5 and spec.i_znorbit == 4 and spec.calc().backshift == 3
+    assert spec.calc().calc_d2zndc2 == 1
+    with pytest.raises(ValueError):
+        _codes(f, calc_name="c", subset=None, max_iter=100, M_divergence=1000.,
+               epsilon_stationnary=1e-3, calc_orbit=True, backshift=0)
+    g = fsm.Perturbation_mandelbrot(str(tmp_path / "b"))
+    g.zoom(precision=30, x="-0.75", y="0.1", dx="1e-10", nx=64, xy_ratio=1., theta_deg=0.)
+    codes, spec = _codes(g, calc_name="c", subset=None, max_iter=1000, M_divergence=1000.,
+                         epsilon_stationnary=1e-3, interior_detect=True, calc_orbit=True,
+                         backshift=7)
+    assert codes[0] == ["zn", "dzndz", "dzndc", "zn_orbit"] and spec.i_znorbit == 3
+    assert spec.calc().backshift == 7
+    settings.precision_mode = "fe32"
+    try:
+        with pytest.raises(ValueError):
+            spec.mode
+    finally:
+        settings.precision_mode = "auto"
+    h = fsm.Perturbation_burning_ship(str(tmp_path / "c"), flavor="Burning ship")
+    h.zoom(precision=30, x="-1.75", y="-0.03", dx="1e-8", nx=64, xy_ratio=1., theta_deg=0.)
+    codes, spec = _codes(h, calc_name="c", subset=None, max_iter=1000, M_divergence=1000.,
+                         calc_orbit=True, backshift=2)
+    assert codes[0][-2:] == ["xn_orbit", "yn_orbit"] and spec.i_znorbit == 6
+    s = fsm.Burning_ship(str(tmp_path / "d"), flavor="Celtic")
+    s.zoom(x=-0.5, y=-0.5, dx=3.5, nx=24, xy_ratio=1., theta_deg=0.)
+    codes, spec = _codes(s, calc_name="c", subset=None, max_iter=100, M_divergence=1000.,
+                         calc_orbit=True, backshift=2)
+    assert spec.nZ == 8 and spec.i_znorbit == 6 and codes[0][6:] == ["xn_orbit", "yn_orbit"]

@@ -126,6 +126,60 @@ def test_std_bs_vs_oracle(ctx, flavor):
     assert np.array_equal(Z.view(np.uint64), d[f"Z_{flavor}"].view(np.uint64))
 
 
+def _std_opts(ctx, pix, center, dx, max_iter, eps, nZ, i_orb, **calc_kw):
+    from fractalshades_gb300 import _native as nat
+    nx = int(round(np.sqrt(pix.size)))
+    xs, ys = axes(pix, nx)
+    n = pix.size
+    dt = np.complex128 if calc_kw.get("flavor", 0) == 0 else np.float64
+    Z = np.zeros((nZ, n), dtype=dt)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    d = load("std_opts")
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, stop_reason=sr, stop_iter=si,
+                      center=center, dx=dx, i_znorbit=i_orb)
+    ctx.std_tiles(nat.make_calc(max_iter=max_iter, M_divergence=1000.,
+                                epsilon_stationnary=eps, **calc_kw), [t])
+    return Z, si, sr
+
+
+def test_std_options_bit_exact_vs_golden(ctx):
+    """d2zndc2 and the orbit point n - backshift of the standard loops
+    (mandelbrot_M2.py:316-317, mandelbrot_Mn.py:325-333, core.py:2965-3056)
+    against the reference's own outputs."""
+    d = load("std_opts")
+    Z, si, sr = _std_opts(ctx, d["pix_m2"], -0.5 + 0j, 3., 400, 0.01, 5, 4,
+                          calc_d2zndc2=True, backshift=3)
+    assert np.array_equal(si, d["stop_iter_m2"]) and np.array_equal(sr, d["stop_reason_m2"])
+    assert np.array_equal(Z.view(np.uint64), d["Z_m2"].view(np.uint64))
+    for nexp in (2, 3):
+        Z, si, sr = _std_opts(ctx, d[f"pix_mn{nexp}"], 0j, 3., 300, 0.01, 5, 4,
+                              calc_d2zndc2=True, backshift=4, nexp=nexp)
+        assert np.array_equal(si, d[f"stop_iter_mn{nexp}"])
+        assert np.array_equal(Z.view(np.uint64), d[f"Z_mn{nexp}"].view(np.uint64)), nexp
+    for fl in (1, 4):
+        Z, si, sr = _std_opts(ctx, d[f"pix_bs{fl}"], -0.5 - 0.5j, 3.5, 200, 0., 8, 6,
+                              flavor=fl, backshift=3)
+        assert np.array_equal(si, d[f"stop_iter_bs{fl}"])
+        assert np.array_equal(Z.view(np.uint64), d[f"Z_bs{fl}"].view(np.uint64)), fl
+
+
+def test_orbit_options_are_validated(ctx):
+    """calc_orbit in the FP32 + exponent form, a row index that collides with
+    the other outputs, a negative backshift and d2zndc2 outside the standard
+    Mandelbrot loop are refused."""
+    from fractalshades_gb300 import _native as nat
+    d = load("std_opts")
+    for kw, nZ, i_orb in (({"backshift": -1}, 3, 0), ({"backshift": 3}, 4, 2),
+                          ({"calc_d2zndc2": True, "flavor": 1}, 6, 0)):
+        with pytest.raises(RuntimeError):
+            _std_opts(ctx, d["pix_m2"][:64], -0.5 + 0j, 3., 10, 0.01, nZ, i_orb, **kw)
+    dd = load("pert_m2_orbit")
+    ref = _ref_from_golden(ctx, dd, False)
+    with pytest.raises(RuntimeError):
+        _run_m2(ctx, dd, ref, "fe32", False)
+
+
 @pytest.mark.parametrize("nexp", [3, 4])
 def test_std_mn_bit_exact_vs_golden(ctx, nexp):
     """Power-n standard loop against the reference's own outputs."""
@@ -171,13 +225,18 @@ def _ref_from_golden(ctx, d, xr_paths):
         nexp=_nexp(d))
 
 
+def _backshift(d):
+    return int(d["backshift"]) if "backshift" in d.files else 0
+
+
 def _run_m2(ctx, d, ref, mode, xr_sem):
     from fractalshades_gb300 import _native as nat
     nx = int(round(np.sqrt(d["pix"].size)))
     xs, ys = axes(d["pix"], nx)
     n = d["pix"].size
     interior = bool(d["interior"])
-    nZ = 2 + int(interior)
+    bs = _backshift(d)
+    nZ = 2 + int(interior) + int(bs > 0)
     Z = np.zeros((nZ, n), dtype=np.complex128)
     U = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
@@ -185,11 +244,12 @@ def _run_m2(ctx, d, ref, mode, xr_sem):
     t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
                       stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
                       drift_m=complex(d["drift_m"]), drift_e=int(d["drift_e"]),
-                      i_dzndz=1 if interior else -1, i_dzndc=nZ - 1)
+                      i_dzndz=1 if interior else -1, i_dzndc=1 + int(interior),
+                      i_znorbit=nZ - 1 if bs > 0 else 0)
     calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
                          epsilon_stationnary=float(d["eps_stat"]), mode=mode,
                          calc_dzndc=True, interior=interior, bla=True,
-                         xr_semantics=xr_sem, nexp=_nexp(d))
+                         xr_semantics=xr_sem, nexp=_nexp(d), backshift=bs)
     ctx.perturb_tiles(calc, [t])
     return Z, U, sr, si
 
@@ -198,6 +258,8 @@ M2_CASES = ["pert_m2_fp64", "pert_m2_cycle", "pert_m2_xr", "pert_m2_xr_div"]
 # power-n model: period-10 nuclei of z^3 + c (interior and escaping views)
 # and of z^4 + c at dx = 1e-305 (Xrange branch)
 MN_CASES = ["pert_mn3_cycle", "pert_mn3_div", "pert_mn4_xr"]
+# calc_orbit (backshift 5, 7, 4): FP64 and Xrange branches, power 2 and 3
+ORBIT_CASES = ["pert_m2_orbit", "pert_m2_xr_orbit", "pert_mn3_orbit"]
 
 
 def _xr_rel(m, e, eref):
@@ -240,7 +302,7 @@ def test_ref_tables_vs_oracle(ctx, case):
             assert np.array_equal(dzz.view(np.uint64), dzzo.view(np.uint64))
 
 
-@pytest.mark.parametrize("case", M2_CASES + MN_CASES)
+@pytest.mark.parametrize("case", M2_CASES + MN_CASES + ORBIT_CASES)
 def test_perturb_m2_reference_branch_vs_oracle(ctx, case):
     """FP64 kernel on the standard-branch cases, XR64 on the Xrange cases."""
     d = load(case)
@@ -250,8 +312,10 @@ def test_perturb_m2_reference_branch_vs_oracle(ctx, case):
     iter_agree(si, d["stop_iter"])
     assert np.mean(sr == d["stop_reason"]) >= 0.9999
     same = (si == d["stop_iter"]).ravel()
-    rel_close(Z[0], d["Z"][0], 1e-6, same)
-    rel_close(Z[-1], d["Z"][-1], 1e-6, same)
+    for k in range(Z.shape[0]):
+        if k == 1 and bool(d["interior"]):
+            continue          # the Xrange branch never writes dzndz back
+        rel_close(Z[k], d["Z"][k], 1e-6, same)
 
 
 def _oracle_bla_noise(d):
@@ -344,7 +408,7 @@ def test_perturb_bs_fe32_vs_oracle(ctx, case):
     assert np.percentile(err, 90) <= 2e-2 and np.max(err) <= 0.2, (np.percentile(err, 90), err.max())
 
 
-@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4"])
+@pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4", "pert_bs_orbit"])
 def test_perturb_bs_vs_oracle(ctx, case):
     from fractalshades_gb300 import _native as nat
     d = load(case)
@@ -359,20 +423,23 @@ def test_perturb_bs_vs_oracle(ctx, case):
     nx = int(round(np.sqrt(d["pix"].size)))
     xs, ys = axes(d["pix"], nx)
     n = d["pix"].size
-    Z = np.zeros((6, n))
+    bs = _backshift(d)
+    nZ = 8 if bs > 0 else 6
+    Z = np.zeros((nZ, n))
     U = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
     si = np.zeros((1, n), dtype=np.int32)
     t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
                       stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
                       drift_m=float(d["driftx_m"]), drift_e=int(d["driftx_e"]),
-                      drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]))
+                      drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]),
+                      i_znorbit=6 if bs > 0 else 0)
     calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]), flavor=fl,
-                         calc_dzndc=True, bla=True)
+                         calc_dzndc=True, bla=True, backshift=bs)
     ctx.perturb_tiles(calc, [t])
     iter_agree(si, d["stop_iter"])
     same = (si == d["stop_iter"]).ravel()
-    for k in range(6):
+    for k in range(nZ):
         rel_close(Z[k], d["Z"][k], 1e-6, same)
 
 
