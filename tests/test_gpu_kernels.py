@@ -173,7 +173,7 @@ def test_orbit_options_are_validated(ctx):
     for kw, nZ, i_orb in (({"backshift": -1}, 3, 0), ({"backshift": 3}, 4, 2),
                           ({"calc_d2zndc2": True, "flavor": 1}, 6, 0)):
         with pytest.raises(RuntimeError):
-            _std_opts(ctx, d["pix_m2"][:64], -0.5 + 0j, 3., 10, 0.01, nZ, i_orb, **kw)
+            _std_opts(ctx, d["pix_m2"], -0.5 + 0j, 3., 10, 0.01, nZ, i_orb, **kw)
     dd = load("pert_m2_orbit")
     ref = _ref_from_golden(ctx, dd, False)
     with pytest.raises(RuntimeError):
