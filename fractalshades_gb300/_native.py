@@ -68,6 +68,21 @@ class Tile(ct.Structure):
     ]
 
 
+class FieldlinesArgs(ct.Structure):
+    _fields_ = [
+        ("npix", I64), ("model", I32), ("c", P), ("z", P), ("nu_frac", P), ("n", P),
+        ("is_backward", I32), ("backshift", I32), ("n_iter", I32), ("k", P), ("phi", P),
+        ("out", P),
+    ]
+
+
+class NormalArgs(ct.Structure):
+    _fields_ = [
+        ("npix", I64), ("kind", I32), ("zn", P), ("dzndc", P), ("d2zndc2", P), ("skew", P),
+        ("out", P),
+    ]
+
+
 class Stats(ct.Structure):
     _fields_ = [
         ("kernel_ms", F64), ("pixels", I64), ("pixel_iters", I64),
@@ -84,8 +99,11 @@ SYMBOLS = [
     "fsg_set_stream", "fsg_sync", "fsg_ref_create", "fsg_ref_destroy",
     "fsg_ref_info", "fsg_ref_download", "fsg_std_tiles", "fsg_perturb_tiles",
     "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel", "fsg_peak_flops",
-    "fsg_std_tiles_noalloc", "fsg_ref_derive_bla",
+    "fsg_std_tiles_noalloc", "fsg_ref_derive_bla", "fsg_postproc_fieldlines",
+    "fsg_postproc_normal",
 ]
+
+FSG_FIELDLINES_MAX_ITER = 64
 
 
 class GPUError(RuntimeError):
@@ -121,6 +139,8 @@ def load():
         L.fsg_last_stats.argtypes = [P, ct.POINTER(Stats)]
         L.fsg_peak_flops.argtypes = [P, I32, ct.POINTER(F64)]
         L.fsg_cancel.argtypes = [P]
+        L.fsg_postproc_fieldlines.argtypes = [P, ct.POINTER(FieldlinesArgs), I32]
+        L.fsg_postproc_normal.argtypes = [P, ct.POINTER(NormalArgs), I32]
         L.fsg_clear_cancel.argtypes = [P]
         _lib = L
         return L
@@ -193,6 +213,42 @@ class Context:
         arr = (Tile * len(tiles))(*tiles)
         return self.check(self.L.fsg_perturb_tiles(self.h, ct.byref(calc), arr, len(tiles), where),
                           "fsg_perturb_tiles")
+
+    # ------------------------------------------------------------------
+    def fieldlines(self, *, model, c, z, nu_frac, n, k, phi, is_backward, backshift):
+        """Fieldlines_pp on the device (host arrays in and out): model 0 for
+        z^2 + c, n for z^n + c, -flavor for the Burning Ship family; z the
+        start points (complex; Burning Ship x + i y)."""
+        c = np.ascontiguousarray(c, dtype=np.complex128)
+        z = np.ascontiguousarray(z, dtype=np.complex128)
+        nu = np.ascontiguousarray(nu_frac, dtype=np.float64)
+        nn = np.ascontiguousarray(n, dtype=np.int32)
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        out = np.empty(c.size, dtype=np.float64)
+        a = FieldlinesArgs()
+        a.npix, a.model = c.size, int(model)
+        a.c, a.z, a.nu_frac, a.n = _p(c), _p(z), _p(nu), _p(nn)
+        a.is_backward, a.backshift, a.n_iter = int(bool(is_backward)), int(backshift), k.size
+        a.k, a.phi, a.out = _p(k), _p(phi), _p(out)
+        self.check(self.L.fsg_postproc_fieldlines(self.h, ct.byref(a), HOST),
+                   "fsg_postproc_fieldlines")
+        return out
+
+    def normal(self, *, kind, zn, dzndc, d2zndc2=None, skew=None):
+        """DEM_normal_pp on the device: kind 0 "potential", 1 "Milnor", 2 the
+        Burning Ship family (dzndc = the 4 Jacobian rows).  Returns the
+        complex unit normal."""
+        zn = np.ascontiguousarray(zn, dtype=np.complex128)
+        dz = np.ascontiguousarray(dzndc, dtype=np.float64 if kind == 2 else np.complex128)
+        d2 = None if d2zndc2 is None else np.ascontiguousarray(d2zndc2, dtype=np.complex128)
+        sk = None if skew is None else np.ascontiguousarray(skew, dtype=np.float64).ravel()
+        out = np.empty(zn.size, dtype=np.complex128)
+        a = NormalArgs()
+        a.npix, a.kind = zn.size, int(kind)
+        a.zn, a.dzndc, a.d2zndc2, a.skew, a.out = _p(zn), _p(dz), _p(d2), _p(sk), _p(out)
+        self.check(self.L.fsg_postproc_normal(self.h, ct.byref(a), HOST), "fsg_postproc_normal")
+        return out
 
 
 class Reference:

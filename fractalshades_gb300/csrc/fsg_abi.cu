@@ -366,6 +366,19 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
 
 }  // namespace
 
+namespace {
+// Stage one host array into the scratch area (FSG_HOST) or take the device
+// pointer as is; `p` advances past the staged bytes.
+template <class T>
+int stage_in(fsg_ctx *ctx, int32_t where, const void *src, size_t bytes, char *&p, const T *&dst) {
+    if (where == FSG_DEVICE || !src) { dst = (const T *)src; return FSG_OK; }
+    CK(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy post-processing input");
+    dst = (const T *)p;
+    p += align_up(bytes);
+    return FSG_OK;
+}
+}  // namespace
+
 extern "C" {
 
 const char *fsg_version(void) { return FSG_VERSION; }
@@ -744,6 +757,91 @@ int fsg_perturb_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
                       int32_t where) {
     if (ctx) cudaSetDevice(ctx->device);
     return run_tiles(ctx, calc, tiles, ntiles, where, true);
+}
+
+// ---------------------------------------------------------------------------
+// post-processing (fsg_postproc.cu)
+// ---------------------------------------------------------------------------
+int fsg_postproc_fieldlines(fsg_ctx *ctx, const fsg_fieldlines *a, int32_t where) {
+    if (!ctx) return FSG_ERR_ARG;
+    if (!a || a->npix < 0 || !a->c || !a->z || !a->nu_frac || !a->n || !a->k || !a->phi || !a->out)
+        return set_err(ctx, FSG_ERR_ARG, "fieldlines: NULL argument");
+    if (a->n_iter < 1 || a->n_iter > FSG_FIELDLINES_MAX_ITER)
+        return set_err(ctx, FSG_ERR_LIMIT, "fieldlines: n_iter outside 1 .. FSG_FIELDLINES_MAX_ITER");
+    if (a->model < -5 || a->model == 1 || a->model > FSG_MN_MAX_EXP)
+        return set_err(ctx, FSG_ERR_ARG, "fieldlines: bad model");
+    if (where != FSG_HOST && where != FSG_DEVICE)
+        return set_err(ctx, FSG_ERR_ARG, "where must be FSG_HOST or FSG_DEVICE");
+    if (a->npix == 0) return FSG_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n = (size_t)a->npix, nk = (size_t)a->n_iter;
+    FieldlinesDev D;
+    D.npix = a->npix; D.model = a->model; D.is_backward = a->is_backward;
+    D.backshift = a->backshift; D.n_iter = a->n_iter;
+    char *p = nullptr;
+    if (where == FSG_HOST) {
+        size_t bytes = 2 * align_up(16 * n) + 2 * align_up(8 * n) + align_up(4 * n) + 2 * align_up(8 * nk);
+        int rc = ensure_scratch(ctx, bytes);
+        if (rc != FSG_OK) return rc;
+        p = ctx->scratch;
+    }
+    int rc = FSG_OK;
+    if ((rc = stage_in(ctx, where, a->c, 16 * n, p, D.c)) != FSG_OK) return rc;
+    if ((rc = stage_in(ctx, where, a->z, 16 * n, p, D.z)) != FSG_OK) return rc;
+    if ((rc = stage_in(ctx, where, a->nu_frac, 8 * n, p, D.nu_frac)) != FSG_OK) return rc;
+    if ((rc = stage_in(ctx, where, a->n, 4 * n, p, D.n)) != FSG_OK) return rc;
+    if ((rc = stage_in(ctx, where, a->k, 8 * nk, p, D.k)) != FSG_OK) return rc;
+    if ((rc = stage_in(ctx, where, a->phi, 8 * nk, p, D.phi)) != FSG_OK) return rc;
+    D.out = where == FSG_HOST ? (double *)p : a->out;
+    fsg_launch_fieldlines(D, ctx->stream);
+    CK(cudaGetLastError(), "fieldlines kernel");
+    if (where == FSG_HOST) {
+        CK(cudaMemcpyAsync(a->out, D.out, 8 * n, cudaMemcpyDeviceToHost, ctx->stream), "copy fieldlines");
+        CK(cudaStreamSynchronize(ctx->stream), "fieldlines");
+    }
+    return FSG_OK;
+}
+
+int fsg_postproc_normal(fsg_ctx *ctx, const fsg_normal *a, int32_t where) {
+    if (!ctx) return FSG_ERR_ARG;
+    if (!a || a->npix < 0 || !a->zn || !a->dzndc || !a->out || (a->kind == 1 && !a->d2zndc2))
+        return set_err(ctx, FSG_ERR_ARG, "normal: NULL argument");
+    if (a->kind < 0 || a->kind > 2) return set_err(ctx, FSG_ERR_ARG, "normal: bad kind");
+    if (where != FSG_HOST && where != FSG_DEVICE)
+        return set_err(ctx, FSG_ERR_ARG, "where must be FSG_HOST or FSG_DEVICE");
+    if (a->npix == 0) return FSG_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n = (size_t)a->npix;
+    NormalDev D;
+    D.npix = a->npix; D.kind = a->kind;
+    D.has_skew = a->skew != nullptr;
+    for (int k = 0; k < 4; k++) D.skew[k] = a->skew ? a->skew[k] : 0.;
+    D.dzndc = nullptr; D.jac = nullptr; D.d2 = nullptr;
+    const size_t dbytes = a->kind == 2 ? 32 * n : 16 * n;
+    char *p = nullptr;
+    if (where == FSG_HOST) {
+        size_t bytes = align_up(16 * n) + align_up(dbytes) + (a->kind == 1 ? align_up(16 * n) : 0)
+                       + align_up(16 * n);
+        int rc = ensure_scratch(ctx, bytes);
+        if (rc != FSG_OK) return rc;
+        p = ctx->scratch;
+    }
+    int rc = FSG_OK;
+    if ((rc = stage_in(ctx, where, a->zn, 16 * n, p, D.zn)) != FSG_OK) return rc;
+    if (a->kind == 2) {
+        if ((rc = stage_in(ctx, where, a->dzndc, dbytes, p, D.jac)) != FSG_OK) return rc;
+    } else if ((rc = stage_in(ctx, where, a->dzndc, dbytes, p, D.dzndc)) != FSG_OK) {
+        return rc;
+    }
+    if (a->kind == 1 && (rc = stage_in(ctx, where, a->d2zndc2, 16 * n, p, D.d2)) != FSG_OK) return rc;
+    D.out = where == FSG_HOST ? (double2 *)p : (double2 *)a->out;
+    fsg_launch_normal(D, ctx->stream);
+    CK(cudaGetLastError(), "normal kernel");
+    if (where == FSG_HOST) {
+        CK(cudaMemcpyAsync(a->out, D.out, 16 * n, cudaMemcpyDeviceToHost, ctx->stream), "copy normal");
+        CK(cudaStreamSynchronize(ctx->stream), "normal");
+    }
+    return FSG_OK;
 }
 
 int fsg_peak_flops(fsg_ctx *ctx, int32_t fp64, double *tflops) {

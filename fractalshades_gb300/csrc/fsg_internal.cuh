@@ -199,6 +199,30 @@ inline int fsg_auto_grid(K kernel, int grid, int block, long long total) {
     return (int)g;
 }
 
+#ifndef FSG_FIELDLINES_MAX_ITER
+#define FSG_FIELDLINES_MAX_ITER 64
+#endif
+// Post-processing arguments (fsg_postproc.cu), device pointers
+struct FieldlinesDev {
+    long long npix;
+    int model, is_backward, backshift, n_iter;
+    const double2 *c, *z;
+    const double *nu_frac;
+    const int *n;
+    const double *k, *phi;
+    double *out;
+};
+struct NormalDev {
+    long long npix;
+    int kind, has_skew;
+    double skew[4];
+    const double2 *zn, *dzndc, *d2;
+    const double *jac;          // Burning Ship: [4][npix] dxnda, dxndb, dynda, dyndb
+    double2 *out;
+};
+void fsg_launch_fieldlines(const FieldlinesDev &A, cudaStream_t s);
+void fsg_launch_normal(const NormalDev &A, cudaStream_t s);
+
 // Kernel launchers (one per translation unit); grid 0 = one persistent wave
 // at full occupancy
 void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s);

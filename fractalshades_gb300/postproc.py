@@ -1,13 +1,16 @@
 """
 Post-processing of the raw iteration results: continuous iteration count
-(potential), distance estimate and raw field access.
+(potential), distance estimate, field lines, DEM normal map and raw field
+access.
 
 Restates the reference's Continuous_iter_pp (postproc.py:267-406,
-Continuous_iter_pp_infinity :1001-1009), DEM_pp (:662-731) and Raw_pp
-(:217-264) over the in-memory raw arrays of ``Fractal.calc_raw``.  The GPU
-kernels also produce the potential and the distance estimate in their
-epilogue; these classes compute them from Z, U, stop_iter in numpy with the
-reference's formulas, so both can be compared.
+Continuous_iter_pp_infinity :1001-1009), DEM_pp (:662-731), Raw_pp
+(:217-264), Fieldlines_pp (:409-530) and DEM_normal_pp (:533-628) over the
+raw arrays of ``Fractal.calc_raw``.  The GPU kernels also produce the
+potential and the distance estimate in their epilogue; Continuous_iter_pp
+and DEM_pp compute them from Z, U, stop_iter in numpy with the reference's
+formulas, so both can be compared.  Field lines and normals run on the GPU
+(csrc/fsg_postproc.cu, fsg_postproc_fieldlines / fsg_postproc_normal).
 """
 import numpy as np
 
@@ -76,7 +79,8 @@ class Continuous_iter_pp(Postproc):
         return dic
 
     def evaluate(self, context):
-        n = self.raw("stop_iter").astype(np.int64)
+        # stop_iter's int32, as the reference's n (postproc.py:392)
+        n = self.raw("stop_iter").astype(np.int32)
         pd = self.potential_dic
         if pd["kind"] != "infinity":
             raise NotImplementedError(f"Potential kind: {pd['kind']} unsupported")
@@ -87,7 +91,8 @@ class Continuous_iter_pp(Postproc):
         nu_frac = -nu_mod
         n = n - nu_div.astype(n.dtype)
         val = (n - self._floor_iter) + nu_frac
-        return val, {"potential_dic": pd, "nu_frac": nu_frac, "n": n}
+        return val, {"potential_dic": pd, "nu_frac": nu_frac, "n": n,
+                     "backshift": getattr(self.state, "backshift", None)}
 
 
 class DEM_pp(Postproc):
@@ -111,6 +116,82 @@ class DEM_pp(Postproc):
         return val, {}
 
 
+class Fieldlines_pp(Postproc):
+    def __init__(self, n_iter=5, swirl=0., endpoint_k=1.0):
+        """Orbit-averaged angle revealing field lines (postproc.py:409-530):
+        n_iter orbit points from zn_orbit (else zn), geometric weights from
+        1 to endpoint_k, random phases scaled by swirl.  Needs
+        Continuous_iter_pp earlier in the batch."""
+        self.n_iter = int(n_iter)
+        self.swirl = swirl
+        self.endpoint_k = endpoint_k
+        if not 1 <= self.n_iter <= 64:
+            raise ValueError("n_iter must be in 1 .. 64")
+
+    def _model(self):
+        """The map the orbit is continued with: 0 z^2 + c (M2_iterate), n
+        z^n + c (the power-n models' Mn_iterate), -flavor (BS_iterate)."""
+        f = self.fractal
+        if not self.holomorphic:
+            return -int(f.flavor_int)
+        return int(getattr(f, "exponent", 0))
+
+    def evaluate(self, context):
+        from . import gpu
+        pd = context["potential_dic"]
+        if pd["kind"] != "infinity":
+            raise ValueError(f"Unsupported potential '{pd['kind']}' for field lines")
+        k_arr = np.geomspace(1., self.endpoint_k, num=self.n_iter)
+        k_arr = k_arr / np.sum(k_arr)
+        rg = np.random.default_rng(0)
+        phi_arr = rg.random(self.n_iter) * self.swirl * np.pi
+        codes = self.fractal.codes[0]
+        backshift = context.get("backshift")
+        if self.holomorphic:
+            key = "zn_orbit" if "zn_orbit" in codes else "zn"
+            z = self.raw(key)
+        else:
+            key = "xn_orbit" if "xn_orbit" in codes else "xn"
+            z = self.raw(key) + 1j * self.raw("yn_orbit" if key == "xn_orbit" else "yn")
+        is_backward = key.endswith("_orbit")
+        if is_backward and backshift is None:
+            raise ValueError("zn_orbit stored without a backshift in the calculation state")
+        xs, ys = self.fractal.image_axes()
+        c_pix = (xs[None, :] + 1j * ys[:, None]).ravel()
+        c_pt = self.fractal.get_std_cpt(c_pix)
+        val = gpu.context().fieldlines(
+            model=self._model(), c=c_pt, z=z, nu_frac=context["nu_frac"], n=context["n"],
+            k=k_arr, phi=phi_arr, is_backward=is_backward,
+            backshift=backshift if is_backward else 0)
+        return val, {}
+
+
+class DEM_normal_pp(Postproc):
+    field_count = 2
+
+    def __init__(self, kind="potential"):
+        """Unit normal of the distance estimate (postproc.py:533-628): kind
+        "potential" (z / dzndc, Burning Ship: J^T z) or "Milnor" (needs the
+        d2zndc2 field); the view's skew is undone.  Evaluates to complex."""
+        if kind not in ("potential", "Milnor"):
+            raise ValueError(kind)
+        self.kind = kind
+
+    def evaluate(self, context):
+        from . import gpu
+        skew = self.fractal.skew
+        if self.kind == "Milnor":
+            out = gpu.context().normal(kind=1, zn=self.raw("zn"), dzndc=self.raw("dzndc"),
+                                       d2zndc2=self.raw("d2zndc2"), skew=skew)
+        elif self.holomorphic:
+            out = gpu.context().normal(kind=0, zn=self.raw("zn"), dzndc=self.raw("dzndc"),
+                                       skew=skew)
+        else:
+            jac = np.stack([self.raw(k) for k in ("dxnda", "dxndb", "dynda", "dyndb")])
+            out = gpu.context().normal(kind=2, zn=self.get_zn(), dzndc=jac, skew=skew)
+        return out, {}
+
+
 class Postproc_batch:
     def __init__(self, fractal, calc_name):
         """A set of post-processings of one calculation."""
@@ -130,6 +211,11 @@ class Postproc_batch:
         for name, pp in self.posts.items():
             val, upd = pp.evaluate(context)
             context.update(upd)
-            out[name] = np.asarray(val, dtype=self.fractal.float_postproc_type).reshape(
-                self.fractal.ny, self.fractal.nx)
+            shape = (self.fractal.ny, self.fractal.nx)
+            if getattr(pp, "field_count", 1) == 2:
+                # the two components, as the reference's XYCoord_wrapper_pp
+                out[name + "_x"] = np.asarray(val.real, self.fractal.float_postproc_type).reshape(shape)
+                out[name + "_y"] = np.asarray(val.imag, self.fractal.float_postproc_type).reshape(shape)
+                continue
+            out[name] = np.asarray(val, dtype=self.fractal.float_postproc_type).reshape(shape)
         return out

@@ -155,6 +155,49 @@ typedef struct {
     int32_t i_znorbit;
 } fsg_tile;
 
+/* Post-processing on the device (postproc.py).  Pointers are host or device
+ * arrays as `where` says (FSG_HOST: the library stages the copies and
+ * returns once the output is back in host memory). */
+#define FSG_FIELDLINES_MAX_ITER 64
+
+/* Fieldlines_pp (postproc.py:409-530, 1038-1160): the orbit-averaged angle
+ * of n_iter + 3 orbit points from the stored start point, smoothed by the
+ * Catmull-Rom weights of the fractional escape count. */
+typedef struct {
+    int64_t npix;
+    int32_t model;            /* 0: z^2 + c; n >= 2: z^n + c; -1 .. -5: Burning
+                                 Ship flavor 1 .. 5                              */
+    const double *c;          /* complex128 [npix]: the pixel's c (get_std_cpt) */
+    const double *z;          /* complex128 [npix]: zn_orbit (or zn); Burning
+                                 Ship: (xn_orbit, yn_orbit) pairs               */
+    const double *nu_frac;    /* float64 [npix]: Continuous_iter_pp's nu_frac   */
+    const int32_t *n;         /* int32 [npix]: Continuous_iter_pp's n           */
+    int32_t is_backward;      /* z is the orbit point n - backshift             */
+    int32_t backshift;
+    int32_t n_iter;           /* 1 .. FSG_FIELDLINES_MAX_ITER                   */
+    const double *k;          /* float64 [n_iter]: weights                      */
+    const double *phi;        /* float64 [n_iter]: phases                       */
+    double *out;              /* float64 [npix]                                 */
+} fsg_fieldlines;
+
+/* DEM_normal_pp (postproc.py:533-628): the unit normal of the distance
+ * estimate. */
+typedef struct {
+    int64_t npix;
+    int32_t kind;             /* 0: "potential", zn / dzndc; 1: "Milnor";
+                                 2: "potential" of the Burning Ship family     */
+    const double *zn;         /* complex128 [npix] (Burning Ship: (xn, yn))     */
+    const double *dzndc;      /* complex128 [npix]; Burning Ship: float64
+                                 [4][npix] dxnda, dxndb, dynda, dyndb           */
+    const double *d2zndc2;    /* complex128 [npix] (kind 1)                     */
+    const double *skew;       /* NULL or float64 [2][2]: the view's skew, undone
+                                 on the normal (core.py:3147-3158)              */
+    double *out;              /* complex128 [npix]                              */
+} fsg_normal;
+
+int fsg_postproc_fieldlines(fsg_ctx *ctx, const fsg_fieldlines *args, int32_t where);
+int fsg_postproc_normal(fsg_ctx *ctx, const fsg_normal *args, int32_t where);
+
 /* Launch statistics of the last fsg_*_tiles call. */
 typedef struct {
     double kernel_ms;          /* device time of the iteration kernel            */

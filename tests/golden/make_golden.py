@@ -601,6 +601,74 @@ def golden_std_opts(out):
     np.savez_compressed(out, **res)
 
 
+def _run_postprocs(f, calc_name, c_pix, Z, U, sr, si, posts):
+    """Fractal.postproc (core.py:2736-2778) on one chunk: the reference's
+    Postproc_batch evaluated post by post, each updating the shared context;
+    returns the float64 values (before the float32 cast of post_array)."""
+    batch = fs.postproc.Postproc_batch(f, calc_name)
+    for name, pp in posts:
+        batch.add_postproc(name, pp)
+    chunk = (0, f.nx, 0, f.ny)
+    codes = f._calc_data[calc_name]["state"].codes
+    complex_dic, int_dic, termination_dic = f.codes_mapping(*codes)
+    batch.set_chunk_data(chunk, None, c_pix, Z, U, sr, si, complex_dic, int_dic,
+                         termination_dic)
+    out = {}
+    for name, pp in batch.posts.items():
+        val, upd = pp[chunk]
+        out[name] = np.asarray(val, dtype=np.float64)
+        batch.update_context(chunk, upd)
+    return out
+
+
+def golden_postproc(out):
+    """Continuous iteration, field lines (zn_orbit, backshift 3) and DEM
+    normals (potential and Milnor) from the reference's postproc classes, for
+    the power-2, power-3 and Burning Ship (flavor 1) standard loops."""
+    res = {}
+    fl_kw = dict(n_iter=5, swirl=0.7, endpoint_k=0.5)
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Mandelbrot(d)
+        f.zoom(x=-0.5, y=0., dx=3., nx=32, xy_ratio=1., theta_deg=0.)
+        f.calc_std_div(calc_name="std", subset=None, max_iter=400, M_divergence=1000.,
+                       epsilon_stationnary=0.01, calc_d2zndc2=True, calc_orbit=True,
+                       backshift=3)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+        r = _run_postprocs(f, "std", c_pix, Z, U, sr, si, [
+            ("cont", fs.postproc.Continuous_iter_pp()),
+            ("fl", fs.postproc.Fieldlines_pp(**fl_kw)),
+            ("dn", fs.postproc.DEM_normal_pp(kind="potential")),
+            ("mil", fs.postproc.DEM_normal_pp(kind="Milnor"))])
+        res.update({f"m2_{k}": v for k, v in r.items()})
+        res.update(m2_pix=c_pix, m2_Z=Z, m2_si=si, m2_cpt=f.get_std_cpt(c_pix))
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Mandelbrot_N(d, exponent=3)
+        f.zoom(x=0., y=0., dx=3., nx=32, xy_ratio=1., theta_deg=0.)
+        f.calc_std_div(calc_name="std", subset=None, max_iter=300, M_divergence=1000.,
+                       epsilon_stationnary=0.01, calc_orbit=True, backshift=3)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+        r = _run_postprocs(f, "std", c_pix, Z, U, sr, si, [
+            ("cont", fs.postproc.Continuous_iter_pp()),
+            ("fl", fs.postproc.Fieldlines_pp(**fl_kw)),
+            ("dn", fs.postproc.DEM_normal_pp(kind="potential"))])
+        res.update({f"mn3_{k}": v for k, v in r.items()})
+        res.update(mn3_pix=c_pix, mn3_Z=Z, mn3_si=si, mn3_cpt=f.get_std_cpt(c_pix))
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Burning_ship(d, flavor="Burning ship")
+        f.zoom(x=-0.5, y=-0.5, dx=3.5, nx=32, xy_ratio=1., theta_deg=0.)
+        f.calc_std_div(calc_name="std", subset=None, max_iter=300, M_divergence=1000.,
+                       calc_orbit=True, backshift=3)
+        c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+        r = _run_postprocs(f, "std", c_pix, Z, U, sr, si, [
+            ("cont", fs.postproc.Continuous_iter_pp()),
+            ("fl", fs.postproc.Fieldlines_pp(**fl_kw)),
+            ("dn", fs.postproc.DEM_normal_pp(kind="potential"))])
+        res.update({f"bs1_{k}": v for k, v in r.items()})
+        res.update(bs1_pix=c_pix, bs1_Z=Z, bs1_si=si, bs1_cpt=f.get_std_cpt(c_pix))
+    res.update(fl_n_iter=5, fl_swirl=0.7, fl_endpoint_k=0.5, backshift=3)
+    np.savez_compressed(out, **res)
+
+
 def opts_cases():
     """The calc_orbit / calc_d2zndc2 options of the standard and perturbation
     loops."""
@@ -807,6 +875,9 @@ def mn_cases():
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "opts":
         opts_cases()
+    elif len(sys.argv) > 2 and sys.argv[2] == "postproc":
+        mpmath.mp.dps = 50
+        golden_postproc(os.path.join(HERE, "postproc.npz"))
     elif len(sys.argv) > 2 and sys.argv[2] == "mn":
         mpmath.mp.dps = 50
         golden_std_mn(os.path.join(HERE, "std_mn.npz"))

@@ -291,3 +291,14 @@ def test_orbit_and_d2_options_codes(tmp_path):
     codes, spec = _codes(s, calc_name="c", subset=None, max_iter=100, M_divergence=1000.,
                          calc_orbit=True, backshift=2)
     assert spec.nZ == 8 and spec.i_znorbit == 6 and codes[0][6:] == ["xn_orbit", "yn_orbit"]
+
+
+def test_std_cpt_matches_reference(tmp_path):
+    """get_std_cpt (core.py:2781-2791): the pixel's c, bit for bit."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "postproc.npz"))
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=-0.5, y=0., dx=3., nx=32, xy_ratio=1., theta_deg=0.)
+    assert np.array_equal(f.get_std_cpt(d["m2_pix"]), d["m2_cpt"])
+    xs, ys = f.image_axes()
+    assert np.array_equal((xs[None, :] + 1j * ys[:, None]).ravel(), d["m2_pix"])

@@ -172,3 +172,31 @@ def test_power_n_calc_raw_vs_oracle(tmp_path, nexp, x, y, dx):
     assert np.array_equal(g.get_raw("s", "stop_iter").ravel(), sis.ravel())
     zn = g.get_raw("s", "zn").ravel()
     assert np.array_equal(zn.view(np.uint64), Zs[0].view(np.uint64))
+
+
+def test_postproc_batch_fieldlines_and_normals(tmp_path):
+    """Mandelbrot with calc_d2zndc2 and calc_orbit (backshift 3), then a
+    Postproc_batch of continuous iteration, field lines and DEM normals
+    (potential, Milnor), against the reference's outputs for the same view."""
+    import fractalshades_gb300.models as fsm
+    from fractalshades_gb300 import postproc as fspp
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "postproc.npz"))
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=-0.5, y=0., dx=3., nx=32, xy_ratio=1., theta_deg=0.)
+    f.calc_std_div(calc_name="std", subset=None, max_iter=400, M_divergence=1000.,
+                   epsilon_stationnary=0.01, calc_d2zndc2=True, calc_orbit=True, backshift=3)
+    f.calc_raw("std")
+    f.float_postproc_type = np.float64
+    b = fspp.Postproc_batch(f, "std")
+    b.add_postproc("cont", fspp.Continuous_iter_pp())
+    b.add_postproc("fl", fspp.Fieldlines_pp(n_iter=5, swirl=0.7, endpoint_k=0.5))
+    b.add_postproc("dn", fspp.DEM_normal_pp(kind="potential"))
+    b.add_postproc("mil", fspp.DEM_normal_pp(kind="Milnor"))
+    out = b.evaluate()
+    cont = out["cont"].ravel()
+    esc = np.isfinite(cont)
+    np.testing.assert_array_equal(cont, d["m2_cont"])
+    np.testing.assert_allclose(out["fl"].ravel()[esc], d["m2_fl"][esc], rtol=0, atol=1e-9)
+    for k in ("dn_x", "dn_y", "mil_x", "mil_y"):
+        np.testing.assert_allclose(out[k].ravel(), d[f"m2_{k}"], rtol=0, atol=1e-12)

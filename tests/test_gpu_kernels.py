@@ -514,3 +514,40 @@ def test_power_n_rejects_fe32_and_mismatched_exponent(ctx):
     for k in (0, 4):
         with pytest.raises(RuntimeError):
             ctx.perturb_tiles(nat.make_calc(max_iter=100, M_divergence=1e3, nexp=k), [t])
+
+
+# ---------------------------------------------------------------------------
+# post-processing kernels (csrc/fsg_postproc.cu) against the reference's
+# Postproc_batch outputs
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("pre,model,i_orb", [("m2", 0, 4), ("mn3", 3, 3), ("bs1", -1, 6)])
+def test_postproc_kernels_vs_reference(ctx, pre, model, i_orb):
+    """Field lines within 1e-9 (CUDA's sin / atan2 against glibc's), the
+    normals within 1e-12 of the reference's values."""
+    from oracle import postproc_ref as ppr
+    d = load("postproc")
+    Z = d[f"{pre}_Z"]
+    si = d[f"{pre}_si"].ravel()
+    zn = Z[0] if model >= 0 else Z[0] + 1j * Z[1]
+    nu, n = ppr.continuous_context(zn, si, 3 if model == 3 else 2, 1000.)
+    k, phi = ppr.fieldlines_params(int(d["fl_n_iter"]), float(d["fl_swirl"]),
+                                   float(d["fl_endpoint_k"]))
+    z = Z[i_orb] if model >= 0 else Z[i_orb] + 1j * Z[i_orb + 1]
+    fl = ctx.fieldlines(model=model, c=d[f"{pre}_cpt"], z=z, nu_frac=nu, n=n, k=k, phi=phi,
+                        is_backward=True, backshift=int(d["backshift"]))
+    esc = np.isfinite(nu)
+    np.testing.assert_allclose(fl[esc], d[f"{pre}_fl"][esc], rtol=0, atol=1e-9)
+    if model >= 0:
+        nv = ctx.normal(kind=0, zn=zn, dzndc=Z[2])
+    else:
+        nv = ctx.normal(kind=2, zn=zn, dzndc=Z[2:6])
+    np.testing.assert_allclose(nv.real, d[f"{pre}_dn_x"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(nv.imag, d[f"{pre}_dn_y"], rtol=0, atol=1e-12)
+    if pre == "m2":
+        mil = ctx.normal(kind=1, zn=zn, dzndc=Z[2], d2zndc2=Z[3])
+        np.testing.assert_allclose(mil.real, d["m2_mil_x"], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(mil.imag, d["m2_mil_y"], rtol=0, atol=1e-12)
+        # the skew is undone on the normal (core.py:3147-3158)
+        skew = np.array([[1.1, 0.2], [-0.3, 0.9]])
+        nvs = ctx.normal(kind=0, zn=zn, dzndc=Z[2], skew=skew)
+        np.testing.assert_allclose(nvs, ppr.normal(0, zn, dzndc=Z[2], skew=skew), atol=1e-12)

@@ -255,3 +255,44 @@ def test_perturb_bs_matches_reference(case):
     assert np.array_equal(sr, d["stop_reason"])
     assert np.array_equal(U, d["U"])
     assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
+
+
+# ---------------------------------------------------------------------------
+# field lines and DEM normals (postproc.py:409-628), golden vectors from the
+# reference's Postproc_batch
+# ---------------------------------------------------------------------------
+def _pp_inputs(d, pre):
+    from oracle import postproc_ref as ppr
+    Z = d[f"{pre}_Z"]
+    si = d[f"{pre}_si"].ravel()
+    zn = Z[0] if pre != "bs1" else Z[0] + 1j * Z[1]
+    deg = 3 if pre == "mn3" else 2
+    nu, n = ppr.continuous_context(zn, si, deg, 1000.)
+    return Z, zn, nu, n
+
+
+@pytest.mark.parametrize("pre,model,i_orb", [("m2", 0, 4), ("mn3", 3, 3), ("bs1", -1, 6)])
+def test_postproc_oracle_matches_reference(pre, model, i_orb):
+    from oracle import postproc_ref as ppr
+    d = load("postproc")
+    Z, zn, nu, n = _pp_inputs(d, pre)
+    np.testing.assert_array_equal(n + nu, d[f"{pre}_cont"])     # Continuous_iter_pp
+    k, phi = ppr.fieldlines_params(int(d["fl_n_iter"]), float(d["fl_swirl"]),
+                                   float(d["fl_endpoint_k"]))
+    z = Z[i_orb] if model >= 0 else Z[i_orb] + 1j * Z[i_orb + 1]
+    fl = ppr.fieldlines(model, d[f"{pre}_cpt"], z, nu, n, k, phi, True, int(d["backshift"]))
+    # escaped pixels: elsewhere the reference casts a NaN to int32, which
+    # depends on the platform (INT_MIN on x86-64, 0 on aarch64)
+    esc = np.isfinite(nu)
+    assert esc.sum() > 500
+    np.testing.assert_allclose(fl[esc], d[f"{pre}_fl"][esc], rtol=0, atol=1e-12)
+    if model >= 0:
+        nv = ppr.normal(0, zn, dzndc=Z[2])
+    else:
+        nv = ppr.normal(2, zn, jac=Z[2:6])
+    np.testing.assert_array_equal(nv.real, d[f"{pre}_dn_x"])
+    np.testing.assert_array_equal(nv.imag, d[f"{pre}_dn_y"])
+    if pre == "m2":
+        mil = ppr.normal(1, zn, dzndc=Z[2], d2zndc2=Z[3])
+        np.testing.assert_allclose(mil.real, d["m2_mil_x"], rtol=0, atol=1e-15)
+        np.testing.assert_allclose(mil.imag, d["m2_mil_y"], rtol=0, atol=1e-15)
