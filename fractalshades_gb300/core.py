@@ -36,6 +36,10 @@ logger = logging.getLogger(__name__)
 
 USER_INTERRUPTED = 1
 
+# core.py:60-72: supersampling option -> points per pixel side
+SUPERSAMPLING_DIC = {"None": None, None: None, "2x2": 2, "3x3": 3, "4x4": 4, "5x5": 5,
+                     "6x6": 6, "7x7": 7}
+
 
 class Fractal:
     REPORT_ITEMS = ["chunk1d_begin", "chunk1d_end", "chunk_pts", "done"]
@@ -354,6 +358,35 @@ class Fractal:
             logger.warning("Interruption signal received")
             return None
         return cycle_dep_args, chunk_subset
+
+    # ------------------------------------------------------------------
+    # final render: raw arrays computed on the fly (core.py:2572-2610)
+    # ------------------------------------------------------------------
+    def evaluate_rawdata_final(self, calc_name, chunk_slice, postproc_options):
+        """Raw arrays of one chunk for a final render, with the
+        postproc_options' jitter and supersampling ("None", "2x2" .. "7x7");
+        nothing is stored.  Returns (subset, c_pix, Z, U, stop_reason,
+        stop_iter), or None when interrupted."""
+        jitter = float(postproc_options.get("jitter", False))
+        supersampling = SUPERSAMPLING_DIC[postproc_options.get("supersampling", "None")]
+        if supersampling is not None and self._calc_data[calc_name]["state"].subset is not None:
+            raise NotImplementedError("supersampling of a subset calculation")
+        (cycle_dep_args, chunk_subset) = self.get_cycling_dep_args(
+            calc_name, chunk_slice, final=True, jitter=jitter, supersampling=supersampling)
+        cycle_indep_args = self._calc_data[calc_name]["cycle_indep_args"]
+        ret_code = self.numba_cycle_call(cycle_dep_args, cycle_indep_args)
+        if ret_code == self.USER_INTERRUPTED:
+            logger.error("Interruption signal received")
+            return None
+        (c_pix, Z, U, stop_reason, stop_iter) = cycle_dep_args
+        return (chunk_subset, c_pix, Z, U, stop_reason, stop_iter)
+
+    def evaluate_data(self, calc_name, chunk_slice, postproc_options):
+        """Raw arrays of a chunk: computed on the fly for a final render,
+        else reloaded from the stored memory maps (core.py:2595-2610)."""
+        if postproc_options.get("final_render", False):
+            return self.evaluate_rawdata_final(calc_name, chunk_slice, postproc_options)
+        return self.reload_data(chunk_slice, calc_name)
 
     # ------------------------------------------------------------------
     # whole image

@@ -40,7 +40,7 @@ class Postproc:
         return self.fractal.holomorphic
 
     def raw(self, key):
-        return self.fractal.get_raw(self.batch.calc_name, key).ravel()
+        return self.batch.raw(key)
 
     def get_zn(self):
         if self.holomorphic:
@@ -88,8 +88,9 @@ class Continuous_iter_pp(Postproc):
         with np.errstate(all="ignore"):
             nu_frac = Continuous_iter_pp_infinity(zn, pd["d"], pd["a_d"], pd["M"])
             nu_div, nu_mod = np.divmod(-nu_frac, 1.)
+            # a NaN nu_div (pixel not escaped) casts to a platform-dependent int
+            n = n - nu_div.astype(n.dtype)
         nu_frac = -nu_mod
-        n = n - nu_div.astype(n.dtype)
         val = (n - self._floor_iter) + nu_frac
         return val, {"potential_dic": pd, "nu_frac": nu_frac, "n": n,
                      "backshift": getattr(self.state, "backshift", None)}
@@ -156,9 +157,7 @@ class Fieldlines_pp(Postproc):
         is_backward = key.endswith("_orbit")
         if is_backward and backshift is None:
             raise ValueError("zn_orbit stored without a backshift in the calculation state")
-        xs, ys = self.fractal.image_axes()
-        c_pix = (xs[None, :] + 1j * ys[:, None]).ravel()
-        c_pt = self.fractal.get_std_cpt(c_pix)
+        c_pt = self.fractal.get_std_cpt(self.batch.c_pix())
         val = gpu.context().fieldlines(
             model=self._model(), c=c_pt, z=z, nu_frac=context["nu_frac"], n=context["n"],
             k=k_arr, phi=phi_arr, is_backward=is_backward,
@@ -198,20 +197,64 @@ class Postproc_batch:
         self.fractal = fractal
         self.calc_name = calc_name
         self.posts = {}
+        self._final = None
 
     def add_postproc(self, postname, postproc):
         postproc.link(self)
         self.posts[postname] = postproc
 
-    def evaluate(self):
+    def raw(self, key):
+        """A raw field, flat: from the final-render arrays being evaluated,
+        else from the calculation's stored results."""
+        if self._final is None:
+            return self.fractal.get_raw(self.calc_name, key).ravel()
+        (_subset, _c_pix, Z, U, sr, si) = self._final
+        complex_codes, int_codes, _ = self.fractal.codes
+        if key in complex_codes:
+            return Z[complex_codes.index(key)]
+        if key in int_codes:
+            return U[int_codes.index(key)]
+        if key == "stop_reason":
+            return sr[0]
+        if key == "stop_iter":
+            return si[0]
+        raise KeyError(key)
+
+    def c_pix(self):
+        """Screen positions of the evaluated points (fractions of dx)."""
+        if self._final is not None:
+            return self._final[1]
+        xs, ys = self.fractal.image_axes()
+        return (xs[None, :] + 1j * ys[:, None]).ravel()
+
+    def evaluate(self, postproc_options=None):
         """Evaluate every post-processing on the whole image; returns
-        {postname: float array (ny, nx)}."""
+        {postname: float array (ny, nx)}.  With postproc_options
+        {"final_render": True, "supersampling": "None" | "2x2" .. "7x7",
+        "jitter": False | float} the raw arrays are computed on the fly on the
+        jittered / supersampled grid (core.py:2572-2593) and the arrays are
+        (ny * s, nx * s)."""
+        from .core import SUPERSAMPLING_DIC
+        opts = postproc_options or {}
+        ssg = 1
+        if opts.get("final_render", False):
+            chunk = (0, self.fractal.nx, 0, self.fractal.ny)
+            self._final = self.fractal.evaluate_rawdata_final(self.calc_name, chunk, opts)
+            if self._final is None:
+                return None
+            ssg = SUPERSAMPLING_DIC[opts.get("supersampling", "None")] or 1
+        try:
+            return self._evaluate(ssg)
+        finally:
+            self._final = None
+
+    def _evaluate(self, ssg):
         out = {}
         context = {}
         for name, pp in self.posts.items():
             val, upd = pp.evaluate(context)
             context.update(upd)
-            shape = (self.fractal.ny, self.fractal.nx)
+            shape = (self.fractal.ny * ssg, self.fractal.nx * ssg)
             if getattr(pp, "field_count", 1) == 2:
                 # the two components, as the reference's XYCoord_wrapper_pp
                 out[name + "_x"] = np.asarray(val.real, self.fractal.float_postproc_type).reshape(shape)

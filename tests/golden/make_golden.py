@@ -669,6 +669,27 @@ def golden_postproc(out):
     np.savez_compressed(out, **res)
 
 
+def golden_pixel_grids(out):
+    """Fractal.chunk_pixel_pos (core.py:1767-1830) with supersampling and
+    jitter, whole image and one inner chunk, xy_ratio 1.5."""
+    res = {}
+    with tempfile.TemporaryDirectory() as d:
+        f = fsm.Mandelbrot(d)
+        f.zoom(x=-0.5, y=0., dx=3., nx=40, xy_ratio=1.5, theta_deg=0.)
+        # float_type follows the calculation's complex_type
+        f.calc_std_div(calc_name="std", subset=None, max_iter=10, M_divergence=1000.,
+                       epsilon_stationnary=0.01)
+        f._calc_data["std"]["state"].complex_type = np.complex128
+        f.complex_type = np.complex128
+        cases = {"plain": (False, None), "ss3": (False, 3), "jit": (0.7, None),
+                 "ss2_jit": (1.0, 2)}
+        for chunk_name, cs in (("full", (0, f.nx, 0, f.ny)), ("inner", (8, 24, 4, 20))):
+            for name, (jit, ssg) in cases.items():
+                res[f"{chunk_name}_{name}"] = f.chunk_pixel_pos(cs, jit, ssg)
+        res["nx"], res["ny"] = f.nx, f.ny
+    np.savez_compressed(out, **res)
+
+
 def opts_cases():
     """The calc_orbit / calc_d2zndc2 options of the standard and perturbation
     loops."""
@@ -878,6 +899,7 @@ if __name__ == "__main__":
     elif len(sys.argv) > 2 and sys.argv[2] == "postproc":
         mpmath.mp.dps = 50
         golden_postproc(os.path.join(HERE, "postproc.npz"))
+        golden_pixel_grids(os.path.join(HERE, "pixel_grids.npz"))
     elif len(sys.argv) > 2 and sys.argv[2] == "mn":
         mpmath.mp.dps = 50
         golden_std_mn(os.path.join(HERE, "std_mn.npz"))

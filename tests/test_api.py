@@ -302,3 +302,18 @@ def test_std_cpt_matches_reference(tmp_path):
     assert np.array_equal(f.get_std_cpt(d["m2_pix"]), d["m2_cpt"])
     xs, ys = f.image_axes()
     assert np.array_equal((xs[None, :] + 1j * ys[:, None]).ravel(), d["m2_pix"])
+
+
+@pytest.mark.parametrize("chunk", ["full", "inner"])
+@pytest.mark.parametrize("case,jitter,ssg", [("plain", False, None), ("ss3", False, 3),
+                                             ("jit", 0.7, None), ("ss2_jit", 1.0, 2)])
+def test_chunk_pixel_pos_matches_reference(tmp_path, chunk, case, jitter, ssg):
+    """Supersampled and jittered grids (core.py:1767-1830), bit for bit."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "pixel_grids.npz"))
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=-0.5, y=0., dx=3., nx=40, xy_ratio=1.5, theta_deg=0.)
+    cs = (0, f.nx, 0, f.ny) if chunk == "full" else (8, 24, 4, 20)
+    assert (f.nx, f.ny) == (int(d["nx"]), int(d["ny"]))
+    got = f.chunk_pixel_pos(cs, jitter, ssg)
+    assert np.array_equal(got, d[f"{chunk}_{case}"])

@@ -200,3 +200,25 @@ def test_postproc_batch_fieldlines_and_normals(tmp_path):
     np.testing.assert_allclose(out["fl"].ravel()[esc], d["m2_fl"][esc], rtol=0, atol=1e-9)
     for k in ("dn_x", "dn_y", "mil_x", "mil_y"):
         np.testing.assert_allclose(out[k].ravel(), d[f"m2_{k}"], rtol=0, atol=1e-12)
+
+
+def test_final_render_supersampling_and_jitter(tmp_path):
+    """Postproc_batch in final-render mode: the raw arrays are computed on the
+    fly on the 2x2-supersampled, jittered grid (core.py:2572-2593) -- the
+    continuous iteration count equals the oracle's on the same points."""
+    import fractalshades_gb300.models as fsm
+    from fractalshades_gb300 import postproc as fspp
+    from oracle import postproc_ref as ppr
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=-0.5, y=0., dx=3., nx=60, xy_ratio=1.5, theta_deg=0.)
+    f.calc_std_div(calc_name="std", subset=None, max_iter=300, M_divergence=1000.,
+                   epsilon_stationnary=0.01)
+    f.float_postproc_type = np.float64
+    b = fspp.Postproc_batch(f, "std")
+    b.add_postproc("cont", fspp.Continuous_iter_pp())
+    out = b.evaluate({"final_render": True, "supersampling": "2x2", "jitter": 0.5})
+    assert out["cont"].shape == (2 * f.ny, 2 * f.nx)
+    pix = np.ravel(f.chunk_pixel_pos((0, f.nx, 0, f.ny), 0.5, 2))
+    Zo, sio, sro = orc.std_m2(pix, -0.5 + 0j, f.lin_mat, 3.0, 300, 1000., 0.01)
+    nu, n = ppr.continuous_context(Zo[0], sio.ravel(), 2, 1000.)
+    np.testing.assert_array_equal(out["cont"].ravel(), n + nu)
