@@ -65,6 +65,7 @@ class Tile(ct.Structure):
         ("Z", P), ("nZ", I32), ("i_dzndz", I32), ("i_dzndc", I32),
         ("U", P), ("stop_reason", P), ("stop_iter", P), ("potential", P), ("dem", P),
         ("dzndc_scale_e", I32), ("i_znorbit", I32),
+        ("proj", I32), ("proj_h", F64), ("proj_ht_re", F64), ("proj_ht_im", F64),
     ]
 
 
@@ -346,10 +347,17 @@ class Reference:
         raise ValueError(which)
 
 
+def _set_proj(t, proj):
+    """proj = (kind, h, Re ht, Im ht) of projection.kernel_params, or None
+    (Cartesian)."""
+    kind, h, hr, hi = proj if proj is not None else (0, 0., 0., 0.)
+    t.proj, t.proj_h, t.proj_ht_re, t.proj_ht_im = int(kind), float(h), float(hr), float(hi)
+
+
 def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None, U=None,
               ref=None, center=0j, dx=0.0, dx_m=0.0, dx_e=0, drift_m=0j, drift_e=0,
               drifty_m=0.0, drifty_e=0, i_dzndz=-1, i_dzndc=-1, potential=None,
-              dem=None, keep=None, dzndc_scale_e=0, i_znorbit=0):
+              dem=None, keep=None, dzndc_scale_e=0, i_znorbit=0, proj=None):
     """Fill a Tile from numpy (host) arrays: either the axes xs / ys of a
     rectangle or an explicit complex128 list of pixel positions ``pix``."""
     t = Tile()
@@ -375,6 +383,7 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
     t.potential, t.dem = _p(potential), _p(dem)
     t.dzndc_scale_e = int(dzndc_scale_e)
     t.i_znorbit = int(i_znorbit)
+    _set_proj(t, proj)
     if keep is not None:
         keep.extend([xs, ys, pix, Z, U, stop_reason, stop_iter, potential, dem])
     return t
@@ -383,7 +392,8 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
 def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_ptr,
                    stop_iter_ptr, U_ptr=0, ref=None, center=0j, dx=0.0, dx_m=0.0,
                    dx_e=0, drift_m=0j, drift_e=0, drifty_m=0.0, drifty_e=0, i_dzndz=-1,
-                   i_dzndc=-1, potential_ptr=0, dem_ptr=0, dzndc_scale_e=0, i_znorbit=0):
+                   i_dzndc=-1, potential_ptr=0, dem_ptr=0, dzndc_scale_e=0, i_znorbit=0,
+                   proj=None):
     """Fill a Tile from raw device pointers (ints)."""
     t = Tile()
     t.nx, t.ny = int(nx), int(ny)
@@ -403,6 +413,7 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
     t.potential, t.dem = potential_ptr or None, dem_ptr or None
     t.dzndc_scale_e = int(dzndc_scale_e)
     t.i_znorbit = int(i_znorbit)
+    _set_proj(t, proj)
     return t
 
 

@@ -327,8 +327,10 @@ class Fractal:
         """Digest of the zoom and calculation parameters (core.py:2029-2041):
         here the GPU calculation options returned by ``iterate``."""
         center = self.x + 1j * self.y
-        return (initialize, iterate, complex(center), self.proj_impl, self.lin_mat,
-                float(self.dx), self._interrupted)
+        # the projection as the kernels' fields (fsg_tile.proj*), in place of
+        # the reference's numba proj_impl
+        return (initialize, iterate, complex(center), fsproj.kernel_params(self.projection),
+                self.lin_mat, float(self.dx), self._interrupted)
 
     def get_cycling_dep_args(self, calc_name, chunk_slice, final=False, jitter=False,
                              supersampling=None):
@@ -665,8 +667,11 @@ class Fractal:
         return arr["subset"], c_pix, arr["Z"], arr["U"], arr["stop_reason"], arr["stop_iter"]
 
     def get_std_cpt(self, c_pix):
-        """c = center + dx * lin_mat . pix (core.py:2781-2794)."""
+        """c = center + dx * lin_mat . proj(pix) (core.py:2781-2794,
+        c_from_pix :3161-3194)."""
         center = complex(self.x + 1j * self.y)
+        if getattr(self.projection, "kernel_kind", 0):
+            c_pix = self.projection.f(np.asarray(c_pix))
         x, y = c_pix.real, c_pix.imag
         m = self.lin_mat
         x1 = m[0, 0] * x + m[0, 1] * y

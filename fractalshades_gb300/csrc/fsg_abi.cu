@@ -152,6 +152,7 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
         return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e applies to the perturbation loops only");
     if (t.dzndc_scale_e < -100000 || t.dzndc_scale_e > 100000)
         return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e out of range");
+    if (t.proj < 0 || t.proj > 1) return set_err(ctx, FSG_ERR_ARG, "bad projection kind");
     if (perturb && calc->flavor != 0) {
         if (calc->mode == FSG_MODE_XR64)
             return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 and FSG_MODE_FE32");
@@ -219,6 +220,7 @@ TileDev make_tile(const fsg_tile &t) {
     d.pot = t.potential; d.dem = t.dem;
     d.dzs = t.dzndc_scale_e;
     d.i_orb = t.i_znorbit;
+    d.proj = t.proj; d.ph = t.proj_h; d.pht_re = t.proj_ht_re; d.pht_im = t.proj_ht_im;
     return d;
 }
 

@@ -355,6 +355,11 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         BSRef<T>::hess(R, w, Ha, Hb, Hc, Hd);
         hd[0] = to_d(scale2(h[0] + Ha, Tl.dzs)); hd[1] = to_d(scale2(h[1] + Hb, Tl.dzs));
         hd[2] = to_d(scale2(h[2] + Hc, Tl.dzs)); hd[3] = to_d(scale2(h[3] + Hd, Tl.dzs));
+        if (Tl.proj) {
+            // Expmap (perturbation.py:1772-1776)
+            const double m = fsg_dzndc_modifier(Tl, ip);
+            hd[0] *= m; hd[1] *= m; hd[2] *= m; hd[3] *= m;
+        }
     }
     double *Z = (double *)Tl.Z;
     if (bs > 0) {

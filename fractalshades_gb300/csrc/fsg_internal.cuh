@@ -70,6 +70,8 @@ struct TileDev {
     double *pot, *dem;
     int dzs;                                   // dzndc scale 2^dzs over the reference's
     int i_orb;                                 // Z row of the orbit point
+    int proj;                                  // 0 Cartesian, 1 Expmap
+    double ph, pht_re, pht_im;                 // Expmap: exp(ph + pht * pix)
 };
 
 // The Burning Ship map of flavor 1..5 (burning_ship.py:82-123 BS_iterate,
@@ -161,6 +163,42 @@ __device__ __forceinline__ void fsg_flush_stats(const WorkDev &W, unsigned long 
     }
 }
 
+// Screen position of pixel ip of a tile
+__device__ __forceinline__ double2 fsg_pixel_raw(const TileDev &T, long long ip) {
+    if (T.pix) return __ldg(&T.pix[ip]);
+    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
+    return make_double2(__ldg(&T.xs[ix]), __ldg(&T.ys[iy]));
+}
+
+// Re(pht * pix): the h coordinate of an Expmap pixel (projection.py:306-314)
+__device__ __forceinline__ double fsg_proj_h(const TileDev &T, double2 p) {
+    return T.pht_re * p.x - T.pht_im * p.y;
+}
+
+// Expmap.f (projection.py:363-373): exp(h_moy + ht * pix).  Not inlined:
+// its transcendental functions stay out of the iteration kernels' register
+// allocation (called once per pixel)
+static __device__ __noinline__ double2 fsg_expmap(double ph, double hr, double hi, double2 p) {
+    const double zr = ph + (hr * p.x - hi * p.y);
+    const double zi = hr * p.y + hi * p.x;
+    const double e = exp(zr);
+    return make_double2(e * cos(zi), e * sin(zi));
+}
+static __device__ __noinline__ double fsg_exp_nl(double x) { return exp(x); }
+
+// The projected screen position (Cartesian: pix)
+__device__ __forceinline__ double2 fsg_pixel(const TileDev &T, long long ip) {
+    double2 p = fsg_pixel_raw(T, ip);
+    if (T.proj == 0) return p;
+    return fsg_expmap(T.ph, T.pht_re, T.pht_im, p);
+}
+
+// Expmap's derivative modifier of the perturbation loops
+// (projection.py:455-473): exp(Re(ht * pix) + h_moy)
+__device__ __forceinline__ double fsg_dzndc_modifier(const TileDev &T, long long ip) {
+    return fsg_exp_nl(fsg_proj_h(T, fsg_pixel_raw(T, ip)) + T.ph);
+}
+
 // Potential (postproc.py:352-406 with Continuous_iter_pp_infinity :1001-1009,
 // d = the degree, a_d = 1) and distance estimate (postproc.py:684-731).
 __device__ __forceinline__ void fsg_epilogue(const TileDev &T, const CalcDev &C, long long ip,
@@ -173,15 +211,13 @@ __device__ __forceinline__ void fsg_epilogue(const TileDev &T, const CalcDev &C,
         double q = floor(x);
         T.pot[ip] = ((double)n - q) - (x - q);
     }
-    if (T.dem) T.dem[ip] = az * log(az) / absd;
+    if (T.dem) {
+        // |get_dzndc| = |dzndc| |df| with Expmap's |df| = exp(Re(ht * pix))
+        if (T.proj) absd *= fsg_exp_nl(fsg_proj_h(T, fsg_pixel_raw(T, ip)));
+        T.dem[ip] = az * log(az) / absd;
+    }
 }
 
-// Screen position of pixel ip of a tile
-__device__ __forceinline__ double2 fsg_pixel(const TileDev &T, long long ip) {
-    if (T.pix) return __ldg(&T.pix[ip]);
-    int ix = (int)(ip % T.nx), iy = (int)(ip / T.nx);
-    return make_double2(__ldg(&T.xs[ix]), __ldg(&T.ys[iy]));
-}
 
 // Persistent grid for a kernel: every SM filled to its occupancy limit,
 // capped by the number of blocks the work needs.  grid > 0 is kept as given.

@@ -86,7 +86,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     for (int32_t i = 0; i < ntiles; i++) {
         const fsg_tile &t = tiles[i];
         if (t.nx <= 0 || t.ny <= 0 || t.nZ < nZ_min || !t.Z || !t.stop_reason || !t.stop_iter
-            || (!t.pix && (!t.xs || !t.ys)))
+            || (!t.pix && (!t.xs || !t.ys)) || t.proj != 0)
             return FSG_ERR_ARG;
         TileDev &d = host.tiles[i];
         memset(&d, 0, sizeof(d));

@@ -219,6 +219,8 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
     }
     Z[ip] = zn;
     if (dzndz_on) Z[T.i_dzndz * np + ip] = dzndz;
+    // Expmap: derivatives times exp(Re(ht pix) + h_moy) (perturbation.py:1387-1388)
+    if (dzndc_on && T.proj) dzndc = rmul(fsg_dzndc_modifier(T, ip), dzndc);
     if (dzndc_on) Z[T.i_dzndc * np + ip] = dzndc;
     if (T.U) T.U[ip] = w;
     T.stop_iter[ip] = n;

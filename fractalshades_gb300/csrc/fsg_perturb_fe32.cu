@@ -448,6 +448,7 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     double2 *Z = (double2 *)T.Z;
     Z[ip] = zn;
     if (dzndz_on) Z[T.i_dzndz * np + ip] = xrsem ? cx(0., 0.) : fe_to_d(as_fe(s.qx, s.qy, s.G));
+    if (dzndc_on && T.proj) dzc = rmul(fsg_dzndc_modifier(T, ip), dzc);
     if (dzndc_on) Z[T.i_dzndc * np + ip] = dzc;
     if (T.U) T.U[ip] = w;
     T.stop_iter[ip] = n;

@@ -141,7 +141,7 @@ def run_std_pixels(cycle_dep_args, cycle_indep_args):
     """numba_cycles replacement (core.py:2935-2963): one tile of pixels given
     as the reference's c_pix array."""
     c_pix, Z, U, stop_reason, stop_iter = cycle_dep_args
-    (_init, spec, center, _proj, lin_mat, dx, interrupted) = cycle_indep_args
+    (_init, spec, center, proj, lin_mat, dx, interrupted) = cycle_indep_args
     if interrupted[0]:
         return 1
     if c_pix.size == 0:
@@ -150,7 +150,8 @@ def run_std_pixels(cycle_dep_args, cycle_indep_args):
     pix = np.ascontiguousarray(c_pix, dtype=np.complex128)
     Zw = Z if Z.flags.c_contiguous else np.ascontiguousarray(Z)
     t = nat.make_tile(pix=pix, lin_mat=lin_mat, Z=Zw, stop_reason=stop_reason,
-                      stop_iter=stop_iter, center=center, dx=dx, i_znorbit=spec.i_znorbit)
+                      stop_iter=stop_iter, center=center, dx=dx, i_znorbit=spec.i_znorbit,
+                      proj=proj)
     rc = ctx.std_tiles(spec.calc(), [t], nat.HOST)
     if Zw is not Z:
         Z[...] = Zw
@@ -163,7 +164,8 @@ def _tile_for(fractal_args, spec, pix=None, xs=None, ys=None, Z=None, U=None, sr
     kw = dict(lin_mat=fractal_args["lin_mat"], Z=Z, U=U, stop_reason=sr, stop_iter=si,
               ref=ref, dx_m=fractal_args["dx_m"], dx_e=fractal_args["dx_e"],
               i_dzndz=spec.i_dzndz, i_dzndc=spec.i_dzndc, potential=pot, dem=dem,
-              dzndc_scale_e=fractal_args.get("dzndc_scale_e", 0), i_znorbit=spec.i_znorbit)
+              dzndc_scale_e=fractal_args.get("dzndc_scale_e", 0), i_znorbit=spec.i_znorbit,
+              proj=fractal_args.get("proj"))
     if spec.flavor == 0:
         kw.update(drift_m=fractal_args["drift_m"], drift_e=fractal_args["drift_e"])
     else:
@@ -218,10 +220,10 @@ def run_image(fractal, xs, ys, cycle_indep_args, potential=True):
                       U=U if nU else None, sr=sr, si=si, pot=pot, dem=dem)
         rc = ctx.perturb_tiles(spec.calc(), [t], nat.HOST)
     else:
-        (_init, spec, center, _proj, lin_mat, dx, interrupted) = cycle_indep_args
+        (_init, spec, center, proj, lin_mat, dx, interrupted) = cycle_indep_args
         t = nat.make_tile(xs=xs, ys=ys, lin_mat=lin_mat, Z=Z, stop_reason=sr, stop_iter=si,
                           center=center, dx=dx, potential=pot, dem=dem,
-                          i_znorbit=spec.i_znorbit)
+                          i_znorbit=spec.i_znorbit, proj=proj)
         rc = ctx.std_tiles(spec.calc(), [t], nat.HOST)
     if rc == nat.FSG_INTERRUPTED:
         return None

@@ -308,9 +308,14 @@ class PerturbationFractal(Fractal):
              driftx_xr, drifty_xr, dx_xr) = pd
         if ref_order is None:
             ref_order = (1 << 62)
+        # the derivative paths' scale: dx times the projection's
+        # (perturbation.py:459-468)
         scale = dx_xr
         if self.projection.scale != 1.:
-            raise NotImplementedError("projection scale != 1")
+            # dx_xr * scale_xr as the reference's Xrange product: the
+            # mantissas' double product
+            sx = fsx.mpf_to_Xrange(self.projection.scale)
+            scale = fsx.XrScalar(dx_xr.m * sx.m, dx_xr.e + sx.e)
         self.kc = kc = self.ref_point_kc()
         if kc.to_standard() == 0.:
             raise RuntimeError(
@@ -339,7 +344,8 @@ class PerturbationFractal(Fractal):
                 "lin_mat": self.lin_mat, "dx_m": dx_xr.m, "dx_e": dx_xr.e,
                 "interrupted": self._interrupted, "kc": kc,
                 "ref_div_iter": ref_div_iter, "ref_order": ref_order, "has_xr": has_xr,
-                "dzndc_scale_e": dzndc_scale_e}
+                "dzndc_scale_e": dzndc_scale_e,
+                "proj": fsproj.kernel_params(self.projection)}
         if holomorphic:
             args.update(drift_m=drift_xr.m, drift_e=drift_xr.e)
         else:
@@ -348,7 +354,10 @@ class PerturbationFractal(Fractal):
         return args
 
     def get_std_cpt(self, c_pix):
+        """c of each pixel in double (perturbation.py:196-207 std_C_from_pix)."""
         center = complex(self.x + 1j * self.y)
+        if getattr(self.projection, "kernel_kind", 0):
+            c_pix = self.projection.f(np.asarray(c_pix))
         x, y = c_pix.real, c_pix.imag
         m = self.lin_mat
         x1 = m[0, 0] * x + m[0, 1] * y

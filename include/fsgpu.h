@@ -153,6 +153,15 @@ typedef struct {
     /* with fsg_calc.backshift > 0: the Z row of the orbit point (complex
        zn_orbit; Burning Ship: xn_orbit, then yn_orbit in the next row) */
     int32_t i_znorbit;
+    /* projection of the screen position before lin_mat (projection.py):
+       0 Cartesian (identity); 1 Expmap, pix -> exp(proj_h + proj_ht * pix)
+       with proj_ht = proj_ht_re + i proj_ht_im (:363-373).  With Expmap the
+       perturbation loops multiply the derivatives at exit by
+       exp(Re(proj_ht * pix) + proj_h) (:455-473, perturbation.py:1387-1388,
+       1772-1776) and the fused distance estimate divides by
+       |df| = exp(Re(proj_ht * pix)) (postproc.py:184-205) */
+    int32_t proj;
+    double proj_h, proj_ht_re, proj_ht_im;
 } fsg_tile;
 
 /* Post-processing on the device (postproc.py).  Pointers are host or device

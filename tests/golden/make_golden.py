@@ -397,12 +397,12 @@ def golden_std_bs(out):
 
 def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
                       interior, bla_eps=1e-6, eps_stat=1e-3, M=1000.,
-                      ref_shift=0j, x_offset="0", backshift=0):
+                      ref_shift=0j, x_offset="0", backshift=0, projection=None):
     with tempfile.TemporaryDirectory() as d:
         f = fsm.Perturbation_mandelbrot(d)
         x = str(mpmath.mpf(x) + mpmath.mpf(x_offset))
         f.zoom(precision=precision, x=x, y=y, dx=dx, nx=nx, xy_ratio=1.,
-               theta_deg=0., projection=fs.projection.Cartesian())
+               theta_deg=0., projection=projection or fs.projection.Cartesian())
         ref_point = mpmath.mpc(x, y) + mpmath.mpc(ref_shift) * mpmath.mpf(dx)
         f.max_iter = max_iter
         f.M_divergence = M
@@ -512,11 +512,11 @@ def golden_perturb_mn(out, *, nexp, x, y, dx, nx, precision, order, max_iter,
 
 
 def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
-                      bla_eps=1e-6, M=1000., backshift=0):
+                      bla_eps=1e-6, M=1000., backshift=0, projection=None):
     with tempfile.TemporaryDirectory() as d:
         f = fsm.Perturbation_burning_ship(d, flavor=flavor)
         f.zoom(precision=precision, x=x, y=y, dx=dx, nx=nx, xy_ratio=1.,
-               theta_deg=0., projection=fs.projection.Cartesian())
+               theta_deg=0., projection=projection or fs.projection.Cartesian())
         ref_point = mpmath.mpc(x, y)
         f.max_iter = max_iter
         f.M_divergence = M
@@ -688,6 +688,53 @@ def golden_pixel_grids(out):
                 res[f"{chunk_name}_{name}"] = f.chunk_pixel_pos(cs, jit, ssg)
         res["nx"], res["ny"] = f.nx, f.ny
     np.savez_compressed(out, **res)
+
+
+def golden_expmap(out):
+    """Standard power-2 loop under an Expmap projection (horizontal and
+    vertical orientations): the projected pixel c = center + dx lin
+    exp(h_moy + ht pix) (core.py:3161-3194, projection.py:363-373)."""
+    res = {}
+    for name, orient in (("h", "horizontal"), ("v", "vertical")):
+        with tempfile.TemporaryDirectory() as d:
+            f = fsm.Mandelbrot(d)
+            proj = fs.projection.Expmap(hmin=0., hmax=4., rotates_df=True, orientation=orient)
+            f.zoom(x=-0.743643887037151, y=0.13182590420533, dx=1e-4, nx=24, xy_ratio=1.,
+                   theta_deg=15., projection=proj)
+            f.calc_std_div(calc_name="std", subset=None, max_iter=2000, M_divergence=1000.,
+                           epsilon_stationnary=0.01)
+            c_pix, Z, U, sr, si, cia = run_tile(f, "std")
+            res.update({f"{name}_pix": c_pix, f"{name}_Z": Z, f"{name}_si": si,
+                        f"{name}_sr": sr, f"{name}_lin_mat": f.lin_mat,
+                        f"{name}_nx": f.nx, f"{name}_ny": f.ny,
+                        f"{name}_xy_ratio": f.xy_ratio,
+                        f"{name}_c": f.get_std_cpt(c_pix)})
+    np.savez_compressed(out, **res)
+
+
+def expmap_cases():
+    # the calculation fingerprint pickles the projection, whose mapping
+    # functions are numba dispatchers in the reference and plain closures
+    # here; the fixtures need no fingerprint
+    fs.core.Fractal.save_fingerprint = lambda self, calc_name, fingerprint: None
+    mpmath.mp.dps = 50
+    golden_expmap(os.path.join(HERE, "std_expmap.npz"))
+    print("std_expmap done", flush=True)
+    mpmath.mp.dps = 30
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_expmap.npz"),
+        x="-0.743643887037151", y="0.131825904205330", dx="2.e-9", nx=12,
+        precision=30, order=None, max_iter=6000, interior=False,
+        projection=fs.projection.Expmap(hmin=0., hmax=5., rotates_df=True,
+                                        orientation="horizontal"))
+    print("pert_m2_expmap done", flush=True)
+    golden_perturb_bs(
+        os.path.join(HERE, "pert_bs_expmap.npz"),
+        x="-1.773934837092732", y="-0.00025062656641604286", dx="4.e-7",
+        nx=10, precision=30, max_iter=5000, flavor="Burning ship",
+        projection=fs.projection.Expmap(hmin=0., hmax=3., rotates_df=True,
+                                        orientation="vertical"))
+    print("pert_bs_expmap done", flush=True)
 
 
 def opts_cases():
@@ -896,6 +943,8 @@ def mn_cases():
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "opts":
         opts_cases()
+    elif len(sys.argv) > 2 and sys.argv[2] == "expmap":
+        expmap_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "postproc":
         mpmath.mp.dps = 50
         golden_postproc(os.path.join(HERE, "postproc.npz"))

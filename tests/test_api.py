@@ -317,3 +317,22 @@ def test_chunk_pixel_pos_matches_reference(tmp_path, chunk, case, jitter, ssg):
     assert (f.nx, f.ny) == (int(d["nx"]), int(d["ny"]))
     got = f.chunk_pixel_pos(cs, jitter, ssg)
     assert np.array_equal(got, d[f"{chunk}_{case}"])
+
+
+@pytest.mark.parametrize("orient,key", [("horizontal", "h"), ("vertical", "v")])
+def test_expmap_zoom_and_pixel_c_match_reference(tmp_path, orient, key):
+    """Expmap (projection.py:226-503): the zoom's adjusted nx / xy_ratio, the
+    pixel grid and each pixel's c (core.py:2781-2791) as the reference's."""
+    import os
+    from fractalshades_gb300 import projection as fsproj
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "std_expmap.npz"))
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=-0.743643887037151, y=0.13182590420533, dx=1e-4, nx=24, xy_ratio=1.,
+           theta_deg=15., projection=fsproj.Expmap(hmin=0., hmax=4., orientation=orient))
+    assert (f.nx, f.ny, f.xy_ratio) == (int(d[f"{key}_nx"]), int(d[f"{key}_ny"]),
+                                        float(d[f"{key}_xy_ratio"]))
+    assert np.array_equal(f.lin_mat, d[f"{key}_lin_mat"])
+    xs, ys = f.image_axes()
+    pix = (xs[None, :] + 1j * ys[:, None]).ravel()
+    assert np.array_equal(pix, d[f"{key}_pix"])
+    np.testing.assert_allclose(f.get_std_cpt(pix), d[f"{key}_c"], rtol=1e-15, atol=0)

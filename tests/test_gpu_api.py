@@ -222,3 +222,20 @@ def test_final_render_supersampling_and_jitter(tmp_path):
     Zo, sio, sro = orc.std_m2(pix, -0.5 + 0j, f.lin_mat, 3.0, 300, 1000., 0.01)
     nu, n = ppr.continuous_context(Zo[0], sio.ravel(), 2, 1000.)
     np.testing.assert_array_equal(out["cont"].ravel(), n + nu)
+
+
+def test_std_expmap_calc_raw_vs_reference(tmp_path):
+    """Mandelbrot under Expmap through the model API (zoom adjusts nx and
+    xy_ratio, the kernels project each pixel) against the reference."""
+    import fractalshades_gb300.models as fsm
+    from fractalshades_gb300 import projection as fsproj
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "std_expmap.npz"))
+    f = fsm.Mandelbrot(str(tmp_path))
+    f.zoom(x=-0.743643887037151, y=0.13182590420533, dx=1e-4, nx=24, xy_ratio=1.,
+           theta_deg=15., projection=fsproj.Expmap(hmin=0., hmax=4.))
+    f.calc_std_div(calc_name="s", subset=None, max_iter=2000, M_divergence=1000.,
+                   epsilon_stationnary=0.01)
+    f.calc_raw("s")
+    si = f.get_raw("s", "stop_iter").ravel()
+    assert np.mean(si == d["h_si"].ravel()) >= 0.995

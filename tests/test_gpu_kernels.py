@@ -551,3 +551,108 @@ def test_postproc_kernels_vs_reference(ctx, pre, model, i_orb):
         skew = np.array([[1.1, 0.2], [-0.3, 0.9]])
         nvs = ctx.normal(kind=0, zn=zn, dzndc=Z[2], skew=skew)
         np.testing.assert_allclose(nvs, ppr.normal(0, zn, dzndc=Z[2], skew=skew), atol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# Expmap projection in the kernels (fsg_tile.proj): CUDA's exp / sin / cos
+# place a pixel's c within an ulp or two of numpy's, so chaotic pixels may
+# take another count; the rest agree to 1e-6
+# ---------------------------------------------------------------------------
+def _expmap(hmax, orient, xy_ratio):
+    from fractalshades_gb300 import projection as fsproj
+    p = fsproj.Expmap(hmin=0., hmax=hmax, orientation=orient)
+    p.xy_ratio = xy_ratio
+    p.make_impl()
+    return p
+
+
+@pytest.mark.parametrize("key", ["h", "v"])
+def test_std_expmap_vs_reference(ctx, key):
+    from fractalshades_gb300 import _native as nat
+    d = load("std_expmap")
+    p = _expmap(4., {"h": "horizontal", "v": "vertical"}[key], float(d[f"{key}_xy_ratio"]))
+    nx = int(d[f"{key}_nx"])
+    xs, ys = axes(d[f"{key}_pix"], nx)
+    n = xs.size * ys.size
+    Z = np.zeros((3, n), dtype=np.complex128)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d[f"{key}_lin_mat"], Z=Z, stop_reason=sr,
+                      stop_iter=si, center=-0.743643887037151 + 0.13182590420533j, dx=1e-4,
+                      proj=p.kernel_params())
+    ctx.std_tiles(nat.make_calc(max_iter=2000, M_divergence=1000., epsilon_stationnary=0.01),
+                  [t])
+    iter_agree(si, d[f"{key}_si"], frac=0.995, tol=2000)
+    same = (si == d[f"{key}_si"]).ravel()
+    rel_close(Z[0], d[f"{key}_Z"][0], 1e-6, same)
+
+
+def _expmap_scale(d, hmoy):
+    """dx * exp(h_moy) as the reference's Xrange product (perturbation.py:459-468)"""
+    import mpmath
+    m, e = mpmath.frexp(mpmath.exp(hmoy))
+    return float(d["dx_m"]) * float(m), int(d["dx_e"]) + int(e)
+
+
+def test_perturb_expmap_vs_reference(ctx):
+    """Power-2 perturbation (FP64) under Expmap: derivative paths at the
+    scale dx exp(h_moy), projected pixels, dzndc times the exit modifier."""
+    from fractalshades_gb300 import _native as nat
+    d = load("pert_m2_expmap")
+    p = _expmap(5., "horizontal", 5. / (2. * np.pi))
+    sm, se = _expmap_scale(d, 2.5)
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    ref = nat.Reference(ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
+                        calc_dzndc=True, scale_m=sm, scale_e=se, bla=True, kc=kc,
+                        bla_eps=float(d["bla_eps"]))
+    dz = ref.download("dzndc")
+    assert np.array_equal(dz.view(np.uint64), d["dZndc"].view(np.uint64))
+    xs = np.unique(d["pix"].real)
+    ys = np.unique(d["pix"].imag)[::-1]
+    assert np.array_equal((xs[None, :] + 1j * ys[:, None]).ravel(), d["pix"])
+    n = d["pix"].size
+    Z = np.zeros((2, n), dtype=np.complex128)
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
+                      stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                      drift_m=complex(d["drift_m"]), drift_e=int(d["drift_e"]), i_dzndc=1,
+                      proj=p.kernel_params())
+    ctx.perturb_tiles(nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                                    calc_dzndc=True, bla=True), [t])
+    iter_agree(si, d["stop_iter"], frac=0.99, tol=6000)
+    same = (si == d["stop_iter"]).ravel()
+    rel_close(Z[0], d["Z"][0], 1e-6, same)
+    rel_close(Z[1], d["Z"][1], 1e-6, same)
+
+
+def test_perturb_bs_expmap_vs_reference(ctx):
+    from fractalshades_gb300 import _native as nat
+    d = load("pert_bs_expmap")
+    fl = int(d["flavor"])
+    xs = np.unique(d["pix"].real)
+    ys = np.unique(d["pix"].imag)[::-1]
+    assert np.array_equal((xs[None, :] + 1j * ys[:, None]).ravel(), d["pix"])
+    p = _expmap(3., "vertical", 2. * np.pi / 3.)     # adjust_to_zoom, vertical h axis
+    sm, se = _expmap_scale(d, 1.5)
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    ref = nat.Reference(ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
+                        flavor=fl, calc_dzndc=True, scale_m=sm, scale_e=se, bla=True, kc=kc,
+                        bla_eps=float(d["bla_eps"]))
+    n = d["pix"].size
+    Z = np.zeros((6, n))
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=d["lin_mat"], Z=Z, U=U, stop_reason=sr,
+                      stop_iter=si, ref=ref, dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+                      drift_m=float(d["driftx_m"]), drift_e=int(d["driftx_e"]),
+                      drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]),
+                      proj=p.kernel_params())
+    ctx.perturb_tiles(nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                                    flavor=fl, calc_dzndc=True, bla=True), [t])
+    iter_agree(si, d["stop_iter"], frac=0.99, tol=5000)
+    same = (si == d["stop_iter"]).ravel()
+    for k in range(6):
+        rel_close(Z[k], d["Z"][k], 1e-5, same)

@@ -296,3 +296,34 @@ def test_postproc_oracle_matches_reference(pre, model, i_orb):
         mil = ppr.normal(1, zn, dzndc=Z[2], d2zndc2=Z[3])
         np.testing.assert_allclose(mil.real, d["m2_mil_x"], rtol=0, atol=1e-15)
         np.testing.assert_allclose(mil.imag, d["m2_mil_y"], rtol=0, atol=1e-15)
+
+
+# ---------------------------------------------------------------------------
+# Expmap projection (projection.py:226-503): the oracle iterates the
+# projected pixels; the perturbation loop's derivative modifier at exit
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("key", ["h", "v"])
+def test_std_expmap_oracle_matches_reference(key):
+    from fractalshades_gb300 import projection as fsproj
+    d = load("std_expmap")
+    proj = fsproj.Expmap(hmin=0., hmax=4., orientation={"h": "horizontal", "v": "vertical"}[key])
+    proj.xy_ratio = float(d[f"{key}_xy_ratio"])
+    proj.make_impl()
+    fp = proj.f(d[f"{key}_pix"])
+    Z, si, sr = orc.std_m2(fp, -0.743643887037151 + 0.13182590420533j, d[f"{key}_lin_mat"],
+                           1e-4, 2000, 1000., 0.01)
+    assert np.array_equal(si, d[f"{key}_si"]) and np.array_equal(sr, d[f"{key}_sr"])
+    assert np.array_equal(Z.view(np.uint64), d[f"{key}_Z"].view(np.uint64))
+
+
+def test_perturb_expmap_oracle_matches_reference():
+    from fractalshades_gb300 import projection as fsproj
+    d = load("pert_m2_expmap")
+    proj = fsproj.Expmap(hmin=0., hmax=5.)
+    proj.xy_ratio = 5. / (2. * np.pi)
+    proj.make_impl()
+    kw = _pm2_inputs(d, False)
+    Z, U, sr, si = orc.perturb_m2(proj.f(d["pix"]), **kw)
+    assert np.array_equal(si, d["stop_iter"]) and np.array_equal(U, d["U"])
+    Z[-1] = Z[-1] * proj.dzndc_modifier(d["pix"])
+    assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
