@@ -108,6 +108,16 @@ class Expmap(Projection):
     def __hash__(self):
         return hash((type(self).__name__,) + tuple(self.init_kwargs.values()))
 
+    def __getstate__(self):
+        # the mapping functions are rebuilt from the parameters (the
+        # calculation fingerprint pickles the projection)
+        return {k: v for k, v in vars(self).items() if k not in ("f", "df", "dfBS")}
+
+    def __setstate__(self, state):
+        self.__dict__.update(state)
+        if hasattr(self, "xy_ratio"):
+            self.make_impl()
+
     def nh(self, fractal):
         return fractal.ny if self.premul_1j else fractal.nx
 
