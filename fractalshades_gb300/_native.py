@@ -359,14 +359,27 @@ def make_tile(*, lin_mat, Z, stop_reason, stop_iter, xs=None, ys=None, pix=None,
               drifty_m=0.0, drifty_e=0, i_dzndz=-1, i_dzndc=-1, potential=None,
               dem=None, keep=None, dzndc_scale_e=0, i_znorbit=0, proj=None):
     """Fill a Tile from numpy (host) arrays: either the axes xs / ys of a
-    rectangle or an explicit complex128 list of pixel positions ``pix``."""
+    rectangle or an explicit complex128 list of pixel positions ``pix``.
+    Inputs are taken as contiguous copies when needed (kept with the Tile);
+    outputs are written in place and must be C-contiguous of the kernels'
+    dtypes."""
     t = Tile()
     if pix is not None:
+        pix = np.ascontiguousarray(pix, dtype=np.complex128)
         t.nx, t.ny = int(pix.size), 1
         t.pix = _p(pix)
     else:
+        xs = np.ascontiguousarray(xs, dtype=np.float64)
+        ys = np.ascontiguousarray(ys, dtype=np.float64)
         t.nx, t.ny = len(xs), len(ys)
         t.xs, t.ys = _p(xs), _p(ys)
+    t._inputs = (xs, ys, pix)
+    for name, a, dts in (("Z", Z, (np.complex128, np.float64)), ("U", U, (np.int32,)),
+                         ("stop_reason", stop_reason, (np.int8,)),
+                         ("stop_iter", stop_iter, (np.int32,)),
+                         ("potential", potential, (np.float64,)), ("dem", dem, (np.float64,))):
+        if a is not None and (not a.flags.c_contiguous or a.dtype not in dts):
+            raise ValueError(f"{name}: a C-contiguous array of dtype {dts[0].__name__} is needed")
     lm = np.asarray(lin_mat, dtype=np.float64).ravel()
     for k in range(4):
         t.lin_mat[k] = lm[k]
