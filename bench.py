@@ -217,7 +217,48 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter):
                  "iter_count_differs_frac": float(np.mean(si_fe != si_64))}}
     for r in refs4:
         r.free()
+    out["host_1100_digits"] = host_leg(syn)
     return out
+
+
+def host_leg(syn):
+    """The arbitrary-precision host side (libfsghost.so on MPFR / MPC) on the
+    1e-1000 configuration's period-16607 nucleus at 1100 digits: orbit,
+    ball-method period, Newton from a seed 1e-550 away, size estimate (one
+    host thread each, the best of 3 for the orbit)."""
+    import time
+    import mpmath
+    from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
+    p, dps = 16607, 1100
+    with mpmath.workdps(dps):
+        c = syn.nucleus(p, dps)
+        prec = mpmath.mp.prec
+        sx, sy = str(c.real).encode(), str(c.imag).encode()
+        orb = np.zeros(p + 1, dtype=np.complex128)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fsFP.perturbation_mandelbrot_FP_loop(orb, True, p, 2000., sx, sy, prec)
+            ts.append(time.perf_counter() - t0)
+        t_orbit = min(ts)
+        t0 = time.perf_counter()
+        order = fsFP.perturbation_mandelbrot_ball_method(sx, sy, prec, b"1e-1000", p + 10, 1e5)
+        t_ball = time.perf_counter() - t0
+        seed = c + mpmath.mpf(10) ** -550
+        t0 = time.perf_counter()
+        ok, cn = fsFP.perturbation_mandelbrot_find_nucleus(
+            str(seed.real).encode(), str(seed.imag).encode(), prec, p, 80,
+            str(mpmath.mpf(2) ** -prec).encode(), b"1e-1000")
+        t_newton = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        fsFP.perturbation_mandelbrot_nucleus_size_estimate(sx, sy, prec, p)
+        t_size = time.perf_counter() - t0
+        newton_err = float(mpmath.log10(abs(cn - c))) if ok else None
+    return {"workload": "period-16607 nucleus at 1100 digits (3654 bits)",
+            "orbit_s": t_orbit, "orbit_it_per_s": p / t_orbit, "ball_s": t_ball,
+            "ball_order": int(order), "newton_s": t_newton, "newton_converged": bool(ok),
+            "newton_log10_err": newton_err, "size_estimate_s": t_size,
+            "arithmetic": "MPFR 4.2 / MPC 1.3, the reference's call sequence"}
 
 
 def traffic_per_launch(nx):
