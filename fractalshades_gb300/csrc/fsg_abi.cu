@@ -17,11 +17,11 @@
 #define FSG_VERSION "fractalshades_gb300 0.1.0 (sm_103a)"
 
 // launchers of fsg_ref.cu
-void fsg_build_paths_m2(const RefDev *Rd, double2 *dzndc, double2 *dzndc_xm, int *dzndc_xe,
-                        double2 *dzndz, double2 *dzndz_xm, int *dzndz_xe, int xr_mode,
+void fsg_build_paths_m2(const RefDev *Rd, int len, double2 *dzndc, double2 *dzndc_xm, int *dzndc_xe,
+                        double2 *dzndz, double2 *dzndz_xm, int *dzndz_xe, int div_iter, int xr_mode,
                         int want_dzndc, int want_dzndz, double scale_m, int scale_e,
                         cudaStream_t s);
-void fsg_build_paths_bs(const RefDev *Rd, double *dXa, double *dXb, double *dYa, double *dYb,
+void fsg_build_paths_bs(const RefDev *Rd, int len, double *dXa, double *dXb, double *dYa, double *dYb,
                         double scale, cudaStream_t s);
 void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *Mbs, double *r,
                    int stages, double kc, double eps, cudaStream_t s);
@@ -603,10 +603,11 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     // builds
     if (d->flavor == 0) {
-        fsg_build_paths_m2(r->dev, dzndc, dzndc_xm, dzndc_xe, dzndz, dzndz_xm, dzndz_xe,
-                           d->xr_paths, d->calc_dzndc, d->calc_dzndz, d->scale_m, d->scale_e, s);
+        fsg_build_paths_m2(r->dev, len, dzndc, dzndc_xm, dzndc_xe, dzndz, dzndz_xm, dzndz_xe,
+                           R.div_iter, d->xr_paths, d->calc_dzndc, d->calc_dzndz, d->scale_m,
+                           d->scale_e, s);
     } else if (d->calc_dzndc) {
-        fsg_build_paths_bs(r->dev, dXa, dXb, dYa, dYb, ldexp(d->scale_m, d->scale_e), s);
+        fsg_build_paths_bs(r->dev, len, dXa, dXb, dYa, dYb, ldexp(d->scale_m, d->scale_e), s);
     }
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
     if (d->flavor != 0) {

@@ -27,63 +27,196 @@ __device__ __forceinline__ xc orbit_xr(const RefDev &R, int i) {
     return xr_from(z);
 }
 
-__global__ void k_dzndc_m2(const RefDev *Rp, double2 *out_std, double2 *out_xm, int *out_xe,
+// The orbit fields the sequential loops read, held in registers: the loops
+// store into the paths, which the compiler cannot prove apart from the
+// descriptor, so reading them through it would reload them every step
+struct OrbitView {
+    const double2 *__restrict__ Zn;
+    const int *__restrict__ xr_slot;
+    const double2 *__restrict__ xr_m;
+    const int *__restrict__ xr_e;
+    int n_xr, nexp;
+    __device__ __forceinline__ explicit OrbitView(const RefDev &R)
+        : Zn(R.Zn), xr_slot(R.xr_slot), xr_m(R.xr_m), xr_e(R.xr_e), n_xr(R.n_xr), nexp(R.nexp) {}
+    __device__ __forceinline__ xc xr(int i) const {
+        int slot = n_xr ? xr_slot[i] : -1;
+        if (slot >= 0) return xc_make(xr_m[slot].x, xr_m[slot].y, xr_e[slot]);
+        return xr_from(Zn[i]);
+    }
+};
+
+// Sequential form (orbits up to FSG_PATH_SCAN_MIN points): one thread, the
+// reference's order, the previous value carried in registers.  The paths are
+// zero-filled by the host (cudaMemsetAsync) before the launch.
+__global__ void k_dzndc_m2(const RefDev *Rp, double2 *__restrict__ out_std,
+                           double2 *__restrict__ out_xm, int *__restrict__ out_xe,
                            int xr_mode, double scale_m, int scale_e) {
     const RefDev &R = *Rp;
-    int len = R.len;
-    int valid = len < R.div_iter ? len : R.div_iter;
-    for (int k = 0; k <= len; k++) {
-        if (xr_mode) { out_xm[k] = cx(0., 0.); out_xe[k] = 0; }
-        else out_std[k] = cx(0., 0.);
-    }
+    const OrbitView O(R);
+    const int len = R.len, order = R.order, nexp = O.nexp;
+    const int valid = len < R.div_iter ? len : R.div_iter;
     int i;
     if (xr_mode) {
+        const xc sc = xc_make(scale_m, 0., scale_e);
+        xc prev = xc_zero();
         for (i = 1; i < valid; i++) {
-            xc zx = orbit_xr(R, i - 1);
-            xc prev = xc_make(out_xm[i - 1].x, out_xm[i - 1].y, out_xe[i - 1]);
-            xc v = xr_add(xr_mul(mn_dfdz_x(R.nexp, zx), prev), xc_make(scale_m, 0., scale_e));
+            xc v = xr_add(xr_mul(mn_dfdz_x(nexp, O.xr(i - 1)), prev), sc);
             out_xm[i] = cx(v.re, v.im); out_xe[i] = v.e;
+            prev = v;
         }
         i -= 1;
-        if (i == R.order - 1) {
-            xc prev = xc_make(out_xm[i].x, out_xm[i].y, out_xe[i]);
-            xc v = xr_add(xr_mul_s(mn_dfdz(R.nexp, R.Zn[i]), prev), xc_make(scale_m, 0., scale_e));
+        if (i == order - 1) {
+            xc v = xr_add(xr_mul_s(mn_dfdz(nexp, O.Zn[i]), prev), sc);
             out_xm[0] = cx(v.re, v.im); out_xe[0] = v.e;
         }
     } else {
-        double scale = ldexp_d(scale_m, scale_e);
-        for (i = 1; i < valid; i++)
-            out_std[i] = caddr(cmul(mn_dfdz(R.nexp, R.Zn[i - 1]), out_std[i - 1]), scale);
+        const double scale = ldexp_d(scale_m, scale_e);
+        double2 prev = cx(0., 0.);
+        double2 znext = O.Zn[0];
+        for (i = 1; i < valid; i++) {
+            const double2 z = znext;
+            znext = O.Zn[i];
+            prev = caddr(cmul(mn_dfdz(nexp, z), prev), scale);
+            out_std[i] = prev;
+        }
         i -= 1;
-        if (i == R.order - 1) out_std[0] = caddr(cmul(mn_dfdz(R.nexp, R.Zn[i]), out_std[i]), scale);
+        if (i == order - 1) out_std[0] = caddr(cmul(mn_dfdz(nexp, O.Zn[i]), prev), scale);
     }
 }
 
-__global__ void k_dzndz_m2(const RefDev *Rp, double2 *out_std, double2 *out_xm, int *out_xe,
-                           int xr_mode) {
+__global__ void k_dzndz_m2(const RefDev *Rp, double2 *__restrict__ out_std,
+                           double2 *__restrict__ out_xm, int *__restrict__ out_xe, int xr_mode) {
     const RefDev &R = *Rp;
-    int len = R.len;
-    int valid = len < R.div_iter ? len : R.div_iter;
-    for (int k = 0; k <= len + 1; k++) {
-        if (xr_mode) { out_xm[k] = cx(0., 0.); out_xe[k] = 0; }
-        else out_std[k] = cx(0., 0.);
-    }
+    const OrbitView O(R);
+    const int len = R.len, nexp = O.nexp;
+    const int valid = len < R.div_iter ? len : R.div_iter;
     int i;
     if (xr_mode) {
         out_xm[1] = cx(1., 0.); out_xe[1] = 0;
+        xc prev = xc_make(1., 0., 0);
         for (i = 2; i < valid; i++) {
-            xc prev = xc_make(out_xm[i - 1].x, out_xm[i - 1].y, out_xe[i - 1]);
-            xc v = xr_mul(mn_dfdz_x(R.nexp, orbit_xr(R, i - 1)), prev);
+            xc v = xr_mul(mn_dfdz_x(nexp, O.xr(i - 1)), prev);
             out_xm[i] = cx(v.re, v.im); out_xe[i] = v.e;
+            prev = v;
         }
-        i -= 1;
+        i -= 1;          // >= 1: prev holds the path at i
+        xc v = xr_mul(mn_dfdz_x(nexp, O.xr(i)), prev);
+        out_xm[len] = cx(v.re, v.im); out_xe[len] = v.e;
+    } else {
+        out_std[1] = cx(1., 0.);
+        double2 prev = cx(1., 0.);
+        double2 znext = O.Zn[1];
+        for (i = 2; i < valid; i++) {
+            const double2 z = znext;
+            znext = O.Zn[i];
+            prev = cmul(mn_dfdz(nexp, z), prev);
+            out_std[i] = prev;
+        }
+        i -= 1;          // >= 1: prev holds the path at i
+        out_std[len] = cmul(mn_dfdz(nexp, O.Zn[i]), prev);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Chunked scan of the same recurrences for long orbits.  D_i = a_i D_{i-1}
+// + s (dZndc; s = 0 for dZndz) is affine: each chunk of FSG_PATH_CHUNK
+// indices is composed into D -> A D + B (Xrange, so no product of a chunk
+// overflows), a single thread chains the chunks to get every chunk's start
+// value, then every chunk is replayed from its start value with the
+// reference's per-step operations.  Results differ from the sequential form
+// only through the chunks' start values (a few ulps).
+// ---------------------------------------------------------------------------
+#define FSG_PATH_CHUNK 256
+
+struct PathScan {
+    int first, end;            // indices [first, end) computed by the recurrence
+    int nchunks;
+    xc *A, *B, *start;         // [nchunks]
+};
+
+// a_i = df/dz(Z_{i-1}) as an Xrange value
+__device__ __forceinline__ xc path_a(const RefDev &R, int i, int xr_mode) {
+    return xr_mode ? mn_dfdz_x(R.nexp, orbit_xr(R, i - 1)) : xr_from(mn_dfdz(R.nexp, R.Zn[i - 1]));
+}
+
+__global__ void k_path_compose(const RefDev *Rp, PathScan P, int xr_mode, int affine, xc s) {
+    const RefDev &R = *Rp;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.nchunks) return;
+    const int lo = P.first + c * FSG_PATH_CHUNK;
+    const int hi = min(lo + FSG_PATH_CHUNK, P.end);
+    xc A = xc_make(1., 0., 0), B = xc_zero();
+    for (int i = lo; i < hi; i++) {
+        const xc a = path_a(R, i, xr_mode);
+        A = xr_mul(a, A);
+        B = affine ? xr_add(xr_mul(a, B), s) : xr_mul(a, B);
+    }
+    P.A[c] = A; P.B[c] = B;
+}
+
+__global__ void k_path_prefix(PathScan P, xc d0) {
+    xc D = d0;
+    for (int c = 0; c < P.nchunks; c++) {
+        P.start[c] = D;
+        D = xr_add(xr_mul(P.A[c], D), P.B[c]);
+    }
+}
+
+__global__ void k_path_fill(const RefDev *Rp, PathScan P, int xr_mode, int affine, double scale_m,
+                            int scale_e, double2 *out_std, double2 *out_xm, int *out_xe) {
+    const RefDev &R = *Rp;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.nchunks) return;
+    const int lo = P.first + c * FSG_PATH_CHUNK;
+    const int hi = min(lo + FSG_PATH_CHUNK, P.end);
+    if (xr_mode) {
+        const xc sc = xc_make(scale_m, 0., scale_e);
+        xc prev = P.start[c];
+        for (int i = lo; i < hi; i++) {
+            const xc a = mn_dfdz_x(R.nexp, orbit_xr(R, i - 1));
+            prev = affine ? xr_add(xr_mul(a, prev), sc) : xr_mul(a, prev);
+            out_xm[i] = cx(prev.re, prev.im); out_xe[i] = prev.e;
+        }
+    } else {
+        const double scale = ldexp_d(scale_m, scale_e);
+        double2 prev = xr_to_std(P.start[c]);
+        for (int i = lo; i < hi; i++) {
+            const double2 a = mn_dfdz(R.nexp, R.Zn[i - 1]);
+            prev = affine ? caddr(cmul(a, prev), scale) : cmul(a, prev);
+            out_std[i] = prev;
+        }
+    }
+}
+
+// the wrapped values at the end of the scanned paths (sequential form's tails)
+__global__ void k_dzndc_tail(const RefDev *Rp, double2 *out_std, double2 *out_xm, int *out_xe,
+                             int xr_mode, double scale_m, int scale_e) {
+    const RefDev &R = *Rp;
+    const int valid = R.len < R.div_iter ? R.len : R.div_iter;
+    const int i = valid - 1;
+    if (i != R.order - 1) return;
+    if (xr_mode) {
+        xc prev = xc_make(out_xm[i].x, out_xm[i].y, out_xe[i]);
+        xc v = xr_add(xr_mul_s(mn_dfdz(R.nexp, R.Zn[i]), prev), xc_make(scale_m, 0., scale_e));
+        out_xm[0] = cx(v.re, v.im); out_xe[0] = v.e;
+    } else {
+        out_std[0] = caddr(cmul(mn_dfdz(R.nexp, R.Zn[i]), out_std[i]), ldexp_d(scale_m, scale_e));
+    }
+}
+
+__global__ void k_dzndz_tail(const RefDev *Rp, double2 *out_std, double2 *out_xm, int *out_xe,
+                             int xr_mode) {
+    const RefDev &R = *Rp;
+    const int len = R.len;
+    const int valid = len < R.div_iter ? len : R.div_iter;
+    const int i = valid - 1 > 1 ? valid - 1 : 1;
+    if (xr_mode) {
+        out_xm[1] = cx(1., 0.); out_xe[1] = 0;
         xc prev = xc_make(out_xm[i].x, out_xm[i].y, out_xe[i]);
         xc v = xr_mul(mn_dfdz_x(R.nexp, orbit_xr(R, i)), prev);
         out_xm[len] = cx(v.re, v.im); out_xe[len] = v.e;
     } else {
         out_std[1] = cx(1., 0.);
-        for (i = 2; i < valid; i++) out_std[i] = cmul(mn_dfdz(R.nexp, R.Zn[i - 1]), out_std[i - 1]);
-        i -= 1;
         out_std[len] = cmul(mn_dfdz(R.nexp, R.Zn[i]), out_std[i]);
     }
 }
@@ -101,25 +234,27 @@ __device__ __forceinline__ void bs_dfdxy(int flavor, double x, double y, double 
            fyx = 2. * sgnr(x) * fabs(y); fyy = 2. * sgnr(y) * fabs(x); }
 }
 
-__global__ void k_dzndc_bs(const RefDev *Rp, double *dXa, double *dXb, double *dYa, double *dYb,
-                           double scale) {
+__global__ void k_dzndc_bs(const RefDev *Rp, double *__restrict__ dXa, double *__restrict__ dXb,
+                           double *__restrict__ dYa, double *__restrict__ dYb, double scale) {
     const RefDev &R = *Rp;
-    int len = R.len;
-    int valid = len < R.div_iter ? len : R.div_iter;
-    for (int k = 0; k <= len; k++) { dXa[k] = 0.; dXb[k] = 0.; dYa[k] = 0.; dYb[k] = 0.; }
+    const double2 *__restrict__ Zn = R.Zn;
+    const int len = R.len, flavor = R.flavor, order = R.order;
+    const int valid = len < R.div_iter ? len : R.div_iter;
+    double a = 0., b = 0., c = 0., d = 0.;       // the Jacobian at index i - 1 (zero-filled path)
     for (int i = 1; i <= valid; i++) {
         int from = i - 1, to = i;
         if (i == valid) {
-            if (!(from == R.order - 1)) break;
+            if (!(from == order - 1)) break;
             to = 0;
         }
         double fxx, fxy, fyx, fyy;
-        bs_dfdxy(R.flavor, R.Zn[from].x, R.Zn[from].y, fxx, fxy, fyx, fyy);
-        double a = dXa[from], b = dXb[from], c = dYa[from], d = dYb[from];
-        dXa[to] = fxx * a + fxy * c + scale;
-        dXb[to] = fxx * b + fxy * d;
-        dYa[to] = fyx * a + fyy * c;
-        dYb[to] = fyx * b + fyy * d - scale;
+        bs_dfdxy(flavor, Zn[from].x, Zn[from].y, fxx, fxy, fyx, fyy);
+        const double na = fxx * a + fxy * c + scale;
+        const double nb = fxx * b + fxy * d;
+        const double nc = fyx * a + fyy * c;
+        const double nd = fyx * b + fyy * d - scale;
+        dXa[to] = na; dXb[to] = nb; dYa[to] = nc; dYb[to] = nd;
+        a = na; b = nb; c = nc; d = nd;
     }
 }
 
@@ -371,18 +506,78 @@ void fsg_build_bs_fr_bla(const double *Mbs, int bla_len, int4 *blaf, cudaStream_
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the C-ABI layer)
 // ---------------------------------------------------------------------------
-void fsg_build_paths_m2(const RefDev *Rd, double2 *dzndc, double2 *dzndc_xm, int *dzndc_xe,
-                        double2 *dzndz, double2 *dzndz_xm, int *dzndz_xe, int xr_mode,
-                        int want_dzndc, int want_dzndz, double scale_m, int scale_e,
-                        cudaStream_t s) {
-    if (want_dzndc) k_dzndc_m2<<<1, 1, 0, s>>>(Rd, dzndc, dzndc_xm, dzndc_xe, xr_mode, scale_m, scale_e);
-    if (want_dzndz) k_dzndz_m2<<<1, 1, 0, s>>>(Rd, dzndz, dzndz_xm, dzndz_xe, xr_mode);
+#define FSG_PATH_SCAN_MIN 65536
+
+static xc xc_host(double re, double im, int e) {
+    xc v;
+    v.re = re; v.im = im; v.e = e;
+    return v;
 }
 
-void fsg_build_paths_bs(const RefDev *Rd, double *dXa, double *dXb, double *dYa, double *dYb,
+static void build_path_scan(const RefDev *Rd, int len, int first, int end, int xr_mode, int affine,
+                            double scale_m, int scale_e, xc d0, double2 *out_std, double2 *out_xm,
+                            int *out_xe, cudaStream_t s) {
+    PathScan P;
+    P.first = first; P.end = end;
+    P.nchunks = end > first ? (end - first + FSG_PATH_CHUNK - 1) / FSG_PATH_CHUNK : 0;
+    if (P.nchunks == 0) return;
+    xc *buf = nullptr;
+    if (cudaMallocAsync((void **)&buf, 3 * sizeof(xc) * (size_t)P.nchunks, s) != cudaSuccess) return;
+    P.A = buf; P.B = buf + P.nchunks; P.start = buf + 2 * P.nchunks;
+    const int tb = 128, nb = (P.nchunks + tb - 1) / tb;
+    const xc sc = xc_host(scale_m, 0., scale_e);
+    k_path_compose<<<nb, tb, 0, s>>>(Rd, P, xr_mode, affine, sc);
+    k_path_prefix<<<1, 1, 0, s>>>(P, d0);
+    k_path_fill<<<nb, tb, 0, s>>>(Rd, P, xr_mode, affine, scale_m, scale_e, out_std, out_xm, out_xe);
+    cudaFreeAsync(buf, s);
+}
+
+// Derivative paths (numba_dZndc_path, numba_dZndz_path): zero-filled, then
+// the recurrence -- sequential in the reference's order up to
+// FSG_PATH_SCAN_MIN points, chunked scan above
+void fsg_build_paths_m2(const RefDev *Rd, int len, double2 *dzndc, double2 *dzndc_xm, int *dzndc_xe,
+                        double2 *dzndz, double2 *dzndz_xm, int *dzndz_xe, int div_iter, int xr_mode,
+                        int want_dzndc, int want_dzndz, double scale_m, int scale_e,
+                        cudaStream_t s) {
+    const int valid = len < div_iter ? len : div_iter;
+    const bool scan = len > FSG_PATH_SCAN_MIN;
+    if (want_dzndc) {
+        if (xr_mode) {
+            cudaMemsetAsync(dzndc_xm, 0, 16 * (size_t)(len + 1), s);
+            cudaMemsetAsync(dzndc_xe, 0, 4 * (size_t)(len + 1), s);
+        } else {
+            cudaMemsetAsync(dzndc, 0, 16 * (size_t)(len + 1), s);
+        }
+        if (!scan) {
+            k_dzndc_m2<<<1, 1, 0, s>>>(Rd, dzndc, dzndc_xm, dzndc_xe, xr_mode, scale_m, scale_e);
+        } else {
+            build_path_scan(Rd, len, 1, valid, xr_mode, 1, scale_m, scale_e, xc_host(0., 0., 0), dzndc,
+                            dzndc_xm, dzndc_xe, s);
+            k_dzndc_tail<<<1, 1, 0, s>>>(Rd, dzndc, dzndc_xm, dzndc_xe, xr_mode, scale_m, scale_e);
+        }
+    }
+    if (want_dzndz) {
+        if (xr_mode) {
+            cudaMemsetAsync(dzndz_xm, 0, 16 * (size_t)(len + 2), s);
+            cudaMemsetAsync(dzndz_xe, 0, 4 * (size_t)(len + 2), s);
+        } else {
+            cudaMemsetAsync(dzndz, 0, 16 * (size_t)(len + 2), s);
+        }
+        if (!scan) {
+            k_dzndz_m2<<<1, 1, 0, s>>>(Rd, dzndz, dzndz_xm, dzndz_xe, xr_mode);
+        } else {
+            build_path_scan(Rd, len, 2, valid, xr_mode, 0, 0., 0, xc_host(1., 0., 0), dzndz,
+                            dzndz_xm, dzndz_xe, s);
+            k_dzndz_tail<<<1, 1, 0, s>>>(Rd, dzndz, dzndz_xm, dzndz_xe, xr_mode);
+        }
+    }
+}
+void fsg_build_paths_bs(const RefDev *Rd, int len, double *dXa, double *dXb, double *dYa, double *dYb,
                         double scale, cudaStream_t s) {
+    for (double *p : {dXa, dXb, dYa, dYb}) cudaMemsetAsync(p, 0, 8 * (size_t)(len + 1), s);
     k_dzndc_bs<<<1, 1, 0, s>>>(Rd, dXa, dXb, dYa, dYb, scale);
 }
+
 
 void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *Mbs, double *r,
                    int stages, double kc, double eps, cudaStream_t s) {

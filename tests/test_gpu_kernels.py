@@ -656,3 +656,34 @@ def test_perturb_bs_expmap_vs_reference(ctx):
     same = (si == d["stop_iter"]).ravel()
     for k in range(6):
         rel_close(Z[k], d["Z"][k], 1e-5, same)
+
+
+@pytest.mark.parametrize("xr", [False, True])
+def test_long_orbit_paths_scan_vs_oracle(ctx, xr):
+    """Orbits above 65,536 points: the derivative paths come from the chunked
+    scan (chunk composites, their prefix, then each chunk replayed in the
+    reference's order); they agree with the oracle's sequential paths to
+    1e-11 relative."""
+    from fractalshades_gb300 import _native as nat
+    rng = np.random.default_rng(7)
+    n = 150_000
+    r = 0.6 * np.sqrt(rng.random(n))
+    Zn = r * np.exp(2j * np.pi * rng.random(n))
+    Zn[0] = 0.
+    ref = nat.Reference(ctx, Zn, div_iter=n, order=None, xr_paths=xr, calc_dzndc=True,
+                        calc_dzndz=True, scale_m=0.5, scale_e=-30, bla=False)
+    dzo = orc.dzndc_path_m2(Zn, n, 1 << 62, xr, 0.5, -30, None, None, None)
+    dzzo = orc.dzndz_path_m2(Zn, n, xr, None, None, None)
+    dz = ref.download("dzndc")
+    dzz = ref.download("dzndz")
+    if xr:
+        for got, exp in ((dz, dzo), (dzz, dzzo)):
+            a = got[0] * np.exp2(got[1].astype(np.float64) - exp[1])
+            ok = np.abs(exp[0]) > 0
+            np.testing.assert_allclose(a[ok], exp[0][ok], rtol=1e-11, atol=0)
+            assert np.all(got[0][~ok] == 0)
+    else:
+        np.testing.assert_allclose(dz, dzo, rtol=1e-11, atol=1e-300)
+        big = np.abs(dzzo) > 1e-250
+        np.testing.assert_allclose(dzz[big], dzzo[big], rtol=1e-11, atol=0)
+        assert np.all(np.abs(dzz[~big]) < 1e-240)
