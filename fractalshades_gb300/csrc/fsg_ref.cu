@@ -45,7 +45,7 @@ struct OrbitView {
     }
 };
 
-// Sequential form (orbits up to FSG_PATH_SCAN_MIN points): one thread, the
+// Sequential form (orbits up to FSG_PATH_SCAN_MIN = 8192 points): one thread, the
 // reference's order, the previous value carried in registers.  The paths are
 // zero-filled by the host (cudaMemsetAsync) before the launch.
 __global__ void k_dzndc_m2(const RefDev *Rp, double2 *__restrict__ out_std,
@@ -506,7 +506,7 @@ void fsg_build_bs_fr_bla(const double *Mbs, int bla_len, int4 *blaf, cudaStream_
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the C-ABI layer)
 // ---------------------------------------------------------------------------
-#define FSG_PATH_SCAN_MIN 65536
+#define FSG_PATH_SCAN_MIN 8192
 
 static xc xc_host(double re, double im, int e) {
     xc v;

@@ -660,7 +660,7 @@ def test_perturb_bs_expmap_vs_reference(ctx):
 
 @pytest.mark.parametrize("xr", [False, True])
 def test_long_orbit_paths_scan_vs_oracle(ctx, xr):
-    """Orbits above 65,536 points: the derivative paths come from the chunked
+    """Orbits above 8,192 points: the derivative paths come from the chunked
     scan (chunk composites, their prefix, then each chunk replayed in the
     reference's order); they agree with the oracle's sequential paths to
     1e-11 relative."""
