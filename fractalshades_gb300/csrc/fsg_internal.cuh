@@ -142,6 +142,12 @@ __device__ __forceinline__ bool fsg_claim(const WorkDev &W, const long long *s_s
     return true;
 }
 
+// the host's interruption flag: sets the launch status and stops claiming
+__device__ __forceinline__ bool fsg_cancelled(const WorkDev &W) {
+    if (*W.cancel) { *W.status = 1; return true; }
+    return false;
+}
+
 __device__ __forceinline__ void fsg_load_starts(const WorkDev &W, long long *s_start) {
     for (int i = threadIdx.x; i <= W.ntiles; i += blockDim.x) s_start[i] = W.start[i];
     __syncthreads();

@@ -29,7 +29,8 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
     const int bs = OPT ? C.backshift : 0;
     const bool d2_on = OPT && C.d2;
     int t; long long ip;
-    while (fsg_claim(W, s_start, t, ip)) {
+    // the interruption flag, polled per pixel like numba_cycles (core.py:2959-2960)
+    while (!fsg_cancelled(W) && fsg_claim(W, s_start, t, ip)) {
         const TileDev &T = W.tiles[t];
         long long np = (long long)T.nx * T.ny;
         double2 c = std_c(T, ip);
@@ -80,7 +81,8 @@ __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
     const int bs = OPT ? C.backshift : 0;
     const bool d2_on = OPT && C.d2;
     int t; long long ip;
-    while (fsg_claim(W, s_start, t, ip)) {
+    // the interruption flag, polled per pixel like numba_cycles (core.py:2959-2960)
+    while (!fsg_cancelled(W) && fsg_claim(W, s_start, t, ip)) {
         const TileDev &T = W.tiles[t];
         long long np = (long long)T.nx * T.ny;
         double2 c = std_c(T, ip);
@@ -140,7 +142,8 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
     const int flavor = C.flavor;
     const int bs = OPT ? C.backshift : 0;
     int t; long long ip;
-    while (fsg_claim(W, s_start, t, ip)) {
+    // the interruption flag, polled per pixel like numba_cycles (core.py:2959-2960)
+    while (!fsg_cancelled(W) && fsg_claim(W, s_start, t, ip)) {
         const TileDev &T = W.tiles[t];
         long long np = (long long)T.nx * T.ny;
         double2 c = std_c(T, ip);

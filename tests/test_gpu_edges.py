@@ -1,0 +1,164 @@
+"""
+Edge cases of the C-ABI and the kernels on the GPU: ragged and degenerate
+tiles, more tiles than one launch takes, max_iter at its smallest,
+first-iteration escapes, a period-1 reference, interruption, and the
+refusals of malformed input (which never reach a kernel).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+LIN = np.array([[1., -0.], [0., 1.]])
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from fractalshades_gb300 import _native as nat
+    c = nat.Context(0)
+    yield c
+    c.close()
+
+
+def _std_tile(nat, xs, ys, center=-0.5 + 0j, dx=3.0, nZ=3):
+    n = len(xs) * len(ys)
+    Z = np.zeros((nZ, n), dtype=np.complex128)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=LIN, Z=Z, stop_reason=sr, stop_iter=si,
+                      center=center, dx=dx)
+    return t, (Z, sr, si)
+
+
+def _check_std(xs, ys, out, max_iter, center=-0.5 + 0j, dx=3.0):
+    pix = (np.asarray(xs)[None, :] + 1j * np.asarray(ys)[:, None]).ravel()
+    Zo, sio, sro = orc.std_m2(pix, center, LIN, dx, max_iter, 1000., 0.01)
+    Z, sr, si = out
+    assert np.array_equal(si, sio) and np.array_equal(sr, sro)
+    assert np.array_equal(Z.view(np.uint64), Zo.view(np.uint64))
+
+
+def test_ragged_and_many_tiles(ctx):
+    """1x1, 1xn, nx1, 3x7 and a 64x48 tile mixed, then 1500 tiles in one
+    call (split into launches of at most 1024 tiles): bit-exact against the
+    oracle."""
+    from fractalshades_gb300 import _native as nat
+    rng = np.random.default_rng(0)
+    shapes = [(1, 1), (1, 17), (13, 1), (3, 7), (64, 48)] + [(1 + rng.integers(4), 1 + rng.integers(4))
+                                                            for _ in range(1495)]
+    tiles, outs, axes = [], [], []
+    for nx, ny in shapes:
+        xs = rng.random(nx) - 0.5
+        ys = rng.random(ny) - 0.5
+        t, out = _std_tile(nat, xs, ys)
+        tiles.append(t); outs.append(out); axes.append((xs, ys))
+    calc = nat.make_calc(max_iter=300, M_divergence=1000., epsilon_stationnary=0.01)
+    ctx.std_tiles(calc, tiles)
+    for (xs, ys), out in zip(axes, outs):
+        _check_std(xs, ys, out, 300)
+
+
+@pytest.mark.parametrize("max_iter", [1, 2, 3])
+def test_smallest_max_iter(ctx, max_iter):
+    """The standard loop never updates at n = max_iter (mandelbrot_M2.py:
+    312-314): max_iter 1 leaves Z at 0 with stop_iter 1."""
+    from fractalshades_gb300 import _native as nat
+    xs = np.linspace(-0.5, 0.5, 9)
+    ys = np.linspace(-0.5, 0.5, 7)
+    t, out = _std_tile(nat, xs, ys)
+    ctx.std_tiles(nat.make_calc(max_iter=max_iter, M_divergence=1000.,
+                                epsilon_stationnary=0.01), [t])
+    _check_std(xs, ys, out, max_iter)
+    if max_iter == 1:
+        assert np.all(out[2] == 1) and np.all(out[0] == 0)
+
+
+def test_first_iteration_escape(ctx):
+    """|c| beyond M escapes at n = 1."""
+    from fractalshades_gb300 import _native as nat
+    xs = np.linspace(-0.5, 0.5, 5)
+    ys = np.linspace(-0.5, 0.5, 5)
+    t, out = _std_tile(nat, xs, ys, center=5000. + 0j, dx=10.)
+    ctx.std_tiles(nat.make_calc(max_iter=100, M_divergence=1000., epsilon_stationnary=0.01), [t])
+    _check_std(xs, ys, out, 100, center=5000. + 0j, dx=10.)
+    assert np.all(out[2] == 1) and np.all(out[1] == 1)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "xr64", "fe32"])
+def test_period_one_reference(ctx, mode):
+    """The reference orbit of c = 0 is 0 forever (order 1): every step is a
+    wrap and a rebase; counts as the oracle's."""
+    from fractalshades_gb300 import _native as nat
+    Zn = np.zeros(2, dtype=np.complex128)
+    xr = mode == "xr64"
+    ref = nat.Reference(ctx, Zn, div_iter=1001, order=1, xr_paths=xr, calc_dzndc=True,
+                        scale_m=0.5, scale_e=-6, bla=False)
+    nx = 16
+    xs = np.linspace(-0.5, 0.5, nx)
+    ys = np.linspace(-0.5, 0.5, nx)
+    n = nx * nx
+    Z = np.zeros((2, n), dtype=np.complex128)
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=LIN, Z=Z, U=U, stop_reason=sr, stop_iter=si,
+                      ref=ref, dx_m=0.5, dx_e=3, drift_m=0j, drift_e=0, i_dzndc=1)
+    ctx.perturb_tiles(nat.make_calc(max_iter=1000, M_divergence=1000., mode=mode,
+                                    calc_dzndc=True, bla=False, xr_semantics=xr), [t])
+    pix = (xs[None, :] + 1j * ys[:, None]).ravel()
+    dz = orc.dzndc_path_m2(Zn, 1001, 1, xr, 0.5, -6)
+    Zo, Uo, sro, sio = orc.perturb_m2(pix, Zn=Zn, ref_div_iter=1001, ref_order=1, lin_mat=LIN,
+                                      dx_m=0.5, dx_e=3, drift_m=0j, drift_e=0, max_iter=1000,
+                                      M=1000., eps_stat=0., xr_mode=xr, dZndc=dz)
+    assert np.mean(si == sio) >= (1.0 if mode != "fe32" else 0.99)
+    assert np.array_equal(sr, sro) or mode == "fe32"
+
+
+def test_cancel_interrupts_every_loop(ctx):
+    """fsg_cancel before a launch: the kernels claim no pixel and the call
+    returns FSG_INTERRUPTED (core.py:2959-2960, perturbation.py:1042); after
+    fsg_clear_cancel the same call completes."""
+    from fractalshades_gb300 import _native as nat
+    xs = np.linspace(-0.5, 0.5, 32)
+    ys = np.linspace(-0.5, 0.5, 32)
+    t, out = _std_tile(nat, xs, ys)
+    calc = nat.make_calc(max_iter=300, M_divergence=1000., epsilon_stationnary=0.01)
+    ctx.cancel()
+    try:
+        assert ctx.std_tiles(calc, [t]) == nat.FSG_INTERRUPTED
+        assert np.all(out[2] == 0)          # nothing computed
+    finally:
+        ctx.clear_cancel()
+    assert ctx.std_tiles(calc, [t]) == nat.FSG_OK
+    _check_std(xs, ys, out, 300)
+
+
+def test_malformed_input_is_refused(ctx):
+    """Errors, not launches: zero-sized or pointer-less tiles, nZ too small,
+    a perturbation tile without reference, max_iter out of range."""
+    from fractalshades_gb300 import _native as nat
+    xs = np.linspace(-0.5, 0.5, 4)
+    ys = np.linspace(-0.5, 0.5, 4)
+    calc = nat.make_calc(max_iter=10, M_divergence=1000.)
+    t, out = _std_tile(nat, xs, ys, nZ=2)
+    with pytest.raises(RuntimeError):
+        ctx.std_tiles(calc, [t])                       # nZ < 3
+    t, out = _std_tile(nat, xs, ys)
+    t.nx = 0
+    with pytest.raises(RuntimeError):
+        ctx.std_tiles(calc, [t])                       # empty tile
+    t, out = _std_tile(nat, xs, ys)
+    t.Z = None
+    with pytest.raises(RuntimeError):
+        ctx.std_tiles(calc, [t])                       # no output
+    t, out = _std_tile(nat, xs, ys)
+    with pytest.raises(RuntimeError):
+        ctx.perturb_tiles(calc, [t])                   # no reference
+    with pytest.raises(RuntimeError):
+        ctx.std_tiles(nat.make_calc(max_iter=0, M_divergence=1000.), [t])
+    with pytest.raises(RuntimeError):
+        ctx.std_tiles(nat.make_calc(max_iter=2 ** 31 - 1, M_divergence=1000.), [t])
+    with pytest.raises(RuntimeError):
+        ctx.std_tiles(calc, [])                        # no tiles
