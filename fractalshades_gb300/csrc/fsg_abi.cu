@@ -352,6 +352,10 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     }
     rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
     if (rc != FSG_OK) return rc;
+    // an interrupted launch leaves the caller's arrays untouched (the
+    // reference discards an interrupted tile, core.py:2545-2547)
+    rc = fsg_sync(ctx);
+    if (rc != FSG_OK) return rc;
     for (int32_t i = 0; i < ntiles; i++) {
         const fsg_tile &t = tiles[i];
         const TileDev &d = td[i];
