@@ -37,7 +37,8 @@ void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla,
                       cudaStream_t s);
 void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
                      const double *dYa, const double *dYb, int4 *hf, cudaStream_t s);
-void fsg_build_bs_fr_bla(const double *Mbs, int bla_len, int4 *blaf, cudaStream_t s);
+void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int4 *blaf,
+                         int2 *rf, cudaStream_t s);
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
@@ -597,12 +598,16 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     R.bla_first = bla_first; R.bla_first_step = bla_first_step; R.bla_nit = bla_nit;
     // FP32+exp tables (Burning Ship)
     int4 *bs_Zf = nullptr, *bs_hf = nullptr, *bs_blaf = nullptr;
+    int2 *bs_rf = nullptr;
     if (d->flavor != 0) {
         RA(bs_Zf, len + 1);
         if (d->calc_dzndc) RA(bs_hf, 2 * (size_t)(len + 1));
-        if (R.bla_len > 0) RA(bs_blaf, 4 * (size_t)R.bla_len);
+        if (R.bla_len > 0) {
+            RA(bs_blaf, 4 * (size_t)R.bla_len);
+            RA(bs_rf, (size_t)R.bla_len);
+        }
     }
-    R.bs_Zf = bs_Zf; R.bs_hf = bs_hf; R.bs_blaf = bs_blaf;
+    R.bs_Zf = bs_Zf; R.bs_hf = bs_hf; R.bs_blaf = bs_blaf; R.bs_rf = bs_rf;
     RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     // builds
@@ -616,7 +621,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
     if (d->flavor != 0) {
         fsg_build_bs_fr(r->dev, len, bs_Zf, dXa, dXb, dYa, dYb, bs_hf, s);
-        fsg_build_bs_fr_bla(Mbs, R.bla_len, bs_blaf, s);
+        fsg_build_bs_fr_bla(Mbs, rbla, R.bla_len, bs_blaf, bs_rf, s);
     }
     if (fe_tables) {
         fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
@@ -683,8 +688,12 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
         }
     }
     int4 *bs_blaf = nullptr;
-    if (R.flavor != 0 && R.bla_len > 0) RA(bs_blaf, 4 * (size_t)R.bla_len);
-    R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.bs_blaf = bs_blaf;
+    int2 *bs_rf = nullptr;
+    if (R.flavor != 0 && R.bla_len > 0) {
+        RA(bs_blaf, 4 * (size_t)R.bla_len);
+        RA(bs_rf, (size_t)R.bla_len);
+    }
+    R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.bs_blaf = bs_blaf; R.bs_rf = bs_rf;
     R.bla_f = bla_f; R.bla_first = bla_first; R.bla_first_step = bla_first_step;
     RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
@@ -694,7 +703,7 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
             fsg_build_fe_bla(r->dev, Mbla, rbla, R.bla_len, bla_f, R.bla_nit, bla_first,
                              bla_first_step, s);
         else if (R.flavor != 0)
-            fsg_build_bs_fr_bla(Mbs, R.bla_len, bs_blaf, s);
+            fsg_build_bs_fr_bla(Mbs, rbla, R.bla_len, bs_blaf, bs_rf, s);
     }
     RCK(cudaGetLastError(), "BLA kernels");
     // no host wait: launches and downloads that use r wait for this event

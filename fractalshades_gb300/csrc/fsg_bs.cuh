@@ -42,11 +42,15 @@ struct fr { float m; int e; };
 #define FR_ZERO_E (-(1 << 29))
 
 FSG_DEV fr fr_zero() { fr r; r.m = 0.f; r.e = FR_ZERO_E; return r; }
-// normalise m * 2^e for |m| < 2^126 (0 and subnormal mantissas give 0)
+// normalise m * 2^e for finite m (0 and subnormal mantissas give 0): the
+// biased exponent of m moves to e and m's own is set to 0 (bit operations)
 FSG_DEV fr fr_norm(float m, int e) {
-    const int b = (__float_as_int(m) >> 23) & 0xff;
-    if (b == 0) return fr_zero();
-    fr r; r.m = m * __int_as_float((254 - b) << 23); r.e = e + (b - 127);
+    const int bits = __float_as_int(m);
+    const int b = (bits >> 23) & 0xff;
+    fr r;
+    r.m = __int_as_float((bits & 0x807fffff) | 0x3f800000);
+    r.e = e + (b - 127);
+    if (b == 0) r = fr_zero();
     return r;
 }
 FSG_DEV fr fr_from_d(double x) {
@@ -62,25 +66,36 @@ FSG_DEV fr fr_from_d(double x) {
     return fr_norm((float)m, be - 1023);
 }
 FSG_DEV double fr_to_d(fr a) { return a.m == 0.f ? 0. : ldexp_d((double)a.m, a.e); }
-// 2^k for k in [-60, 0]
-FSG_DEV float fr_p2(int k) { return __int_as_float((k + 127) << 23); }
+// 2^-d for d >= 0 (0 from d = 127 on)
+FSG_DEV float fr_p2n(int d) { return __int_as_float((127 - min(d, 127)) << 23); }
 
+// Branch-free: the operand of larger exponent (a zero has the smallest) takes
+// the other scaled by 2^-d in one FMA.  From d = 61 on the scaled term is
+// below half an ulp and the sum is the larger operand itself.
 FSG_DEV fr operator+(fr a, fr b) {
-    if (a.m == 0.f) return b;
-    if (b.m == 0.f) return a;
-    const int d = a.e - b.e;
-    if (d >= 0) return d > 60 ? a : fr_norm(fmaf(b.m, fr_p2(-d), a.m), a.e);
-    return d < -60 ? b : fr_norm(fmaf(a.m, fr_p2(d), b.m), b.e);
+    const bool ge = a.e >= b.e;
+    const float mb = ge ? a.m : b.m, ms = ge ? b.m : a.m;
+    const int eb = ge ? a.e : b.e, d = ge ? a.e - b.e : b.e - a.e;
+    return fr_norm(fmaf(ms, fr_p2n(d), mb), eb);
 }
 FSG_DEV fr operator-(fr a) { a.m = -a.m; return a; }
 FSG_DEV fr operator-(fr a, fr b) { return a + (-b); }
 FSG_DEV fr operator*(fr a, fr b) {
-    if (a.m == 0.f || b.m == 0.f) return fr_zero();
-    fr r; r.m = a.m * b.m; r.e = a.e + b.e;              // |m| in [1, 4)
+    fr r; r.m = a.m * b.m; r.e = a.e + b.e;              // |m| in [1, 4) or 0
     if (fabsf(r.m) >= 2.f) { r.m *= 0.5f; r.e += 1; }
+    if (r.m == 0.f) r = fr_zero();
     return r;
 }
-FSG_DEV fr operator*(double s, fr b) { return fr_from_d(s) * b; }
+// product by a literal constant (the closures' 2. * x): FP32 only, exact for
+// the powers of two the loop uses
+FSG_DEV fr operator*(double s, fr b) {
+    if (s == 2. || s == -2.) {
+        if (b.m != 0.f) b.e += 1;
+        if (s < 0.) b.m = -b.m;
+        return b;
+    }
+    return fr_norm((float)s * b.m, b.e);
+}
 FSG_DEV fr &operator+=(fr &a, fr b) { a = a + b; return a; }
 
 // the operations the loop needs, for both real types
@@ -89,6 +104,10 @@ FSG_DEV double to_d(fr x) { return fr_to_d(x); }
 template <class T> FSG_DEV T from_d(double x);
 template <> FSG_DEV double from_d<double>(double x) { return x; }
 template <> FSG_DEV fr from_d<fr>(double x) { return fr_from_d(x); }
+// a literal constant (0, +-1, +-2) of the loop's real type, without FP64
+template <class T> FSG_DEV T cst(float x);
+template <> FSG_DEV double cst<double>(float x) { return (double)x; }
+template <> FSG_DEV fr cst<fr>(float x) { return fr_norm(x, 0); }
 // m * 2^e from a mantissa and an exponent (the Xrange form of c)
 template <class T> FSG_DEV T from_me(double m, int e);
 template <> FSG_DEV double from_me<double>(double m, int e) { return ldexp_d(m, e); }
@@ -113,6 +132,82 @@ FSG_DEV bool abs_le(fr a, fr b) {
     if (b.m == 0.f) return false;
     return a.e != b.e ? a.e < b.e : fabsf(a.m) <= fabsf(b.m);
 }
+
+// |(x, y)| as s * 2^e, s in [1, 2 sqrt 2], in FP32 (z = false: (0, 0))
+struct fr_mod { float s; int e; bool z; };
+FSG_DEV fr_mod fr_modulus2(fr x, fr y, bool squared) {
+    const int e = max(x.e, y.e);
+    const float mx = x.m * fr_p2n(e - x.e), my = y.m * fr_p2n(e - y.e);
+    const float q = fmaf(mx, mx, my * my);
+    fr_mod r; r.s = squared ? q : sqrtf(q); r.e = squared ? 2 * e : e;
+    r.z = x.m == 0.f && y.m == 0.f;
+    return r;
+}
+// v * 2^d as a float, d in [-3, 0]
+FSG_DEV float fr_scale_small(float v, int d) { return v * __int_as_float((127 + d) << 23); }
+
+// The escape test |z|^2 > M2 of the loop (perturbation.py:1636-1639) with z in
+// fr: decided in FP32 unless within 2^-18 of the bound, where the double form
+// of the reference decides (so that the outcome is the FP64 one of the same
+// fr values).
+FSG_DEV bool fr_escaped(fr X, fr Y, fr M2f, double M2) {
+    const fr_mod q = fr_modulus2(X, Y, true);           // s in [1, 8)
+    if (q.z) return 0. > M2;
+    const int d = q.e - M2f.e;
+    if (d >= 1) return true;                            // >= 2 > M2 mantissa
+    if (d <= -4) return false;                          // < 0.5
+    const float t = fr_scale_small(q.s, d);
+    if (fabsf(t - M2f.m) > M2f.m * 0x1p-18f) return t > M2f.m;
+    const double Xd = fr_to_d(X), Yd = fr_to_d(Y);
+    return Xd * Xd + Yd * Yd > M2;
+}
+
+// |dz| < r for a BLA radius r (double r, its fr copy rm * 2^re), the
+// comparison of ref_BLA_get (perturbation.py:2116-2170) in FP32 unless within
+// 2^-18 of r, where the double form decides.
+FSG_DEV bool fr_below(const fr_mod &a, fr xn, fr yn, float rm, int re, double r) {
+    if (rm == 0.f) return false;
+    if (a.z) return 0. < r;
+    const int d = a.e - re;
+    if (d >= 1) return false;                           // >= 2 > rm
+    if (d <= -2) return true;                           // < 0.71 < rm
+    const float t = fr_scale_small(a.s, d);
+    if (fabsf(t - rm) > rm * 0x1p-18f) return t < rm;
+    return hypot(fr_to_d(xn), fr_to_d(yn)) < r;
+}
+
+// ref_BLA_get in the loop's real type: double |dz| against the double radii,
+// or the FP32 modulus against their fr copies
+template <class T> struct BLAGet;
+template <> struct BLAGet<double> {
+    static FSG_DEV int get(const RefDev &R, double xn, double yn, int w, int &ib) {
+        return bla_lookup(R, hypot(xn, yn), w, ib);
+    }
+};
+template <> struct BLAGet<fr> {
+    static FSG_DEV int get(const RefDev &R, fr xn, fr yn, int w, int &ib) {
+        int it = w >> FSG_STG_COMPRESSED;
+        int stages = FSG_STG_COMPRESSED;
+        for (int s = FSG_STG_COMPRESSED; s < R.stages; s++) {
+            stages = s;
+            if (it & 1) break;
+            it >>= 1;
+        }
+        const fr_mod a = fr_modulus2(xn, yn, false);
+        const int invalid_step = R.first_invalid - w;
+        for (int stg = stages; stg >= FSG_STG_COMPRESSED; stg--) {
+            const int step = 1 << stg;
+            if (step >= invalid_step) continue;
+            const int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
+            const int2 rf = __ldg(&R.bs_rf[idx]);
+            if (fr_below(a, xn, yn, __int_as_float(rf.x), rf.y, __ldg(&R.rbla[idx]))) {
+                ib = idx;
+                return step;
+            }
+        }
+        return 0;
+    }
+};
 
 // v * 2^k (k = 0: v)
 FSG_DEV double scale2(double v, int k) { return k == 0 ? v : ldexp_d(v, k); }
@@ -158,12 +253,12 @@ template <class T> FSG_DEV T diffabs(T X, T x) {
     else { if (le0(X + x)) return -x; else return (2. * X + x); }
 }
 template <class T> FSG_DEV T ddiffabsdX(T X, T x) {
-    if (ge0(X)) { if (ge0(X + x)) return from_d<T>(0.); else return from_d<T>(-2.); }
-    else { if (le0(X + x)) return from_d<T>(0.); else return from_d<T>(2.); }
+    if (ge0(X)) { if (ge0(X + x)) return cst<T>(0.f); else return cst<T>(-2.f); }
+    else { if (le0(X + x)) return cst<T>(0.f); else return cst<T>(2.f); }
 }
 template <class T> FSG_DEV T ddiffabsdx(T X, T x) {
-    if (ge0(X)) { if (ge0(X + x)) return from_d<T>(1.); else return from_d<T>(-1.); }
-    else { if (le0(X + x)) return from_d<T>(-1.); else return from_d<T>(1.); }
+    if (ge0(X)) { if (ge0(X + x)) return cst<T>(1.f); else return cst<T>(-1.f); }
+    else { if (le0(X + x)) return cst<T>(-1.f); else return cst<T>(1.f); }
 }
 
 // burning_ship.py:535-619 _p_iter_zn
@@ -275,8 +370,9 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     xr_coexp_r(c_xr.im, c_xr.e, Tl.drifty_m, Tl.drifty_e, ar, br, be);
     const T b = from_me<T>(ar + br, be);
 
-    T xn = from_d<T>(0.), yn = from_d<T>(0.);
-    T h[4] = {from_d<T>(0.), from_d<T>(0.), from_d<T>(0.), from_d<T>(0.)};
+    T xn = cst<T>(0.f), yn = cst<T>(0.f);
+    T h[4] = {cst<T>(0.f), cst<T>(0.f), cst<T>(0.f), cst<T>(0.f)};
+    const fr M2f = fr_from_d(C.M2);
     int w = 0, n = 0; signed char stop = -1; bool dyn = true;
     // calc_orbit snapshots (perturbation.py:1501-1508), FP64 form only: the
     // FP32 + exponent instantiation compiles without them
@@ -289,7 +385,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             int ib;
             // the reference compares the double value of |dz| (0 when it
             // underflows, perturbation.py:1123-1135)
-            int step = bla_lookup(R, hypot(to_d(xn), to_d(yn)), w, ib);
+            int step = BLAGet<T>::get(R, xn, yn, w, ib);
             if (step != 0) {
                 T M[8];
                 BSRef<T>::bla(R, ib, M);
@@ -311,7 +407,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         T X, Y;
         BSRef<T>::orbit(R, w, X, Y);
         if (hess) {
-            T Xa = from_d<T>(0.), Xb = from_d<T>(0.), Ya = from_d<T>(0.), Yb = from_d<T>(0.);
+            T Xa = cst<T>(0.f), Xb = cst<T>(0.f), Ya = cst<T>(0.f), Yb = cst<T>(0.f);
             if (!dyn) BSRef<T>::hess(R, w, Xa, Xb, Ya, Yb);
             bs_hess<T>(flavor, h, xn, yn, X, Y, Xa, Xb, Ya, Yb);
         }
@@ -322,9 +418,13 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         T Xs, Ys;
         BSRef<T>::orbit(R, w, Xs, Ys);
         T XX = xn + Xs, YY = yn + Ys;
-        const double XXd = to_d(XX), YYd = to_d(YY);
-        if (bs > 0) S.take(n, bs, cx(XXd, YYd));                 // :1641-1651
-        if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
+        if constexpr (ORB_FORM) {
+            const double XXd = to_d(XX), YYd = to_d(YY);
+            if (bs > 0) S.take(n, bs, cx(XXd, YYd));             // :1641-1651
+            if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
+        } else {
+            if (fr_escaped(XX, YY, M2f, C.M2)) { stop = 1; break; }
+        }
         if (w >= div_iter - 1) {
             xn = XX; yn = YY;
             if (hess) {

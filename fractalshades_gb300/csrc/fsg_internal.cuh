@@ -53,6 +53,7 @@ struct RefDev {
     const int4 *bs_Zf;          // [len + 1] {X, Y} (Xrange side-table values where present)
     const int4 *bs_hf;          // [2 (len + 1)] {dXa, dXb}, {dYa, dYb}
     const int4 *bs_blaf;        // [4 bla_len] the 8 BLA coefficients, two per int4
+    const int2 *bs_rf;          // [bla_len] the BLA radii {mantissa bits, exponent}
 };
 
 struct TileDev {

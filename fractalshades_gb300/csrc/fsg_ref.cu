@@ -485,11 +485,12 @@ __global__ void k_bs_fr_paths(const double *dXa, const double *dXb, const double
     out[2 * i] = make_int4(a.x, a.y, b.x, b.y);
     out[2 * i + 1] = make_int4(c.x, c.y, d.x, d.y);
 }
-__global__ void k_bs_fr_bla(const double *M, int n, int4 *out) {
+__global__ void k_bs_fr_bla(const double *M, const double *r, int n, int4 *out, int2 *rf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 4 * n) return;
     int2 a = fr_pack(fr_from_d(M[2 * i])), b = fr_pack(fr_from_d(M[2 * i + 1]));
     out[i] = make_int4(a.x, a.y, b.x, b.y);
+    if (i < n) rf[i] = fr_pack(fr_from_d(r[i]));
 }
 
 void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
@@ -498,9 +499,11 @@ void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, con
     k_bs_fr_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (hf) k_bs_fr_paths<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dXa, dXb, dYa, dYb, len + 1, hf);
 }
-void fsg_build_bs_fr_bla(const double *Mbs, int bla_len, int4 *blaf, cudaStream_t s) {
+void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int4 *blaf,
+                         int2 *rf, cudaStream_t s) {
     int tb = 256;
-    if (blaf && bla_len > 0) k_bs_fr_bla<<<(4 * bla_len + tb - 1) / tb, tb, 0, s>>>(Mbs, bla_len, blaf);
+    if (blaf && rf && bla_len > 0)
+        k_bs_fr_bla<<<(4 * bla_len + tb - 1) / tb, tb, 0, s>>>(Mbs, rbla, bla_len, blaf, rf);
 }
 
 // ---------------------------------------------------------------------------
