@@ -345,6 +345,274 @@ FSG_DEV void bs_hess(int flavor, T h[4], T xn, T yn, T X, T Y, T Xa, T Xb, T Ya,
     h[0] = nxa; h[1] = nxb; h[2] = nya; h[3] = nyb;
 }
 
+// ---------------------------------------------------------------------------
+// Frame form of the fr loop.  The delta pair shares one exponent and the
+// Hessian another:  (xn, yn) = (ux, uy) 2^E,  (dxnda, dxndb, dynda, dyndb) =
+// h 2^F,  with (a, b) 2^-E kept as (cux, cuy).  A step then runs the closures'
+// formulas (burning_ship.py:535-859) in plain FP32: the orbit values X, Y are
+// floats (the fa table), products of two deltas carry the factor s = 2^E (0
+// below 2^-127, where those terms are below FP32 resolution against the
+// others), products with the reference Hessian R = Hm 2^g carry 2^(g + E - F)
+// (with the delta) or 2^(g - F) (with the orbit).  A diffabs(P, d) is taken
+// only when its branch is known: P = 0 (|d|, with the reference's derivative
+// convention sgn(0) = +1), or |d| < |P| / 2 (sgn(P) d); otherwise, and at
+// orbit points that are both 0 or outside [2^-60, 2^40], the step runs in fr.
+// The rounding is FP32's as in fr (one rounding per operation, FMAs where the
+// compiler contracts), so the two forms agree to FP32 rounding.
+// ---------------------------------------------------------------------------
+struct BSFrame {
+    float ux, uy; int E;          // deltas
+    float s;                      // 2^E, 0 below 2^-127
+    float cux, cuy;               // (a, b) 2^-E
+    float h[4]; int F;            // Hessian, F = FR_ZERO_E when h = 0
+    float am, bm; int ae, be;     // (a, b) = (am 2^ae, bm 2^be)
+};
+
+// 2^k for k clamped to [-127, 127] (2^-127 reads as 0)
+FSG_DEV float fr_p2c(int k) { return __int_as_float((min(max(k, -127), 127) + 127) << 23); }
+// unbiased exponent of |m| for a normal float, -127 for 0 and subnormals
+FSG_DEV int fr_fexp(float m) { return ((__float_as_int(m) >> 23) & 0xff) - 127; }
+
+FSG_DEV void frame_set_scale(BSFrame &S) {
+    S.s = fr_p2c(S.E);
+    S.cux = S.am * fr_p2c(S.ae - S.E);
+    S.cuy = S.bm * fr_p2c(S.be - S.E);
+}
+FSG_DEV int frame_ec(const BSFrame &S) { return max(S.ae, S.be); }
+
+// fr values -> frame (E >= the exponent of c minus 100, so that (a, b) 2^-E
+// stays finite)
+FSG_DEV void frame_in(BSFrame &S, fr xn, fr yn, const fr h[4]) {
+    S.E = max(max(xn.e, yn.e), frame_ec(S) - 100);
+    S.ux = xn.m * fr_p2c(xn.e - S.E);
+    S.uy = yn.m * fr_p2c(yn.e - S.E);
+    frame_set_scale(S);
+    S.F = max(max(h[0].e, h[1].e), max(h[2].e, h[3].e));
+    for (int k = 0; k < 4; k++) S.h[k] = h[k].m * fr_p2c(h[k].e - S.F);
+}
+FSG_DEV void frame_out(const BSFrame &S, fr &xn, fr &yn, fr h[4]) {
+    xn = fr_norm(S.ux, S.E);
+    yn = fr_norm(S.uy, S.E);
+    for (int k = 0; k < 4; k++) h[k] = fr_norm(S.h[k], S.F);
+}
+// lazy renormalisation: max(|ux|, |uy|) and max |h| kept in [2^-30, 2^30]
+FSG_DEV void frame_renorm(BSFrame &S) {
+    const float m = fmaxf(fabsf(S.ux), fabsf(S.uy));
+    if (!(m >= 0x1p-30f && m <= 0x1p30f)) {
+        int En;
+        if (m < 0x1p-126f) { S.ux = 0.f; S.uy = 0.f; En = frame_ec(S); }
+        else {
+            En = max(S.E + fr_fexp(m), frame_ec(S) - 100);
+            const float sc = fr_p2c(S.E - En);
+            S.ux *= sc; S.uy *= sc;
+        }
+        S.E = En;
+        frame_set_scale(S);
+    }
+    const float mh = fmaxf(fmaxf(fabsf(S.h[0]), fabsf(S.h[1])), fmaxf(fabsf(S.h[2]), fabsf(S.h[3])));
+    if (!(mh >= 0x1p-30f && mh <= 0x1p30f)) {
+        if (mh < 0x1p-126f) {
+            for (int k = 0; k < 4; k++) S.h[k] = 0.f;
+            S.F = FR_ZERO_E;
+        } else {
+            const int k = fr_fexp(mh);
+            const float sc = fr_p2c(-k);
+            for (int j = 0; j < 4; j++) S.h[j] *= sc;
+            S.F += k;
+        }
+    }
+}
+// raise the Hessian's exponent to Fn (> F): entries below 2^(Fn - 127) drop
+FSG_DEV void frame_raise_F(BSFrame &S, int Fn) {
+    const float sc = fr_p2c(S.F - Fn);
+    for (int k = 0; k < 4; k++) S.h[k] *= sc;
+    S.F = Fn;
+}
+// h += Hm 2^g (the rebase's addition of the reference Hessian)
+FSG_DEV void frame_add_hess(BSFrame &S, float4 Hm, int g) {
+    if (Hm.x == 0.f && Hm.y == 0.f && Hm.z == 0.f && Hm.w == 0.f) return;
+    if (g - S.F > 60) frame_raise_F(S, g - 30);
+    const float k0 = fr_p2c(g - S.F);
+    S.h[0] = fmaf(Hm.x, k0, S.h[0]); S.h[1] = fmaf(Hm.y, k0, S.h[1]);
+    S.h[2] = fmaf(Hm.z, k0, S.h[2]); S.h[3] = fmaf(Hm.w, k0, S.h[3]);
+}
+
+// diffabs(P, d) for d = du 2^E and P known by its sign sp (0 when P = 0) and
+// exponent bounds 2^elo <= |P| < 2^(ehi + 1) (burning_ship.py:19-60):
+//   P = 0: |d| (with ddiffabsdX = -2 for d < 0, sgn(0) = +1);
+//   |d| < |P| / 2: sgn(P) d;
+//   |d| > 2^26 |P|: the sign of P + d is d's and 2 P is below FP32 resolution
+//   against d.
+// Returns false when the exponents leave the branch open.
+FSG_DEV bool frame_diffabs(float sp, int elo, int ehi, float du, int E, float &val, float &dX,
+                           float &dx) {
+    const bool neg = du < 0.f;
+    if (sp == 0.f) {
+        val = neg ? -du : du; dX = neg ? -2.f : 0.f; dx = neg ? -1.f : 1.f;
+        return true;
+    }
+    const float ad = fabsf(du);
+    const int ed = ad == 0.f ? FR_ZERO_E : E + fr_fexp(ad);
+    if (ed <= elo - 2) { val = sp * du; dX = 0.f; dx = sp; return true; }
+    if (ed < ehi + 27) return false;
+    if (sp > 0.f) { val = neg ? -du : du; dX = neg ? -2.f : 0.f; dx = neg ? -1.f : 1.f; }
+    else { val = neg ? -du : du; dX = neg ? 0.f : 2.f; dx = neg ? -1.f : 1.f; }
+    return true;
+}
+FSG_DEV float frame_sgn(float v, int e) {           // 0 for an exact 0
+    return e == FR_ZERO_E ? 0.f : (signbit(v) ? -1.f : 1.f);
+}
+
+// One step of the loop at orbit point (X, Y) with the reference Hessian
+// Hm 2^g (zero_ref: the zeros the loop uses right after a dynamic rebase),
+// before renormalisation.  Returns false, leaving S untouched, when the step
+// has to run in fr.
+FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, int eX, int eY,
+                           float4 Hm, int g, bool zero_ref) {
+    const float s = S.s, ux = S.ux, uy = S.uy;
+    const float xs = ux * s, ys = uy * s;                    // xn, yn as floats
+    const float xx2 = ux * (xs + 2.f * X);                   // xn (xn + 2 X)
+    const float yy2 = uy * (ys + 2.f * Y);                   // yn (yn + 2 Y)
+    const float xy = ux * ys;                                // xn yn
+    float v1 = 0.f, dX1 = 0.f, dx1 = 0.f, v2 = 0.f, dX2 = 0.f, dx2 = 0.f;
+    float vy = 0.f, dXy = 0.f, dxy = 0.f;
+    const bool use1 = flavor == 1 || flavor == 5, use2 = flavor >= 4, usey = flavor == 2 || flavor == 3;
+    const float sX = frame_sgn(X, eX), sY = frame_sgn(Y, eY);
+    if (use1) {
+        // P1 = X Y: 2^(eX + eY) <= |P1| < 2^(eX + eY + 2)
+        const float o1 = fmaf(uy, X, fmaf(ux, Y, xy));     // xn yn + xn Y + yn X
+        if (!frame_diffabs(sX * sY, eX + eY, eX + eY + 1, o1, S.E, v1, dX1, dx1)) return false;
+    }
+    if (use2) {
+        // P2 = X^2 - Y^2 in the rounding of the fr closure (a component
+        // below 2^-100 against one above 2^-60 drops out of it)
+        const float P2 = __fsub_rn(__fmul_rn(X, X), __fmul_rn(Y, Y));
+        const int e2 = fr_fexp(fabsf(P2));
+        if (!frame_diffabs(P2 == 0.f ? 0.f : (P2 > 0.f ? 1.f : -1.f), e2, e2, xx2 - yy2, S.E,
+                           v2, dX2, dx2))
+            return false;
+    }
+    if (usey) {
+        if (!frame_diffabs(sY, eY, eY, uy, S.E, vy, dXy, dxy)) return false;
+    }
+    // |Y + yn| and sgn(Y + yn) with sgn(0) = +1 (flavors 2, 3): the branch
+    // is known here, so the sign is sgn(Y) unless |yn| dominates or Y = 0
+    const float ab = fabsf(Y + ys);
+    const float sg = (sY != 0.f && dXy == 0.f) ? sY : (uy < 0.f ? -1.f : 1.f);
+    if (hess) {
+        const bool hz = zero_ref || (Hm.x == 0.f && Hm.y == 0.f && Hm.z == 0.f && Hm.w == 0.f);
+        float k1 = 0.f, k0 = 0.f;
+        if (!hz) {
+            // the terms in 2^(g - F) are products with X or Y
+            const bool need0 = (dX1 != 0.f || dX2 != 0.f || dXy != 0.f) && (X != 0.f || Y != 0.f);
+            if (g + S.E - S.F > 60) frame_raise_F(S, g + S.E - 30);
+            if (need0 && g - S.F > 60) frame_raise_F(S, g - 30);
+            k1 = fr_p2c(g + S.E - S.F);
+            k0 = need0 ? fr_p2c(g - S.F) : 0.f;
+        } else {
+            Hm = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const float h0 = S.h[0], h1 = S.h[1], h2 = S.h[2], h3 = S.h[3];
+        float nxa, nxb, nya, nyb;
+        if (flavor == 1 || flavor == 2) {
+            nxa = 2.f * ((X + xs) * h0 + Hm.x * ux * k1) - 2.f * ((Y + ys) * h2 + Hm.z * uy * k1);
+            nxb = 2.f * ((X + xs) * h1 + Hm.y * ux * k1) - 2.f * ((Y + ys) * h3 + Hm.w * uy * k1);
+        } else if (flavor == 3) {
+            nxa = h0 * (xs + 2.f * X) + ux * (h0 * s + 2.f * Hm.x * k1) - Hm.z * vy * k1
+                  - Y * (Hm.z * dXy * k0 + h2 * dxy) - h2 * ab - sg * (uy * Hm.z * k1 + uy * h2 * s);
+            nxb = h1 * (xs + 2.f * X) + ux * (h1 * s + 2.f * Hm.y * k1) - Hm.w * vy * k1
+                  - Y * (Hm.w * dXy * k0 + h3 * dxy) - h3 * ab - sg * (uy * Hm.w * k1 + uy * h3 * s);
+        } else {
+            const float dxa2 = h0 * (xs + 2.f * X) + ux * (h0 * s + 2.f * Hm.x * k1)
+                               - h2 * (ys + 2.f * Y) - uy * (h2 * s + 2.f * Hm.z * k1);
+            const float dxb2 = h1 * (xs + 2.f * X) + ux * (h1 * s + 2.f * Hm.y * k1)
+                               - h3 * (ys + 2.f * Y) - uy * (h3 * s + 2.f * Hm.w * k1);
+            const float dXa2 = 2.f * (X * Hm.x - Y * Hm.z) * k0;
+            const float dXb2 = 2.f * (X * Hm.y - Y * Hm.w) * k0;
+            nxa = dX2 * dXa2 + dx2 * dxa2;
+            nxb = dX2 * dXb2 + dx2 * dxb2;
+        }
+        if (flavor == 1 || flavor == 5) {
+            const float dxa = (h0 * uy + ux * h2) * s + h0 * Y + h2 * X + (ux * Hm.z + uy * Hm.x) * k1;
+            const float dxb = (h1 * uy + ux * h3) * s + h1 * Y + h3 * X + (ux * Hm.w + uy * Hm.y) * k1;
+            const float dXa = (Hm.x * Y + X * Hm.z) * k0, dXb = (Hm.y * Y + X * Hm.w) * k0;
+            nya = 2.f * (dX1 * dXa + dx1 * dxa);
+            nyb = 2.f * (dX1 * dXb + dx1 * dxb);
+        } else if (flavor == 2) {
+            nya = 2.f * (Hm.x * vy * k1 + X * (dXy * Hm.z * k0 + dxy * h2) + h0 * ab
+                         + sg * (ux * Hm.z * k1 + ux * h2 * s));
+            nyb = 2.f * (Hm.y * vy * k1 + X * (dXy * Hm.w * k0 + dxy * h3) + h1 * ab
+                         + sg * (ux * Hm.w * k1 + ux * h3 * s));
+        } else {
+            nya = 2.f * ((Hm.x * uy + Hm.z * ux) * k1 + X * h2 + Y * h0 + (h0 * uy + ux * h2) * s);
+            nyb = 2.f * ((Hm.y * uy + Hm.w * ux) * k1 + X * h3 + Y * h1 + (h1 * uy + ux * h3) * s);
+        }
+        S.h[0] = nxa; S.h[1] = nxb; S.h[2] = nya; S.h[3] = nyb;
+    }
+    float nx, ny;
+    if (flavor == 1) {
+        nx = xx2 - yy2 + S.cux; ny = 2.f * v1 - S.cuy;
+    } else if (flavor == 2) {
+        nx = xx2 - yy2 + S.cux; ny = 2.f * (X * vy + ux * ab) - S.cuy;
+    } else if (flavor == 3) {
+        nx = xx2 - Y * vy - uy * ab + S.cux; ny = 2.f * (X * uy + Y * ux + xy) - S.cuy;
+    } else if (flavor == 4) {
+        nx = v2 + S.cux; ny = 2.f * (X * uy + Y * ux + xy) - S.cuy;
+    } else {
+        nx = v2 + S.cux; ny = 2.f * v1 - S.cuy;
+    }
+    S.ux = nx; S.uy = ny;
+    return true;
+}
+
+// The step at an orbit point X = Y = 0 (every term is a product of two deltas
+// or c): the deltas' exponent moves to E' = max(2 E, Ec - 100) and the
+// Hessian's to F + E' - E, so that the general step's products "u u s" and
+// "h u s" with s = 2^(2E - E') land in the new frames (its products with X
+// and Y vanish).
+FSG_DEV void bs_frame_step_zero(int flavor, bool hess, BSFrame &S, float4 Hm, int g,
+                                bool zero_ref) {
+    const int E = S.E;
+    const int En = max(2 * E, frame_ec(S) - 100);
+    BSFrame T = S;
+    T.s = fr_p2c(2 * E - En);
+    T.cux = S.am * fr_p2c(S.ae - En);
+    T.cuy = S.bm * fr_p2c(S.be - En);
+    if (T.F != FR_ZERO_E) T.F = S.F + En - E;
+    // all diffabs arguments are 0 here: the step is always taken
+    bs_frame_step(flavor, hess, T, 0.f, 0.f, FR_ZERO_E, FR_ZERO_E, Hm, g, zero_ref);
+    S = T;
+    S.E = En;
+    frame_set_scale(S);
+}
+
+// |X + d| <= |d| for one component (d = du 2^E), as the fr values round:
+// true when X = 0 or |X| < 2^-25 |d| (X + d rounds to d), false when
+// |d| < |X| / 2; open otherwise
+FSG_DEV bool frame_le(float du, int E, int eX, bool &le) {
+    if (eX == FR_ZERO_E) { le = true; return true; }
+    const float ad = fabsf(du);
+    const int ed = ad == 0.f ? FR_ZERO_E : E + fr_fexp(ad);
+    if (ed <= eX - 2) { le = false; return true; }
+    if (ed >= eX + 26) { le = true; return true; }
+    return false;
+}
+// The loop's tests at orbit point (X, Y) (perturbation.py:1627-1711) in the
+// frame form: 0 none, 1 escape, 2 rebase where X + xn, Y + yn round to xn, yn
+// (the deltas stay), 3 to be decided in fr
+FSG_DEV int bs_frame_tests(const BSFrame &S, float X, float Y, int eX, int eY, float M2s,
+                           bool div_rebase) {
+    bool lex, ley;
+    if (S.E > 10) return 3;                             // deltas above 2^40: fr from here
+    if (!frame_le(S.ux, S.E, eX, lex) || !frame_le(S.uy, S.E, eY, ley)) return 3;
+    const float XX = fmaf(S.ux, S.s, X), YY = fmaf(S.uy, S.s, Y);
+    const float q = fmaf(XX, XX, YY * YY);
+    if (fabsf(q - M2s) <= M2s * 0x1p-18f) return 3;
+    if (q > M2s) return 1;
+    if (div_rebase || (lex && ley)) return (lex && ley) ? 2 : 3;
+    return 0;
+}
+
 template <class T> struct IsDouble { static constexpr bool value = false; };
 template <> struct IsDouble<double> { static constexpr bool value = true; };
 
@@ -380,41 +648,110 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     const int bs = ORB_FORM ? C.backshift : 0;
     OrbitSnap<double2> S;
     S.init(bs, cx(0., 0.));
+    // the reference's BLA step (perturbation.py:1520-1545, 1793-1811)
+    auto apply_bla = [&](int step, int ib) {
+        T M[8];
+        BSRef<T>::bla(R, ib, M);
+        n += step; w = (w + step) % order;
+        T nx = M[0] * xn + M[1] * yn + M[4] * a + M[5] * b;
+        T ny = M[2] * xn + M[3] * yn + M[6] * a + M[7] * b;
+        xn = nx; yn = ny;
+        if (hess) {
+            T xa = M[0] * h[0] + M[1] * h[2], xb = M[0] * h[1] + M[1] * h[3];
+            T ya = M[2] * h[0] + M[3] * h[2], yb = M[2] * h[1] + M[3] * h[3];
+            h[0] = xa; h[1] = xb; h[2] = ya; h[3] = yb;
+        }
+        nbla++;
+    };
+    // frame form of the FP32 + exponent loop (BSFrame); the fr values are
+    // current whenever frm is false
+    BSFrame Fm;
+    bool frm = false;
+    float M2s = 0.f;
+    if constexpr (!ORB_FORM) {
+        Fm.am = a.m; Fm.ae = a.e; Fm.bm = b.m; Fm.be = b.e;
+        M2s = (float)C.M2;
+    }
     for (;;) {
-        if (C.bla && (w & 7) == 0) {
-            int ib;
-            // the reference compares the double value of |dz| (0 when it
-            // underflows, perturbation.py:1123-1135)
-            int step = BLAGet<T>::get(R, xn, yn, w, ib);
-            if (step != 0) {
-                T M[8];
-                BSRef<T>::bla(R, ib, M);
-                n += step; w = (w + step) % order;
-                T nx = M[0] * xn + M[1] * yn + M[4] * a + M[5] * b;
-                T ny = M[2] * xn + M[3] * yn + M[6] * a + M[7] * b;
-                xn = nx; yn = ny;
-                if (hess) {
-                    T xa = M[0] * h[0] + M[1] * h[2], xb = M[0] * h[1] + M[1] * h[3];
-                    T ya = M[2] * h[0] + M[3] * h[2], yb = M[2] * h[1] + M[3] * h[3];
-                    h[0] = xa; h[1] = xb; h[2] = ya; h[3] = yb;
+        bool bla_done = false, stepped = false;
+        if constexpr (!ORB_FORM) {
+            if (frm) {
+                if (C.bla && (w & 7) == 0 && (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
+                    int ib;
+                    const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E), fr_norm(Fm.uy, Fm.E), w, ib);
+                    if (step != 0) {
+                        frame_out(Fm, xn, yn, h); frm = false;
+                        apply_bla(step, ib);
+                        continue;
+                    }
                 }
-                nbla++;
-                continue;
+                bla_done = true;
+                const int2 fz = __ldg(&R.bs_fz[w]);
+                bool ok = (fz.x & 5) != 0;
+                if (ok) {
+                    float4 Hm = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (hess && !dyn) Hm = __ldg(&R.bs_fh[w]);
+                    if (fz.x & 4) {
+                        bs_frame_step_zero(flavor, hess, Fm, Hm, fz.y, dyn);
+                    } else {
+                        const float4 fa = __ldg(&R.bs_fa[w]);
+                        ok = bs_frame_step(flavor, hess, Fm, fa.x, fa.y, __float_as_int(fa.z),
+                                           __float_as_int(fa.w), Hm, fz.y, dyn);
+                    }
+                    if (ok) frame_renorm(Fm);
+                }
+                if (ok) {
+                    n += 1;
+                    nfull++;
+                    if (n >= C.max_iter) { stop = 0; frame_out(Fm, xn, yn, h); frm = false; break; }
+                    w += 1;
+                    if (w >= order) w = w % order;
+                    const int2 fzb = __ldg(&R.bs_fz[w]);
+                    const bool divr = w >= div_iter - 1;
+                    int res = 3;
+                    if (fzb.x & 2) {
+                        const float4 fb = __ldg(&R.bs_fa[w]);
+                        res = bs_frame_tests(Fm, fb.x, fb.y, __float_as_int(fb.z),
+                                             __float_as_int(fb.w), M2s, divr);
+                    }
+                    if (res == 0) { dyn = false; continue; }
+                    if (res == 1) { stop = 1; frame_out(Fm, xn, yn, h); frm = false; break; }
+                    if (res == 2) {
+                        // rebase onto an orbit point 0: the deltas stay
+                        if (hess) frame_add_hess(Fm, __ldg(&R.bs_fh[w]), fzb.y);
+                        if (!divr) dyn = true;
+                        w = 0; nreb++; continue;
+                    }
+                    // the tests below decide, on the fr values
+                    frame_out(Fm, xn, yn, h); frm = false;
+                    stepped = true;
+                } else {
+                    frame_out(Fm, xn, yn, h); frm = false;
+                }
             }
         }
-        n += 1;
-        nfull++;
-        T X, Y;
-        BSRef<T>::orbit(R, w, X, Y);
-        if (hess) {
-            T Xa = cst<T>(0.f), Xb = cst<T>(0.f), Ya = cst<T>(0.f), Yb = cst<T>(0.f);
-            if (!dyn) BSRef<T>::hess(R, w, Xa, Xb, Ya, Yb);
-            bs_hess<T>(flavor, h, xn, yn, X, Y, Xa, Xb, Ya, Yb);
+        if (!stepped) {
+            if (C.bla && !bla_done && (w & 7) == 0) {
+                int ib;
+                // the reference compares the double value of |dz| (0 when it
+                // underflows, perturbation.py:1123-1135)
+                const int step = BLAGet<T>::get(R, xn, yn, w, ib);
+                if (step != 0) { apply_bla(step, ib); continue; }
+            }
+            n += 1;
+            nfull++;
+            T X, Y;
+            BSRef<T>::orbit(R, w, X, Y);
+            if (hess) {
+                T Xa = cst<T>(0.f), Xb = cst<T>(0.f), Ya = cst<T>(0.f), Yb = cst<T>(0.f);
+                if (!dyn) BSRef<T>::hess(R, w, Xa, Xb, Ya, Yb);
+                bs_hess<T>(flavor, h, xn, yn, X, Y, Xa, Xb, Ya, Yb);
+            }
+            bs_zn<T>(flavor, xn, yn, X, Y, a, b);
+            if (n >= C.max_iter) { stop = 0; break; }
+            w += 1;
+            if (w >= order) w = w % order;
         }
-        bs_zn<T>(flavor, xn, yn, X, Y, a, b);
-        if (n >= C.max_iter) { stop = 0; break; }
-        w += 1;
-        if (w >= order) w = w % order;
         T Xs, Ys;
         BSRef<T>::orbit(R, w, Xs, Ys);
         T XX = xn + Xs, YY = yn + Ys;
@@ -443,6 +780,14 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                 h[0] += Ha; h[1] += Hb; h[2] += Hc; h[3] += Hd;
             }
             w = 0; nreb++; continue;
+        }
+        if constexpr (!ORB_FORM) {
+            // the frame form takes over while the deltas stay below 2^11 and
+            // the next step can run there
+            if (max(xn.e, yn.e) <= 10 && (__ldg(&R.bs_fz[w]).x & 5)) {
+                frame_in(Fm, xn, yn, h);
+                frm = true;
+            }
         }
     }
     T Xe, Ye;

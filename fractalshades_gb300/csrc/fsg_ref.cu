@@ -493,11 +493,69 @@ __global__ void k_bs_fr_bla(const double *M, const double *r, int n, int4 *out, 
     if (i < n) rf[i] = fr_pack(fr_from_d(r[i]));
 }
 
+// Frame-step tables (fsg_bs.cuh, BSFrame): per orbit index w
+//   fa[w] = {X, Y as floats, exponent of X, exponent of Y}: a component of
+//           magnitude in [2^-60, 2^40) is its float value; one below 2^-100 is
+//           a signed zero (its exponent stays exact); 0 has FR_ZERO_E
+//   fz[w] = {flags, g}: flags bit 0, the frame step may run at w (one
+//           component in [2^-60, 2^40), the other 0, below 2^-100 or in that
+//           range); bit 1, the loop's tests can run at w (each component 0,
+//           below 2^-100 or in [2^-60, 2^40)); bit 2, X = Y = 0 (the step
+//           there is quadratic in the deltas); g the largest exponent of the
+//           reference Hessian at w (0 when it is 0)
+//   fh[w] = {dXa, dXb, dYa, dYb} * 2^-g, entries below 2^-126 of the
+//           largest read as 0
+__device__ __forceinline__ int fr_frame_kind(fr v) {    // 0 zero, 1 tiny, 2 float, 3 other
+    if (v.m == 0.f) return 0;
+    if (v.e < -100) return 1;
+    if (v.e >= -60 && v.e <= 39) return 2;
+    return 3;
+}
+__device__ __forceinline__ float fr_frame_val(fr v, int kind) {
+    if (kind == 2) return v.m * __int_as_float((v.e + 127) << 23);
+    return v.m < 0.f ? -0.f : 0.f;
+}
+__device__ __forceinline__ float fr_rel(fr v, int g) {
+    if (v.m == 0.f) return 0.f;
+    const int k = v.e - g;
+    return k < -126 ? 0.f : v.m * __int_as_float((k + 127) << 23);
+}
+__global__ void k_bs_frame_tab(const int4 *Zf, const int4 *hf, int n, float4 *fa, int2 *fz,
+                               float4 *fh) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 z = Zf[i];
+    fr x, y;
+    x.m = __int_as_float(z.x); x.e = z.y; y.m = __int_as_float(z.z); y.e = z.w;
+    const int kx = fr_frame_kind(x), ky = fr_frame_kind(y);
+    int flags = (kx != 3 && ky != 3) ? 2 : 0;
+    if ((flags & 2) && (kx == 2 || ky == 2)) flags |= 1;
+    if (kx == 0 && ky == 0) flags |= 4;
+    int g = 0;
+    if (hf) {
+        const int4 p = hf[2 * i], q = hf[2 * i + 1];
+        fr h[4];
+        h[0].m = __int_as_float(p.x); h[0].e = p.y; h[1].m = __int_as_float(p.z); h[1].e = p.w;
+        h[2].m = __int_as_float(q.x); h[2].e = q.y; h[3].m = __int_as_float(q.z); h[3].e = q.w;
+        bool any = false;
+        g = -(1 << 30);
+        for (int k = 0; k < 4; k++)
+            if (h[k].m != 0.f) { any = true; g = max(g, h[k].e); }
+        if (!any) g = 0;
+        fh[i] = make_float4(fr_rel(h[0], g), fr_rel(h[1], g), fr_rel(h[2], g), fr_rel(h[3], g));
+    }
+    fa[i] = make_float4(fr_frame_val(x, kx), fr_frame_val(y, ky), __int_as_float(x.e),
+                        __int_as_float(y.e));
+    fz[i] = make_int2(flags, g);
+}
+
 void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
-                     const double *dYa, const double *dYb, int4 *hf, cudaStream_t s) {
+                     const double *dYa, const double *dYb, int4 *hf, float4 *fa, int2 *fz,
+                     float4 *fh, cudaStream_t s) {
     int tb = 256;
     k_bs_fr_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (hf) k_bs_fr_paths<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dXa, dXb, dYa, dYb, len + 1, hf);
+    k_bs_frame_tab<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Zf, hf, len + 1, fa, fz, fh);
 }
 void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int4 *blaf,
                          int2 *rf, cudaStream_t s) {

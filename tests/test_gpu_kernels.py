@@ -408,6 +408,95 @@ def test_perturb_bs_fe32_vs_oracle(ctx, case):
     assert np.percentile(err, 90) <= 2e-2 and np.max(err) <= 0.2, (np.percentile(err, 90), err.max())
 
 
+def _bs_nucleus(kind, real_axis):
+    """A period-p nucleus of the flavor (ball method + Newton at 300 bits on
+    the native host side) and its orbit over one period."""
+    import mpmath
+    from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
+    rng = np.random.default_rng(10 + kind + (100 if real_axis else 0))
+    prec = 300
+    with mpmath.workprec(prec):
+        for _ in range(60):
+            if real_axis:
+                c0 = mpmath.mpc(-1.8 + 0.1 * rng.random(), -0.1 * rng.random())
+            else:
+                c0 = mpmath.mpc(-2 + 2.5 * rng.random(), -1.5 + 2 * rng.random())
+            sx, sy = str(c0.real).encode(), str(c0.imag).encode()
+            order = fsFP.perturbation_nonholomorphic_ball_method(sx, sy, prec, b"0.01", 400,
+                                                                 1e5, kind)
+            if order < 3 or order > 200:
+                continue
+            ok, c = fsFP.perturbation_nonholomorphic_find_any_nucleus(
+                sx, sy, prec, order, 80, str(mpmath.mpf(val=(2, -prec))).encode(), b"1e-60",
+                kind)
+            if not ok:
+                continue
+            orb = np.zeros(order + 1, dtype=np.complex128)
+            fsFP.perturbation_nonholomorphic_FP_loop(orb.view(np.float64), False, order, 2e3,
+                                                     str(c.real).encode(), str(c.imag).encode(),
+                                                     prec, kind)
+            return orb[:order], order
+    pytest.skip("no nucleus found")
+
+
+@pytest.mark.parametrize("dx", [1e-9, 1e-45])
+@pytest.mark.parametrize("kind,real_axis", [(1, True), (1, False), (2, False), (3, False),
+                                            (4, False), (5, False)])
+def test_perturb_bs_fe32_vs_fp64_every_flavor(ctx, kind, real_axis, dx):
+    """The FP32 + exponent Burning Ship loop (fr values and their frame form)
+    against the FP64 kernel on the same reference and tile, every flavor,
+    around nuclei on and off the real axis: iteration counts on >= 99 % of the
+    pixels, z and the Hessian to FP32 accuracy amplified by the orbit.  The
+    Hessian is compared normwise (against the pixel's largest entry) and
+    entry by entry above 1e-6 of it: the frame form holds the four entries on
+    one exponent, so an entry far below the others (the cross terms around a
+    real-axis reference, ~1e-112 of the diagonal) is resolved only to that
+    absolute level."""
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300.synthetic import image_axes
+    Zn, order = _bs_nucleus(kind, real_axis)
+    max_iter, side = 3000, 96
+    m, e = np.frexp(dx)
+    kc = float(np.sqrt(2) * 0.5 * dx * 1.1)
+    ref = nat.Reference(ctx, Zn, div_iter=max_iter + 1, order=order, flavor=kind,
+                        calc_dzndc=True, scale_m=float(m), scale_e=int(e), bla=True, kc=kc,
+                        bla_eps=1e-6)
+    xs, ys = image_axes(side, side)
+    out = {}
+    for mode in ("fp64", "fe32"):
+        n = side * side
+        Z = np.zeros((6, n))
+        U = np.zeros((1, n), dtype=np.int32)
+        sr = -np.ones((1, n), dtype=np.int8)
+        si = np.zeros((1, n), dtype=np.int32)
+        t = nat.make_tile(xs=xs, ys=ys, lin_mat=np.eye(2), Z=Z, U=U, stop_reason=sr,
+                          stop_iter=si, ref=ref, dx_m=float(m), dx_e=int(e), drift_m=0.,
+                          drift_e=0, drifty_m=0., drifty_e=0)
+        calc = nat.make_calc(max_iter=max_iter, M_divergence=1e3, flavor=kind, calc_dzndc=True,
+                             bla=True, mode=mode)
+        ctx.perturb_tiles(calc, [t])
+        out[mode] = (Z, sr, si)
+    Z64, sr64, si64 = out["fp64"]
+    Z32, sr32, si32 = out["fe32"]
+    assert np.mean(si32 == si64) >= 0.99, np.mean(si32 == si64)
+    assert np.mean(sr32 == sr64) >= 0.99
+    same = (si32 == si64).ravel()
+    z64 = np.hypot(Z64[0], Z64[1])[same]
+    dz = np.hypot(Z32[0] - Z64[0], Z32[1] - Z64[1])[same]
+    err = dz / np.maximum(z64, 1e-300)
+    assert np.median(err) <= 1e-3, np.median(err)
+    # the Hessian, relative to its largest entry per pixel, and entry by entry
+    H64, H32 = Z64[2:6][:, same], Z32[2:6][:, same]
+    hmax = np.max(np.abs(H64), axis=0)
+    herr = np.max(np.abs(H32 - H64), axis=0) / np.maximum(hmax, 1e-300)
+    assert np.median(herr) <= 1e-2, np.median(herr)
+    for k in range(4):
+        big = np.abs(H64[k]) > 1e-6 * hmax
+        if np.any(big):
+            ek = np.abs(H32[k] - H64[k])[big] / np.abs(H64[k])[big]
+            assert np.median(ek) <= 1e-2, (k, np.median(ek))
+
+
 @pytest.mark.parametrize("case", ["pert_bs_1", "pert_bs_4", "pert_bs_orbit"])
 def test_perturb_bs_vs_oracle(ctx, case):
     from fractalshades_gb300 import _native as nat
