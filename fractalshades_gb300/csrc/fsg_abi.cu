@@ -36,8 +36,8 @@ void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla,
                       int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
                       cudaStream_t s);
 void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
-                     const double *dYa, const double *dYb, int4 *hf, float4 *fa, int2 *fz,
-                     float4 *fh, cudaStream_t s);
+                     const double *dYa, const double *dYb, int4 *hf, float4 *fa, int4 *fz,
+                     float4 *fh, int div_iter, cudaStream_t s);
 void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int4 *blaf,
                          int2 *rf, cudaStream_t s);
 
@@ -601,7 +601,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     int4 *bs_Zf = nullptr, *bs_hf = nullptr, *bs_blaf = nullptr;
     int2 *bs_rf = nullptr;
     float4 *bs_fa = nullptr, *bs_fh = nullptr;
-    int2 *bs_fz = nullptr;
+    int4 *bs_fz = nullptr;
     if (d->flavor != 0) {
         RA(bs_Zf, len + 1);
         RA(bs_fa, len + 1);
@@ -629,7 +629,8 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     }
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
     if (d->flavor != 0) {
-        fsg_build_bs_fr(r->dev, len, bs_Zf, dXa, dXb, dYa, dYb, bs_hf, bs_fa, bs_fz, bs_fh, s);
+        fsg_build_bs_fr(r->dev, len, bs_Zf, dXa, dXb, dYa, dYb, bs_hf, bs_fa, bs_fz, bs_fh,
+                        R.div_iter, s);
         fsg_build_bs_fr_bla(Mbs, rbla, R.bla_len, bs_blaf, bs_rf, s);
     }
     if (fe_tables) {

@@ -616,14 +616,16 @@ FSG_DEV int bs_frame_tests(const BSFrame &S, float X, float Y, int eX, int eY, f
 template <class T> struct IsDouble { static constexpr bool value = false; };
 template <> struct IsDouble<double> { static constexpr bool value = true; };
 
-template <class T>
+// FL: the flavor as a compile-time constant (1..5), or 0 to read C.flavor
+template <class T, int FL>
 FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                       unsigned long long &nfull, unsigned long long &nbla,
                       unsigned long long &nreb, unsigned long long &itsum) {
     const TileDev &Tl = T_;
     const RefDev &R = *Tl.ref;
     const long long np = (long long)Tl.nx * Tl.ny;
-    const int flavor = C.flavor, hess = C.calc_dzndc;
+    const int flavor = FL ? FL : C.flavor;
+    const bool hess = C.calc_dzndc != 0;
     const int order = R.order, div_iter = R.div_iter;
     // perturbation.py:2260-2280 ref_path_c_from_pix_BS through Xrange values
     double2 pp = fsg_pixel(Tl, ip);
@@ -668,6 +670,8 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     BSFrame Fm;
     bool frm = false;
     float M2s = 0.f;
+    // with |X|, |Y| and the deltas below 2^(eMlim + 1), |Z + dz|^2 < M2 / 8
+    const int eMlim = min((M2f.e >> 1) - 4, 40);
     if constexpr (!ORB_FORM) {
         Fm.am = a.m; Fm.ae = a.e; Fm.bm = b.m; Fm.be = b.e;
         M2s = (float)C.M2;
@@ -676,58 +680,71 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         bool bla_done = false, stepped = false;
         if constexpr (!ORB_FORM) {
             if (frm) {
-                if (C.bla && (w & 7) == 0 && (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
-                    int ib;
-                    const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E), fr_norm(Fm.uy, Fm.E), w, ib);
-                    if (step != 0) {
-                        frame_out(Fm, xn, yn, h); frm = false;
-                        apply_bla(step, ib);
-                        continue;
+            // Steps in the frame form from orbit point w on, until the loop ends
+            // (0), a BLA step was taken (1), the step at w has to run in fr (2) or
+            // the tests at w have to (3); the fr values are current on return.
+            auto frame_run = [&]() -> int {
+                int4 fz = __ldg(&R.bs_fz[w]);
+                for (;;) {
+                    if (C.bla && (w & 7) == 0 && (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
+                        int ib;
+                        const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E), fr_norm(Fm.uy, Fm.E), w, ib);
+                        if (step != 0) {
+                            frame_out(Fm, xn, yn, h);
+                            apply_bla(step, ib);
+                            return 1;
+                        }
                     }
-                }
-                bla_done = true;
-                const int2 fz = __ldg(&R.bs_fz[w]);
-                bool ok = (fz.x & 5) != 0;
-                if (ok) {
+                    if (!(fz.x & 5)) { frame_out(Fm, xn, yn, h); return 2; }
                     float4 Hm = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (hess && !dyn) Hm = __ldg(&R.bs_fh[w]);
                     if (fz.x & 4) {
                         bs_frame_step_zero(flavor, hess, Fm, Hm, fz.y, dyn);
                     } else {
                         const float4 fa = __ldg(&R.bs_fa[w]);
-                        ok = bs_frame_step(flavor, hess, Fm, fa.x, fa.y, __float_as_int(fa.z),
-                                           __float_as_int(fa.w), Hm, fz.y, dyn);
+                        if (!bs_frame_step(flavor, hess, Fm, fa.x, fa.y, __float_as_int(fa.z),
+                                           __float_as_int(fa.w), Hm, fz.y, dyn)) {
+                            frame_out(Fm, xn, yn, h);
+                            return 2;
+                        }
                     }
-                    if (ok) frame_renorm(Fm);
-                }
-                if (ok) {
+                    frame_renorm(Fm);
                     n += 1;
                     nfull++;
-                    if (n >= C.max_iter) { stop = 0; frame_out(Fm, xn, yn, h); frm = false; break; }
+                    if (n >= C.max_iter) { stop = 0; frame_out(Fm, xn, yn, h); return 0; }
                     w += 1;
                     if (w >= order) w = w % order;
-                    const int2 fzb = __ldg(&R.bs_fz[w]);
+                    fz = __ldg(&R.bs_fz[w]);
+                    // deltas below the orbit point's bound: no escape, no rebase
+                    const int ed = Fm.E + fr_fexp(fmaxf(fabsf(Fm.ux), fabsf(Fm.uy)));
+                    if (ed <= min(fz.z, eMlim) && fz.w <= eMlim) { dyn = false; continue; }
                     const bool divr = w >= div_iter - 1;
                     int res = 3;
-                    if (fzb.x & 2) {
+                    if (fz.x & 2) {
                         const float4 fb = __ldg(&R.bs_fa[w]);
-                        res = bs_frame_tests(Fm, fb.x, fb.y, __float_as_int(fb.z),
-                                             __float_as_int(fb.w), M2s, divr);
+                        res = bs_frame_tests(Fm, fb.x, fb.y, __float_as_int(fb.z), __float_as_int(fb.w),
+                                             M2s, divr);
                     }
                     if (res == 0) { dyn = false; continue; }
-                    if (res == 1) { stop = 1; frame_out(Fm, xn, yn, h); frm = false; break; }
+                    if (res == 1) { stop = 1; frame_out(Fm, xn, yn, h); return 0; }
                     if (res == 2) {
-                        // rebase onto an orbit point 0: the deltas stay
-                        if (hess) frame_add_hess(Fm, __ldg(&R.bs_fh[w]), fzb.y);
+                        // rebase where X + xn, Y + yn round to the deltas: they stay
+                        if (hess) frame_add_hess(Fm, __ldg(&R.bs_fh[w]), fz.y);
                         if (!divr) dyn = true;
-                        w = 0; nreb++; continue;
+                        w = 0; nreb++;
+                        fz = __ldg(&R.bs_fz[0]);
+                        continue;
                     }
-                    // the tests below decide, on the fr values
-                    frame_out(Fm, xn, yn, h); frm = false;
-                    stepped = true;
-                } else {
-                    frame_out(Fm, xn, yn, h); frm = false;
+                    frame_out(Fm, xn, yn, h);
+                    return 3;
                 }
+            };
+                frm = false;
+                const int r = frame_run();
+                if (r == 0) break;
+                if (r == 1) continue;
+                bla_done = true;
+                stepped = r == 3;
             }
         }
         if (!stepped) {
@@ -830,8 +847,10 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     itsum += (unsigned long long)n;
 }
 
-template <class T>
-__global__ void __launch_bounds__(256) k_perturb_bs(WorkDev W, CalcDev C) {
+// the FP32 + exponent kernels hold three 256-thread blocks per SM (at most 85
+// registers a thread)
+template <class T, int FL>
+__global__ void __launch_bounds__(256, IsDouble<T>::value ? 1 : 3) k_perturb_bs(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
@@ -839,7 +858,7 @@ __global__ void __launch_bounds__(256) k_perturb_bs(WorkDev W, CalcDev C) {
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
-        pixel_bs<T>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        pixel_bs<T, FL>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
     }
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }

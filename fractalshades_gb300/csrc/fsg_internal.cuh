@@ -55,7 +55,8 @@ struct RefDev {
     const int4 *bs_blaf;        // [4 bla_len] the 8 BLA coefficients, two per int4
     const int2 *bs_rf;          // [bla_len] the BLA radii {mantissa bits, exponent}
     const float4 *bs_fa;        // [len + 1] frame step: {X, Y, exponent of X, of Y}
-    const int2 *bs_fz;          // [len + 1] frame step: {flags, Hessian exponent g}
+    const int4 *bs_fz;          // [len + 1] frame step: {flags, Hessian exponent g,
+                                // no-rebase bound Tw, exponent of max(|X|, |Y|)}
     const float4 *bs_fh;        // [len + 1] frame step: {dXa, dXb, dYa, dYb} * 2^-g
 };
 

@@ -497,12 +497,17 @@ __global__ void k_bs_fr_bla(const double *M, const double *r, int n, int4 *out, 
 //   fa[w] = {X, Y as floats, exponent of X, exponent of Y}: a component of
 //           magnitude in [2^-60, 2^40) is its float value; one below 2^-100 is
 //           a signed zero (its exponent stays exact); 0 has FR_ZERO_E
-//   fz[w] = {flags, g}: flags bit 0, the frame step may run at w (one
+//   fz[w] = {flags, g, Tw, eZ}: flags bit 0, the frame step may run at w (one
 //           component in [2^-60, 2^40), the other 0, below 2^-100 or in that
 //           range); bit 1, the loop's tests can run at w (each component 0,
 //           below 2^-100 or in [2^-60, 2^40)); bit 2, X = Y = 0 (the step
 //           there is quadratic in the deltas); g the largest exponent of the
-//           reference Hessian at w (0 when it is 0)
+//           reference Hessian at w (0 when it is 0); Tw: while the deltas
+//           are below 2^(Tw + 1), X + xn or Y + yn keeps the orbit's sign
+//           and magnitude within a factor 2, so no rebase happens at w
+//           (FR_ZERO_E where the tests must run: X = Y = 0, a component
+//           outside the float range, w >= div_iter - 1); eZ the exponent of
+//           max(|X|, |Y|)
 //   fh[w] = {dXa, dXb, dYa, dYb} * 2^-g, entries below 2^-126 of the
 //           largest read as 0
 __device__ __forceinline__ int fr_frame_kind(fr v) {    // 0 zero, 1 tiny, 2 float, 3 other
@@ -520,8 +525,8 @@ __device__ __forceinline__ float fr_rel(fr v, int g) {
     const int k = v.e - g;
     return k < -126 ? 0.f : v.m * __int_as_float((k + 127) << 23);
 }
-__global__ void k_bs_frame_tab(const int4 *Zf, const int4 *hf, int n, float4 *fa, int2 *fz,
-                               float4 *fh) {
+__global__ void k_bs_frame_tab(const int4 *Zf, const int4 *hf, int n, int div_iter, float4 *fa,
+                               int4 *fz, float4 *fh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int4 z = Zf[i];
@@ -546,16 +551,20 @@ __global__ void k_bs_frame_tab(const int4 *Zf, const int4 *hf, int n, float4 *fa
     }
     fa[i] = make_float4(fr_frame_val(x, kx), fr_frame_val(y, ky), __int_as_float(x.e),
                         __int_as_float(y.e));
-    fz[i] = make_int2(flags, g);
+    int Tw = FR_ZERO_E, eZ = FR_ZERO_E;
+    if (kx != 0) { Tw = max(Tw, x.e - 2); eZ = max(eZ, x.e); }
+    if (ky != 0) { Tw = max(Tw, y.e - 2); eZ = max(eZ, y.e); }
+    if (!(flags & 2) || i >= div_iter - 1) Tw = FR_ZERO_E;
+    fz[i] = make_int4(flags, g, Tw, eZ);
 }
 
 void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
-                     const double *dYa, const double *dYb, int4 *hf, float4 *fa, int2 *fz,
-                     float4 *fh, cudaStream_t s) {
+                     const double *dYa, const double *dYb, int4 *hf, float4 *fa, int4 *fz,
+                     float4 *fh, int div_iter, cudaStream_t s) {
     int tb = 256;
     k_bs_fr_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (hf) k_bs_fr_paths<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dXa, dXb, dYa, dYb, len + 1, hf);
-    k_bs_frame_tab<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Zf, hf, len + 1, fa, fz, fh);
+    k_bs_frame_tab<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Zf, hf, len + 1, div_iter, fa, fz, fh);
 }
 void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int4 *blaf,
                          int2 *rf, cudaStream_t s) {
