@@ -146,34 +146,44 @@ FSG_DEV fr_mod fr_modulus2(fr x, fr y, bool squared) {
 // v * 2^d as a float, d in [-3, 0]
 FSG_DEV float fr_scale_small(float v, int d) { return v * __int_as_float((127 + d) << 23); }
 
+// The double-precision forms of the two comparisons below, for the rare
+// near-ties: out of line so that the compiler does not evaluate them ahead
+// of the branch on every call.
+static __device__ __noinline__ bool fr_escaped_exact(fr X, fr Y, double M2) {
+    const double Xd = fr_to_d(X), Yd = fr_to_d(Y);
+    return Xd * Xd + Yd * Yd > M2;
+}
+static __device__ __noinline__ bool fr_below_exact(fr xn, fr yn, double r) {
+    return hypot(fr_to_d(xn), fr_to_d(yn)) < r;
+}
+
 // The escape test |z|^2 > M2 of the loop (perturbation.py:1636-1639) with z in
 // fr: decided in FP32 unless within 2^-18 of the bound, where the double form
 // of the reference decides (so that the outcome is the FP64 one of the same
 // fr values).
 FSG_DEV bool fr_escaped(fr X, fr Y, fr M2f, double M2) {
     const fr_mod q = fr_modulus2(X, Y, true);           // s in [1, 8)
-    if (q.z) return 0. > M2;
+    if (q.z) return false;                              // M2 > 0
     const int d = q.e - M2f.e;
     if (d >= 1) return true;                            // >= 2 > M2 mantissa
     if (d <= -4) return false;                          // < 0.5
     const float t = fr_scale_small(q.s, d);
     if (fabsf(t - M2f.m) > M2f.m * 0x1p-18f) return t > M2f.m;
-    const double Xd = fr_to_d(X), Yd = fr_to_d(Y);
-    return Xd * Xd + Yd * Yd > M2;
+    return fr_escaped_exact(X, Y, M2);
 }
 
 // |dz| < r for a BLA radius r (double r, its fr copy rm * 2^re), the
 // comparison of ref_BLA_get (perturbation.py:2116-2170) in FP32 unless within
 // 2^-18 of r, where the double form decides.
 FSG_DEV bool fr_below(const fr_mod &a, fr xn, fr yn, float rm, int re, double r) {
-    if (rm == 0.f) return false;
-    if (a.z) return 0. < r;
+    if (rm == 0.f) return false;                        // r = 0
+    if (a.z) return true;                               // 0 < r
     const int d = a.e - re;
     if (d >= 1) return false;                           // >= 2 > rm
     if (d <= -2) return true;                           // < 0.71 < rm
     const float t = fr_scale_small(a.s, d);
     if (fabsf(t - rm) > rm * 0x1p-18f) return t < rm;
-    return hypot(fr_to_d(xn), fr_to_d(yn)) < r;
+    return fr_below_exact(xn, yn, r);
 }
 
 // ref_BLA_get in the loop's real type: double |dz| against the double radii,
