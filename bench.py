@@ -47,6 +47,10 @@ def parse():
                     help="requests of the serving stream (0: skip)")
     ap.add_argument("--no-supplementary", action="store_true",
                     help="skip the standard-loop, 1e-1000 and Burning Ship configurations")
+    ap.add_argument("--legs", default="std,deep,bs,host",
+                    help="supplementary configurations to run (std, deep, bs, host)")
+    ap.add_argument("--bs-tiles", type=int, default=64,
+                    help="Burning Ship tiles of the 64 to run (a smaller case for profiling)")
     ap.add_argument("--bs-max-iter", type=int, default=2000,
                     help="max_iter of the Burning Ship configuration (its own is 5e4: "
                          "minutes in FP64 on one GPU)")
@@ -90,11 +94,14 @@ def serving_leg(n_requests, device):
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
-def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter):
+def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
+                  legs=("std", "deep", "bs", "host"), bs_tiles=64):
     """The other measured configurations, one launch each (kernel time from
     the library's CUDA events, L2 flushed before each launch):
-    the standard loop (800 x 600, width 3), the 1e-1000 zoom with interior
-    detection (FE32 against XR64) and 64 Burning Ship tiles in one launch."""
+    the standard loop (800 x 600, width 3) "std", the 1e-1000 zoom with
+    interior detection (FE32 against XR64) "deep", the Burning Ship tiles in
+    one launch "bs" (the first bs_tiles of the 64) and the host side at 1100
+    digits "host"."""
     out = {}
     f64 = dict(dtype=torch.float64, device=dev)
 
@@ -109,115 +116,119 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter):
             ks.append(ctx.stats()["kernel_ms"])
         return float(np.median(ks)), ctx.stats()
 
-    # standard loop, bit-exact against the oracle in the GPU tests
-    w1 = syn.config1_workload()
-    n1 = w1.nx * w1.ny
-    xs = torch.from_numpy(w1.xs).to(dev)
-    ys = torch.from_numpy(w1.ys).to(dev)
-    Z1 = torch.zeros((3, n1, 2), **f64)
-    sr1 = torch.zeros(n1, dtype=torch.int8, device=dev)
-    si1 = torch.zeros(n1, dtype=torch.int32, device=dev)
-    pot1 = torch.zeros(n1, **f64)
-    t1 = nat.make_tile_ptrs(nx=w1.nx, ny=w1.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
-                            lin_mat=LIN, Z_ptr=Z1.data_ptr(), nZ=3,
-                            stop_reason_ptr=sr1.data_ptr(), stop_iter_ptr=si1.data_ptr(),
-                            center=w1.center, dx=w1.dx, i_dzndz=1, i_dzndc=2,
-                            potential_ptr=pot1.data_ptr())
-    c1 = nat.make_calc(max_iter=w1.max_iter, M_divergence=w1.M, epsilon_stationnary=w1.eps)
-    kms, st = timed(lambda: ctx.std_tiles(c1, [t1], nat.DEVICE), 10, 3)
-    out["standard_m2"] = {
-        "workload": "standard power-2 Mandelbrot 800x600, centre -0.5, width 3, max_iter 1000, "
-                    "M 1e3, eps 0.01 (interior detection, dzndc, potential)",
-        "pixels": n1, "pixel_iters": int(st["pixel_iters"]), "kernel_ms": kms,
-        "value": st["pixel_iters"] / (kms * 1e-3), "unit": "pixel-iter/s", "dtype": "f64",
-        "parity": "bit-exact vs the oracle (tests/test_gpu_kernels.py)"}
-    del Z1, sr1, si1, pot1
+    if "std" in legs:
+        # standard loop, bit-exact against the oracle in the GPU tests
+        w1 = syn.config1_workload()
+        n1 = w1.nx * w1.ny
+        xs = torch.from_numpy(w1.xs).to(dev)
+        ys = torch.from_numpy(w1.ys).to(dev)
+        Z1 = torch.zeros((3, n1, 2), **f64)
+        sr1 = torch.zeros(n1, dtype=torch.int8, device=dev)
+        si1 = torch.zeros(n1, dtype=torch.int32, device=dev)
+        pot1 = torch.zeros(n1, **f64)
+        t1 = nat.make_tile_ptrs(nx=w1.nx, ny=w1.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
+                                lin_mat=LIN, Z_ptr=Z1.data_ptr(), nZ=3,
+                                stop_reason_ptr=sr1.data_ptr(), stop_iter_ptr=si1.data_ptr(),
+                                center=w1.center, dx=w1.dx, i_dzndz=1, i_dzndc=2,
+                                potential_ptr=pot1.data_ptr())
+        c1 = nat.make_calc(max_iter=w1.max_iter, M_divergence=w1.M, epsilon_stationnary=w1.eps)
+        kms, st = timed(lambda: ctx.std_tiles(c1, [t1], nat.DEVICE), 10, 3)
+        out["standard_m2"] = {
+            "workload": "standard power-2 Mandelbrot 800x600, centre -0.5, width 3, max_iter 1000, "
+                        "M 1e3, eps 0.01 (interior detection, dzndc, potential)",
+            "pixels": n1, "pixel_iters": int(st["pixel_iters"]), "kernel_ms": kms,
+            "value": st["pixel_iters"] / (kms * 1e-3), "unit": "pixel-iter/s", "dtype": "f64",
+            "parity": "bit-exact vs the oracle (tests/test_gpu_kernels.py)"}
+        del Z1, sr1, si1, pot1
 
-    # 1e-1000, 4096^2, interior detection: FE32 against XR64
-    w3 = syn.config3_workload()
-    n3 = w3.nx * w3.ny
-    ref3 = nat.Reference(ctx, w3.Zn, div_iter=w3.div_iter, order=w3.order, xr_idx=w3.xr_idx,
-                         xr_m=w3.xr_m, xr_e=w3.xr_e, xr_paths=w3.xr_mode, calc_dzndc=True,
-                         calc_dzndz=True, scale_m=w3.dx_m, scale_e=w3.dx_e, bla=True,
-                         kc=w3.kc, bla_eps=1e-6)
-    xs = torch.from_numpy(w3.xs).to(dev)
-    ys = torch.from_numpy(w3.ys).to(dev)
-    Z3 = torch.zeros((3, n3, 2), **f64)
-    sr3 = torch.zeros(n3, dtype=torch.int8, device=dev)
-    si3 = torch.zeros(n3, dtype=torch.int32, device=dev)
-    t3 = nat.make_tile_ptrs(nx=w3.nx, ny=w3.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
-                            lin_mat=LIN, Z_ptr=Z3.data_ptr(), nZ=3,
-                            stop_reason_ptr=sr3.data_ptr(), stop_iter_ptr=si3.data_ptr(),
-                            ref=ref3, dx_m=w3.dx_m, dx_e=w3.dx_e, drift_m=w3.drift_m,
-                            drift_e=w3.drift_e, i_dzndz=1, i_dzndc=2)
+    if "deep" in legs:
+        # 1e-1000, 4096^2, interior detection: FE32 against XR64
+        w3 = syn.config3_workload()
+        n3 = w3.nx * w3.ny
+        ref3 = nat.Reference(ctx, w3.Zn, div_iter=w3.div_iter, order=w3.order, xr_idx=w3.xr_idx,
+                             xr_m=w3.xr_m, xr_e=w3.xr_e, xr_paths=w3.xr_mode, calc_dzndc=True,
+                             calc_dzndz=True, scale_m=w3.dx_m, scale_e=w3.dx_e, bla=True,
+                             kc=w3.kc, bla_eps=1e-6)
+        xs = torch.from_numpy(w3.xs).to(dev)
+        ys = torch.from_numpy(w3.ys).to(dev)
+        Z3 = torch.zeros((3, n3, 2), **f64)
+        sr3 = torch.zeros(n3, dtype=torch.int8, device=dev)
+        si3 = torch.zeros(n3, dtype=torch.int32, device=dev)
+        t3 = nat.make_tile_ptrs(nx=w3.nx, ny=w3.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
+                                lin_mat=LIN, Z_ptr=Z3.data_ptr(), nZ=3,
+                                stop_reason_ptr=sr3.data_ptr(), stop_iter_ptr=si3.data_ptr(),
+                                ref=ref3, dx_m=w3.dx_m, dx_e=w3.dx_e, drift_m=w3.drift_m,
+                                drift_e=w3.drift_e, i_dzndz=1, i_dzndc=2)
 
-    def c3(mode):
-        return nat.make_calc(max_iter=w3.max_iter, M_divergence=w3.M, epsilon_stationnary=1e-3,
-                             mode=mode, calc_dzndc=True, interior=True, bla=True,
-                             xr_semantics=w3.xr_mode)
-    k_fe, st_fe = timed(lambda: ctx.perturb_tiles(c3("fe32"), [t3], nat.DEVICE), 3, 1)
-    si_fe, sr_fe = si3.cpu().numpy().copy(), sr3.cpu().numpy().copy()
-    k_xr, st_xr = timed(lambda: ctx.perturb_tiles(c3("xr64"), [t3], nat.DEVICE), 1, 0)
-    si_xr, sr_xr = si3.cpu().numpy(), sr3.cpu().numpy()
-    out["deep_m2_1e-1000"] = {
-        "workload": f"perturbation Mandelbrot {w3.nx}x{w3.ny} at dx=1e-1000 on a period-{w3.p} "
-                    "nucleus, 1100 digits, max_iter 1e6, interior detection eps 1e-3, dzndc",
-        "pixels": n3, "pixel_iters": int(st_fe["pixel_iters"]),
-        "fe32": {"kernel_ms": k_fe, "value": st_fe["pixel_iters"] / (k_fe * 1e-3)},
-        "xr64": {"kernel_ms": k_xr, "value": st_xr["pixel_iters"] / (k_xr * 1e-3)},
-        "speedup_fe32_vs_xr64": (st_fe["pixel_iters"] / k_fe) / (st_xr["pixel_iters"] / k_xr),
-        "fe32_vs_xr64": {"iter_count_differs_frac": float(np.mean(si_fe != si_xr)),
-                         "stop_reason_differs_frac": float(np.mean(sr_fe != sr_xr)),
-                         "iter_count_max_abs_diff": int(np.max(np.abs(
-                             si_fe.astype(np.int64) - si_xr)))},
-        "unit": "pixel-iter/s"}
-    ref3.free()
-    del Z3, sr3, si3
+        def c3(mode):
+            return nat.make_calc(max_iter=w3.max_iter, M_divergence=w3.M, epsilon_stationnary=1e-3,
+                                 mode=mode, calc_dzndc=True, interior=True, bla=True,
+                                 xr_semantics=w3.xr_mode)
+        k_fe, st_fe = timed(lambda: ctx.perturb_tiles(c3("fe32"), [t3], nat.DEVICE), 3, 1)
+        si_fe, sr_fe = si3.cpu().numpy().copy(), sr3.cpu().numpy().copy()
+        k_xr, st_xr = timed(lambda: ctx.perturb_tiles(c3("xr64"), [t3], nat.DEVICE), 1, 0)
+        si_xr, sr_xr = si3.cpu().numpy(), sr3.cpu().numpy()
+        out["deep_m2_1e-1000"] = {
+            "workload": f"perturbation Mandelbrot {w3.nx}x{w3.ny} at dx=1e-1000 on a period-{w3.p} "
+                        "nucleus, 1100 digits, max_iter 1e6, interior detection eps 1e-3, dzndc",
+            "pixels": n3, "pixel_iters": int(st_fe["pixel_iters"]),
+            "fe32": {"kernel_ms": k_fe, "value": st_fe["pixel_iters"] / (k_fe * 1e-3)},
+            "xr64": {"kernel_ms": k_xr, "value": st_xr["pixel_iters"] / (k_xr * 1e-3)},
+            "speedup_fe32_vs_xr64": (st_fe["pixel_iters"] / k_fe) / (st_xr["pixel_iters"] / k_xr),
+            "fe32_vs_xr64": {"iter_count_differs_frac": float(np.mean(si_fe != si_xr)),
+                             "stop_reason_differs_frac": float(np.mean(sr_fe != sr_xr)),
+                             "iter_count_max_abs_diff": int(np.max(np.abs(
+                                 si_fe.astype(np.int64) - si_xr)))},
+            "unit": "pixel-iter/s"}
+        ref3.free()
+        del Z3, sr3, si3
 
-    # Burning Ship: 64 tiles of 256..2048 squared, one launch, FP64
-    tiles4 = syn.config4_workload(max_iter=bs_max_iter)
-    refs4, keep, ts = [], [], []
-    for t in tiles4:
-        r = nat.Reference(ctx, t.Zn, div_iter=t.div_iter, order=t.ref_order, flavor=1,
-                          calc_dzndc=True, scale_m=t.dx_m, scale_e=t.dx_e, bla=True, kc=t.kc,
-                          bla_eps=1e-6)
-        m = t.side * t.side
-        xs = torch.from_numpy(t.xs).to(dev)
-        ys = torch.from_numpy(t.ys).to(dev)
-        Z = torch.zeros((6, m), **f64)
-        sr = torch.zeros(m, dtype=torch.int8, device=dev)
-        si = torch.zeros(m, dtype=torch.int32, device=dev)
-        U = torch.zeros(m, dtype=torch.int32, device=dev)
-        keep += [xs, ys, Z, sr, si, U]
-        refs4.append(r)
-        ts.append(nat.make_tile_ptrs(nx=t.side, ny=t.side, xs_ptr=xs.data_ptr(),
-                                     ys_ptr=ys.data_ptr(), lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=6,
-                                     stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
-                                     U_ptr=U.data_ptr(), ref=r, dx_m=t.dx_m, dx_e=t.dx_e,
-                                     drift_m=t.driftx_m, drift_e=t.driftx_e,
-                                     drifty_m=t.drifty_m, drifty_e=t.drifty_e))
-    def c4(mode):
-        return nat.make_calc(max_iter=bs_max_iter, M_divergence=1000., flavor=1,
-                             calc_dzndc=True, bla=True, mode=mode)
-    si4 = keep[4::6]
-    k4f, st4f = timed(lambda: ctx.perturb_tiles(c4("fe32"), ts, nat.DEVICE), 1, 1)
-    si_fe = np.concatenate([t.cpu().numpy() for t in si4])
-    k4, st4 = timed(lambda: ctx.perturb_tiles(c4("fp64"), ts, nat.DEVICE), 1, 0)
-    si_64 = np.concatenate([t.cpu().numpy() for t in si4])
-    out["burning_ship_64_tiles"] = {
-        "workload": f"Burning Ship, 64 tiles of side 256..2048 (log-uniform), widths 1e-200..1e-30, "
-                    f"centres from the BS ball method + Newton at 250 digits, max_iter {bs_max_iter}, "
-                    "M 1e3, Hessian, one launch",
-        "pixels": int(sum(t.side ** 2 for t in tiles4)), "pixel_iters": int(st4["pixel_iters"]),
-        "periods": sorted({t.order for t in tiles4 if t.order}),
-        "kernel_ms": k4, "value": st4["pixel_iters"] / (k4 * 1e-3), "unit": "pixel-iter/s",
-        "dtype": "f64",
-        "fe32": {"kernel_ms": k4f, "value": st4f["pixel_iters"] / (k4f * 1e-3),
-                 "speedup_vs_fp64": (st4f["pixel_iters"] / k4f) / (st4["pixel_iters"] / k4),
-                 "iter_count_differs_frac": float(np.mean(si_fe != si_64))}}
-    for r in refs4:
-        r.free()
-    out["host_1100_digits"] = host_leg(syn)
+    if "bs" in legs:
+        # Burning Ship: 64 tiles of 256..2048 squared, one launch, FP64
+        tiles4 = syn.config4_workload(max_iter=bs_max_iter)[:bs_tiles]
+        refs4, keep, ts = [], [], []
+        for t in tiles4:
+            r = nat.Reference(ctx, t.Zn, div_iter=t.div_iter, order=t.ref_order, flavor=1,
+                              calc_dzndc=True, scale_m=t.dx_m, scale_e=t.dx_e, bla=True, kc=t.kc,
+                              bla_eps=1e-6)
+            m = t.side * t.side
+            xs = torch.from_numpy(t.xs).to(dev)
+            ys = torch.from_numpy(t.ys).to(dev)
+            Z = torch.zeros((6, m), **f64)
+            sr = torch.zeros(m, dtype=torch.int8, device=dev)
+            si = torch.zeros(m, dtype=torch.int32, device=dev)
+            U = torch.zeros(m, dtype=torch.int32, device=dev)
+            keep += [xs, ys, Z, sr, si, U]
+            refs4.append(r)
+            ts.append(nat.make_tile_ptrs(nx=t.side, ny=t.side, xs_ptr=xs.data_ptr(),
+                                         ys_ptr=ys.data_ptr(), lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=6,
+                                         stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
+                                         U_ptr=U.data_ptr(), ref=r, dx_m=t.dx_m, dx_e=t.dx_e,
+                                         drift_m=t.driftx_m, drift_e=t.driftx_e,
+                                         drifty_m=t.drifty_m, drifty_e=t.drifty_e))
+        def c4(mode):
+            return nat.make_calc(max_iter=bs_max_iter, M_divergence=1000., flavor=1,
+                                 calc_dzndc=True, bla=True, mode=mode)
+        si4 = keep[4::6]
+        k4f, st4f = timed(lambda: ctx.perturb_tiles(c4("fe32"), ts, nat.DEVICE), 1, 1)
+        si_fe = np.concatenate([t.cpu().numpy() for t in si4])
+        k4, st4 = timed(lambda: ctx.perturb_tiles(c4("fp64"), ts, nat.DEVICE), 1, 0)
+        si_64 = np.concatenate([t.cpu().numpy() for t in si4])
+        out["burning_ship_64_tiles"] = {
+            "workload": f"Burning Ship, {len(tiles4)} tiles of side 256..2048 (log-uniform), widths 1e-200..1e-30, "
+                        f"centres from the BS ball method + Newton at 250 digits, max_iter {bs_max_iter}, "
+                        "M 1e3, Hessian, one launch",
+            "pixels": int(sum(t.side ** 2 for t in tiles4)), "pixel_iters": int(st4["pixel_iters"]),
+            "periods": sorted({t.order for t in tiles4 if t.order}),
+            "kernel_ms": k4, "value": st4["pixel_iters"] / (k4 * 1e-3), "unit": "pixel-iter/s",
+            "dtype": "f64",
+            "fe32": {"kernel_ms": k4f, "value": st4f["pixel_iters"] / (k4f * 1e-3),
+                     "speedup_vs_fp64": (st4f["pixel_iters"] / k4f) / (st4["pixel_iters"] / k4),
+                     "iter_count_differs_frac": float(np.mean(si_fe != si_64))}}
+        for r in refs4:
+            r.free()
+    if "host" in legs:
+        out["host_1100_digits"] = host_leg(syn)
     return out
 
 
@@ -578,7 +589,8 @@ def run_ours(args):
 
     supp = None
     if not args.no_supplementary and rank == 0:
-        supp = supplementary(ctx, nat, syn, torch, dev, stream, flush, args.bs_max_iter)
+        supp = supplementary(ctx, nat, syn, torch, dev, stream, flush, args.bs_max_iter,
+                             legs=tuple(args.legs.split(",")), bs_tiles=args.bs_tiles)
 
     serving = None
     if args.serving_requests > 0 and rank == 0:
