@@ -419,7 +419,8 @@ FSG_DEV void frame_renorm(BSFrame &S) {
         S.E = En;
         frame_set_scale(S);
     }
-    const float mh = fmaxf(fmaxf(fabsf(S.h[0]), fabsf(S.h[1])), fmaxf(fabsf(S.h[2]), fabsf(S.h[3])));
+    const float mh = fmaxf(fmaxf(fabsf(S.h[0]), fabsf(S.h[1])),
+                           fmaxf(fabsf(S.h[2]), fabsf(S.h[3])));
     if (!(mh >= 0x1p-30f && mh <= 0x1p30f)) {
         if (mh < 0x1p-126f) {
             for (int k = 0; k < 4; k++) S.h[k] = 0.f;
@@ -486,7 +487,8 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
     const float xy = ux * ys;                                // xn yn
     float v1 = 0.f, dX1 = 0.f, dx1 = 0.f, v2 = 0.f, dX2 = 0.f, dx2 = 0.f;
     float vy = 0.f, dXy = 0.f, dxy = 0.f;
-    const bool use1 = flavor == 1 || flavor == 5, use2 = flavor >= 4, usey = flavor == 2 || flavor == 3;
+    const bool use1 = flavor == 1 || flavor == 5, use2 = flavor >= 4;
+    const bool usey = flavor == 2 || flavor == 3;
     const float sX = frame_sgn(X, eX), sY = frame_sgn(Y, eY);
     if (use1) {
         // P1 = X Y: 2^(eX + eY) <= |P1| < 2^(eX + eY + 2)
@@ -529,9 +531,11 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
             nxb = 2.f * ((X + xs) * h1 + Hm.y * ux * k1) - 2.f * ((Y + ys) * h3 + Hm.w * uy * k1);
         } else if (flavor == 3) {
             nxa = h0 * (xs + 2.f * X) + ux * (h0 * s + 2.f * Hm.x * k1) - Hm.z * vy * k1
-                  - Y * (Hm.z * dXy * k0 + h2 * dxy) - h2 * ab - sg * (uy * Hm.z * k1 + uy * h2 * s);
+                  - Y * (Hm.z * dXy * k0 + h2 * dxy) - h2 * ab
+                  - sg * (uy * Hm.z * k1 + uy * h2 * s);
             nxb = h1 * (xs + 2.f * X) + ux * (h1 * s + 2.f * Hm.y * k1) - Hm.w * vy * k1
-                  - Y * (Hm.w * dXy * k0 + h3 * dxy) - h3 * ab - sg * (uy * Hm.w * k1 + uy * h3 * s);
+                  - Y * (Hm.w * dXy * k0 + h3 * dxy) - h3 * ab
+                  - sg * (uy * Hm.w * k1 + uy * h3 * s);
         } else {
             const float dxa2 = h0 * (xs + 2.f * X) + ux * (h0 * s + 2.f * Hm.x * k1)
                                - h2 * (ys + 2.f * Y) - uy * (h2 * s + 2.f * Hm.z * k1);
@@ -543,8 +547,10 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
             nxb = dX2 * dXb2 + dx2 * dxb2;
         }
         if (flavor == 1 || flavor == 5) {
-            const float dxa = (h0 * uy + ux * h2) * s + h0 * Y + h2 * X + (ux * Hm.z + uy * Hm.x) * k1;
-            const float dxb = (h1 * uy + ux * h3) * s + h1 * Y + h3 * X + (ux * Hm.w + uy * Hm.y) * k1;
+            const float dxa = (h0 * uy + ux * h2) * s + h0 * Y + h2 * X
+                              + (ux * Hm.z + uy * Hm.x) * k1;
+            const float dxb = (h1 * uy + ux * h3) * s + h1 * Y + h3 * X
+                              + (ux * Hm.w + uy * Hm.y) * k1;
             const float dXa = (Hm.x * Y + X * Hm.z) * k0, dXb = (Hm.y * Y + X * Hm.w) * k0;
             nya = 2.f * (dX1 * dXa + dx1 * dxa);
             nyb = 2.f * (dX1 * dXb + dx1 * dxb);
@@ -698,7 +704,8 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                 for (;;) {
                     if (C.bla && (w & 7) == 0 && (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
                         int ib;
-                        const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E), fr_norm(Fm.uy, Fm.E), w, ib);
+                        const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E),
+                                                        fr_norm(Fm.uy, Fm.E), w, ib);
                         if (step != 0) {
                             frame_out(Fm, xn, yn, h);
                             apply_bla(step, ib);
@@ -732,8 +739,8 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                     int res = 3;
                     if (fz.x & 2) {
                         const float4 fb = __ldg(&R.bs_fa[w]);
-                        res = bs_frame_tests(Fm, fb.x, fb.y, __float_as_int(fb.z), __float_as_int(fb.w),
-                                             M2s, divr);
+                        res = bs_frame_tests(Fm, fb.x, fb.y, __float_as_int(fb.z),
+                                             __float_as_int(fb.w), M2s, divr);
                     }
                     if (res == 0) { dyn = false; continue; }
                     if (res == 1) { stop = 1; frame_out(Fm, xn, yn, h); return 0; }
@@ -860,7 +867,8 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
 // the FP32 + exponent kernels hold three 256-thread blocks per SM (at most 85
 // registers a thread)
 template <class T, int FL>
-__global__ void __launch_bounds__(256, IsDouble<T>::value ? 1 : 3) k_perturb_bs(WorkDev W, CalcDev C) {
+__global__ void __launch_bounds__(256, IsDouble<T>::value ? 1 : 3)
+k_perturb_bs(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
     unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
