@@ -469,10 +469,15 @@ def run_ours(args):
             dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e, i_dzndc=1,
             potential_ptr=pot.data_ptr(), dem_ptr=dem.data_ptr())
 
+    launch = {}    # mode -> (block, ctas_per_sm) chosen by the autotuner
+
     def calc(mode):
-        return nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=mode,
-                             calc_dzndc=True, interior=False, bla=True,
-                             xr_semantics=w.xr_mode)
+        c = nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=mode,
+                          calc_dzndc=True, interior=False, bla=True,
+                          xr_semantics=w.xr_mode)
+        if mode in launch:
+            c.block, c.ctas_per_sm = launch[mode]
+        return c
 
     def timed_steps(mode, ref, k, warm):
         t, c = tile(ref), calc(mode)
@@ -502,7 +507,12 @@ def run_ours(args):
         return (si.cpu().numpy().copy(), sr.cpu().numpy().copy(),
                 pot.cpu().numpy().copy(), dem.cpu().numpy().copy())
 
-    # headline: FP32 + exponent
+    # headline: FP32 + exponent, at the launch shape the autotuner picks on
+    # this workload (untimed: one launch per candidate)
+    from fractalshades_gb300 import tune
+    tuned = tune.autotune(ctx, calc("fe32"), [tile(refs["xr"])], perturb=True, repeats=1,
+                          store=False)
+    launch["fe32"] = (tuned["block"], tuned["ctas_per_sm"])
     with ClockSampler(local) as clk:
         step_ms, kern_ms, stats = timed_steps("fe32", refs["xr"], args.steps, args.warmup)
     fe_out = snapshot()
@@ -610,7 +620,11 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32exp",
-        "data": "synthetic", "config": config_dict(w, args),
+        "data": "synthetic",
+        "config": dict(config_dict(w, args), launch={
+            "block": tuned["block"], "ctas_per_sm": tuned["ctas_per_sm"],
+            "autotuned_over": [[e["block"], e["ctas_per_sm"], round(e["kernel_ms"], 3)]
+                               for e in tuned["table"]]}),
         "e2e": {"value": e2e_val, "unit": "pixel-iter/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(args.steps),

@@ -52,7 +52,7 @@ class Calc(ct.Structure):
         ("max_iter", I64), ("M_divergence", F64), ("epsilon_stationnary", F64),
         ("mode", I32), ("calc_dzndc", I32), ("interior", I32), ("bla", I32),
         ("flavor", I32), ("xr_semantics", I32), ("nexp", I32),
-        ("backshift", I32), ("calc_d2zndc2", I32),
+        ("backshift", I32), ("calc_d2zndc2", I32), ("block", I32), ("ctas_per_sm", I32),
     ]
 
 
@@ -432,7 +432,7 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
 
 def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
               calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False,
-              nexp=0, backshift=0, calc_d2zndc2=False):
+              nexp=0, backshift=0, calc_d2zndc2=False, block=0, ctas_per_sm=0):
     c = Calc()
     c.max_iter = int(max_iter)
     c.M_divergence = float(M_divergence)
@@ -446,4 +446,6 @@ def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
     c.nexp = int(nexp)
     c.backshift = int(backshift)
     c.calc_d2zndc2 = int(bool(calc_d2zndc2))
+    c.block = int(block)
+    c.ctas_per_sm = int(ctas_per_sm)
     return c

@@ -107,6 +107,13 @@ int ref_alloc(fsg_ctx *ctx, fsg_ref *r, T **p, size_t n) {
     return FSG_OK;
 }
 
+// threads per CTA of the kernel a calculation launches by default, and the
+// largest its launch bounds allow
+static int default_block(const fsg_calc *calc, int perturb) {
+    return (perturb && calc->flavor == 0 && calc->nexp == 0 && calc->mode == FSG_MODE_FE32) ? 128
+                                                                                             : 256;
+}
+
 void ref_release(fsg_ref *r, cudaStream_t s) {
     for (void *p : r->allocs) cudaFreeAsync(p, s);
     r->allocs.clear();
@@ -252,8 +259,9 @@ int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int n
     W.counter = ctx->counter_dev; W.stats = ctx->stats_dev;
     W.cancel = ctx->cancel_dev; W.status = ctx->status_dev;
     CalcDev C = make_calc(calc);
-    const int block = 256;
-    const int grid = 0;   // one persistent wave at the kernel's occupancy limit
+    // one persistent wave at the kernel's occupancy limit, or the tuned shape
+    const int block = calc->block > 0 ? calc->block : default_block(calc, perturb);
+    const int grid = calc->ctas_per_sm > 0 ? -calc->ctas_per_sm : 0;
     CK(cudaEventRecord(ctx->ev0, s), "cudaEventRecord");
     if (!perturb) fsg_launch_std(W, C, grid, block, s);
     else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
@@ -294,6 +302,13 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         return set_err(ctx, FSG_ERR_ARG, "calc_orbit runs in FSG_MODE_FP64 or FSG_MODE_XR64");
     if (calc->calc_d2zndc2 && (perturb || calc->flavor != 0))
         return set_err(ctx, FSG_ERR_ARG, "calc_d2zndc2 applies to the standard Mandelbrot loops");
+    {
+        const int bound = default_block(calc, perturb);
+        if (calc->block < 0 || calc->block % 32 != 0 || calc->block > bound)
+            return set_err(ctx, FSG_ERR_ARG, "block: 0 or a multiple of 32 up to the kernel's 256 "
+                                             "(128 for the FE32 power-2 kernel)");
+        if (calc->ctas_per_sm < 0) return set_err(ctx, FSG_ERR_ARG, "ctas_per_sm must be >= 0");
+    }
     for (int32_t i = 0; i < ntiles; i++) {
         int rc = check_tile(ctx, tiles[i], perturb, calc);
         if (rc != FSG_OK) return rc;

@@ -475,12 +475,13 @@ __global__ void __launch_bounds__(FE32_BLOCK, INTERIOR ? 6 : 7) k_perturb_m2_fe3
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }
 
-void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int /*block*/,
+void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
                              cudaStream_t s) {
+    const int b = (block > 0 && block <= FE32_BLOCK) ? block : FE32_BLOCK;
     if (C.interior)
-        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, FE32_BLOCK, W.total),
-                                  FE32_BLOCK, 0, s>>>(W, C);
+        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, b, W.total), b, 0,
+                                  s>>>(W, C);
     else
-        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, FE32_BLOCK, W.total),
-                                   FE32_BLOCK, 0, s>>>(W, C);
+        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, b, W.total), b, 0,
+                                   s>>>(W, C);
 }

@@ -15,6 +15,7 @@ import threading
 import numpy as np
 
 from . import settings
+from . import tune
 from . import _native as nat
 
 _ctx_lock = threading.Lock()
@@ -28,6 +29,18 @@ def context():
         if _ctx is None:
             _ctx = nat.Context(settings.gpu_device)
         return _ctx
+
+
+_dev_name = None
+
+
+def _shaped_calc(spec, perturb):
+    """The spec's calculation with the launch shape the autotuner cached for
+    its kernel kind (fractalshades_gb300.tune), if any."""
+    global _dev_name
+    if _dev_name is None:
+        _dev_name = tune._device_name(context())
+    return tune.apply(spec.calc(), perturb, _dev_name)
 
 
 def cancel():
@@ -152,7 +165,7 @@ def run_std_pixels(cycle_dep_args, cycle_indep_args):
     t = nat.make_tile(pix=pix, lin_mat=lin_mat, Z=Zw, stop_reason=stop_reason,
                       stop_iter=stop_iter, center=center, dx=dx, i_znorbit=spec.i_znorbit,
                       proj=proj)
-    rc = ctx.std_tiles(spec.calc(), [t], nat.HOST)
+    rc = ctx.std_tiles(_shaped_calc(spec, False), [t], nat.HOST)
     if Zw is not Z:
         Z[...] = Zw
     return _check_rc(rc)
@@ -191,7 +204,7 @@ def run_perturb_pixels(cycle_dep_args, cycle_indep_args):
     Zw = Z if Z.flags.c_contiguous else np.ascontiguousarray(Z)
     Uw = U if U.shape[0] > 0 else None
     t = _tile_for(args, spec, pix=pix, Z=Zw, U=Uw, sr=stop_reason, si=stop_iter)
-    rc = ctx.perturb_tiles(spec.calc(), [t], nat.HOST)
+    rc = ctx.perturb_tiles(_shaped_calc(spec, True), [t], nat.HOST)
     if Zw is not Z:
         Z[...] = Zw
     return _check_rc(rc)
@@ -218,13 +231,13 @@ def run_image(fractal, xs, ys, cycle_indep_args, potential=True):
             dem = None
         t = _tile_for(cycle_indep_args, spec, xs=xs, ys=ys, Z=Z,
                       U=U if nU else None, sr=sr, si=si, pot=pot, dem=dem)
-        rc = ctx.perturb_tiles(spec.calc(), [t], nat.HOST)
+        rc = ctx.perturb_tiles(_shaped_calc(spec, True), [t], nat.HOST)
     else:
         (_init, spec, center, proj, lin_mat, dx, interrupted) = cycle_indep_args
         t = nat.make_tile(xs=xs, ys=ys, lin_mat=lin_mat, Z=Z, stop_reason=sr, stop_iter=si,
                           center=center, dx=dx, potential=pot, dem=dem,
                           i_znorbit=spec.i_znorbit, proj=proj)
-        rc = ctx.std_tiles(spec.calc(), [t], nat.HOST)
+        rc = ctx.std_tiles(_shaped_calc(spec, False), [t], nat.HOST)
     if rc == nat.FSG_INTERRUPTED:
         return None
     return {"Z": Z, "U": U[:nU], "stop_reason": sr[0], "stop_iter": si[0],

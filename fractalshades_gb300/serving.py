@@ -38,6 +38,7 @@ import numpy as np
 
 from . import _native as nat
 from . import synthetic as syn
+from . import tune
 from .numpy_utils import xrange as fsx
 from . import settings
 
@@ -219,6 +220,8 @@ class TileServer:
         calc = nat.make_calc(max_iter=batch[0].max_iter, M_divergence=self.M, mode=self.mode,
                              calc_dzndc=True, interior=False, bla=True,
                              xr_semantics=batch[0]._view[3])
+        # the launch shape the autotuner cached for this kernel kind, if any
+        calc = tune.apply(calc, True, tune._device_name(slot.ctx))
         slot.ctx.perturb_tiles(calc, tiles, nat.DEVICE)
         with torch.cuda.stream(slot.stream):
             for req in batch:

@@ -116,6 +116,15 @@ typedef struct {
                                  derivative d2zndc2 in Z row 3
                                  (mandelbrot_M2.py:316-317,
                                  mandelbrot_Mn.py:325-333)                    */
+    int32_t block;            /* launch shape (chosen by the autotuner,
+                                 fractalshades_gb300/tune.py): threads per
+                                 CTA, 0 = the kernel's default (256; 128 for
+                                 the FE32 power-2 kernel), else a multiple of
+                                 32 up to that default                        */
+    int32_t ctas_per_sm;      /* resident CTAs per SM of the persistent grid,
+                                 0 = the occupancy limit, else at most that
+                                 many (the allocation-free entry point keeps
+                                 its fixed shape)                             */
 } fsg_calc;
 
 /* One tile: a rectangle of pixels with its own view and outputs. */
