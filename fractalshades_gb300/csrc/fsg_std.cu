@@ -21,50 +21,99 @@ __device__ __forceinline__ double2 std_c(const TileDev &T, long long ip) {
 
 // OPT: the optional outputs d2zndc2 (mandelbrot_M2.py:316-317) and the orbit
 // point n - backshift (core.py:2965-3004)
+#define FSG_STD_CHUNK 16        // steps between two block-level compaction checks
+
 template <bool OPT>
 __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    // pixel states moved by the compaction (one slot per thread)
+    __shared__ double2 s_c[256], s_zn[256], s_dzndz[256], s_dzndc[256];
+    __shared__ double2 s_d2[OPT ? 256 : 1];
+    __shared__ OrbitSnap<double2> s_S[OPT ? 256 : 1];
+    __shared__ long long s_ip[256];
+    __shared__ int s_t[256], s_n[256];
+    __shared__ int s_cnt;
     fsg_load_starts(W, s_start);
     unsigned long long it_sum = 0, steps = 0;
     const int bs = OPT ? C.backshift : 0;
     const bool d2_on = OPT && C.d2;
-    int t; long long ip;
-    // the interruption flag, polled per pixel like numba_cycles (core.py:2959-2960)
-    while (!fsg_cancelled(W) && fsg_claim(W, s_start, t, ip)) {
-        const TileDev &T = W.tiles[t];
-        long long np = (long long)T.nx * T.ny;
-        double2 c = std_c(T, ip);
-        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.), d2 = cx(0., 0.);
-        OrbitSnap<double2> S;
-        if (OPT) S.init(bs, zn);
-        int n = 0; signed char reason = -1;
-        for (;;) {
+    // One pass of the inner loop is one step of the lane's pixel; a lane
+    // whose pixel stops stores it and takes the next one within the pass.
+    // Every FSG_STD_CHUNK steps the block counts its live pixels: once the
+    // queue is empty and at most 3/4 of the threads hold one, the states move
+    // (bit for bit) to the block's first threads, so that the long pixels of
+    // the tail run in full warps -- a warp's FP64 instruction costs the pipe
+    // the same with 2 active lanes as with 32.  The interruption flag is
+    // polled per pixel, like numba_cycles (core.py:2959-2960).
+    int t = 0; long long ip = 0;
+    double2 c = cx(0., 0.), zn = c, dzndz = c, dzndc = c, d2 = c;
+    OrbitSnap<double2> S;
+    int n = 0;
+    bool have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
+    bool drained = !have;
+    if (have) { c = std_c(W.tiles[t], ip); if (OPT) S.init(bs, zn); }
+    for (;;) {
+        for (int k = 0; k < FSG_STD_CHUNK && have; k++) {
             n += 1;
+            signed char reason = -1;
             bool stop = true;
-            if (n >= C.max_iter) { reason = 0; goto snap; }
-            if (d2_on) d2 = rmul(2., cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
-            dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);
-            dzndz = cmul(rmul(2., dzndz), zn);
-            zn = cadd(cmul(zn, zn), c);
-            if (n == 1) dzndz = cx(1., 0.);
-            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; goto snap; }
-            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; goto snap; }
-            stop = false;
-        snap:
+            if (n >= C.max_iter) {
+                reason = 0;
+            } else {
+                if (d2_on) d2 = rmul(2., cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
+                dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);
+                dzndz = cmul(rmul(2., dzndz), zn);
+                zn = cadd(cmul(zn, zn), c);
+                if (n == 1) dzndz = cx(1., 0.);
+                if (zn.x * zn.x + zn.y * zn.y > C.M2) reason = 1;
+                else if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) reason = 2;
+                else stop = false;
+            }
             if (OPT && bs > 0) S.take(n, bs, zn);
-            if (stop) break;
+            if (stop) {
+                const TileDev &T = W.tiles[t];
+                const long long np = (long long)T.nx * T.ny;
+                double2 *Z = (double2 *)T.Z;
+                Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
+                if (d2_on) Z[3 * np + ip] = d2;
+                if (OPT && bs > 0) {
+                    double2 zo = S.z2;
+                    for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(cmul(zo, zo), c);   // M2_iterate
+                    Z[(long long)T.i_orb * np + ip] = zo;
+                }
+                T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
+                it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+                have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
+                if (have) {
+                    c = std_c(W.tiles[t], ip);
+                    zn = cx(0., 0.); dzndz = zn; dzndc = zn; d2 = zn; n = 0;
+                    if (OPT) S.init(bs, zn);
+                } else {
+                    drained = true;
+                }
+            }
         }
-        double2 *Z = (double2 *)T.Z;
-        Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
-        if (d2_on) Z[3 * np + ip] = d2;
-        if (OPT && bs > 0) {
-            double2 zo = S.z2;
-            for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(cmul(zo, zo), c);   // M2_iterate
-            Z[(long long)T.i_orb * np + ip] = zo;
+        const int live = __syncthreads_count(have);
+        if (live == 0) break;
+        if (__syncthreads_or(drained) && 4 * live <= 3 * (int)blockDim.x) {
+            if (threadIdx.x == 0) s_cnt = 0;
+            __syncthreads();
+            if (have) {
+                const int j = atomicAdd(&s_cnt, 1);
+                s_c[j] = c; s_zn[j] = zn; s_dzndz[j] = dzndz; s_dzndc[j] = dzndc;
+                s_ip[j] = ip; s_t[j] = t; s_n[j] = n;
+                if (OPT) { s_d2[j] = d2; s_S[j] = S; }
+            }
+            __syncthreads();
+            have = (int)threadIdx.x < live;
+            if (have) {
+                const int j = threadIdx.x;
+                c = s_c[j]; zn = s_zn[j]; dzndz = s_dzndz[j]; dzndc = s_dzndc[j];
+                ip = s_ip[j]; t = s_t[j]; n = s_n[j];
+                if (OPT) { d2 = s_d2[j]; S = s_S[j]; }
+            }
+            __syncthreads();
         }
-        T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
-        fsg_epilogue(T, C, ip, zn, hypot(dzndc.x, dzndc.y), n);
-        it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
     }
     fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
 }
@@ -80,21 +129,22 @@ __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
     const double deg = (double)nexp;
     const int bs = OPT ? C.backshift : 0;
     const bool d2_on = OPT && C.d2;
-    int t; long long ip;
-    // the interruption flag, polled per pixel like numba_cycles (core.py:2959-2960)
-    while (!fsg_cancelled(W) && fsg_claim(W, s_start, t, ip)) {
-        const TileDev &T = W.tiles[t];
-        long long np = (long long)T.nx * T.ny;
-        double2 c = std_c(T, ip);
-        double2 zn = cx(0., 0.), dzndz = cx(0., 0.), dzndc = cx(0., 0.), d2 = cx(0., 0.);
-        OrbitSnap<double2> S;
-        if (OPT) S.init(bs, zn);
-        int n = 0; signed char reason = -1;
-        for (;;) {
-            n += 1;
-            bool stop = true;
+    // lanes step together; a stopped pixel is stored and the next one taken
+    // within the pass (k_std_m2)
+    int t = 0; long long ip = 0;
+    double2 c = cx(0., 0.), zn = c, dzndz = c, dzndc = c, d2 = c;
+    OrbitSnap<double2> S;
+    int n = 0;
+    bool have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
+    if (have) { c = std_c(W.tiles[t], ip); if (OPT) S.init(bs, zn); }
+    while (have) {
+        n += 1;
+        signed char reason = -1;
+        bool stop = true;
+        if (n >= C.max_iter) {
+            reason = 0;
+        } else {
             double2 zm1, zm;
-            if (n >= C.max_iter) { reason = 0; goto snap; }
             if (d2_on) {
                 // mandelbrot_Mn.py:325-333; the reference's recurrence
                 // multiplies by dzndz where d/dc of n z^(n-1) dzndc has dzndc
@@ -111,24 +161,31 @@ __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
             dzndz = cmul(rmul(deg, dzndz), zm1);
             zn = cadd(zm, c);
             if (n == 1) dzndz = cx(1., 0.);
-            if (zn.x * zn.x + zn.y * zn.y > C.M2) { reason = 1; goto snap; }
-            if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) { reason = 2; goto snap; }
-            stop = false;
-        snap:
-            if (OPT && bs > 0) S.take(n, bs, zn);
-            if (stop) break;
+            if (zn.x * zn.x + zn.y * zn.y > C.M2) reason = 1;
+            else if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) reason = 2;
+            else stop = false;
         }
-        double2 *Z = (double2 *)T.Z;
-        Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
-        if (d2_on) Z[3 * np + ip] = d2;
-        if (OPT && bs > 0) {
-            double2 zo = S.z2;
-            for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(mn_ipow(zo, nexp), c);   // Mn_iterate
-            Z[(long long)T.i_orb * np + ip] = zo;
+        if (OPT && bs > 0) S.take(n, bs, zn);
+        if (stop) {
+            const TileDev &T = W.tiles[t];
+            const long long np = (long long)T.nx * T.ny;
+            double2 *Z = (double2 *)T.Z;
+            Z[ip] = zn; Z[np + ip] = dzndz; Z[2 * np + ip] = dzndc;
+            if (d2_on) Z[3 * np + ip] = d2;
+            if (OPT && bs > 0) {
+                double2 zo = S.z2;
+                for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(mn_ipow(zo, nexp), c);   // Mn_iterate
+                Z[(long long)T.i_orb * np + ip] = zo;
+            }
+            T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
+            it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+            have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
+            if (have) {
+                c = std_c(W.tiles[t], ip);
+                zn = cx(0., 0.); dzndz = zn; dzndc = zn; d2 = zn; n = 0;
+                if (OPT) S.init(bs, zn);
+            }
         }
-        T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
-        fsg_epilogue(T, C, ip, zn, hypot(dzndc.x, dzndc.y), n);
-        it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
     }
     fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
 }
@@ -141,24 +198,27 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
     unsigned long long it_sum = 0, steps = 0;
     const int flavor = C.flavor;
     const int bs = OPT ? C.backshift : 0;
-    int t; long long ip;
-    // the interruption flag, polled per pixel like numba_cycles (core.py:2959-2960)
-    while (!fsg_cancelled(W) && fsg_claim(W, s_start, t, ip)) {
-        const TileDev &T = W.tiles[t];
-        long long np = (long long)T.nx * T.ny;
-        double2 c = std_c(T, ip);
-        double a = c.x, b = c.y;
-        double X = 0., Y = 0., dXdA = 0., dXdB = 0., dYdA = 0., dYdB = 0.;
-        OrbitSnap<double2> S;
+    // lanes step together; a stopped pixel is stored and the next one taken
+    // within the pass (k_std_m2)
+    int t = 0; long long ip = 0;
+    double a = 0., b = 0.;
+    double X = 0., Y = 0., dXdA = 0., dXdB = 0., dYdA = 0., dYdB = 0.;
+    OrbitSnap<double2> S;
+    int n = 0;
+    bool have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
+    if (have) {
+        const double2 c = std_c(W.tiles[t], ip);
+        a = c.x; b = c.y;
         if (OPT) S.init(bs, cx(0., 0.));
-        int n = 0; signed char reason = -1;
-        for (;;) {
-            n += 1;
-            if (n >= C.max_iter) {
-                reason = 0;
-                if (OPT && bs > 0) S.take(n, bs, cx(X, Y));
-                break;
-            }
+    }
+    while (have) {
+        n += 1;
+        signed char reason = -1;
+        bool stop = true;
+        if (n >= C.max_iter) {
+            reason = 0;
+            if (OPT && bs > 0) S.take(n, bs, cx(X, Y));
+        } else {
             double nX, nY, nXa, nXb, nYa, nYb;
             if (flavor == 1) {
                 nX = X * X - Y * Y + a;
@@ -201,8 +261,12 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
             X = nX; Y = nY; dXdA = nXa; dXdB = nXb; dYdA = nYa; dYdB = nYb;
             bool esc = X * X + Y * Y > C.M2;
             if (OPT && bs > 0) S.take(n, bs, cx(X, Y));
-            if (esc) { reason = 1; break; }
+            if (esc) reason = 1;
+            else stop = false;
         }
+        if (!stop) continue;
+        const TileDev &T = W.tiles[t];
+        const long long np = (long long)T.nx * T.ny;
         double *Z = (double *)T.Z;
         Z[ip] = X; Z[np + ip] = Y; Z[2 * np + ip] = dXdA; Z[3 * np + ip] = dXdB;
         Z[4 * np + ip] = dYdA; Z[5 * np + ip] = dYdB;
@@ -217,11 +281,52 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
             Z[(long long)(T.i_orb + 1) * np + ip] = yo;
         }
         T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
-        double absd = 0.5 * (hypot(dXdA + dYdB, dXdB - dYdA) + hypot(dXdA - dYdB, dXdB + dYdA));
-        fsg_epilogue(T, C, ip, cx(X, Y), absd, n);
         it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+        have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
+        if (have) {
+            const double2 c = std_c(W.tiles[t], ip);
+            a = c.x; b = c.y;
+            X = 0.; Y = 0.; dXdA = 0.; dXdB = 0.; dYdA = 0.; dYdB = 0.; n = 0;
+            if (OPT) S.init(bs, cx(0., 0.));
+        }
     }
     fsg_flush_stats(W, it_sum, steps, 0ULL, 0ULL);
+}
+
+// Potential and distance estimate of every pixel of the launch, from the
+// values the iteration kernel stored (zn, dzndc or the Jacobian, stop_iter):
+// the same formulas on the same values as an in-loop epilogue, run here so
+// that the lanes of a warp take them together.  Within the iteration kernel a
+// pixel escapes after ~25 iterations on average and its FP64 logarithms ran
+// while the other lanes of its warp waited (8.8 of 32 lanes active).
+template <bool BS>
+__global__ void __launch_bounds__(256) k_std_epilogue(WorkDev W, CalcDev C) {
+    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    fsg_load_starts(W, s_start);
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < W.total;
+         g += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = W.ntiles - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_start[mid] <= g) lo = mid; else hi = mid - 1;
+        }
+        const TileDev &T = W.tiles[lo];
+        if (T.pot == nullptr && T.dem == nullptr) continue;
+        const long long ip = g - s_start[lo], np = (long long)T.nx * T.ny;
+        const int n = T.stop_iter[ip];
+        if (BS) {
+            const double *Z = (const double *)T.Z;
+            const double dXdA = Z[2 * np + ip], dXdB = Z[3 * np + ip];
+            const double dYdA = Z[4 * np + ip], dYdB = Z[5 * np + ip];
+            const double absd = 0.5 * (hypot(dXdA + dYdB, dXdB - dYdA) +
+                                       hypot(dXdA - dYdB, dXdB + dYdA));
+            fsg_epilogue(T, C, ip, cx(Z[ip], Z[np + ip]), absd, n);
+        } else {
+            const double2 *Z = (const double2 *)T.Z;
+            const double2 d = Z[2 * np + ip];
+            fsg_epilogue(T, C, ip, Z[ip], hypot(d.x, d.y), n);
+        }
+    }
 }
 
 template <bool OPT>
@@ -232,6 +337,12 @@ static void launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, 
         k_std_m2<OPT><<<fsg_auto_grid(k_std_m2<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
     else
         k_std_bs<OPT><<<fsg_auto_grid(k_std_bs<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+    if (C.flavor == 0)
+        k_std_epilogue<false><<<fsg_auto_grid(k_std_epilogue<false>, 0, 256, W.total), 256, 0, s>>>(
+            W, C);
+    else
+        k_std_epilogue<true><<<fsg_auto_grid(k_std_epilogue<true>, 0, 256, W.total), 256, 0, s>>>(
+            W, C);
 }
 
 void fsg_launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
