@@ -478,13 +478,16 @@ FSG_DEV float frame_sgn(float v, int e) {           // 0 for an exact 0
 // Hm 2^g (zero_ref: the zeros the loop uses right after a dynamic rebase),
 // before renormalisation.  Returns false, leaving S untouched, when the step
 // has to run in fr.
+// DEEP: s = 0 (the deltas below 2^-127), where every product of two deltas,
+// or of a delta and the Hessian, is 0 in the frame: those terms are left out.
+template <bool DEEP>
 FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, int eX, int eY,
                            float4 Hm, int g, bool zero_ref) {
-    const float s = S.s, ux = S.ux, uy = S.uy;
-    const float xs = ux * s, ys = uy * s;                    // xn, yn as floats
-    const float xx2 = ux * (xs + 2.f * X);                   // xn (xn + 2 X)
-    const float yy2 = uy * (ys + 2.f * Y);                   // yn (yn + 2 Y)
-    const float xy = ux * ys;                                // xn yn
+    const float s = DEEP ? 0.f : S.s, ux = S.ux, uy = S.uy;
+    const float xs = DEEP ? 0.f : ux * s, ys = DEEP ? 0.f : uy * s;   // xn, yn as floats
+    const float xx2 = ux * (DEEP ? 2.f * X : xs + 2.f * X);           // xn (xn + 2 X)
+    const float yy2 = uy * (DEEP ? 2.f * Y : ys + 2.f * Y);           // yn (yn + 2 Y)
+    const float xy = DEEP ? 0.f : ux * ys;                            // xn yn
     float v1 = 0.f, dX1 = 0.f, dx1 = 0.f, v2 = 0.f, dX2 = 0.f, dx2 = 0.f;
     float vy = 0.f, dXy = 0.f, dxy = 0.f;
     const bool use1 = flavor == 1 || flavor == 5, use2 = flavor >= 4;
@@ -492,7 +495,8 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
     const float sX = frame_sgn(X, eX), sY = frame_sgn(Y, eY);
     if (use1) {
         // P1 = X Y: 2^(eX + eY) <= |P1| < 2^(eX + eY + 2)
-        const float o1 = fmaf(uy, X, fmaf(ux, Y, xy));     // xn yn + xn Y + yn X
+        // xn yn + xn Y + yn X
+        const float o1 = DEEP ? fmaf(uy, X, ux * Y) : fmaf(uy, X, fmaf(ux, Y, xy));
         if (!frame_diffabs(sX * sY, eX + eY, eX + eY + 1, o1, S.E, v1, dX1, dx1)) return false;
     }
     if (use2) {
@@ -509,7 +513,7 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
     }
     // |Y + yn| and sgn(Y + yn) with sgn(0) = +1 (flavors 2, 3): the branch
     // is known here, so the sign is sgn(Y) unless |yn| dominates or Y = 0
-    const float ab = fabsf(Y + ys);
+    const float ab = DEEP ? fabsf(Y) : fabsf(Y + ys);
     const float sg = (sY != 0.f && dXy == 0.f) ? sY : (uy < 0.f ? -1.f : 1.f);
     if (hess) {
         const bool hz = zero_ref || (Hm.x == 0.f && Hm.y == 0.f && Hm.z == 0.f && Hm.w == 0.f);
@@ -526,7 +530,42 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
         }
         const float h0 = S.h[0], h1 = S.h[1], h2 = S.h[2], h3 = S.h[3];
         float nxa, nxb, nya, nyb;
-        if (flavor == 1 || flavor == 2) {
+        if (DEEP) {
+            // the same closures without the terms in s (xn = yn = 0 against X, Y)
+            if (flavor == 1 || flavor == 2) {
+                nxa = 2.f * (X * h0 + Hm.x * ux * k1) - 2.f * (Y * h2 + Hm.z * uy * k1);
+                nxb = 2.f * (X * h1 + Hm.y * ux * k1) - 2.f * (Y * h3 + Hm.w * uy * k1);
+            } else if (flavor == 3) {
+                nxa = h0 * (2.f * X) + ux * (2.f * Hm.x * k1) - Hm.z * vy * k1
+                      - Y * (Hm.z * dXy * k0 + h2 * dxy) - h2 * ab - sg * (uy * Hm.z * k1);
+                nxb = h1 * (2.f * X) + ux * (2.f * Hm.y * k1) - Hm.w * vy * k1
+                      - Y * (Hm.w * dXy * k0 + h3 * dxy) - h3 * ab - sg * (uy * Hm.w * k1);
+            } else {
+                const float dxa2 = h0 * (2.f * X) + ux * (2.f * Hm.x * k1)
+                                   - h2 * (2.f * Y) - uy * (2.f * Hm.z * k1);
+                const float dxb2 = h1 * (2.f * X) + ux * (2.f * Hm.y * k1)
+                                   - h3 * (2.f * Y) - uy * (2.f * Hm.w * k1);
+                const float dXa2 = 2.f * (X * Hm.x - Y * Hm.z) * k0;
+                const float dXb2 = 2.f * (X * Hm.y - Y * Hm.w) * k0;
+                nxa = dX2 * dXa2 + dx2 * dxa2;
+                nxb = dX2 * dXb2 + dx2 * dxb2;
+            }
+            if (flavor == 1 || flavor == 5) {
+                const float dxa = h0 * Y + h2 * X + (ux * Hm.z + uy * Hm.x) * k1;
+                const float dxb = h1 * Y + h3 * X + (ux * Hm.w + uy * Hm.y) * k1;
+                const float dXa = (Hm.x * Y + X * Hm.z) * k0, dXb = (Hm.y * Y + X * Hm.w) * k0;
+                nya = 2.f * (dX1 * dXa + dx1 * dxa);
+                nyb = 2.f * (dX1 * dXb + dx1 * dxb);
+            } else if (flavor == 2) {
+                nya = 2.f * (Hm.x * vy * k1 + X * (dXy * Hm.z * k0 + dxy * h2) + h0 * ab
+                             + sg * (ux * Hm.z * k1));
+                nyb = 2.f * (Hm.y * vy * k1 + X * (dXy * Hm.w * k0 + dxy * h3) + h1 * ab
+                             + sg * (ux * Hm.w * k1));
+            } else {
+                nya = 2.f * ((Hm.x * uy + Hm.z * ux) * k1 + X * h2 + Y * h0);
+                nyb = 2.f * ((Hm.y * uy + Hm.w * ux) * k1 + X * h3 + Y * h1);
+            }
+        } else if (flavor == 1 || flavor == 2) {
             nxa = 2.f * ((X + xs) * h0 + Hm.x * ux * k1) - 2.f * ((Y + ys) * h2 + Hm.z * uy * k1);
             nxb = 2.f * ((X + xs) * h1 + Hm.y * ux * k1) - 2.f * ((Y + ys) * h3 + Hm.w * uy * k1);
         } else if (flavor == 3) {
@@ -546,7 +585,8 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
             nxa = dX2 * dXa2 + dx2 * dxa2;
             nxb = dX2 * dXb2 + dx2 * dxb2;
         }
-        if (flavor == 1 || flavor == 5) {
+        if (DEEP) {
+        } else if (flavor == 1 || flavor == 5) {
             const float dxa = (h0 * uy + ux * h2) * s + h0 * Y + h2 * X
                               + (ux * Hm.z + uy * Hm.x) * k1;
             const float dxb = (h1 * uy + ux * h3) * s + h1 * Y + h3 * X
@@ -571,9 +611,10 @@ FSG_DEV bool bs_frame_step(int flavor, bool hess, BSFrame &S, float X, float Y, 
     } else if (flavor == 2) {
         nx = xx2 - yy2 + S.cux; ny = 2.f * (X * vy + ux * ab) - S.cuy;
     } else if (flavor == 3) {
-        nx = xx2 - Y * vy - uy * ab + S.cux; ny = 2.f * (X * uy + Y * ux + xy) - S.cuy;
+        nx = xx2 - Y * vy - uy * ab + S.cux;
+        ny = 2.f * (DEEP ? X * uy + Y * ux : X * uy + Y * ux + xy) - S.cuy;
     } else if (flavor == 4) {
-        nx = v2 + S.cux; ny = 2.f * (X * uy + Y * ux + xy) - S.cuy;
+        nx = v2 + S.cux; ny = 2.f * (DEEP ? X * uy + Y * ux : X * uy + Y * ux + xy) - S.cuy;
     } else {
         nx = v2 + S.cux; ny = 2.f * v1 - S.cuy;
     }
@@ -596,7 +637,7 @@ FSG_DEV void bs_frame_step_zero(int flavor, bool hess, BSFrame &S, float4 Hm, in
     T.cuy = S.bm * fr_p2c(S.be - En);
     if (T.F != FR_ZERO_E) T.F = S.F + En - E;
     // all diffabs arguments are 0 here: the step is always taken
-    bs_frame_step(flavor, hess, T, 0.f, 0.f, FR_ZERO_E, FR_ZERO_E, Hm, g, zero_ref);
+    bs_frame_step<false>(flavor, hess, T, 0.f, 0.f, FR_ZERO_E, FR_ZERO_E, Hm, g, zero_ref);
     S = T;
     S.E = En;
     frame_set_scale(S);
@@ -719,8 +760,13 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                         bs_frame_step_zero(flavor, hess, Fm, Hm, fz.y, dyn);
                     } else {
                         const float4 fa = __ldg(&R.bs_fa[w]);
-                        if (!bs_frame_step(flavor, hess, Fm, fa.x, fa.y, __float_as_int(fa.z),
-                                           __float_as_int(fa.w), Hm, fz.y, dyn)) {
+                        const int eX = __float_as_int(fa.z), eY = __float_as_int(fa.w);
+                        const bool ok = Fm.s == 0.f
+                            ? bs_frame_step<true>(flavor, hess, Fm, fa.x, fa.y, eX, eY, Hm,
+                                                  fz.y, dyn)
+                            : bs_frame_step<false>(flavor, hess, Fm, fa.x, fa.y, eX, eY, Hm,
+                                                   fz.y, dyn);
+                        if (!ok) {
                             frame_out(Fm, xn, yn, h);
                             return 2;
                         }
