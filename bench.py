@@ -402,6 +402,23 @@ def run_reference(args):
     return 0
 
 
+def job_seconds(rank_seconds, dist=None, device="cpu"):
+    """The job's time over its replicas: the slowest rank's (max over ranks,
+    returned on every rank); a rank's own time without a process group."""
+    if dist is None:
+        return float(rank_seconds)
+    import torch
+    t = torch.tensor([float(rank_seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(pixel_iters_per_step, steps, world, seconds):
+    """Whole-job pixel-iterations/s: every rank runs its own replica of the
+    workload (weak scaling), the job takes the slowest rank's time."""
+    return pixel_iters_per_step * steps * world / seconds
+
+
 def config_dict(w, args):
     return {"workload": "perturbation Mandelbrot 2048x2048 at dx=1e-300 on a period-p nucleus",
             "nx": w.nx, "ny": w.ny, "dx": "1e-300", "period": w.p, "digits": w.dps,
@@ -517,12 +534,8 @@ def run_ours(args):
         step_ms, kern_ms, stats = timed_steps("fe32", refs["xr"], args.steps, args.warmup)
     fe_out = snapshot()
     pix_iters = stats[-1]["pixel_iters"]
-    total_s = sum(step_ms) / 1e3
-    if dist:
-        tt = torch.tensor([total_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_s = float(tt.item())
-    value = pix_iters * args.steps * world / total_s
+    total_s = job_seconds(sum(step_ms) / 1e3, dist, dev)
+    value = job_value(pix_iters, args.steps, world, total_s)
     st = stats[-1]
     flops = st["full_steps"] * FLOPS_FULL + st["bla_steps"] * FLOPS_BLA
     kms = float(np.mean(kern_ms))
