@@ -71,6 +71,8 @@ struct fsg_ref {
     int64_t len = 0;
     int xr_paths = 0, flavor = 0, has_dzndc = 0, has_dzndz = 0;
     int nexp = 0;                 // 0: power-2 model, n: power-n model
+    int bla_req = 0;              // built with a BLA tree (empty below 8 orbit points,
+                                  // where no BLA step is ever valid)
     fsg_ref *base = nullptr;      // fsg_ref_derive_bla: owner of the shared tables
     int derived = 0;              // live references derived from this one
     cudaEvent_t ready = nullptr;  // derived references: recorded after the BLA build;
@@ -154,8 +156,8 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
             return set_err(ctx, FSG_ERR_ARG, "Xrange mode needs Xrange derivative paths");
         if (calc->mode == FSG_MODE_FP64 && t.ref->xr_paths && (calc->calc_dzndc || calc->interior))
             return set_err(ctx, FSG_ERR_ARG, "FP64 mode needs standard derivative paths");
-        if (calc->bla && t.ref->host.bla_len <= 0)
-            return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference has no BLA tree");
+        if (calc->bla && !t.ref->bla_req)
+            return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference was built without it");
     }
     if (t.dzndc_scale_e != 0 && !perturb)
         return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e applies to the perturbation loops only");
@@ -167,8 +169,8 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
             return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 and FSG_MODE_FE32");
         if (calc->calc_dzndc && !t.ref->has_dzndc)
             return set_err(ctx, FSG_ERR_ARG, "calc_hessian requested but the reference has no Jacobian paths");
-        if (calc->bla && t.ref->host.bla_len <= 0)
-            return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference has no BLA tree");
+        if (calc->bla && !t.ref->bla_req)
+            return set_err(ctx, FSG_ERR_ARG, "BLA requested but the reference was built without it");
     }
     int nZ_min = perturb ? (calc->flavor == 0 ? 1 + (calc->interior ? 1 : 0) + (calc->calc_dzndc ? 1 : 0)
                                               : (calc->calc_dzndc ? 6 : 2))
@@ -520,6 +522,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (!r) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
     r->len = len; r->flavor = d->flavor; r->xr_paths = d->xr_paths;
     r->has_dzndc = d->calc_dzndc; r->has_dzndz = (d->flavor == 0) && d->calc_dzndz;
+    r->bla_req = d->bla != 0;
     RefDev &R = r->host;
     memset(&R, 0, sizeof(R));
     R.len = len;
@@ -686,6 +689,7 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
     if (!r) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
     r->len = base->len; r->flavor = base->flavor; r->xr_paths = base->xr_paths;
     r->has_dzndc = base->has_dzndc; r->has_dzndz = base->has_dzndz;
+    r->bla_req = 1;
     r->nexp = base->nexp;
     r->base = base;
     RefDev &R = r->host;

@@ -743,7 +743,8 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             auto frame_run = [&]() -> int {
                 int4 fz = __ldg(&R.bs_fz[w]);
                 for (;;) {
-                    if (C.bla && (w & 7) == 0 && (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
+                    if (C.bla && R.bla_len > 0 && (w & 7) == 0 &&
+                        (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
                         int ib;
                         const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E),
                                                         fr_norm(Fm.uy, Fm.E), w, ib);
@@ -811,7 +812,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             }
         }
         if (!stepped) {
-            if (C.bla && !bla_done && (w & 7) == 0) {
+            if (C.bla && R.bla_len > 0 && !bla_done && (w & 7) == 0) {
                 int ib;
                 // the reference compares the double value of |dz| (0 when it
                 // underflows, perturbation.py:1123-1135)

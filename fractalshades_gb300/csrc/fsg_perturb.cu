@@ -54,7 +54,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
 
     for (;;) {
         // BLA step :1121-1154
-        if (C.bla && (w & 7) == 0) {
+        if (C.bla && R.bla_len > 0 && (w & 7) == 0) {
             int ib;
             int step = bla_lookup(R, hypot(zn.x, zn.y), w, ib);
             if (step != 0) {

@@ -440,8 +440,7 @@ def _bs_nucleus(kind, real_axis):
 
 
 @pytest.mark.parametrize("dx", [1e-9, 1e-45])
-@pytest.mark.parametrize("kind,real_axis", [(1, True), (1, False), (2, False), (3, False),
-                                            (4, False), (5, False)])
+@pytest.mark.parametrize("kind,real_axis", [(k, r) for k in (1, 2, 3, 4, 5) for r in (True, False)])
 def test_perturb_bs_fe32_vs_fp64_every_flavor(ctx, kind, real_axis, dx):
     """The FP32 + exponent Burning Ship loop (fr values and their frame form)
     against the FP64 kernel on the same reference and tile, every flavor,
