@@ -77,7 +77,10 @@ typedef struct {
     int32_t calc_dzndz;       /* build dZndz (M2, interior detection)            */
     double scale_m;           /* dx * projection.scale as a float64 Xrange       */
     int32_t scale_e;
-    int32_t bla;              /* build the BLA tree                              */
+    int32_t bla;              /* build the BLA tree (empty below 8 orbit points,
+                                 where no BLA step is valid: a calculation with
+                                 bla on then takes full steps only, as the
+                                 reference's ref_BLA_get does)                */
     double kc;                /* to_standard(kc) (perturbation.py:1830)          */
     double bla_eps;
     int32_t nexp;             /* flavor 0 only: 0 = the power-2 model
@@ -95,7 +98,8 @@ typedef struct {
     int32_t mode;             /* FSG_MODE_*                                      */
     int32_t calc_dzndc;       /* M2: dzndc; BS: calc_hessian                     */
     int32_t interior;         /* M2 interior_detect (dzndz)                      */
-    int32_t bla;              /* BLA_activated                                   */
+    int32_t bla;              /* BLA_activated: every tile's reference must have
+                                 been created with fsg_ref_desc.bla            */
     int32_t flavor;           /* 0 = M2, 1..5 Burning Ship                       */
     int32_t xr_semantics;     /* FE32 only: follow the Xrange branch's rebase
                                  confirmation (reference xr_detect_activated)    */
