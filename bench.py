@@ -284,6 +284,30 @@ def traffic_per_launch(nx):
     return int(rec["bytes_per_launch"]) if nx == 2048 else None
 
 
+# algorithmic bytes per pixel of a headline launch: the outputs zn and
+# dzndc (complex128), U and stop_iter (int32), stop_reason (int8), potential
+# and DEM (float64); the orbit tables are read once and stay in L2
+BYTES_PER_PIXEL = 16 + 16 + 4 + 4 + 1 + 8 + 8
+
+
+def hbm_roofline(npix, naxes, kernel_ms, traffic):
+    """The launch against the HBM roofline: algorithmic bytes (outputs and
+    the pixel axes) over the kernel time, against the measured copy bandwidth
+    of this pool (6.8 TB/s fallback).  The kernel is bound by instruction
+    issue, so this fraction is small by construction."""
+    peak, src = 6800.0, "fallback (one earlier GB300 measurement)"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "measured copy bandwidth of this pool"
+    except (OSError, ValueError, KeyError):
+        pass
+    nbytes = npix * BYTES_PER_PIXEL + 8 * naxes
+    achieved = nbytes / (kernel_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": nbytes,
+            "peak_source": src}
+
+
 class ClockSampler:
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -648,6 +672,7 @@ def run_ours(args):
                      "flops_per_step": {"full": FLOPS_FULL, "bla": FLOPS_BLA},
                      "executed_steps": {"full": st["full_steps"], "bla": st["bla_steps"]},
                      "kernel_ms": kms},
+        "roofline_hbm": hbm_roofline(n, w.nx + w.ny, kms, traffic_per_launch(args.nx)),
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "paths": {
