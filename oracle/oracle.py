@@ -2,8 +2,8 @@
 ctypes front-end of the CPU oracle (fs_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
-bench.py's CPU-baseline leg, as the checker.  The product package never imports
-it.  Array conventions follow the reference: complex128 arrays, Z[nZ, npts],
+bench.py's CPU-baseline leg, as the result the GPU path is compared with.  The
+product package never imports it.  Array conventions follow the reference: complex128 arrays, Z[nZ, npts],
 U int32[nU, npts], stop_reason int8[1, npts], stop_iter int32[1, npts].
 """
 import ctypes as ct

@@ -1,7 +1,7 @@
 """
 CPU restatement of the reference's field-lines and DEM-normal post-processing
--- TEST INFRASTRUCTURE (only tests use it), the checker of
-csrc/fsg_postproc.cu.
+-- TEST INFRASTRUCTURE (only tests use it): what the tests compare
+csrc/fsg_postproc.cu with.
 
 Follows src/fractalshades/postproc.py of the reference: Continuous_iter_pp's
 context (:352-406, :1001-1009), Fieldlines_pp (:409-530) with
