@@ -24,6 +24,7 @@ FSG_ERR_NODEV = -4
 FSG_ERR_LIMIT = -5
 FSG_NOALLOC_MAX_TILES = 64
 FSG_MN_MAX_EXP = 32
+FSG_MAX_ITER_LIMIT = (1 << 30) - 1
 
 MODE_FP64 = 0
 MODE_XR64 = 1

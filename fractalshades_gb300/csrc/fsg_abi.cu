@@ -289,8 +289,8 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         }
         return FSG_OK;
     }
-    if (calc->max_iter <= 0 || calc->max_iter > INT_MAX / 2)
-        return set_err(ctx, FSG_ERR_ARG, "max_iter out of range (1 .. 2^30)");
+    if (calc->max_iter <= 0 || calc->max_iter > FSG_MAX_ITER_LIMIT)
+        return set_err(ctx, FSG_ERR_ARG, "max_iter out of range (1 .. 2^30 - 1)");
     if (calc->flavor < 0 || calc->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
     if (calc->mode < 0 || calc->mode > 2) return set_err(ctx, FSG_ERR_ARG, "bad mode");
     {

@@ -21,6 +21,10 @@
 //   * the first call on a device resolves the array's device address with that
 //     device current (cudaGetSymbolAddress); make that first call before any
 //     stream capture.
+// The descriptors reach the array as the parameter of a small upload kernel
+// launched on the caller's stream (about 17 KB, inside the 32 KB parameter
+// limit), so no host-to-device copy from the caller's stack is involved and
+// the call never waits for the stream.
 #include <cstddef>
 #include <cstring>
 #include <mutex>
@@ -39,9 +43,35 @@ struct NoallocScratch {
     TileDev tiles[FSG_NOALLOC_MAX_TILES];
 };
 
+// What the upload kernel receives by value: the tile offsets and descriptors
+struct NoallocUpload {
+    long long start[FSG_NOALLOC_MAX_TILES + 1];
+    TileDev tiles[FSG_NOALLOC_MAX_TILES];
+    int ntiles;
+};
+static_assert(sizeof(NoallocUpload) <= 32000, "upload parameter beyond the kernel parameter limit");
+static_assert(sizeof(TileDev) % 8 == 0, "descriptors are copied as 8-byte words");
+
 }  // namespace
 
 static __device__ __align__(256) unsigned char fsg_noalloc_scratch[sizeof(NoallocScratch)];
+
+// Clears the counter, statistics, status and cancel words and copies the
+// call's descriptors into the array (device code names the array directly).
+static __global__ void __launch_bounds__(256) k_noalloc_upload(const NoallocUpload u) {
+    NoallocScratch *S = reinterpret_cast<NoallocScratch *>(fsg_noalloc_scratch);
+    if (threadIdx.x == 0) {
+        S->counter = 0ULL;
+        for (int k = 0; k < 4; k++) S->stats[k] = 0ULL;
+        S->status = 0;
+        S->cancel = 0;
+    }
+    for (int i = threadIdx.x; i <= u.ntiles; i += blockDim.x) S->start[i] = u.start[i];
+    const int words = u.ntiles * (int)(sizeof(TileDev) / 8);
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(u.tiles);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(S->tiles);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
 
 namespace {
 
@@ -68,7 +98,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
                                      int32_t ntiles, void *stream) {
     if (!calc || !tiles || ntiles <= 0) return FSG_ERR_ARG;
     if (ntiles > FSG_NOALLOC_MAX_TILES) return FSG_ERR_LIMIT;
-    if (calc->max_iter <= 0 || calc->max_iter > (1 << 30)) return FSG_ERR_ARG;
+    if (calc->max_iter <= 0 || calc->max_iter > FSG_MAX_ITER_LIMIT) return FSG_ERR_ARG;
     if (calc->flavor < 0 || calc->flavor > 5) return FSG_ERR_ARG;
     if (calc->nexp != 0 && (calc->flavor != 0 || calc->nexp < 2)) return FSG_ERR_ARG;
     if (calc->nexp > FSG_MN_MAX_EXP) return FSG_ERR_LIMIT;
@@ -80,7 +110,8 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     NoallocScratch *S = nullptr;
     if (scratch_address(device, &S) != cudaSuccess) return FSG_ERR_CUDA;
 
-    NoallocScratch host;            // descriptors staged on the caller's stack
+    NoallocUpload host;             // the upload kernel's parameter
+    host.ntiles = ntiles;
     long long total = 0;
     host.start[0] = 0;
     for (int32_t i = 0; i < ntiles; i++) {
@@ -101,12 +132,14 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
         host.start[i + 1] = total;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    // counter, statistics, status and cancel word must start at zero
-    if (cudaMemsetAsync(S, 0, offsetof(NoallocScratch, start), s) != cudaSuccess) return FSG_ERR_CUDA;
-    if (cudaMemcpyAsync(S->start, host.start, sizeof(long long) * (ntiles + 1),
-                        cudaMemcpyHostToDevice, s) != cudaSuccess) return FSG_ERR_CUDA;
-    if (cudaMemcpyAsync(S->tiles, host.tiles, sizeof(TileDev) * ntiles,
-                        cudaMemcpyHostToDevice, s) != cudaSuccess) return FSG_ERR_CUDA;
+    // An error left pending by the caller's earlier CUDA work on this thread
+    // is consumed here, so that the status below reports this call's own
+    // launches only.
+    (void)cudaGetLastError();
+    // counter, statistics, status and cancel word cleared, descriptors
+    // copied: the launch carries them as its parameter
+    k_noalloc_upload<<<1, 256, 0, s>>>(host);
+    if (cudaGetLastError() != cudaSuccess) return FSG_ERR_CUDA;
     WorkDev W;
     W.tiles = S->tiles; W.start = S->start; W.ntiles = ntiles; W.total = total;
     W.counter = &S->counter; W.stats = S->stats;

@@ -51,6 +51,8 @@ extern "C" {
 #define FSG_MODE_FE32 2  /* float mantissa + int32 exponent deltas (fast form)           */
 
 #define FSG_MN_MAX_EXP 32  /* largest exponent of the power-n model                      */
+#define FSG_MAX_ITER_LIMIT 0x3fffffff  /* largest max_iter, 2^30 - 1: n + a BLA step stays
+                                        * inside int32 */
 
 /* where the tile buffers live */
 #define FSG_HOST 0       /* host pointers: the library stages the copies            */
@@ -295,6 +297,13 @@ int fsg_clear_cancel(fsg_ctx *ctx);
  *     other streams or host threads, race on it;
  *   - the first call on a device resolves the array's address with that device
  *     current; make that first call before any stream capture;
+ *   - the descriptors travel as the parameter of a small upload kernel on
+ *     `stream`: the call makes no host-to-device copy and does not wait for
+ *     the stream;
+ *   - an error left pending by earlier CUDA work of the calling thread is
+ *     consumed on entry (cudaGetLastError), so FSG_ERR_CUDA reports this
+ *     call's own launches;
+ *   - max_iter in 1 .. FSG_MAX_ITER_LIMIT, like fsg_std_tiles;
  *   - not cancellable (fsg_cancel does not apply). */
 #define FSG_NOALLOC_MAX_TILES 64
 int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,

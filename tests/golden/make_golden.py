@@ -30,7 +30,9 @@ floating point operation once, in source order, with IEEE rounding, which is
 what the oracle restates (the jitted reference may contract some operations
 into FMAs under ``fastmath=True``).
 
-Usage: python tests/golden/make_golden.py [reference_src_dir]
+Usage: python tests/golden/make_golden.py <reference_src_dir> [case]
+(or the source directory in $FRACTALSHADES_SRC: the reference's ``src``
+folder, the one holding the ``fractalshades`` package).
 Writes tests/golden/*.npz (small fixtures, committed).
 """
 import os
@@ -42,7 +44,10 @@ import numpy as np
 import mpmath
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+REF_SRC = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FRACTALSHADES_SRC")
+if not REF_SRC or not os.path.isdir(os.path.join(REF_SRC, "fractalshades")):
+    sys.exit("usage: make_golden.py <reference_src_dir> [case]  (the folder that holds the "
+             "reference's fractalshades package; or set FRACTALSHADES_SRC)")
 
 
 # --------------------------------------------------------------------------

@@ -84,6 +84,90 @@ def test_noalloc_matches_std_tiles_twice(flavor, center, dx):
             assert np.array_equal(got[k].view(np.uint8), expected[k].view(np.uint8)), (call, k)
 
 
+def test_noalloc_several_tiles_pix_and_power_n():
+    """Three tiles of different sizes in one call -- a rectangle, an explicit
+    list of pixel positions (pix) and a smaller rectangle -- on the power-3
+    model: the per-tile offsets, the pix input and the power-n kernel all go
+    through the allocation-free path; bit-exact against fsg_std_tiles, twice."""
+    torch = pytest.importorskip("torch")
+    from fractalshades_gb300 import _native as nat
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    L = nat.load()
+    L.fsg_std_tiles_noalloc.argtypes = [ct.POINTER(nat.Calc), ct.POINTER(nat.Tile), ct.c_int32,
+                                        ct.c_void_p]
+    calc = nat.make_calc(max_iter=500, M_divergence=1000., epsilon_stationnary=0.01, nexp=3)
+    a, nza = _device_case(torch, dev, 200, 150, 0)
+    c, nzc = _device_case(torch, dev, 64, 48, 0)
+    rng = np.random.default_rng(11)
+    npix = 777
+    pos = (rng.uniform(-0.5, 0.5, npix) + 1j * rng.uniform(-0.5, 0.5, npix)).astype(np.complex128)
+    pix = torch.from_numpy(pos.view(np.float64).copy()).to(dev)
+    b = {"Z": torch.zeros((3, 2 * npix), dtype=torch.float64, device=dev),
+         "sr": torch.zeros(npix, dtype=torch.int8, device=dev),
+         "si": torch.zeros(npix, dtype=torch.int32, device=dev),
+         "pot": torch.zeros(npix, dtype=torch.float64, device=dev),
+         "dem": torch.zeros(npix, dtype=torch.float64, device=dev)}
+    tb = _tile(nat, dict(b, xs=pix, ys=pix), npix, 1, 3, -0.2 + 0.1j, 2.5)
+    tb.xs, tb.ys, tb.pix = None, None, pix.data_ptr()
+    tiles_py = [_tile(nat, a, 200, 150, nza, 0.1 + 0.2j, 2.8), tb,
+                _tile(nat, c, 64, 48, nzc, -0.6 + 0.6j, 0.3)]
+    bufs = [a, b, c]
+
+    ctx = nat.Context(0)
+    ctx.std_tiles(calc, tiles_py, nat.DEVICE)
+    ctx.sync()
+    expected = [_snapshot(x) for x in bufs]
+    ctx.close()
+    assert any((e["sr"] == 1).any() and (e["sr"] != 1).any() for e in expected)
+
+    stream = torch.cuda.current_stream(dev)
+    tiles = (nat.Tile * 3)(*tiles_py)
+    for call in range(2):
+        for x in bufs:
+            for k in ("Z", "pot", "dem"):
+                x[k].fill_(-7.0)
+            x["sr"].fill_(99)
+            x["si"].fill_(-1)
+        torch.cuda.synchronize(dev)
+        rc = L.fsg_std_tiles_noalloc(ct.byref(calc), tiles, 3, ct.c_void_p(stream.cuda_stream))
+        assert rc == nat.FSG_OK, f"call {call}: code {rc}"
+        torch.cuda.synchronize(dev)
+        for i, x in enumerate(bufs):
+            got = _snapshot(x)
+            for k in expected[i]:
+                assert np.array_equal(got[k].view(np.uint8), expected[i][k].view(np.uint8)), \
+                    (call, i, k)
+
+
+def test_noalloc_max_iter_bound_matches_std_tiles():
+    """Both entry points accept max_iter up to FSG_MAX_ITER_LIMIT and refuse
+    the next value."""
+    torch = pytest.importorskip("torch")
+    from fractalshades_gb300 import _native as nat
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    L = nat.load()
+    L.fsg_std_tiles_noalloc.argtypes = [ct.POINTER(nat.Calc), ct.POINTER(nat.Tile), ct.c_int32,
+                                        ct.c_void_p]
+    b, nZ = _device_case(torch, dev, 16, 16, 0)
+    t = _tile(nat, b, 16, 16, nZ, 20. + 20.j, 1.0)      # every pixel escapes at once
+    tiles = (nat.Tile * 1)(t)
+    stream = torch.cuda.current_stream(dev)
+    ctx = nat.Context(0)
+    try:
+        for mi, ok in ((nat.FSG_MAX_ITER_LIMIT, True), (nat.FSG_MAX_ITER_LIMIT + 1, False)):
+            calc = nat.make_calc(max_iter=mi, M_divergence=1000.)
+            rc = L.fsg_std_tiles_noalloc(ct.byref(calc), tiles, 1, ct.c_void_p(stream.cuda_stream))
+            assert (rc == nat.FSG_OK) == ok, (mi, rc)
+            rc2 = L.fsg_std_tiles(ctx.h, ct.byref(calc), tiles, 1, nat.DEVICE)
+            assert (rc2 == nat.FSG_OK) == ok, (mi, rc2)
+            torch.cuda.synchronize(dev)
+            ctx.sync()
+    finally:
+        ctx.close()
+
+
 def test_noalloc_rejects_too_many_tiles():
     pytest.importorskip("torch")
     from fractalshades_gb300 import _native as nat
