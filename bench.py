@@ -47,10 +47,15 @@ def parse():
                     help="requests of the serving stream (0: skip)")
     ap.add_argument("--no-supplementary", action="store_true",
                     help="skip the standard-loop, 1e-1000 and Burning Ship configurations")
-    ap.add_argument("--legs", default="std,deep,bs,host",
-                    help="supplementary configurations to run (std, deep, bs, host)")
+    ap.add_argument("--legs", default="std,deep,edge,bs,host",
+                    help="supplementary configurations to run (std, deep, edge, bs, host)")
     ap.add_argument("--bs-tiles", type=int, default=64,
                     help="Burning Ship tiles of the 64 to run (a smaller case for profiling)")
+    ap.add_argument("--parity-pixels", type=int, default=262144,
+                    help="seeded pixels of the headline image checked against the oracle "
+                         "(0: skip)")
+    ap.add_argument("--edge-nx", type=int, default=1024,
+                    help="side of the boundary-straddling view (supplementary leg 'edge')")
     ap.add_argument("--bs-max-iter", type=int, default=2000,
                     help="max_iter of the Burning Ship configuration (its own is 5e4: "
                          "minutes in FP64 on one GPU)")
@@ -95,7 +100,8 @@ def serving_leg(n_requests, device):
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
-                  legs=("std", "deep", "bs", "host"), bs_tiles=64):
+                  legs=("std", "deep", "edge", "bs", "host"), bs_tiles=64, edge_nx=1024,
+                  parity_pixels=16384):
     """The other measured configurations, one launch each (kernel time from
     the library's CUDA events, L2 flushed before each launch):
     the standard loop (800 x 600, width 3) "std", the 1e-1000 zoom with
@@ -164,10 +170,24 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
             return nat.make_calc(max_iter=w3.max_iter, M_divergence=w3.M, epsilon_stationnary=1e-3,
                                  mode=mode, calc_dzndc=True, interior=True, bla=True,
                                  xr_semantics=w3.xr_mode)
+        idx3 = sample_indices(n3, parity_pixels, 13)
+        idx3_dev = torch.from_numpy(idx3).to(dev)
         k_fe, st_fe = timed(lambda: ctx.perturb_tiles(c3("fe32"), [t3], nat.DEVICE), 3, 1)
         si_fe, sr_fe = si3.cpu().numpy().copy(), sr3.cpu().numpy().copy()
+        s_fe = gather_outputs(idx3_dev, Z3, si3, sr3, 2)
         k_xr, st_xr = timed(lambda: ctx.perturb_tiles(c3("xr64"), [t3], nat.DEVICE), 1, 0)
         si_xr, sr_xr = si3.cpu().numpy(), sr3.cpu().numpy()
+        s_xr = gather_outputs(idx3_dev, Z3, si3, sr3, 2)
+        if parity_pixels > 0:
+            t0 = time.perf_counter()
+            o3 = oracle_pixels(w3, idx3, oracle_kw(w3, interior=True, eps_stat=1e-3))
+            par3 = {"sample": f"{idx3.size} seeded random pixels", "oracle_s": time.perf_counter() - t0,
+                    "oracle": "strict C restatement, Xrange branch, interior detection",
+                    "fe32": parity_table(s_fe, o3, w3.M), "xr64": parity_table(s_xr, o3, w3.M),
+                    "stop_reasons_oracle": {str(k): int(v) for k, v in zip(
+                        *np.unique(o3["sr"], return_counts=True))}}
+        else:
+            par3 = None
         out["deep_m2_1e-1000"] = {
             "workload": f"perturbation Mandelbrot {w3.nx}x{w3.ny} at dx=1e-1000 on a period-{w3.p} "
                         "nucleus, 1100 digits, max_iter 1e6, interior detection eps 1e-3, dzndc",
@@ -179,9 +199,13 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
                              "stop_reason_differs_frac": float(np.mean(sr_fe != sr_xr)),
                              "iter_count_max_abs_diff": int(np.max(np.abs(
                                  si_fe.astype(np.int64) - si_xr)))},
+            "vs_oracle": par3,
             "unit": "pixel-iter/s"}
         ref3.free()
         del Z3, sr3, si3
+
+    if "edge" in legs:
+        out["edge_m2_p2562"] = edge_leg(ctx, nat, syn, torch, dev, timed, edge_nx, parity_pixels)
 
     if "bs" in legs:
         # Burning Ship: 64 tiles of 256..2048 squared, one launch, FP64
@@ -229,6 +253,79 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
             r.free()
     if "host" in legs:
         out["host_1100_digits"] = host_leg(syn)
+    return out
+
+
+def edge_leg(ctx, nat, syn, torch, dev, timed, nx, parity_pixels):
+    """The boundary-straddling view of the headline's period-2562 nucleus:
+    width 1.6e-9 (about four times its size estimate), max_iter 2e5, BLA on,
+    dzndc, potential and DEM; about half the pixels escape.  The reference
+    runs its FP64 branch at this width: FE32 and FP64 are compared with the
+    oracle's FP64 branch, XR64 with the oracle's Xrange branch on the same
+    view (the branch forced), on a seeded pixel sample.  Two oracle-only rows
+    give the scale of the differences: the Xrange branch against the FP64
+    branch, and the FP64 branch against itself with every pixel's c offset
+    moved by a relative 2^-24 (one FP32 rounding)."""
+    we = syn.edge_workload(nx=nx)
+    wx = syn.edge_workload(nx=nx, xr_mode=True)
+    n = we.nx * we.ny
+    f64 = dict(dtype=torch.float64, device=dev)
+    refs = {}
+    for key, wk in (("std", we), ("xr", wx)):
+        refs[key] = nat.Reference(ctx, wk.Zn, div_iter=wk.div_iter, order=wk.order,
+                                  xr_idx=wk.xr_idx, xr_m=wk.xr_m, xr_e=wk.xr_e,
+                                  xr_paths=(key == "xr"), calc_dzndc=True, scale_m=wk.dx_m,
+                                  scale_e=wk.dx_e, bla=True, kc=wk.kc, bla_eps=1e-6)
+    xs = torch.from_numpy(we.xs).to(dev)
+    ys = torch.from_numpy(we.ys).to(dev)
+    Z = torch.zeros((2, n, 2), **f64)
+    sr = torch.zeros(n, dtype=torch.int8, device=dev)
+    si = torch.zeros(n, dtype=torch.int32, device=dev)
+    U = torch.zeros(n, dtype=torch.int32, device=dev)
+    pot = torch.zeros(n, **f64)
+    dem = torch.zeros(n, **f64)
+    idx = sample_indices(n, parity_pixels, 17)
+    idx_dev = torch.from_numpy(idx).to(dev)
+    out = {"workload": f"perturbation Mandelbrot {we.nx}x{we.ny} at dx=1.6e-9 on the period-"
+                       f"{we.p} nucleus of the headline (400 digits), max_iter 2e5, BLA eps 1e-6, "
+                       "dzndc, potential, DEM", "pixels": n}
+    samples = {}
+    for form, key, wk, xsem in (("fe32", "std", we, False), ("fp64", "std", we, False),
+                                ("xr64", "xr", wx, True)):
+        t = nat.make_tile_ptrs(nx=wk.nx, ny=wk.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
+                               lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=2,
+                               stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
+                               U_ptr=U.data_ptr(), ref=refs[key], dx_m=wk.dx_m, dx_e=wk.dx_e,
+                               drift_m=wk.drift_m, drift_e=wk.drift_e, i_dzndc=1,
+                               potential_ptr=pot.data_ptr(), dem_ptr=dem.data_ptr())
+        c = nat.make_calc(max_iter=wk.max_iter, M_divergence=wk.M, mode=form, calc_dzndc=True,
+                          interior=False, bla=True, xr_semantics=xsem)
+        kms, st = timed(lambda: ctx.perturb_tiles(c, [t], nat.DEVICE), 1 if form == "fe32" else 1,
+                        1 if form == "fe32" else 0)
+        samples[form] = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
+        srn = sr.cpu().numpy()
+        out[form] = {"kernel_ms": kms, "value": st["pixel_iters"] / (kms * 1e-3),
+                     "pixel_iters": int(st["pixel_iters"]), "escaped_frac": float(np.mean(srn == 1))}
+    out["speedup_fe32_vs_fp64"] = out["fe32"]["value"] / out["fp64"]["value"]
+    out["speedup_fe32_vs_xr64"] = out["fe32"]["value"] / out["xr64"]["value"]
+    for r in refs.values():
+        r.free()
+    if parity_pixels > 0:
+        t0 = time.perf_counter()
+        kw = oracle_kw(we)
+        o_std = oracle_pixels(we, idx, kw)
+        o_xr = oracle_pixels(wx, idx, oracle_kw(wx))
+        o_shift = oracle_pixels(we, idx, dict(kw, lin_mat=LIN * (1. + 2. ** -24)))
+        out["vs_oracle"] = {
+            "sample": f"{idx.size} seeded random pixels",
+            "oracle": "strict C restatement; FP64 branch (the reference's at this width) and "
+                      "Xrange branch",
+            "oracle_s": time.perf_counter() - t0,
+            "fe32_vs_fp64_branch": parity_table(samples["fe32"], o_std, we.M),
+            "fp64_vs_fp64_branch": parity_table(samples["fp64"], o_std, we.M),
+            "xr64_vs_xrange_branch": parity_table(samples["xr64"], o_xr, we.M),
+            "oracle_xrange_vs_fp64_branch": parity_table(o_xr, o_std, we.M),
+            "oracle_c_offset_2^-24_vs_fp64_branch": parity_table(o_shift, o_std, we.M)}
     return out
 
 
@@ -360,43 +457,162 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU leg: the oracle (C restatement of the reference's loop) on host cores
+# CPU legs: the oracle (C restatement of the reference's loop) on host cores
 # ---------------------------------------------------------------------------
-def cpu_sample(w, target_s=10.0, threads=None):
-    """Time the oracle's Xrange-branch loop (the reference's branch at
-    dx = 1e-300) on a seeded random sample of pixels, on all host cores."""
+CPU_TILE = 200          # the reference's tile side (settings.py:34)
+
+
+def oracle_kw(w, interior=False, eps_stat=0.):
+    """Orbit-derived inputs of the oracle for a power-2 workload (BLA tree,
+    derivative paths), the reference's branch given by ``w.xr_mode``."""
     from oracle import oracle as orc
-    threads = threads or os.cpu_count() or 1
     Mb, rb, _, st = orc.make_bla_m2(w.Zn, w.kc, 1e-6)
     dz = orc.dzndc_path_m2(w.Zn, w.div_iter, w.order, w.xr_mode, w.dx_m, w.dx_e,
                            w.xr_idx, w.xr_m, w.xr_e)
     kw = dict(Zn=w.Zn, ref_div_iter=w.div_iter, ref_order=w.order, lin_mat=LIN,
               dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e,
-              max_iter=w.max_iter, M=w.M, eps_stat=0., xr_mode=w.xr_mode,
-              bla=(Mb, rb, st), dZndc=dz, xr_idx=w.xr_idx, xr_m=w.xr_m, xr_e=w.xr_e)
-    rng = np.random.default_rng(7)
+              max_iter=w.max_iter, M=w.M, eps_stat=eps_stat, xr_mode=w.xr_mode,
+              bla=(Mb, rb, st), dZndc=dz, xr_idx=w.xr_idx, xr_m=w.xr_m, xr_e=w.xr_e,
+              interior=interior)
+    if interior:
+        kw["dZndz"] = orc.dzndz_path_m2(w.Zn, w.div_iter, w.xr_mode, w.xr_idx, w.xr_m, w.xr_e)
+    return kw
 
-    def chunk(n):
-        ix = rng.integers(0, w.nx, n)
-        iy = rng.integers(0, w.ny, n)
-        return w.xs[ix] + 1j * w.ys[iy]
 
-    # calibrate on a small chunk, then size the sample to ~target_s
-    t0 = time.perf_counter()
-    _, _, _, si = orc.perturb_m2(chunk(64), **kw)
-    dt = max(time.perf_counter() - t0, 1e-4)
-    per_px = dt / 64
-    n_total = int(max(threads * 64, min(2_000_000, target_s * threads / per_px)))
-    per = max(1, n_total // threads)
-    chunks = [chunk(per) for _ in range(threads)]
+def oracle_threads():
+    return os.cpu_count() or 1
+
+
+def oracle_pixels(w, idx, kw, threads=None, fast=False):
+    """The oracle at flat pixel indices ``idx`` (row-major, x fastest) of the
+    workload's image, split over host threads (ctypes releases the GIL).
+    Returns stop_iter, stop_reason, zn, dzndc (and dzndz with interior)."""
+    from oracle import oracle as orc
+    threads = threads or oracle_threads()
+    pix = w.xs[idx % w.nx] + 1j * w.ys[idx // w.nx]
+    parts = np.array_split(np.arange(idx.size), max(1, min(threads * 4, idx.size)))
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(lambda ii: orc.perturb_m2(pix[ii], fast=fast, **kw), parts))
+    Z = np.concatenate([r[0] for r in res], axis=1)
+    out = {"si": np.concatenate([r[3][0] for r in res]),
+           "sr": np.concatenate([r[2][0] for r in res]),
+           "zn": Z[0], "dzndc": Z[-1]}
+    return out
+
+
+def potential_dem(zn, dzndc, n, M, d=2.):
+    """Potential (postproc.py:352-406, Continuous_iter_pp_infinity
+    :1001-1009 with a_d = 1) and distance estimate (postproc.py:684-731)
+    from the raw outputs, in float64: the formula of the kernels' fused
+    epilogue, applied to the oracle's outputs."""
+    with np.errstate(all="ignore"):
+        az = np.abs(zn)
+        x = np.log(np.log(az) / np.log(M)) / np.log(d)
+        q = np.floor(x)
+        pot = (n.astype(np.float64) - q) - (x - q)
+        dem = az * np.log(az) / np.abs(dzndc)
+    return pot, dem
+
+
+def parity_table(gpu, ref, M):
+    """Per output, one GPU form against the oracle on the same pixels:
+    iteration counts, stop reasons, and -- on the pixels whose counts agree --
+    the largest relative error of zn and dzndc, and on those that escaped
+    (stop reason 1) of the potential and the distance estimate."""
+    si, so = gpu["si"].astype(np.int64), ref["si"].astype(np.int64)
+    d = np.abs(si - so)
+    same = d == 0
+    esc = same & (ref["sr"] == 1) & (gpu["sr"] == 1)
+
+    def rel(a, b, m):
+        with np.errstate(all="ignore"):
+            r = np.abs(a - b) / np.abs(b)
+        r = r[m & np.isfinite(r)]
+        return (float(r.max()), float(np.median(r))) if r.size else (0.0, 0.0)
+    pg, dg = potential_dem(gpu["zn"], gpu["dzndc"], gpu["si"], M)
+    pg, dg = gpu.get("pot", pg), gpu.get("dem", dg)      # the kernel's own epilogue
+    po, do = potential_dem(ref["zn"], ref["dzndc"], ref["si"], M)
+    t = {"pixels": int(si.size), "escaped": int((ref["sr"] == 1).sum()),
+         "iter_count_differs_frac": float(np.mean(~same)),
+         "iter_count_max_abs_diff": int(d.max()) if d.size else 0,
+         "iter_count_differs_by_more_than_1_frac": float(np.mean(d > 1)),
+         "stop_reason_differs_frac": float(np.mean(gpu["sr"] != ref["sr"]))}
+    for k, (a, b, m) in {"zn": (gpu["zn"], ref["zn"], same),
+                         "dzndc": (gpu["dzndc"], ref["dzndc"], same),
+                         "potential": (pg, po, esc), "dem": (dg, do, esc)}.items():
+        mx, md = rel(a, b, m)
+        t[k + "_max_rel_err"], t[k + "_median_rel_err"] = mx, md
+    return t
+
+
+def sample_indices(n, k, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(k, n), replace=False)).astype(np.int64)
+
+
+def gather_outputs(idx_dev, Z, si, sr, i_dzndc, pot=None, dem=None):
+    """A GPU form's outputs at the sampled pixels (device gather, one copy);
+    with ``pot`` / ``dem`` the kernel's own fused potential and distance
+    estimate."""
+    zn = Z[0].index_select(0, idx_dev).cpu().numpy()
+    dz = Z[i_dzndc].index_select(0, idx_dev).cpu().numpy()
+    out = {"si": si.index_select(0, idx_dev).cpu().numpy(),
+           "sr": sr.index_select(0, idx_dev).cpu().numpy(),
+           "zn": zn[:, 0] + 1j * zn[:, 1], "dzndc": dz[:, 0] + 1j * dz[:, 1]}
+    if pot is not None:
+        out["pot"] = pot.index_select(0, idx_dev).cpu().numpy()
+    if dem is not None:
+        out["dem"] = dem.index_select(0, idx_dev).cpu().numpy()
+    return out
+
+
+def image_tiles(nx, ny, side=CPU_TILE):
+    """The reference's tiling of an image (core.py:1767-1830): origins and
+    sizes of the side x side tiles, row-major."""
+    return [(x0, y0, min(side, nx - x0), min(side, ny - y0))
+            for y0 in range(0, ny, side) for x0 in range(0, nx, side)]
+
+
+def cpu_baseline(w, target_s=10.0, threads=None, seed=7, min_tiles=4, n_tiles=None, kw=None):
+    """The reference's CPU path restated: the -ffast-math oracle
+    (numba fastmath=True, perturbation.py:988, 1075) over a seeded subset of
+    whole 200 x 200 tiles of the image, one tile per task on a pool of one
+    thread per host core (mthreading.py:48-68).  The subset is ``n_tiles``
+    tiles, or sized from a one-tile calibration to about ``target_s`` of wall
+    time (at least ``min_tiles`` and 1 % of the image)."""
+    threads = threads or oracle_threads()
+    kw = kw or oracle_kw(w)
+    tiles = image_tiles(w.nx, w.ny)
+    order = np.random.default_rng(seed).permutation(len(tiles))
+
+    def run_tile(k):
+        x0, y0, tx, ty = tiles[k]
+        X, Y = np.meshgrid(w.xs[x0:x0 + tx], w.ys[y0:y0 + ty])
+        from oracle import oracle as orc
+        return orc.perturb_m2((X + 1j * Y).ravel(), fast=True, **kw)[3]
+
+    if n_tiles is None:
+        t0 = time.perf_counter()
+        run_tile(order[0])
+        per_tile = max(time.perf_counter() - t0, 1e-3)
+        n_tiles = int(max(min_tiles, min(len(tiles), target_s * threads / per_tile)))
+        n_tiles = max(n_tiles, int(np.ceil(0.01 * len(tiles))))
+    k = min(int(n_tiles), len(tiles))
+    pick = order[:k]
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        res = list(ex.map(lambda p: orc.perturb_m2(p, **kw)[3], chunks))
+        res = list(ex.map(run_tile, pick))
     dt = time.perf_counter() - t0
-    iters = float(sum(r.sum() for r in res))
+    iters = float(sum(float(r.sum()) for r in res))
+    npx = int(sum(r.size for r in res))
     return {"value": iters / dt, "unit": "pixel-iter/s", "cores": threads, "kind": "port",
-            "sample": f"{per * threads} random pixels of the 2048x2048 image "
-                      f"({iters:.3e} pixel-iterations, {dt:.2f} s), Xrange branch, BLA on"}
+            "sample": f"{k} of the {len(tiles)} whole {CPU_TILE}x{CPU_TILE} tiles of the "
+                      f"{w.nx}x{w.ny} image (seeded, {100.0 * npx / (w.nx * w.ny):.1f} % of the "
+                      f"pixels, {iters:.3e} pixel-iterations in {dt:.2f} s), one tile per task "
+                      f"on {threads} threads; Xrange branch, BLA on",
+            "build": "oracle/fs_oracle.c at -O2 -ffast-math -fno-tree-vectorize "
+                     "(libfs_oracle_fast.so)",
+            "tiles": k, "extrapolated_full_image_s": dt * (w.nx * w.ny) / max(npx, 1)}
 
 
 def run_reference(args):
@@ -408,8 +624,11 @@ def run_reference(args):
     from fractalshades_gb300 import synthetic as syn
     w = syn.config2_workload(nx=args.nx)
     vals = []
+    kw = oracle_kw(w)
+    n_tiles = None          # sized once, by the first (warm-up) step's calibration
     for s in range(args.warmup + args.steps):
-        r = cpu_sample(w, target_s=4.0)
+        r = cpu_baseline(w, target_s=3.0, seed=7 + s, n_tiles=n_tiles, kw=kw)
+        n_tiles = r["tiles"]
         if s >= args.warmup:
             vals.append(r["value"])
     v = float(np.median(vals))
@@ -419,7 +638,8 @@ def run_reference(args):
             "dtype": "f64+i32exp", "data": "synthetic",
             "config": config_dict(w, args),
             "cpu_baseline": {"value": v, "unit": "pixel-iter/s", "cores": r["cores"],
-                             "kind": "port", "sample": r["sample"]},
+                             "kind": "port", "sample": "per step: " + r["sample"],
+                             "build": r["build"]},
             "e2e": {"value": v, "unit": "pixel-iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -501,6 +721,10 @@ def run_ours(args):
     pot = torch.zeros(n, **f64)
     dem = torch.zeros(n, **f64)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    # seeded pixels of the image whose outputs are checked against the oracle
+    idx = sample_indices(n, args.parity_pixels, 11)
+    idx_dev = torch.from_numpy(idx).to(dev)
+    samples = {}
 
     def tile(ref):
         return nat.make_tile_ptrs(
@@ -557,6 +781,7 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         step_ms, kern_ms, stats = timed_steps("fe32", refs["xr"], args.steps, args.warmup)
     fe_out = snapshot()
+    samples["fe32"] = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
     pix_iters = stats[-1]["pixel_iters"]
     total_s = job_seconds(sum(step_ms) / 1e3, dist, dev)
     value = job_value(pix_iters, args.steps, world, total_s)
@@ -569,7 +794,9 @@ def run_ours(args):
     k64 = max(1, min(2, args.steps))
     xr_step, xr_kern, xr_stats = timed_steps("xr64", refs["xr"], k64, 1)
     xr_out = snapshot()
+    samples["xr64"] = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
     fp_step, fp_kern, fp_stats = timed_steps("fp64", refs["std"], k64, 1)
+    samples["fp64"] = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
     value_xr = xr_stats[-1]["pixel_iters"] / (np.mean(xr_step) / 1e3)
     value_fp = fp_stats[-1]["pixel_iters"] / (np.mean(fp_step) / 1e3)
     fl64 = xr_stats[-1]["full_steps"] * FLOPS_FULL + xr_stats[-1]["bla_steps"] * FLOPS_BLA
@@ -637,7 +864,9 @@ def run_ours(args):
     supp = None
     if not args.no_supplementary and rank == 0:
         supp = supplementary(ctx, nat, syn, torch, dev, stream, flush, args.bs_max_iter,
-                             legs=tuple(args.legs.split(",")), bs_tiles=args.bs_tiles)
+                             legs=tuple(args.legs.split(",")), bs_tiles=args.bs_tiles,
+                             edge_nx=args.edge_nx,
+                             parity_pixels=min(16384, args.parity_pixels))
 
     serving = None
     if args.serving_requests > 0 and rank == 0:
@@ -648,9 +877,20 @@ def run_ours(args):
             dist.barrier()
         return 0
 
+    # the headline's outputs against the oracle (the reference's Xrange
+    # branch at this width) on the sampled pixels, per form and output
+    parity = None
+    if idx.size:
+        t0 = time.perf_counter()
+        o2 = oracle_pixels(w, idx, oracle_kw(w))
+        parity = {"sample": f"{idx.size} seeded random pixels of the {w.nx}x{w.ny} image",
+                  "oracle": "strict C restatement of the reference's loop, Xrange branch",
+                  "oracle_s": time.perf_counter() - t0,
+                  "forms": {k: parity_table(v, o2, w.M) for k, v in samples.items()}}
+
     cpu = None
     if world == 1 and not args.no_cpu:
-        cpu = cpu_sample(w, target_s=10.0)
+        cpu = cpu_baseline(w, target_s=10.0)
 
     line = {
         "metric": METRIC, "value": value, "unit": "pixel-iter/s", "n_gpus": world,
@@ -684,6 +924,7 @@ def run_ours(args):
             "speedup_fe32_vs_fp64": value / value_fp if value_fp else None,
         },
         "accuracy_fe32_vs_xr64": accuracy,
+        "parity_vs_oracle": parity,
         "serving": serving,
         "supplementary": supp,
         "tile_latency_ms": {"p50": float(np.percentile(lat, 50)),

@@ -439,12 +439,22 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             }
         }
     }
-    // end of iterations (:1375-1385)
+    // end of iterations (:1375-1385): the read-out sums in double (Xrange),
+    // from the double forms of the orbit and of the reference derivative
     fe dzf = as_fe(s.ux, s.uy, s.E);
     double2 zn = cadd(fe_to_d(dzf), __ldg(&R.Zn[w]));
     double2 dzc = cx(0., 0.);
     // dzndc in the tile's unit: the reference's scale times 2^dzs
-    if (dzndc_on) dzc = fe_to_d(fe_scale2(fe_add(as_fe(s.vx, s.vy, s.F), ld_fe(R.dZndc_f, w)), T.dzs));
+    if (dzndc_on) {
+        const xc v = (s.F == FE_ZERO_E || (s.vx == 0.f && s.vy == 0.f))
+                         ? xc_zero() : xc_make((double)s.vx, (double)s.vy, s.F);
+        const xc D = R.dZndc_xm ? xc_make(__ldg(&R.dZndc_xm[w]).x, __ldg(&R.dZndc_xm[w]).y,
+                                          __ldg(&R.dZndc_xe[w]))
+                                : xr_from(__ldg(&R.dZndc[w]));
+        xc t = xr_add(v, D);
+        t.e += T.dzs;
+        dzc = xr_to_std(t);
+    }
     double2 *Z = (double2 *)T.Z;
     Z[ip] = zn;
     if (dzndz_on) Z[T.i_dzndz * np + ip] = xrsem ? cx(0., 0.) : fe_to_d(as_fe(s.qx, s.qy, s.G));

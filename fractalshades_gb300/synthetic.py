@@ -115,17 +115,21 @@ def image_axes(nx, ny, xy_ratio=1.0, chunk=None):
     return np.ascontiguousarray(xs), np.ascontiguousarray(ys)
 
 
-def prepare_m2(*, p, dps, dx, nx, ny=None, max_iter, M=1000., center=None, offset=(0, 0)):
+def prepare_m2(*, p, dps, dx, nx, ny=None, max_iter, M=1000., center=None, offset=(0, 0),
+               xr_mode=None):
     """Orbit and view for a power-2 Mandelbrot perturbation render centred on
     the period-p nucleus (or ``center``), shifted by ``offset`` (in units of
-    dx).  The reference point is the nucleus; the orbit wraps at p."""
+    dx).  The reference point is the nucleus; the orbit wraps at p.
+    ``xr_mode``: the Xrange branch on or off whatever the width (None: the
+    reference's switch, dx < settings.xrange_zoom_level)."""
     ny = ny or nx
     with mpmath.workdps(dps):
         c = center if center is not None else nucleus(p, dps)
         dxm = mpmath.mpf(dx)
         view = c + mpmath.mpc(offset[0], offset[1]) * dxm
         prec = mpmath.mp.prec
-        xr_mode = dxm < settings.xrange_zoom_level
+        if xr_mode is None:
+            xr_mode = dxm < settings.xrange_zoom_level
         ref_len = min(p, max_iter + 1)
         Zn = np.empty(ref_len, dtype=np.complex128)
         if ref_len == max_iter + 1:
@@ -184,6 +188,17 @@ def config1_workload():
     xs, ys = image_axes(nx, ny, nx / ny)
     return StdWorkload(nx=nx, ny=ny, center=-0.5 + 0j, dx=3.0, max_iter=1000, M=1000.,
                        eps=0.01, xs=xs, ys=ys)
+
+
+def edge_workload(nx=1024, max_iter=200000, xr_mode=None, seed=2):
+    """The period-2562 nucleus of ``config2_workload`` at width 1.6e-9, about
+    four times its nucleus size estimate (3.9e-10, FP_loop.pyx:457-604): the
+    minibrot and its surroundings, where about half the pixels escape after
+    2.6e3 .. 2e5 iterations.  A boundary-straddling correctness view (the
+    1e-300 image is interior everywhere)."""
+    p = int(np.random.default_rng(seed).integers(300, 3001))
+    return prepare_m2(p=p, dps=400, dx="1.6e-9", nx=nx, max_iter=max_iter, M=1000.,
+                      xr_mode=xr_mode)
 
 
 def config3_workload(seed=3, nx=4096, max_iter=1000000):

@@ -15,8 +15,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfs_oracle.so")
+FAST_LIB_PATH = os.path.join(HERE, "_build", "libfs_oracle_fast.so")
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 P = ct.c_void_p
 I32, I64, F64 = ct.c_int32, ct.c_int64, ct.c_double
@@ -26,17 +27,19 @@ def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
-def lib():
-    global _lib
+def lib(fast=False):
+    """The strict build (the parity checker), or with ``fast`` the
+    -ffast-math build that times the CPU baseline (oracle/Makefile)."""
     with _lock:
-        if _lib is None:
+        if fast not in _libs:
+            path = FAST_LIB_PATH if fast else LIB_PATH
             src = os.path.join(HERE, "fs_oracle.c")
-            if (not os.path.exists(LIB_PATH)
-                    or os.path.getmtime(LIB_PATH) < os.path.getmtime(src)):
+            if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
                 build()
-            _lib = ct.CDLL(LIB_PATH)
-            _declare(_lib)
-        return _lib
+            L = ct.CDLL(path)
+            _declare(L)
+            _libs[fast] = L
+        return _libs[fast]
 
 
 class PM2Args(ct.Structure):
@@ -253,9 +256,10 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
                drift_m, drift_e, max_iter, M, eps_stat, xr_mode,
                calc_dzndc=True, interior=False, bla=None, dZndc=None,
                dZndz=None, xr_idx=None, xr_m=None, xr_e=None,
-               carryover=False, Z0=None, nexp=0, backshift=0):
+               carryover=False, Z0=None, nexp=0, backshift=0, fast=False):
     """bla: (M_bla complex flat, r_bla, stages) or None.  dZndc / dZndz are
-    complex arrays (standard form) or (mantissa, exp) tuples (Xrange form)."""
+    complex arrays (standard form) or (mantissa, exp) tuples (Xrange form).
+    fast: the -ffast-math build (timing only)."""
     pix = _c(pix, np.complex128)
     n = pix.size
     Zn = _c(Zn, np.complex128)
@@ -314,7 +318,7 @@ def perturb_m2(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
     U = np.zeros((1, n), dtype=np.int32)
     si = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
-    lib().orc_perturb_m2(ct.byref(a), n, _p(pix), _p(Z), nZ, _p(U), _p(sr), _p(si))
+    lib(fast).orc_perturb_m2(ct.byref(a), n, _p(pix), _p(Z), nZ, _p(U), _p(sr), _p(si))
     return Z, U, sr, si
 
 

@@ -233,8 +233,11 @@ import fractalshades.numpy_utils.xrange as fsx   # noqa: E402
 # --------------------------------------------------------------------------
 # Helpers
 # --------------------------------------------------------------------------
-def mp_orbit(c, max_iter, M, need_xr, ref_orbit_len):
-    """mpmath restatement of FP_loop.pyx:274-421 (orbit stored as float64)."""
+def mp_orbit(c, max_iter, M, need_xr, ref_orbit_len, xr_threshold=None):
+    """mpmath restatement of FP_loop.pyx:274-421 (orbit stored as float64).
+    ``xr_threshold``: the side-table threshold; FP_loop.pyx:143 reads
+    settings.xrange_zoom_level once, when the module is imported."""
+    tshold = fs.settings.xrange_zoom_level if xr_threshold is None else xr_threshold
     orbit = np.zeros(ref_orbit_len, dtype=np.complex128)
     z = mpmath.mpc(0)
     xr_dict = {}
@@ -247,7 +250,7 @@ def mp_orbit(c, max_iter, M, need_xr, ref_orbit_len):
         abs_i = np.hypot(x, y)
         if abs_i > M:
             break
-        if need_xr and abs_i < fs.settings.xrange_zoom_level:
+        if need_xr and abs_i < tshold:
             xr_dict[i] = fsx.mpc_to_Xrange(z)
     if i == ref_orbit_len - 1 and abs_i <= M:
         i += 1
@@ -311,13 +314,13 @@ def mp_nucleus(p, dps, seed_frac=0.):
         return c
 
 
-def store_orbit(f, ref_point, order, max_iter, M):
+def store_orbit(f, ref_point, order, max_iter, M, xr_threshold=None):
     """Store an orbit where the reference looks for it (perturbation.py:256-274)."""
     ref_orbit_len = max_iter + 1
     if order is not None:
         ref_orbit_len = min(order, ref_orbit_len)
     i, orbit, xr_dict = mp_orbit(ref_point, max_iter, 2 * M,
-                                 f.xr_detect_activated, ref_orbit_len)
+                                 f.xr_detect_activated, ref_orbit_len, xr_threshold)
     init_kwargs = f.init_kwargs
     del init_kwargs["directory"]
     FP_params = {
@@ -402,7 +405,27 @@ def golden_std_bs(out):
 
 def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
                       interior, bla_eps=1e-6, eps_stat=1e-3, M=1000.,
-                      ref_shift=0j, x_offset="0", backshift=0, projection=None):
+                      ref_shift=0j, x_offset="0", backshift=0, projection=None,
+                      xr_zoom_level=None):
+    """``xr_zoom_level``: settings.xrange_zoom_level while the view is set up
+    and iterated (the Xrange branch then runs at widths below it); the orbit's
+    side table keeps the import-time threshold 1e-300 (FP_loop.pyx:143)."""
+    saved = fs.settings.xrange_zoom_level
+    if xr_zoom_level is not None:
+        fs.settings.xrange_zoom_level = xr_zoom_level
+    try:
+        _golden_perturb_m2(out, x=x, y=y, dx=dx, nx=nx, precision=precision, order=order,
+                           max_iter=max_iter, interior=interior, bla_eps=bla_eps,
+                           eps_stat=eps_stat, M=M, ref_shift=ref_shift, x_offset=x_offset,
+                           backshift=backshift, projection=projection,
+                           xr_threshold=None if xr_zoom_level is None else saved)
+    finally:
+        fs.settings.xrange_zoom_level = saved
+
+
+def _golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
+                       interior, bla_eps, eps_stat, M, ref_shift, x_offset, backshift,
+                       projection, xr_threshold):
     with tempfile.TemporaryDirectory() as d:
         f = fsm.Perturbation_mandelbrot(d)
         x = str(mpmath.mpf(x) + mpmath.mpf(x_offset))
@@ -411,7 +434,7 @@ def golden_perturb_m2(out, *, x, y, dx, nx, precision, order, max_iter,
         ref_point = mpmath.mpc(x, y) + mpmath.mpc(ref_shift) * mpmath.mpf(dx)
         f.max_iter = max_iter
         f.M_divergence = M
-        FP_params, orbit = store_orbit(f, ref_point, order, max_iter, M)
+        FP_params, orbit = store_orbit(f, ref_point, order, max_iter, M, xr_threshold)
         f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
                        M_divergence=M, epsilon_stationnary=eps_stat,
                        BLA_eps=bla_eps, interior_detect=interior,
@@ -945,8 +968,46 @@ def mn_cases():
     print("pert_mn4_xr done", flush=True)
 
 
+def p2562_cases(nx_edge=16, nx_edge_xr=4):
+    """The period-2562 nucleus at 400 digits of the 2048 x 2048, dx = 1e-300
+    workload (seed 2), read from fractalshades_gb300/data/nuclei.json where
+    the Newton + ball-method search stored it; max_iter 2e5, BLA eps 1e-6,
+    escape radius 1e3, dzndc.
+      * p2562_1e300: the workload's own width, the Xrange branch, every
+        pixel interior (78 periods, BLA stages up to 11);
+      * p2562_edge: width 1.6e-9, about four times the nucleus size estimate
+        (3.9e-10): the minibrot and its surroundings, about half the pixels
+        escaping after 2.6e3 .. 2e5 iterations; FP64 branch;
+      * p2562_edge_xr: the same view on the Xrange branch
+        (settings.xrange_zoom_level raised to 1e-5), on a coarser grid (the
+        Xrange branch runs ~50x slower as plain Python).
+    About an hour of CPU in all (16 + 256 + 16 pixels)."""
+    import json
+    dps = 400
+    mpmath.mp.dps = dps
+    nuc = os.path.join(os.path.dirname(os.path.dirname(HERE)), "fractalshades_gb300", "data",
+                       "nuclei.json")
+    with open(nuc) as fh:
+        rec = json.load(fh)["2562:400"]
+    x, y = rec[0], rec[1]
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_p2562_1e300.npz"), x=x, y=y, dx="1.e-300", nx=4,
+        precision=dps, order=2562, max_iter=200000, interior=False)
+    print("pert_m2_p2562_1e300 done", flush=True)
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_p2562_edge.npz"), x=x, y=y, dx="1.6e-9", nx=nx_edge,
+        precision=dps, order=2562, max_iter=200000, interior=False)
+    print("pert_m2_p2562_edge done", flush=True)
+    golden_perturb_m2(
+        os.path.join(HERE, "pert_m2_p2562_edge_xr.npz"), x=x, y=y, dx="1.6e-9", nx=nx_edge_xr,
+        precision=dps, order=2562, max_iter=200000, interior=False, xr_zoom_level=1e-5)
+    print("pert_m2_p2562_edge_xr done", flush=True)
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "opts":
+    if len(sys.argv) > 2 and sys.argv[2] == "p2562":
+        p2562_cases()
+    elif len(sys.argv) > 2 and sys.argv[2] == "opts":
         opts_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "expmap":
         expmap_cases()
