@@ -47,8 +47,9 @@ def parse():
                     help="requests of the serving stream (0: skip)")
     ap.add_argument("--no-supplementary", action="store_true",
                     help="skip the standard-loop, 1e-1000 and Burning Ship configurations")
-    ap.add_argument("--legs", default="std,deep,edge,bs,host",
-                    help="supplementary configurations to run (std, deep, edge, bs, host)")
+    ap.add_argument("--legs", default="std,deep,edge,seahorse,bs,host",
+                    help="supplementary configurations to run (std, deep, edge, seahorse, bs, "
+                         "host)")
     ap.add_argument("--bs-tiles", type=int, default=64,
                     help="Burning Ship tiles of the 64 to run (a smaller case for profiling)")
     ap.add_argument("--parity-pixels", type=int, default=262144,
@@ -56,6 +57,9 @@ def parse():
                          "(0: skip)")
     ap.add_argument("--edge-nx", type=int, default=1024,
                     help="side of the boundary-straddling view (supplementary leg 'edge')")
+    ap.add_argument("--no-headline", action="store_true",
+                    help="run the supplementary legs only (a profiling case: no headline "
+                         "steps, no bench line)")
     ap.add_argument("--bs-max-iter", type=int, default=2000,
                     help="max_iter of the Burning Ship configuration (its own is 5e4: "
                          "minutes in FP64 on one GPU)")
@@ -100,7 +104,7 @@ def serving_leg(n_requests, device):
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
-                  legs=("std", "deep", "edge", "bs", "host"), bs_tiles=64, edge_nx=1024,
+                  legs=("std", "deep", "edge", "seahorse", "bs", "host"), bs_tiles=64, edge_nx=1024,
                   parity_pixels=16384):
     """The other measured configurations, one launch each (kernel time from
     the library's CUDA events, L2 flushed before each launch):
@@ -205,7 +209,23 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
         del Z3, sr3, si3
 
     if "edge" in legs:
-        out["edge_m2_p2562"] = edge_leg(ctx, nat, syn, torch, dev, timed, edge_nx, parity_pixels)
+        # the headline's nucleus at width 1.6e-9: the minibrot and its
+        # surroundings, about half the pixels escape (FP64 branch at this
+        # width; XR64 on the same view with the Xrange branch forced)
+        we = syn.edge_workload(nx=edge_nx)
+        out["edge_m2_p2562"] = view_leg(
+            ctx, nat, torch, dev, timed, we, syn.edge_workload(nx=edge_nx, xr_mode=True),
+            min(parity_pixels, 8192), 17,
+            f"perturbation Mandelbrot {we.nx}x{we.ny} at dx=1.6e-9 on the period-{we.p} nucleus "
+            "of the headline (400 digits), max_iter 2e5, BLA eps 1e-6, dzndc, potential, DEM")
+
+    if "seahorse" in legs:
+        ws = syn.seahorse_workload(nx=1024)
+        out["seahorse_m2"] = view_leg(
+            ctx, nat, torch, dev, timed, ws, None, min(parity_pixels, 16384), 19,
+            "perturbation Mandelbrot 1024x1024, seahorse valley -0.743643887037151 + "
+            "0.131825904205330i, width 2e-9, reference at the centre (no period), max_iter 6000, "
+            "every pixel escapes (median 1061 iterations)")
 
     if "bs" in legs:
         # Burning Ship: 64 tiles of 256..2048 squared, one launch, FP64
@@ -256,25 +276,25 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
     return out
 
 
-def edge_leg(ctx, nat, syn, torch, dev, timed, nx, parity_pixels):
-    """The boundary-straddling view of the headline's period-2562 nucleus:
-    width 1.6e-9 (about four times its size estimate), max_iter 2e5, BLA on,
-    dzndc, potential and DEM; about half the pixels escape.  The reference
-    runs its FP64 branch at this width: FE32 and FP64 are compared with the
-    oracle's FP64 branch, XR64 with the oracle's Xrange branch on the same
-    view (the branch forced), on a seeded pixel sample.  Two oracle-only rows
-    give the scale of the differences: the Xrange branch against the FP64
-    branch, and the FP64 branch against itself with every pixel's c offset
-    moved by a relative 2^-24 (one FP32 rounding)."""
-    we = syn.edge_workload(nx=nx)
-    wx = syn.edge_workload(nx=nx, xr_mode=True)
+def view_leg(ctx, nat, torch, dev, timed, we, wx, parity_pixels, seed, workload):
+    """One view in the three forms, one launch each (L2 flushed, kernel time
+    from the library's events): FE32 and FP64 on the reference's branch for
+    the view's width (``we``), XR64 on the Xrange branch (``wx``, the same
+    view with the branch forced; skipped when None).  On a seeded pixel
+    sample the outputs are compared with the oracle per output: FE32 and
+    FP64 with the oracle's branch of ``we``, XR64 with the oracle's Xrange
+    branch; two oracle-only rows give the scale of the differences (the
+    Xrange branch against the other, and the oracle against itself with
+    every pixel's c offset moved by a relative 2^-24, one FP32 rounding)."""
     n = we.nx * we.ny
     f64 = dict(dtype=torch.float64, device=dev)
     refs = {}
     for key, wk in (("std", we), ("xr", wx)):
+        if wk is None:
+            continue
         refs[key] = nat.Reference(ctx, wk.Zn, div_iter=wk.div_iter, order=wk.order,
                                   xr_idx=wk.xr_idx, xr_m=wk.xr_m, xr_e=wk.xr_e,
-                                  xr_paths=(key == "xr"), calc_dzndc=True, scale_m=wk.dx_m,
+                                  xr_paths=bool(wk.xr_mode), calc_dzndc=True, scale_m=wk.dx_m,
                                   scale_e=wk.dx_e, bla=True, kc=wk.kc, bla_eps=1e-6)
     xs = torch.from_numpy(we.xs).to(dev)
     ys = torch.from_numpy(we.ys).to(dev)
@@ -284,48 +304,54 @@ def edge_leg(ctx, nat, syn, torch, dev, timed, nx, parity_pixels):
     U = torch.zeros(n, dtype=torch.int32, device=dev)
     pot = torch.zeros(n, **f64)
     dem = torch.zeros(n, **f64)
-    idx = sample_indices(n, parity_pixels, 17)
+    idx = sample_indices(n, parity_pixels, seed)
     idx_dev = torch.from_numpy(idx).to(dev)
-    out = {"workload": f"perturbation Mandelbrot {we.nx}x{we.ny} at dx=1.6e-9 on the period-"
-                       f"{we.p} nucleus of the headline (400 digits), max_iter 2e5, BLA eps 1e-6, "
-                       "dzndc, potential, DEM", "pixels": n}
+    out = {"workload": workload, "pixels": n}
     samples = {}
-    for form, key, wk, xsem in (("fe32", "std", we, False), ("fp64", "std", we, False),
-                                ("xr64", "xr", wx, True)):
+    forms = [("fe32", "std", we), ("fp64", "std", we)]
+    if wx is not None:
+        forms.append(("xr64", "xr", wx))
+    for form, key, wk in forms:
+        mode = form if not (form == "fp64" and wk.xr_mode) else "xr64"
         t = nat.make_tile_ptrs(nx=wk.nx, ny=wk.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
                                lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=2,
                                stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
                                U_ptr=U.data_ptr(), ref=refs[key], dx_m=wk.dx_m, dx_e=wk.dx_e,
                                drift_m=wk.drift_m, drift_e=wk.drift_e, i_dzndc=1,
                                potential_ptr=pot.data_ptr(), dem_ptr=dem.data_ptr())
-        c = nat.make_calc(max_iter=wk.max_iter, M_divergence=wk.M, mode=form, calc_dzndc=True,
-                          interior=False, bla=True, xr_semantics=xsem)
-        kms, st = timed(lambda: ctx.perturb_tiles(c, [t], nat.DEVICE), 1 if form == "fe32" else 1,
-                        1 if form == "fe32" else 0)
+        c = nat.make_calc(max_iter=wk.max_iter, M_divergence=wk.M, mode=mode, calc_dzndc=True,
+                          interior=False, bla=True, xr_semantics=bool(wk.xr_mode))
+        warm = 1 if form == "fe32" else 0
+        kms, st = timed(lambda: ctx.perturb_tiles(c, [t], nat.DEVICE), 3 if form == "fe32" else 1,
+                        warm)
         samples[form] = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
         srn = sr.cpu().numpy()
         out[form] = {"kernel_ms": kms, "value": st["pixel_iters"] / (kms * 1e-3),
-                     "pixel_iters": int(st["pixel_iters"]), "escaped_frac": float(np.mean(srn == 1))}
+                     "pixel_iters": int(st["pixel_iters"]), "full_steps": int(st["full_steps"]),
+                     "bla_steps": int(st["bla_steps"]), "rebases": int(st["rebases"]),
+                     "escaped_frac": float(np.mean(srn == 1))}
     out["speedup_fe32_vs_fp64"] = out["fe32"]["value"] / out["fp64"]["value"]
-    out["speedup_fe32_vs_xr64"] = out["fe32"]["value"] / out["xr64"]["value"]
+    if "xr64" in out:
+        out["speedup_fe32_vs_xr64"] = out["fe32"]["value"] / out["xr64"]["value"]
     for r in refs.values():
         r.free()
     if parity_pixels > 0:
         t0 = time.perf_counter()
         kw = oracle_kw(we)
         o_std = oracle_pixels(we, idx, kw)
-        o_xr = oracle_pixels(wx, idx, oracle_kw(wx))
+        br = "Xrange" if we.xr_mode else "FP64"
+        rows = {"sample": f"{idx.size} seeded random pixels",
+                "oracle": f"strict C restatement; {br} branch (the reference's at this width)"}
+        rows[f"fe32_vs_{br.lower()}_branch"] = parity_table(samples["fe32"], o_std, we.M)
+        rows[f"fp64_vs_{br.lower()}_branch"] = parity_table(samples["fp64"], o_std, we.M)
+        if wx is not None:
+            o_xr = oracle_pixels(wx, idx, oracle_kw(wx))
+            rows["xr64_vs_xrange_branch"] = parity_table(samples["xr64"], o_xr, we.M)
+            rows["oracle_xrange_vs_fp64_branch"] = parity_table(o_xr, o_std, we.M)
         o_shift = oracle_pixels(we, idx, dict(kw, lin_mat=LIN * (1. + 2. ** -24)))
-        out["vs_oracle"] = {
-            "sample": f"{idx.size} seeded random pixels",
-            "oracle": "strict C restatement; FP64 branch (the reference's at this width) and "
-                      "Xrange branch",
-            "oracle_s": time.perf_counter() - t0,
-            "fe32_vs_fp64_branch": parity_table(samples["fe32"], o_std, we.M),
-            "fp64_vs_fp64_branch": parity_table(samples["fp64"], o_std, we.M),
-            "xr64_vs_xrange_branch": parity_table(samples["xr64"], o_xr, we.M),
-            "oracle_xrange_vs_fp64_branch": parity_table(o_xr, o_std, we.M),
-            "oracle_c_offset_2^-24_vs_fp64_branch": parity_table(o_shift, o_std, we.M)}
+        rows[f"oracle_c_offset_2^-24_vs_{br.lower()}_branch"] = parity_table(o_shift, o_std, we.M)
+        rows["oracle_s"] = time.perf_counter() - t0
+        out["vs_oracle"] = rows
     return out
 
 
@@ -694,10 +720,19 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
 
-    w = syn.config2_workload(nx=args.nx)
-    n = w.nx * w.ny
     ctx = nat.Context(local)
     ctx.set_stream(stream.cuda_stream)
+    if args.no_headline:
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+        supp = supplementary(ctx, nat, syn, torch, dev, stream, flush, args.bs_max_iter,
+                             legs=tuple(args.legs.split(",")), bs_tiles=args.bs_tiles,
+                             edge_nx=args.edge_nx,
+                             parity_pixels=min(16384, args.parity_pixels))
+        print(json.dumps({"note": "supplementary legs only (--no-headline)",
+                          "supplementary": supp}), flush=True)
+        return 0
+    w = syn.config2_workload(nx=args.nx)
+    n = w.nx * w.ny
     peak32 = ctx.peak_tflops(False)
     peak64 = ctx.peak_tflops(True)
 

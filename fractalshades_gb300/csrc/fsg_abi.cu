@@ -31,9 +31,11 @@ void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzn
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
                          int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                         double kc, int4 *bla_chain, int2 *bla_chain_step,
                          cudaStream_t s);
 void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
                       int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
+                      double kc, int4 *bla_chain, int2 *bla_chain_step,
                       cudaStream_t s);
 void fsg_build_bs_fr(const RefDev *Rd, int len, int4 *Zf, const double *dXa, const double *dXb,
                      const double *dYa, const double *dYb, int4 *hf, float4 *fa, int4 *fz,
@@ -598,8 +600,9 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.stages = stages;
     // fe tables (M2)
     int4 *Zf = nullptr, *Zp = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_f = nullptr,
-         *bla_first = nullptr;
+         *bla_first = nullptr, *bla_chain = nullptr;
     int *bla_first_step = nullptr;
+    int2 *bla_chain_step = nullptr;
     const int bla_nit = (len >> 3) + 1;
     const bool fe_tables = d->flavor == 0 && d->nexp == 0;   // FE32 is the power-2 form
     if (fe_tables) {
@@ -611,10 +614,13 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
             RA(bla_f, 2 * (size_t)R.bla_len);
             RA(bla_first, 2 * (size_t)bla_nit);
             RA(bla_first_step, (size_t)bla_nit);
+            RA(bla_chain, 2 * (size_t)bla_nit);
+            RA(bla_chain_step, (size_t)bla_nit);
         }
     }
     R.Zf = Zf; R.Zp = Zp; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f = bla_f;
     R.bla_first = bla_first; R.bla_first_step = bla_first_step; R.bla_nit = bla_nit;
+    R.bla_chain = bla_chain; R.bla_chain_step = bla_chain_step;
     // FP32+exp tables (Burning Ship)
     int4 *bs_Zf = nullptr, *bs_hf = nullptr, *bs_blaf = nullptr;
     int2 *bs_rf = nullptr;
@@ -654,7 +660,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (fe_tables) {
         fsg_build_fe_tables(r->dev, len, Zf, dzndc, dzndc_xm, dzndc_xe, dzndc_f, dzndz, dzndz_xm,
                             dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_f, bla_nit, bla_first,
-                            bla_first_step, s);
+                            bla_first_step, d->kc, bla_chain, bla_chain_step, s);
         fsg_build_plain_orbit(r->dev, len, Zf, Zp, s);
     }
     RCK(cudaGetLastError(), "reference table kernels");
@@ -701,7 +707,9 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
 #define RA(ptr, n) do { rc = ref_alloc(ctx, r, &(ptr), (n)); if (rc != FSG_OK) { ref_release(r, s); delete r; return rc; } } while (0)
 #define RCK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { ref_release(r, s); delete r; return cuda_err(ctx, e_, what); } } while (0)
     double2 *Mbla = nullptr; double *Mbs = nullptr, *rbla = nullptr;
-    int4 *bla_f = nullptr, *bla_first = nullptr; int *bla_first_step = nullptr;
+    int4 *bla_f = nullptr, *bla_first = nullptr, *bla_chain = nullptr;
+    int *bla_first_step = nullptr;
+    int2 *bla_chain_step = nullptr;
     R.bla_len = 0;
     if (L > 0) {
         if (R.flavor == 0) RA(Mbla, 4 * (size_t)L); else RA(Mbs, 16 * (size_t)L);
@@ -714,6 +722,8 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
             RA(bla_f, 2 * (size_t)R.bla_len);
             RA(bla_first, 2 * (size_t)R.bla_nit);
             RA(bla_first_step, (size_t)R.bla_nit);
+            RA(bla_chain, 2 * (size_t)R.bla_nit);
+            RA(bla_chain_step, (size_t)R.bla_nit);
         }
     }
     int4 *bs_blaf = nullptr;
@@ -724,13 +734,14 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
     }
     R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.bs_blaf = bs_blaf; R.bs_rf = bs_rf;
     R.bla_f = bla_f; R.bla_first = bla_first; R.bla_first_step = bla_first_step;
+    R.bla_chain = bla_chain; R.bla_chain_step = bla_chain_step;
     RCK(cudaMallocAsync((void **)&r->dev, sizeof(RefDev), s), "cudaMallocAsync(reference descriptor)");
     RCK(cudaMemcpyAsync(r->dev, &R, sizeof(RefDev), cudaMemcpyHostToDevice, s), "upload descriptor");
     if (R.bla_len > 0) {
         fsg_build_bla(r->dev, R.flavor, len, Mbla, Mbs, rbla, R.stages, kc, bla_eps, s);
         if (R.flavor == 0 && R.nexp == 0)
             fsg_build_fe_bla(r->dev, Mbla, rbla, R.bla_len, bla_f, R.bla_nit, bla_first,
-                             bla_first_step, s);
+                             bla_first_step, kc, bla_chain, bla_chain_step, s);
         else if (R.flavor != 0)
             fsg_build_bs_fr_bla(Mbs, rbla, R.bla_len, bs_blaf, bs_rf, s);
     }

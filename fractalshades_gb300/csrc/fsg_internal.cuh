@@ -48,6 +48,10 @@ struct RefDev {
     const int4 *bla_first;      // [2 bla_nit] per start index it = w / 8, the first
                                 // stage ref_BLA_get tries there: its bla_f record
     const int *bla_first_step;  // [bla_nit] that stage's step, 0 when none is tried
+    const int4 *bla_chain;      // [2 bla_nit] per start index, the composite of the run of
+                                // first candidates from there (header and payload as bla_f)
+    const int2 *bla_chain_step; // [bla_nit] {iterations of that run, its BLA steps}, {0, 0}
+                                // when none is stored
     int bla_nit;                // (len >> 3) + 1
     // Burning Ship FP32+exp tables: reals as {mantissa bits, exponent} pairs
     const int4 *bs_Zf;          // [len + 1] {X, Y} (Xrange side-table values where present)

@@ -21,7 +21,10 @@
 //     extended |Z + dz|^2 <= |dz|^2 confirmation.
 // The BLA validity test |dz| < r is |u|^2 < r^2 2^(-2E) in FP32 with the
 // exponent gap clamped (to_standard(dz), which the reference compares, is 0
-// only below every r > 0).
+// only below every r > 0), in double at near-ties.  Runs of consecutive BLA
+// steps (each on the largest admissible stage) are applied as one composite
+// step where the composite's radius admits dz (fsg_ref.cu, k_fe_bla_chain):
+// the same iterations, the same decisions, one step.
 #include "fsg_internal.cuh"
 
 // 2^k as a float for k in [-126, 127]; 0 below; k > 127 is clamped (callers
@@ -138,15 +141,36 @@ __device__ __forceinline__ bool stationary_fast(float qx, float qy, int G, int4 
     return fmaf(x, x, y * y) < eps2 * __int_as_float((d + 127) << 23);
 }
 
-// |dz| < r for the BLA entry whose header is H = {r mantissa bits, r exponent,
-// A exponent, B exponent}, as |u|^2 < rm^2 2^(2 (re - E)).  u is normalised
-// (|u| in [2^-30, 2^31) or 0), so exponent gaps beyond +-126 are decided by
-// the clamp alone; r = 0 (rm = 0) admits nothing, dz = 0 any r > 0 -- the
-// reference's strict 0 < r.
-__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H) {
+// The BLA validity test at a near-tie, in double (ref_BLA_get,
+// perturbation.py:2116-2170): |to_standard(dz)| < r with the entry's double
+// radius (taken in ~1 of 10^5 lookups).
+static __device__ __forceinline__ bool bla_ok_double(const double *rbla, int idx, float ux,
+                                                  float uy, int E) {
+    const double2 d = fe_to_d(fe_make(ux, uy, E));
+    return hypot(d.x, d.y) < __ldg(&rbla[idx]);
+}
+
+// |dz| < r in FP32 for a header H = {r mantissa bits, r exponent, ...}
+__device__ __forceinline__ bool bla_ok_plain(const Lane &s, int4 H) {
     const int d = min(max(2 * (H.y - s.E), -126), 126);
     const float rm = __int_as_float(H.x);
     return fmaf(s.ux, s.ux, s.uy * s.uy) < (rm * rm) * __int_as_float((d + 127) << 23);
+}
+
+// |dz| < r for BLA entry idx whose header is H = {r mantissa bits, r
+// exponent, A exponent, B exponent}, as |u|^2 < rm^2 2^(2 (re - E)).  u is
+// normalised (|u| in [2^-30, 2^31) or 0), so exponent gaps beyond +-126 are
+// decided by the clamp alone; r = 0 (rm = 0) admits nothing, dz = 0 any
+// r > 0 -- the reference's strict 0 < r.  Within 2^-18 of a tie (the FP32
+// radius and |u|^2 carry ~2^-23 of rounding) the double test decides.
+__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H, const double *rbla, int idx) {
+    const int d = min(max(2 * (H.y - s.E), -126), 126);
+    const float rm = __int_as_float(H.x);
+    const float lhs = fmaf(s.ux, s.ux, s.uy * s.uy);
+    const float rhs = (rm * rm) * __int_as_float((d + 127) << 23);
+    if (fabsf(lhs - rhs) <= 0x1p-18f * rhs && d > -126 && d < 126)
+        return bla_ok_double(rbla, idx, s.ux, s.uy, s.E);
+    return lhs < rhs;
 }
 
 // ref_BLA_get (perturbation.py:2116-2170): the largest stage from
@@ -158,25 +182,37 @@ __device__ __forceinline__ bool bla_ok(const Lane &s, int4 H) {
 // stage does: after the first candidate the search tests stage 3, then the
 // stages between.
 __device__ __forceinline__ int bla_find(const int4 *__restrict__ T, const int4 *__restrict__ FF,
-                                        const int *__restrict__ FS, const Lane &s, int w,
-                                        int4 &H, int4 &P) {
+                                        const int *__restrict__ FS, const double *rbla,
+                                        const Lane &s, int w, int4 &H, int4 &P) {
     const int it = w >> FSG_STG_COMPRESSED;
     const int st = __ldg(&FS[it]);
     H = __ldg(&FF[2 * it]);
     P = __ldg(&FF[2 * it + 1]);
     if (st == 0) return 0;
-    if (bla_ok(s, H)) return st;
-    if (st == 8) return 0;
     const int i0 = 2 * it;
+    // BLA_index(i, stg) = 2 i + 2^stg - 1 over the stored stages (stg - 3)
+    if (bla_ok(s, H, rbla, i0 + (st >> FSG_STG_COMPRESSED) - 1)) return st;
+    if (st == 8) return 0;
     const int4 H3 = __ldg(&T[2 * i0]);
-    if (!bla_ok(s, H3)) return 0;
+    if (!bla_ok(s, H3, rbla, i0)) return 0;
     for (int stg = 30 - __clz(st); stg > FSG_STG_COMPRESSED; stg--) {
         const int idx = i0 + (1 << (stg - FSG_STG_COMPRESSED)) - 1;
         H = __ldg(&T[2 * idx]);
-        if (bla_ok(s, H)) { P = __ldg(&T[2 * idx + 1]); return 1 << stg; }
+        if (bla_ok(s, H, rbla, idx)) { P = __ldg(&T[2 * idx + 1]); return 1 << stg; }
     }
     H = H3; P = __ldg(&T[2 * i0 + 1]);
     return 1 << FSG_STG_COMPRESSED;
+}
+
+// The componentwise dynamic-rebase test on the double values (the
+// reference's std values, to_standard() underflow included), taken only when
+// the FP32 test is within its rounding of a tie, or for values outside the
+// float range.
+static __device__ __forceinline__ int rebase_test_double(fe dz, const double2 *Zn, int w) {
+    const double2 dd = fe_to_d(dz);
+    const double2 Zd = __ldg(&Zn[w]);
+    const double2 ZZd = cadd(dd, Zd);
+    return (fabs(ZZd.x) <= fabs(dd.x)) && (fabs(ZZd.y) <= fabs(dd.y));
 }
 
 // rebase bookkeeping shared by the three rebase kinds: dzndc += dZndc_w,
@@ -194,10 +230,11 @@ __device__ __forceinline__ void rebase_derivs(Lane &s, const RefDev &R, int w, i
     }
 }
 
+// One pixel; returns its iteration count and adds its executed full steps,
+// BLA steps and rebases to the (per-pixel, 32-bit) counters.
 template <bool INTERIOR>
-__device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, long long ip,
-                                           unsigned long long &nfull, unsigned long long &nbla,
-                                           unsigned long long &nreb, unsigned long long &itsum) {
+__device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, long long ip,
+                                          unsigned &nfull, unsigned &nbla, unsigned &nreb) {
     const RefDev &R = *T.ref;
     const long long np = (long long)T.nx * T.ny;
     const bool dzndz_on = INTERIOR, dzndc_on = C.calc_dzndc;
@@ -215,6 +252,8 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     const int4 *__restrict__ bla_f = R.bla_f;
     const int4 *__restrict__ bla_first = R.bla_first;
     const int *__restrict__ bla_first_step = R.bla_first_step;
+    const int4 *__restrict__ bla_chain = R.bla_chain;
+    const int2 *__restrict__ bla_chain_step = R.bla_chain_step;
     // c from the pixel (perturbation.py:2214-2230) in Xrange, then fe
     double2 pp = fsg_pixel(T, ip);
     double x1 = T.lin[0] * pp.x + T.lin[1] * pp.y;
@@ -241,7 +280,21 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
         // continue saw w < div_iter - 1, or a BLA jump stopped short of it)
         if (bla_on && (w & 7) == 0 && w < first_invalid) {
             int4 H, P;
-            const int step = bla_find(bla_f, bla_first, bla_first_step, s, w, H, P);
+            int step = bla_find(bla_f, bla_first, bla_first_step, R.rbla, s, w, H, P);
+            // when the first candidate is taken, the run of first candidates
+            // from here, composed (its radius is at most 0.9 of the first
+            // candidate's and carries that margin: no tie test)
+            if (step != 0 && step == __ldg(&bla_first_step[w >> FSG_STG_COMPRESSED])) {
+                const int2 cs = __ldg(&bla_chain_step[w >> FSG_STG_COMPRESSED]);
+                if (cs.y >= 2) {
+                    const int4 Hc = __ldg(&bla_chain[2 * (w >> FSG_STG_COMPRESSED)]);
+                    if (bla_ok_plain(s, Hc)) {
+                        H = Hc;
+                        P = __ldg(&bla_chain[2 * (w >> FSG_STG_COMPRESSED) + 1]);
+                        step = cs.x;
+                    }
+                }
+            }
             if (step != 0) {
                 const float Ax = __int_as_float(P.x), Ay = __int_as_float(P.y);
                 const float Bx = __int_as_float(P.z), By = __int_as_float(P.w);
@@ -275,17 +328,24 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             }
         }
         // ---------------- full step (perturbation.py:1158-1214) ------------
-        // (u = 0 counts as 2^(E - 127): the limit FE_ZERO_E of a zero or
-        // out-of-range orbit value never passes)
-        if (Zc.z >= s.E + mag_b(s) - 127) {
-            // run of fast steps (|dz| < 2^-26 |Z| at each), up to the next
-            // event that needs the general tests: a BLA attempt (w % 8 == 0),
-            // max_iter, the reference's divergence rebase, the orbit's wrap
+        // A run of FP32 steps when Z_w is a normal float (2^-100 .. 2^100) and
+        // |dz| < 2^100: dz' = dz (dz + 2 Z) + dc in dz's frame,
+        // u' = u (2 Z + dz) + cu, and the derivatives with 2 (Z + dz) -- for
+        // |dz| < 2^-26 |Z| the dz terms vanish below FP32 resolution.
+        // (u = 0 counts as 2^(E - 127).)  Below E = -126 the plain value of
+        // dz flushes to 0, which is exact only in the |dz| < 2^-26 |Z| regime.
+        const int md0 = s.E + mag_b(s) - 127;     // exponent of |dz|inf
+        if (Zc.z != FE_ZERO_E && md0 <= 100 && (Zc.z >= md0 || s.E >= -126)) {
+            // the run lasts up to the next event that needs the general
+            // tests -- a BLA attempt (w % 8 == 0), max_iter, the reference's
+            // divergence rebase, the orbit's wrap -- or until a step's tests
+            // (escape, rebase) cannot be decided in FP32
             int k = order - w;
             if (bla_on) k = min(k, 8 - (w & 7));
             k = min(k, max(div_iter - 1 - w, 1));
             k = max(min(k, max_iter - n), 1);
             set_cu(s, cmx, cmy, Ec);
+            float sE = p2f(s.E);
             int4 Dv = make_int4(0, 0, FE_ZERO_E, 0);
             if (dzndc_on && !dyn) Dv = __ldg(&dZndc_f[w]);
             // dzndz: the reference derivative is dZndz_0 once nullified, else
@@ -297,6 +357,7 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             }
             int j = 0;
             bool esc = false, stat = false;
+            bool tiny = Zc.z >= md0;               // |dz| < 2^-26 |Z| at this step
             for (;;) {
                 // next entries (w + 1 <= order <= len, inside the tables)
                 const int4 Zn = __ldg(&Zp[w + 1]);
@@ -304,11 +365,22 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
                 if (dzndc_on) Dn = __ldg(&dZndc_f[w + 1]);
                 if (INTERIOR) Qn = nullify ? Q0 : __ldg(&dZndz_f[w + 1]);
                 const float Zx = __int_as_float(Zc.x), Zy = __int_as_float(Zc.y);   // 2 Z
-                if (dzndc_on) deriv_fast(s.vx, s.vy, s.F, Dv, Zx, Zy, s);
-                if (INTERIOR) deriv_fast(s.qx, s.qy, s.G, Qv, Zx, Zy, s);
-                const float nx = fmaf(Zx, s.ux, fmaf(-Zy, s.uy, s.cux));
-                const float ny = fmaf(Zx, s.uy, fmaf(Zy, s.ux, s.cuy));
-                s.ux = nx; s.uy = ny;
+                if (tiny) {
+                    // the dz terms are below FP32 resolution: u' = 2 Z u + cu
+                    if (dzndc_on) deriv_fast(s.vx, s.vy, s.F, Dv, Zx, Zy, s);
+                    if (INTERIOR) deriv_fast(s.qx, s.qy, s.G, Qv, Zx, Zy, s);
+                    const float nx = fmaf(Zx, s.ux, fmaf(-Zy, s.uy, s.cux));
+                    const float ny = fmaf(Zx, s.uy, fmaf(Zy, s.ux, s.cuy));
+                    s.ux = nx; s.uy = ny;
+                } else {
+                    const float ex = s.ux * sE, ey = s.uy * sE;                      // dz
+                    const float tx = Zx + ex, ty = Zy + ey;                          // 2 Z + dz
+                    if (dzndc_on) deriv_fast(s.vx, s.vy, s.F, Dv, tx + ex, ty + ey, s);
+                    if (INTERIOR) deriv_fast(s.qx, s.qy, s.G, Qv, tx + ex, ty + ey, s);
+                    const float nx = fmaf(tx, s.ux, fmaf(-ty, s.uy, s.cux));
+                    const float ny = fmaf(tx, s.uy, fmaf(ty, s.ux, s.cuy));
+                    s.ux = nx; s.uy = ny;
+                }
                 j++; w++;
                 if (j == k) break;
                 Zc = Zn; Dv = Dn; Qv = Qn;
@@ -322,10 +394,29 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
                     if (st) { stat = true; break; }
                 }
                 int b = mag_b(s);
-                if ((unsigned)(b - 97) > 60u) { renorm_u(s, cmx, cmy, Ec); b = mag_b(s); }
-                if (Zc.z < s.E + b - 127) break;           // next step is not fast
+                if ((unsigned)(b - 97) > 60u) { renorm_u(s, cmx, cmy, Ec); b = mag_b(s); sE = p2f(s.E); }
+                const int md = s.E + b - 127;
                 const float Zx2 = __int_as_float(Zc.x), Zy2 = __int_as_float(Zc.y);
-                if (Zx2 * Zx2 + Zy2 * Zy2 > M2f4) { esc = true; break; }
+                tiny = Zc.z >= md;                 // false for FE_ZERO_E
+                if (tiny) {
+                    // |dz| < 2^-26 |Z|: ZZ = Z to FP32 resolution and
+                    // |Z|inf >= 4 |dz|inf rules the rebase out
+                    if (Zx2 * Zx2 + Zy2 * Zy2 > M2f4) { esc = true; break; }
+                } else {
+                    // Z out of the float range or 0, dz too large, or dz's
+                    // plain value out of range: the next step in exact form
+                    if (Zc.z == FE_ZERO_E || md > 100 || s.E < -126) break;
+                    // escape (:1252-1279) and the componentwise rebase test
+                    // (:1317-1320) in FP32: "no rebase" is certain when a
+                    // component of |Z + dz| exceeds that of |dz| by more than
+                    // 2^-20 of the magnitudes (Z carries 2^-24 of rounding);
+                    // otherwise the general tests decide, in double at ties
+                    const float fx = s.ux * sE, fy = s.uy * sE;
+                    const float hx = fmaf(0.5f, Zx2, fx), hy = fmaf(0.5f, Zy2, fy);
+                    if (hx * hx + hy * hy > M2f) { esc = true; break; }
+                    const float tau = 0x1p-21f * (fabsf(Zx2) + fabsf(Zy2)) + 0x1p-20f * (fabsf(fx) + fabsf(fy));
+                    if (!(fabsf(hx) - fabsf(fx) > tau || fabsf(hy) - fabsf(fy) > tau)) break;
+                }
                 dyn = false;
             }
             renorm_u(s, cmx, cmy, Ec);
@@ -410,13 +501,22 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
             Zc = __ldg(&Zp[0]);
             continue;
         }
-        // dynamic rebase: integer pre-rejection, then the double-range test
+        // dynamic rebase (:1317-1320): integer pre-rejection (|Z|inf >=
+        // 4 |dz|inf), then the componentwise test in FP32 when both values
+        // are normal floats, in double (the reference's std values) when the
+        // FP32 test lies within its rounding of a tie
         dyn = false;
         if (Zn.e < dz.e + 2) {
-            double2 dd = fe_to_d(dz);
-            double2 Zd = __ldg(&R.Zn[w]);
-            double2 ZZd = cadd(dd, Zd);
-            dyn = (fabs(ZZd.x) <= fabs(dd.x)) && (fabs(ZZd.y) <= fabs(dd.y));
+            int dec = 2;                                  // 0 no, 1 yes, 2 undecided
+            if (Zn.e > -100 && Zn.e < 100 && dz.e > -100 && dz.e < 100) {
+                const float tau = 0x1p-21f * (fabsf(zf.x) + fabsf(zf.y))
+                                  + 0x1p-20f * (fabsf(df.x) + fabsf(df.y));
+                const float ax = fabsf(XX) - fabsf(df.x), ay = fabsf(YY) - fabsf(df.y);
+                if (ax > tau || ay > tau) dec = 0;
+                else if (ax < -tau && ay < -tau) dec = 1;
+            }
+            if (dec == 2) dec = rebase_test_double(dz, R.Zn, w);
+            dyn = dec == 1;
             if (dyn) {
                 fe ZZ = fe_add(dz, Zn);
                 bool ok = true;
@@ -464,7 +564,7 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
     T.stop_iter[ip] = n;
     T.stop_reason[ip] = stop;
     fsg_epilogue(T, C, ip, zn, hypot(dzc.x, dzc.y), n);
-    itsum += (unsigned long long)n;
+    return n;
 }
 
 // 128-thread blocks, 7 per SM: 72 registers a thread without spills, 28 warps
@@ -474,15 +574,24 @@ __device__ __forceinline__ void pixel_fe32(const TileDev &T, const CalcDev &C, l
 template <bool INTERIOR>
 __global__ void __launch_bounds__(FE32_BLOCK, INTERIOR ? 6 : 7) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    // per-thread statistics (iterations, full steps, BLA steps, rebases) in
+    // shared memory: 64-bit accumulators would hold 8 registers in the loop
+    __shared__ unsigned long long s_acc[4][FE32_BLOCK];
+    for (int k = 0; k < 4; k++) s_acc[k][threadIdx.x] = 0ULL;
     fsg_load_starts(W, s_start);
-    unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
     int t; long long ip;
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
-        pixel_fe32<INTERIOR>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        unsigned nfull = 0, nbla = 0, nreb = 0;
+        const int n = pixel_fe32<INTERIOR>(W.tiles[t], C, ip, nfull, nbla, nreb);
+        s_acc[0][threadIdx.x] += (unsigned long long)n;
+        s_acc[1][threadIdx.x] += nfull;
+        s_acc[2][threadIdx.x] += nbla;
+        s_acc[3][threadIdx.x] += nreb;
     }
-    fsg_flush_stats(W, itsum, nfull, nbla, nreb);
+    fsg_flush_stats(W, s_acc[0][threadIdx.x], s_acc[1][threadIdx.x], s_acc[2][threadIdx.x],
+                    s_acc[3][threadIdx.x]);
 }
 
 void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,

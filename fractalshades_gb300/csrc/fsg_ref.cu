@@ -449,6 +449,69 @@ __global__ void k_fe_bla_first(const RefDev *Rp, const int4 *F, int nit, int4 *F
     FF[2 * it] = h; FF[2 * it + 1] = p; FS[it] = step;
 }
 
+// |a| of an Xrange complex as a double (0 below, inf above the double range)
+__device__ __forceinline__ double xabs_d(xc a) {
+    if (a.re == 0. && a.im == 0.) return 0.;
+    return ldexp_d(hypot(a.re, a.im), a.e);
+}
+
+// Chains of first BLA candidates.  A BLA step of ref_BLA_get ends on a
+// multiple of 8, where the next attempt starts (perturbation.py:1121-1154),
+// so when every first candidate (the largest admissible stage) is valid the
+// reference takes a run of BLA steps with no full step between them.  Their
+// composite dz -> P dz + Q dc (P = A_L .. A_1, Q = sum of A_L .. A_{j+1} B_j)
+// is valid wherever each step is: with |dc| <= kc,
+//   |dz_j| <= |P_j| |dz| + |Q_j| kc < r_j   for every j,
+// that is |dz| < min_j (r_j - |Q_j| kc) / |P_j|.  The table holds, per start
+// index, that radius times 0.9 (every step of the run then passes with a
+// margin), P and Q as an fe record like the tree's, the run's iterations and
+// its number of steps.  A run stops before a step that would cut the radius
+// below a quarter of the shorter run's (a long run that rarely applies) and
+// after 64 steps; runs of fewer than 2 steps are not stored.
+__global__ void k_fe_bla_chain(const RefDev *Rp, const int *FS, int nit, double kc, int4 *CH,
+                               int2 *CS) {
+    const RefDev &R = *Rp;
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nit) return;
+    xc P = xr_from(cx(1., 0.)), Q = xc_zero();
+    double rc = -1.;                       // < 0: no bound yet
+    int j = it, total = 0, count = 0;
+    while (j < nit && count < 64) {
+        const int step = FS[j];
+        if (step == 0) break;
+        const int idx = 2 * j + (step >> FSG_STG_COMPRESSED) - 1;
+        if (idx >= R.bla_len) break;
+        const double num = R.rbla[idx] - xabs_d(Q) * kc;
+        if (!(num > 0.)) break;
+        const double pm = hypot(P.re, P.im);
+        const double lim = (pm == 0.) ? INFINITY : ldexp_d(num / pm, -P.e);
+        if (!(lim > 0.)) break;
+        if (rc >= 0. && lim < 0.25 * rc) break;
+        rc = (rc < 0.) ? lim : fmin(rc, lim);
+        const double2 A = R.Mbla[2 * idx], B = R.Mbla[2 * idx + 1];
+        P = xr_mul_s(A, P);
+        Q = xr_add(xr_mul_s(A, Q), xr_from(B));
+        total += step; count++;
+        j += step >> FSG_STG_COMPRESSED;
+    }
+    int4 h = make_int4(0, FE_ZERO_E, 0, 0), p = make_int4(0, 0, 0, 0);
+    if (count >= 2 && rc > 0. && rc < INFINITY) {
+        const fe a = fe_norm(fe_from_xc(P)), b = fe_norm(fe_from_xc(Q));
+        const fe rf = fe_norm(fe_from_d(cx(0.9 * rc, 0.)));
+        if (rf.e != FE_ZERO_E && a.e != FE_ZERO_E) {
+            h = make_int4(__float_as_int(rf.x), rf.e, a.e, b.e);
+            p = make_int4(__float_as_int(a.x), __float_as_int(a.y), __float_as_int(b.x),
+                          __float_as_int(b.y));
+        } else {
+            total = 0; count = 0;
+        }
+    } else {
+        total = 0; count = 0;
+    }
+    CH[2 * it] = h; CH[2 * it + 1] = p;
+    CS[it] = make_int2(total, count);
+}
+
 // ---------------------------------------------------------------------------
 // Burning Ship FP32+exp tables (fr pairs, fsg_bs.cuh)
 // ---------------------------------------------------------------------------
@@ -678,28 +741,32 @@ void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, 
 
 void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
                       int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
-                      cudaStream_t s);
+                      double kc, int4 *bla_chain, int2 *bla_chain_step, cudaStream_t s);
 
 void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzndc,
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
                          int4 *dzndz_f, const double2 *Mbla, const double *rbla, int bla_len,
                          int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
-                         cudaStream_t s) {
+                         double kc, int4 *bla_chain, int2 *bla_chain_step, cudaStream_t s) {
     int tb = 256;
     k_fe_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf);
     if (dzndc_f) k_fe_path<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(dzndc, dzndc_xm, dzndc_xe, len + 1, dzndc_f);
     if (dzndz_f) k_fe_path<<<(len + 2 + tb - 1) / tb, tb, 0, s>>>(dzndz, dzndz_xm, dzndz_xe, len + 2, dzndz_f);
-    fsg_build_fe_bla(Rd, Mbla, rbla, bla_len, bla_f, bla_nit, bla_first, bla_first_step, s);
+    fsg_build_fe_bla(Rd, Mbla, rbla, bla_len, bla_f, bla_nit, bla_first, bla_first_step, kc,
+                     bla_chain, bla_chain_step, s);
 }
 
 void fsg_build_fe_bla(const RefDev *Rd, const double2 *Mbla, const double *rbla, int bla_len,
                       int4 *bla_f, int bla_nit, int4 *bla_first, int *bla_first_step,
-                      cudaStream_t s) {
+                      double kc, int4 *bla_chain, int2 *bla_chain_step, cudaStream_t s) {
     int tb = 256;
     if (bla_f && bla_len > 0) {
         k_fe_bla<<<(bla_len + tb - 1) / tb, tb, 0, s>>>(Mbla, rbla, bla_len, bla_f);
         k_fe_bla_first<<<(bla_nit + tb - 1) / tb, tb, 0, s>>>(Rd, bla_f, bla_nit, bla_first,
                                                               bla_first_step);
+        if (bla_chain)
+            k_fe_bla_chain<<<(bla_nit + tb - 1) / tb, tb, 0, s>>>(Rd, bla_first_step, bla_nit, kc,
+                                                                  bla_chain, bla_chain_step);
     }
 }

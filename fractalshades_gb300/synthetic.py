@@ -119,7 +119,10 @@ def prepare_m2(*, p, dps, dx, nx, ny=None, max_iter, M=1000., center=None, offse
                xr_mode=None):
     """Orbit and view for a power-2 Mandelbrot perturbation render centred on
     the period-p nucleus (or ``center``), shifted by ``offset`` (in units of
-    dx).  The reference point is the nucleus; the orbit wraps at p.
+    dx).  The reference point is the nucleus; the orbit wraps at p.  With
+    ``p=None`` the reference is ``center`` itself, without period: its orbit
+    has max_iter + 1 points, diverges at its exit index and has no order
+    (2^62, perturbation.py:455-456).
     ``xr_mode``: the Xrange branch on or off whatever the width (None: the
     reference's switch, dx < settings.xrange_zoom_level)."""
     ny = ny or nx
@@ -130,11 +133,14 @@ def prepare_m2(*, p, dps, dx, nx, ny=None, max_iter, M=1000., center=None, offse
         prec = mpmath.mp.prec
         if xr_mode is None:
             xr_mode = dxm < settings.xrange_zoom_level
-        ref_len = min(p, max_iter + 1)
-        Zn = np.empty(ref_len, dtype=np.complex128)
+        ref_len = min(p, max_iter + 1) if p else max_iter + 1
+        Zn = np.zeros(ref_len, dtype=np.complex128)
+        div_iter = max_iter + 1
         if ref_len == max_iter + 1:
             i, _, xr = fsFP.perturbation_mandelbrot_FP_loop(
                 Zn, xr_mode, max_iter, 2 * M, str(c.real), str(c.imag), prec)
+            if not p:
+                div_iter = int(i)
         else:
             full = np.empty(ref_len, dtype=np.complex128)
             i, _, xr = fsFP.perturbation_mandelbrot_FP_loop(
@@ -152,7 +158,8 @@ def prepare_m2(*, p, dps, dx, nx, ny=None, max_iter, M=1000., center=None, offse
     xs, ys = image_axes(nx, ny, nx / ny)
     return M2Workload(
         p=p, dps=dps, center=view, dx=dxm, nx=nx, ny=ny, max_iter=max_iter, M=M, Zn=Zn,
-        div_iter=max_iter + 1, order=p, xr_idx=idx, xr_m=m, xr_e=e, xr_mode=bool(xr_mode),
+        div_iter=div_iter, order=p if p else (1 << 62), xr_idx=idx, xr_m=m, xr_e=e,
+        xr_mode=bool(xr_mode),
         dx_m=dx_xr.m, dx_e=dx_xr.e, drift_m=drift.m, drift_e=drift.e,
         kc=kc_xr.to_standard(), xs=xs, ys=ys)
 
@@ -199,6 +206,15 @@ def edge_workload(nx=1024, max_iter=200000, xr_mode=None, seed=2):
     p = int(np.random.default_rng(seed).integers(300, 3001))
     return prepare_m2(p=p, dps=400, dx="1.6e-9", nx=nx, max_iter=max_iter, M=1000.,
                       xr_mode=xr_mode)
+
+
+def seahorse_workload(nx=1024, max_iter=6000):
+    """An escape-dominated view: the seahorse valley at
+    -0.743643887037151 + 0.131825904205330 i, width 2e-9, 30 digits,
+    max_iter 6000, the reference at the centre (no period; it diverges)."""
+    with mpmath.workdps(30):
+        c = mpmath.mpc("-0.743643887037151", "0.131825904205330")
+    return prepare_m2(p=None, dps=30, dx="2.e-9", nx=nx, max_iter=max_iter, M=1000., center=c)
 
 
 def config3_workload(seed=3, nx=4096, max_iter=1000000):

@@ -1004,9 +1004,31 @@ def p2562_cases(nx_edge=16, nx_edge_xr=4):
     print("pert_m2_p2562_edge_xr done", flush=True)
 
 
+def bs_flavor_cases():
+    """Perturbation Burning Ship flavors 2, 3 and 5 (Perpendicular burning
+    ship, Shark fin, Buffalo; burning_ship.py:535-859), and flavor 4 (Celtic)
+    on a second view, FP64 branch: each centred on a point of its own set's
+    boundary whose orbit escapes after ~3000 iterations (found with the
+    standard loop on a grid), width 1e-5, so that the reference diverges and
+    escaping and non-escaping pixels mix."""
+    mpmath.mp.dps = 30
+    for fl, flav, x, y, name in (
+            (2, "Perpendicular burning ship", "-0.5710063401785717", "-0.6660741479166669",
+             "pert_bs_2"),
+            (3, "Shark fin", "-0.6922635670582709", "-0.3510271929824563", "pert_bs_3"),
+            (4, "Celtic", "-0.7584971274906015", "-0.8352377380482457", "pert_bs_4e"),
+            (5, "Buffalo", "-1.5394062147086462", "0.2671241854166664", "pert_bs_5")):
+        golden_perturb_bs(
+            os.path.join(HERE, name + ".npz"), x=x, y=y, dx="1.e-5",
+            nx=14, precision=30, max_iter=5000, flavor=flav)
+        print(name + " done", flush=True)
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "p2562":
         p2562_cases()
+    elif len(sys.argv) > 2 and sys.argv[2] == "bs_flavors":
+        bs_flavor_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "opts":
         opts_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "expmap":
