@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(PKG, "_lib", "libfsgpu.so")
 
 FSG_OK = 0
 FSG_INTERRUPTED = 1
+FSG_BUDGET = 2
 FSG_ERR_ARG = -1
 FSG_ERR_CUDA = -2
 FSG_ERR_NOMEM = -3
@@ -54,6 +55,7 @@ class Calc(ct.Structure):
         ("mode", I32), ("calc_dzndc", I32), ("interior", I32), ("bla", I32),
         ("flavor", I32), ("xr_semantics", I32), ("nexp", I32),
         ("backshift", I32), ("calc_d2zndc2", I32), ("block", I32), ("ctas_per_sm", I32),
+        ("iter_budget", I64),
     ]
 
 
@@ -102,8 +104,18 @@ SYMBOLS = [
     "fsg_ref_info", "fsg_ref_download", "fsg_std_tiles", "fsg_perturb_tiles",
     "fsg_last_stats", "fsg_cancel", "fsg_clear_cancel", "fsg_peak_flops",
     "fsg_std_tiles_noalloc", "fsg_ref_derive_bla", "fsg_postproc_fieldlines",
-    "fsg_postproc_normal",
+    "fsg_postproc_normal", "fsg_serve_open", "fsg_submit", "fsg_poll", "fsg_serve_info",
+    "fsg_serve_close",
 ]
+
+FSG_SERVE_FIFO = 0
+FSG_SERVE_SHORTEST = 1
+FSG_PENDING = 3
+
+
+class ServeStats(ct.Structure):
+    _fields_ = [("queued", I64), ("running", I64), ("reserved_bytes", I64),
+                ("peak_reserved_bytes", I64), ("budget_bytes", I64), ("slots", I32)]
 
 FSG_FIELDLINES_MAX_ITER = 64
 
@@ -144,6 +156,11 @@ def load():
         L.fsg_postproc_fieldlines.argtypes = [P, ct.POINTER(FieldlinesArgs), I32]
         L.fsg_postproc_normal.argtypes = [P, ct.POINTER(NormalArgs), I32]
         L.fsg_clear_cancel.argtypes = [P]
+        L.fsg_serve_open.argtypes = [P, I64, I32, I32]
+        L.fsg_submit.argtypes = [P, ct.POINTER(Calc), ct.POINTER(Tile), I32, F64, ct.POINTER(I64)]
+        L.fsg_poll.argtypes = [P, I64]
+        L.fsg_serve_info.argtypes = [P, ct.POINTER(ServeStats)]
+        L.fsg_serve_close.argtypes = [P]
         _lib = L
         return L
 
@@ -177,7 +194,7 @@ class Context:
             pass
 
     def check(self, rc, what):
-        if rc == FSG_OK or rc == FSG_INTERRUPTED:
+        if rc == FSG_OK or rc == FSG_INTERRUPTED or rc == FSG_BUDGET:
             return rc
         msg = self.L.fsg_last_error(self.h).decode()
         raise GPUError(f"{what} failed (code {rc}): {msg}")
@@ -215,6 +232,42 @@ class Context:
         arr = (Tile * len(tiles))(*tiles)
         return self.check(self.L.fsg_perturb_tiles(self.h, ct.byref(calc), arr, len(tiles), where),
                           "fsg_perturb_tiles")
+
+    # ------------------------------------------------------------------
+    # serving queue (fsg_serve_open / fsg_submit / fsg_poll)
+    def serve_open(self, hbm_budget, slots, order="fifo"):
+        o = {"fifo": FSG_SERVE_FIFO, "shortest": FSG_SERVE_SHORTEST}[order]
+        self._serve_keep = {}
+        self.check(self.L.fsg_serve_open(self.h, int(hbm_budget), int(slots), o),
+                   "fsg_serve_open")
+
+    def submit(self, calc, tiles, expected_work=0.0, keep=None):
+        """Queue host-buffer tiles; returns the ticket.  The tiles' arrays
+        (and ``keep``) are held until the request is polled finished."""
+        arr = (Tile * len(tiles))(*tiles)
+        t = I64(0)
+        self.check(self.L.fsg_submit(self.h, ct.byref(calc), arr, len(tiles),
+                                     float(expected_work), ct.byref(t)), "fsg_submit")
+        self._serve_keep[t.value] = (arr, calc, tiles, keep)
+        return t.value
+
+    def poll(self, ticket):
+        """None while the request is queued or running, else its outcome
+        (FSG_OK, FSG_BUDGET or FSG_INTERRUPTED; errors raise)."""
+        rc = self.L.fsg_poll(self.h, int(ticket))
+        if rc == FSG_PENDING:
+            return None
+        self._serve_keep.pop(int(ticket), None)
+        return self.check(rc, "fsg_poll")
+
+    def serve_info(self):
+        st = ServeStats()
+        self.check(self.L.fsg_serve_info(self.h, ct.byref(st)), "fsg_serve_info")
+        return {k: getattr(st, k) for k, _ in ServeStats._fields_}
+
+    def serve_close(self):
+        self.check(self.L.fsg_serve_close(self.h), "fsg_serve_close")
+        self._serve_keep = {}
 
     # ------------------------------------------------------------------
     def fieldlines(self, *, model, c, z, nu_frac, n, k, phi, is_backward, backshift):
@@ -433,7 +486,8 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
 
 def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
               calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False,
-              nexp=0, backshift=0, calc_d2zndc2=False, block=0, ctas_per_sm=0):
+              nexp=0, backshift=0, calc_d2zndc2=False, block=0, ctas_per_sm=0,
+              iter_budget=0):
     c = Calc()
     c.max_iter = int(max_iter)
     c.M_divergence = float(M_divergence)
@@ -449,4 +503,5 @@ def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
     c.calc_d2zndc2 = int(bool(calc_d2zndc2))
     c.block = int(block)
     c.ctas_per_sm = int(ctas_per_sm)
+    c.iter_budget = int(iter_budget)
     return c

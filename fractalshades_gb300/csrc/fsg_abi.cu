@@ -7,6 +7,8 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -45,7 +47,10 @@ void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
+struct ServeState;   // the serving queue (fsg_serve_open), below
+
 struct fsg_ctx {
+    ServeState *serve = nullptr;
     int device = 0;
     int sm_count = 0;
     cudaStream_t own_stream = nullptr;
@@ -54,6 +59,7 @@ struct fsg_ctx {
     volatile int *cancel_host = nullptr;   // pinned, mapped
     int *cancel_dev = nullptr;             // device alias of cancel_host
     int *status_dev = nullptr;
+    unsigned long long *used_dev = nullptr;  // iterations counted against the budget
     unsigned long long *counter_dev = nullptr;
     unsigned long long *stats_dev = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_desc = nullptr;
@@ -237,60 +243,80 @@ TileDev make_tile(const fsg_tile &t) {
     return d;
 }
 
-// Launch the iteration kernel over ntiles device-resident tiles.
-int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int ntiles,
-                 bool perturb) {
+// The launch resources of one stream: the context's own, or a serving slot's
+struct LaunchRes {
+    cudaStream_t stream;
+    TileDev *tiles_host; long long *start_host;        // pinned staging
+    TileDev *tiles_dev; long long *start_dev;
+    unsigned long long *counter_dev, *stats_dev, *used_dev;
+    int *status_dev;
+    cudaEvent_t ev_desc;       // staging reuse (nullptr: the caller orders it)
+    cudaEvent_t ev0, ev1;      // kernel timing (nullptr: none)
+};
+
+// Launch the iteration kernel over ntiles device-resident tiles on L.stream.
+int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const TileDev *tiles,
+              int ntiles, bool perturb) {
     // the descriptor staging buffer is reused: wait for the previous upload
-    CK(cudaEventSynchronize(ctx->ev_desc), "cudaEventSynchronize(descriptor upload)");
+    if (L.ev_desc) CK(cudaEventSynchronize(L.ev_desc), "cudaEventSynchronize(descriptor upload)");
     long long total = 0;
-    ctx->start_host[0] = 0;
+    L.start_host[0] = 0;
     for (int i = 0; i < ntiles; i++) {
-        ctx->tiles_host[i] = tiles[i];
+        L.tiles_host[i] = tiles[i];
         total += (long long)tiles[i].nx * tiles[i].ny;
-        ctx->start_host[i + 1] = total;
+        L.start_host[i + 1] = total;
     }
-    cudaStream_t s = ctx->stream;
-    CK(cudaMemcpyAsync(ctx->tiles_dev, ctx->tiles_host, sizeof(TileDev) * ntiles,
+    cudaStream_t s = L.stream;
+    CK(cudaMemcpyAsync(L.tiles_dev, L.tiles_host, sizeof(TileDev) * ntiles,
                        cudaMemcpyHostToDevice, s), "copy tile descriptors");
-    CK(cudaMemcpyAsync(ctx->start_dev, ctx->start_host, sizeof(long long) * (ntiles + 1),
+    CK(cudaMemcpyAsync(L.start_dev, L.start_host, sizeof(long long) * (ntiles + 1),
                        cudaMemcpyHostToDevice, s), "copy tile offsets");
-    CK(cudaEventRecord(ctx->ev_desc, s), "cudaEventRecord");
-    CK(cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), s), "reset counter");
-    CK(cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), s), "reset stats");
-    CK(cudaMemsetAsync(ctx->status_dev, 0, sizeof(int), s), "reset status");
+    if (L.ev_desc) CK(cudaEventRecord(L.ev_desc, s), "cudaEventRecord");
+    CK(cudaMemsetAsync(L.counter_dev, 0, sizeof(unsigned long long), s), "reset counter");
+    CK(cudaMemsetAsync(L.stats_dev, 0, 4 * sizeof(unsigned long long), s), "reset stats");
+    CK(cudaMemsetAsync(L.status_dev, 0, sizeof(int), s), "reset status");
+    CK(cudaMemsetAsync(L.used_dev, 0, sizeof(unsigned long long), s), "reset budget");
     WorkDev W;
-    W.tiles = ctx->tiles_dev; W.start = ctx->start_dev; W.ntiles = ntiles; W.total = total;
-    W.counter = ctx->counter_dev; W.stats = ctx->stats_dev;
-    W.cancel = ctx->cancel_dev; W.status = ctx->status_dev;
+    W.tiles = L.tiles_dev; W.start = L.start_dev; W.ntiles = ntiles; W.total = total;
+    W.counter = L.counter_dev; W.stats = L.stats_dev;
+    W.cancel = ctx->cancel_dev; W.status = L.status_dev;
+    W.budget = (unsigned long long)calc->iter_budget; W.used = L.used_dev;
     CalcDev C = make_calc(calc);
     // one persistent wave at the kernel's occupancy limit, or the tuned shape
     const int block = calc->block > 0 ? calc->block : default_block(calc, perturb);
     const int grid = calc->ctas_per_sm > 0 ? -calc->ctas_per_sm : 0;
-    CK(cudaEventRecord(ctx->ev0, s), "cudaEventRecord");
+    if (L.ev0) CK(cudaEventRecord(L.ev0, s), "cudaEventRecord");
     if (!perturb) fsg_launch_std(W, C, grid, block, s);
     else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
     else if (calc->mode == FSG_MODE_FE32) fsg_launch_perturb_bs_fe32(W, C, grid, block, s);
     else fsg_launch_perturb(W, C, grid, block, s);
     CK(cudaGetLastError(), "kernel launch");
-    CK(cudaEventRecord(ctx->ev1, s), "cudaEventRecord");
+    if (L.ev1) CK(cudaEventRecord(L.ev1, s), "cudaEventRecord");
+    return FSG_OK;
+}
+
+// Launch on the context's own stream, timed.
+int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int ntiles,
+                 bool perturb) {
+    LaunchRes L;
+    L.stream = ctx->stream;
+    L.tiles_host = ctx->tiles_host; L.start_host = ctx->start_host;
+    L.tiles_dev = ctx->tiles_dev; L.start_dev = ctx->start_dev;
+    L.counter_dev = ctx->counter_dev; L.stats_dev = ctx->stats_dev; L.used_dev = ctx->used_dev;
+    L.status_dev = ctx->status_dev;
+    L.ev_desc = ctx->ev_desc; L.ev0 = ctx->ev0; L.ev1 = ctx->ev1;
+    int rc = launch_on(ctx, L, calc, tiles, ntiles, perturb);
+    if (rc != FSG_OK) return rc;
     ctx->timed = true;
+    long long total = 0;
+    for (int i = 0; i < ntiles; i++) total += (long long)tiles[i].nx * tiles[i].ny;
     ctx->last_pixels = total;
     return FSG_OK;
 }
 
-int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
-              int32_t where, bool perturb) {
-    if (!ctx) return FSG_ERR_ARG;
-    if (!calc || !tiles || ntiles <= 0) return set_err(ctx, FSG_ERR_ARG, "no tiles");
-    if (ntiles > FSG_MAX_TILES_PER_LAUNCH) {
-        // split into several launches of at most FSG_MAX_TILES_PER_LAUNCH tiles
-        for (int32_t i = 0; i < ntiles; i += FSG_MAX_TILES_PER_LAUNCH) {
-            int32_t n = ntiles - i < FSG_MAX_TILES_PER_LAUNCH ? ntiles - i : FSG_MAX_TILES_PER_LAUNCH;
-            int rc = run_tiles(ctx, calc, tiles + i, n, where, perturb);
-            if (rc != FSG_OK) return rc;
-        }
-        return FSG_OK;
-    }
+// The checks of a calculation and its tiles (at most FSG_MAX_TILES_PER_LAUNCH)
+int check_calc_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+                     bool perturb) {
     if (calc->max_iter <= 0 || calc->max_iter > FSG_MAX_ITER_LIMIT)
         return set_err(ctx, FSG_ERR_ARG, "max_iter out of range (1 .. 2^30 - 1)");
     if (calc->flavor < 0 || calc->flavor > 5) return set_err(ctx, FSG_ERR_ARG, "bad flavor");
@@ -302,6 +328,7 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     if (perturb && calc->nexp != 0 && calc->mode == FSG_MODE_FE32)
         return set_err(ctx, FSG_ERR_ARG, "the power-n model runs in FSG_MODE_FP64 or FSG_MODE_XR64");
     if (calc->backshift < 0) return set_err(ctx, FSG_ERR_ARG, "backshift must be >= 0");
+    if (calc->iter_budget < 0) return set_err(ctx, FSG_ERR_ARG, "iter_budget must be >= 0");
     if (calc->backshift > 0 && perturb && calc->mode == FSG_MODE_FE32)
         return set_err(ctx, FSG_ERR_ARG, "calc_orbit runs in FSG_MODE_FP64 or FSG_MODE_XR64");
     if (calc->calc_d2zndc2 && (perturb || calc->flavor != 0))
@@ -317,21 +344,25 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         int rc = check_tile(ctx, tiles[i], perturb, calc);
         if (rc != FSG_OK) return rc;
     }
-    // tables of derived references may still be building on another stream:
-    // the launch stream waits for them on the device
+    return FSG_OK;
+}
+
+// tables of derived references may still be building on another stream:
+// the launch stream waits for them on the device
+int wait_references(fsg_ctx *ctx, const fsg_tile *tiles, int32_t ntiles, cudaStream_t s) {
     for (int32_t i = 0; i < ntiles; i++) {
         fsg_ref *r = tiles[i].ref;
         if (r && r->ready && (i == 0 || tiles[i - 1].ref != r))
-            CK(cudaStreamWaitEvent(ctx->stream, r->ready, 0), "cudaStreamWaitEvent(reference)");
+            CK(cudaStreamWaitEvent(s, r->ready, 0), "cudaStreamWaitEvent(reference)");
     }
-    std::vector<TileDev> td(ntiles);
-    if (where == FSG_DEVICE) {
-        for (int32_t i = 0; i < ntiles; i++) td[i] = make_tile(tiles[i]);
-        return launch_tiles(ctx, calc, td.data(), ntiles, perturb);
-    }
-    if (where != FSG_HOST) return set_err(ctx, FSG_ERR_ARG, "where must be FSG_HOST or FSG_DEVICE");
-    // host buffers: stage in the grow-only device scratch area
-    const size_t zsz = (calc->flavor == 0) ? 16 : 8;
+    return FSG_OK;
+}
+
+size_t zbytes(const fsg_calc *calc) { return calc->flavor == 0 ? 16 : 8; }
+
+// device bytes that host-buffer tiles occupy once staged
+size_t staged_bytes(const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles) {
+    const size_t zsz = zbytes(calc);
     size_t bytes = 0;
     for (int32_t i = 0; i < ntiles; i++) {
         const fsg_tile &t = tiles[i];
@@ -342,10 +373,14 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         if (t.potential) bytes += align_up(8 * np);
         if (t.dem) bytes += align_up(8 * np);
     }
-    int rc = ensure_scratch(ctx, bytes);
-    if (rc != FSG_OK) return rc;
-    char *p = ctx->scratch;
-    cudaStream_t s = ctx->stream;
+    return bytes;
+}
+
+// Copy host-buffer tiles' inputs to the device area at p (staged_bytes long)
+// and lay out their outputs there, on stream s; td receives the descriptors.
+int stage_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+                char *p, cudaStream_t s, TileDev *td) {
+    const size_t zsz = zbytes(calc);
     for (int32_t i = 0; i < ntiles; i++) {
         fsg_tile t = tiles[i];
         size_t np = (size_t)t.nx * t.ny;
@@ -366,17 +401,21 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         CK(cudaMemsetAsync(t.Z, 0, zsz * t.nZ * np, s), "zero Z");
         t.U = tiles[i].U ? (int32_t *)p : nullptr; p += align_up(4 * np);
         t.stop_reason = (int8_t *)p; p += align_up(np);
+        // -1 until a pixel stops: what a launch cut by its budget returns
+        // for the pixels it did not run
+        CK(cudaMemsetAsync(t.stop_reason, 0xff, np, s), "init stop_reason");
         t.stop_iter = (int32_t *)p; p += align_up(4 * np);
         if (t.potential) { t.potential = (double *)p; p += align_up(8 * np); }
         if (t.dem) { t.dem = (double *)p; p += align_up(8 * np); }
         td[i] = make_tile(t);
     }
-    rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
-    if (rc != FSG_OK) return rc;
-    // an interrupted launch leaves the caller's arrays untouched (the
-    // reference discards an interrupted tile, core.py:2545-2547)
-    rc = fsg_sync(ctx);
-    if (rc != FSG_OK) return rc;
+    return FSG_OK;
+}
+
+// Copy staged outputs back into the caller's host buffers, on stream s.
+int copy_back(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+              const TileDev *td, cudaStream_t s) {
+    const size_t zsz = zbytes(calc);
     for (int32_t i = 0; i < ntiles; i++) {
         const fsg_tile &t = tiles[i];
         const TileDev &d = td[i];
@@ -388,7 +427,49 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         if (t.potential) CK(cudaMemcpyAsync(t.potential, d.pot, 8 * np, cudaMemcpyDeviceToHost, s), "copy potential back");
         if (t.dem) CK(cudaMemcpyAsync(t.dem, d.dem, 8 * np, cudaMemcpyDeviceToHost, s), "copy dem back");
     }
-    return fsg_sync(ctx);
+    return FSG_OK;
+}
+
+int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+              int32_t where, bool perturb) {
+    if (!ctx) return FSG_ERR_ARG;
+    if (!calc || !tiles || ntiles <= 0) return set_err(ctx, FSG_ERR_ARG, "no tiles");
+    if (ntiles > FSG_MAX_TILES_PER_LAUNCH) {
+        // split into several launches of at most FSG_MAX_TILES_PER_LAUNCH tiles
+        for (int32_t i = 0; i < ntiles; i += FSG_MAX_TILES_PER_LAUNCH) {
+            int32_t n = ntiles - i < FSG_MAX_TILES_PER_LAUNCH ? ntiles - i : FSG_MAX_TILES_PER_LAUNCH;
+            int rc = run_tiles(ctx, calc, tiles + i, n, where, perturb);
+            if (rc != FSG_OK) return rc;
+        }
+        return FSG_OK;
+    }
+    int rc = check_calc_tiles(ctx, calc, tiles, ntiles, perturb);
+    if (rc != FSG_OK) return rc;
+    rc = wait_references(ctx, tiles, ntiles, ctx->stream);
+    if (rc != FSG_OK) return rc;
+    std::vector<TileDev> td(ntiles);
+    if (where == FSG_DEVICE) {
+        for (int32_t i = 0; i < ntiles; i++) td[i] = make_tile(tiles[i]);
+        return launch_tiles(ctx, calc, td.data(), ntiles, perturb);
+    }
+    if (where != FSG_HOST) return set_err(ctx, FSG_ERR_ARG, "where must be FSG_HOST or FSG_DEVICE");
+    // host buffers: stage in the grow-only device scratch area
+    rc = ensure_scratch(ctx, staged_bytes(calc, tiles, ntiles));
+    if (rc != FSG_OK) return rc;
+    rc = stage_tiles(ctx, calc, tiles, ntiles, ctx->scratch, ctx->stream, td.data());
+    if (rc != FSG_OK) return rc;
+    rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
+    if (rc != FSG_OK) return rc;
+    // an interrupted launch leaves the caller's arrays untouched (the
+    // reference discards an interrupted tile, core.py:2545-2547); one cut by
+    // its budget returns what it ran (stop_reason -1 elsewhere)
+    rc = fsg_sync(ctx);
+    if (rc != FSG_OK && rc != FSG_BUDGET) return rc;
+    const int launch_rc = rc;
+    rc = copy_back(ctx, calc, tiles, ntiles, td.data(), ctx->stream);
+    if (rc != FSG_OK) return rc;
+    rc = fsg_sync(ctx);
+    return rc == FSG_OK ? launch_rc : rc;
 }
 
 }  // namespace
@@ -431,6 +512,7 @@ int fsg_ctx_create(int device, fsg_ctx **out) {
         ctx->cancel_host = h;
         if (cudaHostGetDevicePointer((void **)&ctx->cancel_dev, h, 0) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
         if (cudaMalloc((void **)&ctx->status_dev, sizeof(int)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
+        if (cudaMalloc((void **)&ctx->used_dev, sizeof(unsigned long long)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
         if (cudaMalloc((void **)&ctx->counter_dev, sizeof(unsigned long long)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
         if (cudaMalloc((void **)&ctx->stats_dev, 4 * sizeof(unsigned long long)) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
         if (cudaMalloc((void **)&ctx->tiles_dev, sizeof(TileDev) * FSG_MAX_TILES_PER_LAUNCH) != cudaSuccess) { rc = FSG_ERR_NOMEM; break; }
@@ -449,9 +531,11 @@ int fsg_ctx_create(int device, fsg_ctx **out) {
 int fsg_ctx_destroy(fsg_ctx *ctx) {
     if (!ctx) return FSG_OK;
     cudaSetDevice(ctx->device);
+    if (ctx->serve) fsg_serve_close(ctx);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->status_dev) cudaFree(ctx->status_dev);
+    if (ctx->used_dev) cudaFree(ctx->used_dev);
     if (ctx->counter_dev) cudaFree(ctx->counter_dev);
     if (ctx->stats_dev) cudaFree(ctx->stats_dev);
     if (ctx->tiles_dev) cudaFree(ctx->tiles_dev);
@@ -483,7 +567,7 @@ int fsg_sync(fsg_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
     int st = 0;
     CK(cudaMemcpy(&st, ctx->status_dev, sizeof(int), cudaMemcpyDeviceToHost), "read status");
-    return st ? FSG_INTERRUPTED : FSG_OK;
+    return st == 1 ? FSG_INTERRUPTED : (st == 2 ? FSG_BUDGET : FSG_OK);
 }
 
 int fsg_cancel(fsg_ctx *ctx) {
@@ -941,6 +1025,278 @@ int fsg_last_stats(const fsg_ctx *cctx, fsg_stats *out) {
     out->full_steps = (int64_t)st[1];
     out->bla_steps = (int64_t)st[2];
     out->rebases = (int64_t)st[3];
+    return FSG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Serving queue.  Requests of host-buffer tiles are queued, admitted when a
+// launch slot is free and their staged device buffers fit in the HBM budget,
+// and run on the slots' own streams, so that several overlap on the device.
+// A slot owns its stream, work counter, statistics, budget and status words
+// and descriptor staging; a request's device buffers are one stream-ordered
+// allocation on its slot's stream, released when its results are back.
+// ---------------------------------------------------------------------------
+struct ServeSlot {
+    cudaStream_t stream = nullptr;
+    TileDev *tiles_host = nullptr; long long *start_host = nullptr;
+    TileDev *tiles_dev = nullptr; long long *start_dev = nullptr;
+    unsigned long long *words = nullptr;   // counter, stats[4], used
+    int *status_dev = nullptr;
+    cudaEvent_t done = nullptr;
+    int64_t ticket = -1;                   // running request, -1 when free
+};
+
+struct ServeReq {
+    fsg_calc calc;
+    std::vector<fsg_tile> tiles;
+    std::vector<TileDev> td;
+    bool perturb = false;
+    double work = 0.;
+    size_t bytes = 0;
+    int state = 0;                         // 0 queued, 1 running, 2 done
+    int rc = FSG_OK;
+    void *block = nullptr;
+    int slot = -1;
+};
+
+struct ServeState {
+    std::mutex m;
+    int64_t budget = 0;
+    int order = FSG_SERVE_FIFO;
+    std::vector<ServeSlot> slots;
+    std::map<int64_t, ServeReq> reqs;
+    int64_t next = 1;
+    int64_t reserved = 0, peak = 0;
+    int64_t queued = 0, running = 0;
+};
+
+namespace {
+
+void serve_free_slots(ServeState *S) {
+    for (ServeSlot &sl : S->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.tiles_host) cudaFreeHost(sl.tiles_host);
+        if (sl.start_host) cudaFreeHost(sl.start_host);
+        if (sl.tiles_dev) cudaFree(sl.tiles_dev);
+        if (sl.start_dev) cudaFree(sl.start_dev);
+        if (sl.words) cudaFree(sl.words);
+        if (sl.status_dev) cudaFree(sl.status_dev);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    S->slots.clear();
+}
+
+// Start a queued request on slot k (the caller holds the lock).  A failure
+// marks the request done with its error code.
+void serve_start(fsg_ctx *ctx, ServeState *S, int k, int64_t ticket, ServeReq &R) {
+    ServeSlot &sl = S->slots[k];
+    R.state = 1; R.slot = k; sl.ticket = ticket;
+    S->queued--; S->running++;
+    S->reserved += (int64_t)R.bytes;
+    if (S->reserved > S->peak) S->peak = S->reserved;
+    int rc = FSG_OK;
+    cudaError_t e = cudaMallocAsync(&R.block, R.bytes, sl.stream);
+    if (e != cudaSuccess) rc = cuda_err(ctx, e, "cudaMallocAsync(request)");
+    if (rc == FSG_OK) rc = wait_references(ctx, R.tiles.data(), (int32_t)R.tiles.size(), sl.stream);
+    if (rc == FSG_OK) {
+        R.td.resize(R.tiles.size());
+        rc = stage_tiles(ctx, &R.calc, R.tiles.data(), (int32_t)R.tiles.size(), (char *)R.block,
+                         sl.stream, R.td.data());
+    }
+    if (rc == FSG_OK) {
+        LaunchRes L;
+        L.stream = sl.stream;
+        L.tiles_host = sl.tiles_host; L.start_host = sl.start_host;
+        L.tiles_dev = sl.tiles_dev; L.start_dev = sl.start_dev;
+        L.counter_dev = sl.words; L.stats_dev = sl.words + 1; L.used_dev = sl.words + 5;
+        L.status_dev = sl.status_dev;
+        // the slot's staging is reused only after its request has retired
+        L.ev_desc = nullptr; L.ev0 = nullptr; L.ev1 = nullptr;
+        rc = launch_on(ctx, L, &R.calc, R.td.data(), (int)R.td.size(), R.perturb);
+    }
+    if (rc == FSG_OK) {
+        e = cudaEventRecord(sl.done, sl.stream);
+        if (e != cudaSuccess) rc = cuda_err(ctx, e, "cudaEventRecord(request)");
+    }
+    if (rc != FSG_OK) {
+        cudaStreamSynchronize(sl.stream);
+        if (R.block) cudaFreeAsync(R.block, sl.stream);
+        R.block = nullptr;
+        S->reserved -= (int64_t)R.bytes;
+        S->running--;
+        sl.ticket = -1;
+        R.state = 2; R.rc = rc;
+    }
+}
+
+// Retire finished requests: results into the caller's buffers (unless the
+// launch was interrupted), device buffers released.
+void serve_retire(fsg_ctx *ctx, ServeState *S) {
+    for (ServeSlot &sl : S->slots) {
+        if (sl.ticket < 0) continue;
+        if (cudaEventQuery(sl.done) != cudaSuccess) continue;
+        ServeReq &R = S->reqs[sl.ticket];
+        int st = 0, rc = FSG_OK;
+        cudaError_t e = cudaMemcpyAsync(&st, sl.status_dev, sizeof(int), cudaMemcpyDeviceToHost,
+                                        sl.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sl.stream);
+        if (e != cudaSuccess) rc = cuda_err(ctx, e, "read request status");
+        const int launch_rc = st == 1 ? FSG_INTERRUPTED : (st == 2 ? FSG_BUDGET : FSG_OK);
+        if (rc == FSG_OK && launch_rc != FSG_INTERRUPTED) {
+            rc = copy_back(ctx, &R.calc, R.tiles.data(), (int32_t)R.tiles.size(), R.td.data(),
+                           sl.stream);
+            if (rc == FSG_OK) {
+                e = cudaStreamSynchronize(sl.stream);
+                if (e != cudaSuccess) rc = cuda_err(ctx, e, "copy request back");
+            }
+        }
+        cudaFreeAsync(R.block, sl.stream);
+        R.block = nullptr;
+        S->reserved -= (int64_t)R.bytes;
+        S->running--;
+        R.state = 2;
+        R.rc = rc == FSG_OK ? launch_rc : rc;
+        sl.ticket = -1;
+    }
+}
+
+// Admit queued requests in the configured order while a slot is free and the
+// next request fits in the budget (the next one waits: no overtaking).
+void serve_admit(fsg_ctx *ctx, ServeState *S) {
+    for (;;) {
+        int k = -1;
+        for (int i = 0; i < (int)S->slots.size(); i++)
+            if (S->slots[i].ticket < 0) { k = i; break; }
+        if (k < 0) return;
+        int64_t best = -1;
+        for (auto &kv : S->reqs) {
+            if (kv.second.state != 0) continue;
+            if (best < 0) { best = kv.first; if (S->order == FSG_SERVE_FIFO) break; continue; }
+            if (kv.second.work < S->reqs[best].work) best = kv.first;
+        }
+        if (best < 0) return;
+        ServeReq &R = S->reqs[best];
+        if (S->reserved + (int64_t)R.bytes > S->budget) return;
+        serve_start(ctx, S, k, best, R);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsg_serve_open(fsg_ctx *ctx, int64_t hbm_budget_bytes, int32_t slots, int32_t order) {
+    if (!ctx) return FSG_ERR_ARG;
+    if (ctx->serve) return set_err(ctx, FSG_ERR_ARG, "the serving queue is already open");
+    if (hbm_budget_bytes <= 0 || slots <= 0 || slots > 64)
+        return set_err(ctx, FSG_ERR_ARG, "serving: budget > 0 and 1 .. 64 slots");
+    if (order != FSG_SERVE_FIFO && order != FSG_SERVE_SHORTEST)
+        return set_err(ctx, FSG_ERR_ARG, "serving: order FSG_SERVE_FIFO or FSG_SERVE_SHORTEST");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ServeState *S = new (std::nothrow) ServeState();
+    if (!S) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
+    S->budget = hbm_budget_bytes; S->order = order;
+    S->slots.resize(slots);
+    const size_t nt = FSG_MAX_TILES_PER_LAUNCH;
+    for (ServeSlot &sl : S->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&sl.tiles_host, sizeof(TileDev) * nt);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&sl.start_host, sizeof(long long) * (nt + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&sl.tiles_dev, sizeof(TileDev) * nt);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&sl.start_dev, sizeof(long long) * (nt + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&sl.words, 6 * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&sl.status_dev, sizeof(int));
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            serve_free_slots(S);
+            delete S;
+            return cuda_err(ctx, e, "serving slot");
+        }
+    }
+    ctx->serve = S;
+    return FSG_OK;
+}
+
+int fsg_submit(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+               double expected_work, int64_t *ticket) {
+    if (!ctx || !ticket) return FSG_ERR_ARG;
+    *ticket = 0;
+    ServeState *S = ctx->serve;
+    if (!S) return set_err(ctx, FSG_ERR_ARG, "fsg_serve_open first");
+    if (!calc || !tiles || ntiles <= 0) return set_err(ctx, FSG_ERR_ARG, "no tiles");
+    if (ntiles > FSG_MAX_TILES_PER_LAUNCH)
+        return set_err(ctx, FSG_ERR_LIMIT, "more tiles than one launch takes");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const bool perturb = tiles[0].ref != nullptr;
+    for (int32_t i = 1; i < ntiles; i++)
+        if ((tiles[i].ref != nullptr) != perturb)
+            return set_err(ctx, FSG_ERR_ARG, "a request mixes perturbation and standard tiles");
+    int rc = check_calc_tiles(ctx, calc, tiles, ntiles, perturb);
+    if (rc != FSG_OK) return rc;
+    const size_t bytes = staged_bytes(calc, tiles, ntiles);
+    std::lock_guard<std::mutex> lock(S->m);
+    if ((int64_t)bytes > S->budget)
+        return set_err(ctx, FSG_ERR_LIMIT, "request larger than the serving budget");
+    const int64_t t = S->next++;
+    ServeReq &R = S->reqs[t];
+    R.calc = *calc;
+    R.tiles.assign(tiles, tiles + ntiles);
+    R.perturb = perturb;
+    long long px = 0;
+    for (int32_t i = 0; i < ntiles; i++) px += (long long)tiles[i].nx * tiles[i].ny;
+    R.work = expected_work > 0. ? expected_work : (double)px;
+    R.bytes = bytes;
+    S->queued++;
+    serve_retire(ctx, S);
+    serve_admit(ctx, S);
+    *ticket = t;
+    return FSG_OK;
+}
+
+int fsg_poll(fsg_ctx *ctx, int64_t ticket) {
+    if (!ctx) return FSG_ERR_ARG;
+    ServeState *S = ctx->serve;
+    if (!S) return set_err(ctx, FSG_ERR_ARG, "fsg_serve_open first");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    std::lock_guard<std::mutex> lock(S->m);
+    serve_retire(ctx, S);
+    serve_admit(ctx, S);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return set_err(ctx, FSG_ERR_ARG, "unknown ticket");
+    if (it->second.state != 2) return FSG_PENDING;
+    const int rc = it->second.rc;
+    S->reqs.erase(it);
+    return rc;
+}
+
+int fsg_serve_info(fsg_ctx *ctx, fsg_serve_stats *out) {
+    if (!ctx || !out) return FSG_ERR_ARG;
+    ServeState *S = ctx->serve;
+    if (!S) return set_err(ctx, FSG_ERR_ARG, "fsg_serve_open first");
+    std::lock_guard<std::mutex> lock(S->m);
+    out->queued = S->queued; out->running = S->running;
+    out->reserved_bytes = S->reserved; out->peak_reserved_bytes = S->peak;
+    out->budget_bytes = S->budget; out->slots = (int32_t)S->slots.size();
+    return FSG_OK;
+}
+
+int fsg_serve_close(fsg_ctx *ctx) {
+    if (!ctx) return FSG_ERR_ARG;
+    ServeState *S = ctx->serve;
+    if (!S) return FSG_OK;
+    cudaSetDevice(ctx->device);
+    {
+        std::lock_guard<std::mutex> lock(S->m);
+        for (ServeSlot &sl : S->slots)
+            if (sl.stream) cudaStreamSynchronize(sl.stream);
+        serve_retire(ctx, S);
+        serve_free_slots(S);
+    }
+    delete S;
+    ctx->serve = nullptr;
     return FSG_OK;
 }
 

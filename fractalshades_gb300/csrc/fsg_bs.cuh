@@ -923,7 +923,9 @@ k_perturb_bs(WorkDev W, CalcDev C) {
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
+        const unsigned long long before = itsum;
         pixel_bs<T, FL>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        fsg_account(W, itsum - before);
     }
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }

@@ -133,12 +133,21 @@ struct WorkDev {
     unsigned long long *counter;
     unsigned long long *stats;       // [4]: pixel_iters, full_steps, bla_steps, rebases
     volatile int *cancel;            // mapped host flag
-    int *status;                     // device status word (1 = interrupted)
+    int *status;                     // device status word (1 = interrupted, 2 = budget)
+    unsigned long long budget;       // iteration budget of the launch (0: none)
+    unsigned long long *used;        // iterations of the pixels finished so far
 };
 
-// Claim the next pixel: returns false when the work is exhausted.
+// Claim the next pixel: returns false when the work is exhausted, or when
+// the pixels finished so far have used the launch's iteration budget (the
+// status word then reads 2; pixels already claimed run to their end, the
+// others are left as they were for the caller to submit again).
 __device__ __forceinline__ bool fsg_claim(const WorkDev &W, const long long *s_start,
                                           int &t, long long &ip) {
+    if (W.budget && *(volatile unsigned long long *)W.used >= W.budget) {
+        *W.status = 2;
+        return false;
+    }
     unsigned long long g = atomicAdd(W.counter, 1ULL);
     if ((long long)g >= W.total) return false;
     int lo = 0, hi = W.ntiles - 1;
@@ -149,6 +158,11 @@ __device__ __forceinline__ bool fsg_claim(const WorkDev &W, const long long *s_s
     t = lo;
     ip = (long long)g - s_start[lo];
     return true;
+}
+
+// a finished pixel's iterations, counted against the launch's budget
+__device__ __forceinline__ void fsg_account(const WorkDev &W, unsigned long long n) {
+    if (W.budget) atomicAdd(W.used, n);
 }
 
 // the host's interruption flag: sets the launch status and stops claiming

@@ -103,6 +103,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     if (calc->nexp != 0 && (calc->flavor != 0 || calc->nexp < 2)) return FSG_ERR_ARG;
     if (calc->nexp > FSG_MN_MAX_EXP) return FSG_ERR_LIMIT;
     if (calc->backshift != 0 || calc->calc_d2zndc2 != 0) return FSG_ERR_ARG;  // fsg_std_tiles
+    if (calc->iter_budget != 0) return FSG_ERR_ARG;     // no budget counter in the array
     const int nZ_min = calc->flavor == 0 ? 3 : 6;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return FSG_ERR_NODEV;
@@ -144,6 +145,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     W.tiles = S->tiles; W.start = S->start; W.ntiles = ntiles; W.total = total;
     W.counter = &S->counter; W.stats = S->stats;
     W.cancel = &S->cancel; W.status = &S->status;
+    W.budget = 0ULL; W.used = nullptr;
     CalcDev C;
     C.max_iter = (int)calc->max_iter;
     C.M2 = calc->M_divergence * calc->M_divergence;

@@ -238,7 +238,9 @@ __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
     while (true) {
         if (*W.cancel) { *W.status = 1; break; }
         if (!fsg_claim(W, s_start, t, ip)) break;
+        const unsigned long long before = itsum;
         pixel_m2<XR, MN, ORB>(W.tiles[t], C, ip, nfull, nbla, nreb, itsum);
+        fsg_account(W, itsum - before);
     }
     fsg_flush_stats(W, itsum, nfull, nbla, nreb);
 }

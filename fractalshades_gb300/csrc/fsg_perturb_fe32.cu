@@ -585,6 +585,7 @@ __global__ void __launch_bounds__(FE32_BLOCK, INTERIOR ? 6 : 7) k_perturb_m2_fe3
         if (!fsg_claim(W, s_start, t, ip)) break;
         unsigned nfull = 0, nbla = 0, nreb = 0;
         const int n = pixel_fe32<INTERIOR>(W.tiles[t], C, ip, nfull, nbla, nreb);
+        fsg_account(W, (unsigned long long)n);
         s_acc[0][threadIdx.x] += (unsigned long long)n;
         s_acc[1][threadIdx.x] += nfull;
         s_acc[2][threadIdx.x] += nbla;

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
                     Z[(long long)T.i_orb * np + ip] = zo;
                 }
                 T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
-                it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+                it_sum += (unsigned long long)n; fsg_account(W, (unsigned long long)n); steps += (unsigned long long)(n - 1);
                 have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
                 if (have) {
                     c = std_c(W.tiles[t], ip);
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
                     Z[(long long)T.i_orb * np + ip] = zo;
                 }
                 T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
-                it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+                it_sum += (unsigned long long)n; fsg_account(W, (unsigned long long)n); steps += (unsigned long long)(n - 1);
                 have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
             drained |= !have;
                 if (have) {
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
                 Z[(long long)(T.i_orb + 1) * np + ip] = yo;
             }
             T.stop_iter[ip] = n; T.stop_reason[ip] = reason;
-            it_sum += (unsigned long long)n; steps += (unsigned long long)(n - 1);
+            it_sum += (unsigned long long)n; fsg_account(W, (unsigned long long)n); steps += (unsigned long long)(n - 1);
             have = !fsg_cancelled(W) && fsg_claim(W, s_start, t, ip);
             drained |= !have;
             if (have) {

@@ -38,6 +38,7 @@ extern "C" {
 
 #define FSG_OK 0
 #define FSG_INTERRUPTED 1      /* USER_INTERRUPTED (perturbation.py:984)      */
+#define FSG_BUDGET 2           /* the launch's fsg_calc.iter_budget was used   */
 #define FSG_ERR_ARG (-1)
 #define FSG_ERR_CUDA (-2)
 #define FSG_ERR_NOMEM (-3)
@@ -131,6 +132,15 @@ typedef struct {
                                  0 = the occupancy limit, else at most that
                                  many (the allocation-free entry point keeps
                                  its fixed shape)                             */
+    int64_t iter_budget;      /* 0: none.  Else the launch stops claiming pixels
+                                 once the pixels it finished have used this many
+                                 iterations: pixels already claimed run to their
+                                 end, the others keep their stop_reason (-1 for
+                                 the reference's fresh arrays, core.py:2070-2073;
+                                 host-buffer calls copy -1 back for them), and the
+                                 call returns FSG_BUDGET -- submit those pixels
+                                 again to finish.  No counterpart in the
+                                 reference (it runs a tile to its end)         */
 } fsg_calc;
 
 /* One tile: a rectangle of pixels with its own view and outputs. */
@@ -280,6 +290,48 @@ int fsg_peak_flops(fsg_ctx *ctx, int32_t fp64, double *tflops);
 int fsg_cancel(fsg_ctx *ctx);
 int fsg_clear_cancel(fsg_ctx *ctx);
 
+/* Serving queue for interactive rendering.  No counterpart in the reference,
+ * which renders one image at a time (its GUI runs one script,
+ * gui/guimodel.py); the submit / poll pair is the asynchronous form of
+ * fsg_std_tiles / fsg_perturb_tiles with host buffers, with the reference's
+ * interruption contract (core.py:2545-2547).
+ *   fsg_serve_open: `slots` launch streams of the context (each runs one
+ *     request at a time, so up to `slots` requests overlap on the device) and
+ *     an HBM budget for the requests' staged buffers (their inputs and
+ *     outputs on the device: what fsg_perturb_tiles stages for host buffers);
+ *   fsg_submit: queues a request of host-buffer tiles (at most
+ *     FSG_MAX_TILES_PER_LAUNCH; all perturbation tiles, with references, or
+ *     all standard tiles) and returns its ticket at once.  The caller keeps
+ *     every buffer of the tiles, and the references, alive until fsg_poll
+ *     reports the request finished.  A request is admitted when a slot is
+ *     free and its staged bytes fit in what the budget has left; the next one
+ *     in `order` waits for that (FSG_SERVE_FIFO: arrival order;
+ *     FSG_SERVE_SHORTEST: smallest expected_work first, the caller's estimate,
+ *     e.g. pixels x expected iterations; <= 0 means the pixel count);
+ *     FSG_ERR_LIMIT for a request larger than the whole budget;
+ *   fsg_poll: FSG_PENDING while queued or running; once finished, the
+ *     request's outcome (FSG_OK, FSG_BUDGET, FSG_INTERRUPTED with the
+ *     caller's arrays untouched, or an error code), its results in the
+ *     caller's buffers, and the ticket released.  Polling also retires
+ *     finished launches and admits queued requests: call it regularly;
+ *   fsg_serve_close: waits for running requests, drops queued ones;
+ *     fsg_ctx_destroy closes an open queue.
+ * fsg_cancel interrupts running and later-admitted requests alike. */
+#define FSG_SERVE_FIFO 0
+#define FSG_SERVE_SHORTEST 1
+#define FSG_PENDING 3          /* fsg_poll: the request is not finished yet    */
+typedef struct {
+    int64_t queued, running;
+    int64_t reserved_bytes, peak_reserved_bytes, budget_bytes;
+    int32_t slots;
+} fsg_serve_stats;
+int fsg_serve_open(fsg_ctx *ctx, int64_t hbm_budget_bytes, int32_t slots, int32_t order);
+int fsg_submit(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+               double expected_work, int64_t *ticket);
+int fsg_poll(fsg_ctx *ctx, int64_t ticket);
+int fsg_serve_info(fsg_ctx *ctx, fsg_serve_stats *out);
+int fsg_serve_close(fsg_ctx *ctx);
+
 /* Allocation-free variant of fsg_std_tiles.  It has no counterpart in the
  * reference: it serves callers that cannot call cudaMalloc -- their device
  * memory is reserved up front by another allocator, or they cannot afford the
@@ -304,6 +356,7 @@ int fsg_clear_cancel(fsg_ctx *ctx);
  *     consumed on entry (cudaGetLastError), so FSG_ERR_CUDA reports this
  *     call's own launches;
  *   - max_iter in 1 .. FSG_MAX_ITER_LIMIT, like fsg_std_tiles;
+ *   - no iteration budget (fsg_calc.iter_budget must be 0, else FSG_ERR_ARG);
  *   - not cancellable (fsg_cancel does not apply). */
 #define FSG_NOALLOC_MAX_TILES 64
 int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,

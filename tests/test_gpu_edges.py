@@ -163,3 +163,58 @@ def test_malformed_input_is_refused(ctx):
         ctx.std_tiles(nat.make_calc(max_iter=2 ** 31 - 1, M_divergence=1000.), [t])
     with pytest.raises(RuntimeError):
         ctx.std_tiles(calc, [])                        # no tiles
+
+
+@pytest.mark.parametrize("kind", ["std", "fe32", "fp64"])
+def test_iteration_budget_and_resubmission(ctx, kind):
+    """fsg_calc.iter_budget: a launch stops claiming pixels once the pixels it
+    finished have used the budget and returns FSG_BUDGET; the pixels it did
+    not run keep stop_reason -1 (host buffers); submitting those again
+    completes the image, bit for bit equal to one unbudgeted launch.  (The
+    images hold more pixels than one wave of the persistent grid claims.)"""
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import synthetic as syn
+    if kind == "std":
+        xs, ys = syn.image_axes(800, 600, 4. / 3.)
+        ref, mk_calc = None, lambda b: nat.make_calc(max_iter=1000, M_divergence=1000.,
+                                                     epsilon_stationnary=0.01, iter_budget=b)
+        nZ, tile_kw, run = 3, dict(center=-0.5 + 0j, dx=3.0), ctx.std_tiles
+    else:
+        w = syn.seahorse_workload(nx=512)
+        xs, ys = w.xs, w.ys
+        ref = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order, calc_dzndc=True,
+                            scale_m=w.dx_m, scale_e=w.dx_e, bla=True, kc=w.kc, bla_eps=1e-6)
+        mk_calc = lambda b: nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=kind,
+                                          calc_dzndc=True, bla=True, iter_budget=b)
+        nZ = 2
+        tile_kw = dict(ref=ref, dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m,
+                       drift_e=w.drift_e, i_dzndc=1)
+        run = ctx.perturb_tiles
+    pix = (np.asarray(xs)[None, :] + 1j * np.asarray(ys)[:, None]).ravel()
+    n = pix.size
+
+    def launch(p, budget):
+        p = np.ascontiguousarray(p)
+        Z = np.zeros((nZ, p.size), dtype=np.complex128)
+        sr = -np.ones((1, p.size), dtype=np.int8)
+        si = np.zeros((1, p.size), dtype=np.int32)
+        t = nat.make_tile(pix=p, lin_mat=LIN, Z=Z, stop_reason=sr, stop_iter=si, **tile_kw)
+        rc = run(mk_calc(budget), [t])
+        return rc, Z, sr[0], si[0]
+
+    rc, Zf, srf, sif = launch(pix, 0)
+    assert rc == nat.FSG_OK
+    budget = int(sif.astype(np.int64).sum() // 5)
+    rc, Z1, sr1, si1 = launch(pix, budget)
+    assert rc == nat.FSG_BUDGET
+    left = np.flatnonzero(sr1 == -1)
+    assert 0 < left.size < n
+    # claims stop only once the finished pixels reach the budget
+    assert si1[sr1 != -1].astype(np.int64).sum() >= budget
+    rc, Z2, sr2, si2 = launch(pix[left], 0)
+    assert rc == nat.FSG_OK
+    Z1[:, left], sr1[left], si1[left] = Z2, sr2, si2
+    assert np.array_equal(si1, sif) and np.array_equal(sr1, srf)
+    assert np.array_equal(Z1.view(np.uint64), Zf.view(np.uint64))
+    if ref is not None:
+        ref.free()
