@@ -47,9 +47,9 @@ def parse():
                     help="requests of the serving stream (0: skip)")
     ap.add_argument("--no-supplementary", action="store_true",
                     help="skip the standard-loop, 1e-1000 and Burning Ship configurations")
-    ap.add_argument("--legs", default="std,deep,edge,seahorse,bs,host",
+    ap.add_argument("--legs", default="std,deep,edge,seahorse,bs,bs_edge,model_api,host",
                     help="supplementary configurations to run (std, deep, edge, seahorse, bs, "
-                         "host)")
+                         "bs_edge, model_api, host)")
     ap.add_argument("--bs-tiles", type=int, default=64,
                     help="Burning Ship tiles of the 64 to run (a smaller case for profiling)")
     ap.add_argument("--parity-pixels", type=int, default=262144,
@@ -60,26 +60,17 @@ def parse():
     ap.add_argument("--no-headline", action="store_true",
                     help="run the supplementary legs only (a profiling case: no headline "
                          "steps, no bench line)")
-    ap.add_argument("--bs-max-iter", type=int, default=2000,
-                    help="max_iter of the Burning Ship configuration (its own is 5e4: "
-                         "minutes in FP64 on one GPU)")
+    ap.add_argument("--bs-max-iter", type=int, default=50000,
+                    help="max_iter of the Burning Ship configuration (its own, 5e4; FP64 runs "
+                         "on a subset of the tiles)")
     return ap.parse_args()
 
 
-def serving_leg(n_requests, device):
-    """The serving stream: Poisson arrivals at 200/s, tiles of 256..2048
-    squared, widths log-uniform in [1e-1000, 1e-10] around 8 seeded period-p
-    nuclei (1100 digits), max_iter 2e5, FP32+exp deltas, 120 GB HBM budget."""
-    from fractalshades_gb300 import serving as srv
-    rng = np.random.default_rng(5)
-    periods = [int(p) for p in rng.integers(300, 3001, 8)]
-    t0 = time.perf_counter()
-    centers = [srv.make_center(p, 1100, 200000) for p in periods]
-    setup_s = time.perf_counter() - t0
-    reqs = srv.request_stream(centers, n_requests, rate=200.0, seed=5)
-    server = srv.TileServer(centers, hbm_budget=120 * 2 ** 30, n_slots=3,
+def _serve_once(srv, centers, reqs, budget, order, device, n_slots=None):
+    server = srv.TileServer(centers, hbm_budget=budget, n_slots=n_slots,
                             max_batch_pixels=8 * 2 ** 20, mode="fe32", device=device,
-                            keep_results=False)
+                            keep_results=False, order=order)
+    slots = len(server.slots)
     t0 = time.perf_counter()
     try:
         done = server.run(reqs, realtime=True, timeout=600)
@@ -87,24 +78,52 @@ def serving_leg(n_requests, device):
         wall = time.perf_counter() - t0
         server.close()
     lat = np.array([(r.done - r.arrival) * 1e3 for r in done])
+    sides = np.array([r.side for r in done])
     iters = float(sum(r.pixel_iters for r in done))
-    return {"requests": len(done), "rate_per_s": 200.0, "wall_s": wall,
-            "arrival_span_s": float(max(r.arrival for r in done) - t0),
-            "pixel_iters": iters, "results_to_host_gb": float(
-                sum(r.side ** 2 for r in done) * srv.BYTES_PER_PIXEL / 1e9),
-            "pixel_iter_per_s": iters / wall, "latency_ms": {
-                "p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                "max": float(lat.max())},
-            "slots": 3, "hbm_budget_gb": 120, "peak_reserved_gb": server.max_reserved / 2 ** 30,
-            "centers": periods, "center_setup_s": setup_s,
-            "sides": [256, 512, 1024, 2048], "widths": "1e-1000 .. 1e-10 log-uniform"}
+
+    def pct(a):
+        return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)),
+                "max": float(a.max()), "n": int(a.size)}
+    return {"order": order, "slots": slots, "hbm_budget_gb": budget / 2 ** 30,
+            "peak_reserved_gb": server.max_reserved / 2 ** 30, "requests": len(done),
+            "wall_s": wall, "pixel_iters": iters, "pixel_iter_per_s": iters / wall,
+            "latency_ms": pct(lat),
+            "latency_ms_by_side": {str(k): pct(lat[sides == k]) for k in sorted(set(sides))},
+            "results_to_host_gb": float(sum(r.side ** 2 for r in done) * srv.BYTES_PER_PIXEL
+                                        / 1e9)}
+
+
+def serving_leg(n_requests, device):
+    """The serving stream: Poisson arrivals at 200/s, tiles of 256..2048
+    squared, widths log-uniform in [1e-1000, 1e-10] around 8 seeded period-p
+    nuclei (1100 digits), max_iter 2e5, FP32+exp deltas, 120 GB HBM budget --
+    served in arrival order and shortest-expected-work first; then the first
+    300 requests under a 1 GB budget, where admission by HBM binds."""
+    from fractalshades_gb300 import serving as srv
+    rng = np.random.default_rng(5)
+    periods = [int(p) for p in rng.integers(300, 3001, 8)]
+    t0 = time.perf_counter()
+    centers = [srv.make_center(p, 1100, 200000) for p in periods]
+    setup_s = time.perf_counter() - t0
+    out = {"rate_per_s": 200.0, "centers": periods, "center_setup_s": setup_s,
+           "sides": [256, 512, 1024, 2048], "widths": "1e-1000 .. 1e-10 log-uniform",
+           "slots_rule": "as many as the budget holds 8 Mpixel batches, at most 4 (one "
+                         "persistent launch fills the GPU)"}
+    for order in ("fifo", "shortest"):
+        reqs = srv.request_stream(centers, n_requests, rate=200.0, seed=5)
+        out[order] = _serve_once(srv, centers, reqs, 120 * 2 ** 30, order, device)
+    reqs = srv.request_stream(centers, min(300, n_requests), rate=200.0, seed=5)
+    out["fifo_1gb"] = _serve_once(srv, centers, reqs, 2 ** 30, "fifo", device)
+    return out
 
 
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
-                  legs=("std", "deep", "edge", "seahorse", "bs", "host"), bs_tiles=64, edge_nx=1024,
+                  legs=("std", "deep", "edge", "seahorse", "bs", "bs_edge", "model_api", "host"),
+                  bs_tiles=64,
+                  edge_nx=1024,
                   parity_pixels=16384):
     """The other measured configurations, one launch each (kernel time from
     the library's CUDA events, L2 flushed before each launch):
@@ -228,52 +247,93 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
             "every pixel escapes (median 1061 iterations)")
 
     if "bs" in legs:
-        # Burning Ship: 64 tiles of 256..2048 squared, one launch, FP64
-        tiles4 = syn.config4_workload(max_iter=bs_max_iter)[:bs_tiles]
-        refs4, keep, ts = [], [], []
-        for t in tiles4:
-            r = nat.Reference(ctx, t.Zn, div_iter=t.div_iter, order=t.ref_order, flavor=1,
-                              calc_dzndc=True, scale_m=t.dx_m, scale_e=t.dx_e, bla=True, kc=t.kc,
-                              bla_eps=1e-6)
-            m = t.side * t.side
-            xs = torch.from_numpy(t.xs).to(dev)
-            ys = torch.from_numpy(t.ys).to(dev)
-            Z = torch.zeros((6, m), **f64)
-            sr = torch.zeros(m, dtype=torch.int8, device=dev)
-            si = torch.zeros(m, dtype=torch.int32, device=dev)
-            U = torch.zeros(m, dtype=torch.int32, device=dev)
-            keep += [xs, ys, Z, sr, si, U]
-            refs4.append(r)
-            ts.append(nat.make_tile_ptrs(nx=t.side, ny=t.side, xs_ptr=xs.data_ptr(),
-                                         ys_ptr=ys.data_ptr(), lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=6,
-                                         stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
-                                         U_ptr=U.data_ptr(), ref=r, dx_m=t.dx_m, dx_e=t.dx_e,
-                                         drift_m=t.driftx_m, drift_e=t.driftx_e,
-                                         drifty_m=t.drifty_m, drifty_e=t.drifty_e))
-        def c4(mode):
-            return nat.make_calc(max_iter=bs_max_iter, M_divergence=1000., flavor=1,
-                                 calc_dzndc=True, bla=True, mode=mode)
-        si4 = keep[4::6]
-        k4f, st4f = timed(lambda: ctx.perturb_tiles(c4("fe32"), ts, nat.DEVICE), 1, 1)
-        si_fe = np.concatenate([t.cpu().numpy() for t in si4])
-        k4, st4 = timed(lambda: ctx.perturb_tiles(c4("fp64"), ts, nat.DEVICE), 1, 0)
-        si_64 = np.concatenate([t.cpu().numpy() for t in si4])
-        out["burning_ship_64_tiles"] = {
-            "workload": f"Burning Ship, {len(tiles4)} tiles of side 256..2048 (log-uniform), widths 1e-200..1e-30, "
-                        f"centres from the BS ball method + Newton at 250 digits, max_iter {bs_max_iter}, "
-                        "M 1e3, Hessian, one launch",
-            "pixels": int(sum(t.side ** 2 for t in tiles4)), "pixel_iters": int(st4["pixel_iters"]),
-            "periods": sorted({t.order for t in tiles4 if t.order}),
-            "kernel_ms": k4, "value": st4["pixel_iters"] / (k4 * 1e-3), "unit": "pixel-iter/s",
-            "dtype": "f64",
-            "fe32": {"kernel_ms": k4f, "value": st4f["pixel_iters"] / (k4f * 1e-3),
-                     "speedup_vs_fp64": (st4f["pixel_iters"] / k4f) / (st4["pixel_iters"] / k4),
-                     "iter_count_differs_frac": float(np.mean(si_fe != si_64))}}
-        for r in refs4:
-            r.free()
+        # Burning Ship: 64 tiles of 256..2048 squared at max_iter 5e4 -- FE32
+        # over all of them in one launch; FP64 (and FE32 again) on a subset of
+        # ~2.5 % of the pixels, labelled (FP64 over all 64 tiles takes ~14 min
+        # on GB300's FP64 pipe)
+        out["burning_ship_64_tiles"] = bs_leg(
+            ctx, nat, torch, dev, timed, syn.config4_workload(max_iter=bs_max_iter)[:bs_tiles],
+            bs_max_iter, 0.025,
+            f"Burning Ship, {{n}} tiles of side 256..2048 (log-uniform), widths 1e-200..1e-30, "
+            f"centres from the BS ball method + Newton at 250 digits, max_iter {bs_max_iter}, "
+            "M 1e3, Hessian, one launch")
+    if "bs_edge" in legs:
+        # the same centres, each tile four times its nucleus' size estimate
+        # wide (boundary-straddling: pixels escape), first 16 tiles, all forms
+        out["burning_ship_edge_16_tiles"] = bs_leg(
+            ctx, nat, torch, dev, timed,
+            syn.config4_workload(max_iter=bs_max_iter, n_tiles=16, edge=True),
+            bs_max_iter, 1.0,
+            f"Burning Ship, {{n}} tiles of the 64-tile workload's first centres, each 4 x its "
+            f"nucleus size estimate wide, max_iter {bs_max_iter}, M 1e3, Hessian, one launch")
+    if "model_api" in legs:
+        out["model_api_e2e"] = model_api_leg(syn)
     if "host" in legs:
         out["host_1100_digits"] = host_leg(syn)
     return out
+
+
+def bs_leg(ctx, nat, torch, dev, timed, tiles4, max_iter, fp64_frac, workload):
+    """Burning Ship tiles in one launch: FE32 over all of them, then FP64 and
+    FE32 over the first tiles holding ``fp64_frac`` of the pixels (the
+    like-for-like ratio and the iteration-count agreement are taken there)."""
+    f64 = dict(dtype=torch.float64, device=dev)
+    refs4, keep, ts = [], [], []
+    for t in tiles4:
+        r = nat.Reference(ctx, t.Zn, div_iter=t.div_iter, order=t.ref_order, flavor=1,
+                          calc_dzndc=True, scale_m=t.dx_m, scale_e=t.dx_e, bla=True, kc=t.kc,
+                          bla_eps=1e-6)
+        m = t.side * t.side
+        xs = torch.from_numpy(t.xs).to(dev)
+        ys = torch.from_numpy(t.ys).to(dev)
+        Z = torch.zeros((6, m), **f64)
+        sr = torch.zeros(m, dtype=torch.int8, device=dev)
+        si = torch.zeros(m, dtype=torch.int32, device=dev)
+        U = torch.zeros(m, dtype=torch.int32, device=dev)
+        keep.append((xs, ys, Z, sr, si, U))
+        refs4.append(r)
+        ts.append(nat.make_tile_ptrs(nx=t.side, ny=t.side, xs_ptr=xs.data_ptr(),
+                                     ys_ptr=ys.data_ptr(), lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=6,
+                                     stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
+                                     U_ptr=U.data_ptr(), ref=r, dx_m=t.dx_m, dx_e=t.dx_e,
+                                     drift_m=t.driftx_m, drift_e=t.driftx_e,
+                                     drifty_m=t.drifty_m, drifty_e=t.drifty_e))
+
+    def c4(mode):
+        return nat.make_calc(max_iter=max_iter, M_divergence=1000., flavor=1,
+                             calc_dzndc=True, bla=True, mode=mode)
+    npx = np.array([t.side ** 2 for t in tiles4])
+    k_sub = int(np.searchsorted(np.cumsum(npx), fp64_frac * npx.sum(), side="right"))
+    k_sub = max(1, min(len(tiles4), k_sub))
+    sub = ts[:k_sub]
+
+    def counts(k):
+        return np.concatenate([keep[i][4].cpu().numpy() for i in range(k)])
+    k_all, st_all = timed(lambda: ctx.perturb_tiles(c4("fe32"), ts, nat.DEVICE), 1, 0)
+    esc = float(np.mean(np.concatenate([keep[i][3].cpu().numpy() for i in range(len(ts))]) == 1))
+    kf, stf = timed(lambda: ctx.perturb_tiles(c4("fe32"), sub, nat.DEVICE), 1, 0)
+    si_fe = counts(k_sub)
+    k64, st64 = timed(lambda: ctx.perturb_tiles(c4("fp64"), sub, nat.DEVICE), 1, 0)
+    si_64 = counts(k_sub)
+    for r in refs4:
+        r.free()
+    v_fe, v_64 = stf["pixel_iters"] / (kf * 1e-3), st64["pixel_iters"] / (k64 * 1e-3)
+    return {
+        "workload": workload.format(n=len(tiles4)),
+        "pixels": int(npx.sum()), "escaped_frac": esc,
+        "periods": sorted({t.order for t in tiles4 if t.order}),
+        "fe32": {"tiles": len(tiles4), "kernel_ms": k_all, "pixel_iters": int(st_all["pixel_iters"]),
+                 "value": st_all["pixel_iters"] / (k_all * 1e-3), "full_steps": int(st_all["full_steps"]),
+                 "bla_steps": int(st_all["bla_steps"])},
+        "subset": {"tiles": k_sub, "pixels": int(npx[:k_sub].sum()),
+                   "pixel_frac": float(npx[:k_sub].sum() / npx.sum()),
+                   "fe32": {"kernel_ms": kf, "value": v_fe},
+                   "fp64": {"kernel_ms": k64, "value": v_64, "pixel_iters": int(st64["pixel_iters"])},
+                   "speedup_fe32_vs_fp64": v_fe / v_64,
+                   "iter_count_differs_frac": float(np.mean(si_fe != si_64)),
+                   "fp64_all_tiles_extrapolated_s": (k64 * 1e-3) * st_all["pixel_iters"]
+                                                    / max(st64["pixel_iters"], 1)},
+        "unit": "pixel-iter/s"}
 
 
 def view_leg(ctx, nat, torch, dev, timed, we, wx, parity_pixels, seed, workload):
@@ -353,6 +413,44 @@ def view_leg(ctx, nat, torch, dev, timed, we, wx, parity_pixels, seed, workload)
         rows["oracle_s"] = time.perf_counter() - t0
         out["vs_oracle"] = rows
     return out
+
+
+def model_api_leg(syn, nx=2048):
+    """The headline view through the reference's model API, as a
+    Fractalshades script runs it: Perturbation_mandelbrot.zoom ->
+    calc_std_div -> calc_raw (precision_mode "fe32"), which computes the
+    reference orbit on the host, renders the image on the GPU from pageable
+    numpy arrays and writes the raw arrays to the memory maps on disk.  The
+    first call includes the orbit (its Newton refinement and ball method at
+    400 digits); the repeat, under a new calc name, reuses the stored orbit."""
+    import tempfile
+    import mpmath
+    import fractalshades_gb300.models as fsm
+    from fractalshades_gb300 import settings
+    w = syn.config2_workload(nx=8)
+    with mpmath.workdps(400):
+        x, y = str(w.center.real), str(w.center.imag)
+    old = settings.precision_mode
+    settings.precision_mode = "fe32"
+    res = {}
+    try:
+        with tempfile.TemporaryDirectory() as d:
+            f = fsm.Perturbation_mandelbrot(d)
+            f.zoom(precision=400, x=x, y=y, dx="1e-300", nx=nx, xy_ratio=1., theta_deg=0.)
+            for key in ("first", "repeat"):
+                f.calc_std_div(calc_name=key, subset=None, max_iter=200000, M_divergence=1000.,
+                               epsilon_stationnary=1e-3, BLA_eps=1e-6, interior_detect=False,
+                               calc_dzndc=True)
+                t0 = time.perf_counter()
+                f.calc_raw(key)
+                dt = time.perf_counter() - t0
+                it = float(f.get_raw(key, "stop_iter").astype(np.int64).sum())
+                res[key] = {"s": dt, "pixel_iters": it, "value": it / dt}
+    finally:
+        settings.precision_mode = old
+    return {"workload": f"the {nx}x{nx} 1e-300 view on the period-{w.p} nucleus through "
+                        "Perturbation_mandelbrot.calc_raw (fe32), raw arrays written to the "
+                        "memory maps", **res, "unit": "pixel-iter/s"}
 
 
 def host_leg(syn):

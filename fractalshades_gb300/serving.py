@@ -95,9 +95,14 @@ class TileServer:
     """Continuous-batching server of perturbation tiles (FP32+exponent kernel
     by default)."""
 
-    def __init__(self, centers, *, hbm_budget=120 * 2 ** 30, n_slots=3,
+    def __init__(self, centers, *, hbm_budget=120 * 2 ** 30, n_slots=None, max_slots=4,
                  max_batch_pixels=8 * 2 ** 20, mode="fe32", M=1000., bla_eps=1e-6,
-                 device=0, keep_results=True):
+                 device=0, keep_results=True, order="fifo"):
+        """n_slots None: as many slots as the HBM budget holds batches of
+        max_batch_pixels, at most max_slots (one persistent launch already
+        fills the GPU; more concurrent launches only fill the tails).
+        order "fifo" admits by arrival, "shortest" the smallest expected work
+        first (``expected_work``)."""
         import torch
         self.torch = torch
         self.device = torch.device("cuda", device)
@@ -108,6 +113,12 @@ class TileServer:
         self.M = M
         self.bla_eps = bla_eps
         self.max_batch_pixels = int(max_batch_pixels)
+        if n_slots is None:
+            n_slots = max(1, min(int(max_slots),
+                                 self.hbm_budget // (self.max_batch_pixels * BYTES_PER_PIXEL)))
+        if order not in ("fifo", "shortest"):
+            raise ValueError("order: 'fifo' or 'shortest'")
+        self.order = order
         self.slots = [_Slot(torch, self.device, i) for i in range(n_slots)]
         # reference builds on a high-priority stream of their own: their
         # kernels are scheduled first as SMs free up, and launches wait for
@@ -261,7 +272,16 @@ class TileServer:
         slot.busy = False
         slot.batch = None
 
+    def expected_work(self, req):
+        """Expected executed steps of a request: its pixels times the orbit
+        periods up to max_iter times the steps of a period (about log2 p BLA
+        steps and ten full steps; interior pixels run to max_iter)."""
+        p = max(self.centers[req.center].p, 2)
+        return req.side * req.side * (req.max_iter / p) * (math.log2(p) + 10.)
+
     def _admit(self, slot):
+        if self.order == "shortest" and len(self.pending) > 1:
+            self.pending = collections.deque(sorted(self.pending, key=self.expected_work))
         batch = []
         pixels = 0
         while self.pending:

@@ -267,19 +267,38 @@ def bs_center(rng, dps, kind=1, radius="1e-3", tries=64, max_iter=50000):
         return (x0, y0), mpmath.mpc(x0, y0), None
 
 
-def config4_workload(seed=4, n_tiles=64, max_iter=50000, M=1000., kind=1, dps=250):
+def config4_workload(seed=4, n_tiles=64, max_iter=50000, M=1000., kind=1, dps=250,
+                     newton=True, edge=False):
     """64 Burning Ship tiles, side round(exp(U[ln 256, ln 2048])), width
     10^U[-200, -30], each on its own centre (``bs_center``) with its own
-    250-digit reference orbit; max_iter 5e4, escape radius 1e3."""
+    250-digit reference orbit; max_iter 5e4, escape radius 1e3.
+    newton=False: the raw seeded points are the centres (the reference's
+    fallback when no nucleus is found, perturbation.py:747-757) -- points off
+    the real axis; the widths are drawn the same way.
+    edge=True: each tile whose centre is a nucleus takes as width four times
+    that nucleus' size estimate (FP_loop.pyx:2100-2356), so that it straddles
+    the minibrot's boundary and pixels escape (the seeded width where there is
+    no nucleus or the estimate is not a finite size below 1)."""
     rng = np.random.default_rng(seed)
     tiles = []
     for _ in range(n_tiles):
         side = int(round(np.exp(rng.uniform(np.log(256), np.log(2048)))))
         width_exp = rng.uniform(-200, -30)
-        seed_pt, c, order = bs_center(rng, dps, kind)
+        if newton:
+            seed_pt, c, order = bs_center(rng, dps, kind)
+        else:
+            x0, y0 = -1.8 + 0.1 * rng.random(), -0.1 * rng.random()
+            with mpmath.workdps(dps):
+                seed_pt, c, order = (x0, y0), mpmath.mpc(x0, y0), None
         with mpmath.workdps(dps):
             dxm = mpmath.mpf(10) ** mpmath.mpf(width_exp)
             prec = mpmath.mp.prec
+            if edge and order:
+                size, _ = fsFP.perturbation_nonholomorphic_nucleus_size_estimate(
+                    str(c.real), str(c.imag), prec, order, kind)
+                size = abs(mpmath.mpf(size))
+                if mpmath.isfinite(size) and 0 < size < 1:
+                    dxm = 4 * size
             ref_len = min(order, max_iter + 1) if order else max_iter + 1
             orb = np.empty(max_iter + 1 if not order else ref_len, dtype=np.complex128)
             i, _, _ = fsFP.perturbation_nonholomorphic_FP_loop(

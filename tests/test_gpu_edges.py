@@ -204,7 +204,10 @@ def test_iteration_budget_and_resubmission(ctx, kind):
 
     rc, Zf, srf, sif = launch(pix, 0)
     assert rc == nat.FSG_OK
-    budget = int(sif.astype(np.int64).sum() // 5)
+    # a fifth of the image's iterations; 1 % on the standard view, where
+    # pixels escaping in a few iterations claim the rest of the image before
+    # the interior ones, which carry most of the iterations, finish
+    budget = int(sif.astype(np.int64).sum() // (100 if kind == "std" else 5))
     rc, Z1, sr1, si1 = launch(pix, budget)
     assert rc == nat.FSG_BUDGET
     left = np.flatnonzero(sr1 == -1)
