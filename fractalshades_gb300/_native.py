@@ -377,7 +377,8 @@ class Reference:
             pass
 
     def download(self, which):
-        """Tables built on the device: 'dzndc', 'dzndz', 'bla', 'bs_paths'."""
+        """Tables built on the device: 'dzndc', 'dzndz', 'bla', 'bs_paths',
+        'bs_xpaths' (Xrange branch: mantissas and exponents)."""
         n = self.len
         L, c = self.ctx.L, self.ctx
         if which in ("dzndc", "dzndz"):
@@ -398,6 +399,11 @@ class Reference:
             out = np.zeros(4 * n)
             c.check(L.fsg_ref_download(c.h, self.h, 3, _p(out), None), "fsg_ref_download")
             return out.reshape(4, n)
+        if which == "bs_xpaths":
+            m = np.zeros(4 * n)
+            e = np.zeros(4 * n, dtype=np.int32)
+            c.check(L.fsg_ref_download(c.h, self.h, 4, _p(m), _p(e)), "fsg_ref_download")
+            return m.reshape(4, n), e.reshape(4, n)
         raise ValueError(which)
 
 

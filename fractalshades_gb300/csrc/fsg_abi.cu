@@ -25,6 +25,8 @@ void fsg_build_paths_m2(const RefDev *Rd, int len, double2 *dzndc, double2 *dznd
                         cudaStream_t s);
 void fsg_build_paths_bs(const RefDev *Rd, int len, double *dXa, double *dXb, double *dYa, double *dYb,
                         double scale, cudaStream_t s);
+void fsg_build_paths_bs_xr(const RefDev *Rd, int len, double *pm, int *pe, double scale_m,
+                           int scale_e, cudaStream_t s);
 void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *Mbs, double *r,
                    int stages, double kc, double eps, cudaStream_t s);
 void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, cudaStream_t s);
@@ -173,8 +175,8 @@ int check_tile(fsg_ctx *ctx, const fsg_tile &t, bool perturb, const fsg_calc *ca
         return set_err(ctx, FSG_ERR_ARG, "dzndc_scale_e out of range");
     if (t.proj < 0 || t.proj > 1) return set_err(ctx, FSG_ERR_ARG, "bad projection kind");
     if (perturb && calc->flavor != 0) {
-        if (calc->mode == FSG_MODE_XR64)
-            return set_err(ctx, FSG_ERR_ARG, "Burning Ship perturbation supports FSG_MODE_FP64 and FSG_MODE_FE32");
+        if (calc->mode == FSG_MODE_XR64 && calc->calc_dzndc && !t.ref->xr_paths)
+            return set_err(ctx, FSG_ERR_ARG, "Xrange mode needs Xrange Jacobian paths (fsg_ref_desc.xr_paths)");
         if (calc->calc_dzndc && !t.ref->has_dzndc)
             return set_err(ctx, FSG_ERR_ARG, "calc_hessian requested but the reference has no Jacobian paths");
         if (calc->bla && !t.ref->bla_req)
@@ -654,6 +656,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     double2 *dzndc = nullptr, *dzndc_xm = nullptr, *dzndz = nullptr, *dzndz_xm = nullptr;
     int *dzndc_xe = nullptr, *dzndz_xe = nullptr;
     double *dXa = nullptr, *dXb = nullptr, *dYa = nullptr, *dYb = nullptr;
+    double *bs_xpm = nullptr; int *bs_xpe = nullptr;
     if (d->flavor == 0) {
         if (d->calc_dzndc) {
             if (d->xr_paths) { RA(dzndc_xm, len + 1); RA(dzndc_xe, len + 1); }
@@ -665,10 +668,12 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
         }
     } else if (d->calc_dzndc) {
         RA(dXa, len + 1); RA(dXb, len + 1); RA(dYa, len + 1); RA(dYb, len + 1);
+        if (d->xr_paths) { RA(bs_xpm, 4 * (size_t)(len + 1)); RA(bs_xpe, 4 * (size_t)(len + 1)); }
     }
     R.dZndc = dzndc; R.dZndc_xm = dzndc_xm; R.dZndc_xe = dzndc_xe;
     R.dZndz = dzndz; R.dZndz_xm = dzndz_xm; R.dZndz_xe = dzndz_xe;
     R.dXa = dXa; R.dXb = dXb; R.dYa = dYa; R.dYb = dYb;
+    R.bs_xpm = bs_xpm; R.bs_xpe = bs_xpe;
     // BLA
     int L = len / 8;
     double2 *Mbla = nullptr; double *Mbs = nullptr, *rbla = nullptr;
@@ -734,6 +739,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
                            d->scale_e, s);
     } else if (d->calc_dzndc) {
         fsg_build_paths_bs(r->dev, len, dXa, dXb, dYa, dYb, ldexp(d->scale_m, d->scale_e), s);
+        if (bs_xpm) fsg_build_paths_bs_xr(r->dev, len, bs_xpm, bs_xpe, d->scale_m, d->scale_e, s);
     }
     if (R.bla_len > 0) fsg_build_bla(r->dev, d->flavor, len, Mbla, Mbs, rbla, stages, d->kc, d->bla_eps, s);
     if (d->flavor != 0) {
@@ -882,6 +888,16 @@ int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0, vo
         CK(cudaMemcpy(o + len, R.dXb, 8 * len, cudaMemcpyDeviceToHost), "download");
         CK(cudaMemcpy(o + 2 * len, R.dYa, 8 * len, cudaMemcpyDeviceToHost), "download");
         CK(cudaMemcpy(o + 3 * len, R.dYb, 8 * len, cudaMemcpyDeviceToHost), "download");
+        return FSG_OK;
+    }
+    if (which == 4) {
+        if (!R.bs_xpm || !out1) return set_err(ctx, FSG_ERR_ARG, "no Xrange Jacobian paths");
+        double *o = (double *)out0;
+        int *oe = (int *)out1;
+        for (int k = 0; k < 4; k++) {
+            CK(cudaMemcpy(o + k * len, R.bs_xpm + k * (len + 1), 8 * len, cudaMemcpyDeviceToHost), "download");
+            CK(cudaMemcpy(oe + k * len, R.bs_xpe + k * (len + 1), 4 * len, cudaMemcpyDeviceToHost), "download");
+        }
         return FSG_OK;
     }
     return set_err(ctx, FSG_ERR_ARG, "bad table selector");

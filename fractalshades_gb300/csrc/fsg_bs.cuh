@@ -98,16 +98,29 @@ FSG_DEV fr operator*(double s, fr b) {
 }
 FSG_DEV fr &operator+=(fr &a, fr b) { a = a + b; return a; }
 
-// the operations the loop needs, for both real types
+// xf: the reference's float64 Xrange record (numba_xr.py), the real type of
+// the Xrange branch.  Constants are the unnormalised records {x, 0}, so that a
+// constant times a record rounds as the reference's float * Xrange.
+FSG_DEV xf operator+(xf a, xf b) { return xf_add(a, b); }
+FSG_DEV xf operator-(xf a) { a.m = -a.m; return a; }
+FSG_DEV xf operator-(xf a, xf b) { return xf_sub(a, b); }
+FSG_DEV xf operator*(xf a, xf b) { return xf_mul(a, b); }
+FSG_DEV xf operator*(double s, xf b) { return xf_mul_s(s, b); }
+FSG_DEV xf &operator+=(xf &a, xf b) { a = a + b; return a; }
+
+// the operations the loop needs, for every real type
 FSG_DEV double to_d(double x) { return x; }
 FSG_DEV double to_d(fr x) { return fr_to_d(x); }
+FSG_DEV double to_d(xf x) { return xf_to_std(x); }
 template <class T> FSG_DEV T from_d(double x);
 template <> FSG_DEV double from_d<double>(double x) { return x; }
 template <> FSG_DEV fr from_d<fr>(double x) { return fr_from_d(x); }
+template <> FSG_DEV xf from_d<xf>(double x) { return xr_from_r(x); }      // to_Xrange_scalar
 // a literal constant (0, +-1, +-2) of the loop's real type, without FP64
 template <class T> FSG_DEV T cst(float x);
 template <> FSG_DEV double cst<double>(float x) { return (double)x; }
 template <> FSG_DEV fr cst<fr>(float x) { return fr_norm(x, 0); }
+template <> FSG_DEV xf cst<xf>(float x) { return xf_make((double)x, 0); }
 // m * 2^e from a mantissa and an exponent (the Xrange form of c)
 template <class T> FSG_DEV T from_me(double m, int e);
 template <> FSG_DEV double from_me<double>(double m, int e) { return ldexp_d(m, e); }
@@ -116,17 +129,23 @@ template <> FSG_DEV fr from_me<fr>(double m, int e) {
     if (r.m != 0.f) r.e += e;
     return r;
 }
+template <> FSG_DEV xf from_me<xf>(double m, int e) { return xf_make(m, e); }
 FSG_DEV bool ge0(double x) { return x >= 0.; }
 FSG_DEV bool ge0(fr x) { return x.m >= 0.f; }
+FSG_DEV bool ge0(xf x) { return xf_ge_s(x, 0.); }
 FSG_DEV bool le0(double x) { return x <= 0.; }
 FSG_DEV bool le0(fr x) { return x.m <= 0.f; }
+FSG_DEV bool le0(xf x) { return xf_le_s(x, 0.); }
 FSG_DEV double absT(double x) { return fabs(x); }
 FSG_DEV fr absT(fr x) { x.m = fabsf(x.m); return x; }
+FSG_DEV xf absT(xf x) { x.m = fabs(x.m); return x; }
 // sgn with 0 mapped to +1 (burning_ship.py:12-17)
 FSG_DEV double sgnT(double x) { return x < 0. ? -1. : 1.; }
 FSG_DEV fr sgnT(fr x) { fr r; r.m = x.m < 0.f ? -1.f : 1.f; r.e = 0; return r; }
+FSG_DEV xf sgnT(xf x) { return xf_make(xf_lt_s(x, 0.) ? -1. : 1., 0); }
 // |a| <= |b|
 FSG_DEV bool abs_le(double a, double b) { return fabs(a) <= fabs(b); }
+FSG_DEV bool abs_le(xf a, xf b) { a.m = fabs(a.m); b.m = fabs(b.m); return xf_le(a, b); }
 FSG_DEV bool abs_le(fr a, fr b) {
     if (a.m == 0.f) return true;
     if (b.m == 0.f) return false;
@@ -222,6 +241,15 @@ template <> struct BLAGet<fr> {
 // v * 2^k (k = 0: v)
 FSG_DEV double scale2(double v, int k) { return k == 0 ? v : ldexp_d(v, k); }
 FSG_DEV fr scale2(fr v, int k) { if (v.m != 0.f) v.e += k; return v; }
+FSG_DEV xf scale2(xf v, int k) { v.e += k; return v; }
+
+// ref_BLA_get on the Xrange branch: the standard values of the deltas (0
+// below the double range, perturbation.py:1520-1527)
+template <> struct BLAGet<xf> {
+    static FSG_DEV int get(const RefDev &R, xf xn, xf yn, int w, int &ib) {
+        return bla_lookup(R, hypot(xf_to_std(xn), xf_to_std(yn)), w, ib);
+    }
+};
 
 // Reads of the reference's tables in the loop's real type: the double
 // tables themselves, or their fr copies (orbit values from the Xrange side
@@ -254,6 +282,38 @@ template <> struct BSRef<fr> {
             int4 v = __ldg(&R.bs_blaf[4 * ib + k]);
             M[2 * k] = lo(v); M[2 * k + 1] = hi(v);
         }
+    }
+};
+
+// The Xrange branch: ensure_xr_BS (perturbation.py:2182-2193) -- the side
+// table's value where the orbit holds one, else the standard value as a
+// record; the Xrange Jacobian paths; the BLA coefficients as float64 (the
+// reference multiplies them float * Xrange: unnormalised records {M, 0})
+template <> struct BSRef<xf> {
+    static FSG_DEV bool table(const RefDev &R, int w, xf &X, xf &Y) {
+        const int s = (R.n_xr > 0 && w < R.len) ? __ldg(&R.xr_slot[w]) : -1;
+        if (s < 0) return false;
+        const double *m = (const double *)R.xr_m;
+        X = xf_make(__ldg(&m[s]), __ldg(&R.xr_e[s]));
+        Y = xf_make(__ldg(&m[R.n_xr + s]), __ldg(&R.xr_e[R.n_xr + s]));
+        return true;
+    }
+    static FSG_DEV void orbit(const RefDev &R, int w, xf &X, xf &Y) {
+        if (!table(R, w, X, Y)) {
+            const double2 z = __ldg(&R.Zn[w]);
+            X = xr_from_r(z.x); Y = xr_from_r(z.y);
+        }
+    }
+    static FSG_DEV void hess(const RefDev &R, int w, xf &a, xf &b, xf &c, xf &d) {
+        const int L = R.len + 1;
+        a = xf_make(__ldg(&R.bs_xpm[w]), __ldg(&R.bs_xpe[w]));
+        b = xf_make(__ldg(&R.bs_xpm[L + w]), __ldg(&R.bs_xpe[L + w]));
+        c = xf_make(__ldg(&R.bs_xpm[2 * L + w]), __ldg(&R.bs_xpe[2 * L + w]));
+        d = xf_make(__ldg(&R.bs_xpm[3 * L + w]), __ldg(&R.bs_xpe[3 * L + w]));
+    }
+    static FSG_DEV void bla(const RefDev &R, int ib, xf M[8]) {
+        const double *p = R.Mbla_bs + 8 * ib;
+        for (int k = 0; k < 8; k++) M[k] = xf_make(__ldg(p + k), 0);
     }
 };
 
@@ -672,6 +732,10 @@ FSG_DEV int bs_frame_tests(const BSFrame &S, float X, float Y, int eX, int eY, f
 
 template <class T> struct IsDouble { static constexpr bool value = false; };
 template <> struct IsDouble<double> { static constexpr bool value = true; };
+template <class T> struct IsFr { static constexpr bool value = false; };
+template <> struct IsFr<fr> { static constexpr bool value = true; };
+template <class T> struct IsXr { static constexpr bool value = false; };
+template <> struct IsXr<xf> { static constexpr bool value = true; };
 
 // FL: the flavor as a compile-time constant (1..5), or 0 to read C.flavor
 template <class T, int FL>
@@ -701,9 +765,11 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     T h[4] = {cst<T>(0.f), cst<T>(0.f), cst<T>(0.f), cst<T>(0.f)};
     const fr M2f = fr_from_d(C.M2);
     int w = 0, n = 0; signed char stop = -1; bool dyn = true;
-    // calc_orbit snapshots (perturbation.py:1501-1508), FP64 form only: the
-    // FP32 + exponent instantiation compiles without them
-    constexpr bool ORB_FORM = IsDouble<T>::value;
+    // calc_orbit snapshots (perturbation.py:1501-1508), the reference's two
+    // forms only: the FP32 + exponent instantiation compiles without them
+    constexpr bool FR_FORM = IsFr<T>::value;
+    constexpr bool XR_FORM = IsXr<T>::value;
+    constexpr bool ORB_FORM = !FR_FORM;
     const int bs = ORB_FORM ? C.backshift : 0;
     OrbitSnap<double2> S;
     S.init(bs, cx(0., 0.));
@@ -729,13 +795,13 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
     float M2s = 0.f;
     // with |X|, |Y| and the deltas below 2^(eMlim + 1), |Z + dz|^2 < M2 / 8
     const int eMlim = min((M2f.e >> 1) - 4, 40);
-    if constexpr (!ORB_FORM) {
+    if constexpr (FR_FORM) {
         Fm.am = a.m; Fm.ae = a.e; Fm.bm = b.m; Fm.be = b.e;
         M2s = (float)C.M2;
     }
     for (;;) {
         bool bla_done = false, stepped = false;
-        if constexpr (!ORB_FORM) {
+        if constexpr (FR_FORM) {
             if (frm) {
             // Steps in the frame form from orbit point w on, until the loop ends
             // (0), a BLA step was taken (1), the step at w has to run in fr (2) or
@@ -833,6 +899,45 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             w += 1;
             if (w >= order) w = w % order;
         }
+        if constexpr (XR_FORM) {
+            // the Xrange branch's tests (perturbation.py:1627-1731): escape on
+            // the standard values; rebase when the reference diverges from
+            // the standard sum; the dynamic rebase tested componentwise on the
+            // standard values, then confirmed with |Z + z|^2 <= |z|^2 in
+            // Xrange (with the side table's value of the orbit where it holds
+            // one) -- a refused confirmation leaves bool_dyn_rebase set
+            const double2 Zs = __ldg(&R.Zn[w]);
+            const double xs = to_d(xn), ys = to_d(yn);
+            const double XXd = xs + Zs.x, YYd = ys + Zs.y;
+            if (bs > 0) S.take(n, bs, cx(XXd, YYd));
+            if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
+            if (w >= div_iter - 1) {
+                xn = from_d<T>(XXd); yn = from_d<T>(YYd);
+                if (hess) {
+                    T Ha, Hb, Hc, Hd;
+                    BSRef<T>::hess(R, w, Ha, Hb, Hc, Hd);
+                    h[0] += Ha; h[1] += Hb; h[2] += Hc; h[3] += Hd;
+                }
+                w = 0; nreb++; continue;
+            }
+            dyn = (fabs(XXd) <= fabs(xs)) && (fabs(YYd) <= fabs(ys));
+            if (dyn) {
+                T Xt, Yt;
+                const bool tab = BSRef<T>::table(R, w, Xt, Yt);
+                const T XXx = tab ? xn + Xt : xf_add_s(xn, Zs.x);
+                const T YYx = tab ? yn + Yt : xf_add_s(yn, Zs.y);
+                if (xf_le(XXx * XXx + YYx * YYx, xn * xn + yn * yn)) {
+                    xn = XXx; yn = YYx;
+                    if (hess) {
+                        T Ha, Hb, Hc, Hd;
+                        BSRef<T>::hess(R, w, Ha, Hb, Hc, Hd);
+                        h[0] += Ha; h[1] += Hb; h[2] += Hc; h[3] += Hd;
+                    }
+                    w = 0; nreb++; continue;
+                }
+            }
+            continue;
+        }
         T Xs, Ys;
         BSRef<T>::orbit(R, w, Xs, Ys);
         T XX = xn + Xs, YY = yn + Ys;
@@ -862,7 +967,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             }
             w = 0; nreb++; continue;
         }
-        if constexpr (!ORB_FORM) {
+        if constexpr (FR_FORM) {
             // the frame form takes over while the deltas stay below 2^11 and
             // the next step can run there
             if (max(xn.e, yn.e) <= 10 && (__ldg(&R.bs_fz[w]).x & 5)) {
@@ -871,9 +976,17 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             }
         }
     }
-    T Xe, Ye;
-    BSRef<T>::orbit(R, w, Xe, Ye);
-    const double xo = to_d(xn + Xe), yo = to_d(yn + Ye);
+    // end of iterations (:1745-1757): the Xrange branch adds the standard
+    // orbit value to the Xrange delta
+    double xo, yo;
+    if constexpr (XR_FORM) {
+        const double2 Zs = __ldg(&R.Zn[w]);
+        xo = to_d(xf_add_s(xn, Zs.x)); yo = to_d(xf_add_s(yn, Zs.y));
+    } else {
+        T Xe, Ye;
+        BSRef<T>::orbit(R, w, Xe, Ye);
+        xo = to_d(xn + Xe); yo = to_d(yn + Ye);
+    }
     double hd[4] = {0., 0., 0., 0.};
     if (hess) {
         // the Hessian in the tile's unit: the reference's scale times 2^dzs
@@ -914,7 +1027,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
 // the FP32 + exponent kernels hold three 256-thread blocks per SM (at most 85
 // registers a thread)
 template <class T, int FL>
-__global__ void __launch_bounds__(256, IsDouble<T>::value ? 1 : 3)
+__global__ void __launch_bounds__(256, IsFr<T>::value ? 3 : 1)
 k_perturb_bs(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);

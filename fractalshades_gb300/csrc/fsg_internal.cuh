@@ -30,6 +30,8 @@ struct RefDev {
     const double2 *dZndz_xm; const int *dZndz_xe;
     // BS Jacobian paths
     const double *dXa, *dXb, *dYa, *dYb;        // [len + 1]
+    const double *bs_xpm; const int *bs_xpe;    // Xrange branch: [4][len + 1] dXa, dXb, dYa,
+                                                // dYb as float64 Xrange records
     // BLA tree (compressed, perturbation.py:1819-1881)
     const double2 *Mbla;        // M2: [bla_len][2] (A, B)
     const double *Mbla_bs;      // BS: [bla_len][8]

@@ -133,6 +133,39 @@ FSG_DEV bool xf_lt_s(xf a, double x) {
 FSG_DEV bool xf_le(xf a, xf b) {
     double o0, o1; int e; xr_coexp_r(a.m, a.e, b.m, b.e, o0, o1, e); return o0 <= o1;
 }
+// real Xrange records (numba_xr.py on float64 Xrange): add / sub through the
+// co-exponent, lazy renormalisation of products, float * Xrange
+FSG_DEV xf xf_make(double m, int e) { xf r; r.m = m; r.e = e; return r; }
+FSG_DEV xf xr_from_r(double x) { int e; double m = xr_norm_real(x, 0, e); return xf_make(m, e); }
+FSG_DEV xf xf_add(xf a, xf b) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, b.m, b.e, o0, o1, e); return xf_make(o0 + o1, e);
+}
+FSG_DEV xf xf_sub(xf a, xf b) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, b.m, b.e, o0, o1, e); return xf_make(o0 - o1, e);
+}
+// Xrange + float: the float as a record (normalised only out of +-2^100)
+FSG_DEV xf xf_add_s(xf a, double x) {
+    xf b = xr_need_renorm_r(x) ? xr_from_r(x) : xf_make(x, 0);
+    return xf_add(a, b);
+}
+FSG_DEV xf xf_mul(xf a, xf b) {
+    const double m = a.m * b.m;
+    const int e = (int)((unsigned)a.e + (unsigned)b.e);
+    if (xr_need_renorm_r(m)) { int eo; double nm = xr_norm_real(m, e, eo); return xf_make(nm, eo); }
+    return xf_make(m, e);
+}
+FSG_DEV xf xf_mul_s(double s, xf b) {
+    const double m = s * b.m;
+    if (xr_need_renorm_r(m)) { int eo; double nm = xr_norm_real(m, b.e, eo); return xf_make(nm, eo); }
+    return xf_make(m, b.e);
+}
+FSG_DEV bool xf_ge_s(xf a, double x) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, x, 0, o0, o1, e); return o0 >= o1;
+}
+FSG_DEV bool xf_le_s(xf a, double x) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, x, 0, o0, o1, e); return o0 <= o1;
+}
+
 // ldexp(1., e) for any int e (exact power of two, 0 below 2^-1074, inf above)
 FSG_DEV double pow2d(int e) {
     if (e > 1023) return __longlong_as_double(0x7ff0000000000000LL);
@@ -147,6 +180,10 @@ FSG_DEV double2 xr_to_std(xc a) {
     xr_coexp_r(nre, ere, nim, eim, cr, ci, ce);
     return rmul(pow2d(ce), cx(cr, ci));
 }
+// to_standard of a real Xrange record
+FSG_DEV double ldexp_d(double m, int e);
+FSG_DEV double xf_to_std(xf a) { return a.m == 0. ? 0. * a.m : ldexp_d(a.m, a.e); }
+
 // ldexp(m, e) with one rounding (m is in [1, 2) or a small normal number)
 FSG_DEV double ldexp_d(double m, int e) {
     if (e >= -1022 && e <= 1023) return m * pow2d(e);

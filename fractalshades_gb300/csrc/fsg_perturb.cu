@@ -248,6 +248,8 @@ __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
 // Burning Ship family, double deltas: fsg_bs.cuh instantiated on double
 // (compiled here, without FMA contraction)
 template __global__ void k_perturb_bs<double, 0>(WorkDev W, CalcDev C);
+// ... and on float64 Xrange records: the reference's Xrange branch
+template __global__ void k_perturb_bs<xf, 0>(WorkDev W, CalcDev C);
 
 template <bool XR, bool MN, bool ORB>
 static void launch_m2(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
@@ -265,7 +267,10 @@ static void launch_m2_orb(const WorkDev &W, const CalcDev &C, int grid, int bloc
 }
 
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    if (C.flavor != 0)
+    if (C.flavor != 0 && C.mode == 1)
+        k_perturb_bs<xf, 0><<<fsg_auto_grid(k_perturb_bs<xf, 0>, grid, block, W.total), block, 0,
+                           s>>>(W, C);
+    else if (C.flavor != 0)
         k_perturb_bs<double, 0><<<fsg_auto_grid(k_perturb_bs<double, 0>, grid, block, W.total), block, 0,
                                s>>>(W, C);
     else if (C.backshift > 0)

@@ -258,6 +258,61 @@ __global__ void k_dzndc_bs(const RefDev *Rp, double *__restrict__ dXa, double *_
     }
 }
 
+// numba_dZndc_path_BS, Xrange branch (perturbation.py:2339-2438): the
+// Jacobian path as float64 Xrange records from the orbit's Xrange values
+// (ensure_xr_BS: the side table's value where the orbit holds one), with the
+// derivatives of burning_ship.py:441-532 on records -- the float factors
+// (2., the signs) first, as the reference's 2. * sgn(x) * abs(y)
+__device__ __forceinline__ double sgn_x(xf x) { return xf_lt_s(x, 0.) ? -1. : 1.; }
+__device__ __forceinline__ xf abs_x(xf x) { x.m = fabs(x.m); return x; }
+__device__ __forceinline__ void bs_dfdxy_x(int flavor, xf x, xf y, xf &fxx, xf &fxy, xf &fyx,
+                                           xf &fyy) {
+    if (flavor == 1) {
+        fxx = xf_mul_s(2., x); fxy = xf_mul_s(-2., y);
+        fyx = xf_mul_s(2. * sgn_x(x), abs_x(y)); fyy = xf_mul_s(2. * sgn_x(y), abs_x(x));
+    } else if (flavor == 2) {
+        fxx = xf_mul_s(2., x); fxy = xf_mul_s(-2., y);
+        fyx = xf_mul_s(2., abs_x(y)); fyy = xf_mul_s(2. * sgn_x(y), x);
+    } else if (flavor == 3) {
+        fxx = xf_mul_s(2., x); fxy = xf_mul_s(-2., abs_x(y));
+        fyx = xf_mul_s(2., y); fyy = xf_mul_s(2., x);
+    } else {
+        const double sq = sgn_x(xf_sub(xf_mul(x, x), xf_mul(y, y)));
+        fxx = xf_mul_s(2. * sq, x); fxy = xf_mul_s(-2. * sq, y);
+        if (flavor == 4) { fyx = xf_mul_s(2., y); fyy = xf_mul_s(2., x); }
+        else { fyx = xf_mul_s(2. * sgn_x(x), abs_x(y)); fyy = xf_mul_s(2. * sgn_x(y), abs_x(x)); }
+    }
+}
+
+__global__ void k_dzndc_bs_xr(const RefDev *Rp, double *__restrict__ pm, int *__restrict__ pe,
+                              double scale_m, int scale_e) {
+    const RefDev &R = *Rp;
+    const int len = R.len, flavor = R.flavor, order = R.order, L = len + 1;
+    const int valid = len < R.div_iter ? len : R.div_iter;
+    const xf dx = xf_make(scale_m, scale_e);
+    const double *tm = (const double *)R.xr_m;
+    xf a = xf_make(0., 0), b = a, c = a, d = a;   // the Jacobian at index i - 1
+    for (int i = 1; i <= valid; i++) {
+        int from = i - 1, to = i;
+        if (i == valid) {
+            if (!(from == order - 1)) break;
+            to = 0;
+        }
+        const int s = (R.n_xr > 0 && from < len) ? R.xr_slot[from] : -1;
+        const xf X = s >= 0 ? xf_make(tm[s], R.xr_e[s]) : xr_from_r(R.Zn[from].x);
+        const xf Y = s >= 0 ? xf_make(tm[R.n_xr + s], R.xr_e[R.n_xr + s]) : xr_from_r(R.Zn[from].y);
+        xf fxx, fxy, fyx, fyy;
+        bs_dfdxy_x(flavor, X, Y, fxx, fxy, fyx, fyy);
+        const xf na = xf_add(xf_add(xf_mul(fxx, a), xf_mul(fxy, c)), dx);
+        const xf nb = xf_add(xf_mul(fxx, b), xf_mul(fxy, d));
+        const xf nc = xf_add(xf_mul(fyx, a), xf_mul(fyy, c));
+        const xf nd = xf_sub(xf_add(xf_mul(fyx, b), xf_mul(fyy, d)), dx);
+        pm[to] = na.m; pe[to] = na.e; pm[L + to] = nb.m; pe[L + to] = nb.e;
+        pm[2 * L + to] = nc.m; pe[2 * L + to] = nc.e; pm[3 * L + to] = nd.m; pe[3 * L + to] = nd.e;
+        a = na; b = nb; c = nc; d = nd;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // BLA tree
 // ---------------------------------------------------------------------------
@@ -705,6 +760,13 @@ void fsg_build_paths_m2(const RefDev *Rd, int len, double2 *dzndc, double2 *dznd
         }
     }
 }
+void fsg_build_paths_bs_xr(const RefDev *Rd, int len, double *pm, int *pe, double scale_m,
+                           int scale_e, cudaStream_t s) {
+    cudaMemsetAsync(pm, 0, 4 * 8 * (size_t)(len + 1), s);
+    cudaMemsetAsync(pe, 0, 4 * 4 * (size_t)(len + 1), s);
+    k_dzndc_bs_xr<<<1, 1, 0, s>>>(Rd, pm, pe, scale_m, scale_e);
+}
+
 void fsg_build_paths_bs(const RefDev *Rd, int len, double *dXa, double *dXb, double *dYa, double *dYb,
                         double scale, cudaStream_t s) {
     for (double *p : {dXa, dXb, dYa, dYb}) cudaMemsetAsync(p, 0, 8 * (size_t)(len + 1), s);

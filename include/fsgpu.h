@@ -271,7 +271,9 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps,
 /* Copy tables back to the host (tests).  which: 0 dZndc (complex128 [len]) or
  * its Xrange form (mantissa complex128 [len] + exp int32 [len]), 1 dZndz
  * ([len + 1]), 2 BLA (M complex128 [bla_len][2], r float64 [bla_len]),
- * 3 BS Jacobian paths (4 x float64 [len]).  Sizes via fsg_ref_info. */
+ * 3 BS Jacobian paths (4 x float64 [len]), 4 BS Jacobian paths as Xrange
+ * records (out0 4 x float64 [len] mantissas, out1 4 x int32 [len] exponents;
+ * references created with xr_paths).  Sizes via fsg_ref_info. */
 int fsg_ref_info(const fsg_ref *ref, int64_t *len, int64_t *bla_len, int32_t *stages);
 int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0,
                      void *out1);

@@ -1274,3 +1274,363 @@ EXPORT int orc_perturb_bs(const orc_pbs_args *P, int64_t npts, const double *pix
     }
     return 0;
 }
+
+/* ========================================================================= */
+/* Burning Ship perturbation, Xrange branch (xr_detect_activated):            */
+/* perturbation.py:1468-1791 with the deltas, c and the Jacobian as float64   */
+/* Xrange records; the closures of models/burning_ship.py:19-60, 535-859 are  */
+/* the double ones above, each operation on Xrange operands (numba_xr.py), in */
+/* the same order.  Derivative paths: numba_dZndc_path_BS's Xrange branch     */
+/* (perturbation.py:2339-2438) with incr_deriv_ref_BS (:2440-2463).           */
+/* ========================================================================= */
+#define XA(a, b) xf_add((a), (b))
+#define XS(a, b) xf_sub((a), (b))
+#define XM(a, b) xf_mul((a), (b))
+#define XK(s, b) xf_mul_s((s), (b))            /* float * Xrange */
+static inline xf xf_neg(xf a) { a.m = -a.m; return a; }
+static inline xf xf_abs(xf a) { a.m = fabs(a.m); return a; }
+static inline int xf_ge0(xf a) { return xf_ge_s(a, 0.); }
+static inline int xf_le0(xf a) { return xf_le_s(a, 0.); }
+static inline double xf_sgn(xf a) { return xf_lt_s(a, 0.) ? -1. : 1.; }
+static const xf XF0 = {0., 0};
+
+/* burning_ship.py:19-60 on Xrange operands */
+static inline xf diffabs_x(xf X, xf x) {
+    if (xf_ge0(X)) { if (xf_ge0(XA(X, x))) return XK(1., x); return xf_neg(XA(XK(2., X), x)); }
+    if (xf_le0(XA(X, x))) return xf_neg(x);
+    return XA(XK(2., X), x);
+}
+static inline double ddiffabsdX_x(xf X, xf x) {
+    if (xf_ge0(X)) return xf_ge0(XA(X, x)) ? 0. : -2.;
+    return xf_le0(XA(X, x)) ? 0. : 2.;
+}
+static inline double ddiffabsdx_x(xf X, xf x) {
+    if (xf_ge0(X)) return xf_ge0(XA(X, x)) ? 1. : -1.;
+    return xf_le0(XA(X, x)) ? -1. : 1.;
+}
+
+/* xn * (xn + 2 X) - yn * (yn + 2 Y) */
+static inline xf bsx_sq(xf xn, xf yn, xf X, xf Y) {
+    return XS(XM(xn, XA(xn, XK(2., X))), XM(yn, XA(yn, XK(2., Y))));
+}
+/* xn * yn + xn * Y + yn * X */
+static inline xf bsx_cross(xf xn, xf yn, xf X, xf Y) {
+    return XA(XA(XM(xn, yn), XM(xn, Y)), XM(yn, X));
+}
+/* X * yn + Y * xn + xn * yn */
+static inline xf bsx_cross2(xf xn, xf yn, xf X, xf Y) {
+    return XA(XA(XM(X, yn), XM(Y, xn)), XM(xn, yn));
+}
+
+static inline void bsx_p_iter_zn(int flavor, xf *x, xf *y, xf X, xf Y, xf a, xf b) {
+    xf nx, ny, xn = *x, yn = *y;
+    switch (flavor) {
+    case 1:
+        nx = XA(bsx_sq(xn, yn, X, Y), a);
+        ny = XS(XK(2., diffabs_x(XM(X, Y), bsx_cross(xn, yn, X, Y))), b);
+        break;
+    case 2:
+        nx = XA(bsx_sq(xn, yn, X, Y), a);
+        ny = XS(XK(2., XA(XM(X, diffabs_x(Y, yn)), XM(xn, xf_abs(XA(Y, yn))))), b);
+        break;
+    case 3:
+        nx = XA(XS(XS(XM(xn, XA(xn, XK(2., X))), XM(Y, diffabs_x(Y, yn))),
+                   XM(yn, xf_abs(XA(Y, yn)))), a);
+        ny = XS(XK(2., bsx_cross2(xn, yn, X, Y)), b);
+        break;
+    case 4:
+        nx = XA(diffabs_x(XS(XM(X, X), XM(Y, Y)), bsx_sq(xn, yn, X, Y)), a);
+        ny = XS(XK(2., bsx_cross2(xn, yn, X, Y)), b);
+        break;
+    default: {
+        xf ref_xyn = XM(X, Y), ref_x2my2 = XS(XM(X, X), XM(Y, Y));
+        nx = XA(diffabs_x(ref_x2my2, bsx_sq(xn, yn, X, Y)), a);
+        ny = XS(XK(2., diffabs_x(ref_xyn, bsx_cross(xn, yn, X, Y))), b);
+    } break;
+    }
+    *x = nx; *y = ny;
+}
+
+/* d/da of xn * yn + xn * Y + yn * X (flavors 1, 5): the six products in order */
+static inline xf bsx_dcross(xf xa, xf ya, xf xn, xf yn, xf X, xf Y, xf Xa, xf Ya) {
+    return XA(XA(XA(XA(XA(XM(xa, yn), XM(xn, ya)), XM(xa, Y)), XM(xn, Ya)), XM(ya, X)),
+              XM(yn, Xa));
+}
+/* d/da of xn (xn + 2 X) - yn (yn + 2 Y) (flavors 4, 5) */
+static inline xf bsx_dsq(xf xa, xf ya, xf xn, xf yn, xf X, xf Y, xf Xa, xf Ya) {
+    return XS(XS(XA(XM(xa, XA(xn, XK(2., X))), XM(xn, XA(xa, XK(2., Xa)))),
+                 XM(ya, XA(yn, XK(2., Y)))), XM(yn, XA(ya, XK(2., Ya))));
+}
+/* 2 (Xa yn + X ya + Ya xn + Y xa + xa yn + xn ya) (flavors 3, 4) */
+static inline xf bsx_dcross2(xf xa, xf ya, xf xn, xf yn, xf X, xf Y, xf Xa, xf Ya) {
+    return XK(2., XA(XA(XA(XA(XA(XM(Xa, yn), XM(X, ya)), XM(Ya, xn)), XM(Y, xa)), XM(xa, yn)),
+                     XM(xn, ya)));
+}
+/* 2 ((X + xn) xa + Xa xn) - 2 ((Y + yn) ya + Ya yn) (flavor 1) */
+static inline xf bsx_dsq1(xf xa, xf ya, xf xn, xf yn, xf X, xf Y, xf Xa, xf Ya) {
+    return XS(XK(2., XA(XM(XA(X, xn), xa), XM(Xa, xn))),
+              XK(2., XA(XM(XA(Y, yn), ya), XM(Ya, yn))));
+}
+
+/* burning_ship.py:622-859 on Xrange operands; h = (dxnda, dxndb, dynda, dyndb) */
+static inline void bsx_p_iter_hessian(int flavor, xf *h, xf xn, xf yn, xf X, xf Y,
+                                      xf Xa, xf Xb, xf Ya, xf Yb) {
+    xf xa = h[0], xb = h[1], ya = h[2], yb = h[3];
+    xf nxa, nxb, nya, nyb;
+    switch (flavor) {
+    case 1: {
+        xf opX = XM(X, Y);
+        xf dXa = XA(XM(Xa, Y), XM(X, Ya)), dXb = XA(XM(Xb, Y), XM(X, Yb));
+        xf opx = bsx_cross(xn, yn, X, Y);
+        xf dxa = bsx_dcross(xa, ya, xn, yn, X, Y, Xa, Ya);
+        xf dxb = bsx_dcross(xb, yb, xn, yn, X, Y, Xb, Yb);
+        double dX = ddiffabsdX_x(opX, opx), dx = ddiffabsdx_x(opX, opx);
+        nxa = bsx_dsq1(xa, ya, xn, yn, X, Y, Xa, Ya);
+        nxb = bsx_dsq1(xb, yb, xn, yn, X, Y, Xb, Yb);
+        nya = XK(2., XA(XK(dX, dXa), XK(dx, dxa)));
+        nyb = XK(2., XA(XK(dX, dXb), XK(dx, dxb)));
+    } break;
+    case 2: {
+        xf da = diffabs_x(Y, yn);
+        double dX = ddiffabsdX_x(Y, yn), dx = ddiffabsdx_x(Y, yn);
+        xf Yy = XA(Y, yn), ab = xf_abs(Yy);
+        double sg = xf_sgn(Yy);
+        nxa = XK(2., XS(XA(XM(XA(X, xn), xa), XM(Xa, xn)), XA(XM(XA(Y, yn), ya), XM(Ya, yn))));
+        nxb = XK(2., XS(XA(XM(XA(X, xn), xb), XM(Xb, xn)), XA(XM(XA(Y, yn), yb), XM(Yb, yn))));
+        nya = XK(2., XA(XA(XA(XM(Xa, da), XM(X, XA(XK(dX, Ya), XK(dx, ya)))), XM(xa, ab)),
+                        XM(XK(sg, xn), XA(Ya, ya))));
+        nyb = XK(2., XA(XA(XA(XM(Xb, da), XM(X, XA(XK(dX, Yb), XK(dx, yb)))), XM(xb, ab)),
+                        XM(XK(sg, xn), XA(Yb, yb))));
+    } break;
+    case 3: {
+        xf da = diffabs_x(Y, yn);
+        double dX = ddiffabsdX_x(Y, yn), dx = ddiffabsdx_x(Y, yn);
+        xf Yy = XA(Y, yn), ab = xf_abs(Yy);
+        double sg = xf_sgn(Yy);
+        nxa = XS(XS(XS(XS(XA(XM(xa, XA(xn, XK(2., X))), XM(xn, XA(xa, XK(2., Xa)))), XM(Ya, da)),
+                       XM(Y, XA(XK(dX, Ya), XK(dx, ya)))), XM(ya, ab)),
+                 XM(XK(sg, yn), XA(Ya, ya)));
+        nxb = XS(XS(XS(XS(XA(XM(xb, XA(xn, XK(2., X))), XM(xn, XA(xb, XK(2., Xb)))), XM(Yb, da)),
+                       XM(Y, XA(XK(dX, Yb), XK(dx, yb)))), XM(yb, ab)),
+                 XM(XK(sg, yn), XA(Yb, yb)));
+        nya = bsx_dcross2(xa, ya, xn, yn, X, Y, Xa, Ya);
+        nyb = bsx_dcross2(xb, yb, xn, yn, X, Y, Xb, Yb);
+    } break;
+    case 4: {
+        xf opX = XS(XM(X, X), XM(Y, Y));
+        xf dXa = XK(2., XS(XM(X, Xa), XM(Y, Ya))), dXb = XK(2., XS(XM(X, Xb), XM(Y, Yb)));
+        xf opx = bsx_sq(xn, yn, X, Y);
+        xf dxa = bsx_dsq(xa, ya, xn, yn, X, Y, Xa, Ya);
+        xf dxb = bsx_dsq(xb, yb, xn, yn, X, Y, Xb, Yb);
+        double dX = ddiffabsdX_x(opX, opx), dx = ddiffabsdx_x(opX, opx);
+        nxa = XA(XK(dX, dXa), XK(dx, dxa));
+        nxb = XA(XK(dX, dXb), XK(dx, dxb));
+        nya = bsx_dcross2(xa, ya, xn, yn, X, Y, Xa, Ya);
+        nyb = bsx_dcross2(xb, yb, xn, yn, X, Y, Xb, Yb);
+    } break;
+    default: {
+        xf opX = XS(XM(X, X), XM(Y, Y));
+        xf dXa = XK(2., XS(XM(X, Xa), XM(Y, Ya))), dXb = XK(2., XS(XM(X, Xb), XM(Y, Yb)));
+        xf opx = bsx_sq(xn, yn, X, Y);
+        xf dxa = bsx_dsq(xa, ya, xn, yn, X, Y, Xa, Ya);
+        xf dxb = bsx_dsq(xb, yb, xn, yn, X, Y, Xb, Yb);
+        double dX = ddiffabsdX_x(opX, opx), dx = ddiffabsdx_x(opX, opx);
+        nxa = XA(XK(dX, dXa), XK(dx, dxa));
+        nxb = XA(XK(dX, dXb), XK(dx, dxb));
+        xf opX2 = XM(X, Y);
+        xf dXa2 = XA(XM(Xa, Y), XM(X, Ya)), dXb2 = XA(XM(Xb, Y), XM(X, Yb));
+        xf opx2 = bsx_cross(xn, yn, X, Y);
+        xf dxa2 = bsx_dcross(xa, ya, xn, yn, X, Y, Xa, Ya);
+        xf dxb2 = bsx_dcross(xb, yb, xn, yn, X, Y, Xb, Yb);
+        double dX2 = ddiffabsdX_x(opX2, opx2), dx2 = ddiffabsdx_x(opX2, opx2);
+        nya = XK(2., XA(XK(dX2, dXa2), XK(dx2, dxa2)));
+        nyb = XK(2., XA(XK(dX2, dXb2), XK(dx2, dxb2)));
+    } break;
+    }
+    h[0] = nxa; h[1] = nxb; h[2] = nya; h[3] = nyb;
+}
+
+/* models/burning_ship.py:441-532 on Xrange operands: the float factors
+ * (2., the signs) first, as the reference's 2. * sgn(x) * abs(y) */
+static inline void bsx_dfdxy(int flavor, xf x, xf y, xf *fxx, xf *fxy, xf *fyx, xf *fyy) {
+    switch (flavor) {
+    case 1: *fxx = XK(2., x); *fxy = XK(-2., y); *fyx = XK(2. * xf_sgn(x), xf_abs(y));
+            *fyy = XK(2. * xf_sgn(y), xf_abs(x)); break;
+    case 2: *fxx = XK(2., x); *fxy = XK(-2., y); *fyx = XK(2., xf_abs(y));
+            *fyy = XK(2. * xf_sgn(y), x); break;
+    case 3: *fxx = XK(2., x); *fxy = XK(-2., xf_abs(y)); *fyx = XK(2., y); *fyy = XK(2., x); break;
+    case 4: { double s = xf_sgn(XS(XM(x, x), XM(y, y)));
+              *fxx = XK(2. * s, x); *fxy = XK(-2. * s, y); *fyx = XK(2., y); *fyy = XK(2., x); } break;
+    default: { double s = xf_sgn(XS(XM(x, x), XM(y, y)));
+               *fxx = XK(2. * s, x); *fxy = XK(-2. * s, y);
+               *fyx = XK(2. * xf_sgn(x), xf_abs(y)); *fyy = XK(2. * xf_sgn(y), xf_abs(x)); } break;
+    }
+}
+
+/* The BS orbit's side table: perturbation.py:2591-2663 ref_path_get_BS as a
+ * membership lookup (the cursor is an optimisation of it). */
+typedef struct {
+    int32_t n; const int32_t *idx; const double *xm, *ym; const int32_t *xe, *ye;
+} xr_table_bs;
+static inline int xr_lookup_bs(const xr_table_bs *t, int64_t w, xf *X, xf *Y) {
+    int lo = 0, hi = t->n - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        if (t->idx[mid] == w) {
+            X->m = t->xm[mid]; X->e = t->xe[mid]; Y->m = t->ym[mid]; Y->e = t->ye[mid];
+            return 1;
+        }
+        if (t->idx[mid] < w) lo = mid + 1; else hi = mid - 1;
+    }
+    return 0;
+}
+/* ensure_xr_BS (perturbation.py:2182-2193): the side-table value, else the
+ * standard value as Xrange */
+static inline void bsx_ref(const xr_table_bs *t, const double *Zn, int64_t w, xf *X, xf *Y,
+                           int *is_xr) {
+    *is_xr = t->n > 0 && xr_lookup_bs(t, w, X, Y);
+    if (!*is_xr) { *X = xr_from_r(Zn[2 * w]); *Y = xr_from_r(Zn[2 * w + 1]); }
+}
+
+/* numba_dZndc_path_BS, Xrange branch: out_m / out_e [4][len] (dXnda, dXndb,
+ * dYnda, dYndb); scale = dx * projection scale as a float64 Xrange */
+EXPORT void orc_dzndc_path_bs_xr(const double *Zn, int64_t len, int64_t ref_div_iter,
+                                 int64_t ref_order, int32_t flavor, double scale_m,
+                                 int32_t scale_e, int32_t n_xr, const int32_t *xr_idx,
+                                 const double *xr_xm, const int32_t *xr_xe, const double *xr_ym,
+                                 const int32_t *xr_ye, double *out_m, int32_t *out_e) {
+    const xr_table_bs t = {n_xr, xr_idx, xr_xm, xr_ym, xr_xe, xr_ye};
+    const xf dx = {scale_m, scale_e};
+    int64_t valid = len < ref_div_iter ? len : ref_div_iter;
+    for (int64_t k = 0; k < 4 * len; k++) { out_m[k] = 0.; out_e[k] = 0; }
+#define PM(j, i) out_m[(j) * len + (i)]
+#define PE(j, i) out_e[(j) * len + (i)]
+    int64_t i;
+    for (i = 1; i <= valid; i++) {
+        int64_t from = i - 1, to = i;
+        if (i == valid) {
+            if (!(from == ref_order - 1)) break;
+            to = 0;
+        }
+        xf X, Y; int isx;
+        bsx_ref(&t, Zn, from, &X, &Y, &isx);
+        xf fxx, fxy, fyx, fyy;
+        bsx_dfdxy(flavor, X, Y, &fxx, &fxy, &fyx, &fyy);
+        xf a = {PM(0, from), PE(0, from)}, b = {PM(1, from), PE(1, from)};
+        xf c = {PM(2, from), PE(2, from)}, d = {PM(3, from), PE(3, from)};
+        xf r[4];
+        r[0] = XA(XA(XM(fxx, a), XM(fxy, c)), dx);
+        r[1] = XA(XM(fxx, b), XM(fxy, d));
+        r[2] = XA(XM(fyx, a), XM(fyy, c));
+        r[3] = XS(XA(XM(fyx, b), XM(fyy, d)), dx);
+        for (int j = 0; j < 4; j++) { PM(j, to) = r[j].m; PE(j, to) = r[j].e; }
+    }
+#undef PM
+#undef PE
+}
+
+typedef struct {
+    const double *Zn; int64_t ref_len; int64_t ref_div_iter; int64_t ref_order;
+    int32_t n_xr; const int32_t *xr_idx; const double *xr_xm; const int32_t *xr_xe;
+    const double *xr_ym; const int32_t *xr_ye;
+    const double *path_m; const int32_t *path_e;          /* [4][ref_len] Xrange Jacobian */
+    const double *M_bla; const double *r_bla; int32_t stages_bla; int32_t bla_on;
+    int64_t max_iter; double M2; int32_t flavor; int32_t calc_hessian;
+    double lin_mat[4]; double dx_m; int32_t dx_e; double driftx_m; int32_t driftx_e;
+    double drifty_m; int32_t drifty_e;
+} orc_pbs_xr_args;
+
+EXPORT int orc_perturb_bs_xr(const orc_pbs_xr_args *P, int64_t npts, const double *pix,
+                             double *Zout, int32_t nZ, int32_t *U, int8_t *stop_reason,
+                             int32_t *stop_iter) {
+    const int64_t order = P->ref_order, div_iter = P->ref_div_iter, plen = P->ref_len;
+    const int hess = P->calc_hessian;
+    const xr_table_bs t = {P->n_xr, P->xr_idx, P->xr_xm, P->xr_ym, P->xr_xe, P->xr_ye};
+    int64_t first_invalid = plen;
+    if (div_iter < first_invalid) first_invalid = div_iter;
+    if (order < first_invalid) first_invalid = order;
+#define PATH(j, w) ((xf){P->path_m[(j) * plen + (w)], P->path_e[(j) * plen + (w)]})
+    for (int64_t ip = 0; ip < npts; ip++) {
+        /* perturbation.py:2260-2280 ref_path_c_from_pix_BS */
+        double px = pix[2 * ip], py = pix[2 * ip + 1];
+        double x1 = P->lin_mat[0] * px + P->lin_mat[1] * py;
+        double y1 = P->lin_mat[2] * px + P->lin_mat[3] * py;
+        xf dxr = {P->dx_m, P->dx_e};
+        xc c_xr = xf_mul_c(dxr, C(x1, y1));
+        xf ddx = {P->driftx_m, P->driftx_e}, ddy = {P->drifty_m, P->drifty_e};
+        xf cre = {c_xr.re, c_xr.e}, cim = {c_xr.im, c_xr.e};
+        const xf a_xr = XA(cre, ddx), b_xr = XA(cim, ddy);
+        /* numba_initialize_BS: the Xrange deltas from the tile's Z, the
+         * standard copies as the tile's values */
+        double xs = Zout[ip], ys = Zout[npts + ip];
+        xf xn = xr_from_r(xs), yn = xr_from_r(ys);
+        xf h[4] = {XF0, XF0, XF0, XF0};
+        if (hess) for (int k = 0; k < 4; k++) h[k] = xr_from_r(Zout[(2 + k) * npts + ip]);
+        int64_t w = 0, n = 0; int8_t stop = -1; int dyn = 1;
+        for (;;) {
+            if (P->bla_on && (w & 7) == 0) {                   /* :1520-1545 */
+                int64_t ib;
+                int64_t step = bla_get(P->r_bla, P->stages_bla, hypot(xs, ys), w, first_invalid, &ib);
+                if (step != 0) {
+                    const double *M = P->M_bla + 8 * ib;
+                    n += step; w = (w + step) % order;
+                    xf nx = XA(XA(XA(XK(M[0], xn), XK(M[1], yn)), XK(M[4], a_xr)), XK(M[5], b_xr));
+                    xf ny = XA(XA(XA(XK(M[2], xn), XK(M[3], yn)), XK(M[6], a_xr)), XK(M[7], b_xr));
+                    xn = nx; yn = ny;
+                    xs = xf_to_std(xn); ys = xf_to_std(yn);
+                    if (hess) {
+                        xf xa = XA(XK(M[0], h[0]), XK(M[1], h[2])), xb = XA(XK(M[0], h[1]), XK(M[1], h[3]));
+                        xf ya = XA(XK(M[2], h[0]), XK(M[3], h[2])), yb = XA(XK(M[2], h[1]), XK(M[3], h[3]));
+                        h[0] = xa; h[1] = xb; h[2] = ya; h[3] = yb;
+                    }
+                    continue;
+                }
+            }
+            n += 1;                                                /* :1548-1611 */
+            xf X, Y; int isx;
+            bsx_ref(&t, P->Zn, w, &X, &Y, &isx);
+            if (hess) {
+                xf Xa = XF0, Xb = XF0, Ya = XF0, Yb = XF0;
+                if (!dyn) { Xa = PATH(0, w); Xb = PATH(1, w); Ya = PATH(2, w); Yb = PATH(3, w); }
+                bsx_p_iter_hessian(P->flavor, h, xn, yn, X, Y, Xa, Xb, Ya, Yb);
+            }
+            bsx_p_iter_zn(P->flavor, &xn, &yn, X, Y, a_xr, b_xr);
+            xs = xf_to_std(xn); ys = xf_to_std(yn);
+            if (n >= P->max_iter) { stop = 0; break; }
+            w += 1;
+            if (w >= order) w = w % order;
+            xf Xn, Yn; int isn;                                    /* :1627-1636 */
+            bsx_ref(&t, P->Zn, w, &Xn, &Yn, &isn);
+            double XX = xs + P->Zn[2 * w], YY = ys + P->Zn[2 * w + 1];
+            if (XX * XX + YY * YY > P->M2) { stop = 1; break; }
+            if (w >= div_iter - 1) {                               /* :1660-1684 */
+                xs = XX; ys = YY;
+                xn = xr_from_r(XX); yn = xr_from_r(YY);
+                if (hess) for (int k = 0; k < 4; k++) h[k] = XA(h[k], PATH(k, w));
+                w = 0; continue;
+            }
+            dyn = (fabs(XX) <= fabs(xs)) && (fabs(YY) <= fabs(ys));   /* :1688-1731 */
+            if (dyn) {
+                xf XXx = isn ? XA(xn, Xn) : xf_add_s(xn, P->Zn[2 * w]);
+                xf YYx = isn ? XA(yn, Yn) : xf_add_s(yn, P->Zn[2 * w + 1]);
+                if (xf_le(XA(XM(XXx, XXx), XM(YYx, YYx)), XA(XM(xn, xn), XM(yn, yn)))) {
+                    xn = XXx; yn = YYx;
+                    xs = xf_to_std(XXx); ys = xf_to_std(YYx);
+                    if (hess) for (int k = 0; k < 4; k++) h[k] = XA(h[k], PATH(k, w));
+                    w = 0; continue;
+                }
+            }
+        }
+        U[ip] = (int32_t)w;                                        /* :1745-1757 */
+        Zout[ip] = xf_to_std(xf_add_s(xn, P->Zn[2 * w]));
+        Zout[npts + ip] = xf_to_std(xf_add_s(yn, P->Zn[2 * w + 1]));
+        if (hess) for (int k = 0; k < 4; k++) Zout[(2 + k) * npts + ip] = xf_to_std(XA(h[k], PATH(k, w)));
+        stop_iter[ip] = (int32_t)n; stop_reason[ip] = stop;
+    }
+#undef PATH
+    return 0;
+}
+#undef XA
+#undef XS
+#undef XM
+#undef XK

@@ -57,6 +57,18 @@ class PM2Args(ct.Structure):
     ]
 
 
+class PBSXArgs(ct.Structure):
+    _fields_ = [
+        ("Zn", P), ("ref_len", I64), ("ref_div_iter", I64), ("ref_order", I64),
+        ("n_xr", I32), ("xr_idx", P), ("xr_xm", P), ("xr_xe", P), ("xr_ym", P), ("xr_ye", P),
+        ("path_m", P), ("path_e", P),
+        ("M_bla", P), ("r_bla", P), ("stages_bla", I32), ("bla_on", I32),
+        ("max_iter", I64), ("M2", F64), ("flavor", I32), ("calc_hessian", I32),
+        ("lin_mat", F64 * 4), ("dx_m", F64), ("dx_e", I32),
+        ("driftx_m", F64), ("driftx_e", I32), ("drifty_m", F64), ("drifty_e", I32),
+    ]
+
+
 class PBSArgs(ct.Structure):
     _fields_ = [
         ("Zn", P), ("ref_len", I64), ("ref_div_iter", I64), ("ref_order", I64),
@@ -92,6 +104,10 @@ def _declare(L):
     L.orc_perturb_m2.restype = ct.c_int
     L.orc_perturb_bs.argtypes = [ct.POINTER(PBSArgs), I64, P, P, I32, P, P, P]
     L.orc_perturb_bs.restype = ct.c_int
+    L.orc_dzndc_path_bs_xr.argtypes = [P, I64, I64, I64, I32, F64, I32, I32, P, P, P, P, P,
+                                       P, P]
+    L.orc_perturb_bs_xr.argtypes = [ct.POINTER(PBSXArgs), I64, P, P, I32, P, P, P]
+    L.orc_perturb_bs_xr.restype = ct.c_int
 
 
 def _p(a):
@@ -358,4 +374,72 @@ def perturb_bs(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
     si = np.zeros((1, n), dtype=np.int32)
     sr = -np.ones((1, n), dtype=np.int8)
     lib().orc_perturb_bs(ct.byref(a), n, _p(pix), _p(Z), nZ, _p(U), _p(sr), _p(si))
+    return Z, U, sr, si
+
+
+# ---------------------------------------------------------------------------
+# Burning Ship, Xrange branch (perturbation.py:1468-1791 with xr_detect_activated)
+# ---------------------------------------------------------------------------
+def _bs_xr_table(xr):
+    """xr: (idx, xm, xe, ym, ye) or None -> contiguous arrays (at least one
+    slot, as the reference's)."""
+    if xr is None or len(xr[0]) == 0:
+        return (np.zeros(0, np.int32), np.zeros(1), np.zeros(1, np.int32), np.zeros(1),
+                np.zeros(1, np.int32))
+    idx, xm, xe, ym, ye = xr
+    return (_c(idx, np.int32), _c(xm, np.float64), _c(xe, np.int32), _c(ym, np.float64),
+            _c(ye, np.int32))
+
+
+def dzndc_path_bs_xr(Zn, ref_div_iter, ref_order, flavor, scale_m, scale_e, xr=None):
+    """Xrange Jacobian paths (dXnda, dXndb, dYnda, dYndb): (m [4, len], e [4, len])."""
+    Zn = _c(Zn, np.complex128)
+    n = Zn.size
+    idx, xm, xe, ym, ye = _bs_xr_table(xr)
+    m = np.zeros((4, n))
+    e = np.zeros((4, n), dtype=np.int32)
+    lib().orc_dzndc_path_bs_xr(_p(Zn), n, int(ref_div_iter), int(ref_order), int(flavor),
+                               float(scale_m), int(scale_e), idx.size, _p(idx), _p(xm),
+                               _p(xe), _p(ym), _p(ye), _p(m), _p(e))
+    return m, e
+
+
+def perturb_bs_xr(pix, *, Zn, ref_div_iter, ref_order, lin_mat, dx_m, dx_e,
+                  driftx_m, driftx_e, drifty_m, drifty_e, max_iter, M, flavor,
+                  calc_hessian=True, bla=None, xpaths=None, xr=None):
+    """The Xrange branch: xpaths the Xrange Jacobian paths (m, e), xr the
+    orbit's side table (idx, xm, xe, ym, ye)."""
+    pix = _c(pix, np.complex128)
+    n = pix.size
+    Zn = _c(Zn, np.complex128)
+    keep = []
+    a = PBSXArgs()
+    a.Zn, a.ref_len, a.ref_div_iter, a.ref_order = _p(Zn), Zn.size, int(ref_div_iter), int(ref_order)
+    t = _bs_xr_table(xr)
+    keep += list(t)
+    a.n_xr, a.xr_idx, a.xr_xm, a.xr_xe, a.xr_ym, a.xr_ye = t[0].size, *[_p(v) for v in t]
+    if xpaths is not None:
+        pm, pe = _c(xpaths[0], np.float64), _c(xpaths[1], np.int32)
+        keep += [pm, pe]
+        a.path_m, a.path_e = _p(pm), _p(pe)
+    if bla is not None:
+        Mb = _c(bla[0], np.float64)
+        rb = _c(bla[1], np.float64)
+        keep += [Mb, rb]
+        a.M_bla, a.r_bla, a.stages_bla, a.bla_on = _p(Mb), _p(rb), int(bla[2]), 1
+    else:
+        a.bla_on = 0
+    a.max_iter, a.M2, a.flavor, a.calc_hessian = int(max_iter), M * M, int(flavor), int(calc_hessian)
+    lm = np.asarray(lin_mat, dtype=np.float64).ravel()
+    for k in range(4):
+        a.lin_mat[k] = lm[k]
+    a.dx_m, a.dx_e = float(dx_m), int(dx_e)
+    a.driftx_m, a.driftx_e = float(driftx_m), int(driftx_e)
+    a.drifty_m, a.drifty_e = float(drifty_m), int(drifty_e)
+    nZ = 6 if calc_hessian else 2
+    Z = np.zeros((nZ, n), dtype=np.float64)
+    U = np.zeros((1, n), dtype=np.int32)
+    si = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    lib().orc_perturb_bs_xr(ct.byref(a), n, _p(pix), _p(Z), nZ, _p(U), _p(sr), _p(si))
     return Z, U, sr, si

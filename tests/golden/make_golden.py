@@ -556,18 +556,25 @@ def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
         a, b = ref_point.real, ref_point.imag
         it = f.xnyn_iterate
         i = 0
+        # the side table of FP_loop.pyx:1828-1979: iterations where |X| or |Y|
+        # is below xrange_zoom_level, when the Xrange branch is active
+        xr_dict = {}
+        need_xr = f.xr_detect_activated
         for i in range(1, ref_orbit_len):
             xn, yn = it(xn, yn, a, b)
             orbit[i] = complex(float(xn), float(yn))
             if np.hypot(orbit[i].real, orbit[i].imag) > 2 * M:
                 break
+            if need_xr and (abs(xn) < fs.settings.xrange_zoom_level
+                            or abs(yn) < fs.settings.xrange_zoom_level):
+                xr_dict[i] = (fsx.mpf_to_Xrange(xn).ravel(), fsx.mpf_to_Xrange(yn).ravel())
         if i == ref_orbit_len - 1 and np.hypot(orbit[i].real, orbit[i].imag) <= 2 * M:
             i += 1
         init_kwargs = f.init_kwargs
         del init_kwargs["directory"]
         FP_params = {"ref_point": ref_point, "dps": mpmath.mp.dps,
                      "order": None, "max_iter": max_iter, "FP_code": f.FP_code,
-                     "partials": {}, "xr": {}, "div_iter": i,
+                     "partials": {}, "xr": xr_dict, "div_iter": i,
                      "init_kwargs": init_kwargs, "ref_orbit_len": ref_orbit_len}
         f.save_ref_point(FP_params, orbit)
         f.calc_std_div(calc_name="pert", subset=None, max_iter=max_iter,
@@ -578,6 +585,15 @@ def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
          refy_xr, ref_div_iter, ref_order, driftx_xr, drifty_xr, dx_xr, _p,
          lin_mat, lin_scale_xr, kc, M_bla, r_bla, bla_len, stages_bla, _m,
          _i) = cia
+        xr = bool(f.xr_detect_activated)
+        extra = {"xr_mode": int(xr)}
+        if xr:
+            extra["xr_idx"] = ref_index_xr
+            extra["xr_xm"], extra["xr_xe"] = xr_arrays(refx_xr)
+            extra["xr_ym"], extra["xr_ye"] = xr_arrays(refy_xr)
+            for k, pth in (("dXa", dXa), ("dXb", dXb), ("dYa", dYa), ("dYb", dYb)):
+                extra[k + "_m"], extra[k + "_e"] = xr_arrays(pth)
+            dXa = dXb = dYa = dYb = np.zeros(1)
         np.savez_compressed(
             out, pix=c_pix, Z=Z, U=U, stop_reason=sr, stop_iter=si,
             Zn=Zn_path, dXa=dXa, dXb=dXb, dYa=dYa, dYb=dYb,
@@ -590,7 +606,7 @@ def golden_perturb_bs(out, *, x, y, dx, nx, precision, max_iter, flavor,
             drifty_e=np.asarray(drifty_xr._exp)[0],
             kc_m=np.asarray(kc._mantissa)[0], kc_e=np.asarray(kc._exp)[0],
             max_iter=max_iter, M=M, bla_eps=bla_eps, backshift=backshift,
-            M_bla=M_bla, r_bla=r_bla, stages_bla=stages_bla)
+            M_bla=M_bla, r_bla=r_bla, stages_bla=stages_bla, **extra)
 
 
 def golden_std_opts(out):
@@ -1024,8 +1040,40 @@ def bs_flavor_cases():
         print(name + " done", flush=True)
 
 
+def bs_xr_cases():
+    """Perturbation Burning Ship on the Xrange branch (dx = 1e-305 <
+    xrange_zoom_level): flavor 1 at the centre of pert_bs_1 and flavor 5 at
+    that of pert_bs_5, whose references diverge after ~2200 and ~2900
+    iterations; the deltas start below the double range."""
+    mpmath.mp.dps = 340
+    for fl, flav, x, y, name in (
+            (1, "Burning ship", "-1.773934837092732", "-0.00025062656641604286", "pert_bs_xr_1"),
+            (5, "Buffalo", "-1.5394062147086462", "0.2671241854166664", "pert_bs_xr_5")):
+        golden_perturb_bs(
+            os.path.join(HERE, name + ".npz"), x=x, y=y, dx="1.e-305",
+            nx=5, precision=340, max_iter=5000, flavor=flav)
+        print(name + " done", flush=True)
+
+
+def bs_xr_axis_case():
+    """Burning Ship on the Xrange branch around a point of the real axis
+    (-1.7548776662466927, the real map's superstable period 3): Y_n = 0 on
+    the whole orbit, so every iteration enters the side table of
+    FP_loop.pyx:1828-1979 and the loop reads its Xrange values; no BLA step is
+    valid there (r = eps min(|X|, |Y|) = 0)."""
+    mpmath.mp.dps = 340
+    golden_perturb_bs(
+        os.path.join(HERE, "pert_bs_xr_axis.npz"), x="-1.7548776662466927", y="0",
+        dx="1.e-305", nx=4, precision=340, max_iter=1500, flavor="Burning ship")
+    print("pert_bs_xr_axis done", flush=True)
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "p2562":
+    if len(sys.argv) > 2 and sys.argv[2] == "bs_xr":
+        bs_xr_cases()
+    elif len(sys.argv) > 2 and sys.argv[2] == "bs_xr_axis":
+        bs_xr_axis_case()
+    elif len(sys.argv) > 2 and sys.argv[2] == "p2562":
         p2562_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "bs_flavors":
         bs_flavor_cases()

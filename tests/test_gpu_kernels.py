@@ -820,3 +820,100 @@ def test_long_orbit_paths_scan_vs_oracle(ctx, xr):
         big = np.abs(dzzo) > 1e-250
         np.testing.assert_allclose(dzz[big], dzzo[big], rtol=1e-11, atol=0)
         assert np.all(np.abs(dzz[~big]) < 1e-240)
+
+
+# ---------------------------------------------------------------------------
+# Burning Ship on the Xrange branch (dx = 1e-305, reference-generated): the
+# XR64 kernel against the reference's results, its Xrange Jacobian paths
+# against the oracle's; the FP32 + exponent form on the same cases
+BS_XR_CASES = ["pert_bs_xr_1", "pert_bs_xr_5", "pert_bs_xr_axis"]
+
+
+def _bs_xr_ref(ctx, d):
+    from fractalshades_gb300 import _native as nat
+    fl = int(d["flavor"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    n_xr = int(d["xr_idx"].size)
+    xr_m = np.concatenate([d["xr_xm"], d["xr_ym"]]) if n_xr else None
+    xr_e = np.concatenate([d["xr_xe"], d["xr_ye"]]) if n_xr else None
+    return nat.Reference(ctx, d["Zn"], div_iter=int(d["ref_div_iter"]), order=int(d["ref_order"]),
+                         flavor=fl, xr_idx=d["xr_idx"] if n_xr else None, xr_m=xr_m, xr_e=xr_e,
+                         xr_paths=True, calc_dzndc=True, scale_m=float(d["dx_m"]),
+                         scale_e=int(d["dx_e"]), bla=True, kc=kc, bla_eps=float(d["bla_eps"]))
+
+
+def _run_bs_ref(ctx, d, ref, mode, lin_scale=1.):
+    from fractalshades_gb300 import _native as nat
+    nx = int(round(np.sqrt(d["pix"].size)))
+    xs, ys = axes(d["pix"], nx)
+    n = d["pix"].size
+    Z = np.zeros((6, n))
+    U = np.zeros((1, n), dtype=np.int32)
+    sr = -np.ones((1, n), dtype=np.int8)
+    si = np.zeros((1, n), dtype=np.int32)
+    t = nat.make_tile(xs=xs, ys=ys, lin_mat=np.asarray(d["lin_mat"]) * lin_scale, Z=Z, U=U,
+                      stop_reason=sr, stop_iter=si, ref=ref, dx_m=float(d["dx_m"]),
+                      dx_e=int(d["dx_e"]), drift_m=float(d["driftx_m"]),
+                      drift_e=int(d["driftx_e"]), drifty_m=float(d["drifty_m"]),
+                      drifty_e=int(d["drifty_e"]))
+    calc = nat.make_calc(max_iter=int(d["max_iter"]), M_divergence=float(d["M"]),
+                         flavor=int(d["flavor"]), calc_dzndc=True, bla=True, mode=mode)
+    ctx.perturb_tiles(calc, [t])
+    return Z, U, sr, si
+
+
+def _xr_pairs(m, e):
+    f, k = np.frexp(np.asarray(m, dtype=np.float64))
+    return np.stack([f, np.where(f == 0., 0, np.asarray(e, dtype=np.int64) + k).astype(float)])
+
+
+@pytest.mark.parametrize("case", BS_XR_CASES)
+def test_perturb_bs_xr64_vs_reference(ctx, case):
+    """The XR64 Burning Ship kernel (the reference's Xrange branch, -fmad=false,
+    numba_xr operations in the reference's order): Jacobian paths equal to the
+    oracle's, iteration counts, stop reasons and U equal to the reference's,
+    Z within 1e-6 relative (bit for bit where it runs like the oracle)."""
+    d = load(case)
+    fl = int(d["flavor"])
+    ref = _bs_xr_ref(ctx, d)
+    m, e = ref.download("bs_xpaths")
+    xr = (d["xr_idx"], d["xr_xm"], d["xr_xe"], d["xr_ym"], d["xr_ye"])
+    pm, pe = orc.dzndc_path_bs_xr(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), fl,
+                                  float(d["dx_m"]), int(d["dx_e"]), xr)
+    for j in range(4):
+        assert np.array_equal(_xr_pairs(m[j], e[j]), _xr_pairs(pm[j], pe[j])), j
+    Z, U, sr, si = _run_bs_ref(ctx, d, ref, "xr64")
+    ref.free()
+    iter_agree(si, d["stop_iter"])
+    assert np.array_equal(sr, d["stop_reason"])
+    same = (si == d["stop_iter"]).ravel()
+    for k in range(6):
+        rel_close(Z[k], d["Z"][k], 1e-6, same)
+
+
+@pytest.mark.parametrize("case", BS_XR_CASES)
+def test_perturb_bs_fe32_vs_xrange_reference(ctx, case):
+    """The FP32 + exponent Burning Ship form below the double range against
+    the reference's Xrange branch: counts differ on at most
+    FE32_SENSITIVITY_FACTOR x the case's FP32 sensitivity (the oracle's
+    Xrange branch against itself with c moved by 2^-24) + FE32_ALLOWANCE."""
+    d = load(case)
+    fl = int(d["flavor"])
+    ref = _bs_xr_ref(ctx, d)
+    Z, U, sr, si = _run_bs_ref(ctx, d, ref, "fe32")
+    ref.free()
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    Mb, rb, _, st = orc.make_bla_bs(d["Zn"], fl, kc, float(d["bla_eps"]))
+    xr = (d["xr_idx"], d["xr_xm"], d["xr_xe"], d["xr_ym"], d["xr_ye"])
+    paths = orc.dzndc_path_bs_xr(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), fl,
+                                 float(d["dx_m"]), int(d["dx_e"]), xr)
+    _, _, _, sis = orc.perturb_bs_xr(
+        d["pix"], Zn=d["Zn"], ref_div_iter=int(d["ref_div_iter"]),
+        ref_order=int(d["ref_order"]), lin_mat=np.asarray(d["lin_mat"]) * (1. + 2. ** -24),
+        dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]), driftx_m=float(d["driftx_m"]),
+        driftx_e=int(d["driftx_e"]), drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]),
+        max_iter=int(d["max_iter"]), M=float(d["M"]), flavor=fl, bla=(Mb, rb, st),
+        xpaths=paths, xr=xr)
+    bar = FE32_SENSITIVITY_FACTOR * float(np.mean(sis != d["stop_iter"])) + FE32_ALLOWANCE
+    assert float(np.mean(si != d["stop_iter"])) <= bar
+    assert float(np.mean(sr != d["stop_reason"])) <= bar

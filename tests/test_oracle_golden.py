@@ -344,3 +344,57 @@ def test_perturb_expmap_oracle_matches_reference():
     assert np.array_equal(si, d["stop_iter"]) and np.array_equal(U, d["U"])
     Z[-1] = Z[-1] * proj.dzndc_modifier(d["pix"])
     assert np.array_equal(Z.view(np.uint64), d["Z"].view(np.uint64))
+
+
+# ---------------------------------------------------------------------------
+# Burning Ship on the Xrange branch (dx = 1e-305): flavor 1 and 5 around
+# diverging references, flavor 1 on the real axis (every orbit point in the
+# side table)
+BS_XR_CASES = ["pert_bs_xr_1", "pert_bs_xr_5", "pert_bs_xr_axis"]
+
+
+def _xr_normal(m, e):
+    """Records (m, e) as normalised (mantissa in [0.5, 1), exponent) pairs,
+    zero as (0, 0): equal values give equal pairs."""
+    f, k = np.frexp(np.asarray(m, dtype=np.float64))
+    ex = np.where(f == 0., 0, np.asarray(e, dtype=np.int64) + k)
+    return np.stack([f, ex.astype(np.float64)])
+
+
+def bs_xr_inputs(d):
+    fl = int(d["flavor"])
+    kc = float(np.ldexp(d["kc_m"], d["kc_e"]))
+    Mb, rb, _, st = orc.make_bla_bs(d["Zn"], fl, kc, float(d["bla_eps"]))
+    xr = (d["xr_idx"], d["xr_xm"], d["xr_xe"], d["xr_ym"], d["xr_ye"])
+    paths = orc.dzndc_path_bs_xr(d["Zn"], int(d["ref_div_iter"]), int(d["ref_order"]), fl,
+                                 float(d["dx_m"]), int(d["dx_e"]), xr)
+    return (Mb, rb, st), xr, paths
+
+
+@pytest.mark.parametrize("case", BS_XR_CASES)
+def test_perturb_bs_xr_matches_reference(case):
+    d = load(case)
+    assert int(d["xr_mode"]) == 1
+    fl = int(d["flavor"])
+    bla, xr, paths = bs_xr_inputs(d)
+    assert bla[2] == int(d["stages_bla"])
+    assert np.array_equal(bla[0].view(np.uint64), d["M_bla"].view(np.uint64))
+    assert np.array_equal(bla[1].view(np.uint64), d["r_bla"].view(np.uint64))
+    # the Xrange Jacobian paths: equal values (the reference's host class
+    # normalises its records where numba_xr does not)
+    for j, k in enumerate(["dXa", "dXb", "dYa", "dYb"]):
+        assert np.array_equal(_xr_normal(paths[0][j], paths[1][j]),
+                              _xr_normal(d[k + "_m"], d[k + "_e"])), k
+    Z, U, sr, si = orc.perturb_bs_xr(
+        d["pix"], Zn=d["Zn"], ref_div_iter=int(d["ref_div_iter"]),
+        ref_order=int(d["ref_order"]), lin_mat=d["lin_mat"],
+        dx_m=float(d["dx_m"]), dx_e=int(d["dx_e"]),
+        driftx_m=float(d["driftx_m"]), driftx_e=int(d["driftx_e"]),
+        drifty_m=float(d["drifty_m"]), drifty_e=int(d["drifty_e"]),
+        max_iter=int(d["max_iter"]), M=float(d["M"]), flavor=fl, bla=bla, xpaths=paths, xr=xr)
+    assert np.array_equal(si, d["stop_iter"])
+    assert np.array_equal(sr, d["stop_reason"])
+    assert np.array_equal(U, d["U"])
+    nan = np.isnan(Z)
+    assert np.array_equal(nan, np.isnan(d["Z"]))
+    assert np.array_equal(Z[~nan].view(np.uint64), d["Z"][~nan].view(np.uint64))
