@@ -125,13 +125,13 @@ class PerturbSpec:
                 return "xr64" if self.xr_detect_activated else "fp64"
             return m
         if self.flavor != 0:
-            # Burning Ship: no Xrange kernel; below the double range the
-            # FP32 + exponent form is the one without underflow
+            # Burning Ship: the reference's two branches (Xrange below
+            # dx = 1e-300), or the FP32 + exponent form
             if self.xr_detect_activated:
-                if m in ("fp64", "xr64"):
+                if m == "fp64":
                     raise ValueError("Burning Ship below dx = 1e-300 runs with "
-                                     "precision_mode 'auto' or 'fe32'")
-                return "fe32"
+                                     "precision_mode 'auto', 'xr64' or 'fe32'")
+                return "xr64" if m == "auto" else m
             return "fp64" if m in ("auto", "xr64") else m
         if m == "auto":
             return "xr64" if self.xr_detect_activated else "fp64"

@@ -323,8 +323,10 @@ class PerturbationFractal(Fractal):
                 "the reference calculation precicion.")
         bla_eps = self.BLA_eps
         xr = self.xr_detect_activated
-        # Burning Ship below the double range: the Jacobian paths at the
-        # scale m (dx = m 2^e), the tiles add 2^e (fsg_tile.dzndc_scale_e)
+        # Burning Ship below the double range: the Jacobian paths (double for
+        # the FP32 + exponent form, Xrange records for the Xrange branch) at
+        # the scale m (dx = m 2^e), the tiles add 2^e (fsg_tile.dzndc_scale_e):
+        # the recurrences are linear in the scale and a power of two is exact
         dzndc_scale_e = 0
         if xr and not holomorphic:
             scale = fsx.XrScalar(dx_xr.m, 0)
@@ -335,7 +337,7 @@ class PerturbationFractal(Fractal):
             flavor=0 if holomorphic else self.flavor_int,
             xr_idx=ref_index_xr if has_xr else None,
             xr_m=ref_xr[0] if has_xr else None, xr_e=ref_xr[1] if has_xr else None,
-            xr_paths=xr and holomorphic, calc_dzndc=calc_deriv_c,
+            xr_paths=xr, calc_dzndc=calc_deriv_c,
             calc_dzndz=calc_dZndz, scale_m=scale.m, scale_e=scale.e,
             bla=bla_eps is not None, kc=kc.to_standard(),
             bla_eps=bla_eps if bla_eps is not None else 0.,

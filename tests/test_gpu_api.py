@@ -74,13 +74,16 @@ def test_perturbation_calc_raw_vs_oracle(tmp_path, mode):
     assert agree >= (0.9999 if mode == "auto" else 0.99), agree
 
 
-def test_burning_ship_below_double_range(tmp_path):
+@pytest.mark.parametrize("mode", ["auto", "fe32"])
+def test_burning_ship_below_double_range(tmp_path, mode):
     """Burning Ship below dx = 1e-300 (the reference's Xrange branch): the
-    FP32 + exponent loop with unit-scale Jacobian paths and the tile's scale
-    2^e.  Every pixel of the view escapes at the iteration a direct 340-digit
-    iteration of the map gives, at 1e-310 as at 1e-250 (the FP64 path), and
-    the Hessian per unit of c agrees between the two depths."""
+    XR64 loop ("auto") or the FP32 + exponent loop, with unit-scale Jacobian
+    paths and the tile's scale 2^e.  Every pixel of the view escapes at the
+    iteration a direct 340-digit iteration of the map gives, at 1e-310 as at
+    1e-250 (the FP64 path), and the Hessian per unit of c agrees between the
+    two depths."""
     import fractalshades_gb300.models as fsm
+    from fractalshades_gb300 import settings
     from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
     with mpmath.workdps(340):
         ok, nuc = fsFP.perturbation_nonholomorphic_find_any_nucleus(
@@ -95,14 +98,19 @@ def test_burning_ship_below_double_range(tmp_path):
             if zx * zx + zy * zy > 1e6:
                 break
     out = {}
-    for dx in ("1e-250", "1e-310"):
-        f = fsm.Perturbation_burning_ship(str(tmp_path / dx))
-        f.zoom(precision=340, x=x, y=y, dx=dx, nx=24, xy_ratio=1., theta_deg=0.)
-        f.calc_std_div(calc_name="bs", subset=None, max_iter=2000, M_divergence=1000.,
-                       BLA_eps=1e-6, calc_hessian=True)
-        f.calc_raw("bs")
-        out[dx] = {k: f.get_raw("bs", k) for k in ("stop_iter", "dxnda", "dyndb")}
-        assert f.xr_detect_activated == (dx == "1e-310")
+    old = settings.precision_mode
+    settings.precision_mode = mode
+    try:
+        for dx in ("1e-250", "1e-310"):
+            f = fsm.Perturbation_burning_ship(str(tmp_path / dx))
+            f.zoom(precision=340, x=x, y=y, dx=dx, nx=24, xy_ratio=1., theta_deg=0.)
+            f.calc_std_div(calc_name="bs", subset=None, max_iter=2000, M_divergence=1000.,
+                           BLA_eps=1e-6, calc_hessian=True)
+            f.calc_raw("bs")
+            out[dx] = {k: f.get_raw("bs", k) for k in ("stop_iter", "dxnda", "dyndb")}
+            assert f.xr_detect_activated == (dx == "1e-310")
+    finally:
+        settings.precision_mode = old
     for dx, o in out.items():
         assert np.all(o["stop_iter"] == n0), (dx, np.unique(o["stop_iter"]), n0)
     for k in ("dxnda", "dyndb"):
