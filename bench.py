@@ -412,6 +412,20 @@ def view_leg(ctx, nat, torch, dev, timed, we, wx, parity_pixels, seed, workload)
         rows[f"oracle_c_offset_2^-24_vs_{br.lower()}_branch"] = parity_table(o_shift, o_std, we.M)
         rows["oracle_s"] = time.perf_counter() - t0
         out["vs_oracle"] = rows
+        # every form and the oracle against exact arithmetic on a sub-sample
+        t0 = time.perf_counter()
+        sub = np.sort(np.random.default_rng(seed + 1).choice(
+            idx.size, size=min(DIRECT_PIXELS, idx.size), replace=False))
+        exact = direct_pixels(we, idx[sub])
+        pick = lambda s: {k: v[sub] for k, v in s.items()}     # noqa: E731
+        rows = {"sample": f"{sub.size} of the seeded pixels above",
+                "exact": f"z^2 + c iterated directly at {we.dps} digits (MPFR), dzndc along "
+                         "the exact orbit in double",
+                f"oracle_{br.lower()}_branch": parity_table(pick(o_std), exact, we.M)}
+        for form in samples:
+            rows[form] = parity_table(pick(samples[form]), exact, we.M)
+        rows["direct_s"] = time.perf_counter() - t0
+        out["vs_exact"] = rows
     return out
 
 
@@ -584,6 +598,7 @@ class ClockSampler:
 # CPU legs: the oracle (C restatement of the reference's loop) on host cores
 # ---------------------------------------------------------------------------
 CPU_TILE = 200          # the reference's tile side (settings.py:34)
+DIRECT_PIXELS = 256     # pixels of a view checked against exact arithmetic
 
 
 def oracle_kw(w, interior=False, eps_stat=0.):
@@ -622,6 +637,41 @@ def oracle_pixels(w, idx, kw, threads=None, fast=False):
            "sr": np.concatenate([r[2][0] for r in res]),
            "zn": Z[0], "dzndc": Z[-1]}
     return out
+
+
+def direct_pixels(w, idx, threads=None):
+    """Exact-arithmetic outputs at flat pixel indices ``idx`` of a power-2
+    workload: z -> z^2 + c iterated directly at the workload's digits (the
+    MPFR orbit of the host library, every z_i rounded to double), c the
+    pixel's point (the view centre + dx (x + i y)); stop_iter the first i
+    with |z_i| > M (max_iter and stop reason 0 when there is none), zn = z_i,
+    dzndc per unit of dx from the double recurrence d' = 2 z d + 1 along the
+    exact orbit (linear: no chaotic growth of its rounding)."""
+    import mpmath
+    from fractalshades_gb300.mpmath_utils import FP_loop as fsFP
+    threads = threads or oracle_threads()
+    with mpmath.workdps(w.dps):
+        prec = mpmath.mp.prec
+        dx = mpmath.mpf(w.dx)
+        cs = [w.center + dx * mpmath.mpc(float(w.xs[k % w.nx]), float(w.ys[k // w.nx]))
+              for k in idx]
+        pts = [(mpmath.nstr(c.real, w.dps + 5), mpmath.nstr(c.imag, w.dps + 5)) for c in cs]
+    fdx = float(dx)
+
+    def one(pt):
+        buf = np.zeros(w.max_iter + 1, dtype=np.complex128)
+        i = int(fsFP.perturbation_mandelbrot_FP_loop(buf, False, w.max_iter, w.M, pt[0], pt[1],
+                                                     prec)[0])
+        n = min(i, w.max_iter)
+        d = 0j
+        for z in buf[:n]:
+            d = 2. * z * d + 1.
+        return (n, 1 if i <= w.max_iter else 0, buf[n], d * fdx)
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, pts))
+    return {"si": np.array([r[0] for r in res], dtype=np.int32),
+            "sr": np.array([r[1] for r in res], dtype=np.int8),
+            "zn": np.array([r[2] for r in res]), "dzndc": np.array([r[3] for r in res])}
 
 
 def potential_dem(zn, dzndc, n, M, d=2.):
