@@ -49,22 +49,35 @@ def test_alone_and_mixed_results_are_identical(centers):
 
 
 def test_results_match_a_single_tile_launch(centers):
-    """A served request equals the same tile launched directly with its own
-    reference (the bucketed derivative scale only rescales dzndc)."""
+    """A served request equals, bit for bit, the same tile launched directly
+    with a reference built the way the server builds its own: BLA radii from
+    kc rounded up to its bucket (TileServer.kc_bucket) and the derivative
+    paths at the bucketed scale 2^(e - 1), the tile's dzndc unit set with
+    fsg_tile.dzndc_scale_e."""
     from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import serving as srv
     from fractalshades_gb300 import synthetic as syn
+    from fractalshades_gb300.numpy_utils import xrange as fsx
     import mpmath
     req = _requests(centers)[1]
     got = _run(centers, [req], n_slots=1)[req.rid].result
     cen = centers[req.center]
-    with mpmath.workdps(cen.dps):
-        dx = mpmath.mpf(req.dx)
-        view = cen.c + mpmath.mpc(*req.offset) * dx
     w = syn.prepare_m2(p=cen.p, dps=cen.dps, dx=req.dx, nx=req.side, max_iter=req.max_iter,
                        center=cen.c, offset=req.offset)
+    with mpmath.workdps(cen.dps):
+        dx = mpmath.mpf(req.dx)
+        half = dx / 2
+        shift = -mpmath.mpc(*req.offset) * dx
+        kc = max(abs(shift - mpmath.mpc(sx * half, sy * half))
+                 for sx in (1, -1) for sy in (1, -1)) * mpmath.mpf(1.1)
+    kc_b = srv.TileServer.kc_bucket(fsx.mpf_to_Xrange(kc))
     ctx = nat.Context(0)
-    ref = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order, xr_paths=w.xr_mode,
-                        calc_dzndc=True, scale_m=w.dx_m, scale_e=w.dx_e, bla=True, kc=w.kc)
+    has_xr = cen.xr_idx.size > 0
+    ref = nat.Reference(ctx, cen.Zn, div_iter=req.max_iter + 1, order=cen.p,
+                        xr_idx=cen.xr_idx if has_xr else None,
+                        xr_m=cen.xr_m if has_xr else None, xr_e=cen.xr_e if has_xr else None,
+                        xr_paths=w.xr_mode, calc_dzndc=True, scale_m=0.5, scale_e=1, bla=True,
+                        kc=kc_b)
     n = req.side ** 2
     Z = np.zeros((2, n), dtype=np.complex128)
     U = np.zeros(n, dtype=np.int32)
@@ -72,16 +85,17 @@ def test_results_match_a_single_tile_launch(centers):
     si = np.zeros(n, dtype=np.int32)
     t = nat.make_tile(xs=w.xs, ys=w.ys, lin_mat=np.array([[1., -0.], [0., 1.]]), Z=Z, U=U,
                       stop_reason=sr, stop_iter=si, ref=ref, dx_m=w.dx_m, dx_e=w.dx_e,
-                      drift_m=w.drift_m, drift_e=w.drift_e, i_dzndc=1)
+                      drift_m=w.drift_m, drift_e=w.drift_e, i_dzndc=1,
+                      dzndc_scale_e=w.dx_e - 1)
     ctx.perturb_tiles(nat.make_calc(max_iter=req.max_iter, M_divergence=1000., mode="fe32",
                                     calc_dzndc=True, bla=True, xr_semantics=w.xr_mode), [t])
     ref.free()
     ctx.close()
-    # the BLA radii of the served request use kc rounded up to a power of two
-    assert np.mean(got["stop_iter"] == si) >= 0.99
-    same = got["stop_iter"] == si
-    np.testing.assert_allclose(got["Z"][0][same], Z[0][same], rtol=1e-5, atol=1e-12)
-    np.testing.assert_allclose(np.abs(got["Z"][1][same]), np.abs(Z[1][same]), rtol=1e-4)
+    # the server's rescale of dzndc from the bucket scale to dx
+    Z.view(np.float64).reshape(2, n, 2)[1] *= 2.0 * w.dx_m
+    np.testing.assert_array_equal(got["stop_iter"], si)
+    np.testing.assert_array_equal(got["stop_reason"], sr)
+    assert np.array_equal(got["Z"].view(np.uint8), Z.view(np.uint8))
 
 
 def test_hbm_budget_admission(centers):
