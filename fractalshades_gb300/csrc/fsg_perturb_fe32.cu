@@ -10,21 +10,27 @@
 // dc = cm * 2^Ec (cm normalised).  cu = cm * 2^(Ec - E) is kept with E.
 //
 // Two step kinds:
-//   * fast step, when |dz|_inf < 2^-26 |Z|_inf (almost every step of a deep
-//     zoom): dz^2 and dz * dzndc are below FP32 resolution against 2 Z dz and
-//     Z dzndc, so  u' = 2 Z u + cu  and  v' = 2 (Z v + 2^k D u)  with
-//     k = De + E - F -- plain FP32 FMAs on the orbit's float copy;
-//   * exact step otherwise (Z tiny or zero, rebases, escapes): every operation
-//     in fe arithmetic (fsg_num.cuh), and the reference's tests in their exact
-//     form: the componentwise rebase test on the double values (with
-//     to_standard()'s underflow), then -- following the Xrange branch -- the
-//     extended |Z + dz|^2 <= |dz|^2 confirmation.
+//   * FP32 step, whenever Z_w and dz are normal floats (2^-100 .. 2^100, the
+//     plain value of dz above 2^-126 unless |dz| < 2^-26 |Z|): in dz's frame
+//     u' = u (2 Z + dz) + cu and v' = 2 (Z + dz) v + 2^k D u (k = De + E - F);
+//     while |dz| < 2^-26 |Z| (one exponent compare) the dz terms are below
+//     FP32 resolution and the step is u' = 2 Z u + cu.  Consecutive FP32 steps
+//     run until the next event (BLA attempt, max_iter, divergence rebase, wrap)
+//     or a test FP32 cannot decide;
+//   * exact step otherwise (Z tiny or zero, dz out of float range): every
+//     operation in fe arithmetic (fsg_num.cuh).
+// Tests: escape and the componentwise rebase test in FP32 with a margin for
+// the rounding of Z and dz; within the margin, the reference's exact form --
+// the componentwise test on the double values (with to_standard()'s
+// underflow), then, following the Xrange branch, the extended
+// |Z + dz|^2 <= |dz|^2 confirmation.
 // The BLA validity test |dz| < r is |u|^2 < r^2 2^(-2E) in FP32 with the
 // exponent gap clamped (to_standard(dz), which the reference compares, is 0
-// only below every r > 0), in double at near-ties.  Runs of consecutive BLA
-// steps (each on the largest admissible stage) are applied as one composite
-// step where the composite's radius admits dz (fsg_ref.cu, k_fe_bla_chain):
-// the same iterations, the same decisions, one step.
+// only below every r > 0), in float-float against r's double value at
+// near-ties.  Runs of consecutive BLA steps (each on the largest admissible
+// stage) are applied as one composite step where the composite's radius
+// admits dz (fsg_ref.cu, k_fe_bla_chain): the same iterations, the same
+// decisions, one step.
 #include "fsg_internal.cuh"
 
 // 2^k as a float for k in [-126, 127]; 0 below; k > 127 is clamped (callers
@@ -130,24 +136,54 @@ __device__ __forceinline__ void deriv_fast(float &x, float &y, int &e, int4 Dv, 
     renorm_v(x, y, e);
 }
 
-// |q 2^G + Q|^2 < eps^2 (eps2 a normal float): both terms aligned on the
-// larger exponent e, then compared against eps^2 2^(-2e) with the gap clamped
-__device__ __forceinline__ bool stationary_fast(float qx, float qy, int G, int4 Q, float eps2) {
+// (x^2 + y^2) 2^(2e) < tm 2^te: the float sum of squares against the
+// threshold eps^2 = tm 2^te, held as tm in [1, 2] (rounded up from the double:
+// no float lies strictly between the two) and an int exponent; decided
+// exactly on exponents and mantissas, as fe_abs2_lt's double compare is
+__device__ __forceinline__ bool abs2_below(float x, float y, int e, float tm, int te) {
+    float m2 = fmaf(x, x, y * y);
+    if (m2 == 0.f) return true;
+    int em = fexp(m2);
+    if (em == -127) { m2 *= 0x1p64f; em = fexp(m2) - 64; }       // subnormal sum
+    const float mm = __int_as_float((__float_as_int(m2) & 0x007fffff) | 0x3f800000);
+    const int L = em + 2 * e;
+    return L < te || (L == te && mm < tm);
+}
+
+// |q 2^G + Q|^2 < eps^2: both terms aligned on the larger exponent e
+__device__ __forceinline__ bool stationary_fast(float qx, float qy, int G, int4 Q, float tm,
+                                                int te) {
     const int e = max(G, Q.z);
     const float a = __int_as_float((max(G - e, -127) + 127) << 23);
     const float b = __int_as_float((max(Q.z - e, -127) + 127) << 23);
     const float x = fmaf(qx, a, __int_as_float(Q.x) * b), y = fmaf(qy, a, __int_as_float(Q.y) * b);
-    const int d = min(max(-2 * e, -126), 126);
-    return fmaf(x, x, y * y) < eps2 * __int_as_float((d + 127) << 23);
+    return abs2_below(x, y, e, tm, te);
 }
 
-// The BLA validity test at a near-tie, in double (ref_BLA_get,
-// perturbation.py:2116-2170): |to_standard(dz)| < r with the entry's double
-// radius (taken in ~1 of 10^5 lookups).
-static __device__ __forceinline__ bool bla_ok_double(const double *rbla, int idx, float ux,
-                                                  float uy, int E) {
-    const double2 d = fe_to_d(fe_make(ux, uy, E));
-    return hypot(d.x, d.y) < __ldg(&rbla[idx]);
+// The operands of a rare double test pass through an empty volatile asm
+// inside the test's branch: the compiler cannot evaluate the double
+// arithmetic that depends on them ahead of the branch.
+__device__ __forceinline__ void opaque(float &a, float &b, int &c, int &d) {
+    asm volatile("" : "+f"(a), "+f"(b), "+r"(c), "+r"(d));
+}
+
+// The BLA validity test at a near-tie (ref_BLA_get, perturbation.py:
+// 2116-2170, |to_standard(dz)| < r with the entry's double radius) in
+// float-float arithmetic: |u|^2 < (rm + rl)^2 2^d with r = (rm + rl) 2^re,
+// d = 2 (re - E) in (-126, 126), both sides to ~2^-46 (Dekker products, a
+// two-sum; the differences of the high parts are exact near a tie).  It
+// takes the double test's decision except where |dz| and r agree to ~2^-46
+// (the double test rounds at 2^-53), with no double arithmetic in the loop:
+// a double form here raised the kernel's register use past its limit of 72.
+// Taken in ~1 of 10^5 lookups.
+__device__ __forceinline__ bool bla_ok_tie(float ux, float uy, float rm, float rl, int d) {
+    const float a = ux * ux, ae = fmaf(ux, ux, -a);
+    const float b = uy * uy, be = fmaf(uy, uy, -b);
+    const float sh = a + b, bv = sh - a, sl = ((a - (sh - bv)) + (b - bv)) + (ae + be);
+    const float sc = __int_as_float((d + 127) << 23);
+    const float r2 = rm * rm;
+    const float ch = r2 * sc, cl = (fmaf(rm, rm, -r2) + 2.f * rm * rl) * sc;
+    return (sh - ch) + (sl - cl) < 0.f;
 }
 
 // |dz| < r in FP32 for a header H = {r mantissa bits, r exponent, ...}
@@ -157,19 +193,21 @@ __device__ __forceinline__ bool bla_ok_plain(const Lane &s, int4 H) {
     return fmaf(s.ux, s.ux, s.uy * s.uy) < (rm * rm) * __int_as_float((d + 127) << 23);
 }
 
-// |dz| < r for BLA entry idx whose header is H = {r mantissa bits, r
-// exponent, A exponent, B exponent}, as |u|^2 < rm^2 2^(2 (re - E)).  u is
-// normalised (|u| in [2^-30, 2^31) or 0), so exponent gaps beyond +-126 are
-// decided by the clamp alone; r = 0 (rm = 0) admits nothing, dz = 0 any
-// r > 0 -- the reference's strict 0 < r.  Within 2^-18 of a tie (the FP32
-// radius and |u|^2 carry ~2^-23 of rounding) the double test decides.
-__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H, const double *rbla, int idx) {
+// |dz| < r for BLA entry idx of table T (records of 3 int4, header H = {r
+// mantissa bits, r exponent, A exponent, B exponent}), as |u|^2 < rm^2
+// 2^(2 (re - E)).  u is normalised (|u| in [2^-30, 2^31) or 0), so exponent
+// gaps beyond +-126 are decided by the clamp alone; r = 0 (rm = 0) admits
+// nothing, dz = 0 any r > 0 -- the reference's strict 0 < r.  Within 2^-18
+// of a tie (the FP32 radius and |u|^2 carry ~2^-23 of rounding) the
+// float-float test decides.
+__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H, const int4 *__restrict__ T,
+                                       int idx) {
     const int d = min(max(2 * (H.y - s.E), -126), 126);
     const float rm = __int_as_float(H.x);
     const float lhs = fmaf(s.ux, s.ux, s.uy * s.uy);
     const float rhs = (rm * rm) * __int_as_float((d + 127) << 23);
     if (fabsf(lhs - rhs) <= 0x1p-18f * rhs && d > -126 && d < 126)
-        return bla_ok_double(rbla, idx, s.ux, s.uy, s.E);
+        return bla_ok_tie(s.ux, s.uy, rm, __int_as_float(__ldg(&T[3 * idx + 2]).x), d);
     return lhs < rhs;
 }
 
@@ -182,8 +220,8 @@ __device__ __forceinline__ bool bla_ok(const Lane &s, int4 H, const double *rbla
 // stage does: after the first candidate the search tests stage 3, then the
 // stages between.
 __device__ __forceinline__ int bla_find(const int4 *__restrict__ T, const int4 *__restrict__ FF,
-                                        const int *__restrict__ FS, const double *rbla,
-                                        const Lane &s, int w, int4 &H, int4 &P) {
+                                        const int *__restrict__ FS, const Lane &s, int w,
+                                        int4 &H, int4 &P) {
     const int it = w >> FSG_STG_COMPRESSED;
     const int st = __ldg(&FS[it]);
     H = __ldg(&FF[2 * it]);
@@ -191,16 +229,16 @@ __device__ __forceinline__ int bla_find(const int4 *__restrict__ T, const int4 *
     if (st == 0) return 0;
     const int i0 = 2 * it;
     // BLA_index(i, stg) = 2 i + 2^stg - 1 over the stored stages (stg - 3)
-    if (bla_ok(s, H, rbla, i0 + (st >> FSG_STG_COMPRESSED) - 1)) return st;
+    if (bla_ok(s, H, T, i0 + (st >> FSG_STG_COMPRESSED) - 1)) return st;
     if (st == 8) return 0;
-    const int4 H3 = __ldg(&T[2 * i0]);
-    if (!bla_ok(s, H3, rbla, i0)) return 0;
+    const int4 H3 = __ldg(&T[3 * i0]);
+    if (!bla_ok(s, H3, T, i0)) return 0;
     for (int stg = 30 - __clz(st); stg > FSG_STG_COMPRESSED; stg--) {
         const int idx = i0 + (1 << (stg - FSG_STG_COMPRESSED)) - 1;
-        H = __ldg(&T[2 * idx]);
-        if (bla_ok(s, H, rbla, idx)) { P = __ldg(&T[2 * idx + 1]); return 1 << stg; }
+        H = __ldg(&T[3 * idx]);
+        if (bla_ok(s, H, T, idx)) { P = __ldg(&T[3 * idx + 1]); return 1 << stg; }
     }
-    H = H3; P = __ldg(&T[2 * i0 + 1]);
+    H = H3; P = __ldg(&T[3 * i0 + 1]);
     return 1 << FSG_STG_COMPRESSED;
 }
 
@@ -239,8 +277,12 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
     const long long np = (long long)T.nx * T.ny;
     const bool dzndz_on = INTERIOR, dzndc_on = C.calc_dzndc;
     // the fast interior test needs eps^2 as a normal float
-    const float eps2f = (float)C.eps2;
-    const bool eps_fast = C.eps2 >= 1e-30 && C.eps2 <= 1e30;
+    // eps^2 = tm 2^te for the integer-exponent interior test (any finite
+    // eps^2 > 0; else the double test)
+    const bool eps_fast = C.eps2 > 0. && C.eps2 < INFINITY;
+    int te = 0;
+    const float tm = eps_fast ? __double2float_ru(2. * frexp(C.eps2, &te)) : 0.f;
+    te -= 1;
     const int xrsem = C.xrsem, max_iter = C.max_iter;
     const int order = R.order, div_iter = R.div_iter, first_invalid = R.first_invalid;
     const bool bla_on = C.bla && R.bla_first != nullptr;
@@ -280,7 +322,7 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
         // continue saw w < div_iter - 1, or a BLA jump stopped short of it)
         if (bla_on && (w & 7) == 0 && w < first_invalid) {
             int4 H, P;
-            int step = bla_find(bla_f, bla_first, bla_first_step, R.rbla, s, w, H, P);
+            int step = bla_find(bla_f, bla_first, bla_first_step, s, w, H, P);
             // when the first candidate is taken, the run of first candidates
             // from here, composed (its radius is at most 0.9 of the first
             // candidate's and carries that margin: no tie test)
@@ -386,7 +428,7 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
                 Zc = Zn; Dv = Dn; Qv = Qn;
                 if (INTERIOR) {
                     // (:1224-1246) against the next reference derivative
-                    bool st = eps_fast ? stationary_fast(s.qx, s.qy, s.G, Qn, eps2f)
+                    bool st = eps_fast ? stationary_fast(s.qx, s.qy, s.G, Qn, tm, te)
                                        : fe_abs2_lt(fe_add(as_fe(s.qx, s.qy, s.G),
                                                            fe_make(__int_as_float(Qn.x),
                                                                    __int_as_float(Qn.y), Qn.z)),
@@ -463,7 +505,10 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
         if (dzndz_on) {
             int k = nullify ? 0 : ((n == order) ? R.len : w);
             fe ZdZ = fe_add(as_fe(s.qx, s.qy, s.G), ld_fe(R.dZndz_f, k));
-            if (fe_abs2_lt(ZdZ, C.eps2)) { stop = 2; break; }
+            if (eps_fast ? abs2_below(ZdZ.x, ZdZ.y, ZdZ.e, tm, te) : fe_abs2_lt(ZdZ, C.eps2)) {
+                stop = 2;
+                break;
+            }
         }
         Zc = __ldg(&Zp[w]);
         if (w < div_iter - 1) {
@@ -515,7 +560,12 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
                 if (ax > tau || ay > tau) dec = 0;
                 else if (ax < -tau && ay < -tau) dec = 1;
             }
-            if (dec == 2) dec = rebase_test_double(dz, R.Zn, w);
+            if (dec == 2) {
+                fe d = dz;
+                int wv = w;
+                opaque(d.x, d.y, d.e, wv);
+                dec = rebase_test_double(d, R.Zn, wv);
+            }
             dyn = dec == 1;
             if (dyn) {
                 fe ZZ = fe_add(dz, Zn);
