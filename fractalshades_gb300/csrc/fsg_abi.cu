@@ -700,7 +700,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
         if (d->calc_dzndc) RA(dzndc_f, len + 1);
         if (d->calc_dzndz) RA(dzndz_f, len + 2);
         if (R.bla_len > 0) {
-            RA(bla_f, 3 * (size_t)R.bla_len);
+            RA(bla_f, 2 * (size_t)R.bla_len);
             RA(bla_first, 2 * (size_t)bla_nit);
             RA(bla_first_step, (size_t)bla_nit);
             RA(bla_chain, 2 * (size_t)bla_nit);
@@ -809,7 +809,7 @@ int fsg_ref_derive_bla(fsg_ctx *ctx, fsg_ref *base, double kc, double bla_eps, f
         if (Mbs) RCK(cudaMemsetAsync(Mbs, 0, 128 * (size_t)L, s), "zero BLA");
         R.bla_len = 2 * L;
         if (R.flavor == 0 && R.nexp == 0) {
-            RA(bla_f, 3 * (size_t)R.bla_len);
+            RA(bla_f, 2 * (size_t)R.bla_len);
             RA(bla_first, 2 * (size_t)R.bla_nit);
             RA(bla_first_step, (size_t)R.bla_nit);
             RA(bla_chain, 2 * (size_t)R.bla_nit);

@@ -44,10 +44,10 @@ struct RefDev {
                                 // outside [2^-100, 2^100], 1 if Z is exactly 0}
     const int4 *dZndc_f;        // [len + 1]
     const int4 *dZndz_f;        // [len + 2]
-    const int4 *bla_f;          // [3 bla_len] per entry i: [3i] = {r mantissa bits,
-                                // r exponent, A exponent, B exponent},
-                                // [3i + 1] = {A.x, A.y, B.x, B.y} float bits,
-                                // [3i + 2] = {low part of r's mantissa, 0, 0, 0}
+    const int4 *bla_f;          // [2 bla_len] per entry i: [2i] = {r mantissa bits
+                                // (rounded down with a 2^-20 margin), r exponent,
+                                // A exponent, B exponent},
+                                // [2i + 1] = {A.x, A.y, B.x, B.y} float bits
     const int4 *bla_first;      // [2 bla_nit] per start index it = w / 8, the first
                                 // stage ref_BLA_get tries there: its bla_f record
     const int *bla_first_step;  // [bla_nit] that stage's step, 0 when none is tried

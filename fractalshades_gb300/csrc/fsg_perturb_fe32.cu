@@ -26,8 +26,8 @@
 // |Z + dz|^2 <= |dz|^2 confirmation.
 // The BLA validity test |dz| < r is |u|^2 < r^2 2^(-2E) in FP32 with the
 // exponent gap clamped (to_standard(dz), which the reference compares, is 0
-// only below every r > 0), in float-float against r's double value at
-// near-ties.  Runs of consecutive BLA steps (each on the largest admissible
+// only below every r > 0), against the FP64 radius rounded down with a
+// margin that covers the test's rounding: never a step beyond the radius.  Runs of consecutive BLA steps (each on the largest admissible
 // stage) are applied as one composite step where the composite's radius
 // admits dz (fsg_ref.cu, k_fe_bla_chain): the same iterations, the same
 // decisions, one step.
@@ -167,48 +167,21 @@ __device__ __forceinline__ void opaque(float &a, float &b, int &c, int &d) {
     asm volatile("" : "+f"(a), "+f"(b), "+r"(c), "+r"(d));
 }
 
-// The BLA validity test at a near-tie (ref_BLA_get, perturbation.py:
-// 2116-2170, |to_standard(dz)| < r with the entry's double radius) in
-// float-float arithmetic: |u|^2 < (rm + rl)^2 2^d with r = (rm + rl) 2^re,
-// d = 2 (re - E) in (-126, 126), both sides to ~2^-46 (Dekker products, a
-// two-sum; the differences of the high parts are exact near a tie).  It
-// takes the double test's decision except where |dz| and r agree to ~2^-46
-// (the double test rounds at 2^-53), with no double arithmetic in the loop:
-// a double form here raised the kernel's register use past its limit of 72.
-// Taken in ~1 of 10^5 lookups.
-__device__ __forceinline__ bool bla_ok_tie(float ux, float uy, float rm, float rl, int d) {
-    const float a = ux * ux, ae = fmaf(ux, ux, -a);
-    const float b = uy * uy, be = fmaf(uy, uy, -b);
-    const float sh = a + b, bv = sh - a, sl = ((a - (sh - bv)) + (b - bv)) + (ae + be);
-    const float sc = __int_as_float((d + 127) << 23);
-    const float r2 = rm * rm;
-    const float ch = r2 * sc, cl = (fmaf(rm, rm, -r2) + 2.f * rm * rl) * sc;
-    return (sh - ch) + (sl - cl) < 0.f;
-}
-
-// |dz| < r in FP32 for a header H = {r mantissa bits, r exponent, ...}
-__device__ __forceinline__ bool bla_ok_plain(const Lane &s, int4 H) {
+// |dz| < r for a BLA header H = {r mantissa bits, r exponent, A exponent,
+// B exponent}, as |u|^2 < rm^2 2^(2 (re - E)) in FP32.  u is normalised
+// (|u| in [2^-30, 2^31) or 0), so exponent gaps beyond +-126 are decided by
+// the clamp alone; r = 0 (rm = 0) admits nothing, dz = 0 any r > 0 -- the
+// reference's strict 0 < r.  The table's rm is the FP64 radius rounded down
+// with a 2^-20 margin (fsg_ref.cu, k_fe_bla): the test passes only where
+// |dz| < r holds exactly, so no step goes beyond the FP64 radius; within
+// 2^-19 of it (about 1 lookup in 10^5) the step is declined and the
+// iterations run as full steps.  (An exact decision at those near-ties, in
+// float-float or in double, cost 7 % of the headline: rare code in the
+// lookup lengthened the loop.)
+__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H) {
     const int d = min(max(2 * (H.y - s.E), -126), 126);
     const float rm = __int_as_float(H.x);
     return fmaf(s.ux, s.ux, s.uy * s.uy) < (rm * rm) * __int_as_float((d + 127) << 23);
-}
-
-// |dz| < r for BLA entry idx of table T (records of 3 int4, header H = {r
-// mantissa bits, r exponent, A exponent, B exponent}), as |u|^2 < rm^2
-// 2^(2 (re - E)).  u is normalised (|u| in [2^-30, 2^31) or 0), so exponent
-// gaps beyond +-126 are decided by the clamp alone; r = 0 (rm = 0) admits
-// nothing, dz = 0 any r > 0 -- the reference's strict 0 < r.  Within 2^-18
-// of a tie (the FP32 radius and |u|^2 carry ~2^-23 of rounding) the
-// float-float test decides.
-__device__ __forceinline__ bool bla_ok(const Lane &s, int4 H, const int4 *__restrict__ T,
-                                       int idx) {
-    const int d = min(max(2 * (H.y - s.E), -126), 126);
-    const float rm = __int_as_float(H.x);
-    const float lhs = fmaf(s.ux, s.ux, s.uy * s.uy);
-    const float rhs = (rm * rm) * __int_as_float((d + 127) << 23);
-    if (fabsf(lhs - rhs) <= 0x1p-18f * rhs && d > -126 && d < 126)
-        return bla_ok_tie(s.ux, s.uy, rm, __int_as_float(__ldg(&T[3 * idx + 2]).x), d);
-    return lhs < rhs;
 }
 
 // ref_BLA_get (perturbation.py:2116-2170): the largest stage from
@@ -229,16 +202,16 @@ __device__ __forceinline__ int bla_find(const int4 *__restrict__ T, const int4 *
     if (st == 0) return 0;
     const int i0 = 2 * it;
     // BLA_index(i, stg) = 2 i + 2^stg - 1 over the stored stages (stg - 3)
-    if (bla_ok(s, H, T, i0 + (st >> FSG_STG_COMPRESSED) - 1)) return st;
+    if (bla_ok(s, H)) return st;
     if (st == 8) return 0;
-    const int4 H3 = __ldg(&T[3 * i0]);
-    if (!bla_ok(s, H3, T, i0)) return 0;
+    const int4 H3 = __ldg(&T[2 * i0]);
+    if (!bla_ok(s, H3)) return 0;
     for (int stg = 30 - __clz(st); stg > FSG_STG_COMPRESSED; stg--) {
         const int idx = i0 + (1 << (stg - FSG_STG_COMPRESSED)) - 1;
-        H = __ldg(&T[3 * idx]);
-        if (bla_ok(s, H, T, idx)) { P = __ldg(&T[3 * idx + 1]); return 1 << stg; }
+        H = __ldg(&T[2 * idx]);
+        if (bla_ok(s, H)) { P = __ldg(&T[2 * idx + 1]); return 1 << stg; }
     }
-    H = H3; P = __ldg(&T[3 * i0 + 1]);
+    H = H3; P = __ldg(&T[2 * i0 + 1]);
     return 1 << FSG_STG_COMPRESSED;
 }
 
@@ -325,12 +298,12 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
             int step = bla_find(bla_f, bla_first, bla_first_step, s, w, H, P);
             // when the first candidate is taken, the run of first candidates
             // from here, composed (its radius is at most 0.9 of the first
-            // candidate's and carries that margin: no tie test)
+            // candidate's: the margin covers the FP32 test's rounding)
             if (step != 0 && step == __ldg(&bla_first_step[w >> FSG_STG_COMPRESSED])) {
                 const int2 cs = __ldg(&bla_chain_step[w >> FSG_STG_COMPRESSED]);
                 if (cs.y >= 2) {
                     const int4 Hc = __ldg(&bla_chain[2 * (w >> FSG_STG_COMPRESSED)]);
-                    if (bla_ok_plain(s, Hc)) {
+                    if (bla_ok(s, Hc)) {
                         H = Hc;
                         P = __ldg(&bla_chain[2 * (w >> FSG_STG_COMPRESSED) + 1]);
                         step = cs.x;

@@ -473,17 +473,22 @@ __global__ void k_fe_bla(const double2 *M, const double *r, int n, int4 *F) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     fe a = fe_norm(fe_from_d(M[2 * i])), b = fe_norm(fe_from_d(M[2 * i + 1]));
-    // r as (mantissa in [1, 2), exponent); r = 0 -> exponent FE_ZERO_E; the
-    // low part rl = r 2^-e - rm for the near-tie test (0 outside the range
-    // where the scaling is exact)
+    // r as (mantissa, exponent e); r = 0 -> mantissa 0, exponent FE_ZERO_E.
+    // The mantissa is r 2^-e (1 - 2^-20) rounded down: with it the kernel's
+    // FP32 test |u|^2 < rm^2 2^(2 (e - E)) (two roundings of at most 2^-23 on
+    // the left, one of 2^-24 on the right) holds only where |dz| < r holds
+    // exactly -- no BLA step beyond the FP64 radius; within 2^-19 of it the
+    // step is declined and the iterations run as full steps
     fe rf = fe_norm(fe_from_d(cx(r[i], 0.)));
-    float rl = 0.f;
-    if (rf.e != FE_ZERO_E && rf.e >= -1021 && rf.e <= 1021)
-        rl = (float)(r[i] * pow2d(-rf.e) - (double)rf.x);
-    F[3 * i] = make_int4(__float_as_int(rf.x), rf.e, a.e, b.e);
-    F[3 * i + 1] = make_int4(__float_as_int(a.x), __float_as_int(a.y), __float_as_int(b.x),
+    float rm = 0.f;
+    if (rf.e != FE_ZERO_E) {
+        const double rr = (rf.e >= -1021 && rf.e <= 1021)
+                              ? r[i] * pow2d(-rf.e) : (double)rf.x;
+        rm = __double2float_rd(rr * (1. - 0x1p-20));
+    }
+    F[2 * i] = make_int4(__float_as_int(rm), rf.e, a.e, b.e);
+    F[2 * i + 1] = make_int4(__float_as_int(a.x), __float_as_int(a.y), __float_as_int(b.x),
                              __float_as_int(b.y));
-    F[3 * i + 2] = make_int4(__float_as_int(rl), 0, 0, 0);
 }
 
 // the first stage ref_BLA_get (perturbation.py:2116-2170) tries at each start
@@ -504,7 +509,7 @@ __global__ void k_fe_bla_first(const RefDev *Rp, const int4 *F, int nit, int4 *F
         top = min(top, 31 - __clz(inv - 1));
         if (top >= 3) {
             const int idx = 2 * it + (1 << (top - 3)) - 1;
-            if (idx < R.bla_len) { h = F[3 * idx]; p = F[3 * idx + 1]; step = 1 << top; }
+            if (idx < R.bla_len) { h = F[2 * idx]; p = F[2 * idx + 1]; step = 1 << top; }
         }
     }
     FF[2 * it] = h; FF[2 * it + 1] = p; FS[it] = step;
