@@ -49,6 +49,11 @@ void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
+// Streamed copy-back of host-buffer calls (run_tiles): at most this many
+// launch segments, each of at least this many pixels
+#define FSG_COPY_SEGMENTS 4
+#define FSG_COPY_SEGMENT_PIXELS (1LL << 20)
+
 struct ServeState;   // the serving queue (fsg_serve_open), below
 
 struct fsg_ctx {
@@ -65,6 +70,10 @@ struct fsg_ctx {
     unsigned long long *counter_dev = nullptr;
     unsigned long long *stats_dev = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_desc = nullptr;
+    // streamed copy-back of host-buffer calls: a copy stream and one event
+    // per launch segment
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_seg[FSG_COPY_SEGMENTS] = {};
     bool timed = false;
     int64_t last_pixels = 0;
     // tile descriptors: pinned staging + device copy
@@ -245,6 +254,14 @@ TileDev make_tile(const fsg_tile &t) {
     return d;
 }
 
+// A launch over the pixels [base, end) of its tiles; `first` uploads the
+// descriptors and resets the launch's statistics, status and budget, `last`
+// closes its timing (a streamed call launches several segments in a row).
+struct Segment {
+    long long base, end;
+    bool first, last;
+};
+
 // The launch resources of one stream: the context's own, or a serving slot's
 struct LaunchRes {
     cudaStream_t stream;
@@ -256,30 +273,41 @@ struct LaunchRes {
     cudaEvent_t ev0, ev1;      // kernel timing (nullptr: none)
 };
 
-// Launch the iteration kernel over ntiles device-resident tiles on L.stream.
-int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const TileDev *tiles,
-              int ntiles, bool perturb) {
-    // the descriptor staging buffer is reused: wait for the previous upload
-    if (L.ev_desc) CK(cudaEventSynchronize(L.ev_desc), "cudaEventSynchronize(descriptor upload)");
+long long tiles_pixels(const TileDev *tiles, int ntiles) {
     long long total = 0;
-    L.start_host[0] = 0;
-    for (int i = 0; i < ntiles; i++) {
-        L.tiles_host[i] = tiles[i];
-        total += (long long)tiles[i].nx * tiles[i].ny;
-        L.start_host[i + 1] = total;
-    }
+    for (int i = 0; i < ntiles; i++) total += (long long)tiles[i].nx * tiles[i].ny;
+    return total;
+}
+
+// Launch the iteration kernel over the pixels [seg.base, seg.end) of ntiles
+// device-resident tiles on L.stream.
+int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const TileDev *tiles,
+              int ntiles, bool perturb, const Segment &seg) {
     cudaStream_t s = L.stream;
-    CK(cudaMemcpyAsync(L.tiles_dev, L.tiles_host, sizeof(TileDev) * ntiles,
-                       cudaMemcpyHostToDevice, s), "copy tile descriptors");
-    CK(cudaMemcpyAsync(L.start_dev, L.start_host, sizeof(long long) * (ntiles + 1),
-                       cudaMemcpyHostToDevice, s), "copy tile offsets");
-    if (L.ev_desc) CK(cudaEventRecord(L.ev_desc, s), "cudaEventRecord");
+    if (seg.first) {
+        // the descriptor staging buffer is reused: wait for the previous upload
+        if (L.ev_desc)
+            CK(cudaEventSynchronize(L.ev_desc), "cudaEventSynchronize(descriptor upload)");
+        long long total = 0;
+        L.start_host[0] = 0;
+        for (int i = 0; i < ntiles; i++) {
+            L.tiles_host[i] = tiles[i];
+            total += (long long)tiles[i].nx * tiles[i].ny;
+            L.start_host[i + 1] = total;
+        }
+        CK(cudaMemcpyAsync(L.tiles_dev, L.tiles_host, sizeof(TileDev) * ntiles,
+                           cudaMemcpyHostToDevice, s), "copy tile descriptors");
+        CK(cudaMemcpyAsync(L.start_dev, L.start_host, sizeof(long long) * (ntiles + 1),
+                           cudaMemcpyHostToDevice, s), "copy tile offsets");
+        if (L.ev_desc) CK(cudaEventRecord(L.ev_desc, s), "cudaEventRecord");
+        CK(cudaMemsetAsync(L.stats_dev, 0, 4 * sizeof(unsigned long long), s), "reset stats");
+        CK(cudaMemsetAsync(L.status_dev, 0, sizeof(int), s), "reset status");
+        CK(cudaMemsetAsync(L.used_dev, 0, sizeof(unsigned long long), s), "reset budget");
+    }
     CK(cudaMemsetAsync(L.counter_dev, 0, sizeof(unsigned long long), s), "reset counter");
-    CK(cudaMemsetAsync(L.stats_dev, 0, 4 * sizeof(unsigned long long), s), "reset stats");
-    CK(cudaMemsetAsync(L.status_dev, 0, sizeof(int), s), "reset status");
-    CK(cudaMemsetAsync(L.used_dev, 0, sizeof(unsigned long long), s), "reset budget");
     WorkDev W;
-    W.tiles = L.tiles_dev; W.start = L.start_dev; W.ntiles = ntiles; W.total = total;
+    W.tiles = L.tiles_dev; W.start = L.start_dev; W.ntiles = ntiles;
+    W.base = seg.base; W.total = seg.end;
     W.counter = L.counter_dev; W.stats = L.stats_dev;
     W.cancel = ctx->cancel_dev; W.status = L.status_dev;
     W.budget = (unsigned long long)calc->iter_budget; W.used = L.used_dev;
@@ -287,19 +315,20 @@ int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const Tile
     // one persistent wave at the kernel's occupancy limit, or the tuned shape
     const int block = calc->block > 0 ? calc->block : default_block(calc, perturb);
     const int grid = calc->ctas_per_sm > 0 ? -calc->ctas_per_sm : 0;
-    if (L.ev0) CK(cudaEventRecord(L.ev0, s), "cudaEventRecord");
+    if (L.ev0 && seg.first) CK(cudaEventRecord(L.ev0, s), "cudaEventRecord");
     if (!perturb) fsg_launch_std(W, C, grid, block, s);
     else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
     else if (calc->mode == FSG_MODE_FE32) fsg_launch_perturb_bs_fe32(W, C, grid, block, s);
     else fsg_launch_perturb(W, C, grid, block, s);
     CK(cudaGetLastError(), "kernel launch");
-    if (L.ev1) CK(cudaEventRecord(L.ev1, s), "cudaEventRecord");
+    if (L.ev1 && seg.last) CK(cudaEventRecord(L.ev1, s), "cudaEventRecord");
     return FSG_OK;
 }
 
-// Launch on the context's own stream, timed.
+// Launch on the context's own stream, timed (one segment: the whole launch
+// by default).
 int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int ntiles,
-                 bool perturb) {
+                 bool perturb, const Segment *segp = nullptr) {
     LaunchRes L;
     L.stream = ctx->stream;
     L.tiles_host = ctx->tiles_host; L.start_host = ctx->start_host;
@@ -307,11 +336,11 @@ int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int n
     L.counter_dev = ctx->counter_dev; L.stats_dev = ctx->stats_dev; L.used_dev = ctx->used_dev;
     L.status_dev = ctx->status_dev;
     L.ev_desc = ctx->ev_desc; L.ev0 = ctx->ev0; L.ev1 = ctx->ev1;
-    int rc = launch_on(ctx, L, calc, tiles, ntiles, perturb);
+    const long long total = tiles_pixels(tiles, ntiles);
+    const Segment whole = {0, total, true, true};
+    int rc = launch_on(ctx, L, calc, tiles, ntiles, perturb, segp ? *segp : whole);
     if (rc != FSG_OK) return rc;
     ctx->timed = true;
-    long long total = 0;
-    for (int i = 0; i < ntiles; i++) total += (long long)tiles[i].nx * tiles[i].ny;
     ctx->last_pixels = total;
     return FSG_OK;
 }
@@ -432,6 +461,51 @@ int copy_back(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     return FSG_OK;
 }
 
+// Copy the staged outputs of the pixels [p0, p1) of the concatenated tiles
+// back into the caller's host buffers, on stream s.
+int copy_back_range(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
+                    const TileDev *td, long long p0, long long p1, cudaStream_t s) {
+    const size_t zsz = zbytes(calc);
+    long long ts = 0;
+    for (int32_t i = 0; i < ntiles; i++) {
+        const fsg_tile &t = tiles[i];
+        const TileDev &d = td[i];
+        const long long np = (long long)t.nx * t.ny, te = ts + np;
+        const long long a = (p0 > ts ? p0 : ts) - ts, b = (p1 < te ? p1 : te) - ts;
+        ts = te;
+        if (a >= b) continue;
+        const size_t n = (size_t)(b - a);
+        for (int k = 0; k < t.nZ; k++) {
+            const size_t off = zsz * ((size_t)k * np + a);
+            CK(cudaMemcpyAsync((char *)t.Z + off, (const char *)d.Z + off, zsz * n,
+                               cudaMemcpyDeviceToHost, s), "copy Z back");
+        }
+        if (t.U) CK(cudaMemcpyAsync(t.U + a, d.U + a, 4 * n, cudaMemcpyDeviceToHost, s), "copy U back");
+        CK(cudaMemcpyAsync(t.stop_reason + a, d.stop_reason + a, n, cudaMemcpyDeviceToHost, s),
+           "copy stop_reason back");
+        CK(cudaMemcpyAsync(t.stop_iter + a, d.stop_iter + a, 4 * n, cudaMemcpyDeviceToHost, s),
+           "copy stop_iter back");
+        if (t.potential)
+            CK(cudaMemcpyAsync(t.potential + a, d.pot + a, 8 * n, cudaMemcpyDeviceToHost, s),
+               "copy potential back");
+        if (t.dem)
+            CK(cudaMemcpyAsync(t.dem + a, d.dem + a, 8 * n, cudaMemcpyDeviceToHost, s),
+               "copy dem back");
+    }
+    return FSG_OK;
+}
+
+// Segments of a streamed host-buffer call: a perturbation launch of at least
+// 2 FSG_COPY_SEGMENT_PIXELS pixels runs as up to FSG_COPY_SEGMENTS launches
+// over consecutive pixel ranges, each segment's outputs copied back on the
+// copy stream while the next one computes.
+int copy_segments(bool perturb, long long total) {
+    if (!perturb) return 1;
+    long long k = total / FSG_COPY_SEGMENT_PIXELS;
+    if (k < 2) return 1;
+    return k > FSG_COPY_SEGMENTS ? FSG_COPY_SEGMENTS : (int)k;
+}
+
 int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t ntiles,
               int32_t where, bool perturb) {
     if (!ctx) return FSG_ERR_ARG;
@@ -460,6 +534,37 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     if (rc != FSG_OK) return rc;
     rc = stage_tiles(ctx, calc, tiles, ntiles, ctx->scratch, ctx->stream, td.data());
     if (rc != FSG_OK) return rc;
+    const long long total = tiles_pixels(td.data(), ntiles);
+    const int nseg = copy_segments(perturb, total);
+    if (nseg > 1) {
+        // streamed: segment k computes on the context stream while the
+        // outputs of segment k - 1 travel back on the copy stream.  An
+        // interruption during the call may leave the outputs of the segments
+        // that finished before it written (the reference's loop also writes
+        // its arrays in place; it discards an interrupted tile).
+        // Every segment is queued before the first copy: a copy into pageable
+        // memory returns only once done, and the launches keep the GPU busy
+        // meanwhile.
+        if (*ctx->cancel_host) return FSG_INTERRUPTED;
+        for (int k = 0; k < nseg; k++) {
+            const Segment seg = {total * k / nseg, total * (k + 1) / nseg, k == 0, k == nseg - 1};
+            rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb, &seg);
+            if (rc != FSG_OK) return rc;
+            CK(cudaEventRecord(ctx->ev_seg[k], ctx->stream), "cudaEventRecord(segment)");
+        }
+        for (int k = 0; k < nseg; k++) {
+            CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_seg[k], 0), "cudaStreamWaitEvent(segment)");
+            rc = copy_back_range(ctx, calc, tiles, ntiles, td.data(), total * k / nseg,
+                                 total * (k + 1) / nseg, ctx->copy_stream);
+            if (rc != FSG_OK) return rc;
+        }
+        // the context stream's later work (the next call's staging) waits
+        // for the copies out of the scratch area
+        CK(cudaEventRecord(ctx->ev_seg[nseg - 1], ctx->copy_stream), "cudaEventRecord(copies)");
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_seg[nseg - 1], 0), "cudaStreamWaitEvent(copies)");
+        CK(cudaStreamSynchronize(ctx->copy_stream), "cudaStreamSynchronize(copy stream)");
+        return fsg_sync(ctx);
+    }
     rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
     if (rc != FSG_OK) return rc;
     // an interrupted launch leaves the caller's arrays untouched (the
@@ -507,6 +612,13 @@ int fsg_ctx_create(int device, fsg_ctx **out) {
         if (cudaSetDevice(device) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
         cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
         if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
+        {
+            bool ok = true;
+            for (int k = 0; k < FSG_COPY_SEGMENTS && ok; k++)
+                ok = cudaEventCreateWithFlags(&ctx->ev_seg[k], cudaEventDisableTiming) == cudaSuccess;
+            if (!ok) { rc = FSG_ERR_CUDA; break; }
+        }
         ctx->stream = ctx->own_stream;
         int *h = nullptr;
         if (cudaHostAlloc((void **)&h, sizeof(int), cudaHostAllocMapped) != cudaSuccess) { rc = FSG_ERR_CUDA; break; }
@@ -548,6 +660,12 @@ int fsg_ctx_destroy(fsg_ctx *ctx) {
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev_desc) cudaEventDestroy(ctx->ev_desc);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    for (int k = 0; k < FSG_COPY_SEGMENTS; k++)
+        if (ctx->ev_seg[k]) cudaEventDestroy(ctx->ev_seg[k]);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return FSG_OK;
@@ -1131,7 +1249,8 @@ void serve_start(fsg_ctx *ctx, ServeState *S, int k, int64_t ticket, ServeReq &R
         L.status_dev = sl.status_dev;
         // the slot's staging is reused only after its request has retired
         L.ev_desc = nullptr; L.ev0 = nullptr; L.ev1 = nullptr;
-        rc = launch_on(ctx, L, &R.calc, R.td.data(), (int)R.td.size(), R.perturb);
+        const Segment whole = {0, tiles_pixels(R.td.data(), (int)R.td.size()), true, true};
+        rc = launch_on(ctx, L, &R.calc, R.td.data(), (int)R.td.size(), R.perturb, whole);
     }
     if (rc == FSG_OK) {
         e = cudaEventRecord(sl.done, sl.stream);

@@ -132,7 +132,8 @@ struct WorkDev {
     const TileDev *tiles;
     const long long *start;          // [ntiles + 1] prefix sums of pixel counts
     int ntiles;
-    long long total;
+    long long base;                  // pixels [base, total) of the concatenated tiles:
+    long long total;                 // one launch, or one segment of a streamed call
     unsigned long long *counter;
     unsigned long long *stats;       // [4]: pixel_iters, full_steps, bla_steps, rebases
     volatile int *cancel;            // mapped host flag
@@ -151,15 +152,15 @@ __device__ __forceinline__ bool fsg_claim(const WorkDev &W, const long long *s_s
         *W.status = 2;
         return false;
     }
-    unsigned long long g = atomicAdd(W.counter, 1ULL);
-    if ((long long)g >= W.total) return false;
+    const long long g = W.base + (long long)atomicAdd(W.counter, 1ULL);
+    if (g >= W.total) return false;
     int lo = 0, hi = W.ntiles - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (s_start[mid] <= (long long)g) lo = mid; else hi = mid - 1;
     }
     t = lo;
-    ip = (long long)g - s_start[lo];
+    ip = g - s_start[lo];
     return true;
 }
 

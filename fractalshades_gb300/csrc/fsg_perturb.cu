@@ -253,7 +253,7 @@ template __global__ void k_perturb_bs<xf, 0>(WorkDev W, CalcDev C);
 
 template <bool XR, bool MN, bool ORB>
 static void launch_m2(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    k_perturb_m2<XR, MN, ORB><<<fsg_auto_grid(k_perturb_m2<XR, MN, ORB>, grid, block, W.total),
+    k_perturb_m2<XR, MN, ORB><<<fsg_auto_grid(k_perturb_m2<XR, MN, ORB>, grid, block, W.total - W.base),
                                 block, 0, s>>>(W, C);
 }
 
@@ -268,10 +268,10 @@ static void launch_m2_orb(const WorkDev &W, const CalcDev &C, int grid, int bloc
 
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
     if (C.flavor != 0 && C.mode == 1)
-        k_perturb_bs<xf, 0><<<fsg_auto_grid(k_perturb_bs<xf, 0>, grid, block, W.total), block, 0,
+        k_perturb_bs<xf, 0><<<fsg_auto_grid(k_perturb_bs<xf, 0>, grid, block, W.total - W.base), block, 0,
                            s>>>(W, C);
     else if (C.flavor != 0)
-        k_perturb_bs<double, 0><<<fsg_auto_grid(k_perturb_bs<double, 0>, grid, block, W.total), block, 0,
+        k_perturb_bs<double, 0><<<fsg_auto_grid(k_perturb_bs<double, 0>, grid, block, W.total - W.base), block, 0,
                                s>>>(W, C);
     else if (C.backshift > 0)
         launch_m2_orb<true>(W, C, grid, block, s);

@@ -6,7 +6,7 @@
 
 template <int FL>
 static void launch_bs_fr(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    k_perturb_bs<fr, FL><<<fsg_auto_grid(k_perturb_bs<fr, FL>, grid, block, W.total), block, 0, s>>>(
+    k_perturb_bs<fr, FL><<<fsg_auto_grid(k_perturb_bs<fr, FL>, grid, block, W.total - W.base), block, 0, s>>>(
         W, C);
 }
 

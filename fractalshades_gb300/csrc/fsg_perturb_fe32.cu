@@ -622,9 +622,9 @@ void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int b
                              cudaStream_t s) {
     const int b = (block > 0 && block <= FE32_BLOCK) ? block : FE32_BLOCK;
     if (C.interior)
-        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, b, W.total), b, 0,
+        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, b, W.total - W.base), b, 0,
                                   s>>>(W, C);
     else
-        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, b, W.total), b, 0,
+        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, b, W.total - W.base), b, 0,
                                    s>>>(W, C);
 }

@@ -365,7 +365,7 @@ template <bool BS>
 __global__ void __launch_bounds__(256) k_std_epilogue(WorkDev W, CalcDev C) {
     __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
     fsg_load_starts(W, s_start);
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < W.total;
+    for (long long g = W.base + blockIdx.x * (long long)blockDim.x + threadIdx.x; g < W.total;
          g += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = W.ntiles - 1;
         while (lo < hi) {
@@ -394,16 +394,16 @@ __global__ void __launch_bounds__(256) k_std_epilogue(WorkDev W, CalcDev C) {
 template <bool OPT>
 static void launch_std(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
     if (C.flavor == 0 && C.nexp != 0)
-        k_std_mn<OPT><<<fsg_auto_grid(k_std_mn<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+        k_std_mn<OPT><<<fsg_auto_grid(k_std_mn<OPT>, grid, block, W.total - W.base), block, 0, s>>>(W, C);
     else if (C.flavor == 0)
-        k_std_m2<OPT><<<fsg_auto_grid(k_std_m2<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+        k_std_m2<OPT><<<fsg_auto_grid(k_std_m2<OPT>, grid, block, W.total - W.base), block, 0, s>>>(W, C);
     else
-        k_std_bs<OPT><<<fsg_auto_grid(k_std_bs<OPT>, grid, block, W.total), block, 0, s>>>(W, C);
+        k_std_bs<OPT><<<fsg_auto_grid(k_std_bs<OPT>, grid, block, W.total - W.base), block, 0, s>>>(W, C);
     if (C.flavor == 0)
-        k_std_epilogue<false><<<fsg_auto_grid(k_std_epilogue<false>, 0, 256, W.total), 256, 0, s>>>(
+        k_std_epilogue<false><<<fsg_auto_grid(k_std_epilogue<false>, 0, 256, W.total - W.base), 256, 0, s>>>(
             W, C);
     else
-        k_std_epilogue<true><<<fsg_auto_grid(k_std_epilogue<true>, 0, 256, W.total), 256, 0, s>>>(
+        k_std_epilogue<true><<<fsg_auto_grid(k_std_epilogue<true>, 0, 256, W.total - W.base), 256, 0, s>>>(
             W, C);
 }
 

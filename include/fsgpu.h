@@ -278,6 +278,16 @@ int fsg_ref_info(const fsg_ref *ref, int64_t *len, int64_t *bla_len, int32_t *st
 int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0,
                      void *out1);
 
+/* The iteration over the tiles (one launch of up to FSG_MAX_TILES_PER_LAUNCH
+ * tiles).  With FSG_HOST buffers the call returns once the outputs are in
+ * host memory; a perturbation call of at least 2^21 pixels then runs as up to
+ * four launches over consecutive pixel ranges, each range's outputs copied
+ * back while the next computes (outputs identical to one launch).  Returns
+ * FSG_OK, FSG_BUDGET (fsg_calc.iter_budget reached: the pixels not run keep
+ * stop_reason -1), FSG_INTERRUPTED (fsg_cancel; host buffers are left as
+ * they were, except that a streamed call interrupted while it runs may have
+ * written the ranges finished before -- the reference's loop writes its
+ * arrays in place too, and discards an interrupted tile), or an error. */
 int fsg_std_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
                   int32_t ntiles, int32_t where);
 int fsg_perturb_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,

@@ -221,3 +221,83 @@ def test_iteration_budget_and_resubmission(ctx, kind):
     assert np.array_equal(Z1.view(np.uint64), Zf.view(np.uint64))
     if ref is not None:
         ref.free()
+
+
+@pytest.mark.parametrize("mode", ["fe32", "fp64"])
+def test_streamed_host_call_equals_device_call(ctx, mode):
+    """A host-buffer perturbation call of more than 2^21 pixels runs as
+    consecutive launch segments whose outputs travel back while the next
+    segment computes: the caller's arrays equal, bit for bit, those of one
+    launch on device buffers; with an iteration budget the call returns
+    FSG_BUDGET, the segments after the budget ran out leave stop_reason -1,
+    and resubmitting those pixels completes the image exactly."""
+    import torch
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import synthetic as syn
+    w = syn.seahorse_workload(nx=1536, max_iter=1500)
+    n = w.nx * w.ny
+    ref = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order, calc_dzndc=True,
+                        scale_m=w.dx_m, scale_e=w.dx_e, bla=True, kc=w.kc, bla_eps=1e-6)
+    kw = dict(ref=ref, dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e,
+              i_dzndc=1)
+
+    def calc(budget=0):
+        return nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=mode, calc_dzndc=True,
+                             bla=True, iter_budget=budget)
+
+    def host(xs, ys, budget=0, pix=None):
+        m = pix.size if pix is not None else n
+        Z = np.zeros((2, m), dtype=np.complex128)
+        U = np.zeros(m, dtype=np.int32)
+        sr = -np.ones(m, dtype=np.int8)
+        si = np.zeros(m, dtype=np.int32)
+        pot, dem = np.zeros(m), np.zeros(m)
+        if pix is not None:
+            t = nat.make_tile(pix=pix, lin_mat=LIN, Z=Z, U=U, stop_reason=sr, stop_iter=si,
+                              potential=pot, dem=dem, **kw)
+        else:
+            t = nat.make_tile(xs=xs, ys=ys, lin_mat=LIN, Z=Z, U=U, stop_reason=sr,
+                              stop_iter=si, potential=pot, dem=dem, **kw)
+        rc = ctx.perturb_tiles(calc(budget), [t], nat.HOST)
+        return rc, {"Z": Z, "U": U, "sr": sr, "si": si, "pot": pot, "dem": dem}
+
+    dev = torch.device("cuda:0")
+    f64 = dict(dtype=torch.float64, device=dev)
+    xs, ys = torch.from_numpy(w.xs).to(dev), torch.from_numpy(w.ys).to(dev)
+    d = {"Z": torch.zeros((2, n, 2), **f64), "U": torch.zeros(n, dtype=torch.int32, device=dev),
+         "sr": torch.zeros(n, dtype=torch.int8, device=dev),
+         "si": torch.zeros(n, dtype=torch.int32, device=dev),
+         "pot": torch.zeros(n, **f64), "dem": torch.zeros(n, **f64)}
+    t = nat.make_tile_ptrs(nx=w.nx, ny=w.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
+                           lin_mat=LIN, Z_ptr=d["Z"].data_ptr(), nZ=2,
+                           stop_reason_ptr=d["sr"].data_ptr(), stop_iter_ptr=d["si"].data_ptr(),
+                           U_ptr=d["U"].data_ptr(), potential_ptr=d["pot"].data_ptr(),
+                           dem_ptr=d["dem"].data_ptr(), **kw)
+    assert ctx.perturb_tiles(calc(), [t], nat.DEVICE) == nat.FSG_OK
+    ctx.sync()
+    want = {k: v.cpu().numpy() for k, v in d.items()}
+    want["Z"] = want["Z"].view(np.complex128).reshape(2, n)
+    rc, got = host(w.xs, w.ys)
+    assert rc == nat.FSG_OK
+    for k in want:
+        assert np.array_equal(got[k].view(np.uint8), want[k].view(np.uint8)), k
+    # budget: a quarter of the image's iterations
+    budget = int(want["si"].astype(np.int64).sum() // 4)
+    rc, b = host(w.xs, w.ys, budget)
+    assert rc == nat.FSG_BUDGET
+    left = np.flatnonzero(b["sr"] == -1)
+    assert 0 < left.size < n and left[-1] == n - 1
+    pix = (np.asarray(w.xs)[None, :] + 1j * np.asarray(w.ys)[:, None]).ravel()[left]
+    rc, r = host(None, None, pix=np.ascontiguousarray(pix))
+    assert rc == nat.FSG_OK
+    done = b["sr"] != -1
+    for k in ("Z", "sr", "si"):
+        a = b[k].copy()
+        if k == "Z":
+            a[:, left] = r[k]
+            assert np.array_equal(a.view(np.uint8), want[k].view(np.uint8)), k
+        else:
+            a[left] = r[k]
+            assert np.array_equal(a, want[k]), k
+    assert done.sum() > 0
+    ref.free()
