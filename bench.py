@@ -1086,7 +1086,10 @@ def run_ours(args):
             "autotuned_over": [[e["block"], e["ctas_per_sm"], round(e["kernel_ms"], 3)]
                                for e in tuned["table"]]}),
         "e2e": {"value": e2e_val, "unit": "pixel-iter/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "path": "fsg_perturb_tiles with page-locked host buffers: the kernel reads "
+                        "the axes and writes every output in host memory (NVLink-C2C), "
+                        "timed from the call to its return"},
         "gpu_launches": int(args.steps),
         "roofline": {"bound": "fp32-fma", "achieved": achieved, "peak": peak32,
                      "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,

@@ -434,19 +434,35 @@ class Fractal:
 
     def _store_image(self, calc_name, res):
         """Whole-image raw arrays (image layout) -> per-chunk compressed
-        memory maps, every chunk marked done."""
+        memory maps, every chunk marked done.  The layout is the one
+        update_data_mmaps writes tile by tile; here each map is opened and
+        flushed once for the whole image."""
         ny, nx = self.ny, self.nx
-        Z = res["Z"].reshape(res["Z"].shape[0], ny, nx)
-        U = res["U"].reshape(res["U"].shape[0], ny, nx)
-        sr = res["stop_reason"].reshape(1, ny, nx)
-        si = res["stop_iter"].reshape(1, ny, nx)
+        state = self._calc_data[calc_name]["state"]
+        complex_codes, int_codes, _ = state.codes
+        f_complex, f_int, _ = self._calc_data[calc_name]["saved_codes"]
+        rows = {"Z": [complex_codes.index(c) for c in f_complex],
+                "U": [int_codes.index(c) for c in f_int],
+                "stop_reason": [0], "stop_iter": [0]}
+        src = {"Z": res["Z"].reshape(res["Z"].shape[0], ny, nx),
+               "U": res["U"].reshape(res["U"].shape[0], ny, nx),
+               "stop_reason": res["stop_reason"].reshape(1, ny, nx),
+               "stop_iter": res["stop_iter"].reshape(1, ny, nx)}
+        chunks = []
         for cs in self.chunk_slices():
-            ix, ixx, iy, iyy = cs
-            sl = (slice(None), slice(iy, iyy), slice(ix, ixx))
-            m = (ixx - ix) * (iyy - iy)
-            self.update_data_mmaps(calc_name, cs, Z[sl].reshape(-1, m), U[sl].reshape(-1, m),
-                                   sr[sl].reshape(1, m), si[sl].reshape(1, m))
-            self.update_report_mmap(calc_name, cs, None)
+            rank = self.chunk_rank(cs)
+            chunks.append((rank, self.compressed_beg_end(calc_name, rank), cs))
+        for key in self.SAVE_ARRS:
+            mmap = self.get_data_memmap(calc_name, key, mode="r+")
+            for _rank, (beg, end), (ix, ixx, iy, iyy) in chunks:
+                for field, r in enumerate(rows[key]):
+                    mmap[field, beg:end] = src[key][r, iy:iyy, ix:ixx].ravel()
+            mmap.flush()
+            del mmap
+        mmap = self.get_report_memmap(calc_name, mode="r+")
+        mmap[[c[0] for c in chunks], self.REPORT_ITEMS.index("done")] = 1
+        mmap.flush()
+        del mmap
 
     def get_raw(self, calc_name, key):
         """A raw field in image layout (ny, nx): a complex code (e.g. "zn"),

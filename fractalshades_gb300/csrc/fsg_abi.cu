@@ -495,6 +495,46 @@ int copy_back_range(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, i
     return FSG_OK;
 }
 
+// The device address of a page-locked host array (cudaHostAlloc,
+// cudaHostRegister), nullptr for pageable memory (or a null pointer).
+void *pinned_device_ptr(const void *p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Host-buffer tiles whose every array is page-locked, as device-addressable
+// descriptors in td: the kernels then read the inputs and write the outputs
+// in place (over NVLink-C2C on GB300, as the pixels finish), with no staging
+// and no copy-back.  False when any array is pageable.
+bool pinned_tiles(const fsg_tile *tiles, int32_t ntiles, TileDev *td) {
+    for (int32_t i = 0; i < ntiles; i++) {
+        fsg_tile t = tiles[i];
+        const void *in[3] = {t.pix, t.xs, t.ys};
+        void *out[6] = {t.Z, t.U, t.stop_reason, t.stop_iter, t.potential, t.dem};
+        void *din[3], *dout[6];
+        for (int q = 0; q < 3; q++) {
+            din[q] = pinned_device_ptr(in[q]);
+            if (in[q] && !din[q]) return false;
+        }
+        for (int q = 0; q < 6; q++) {
+            dout[q] = pinned_device_ptr(out[q]);
+            if (out[q] && !dout[q]) return false;
+        }
+        t.pix = (const double *)din[0]; t.xs = (const double *)din[1];
+        t.ys = (const double *)din[2];
+        t.Z = dout[0]; t.U = (int32_t *)dout[1]; t.stop_reason = (int8_t *)dout[2];
+        t.stop_iter = (int32_t *)dout[3]; t.potential = (double *)dout[4];
+        t.dem = (double *)dout[5];
+        td[i] = make_tile(t);
+    }
+    return true;
+}
+
 // Segments of a streamed host-buffer call: a perturbation launch of at least
 // 2 FSG_COPY_SEGMENT_PIXELS pixels runs as up to FSG_COPY_SEGMENTS launches
 // over consecutive pixel ranges, each segment's outputs copied back on the
@@ -529,7 +569,14 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
         return launch_tiles(ctx, calc, td.data(), ntiles, perturb);
     }
     if (where != FSG_HOST) return set_err(ctx, FSG_ERR_ARG, "where must be FSG_HOST or FSG_DEVICE");
-    // host buffers: stage in the grow-only device scratch area
+    if (pinned_tiles(tiles, ntiles, td.data())) {
+        // page-locked host buffers, written in place
+        if (*ctx->cancel_host) return FSG_INTERRUPTED;
+        rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
+        if (rc != FSG_OK) return rc;
+        return fsg_sync(ctx);
+    }
+    // pageable host buffers: stage in the grow-only device scratch area
     rc = ensure_scratch(ctx, staged_bytes(calc, tiles, ntiles));
     if (rc != FSG_OK) return rc;
     rc = stage_tiles(ctx, calc, tiles, ntiles, ctx->scratch, ctx->stream, td.data());

@@ -56,7 +56,8 @@ extern "C" {
                                         * inside int32 */
 
 /* where the tile buffers live */
-#define FSG_HOST 0       /* host pointers: the library stages the copies            */
+#define FSG_HOST 0       /* host pointers: page-locked arrays read and written in
+                            place, pageable ones staged by the library            */
 #define FSG_DEVICE 1     /* device pointers: asynchronous on the context stream     */
 
 typedef struct fsg_ctx fsg_ctx;
@@ -280,13 +281,20 @@ int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0,
 
 /* The iteration over the tiles (one launch of up to FSG_MAX_TILES_PER_LAUNCH
  * tiles).  With FSG_HOST buffers the call returns once the outputs are in
- * host memory; a perturbation call of at least 2^21 pixels then runs as up to
- * four launches over consecutive pixel ranges, each range's outputs copied
- * back while the next computes (outputs identical to one launch).  Returns
- * FSG_OK, FSG_BUDGET (fsg_calc.iter_budget reached: the pixels not run keep
- * stop_reason -1), FSG_INTERRUPTED (fsg_cancel; host buffers are left as
- * they were, except that a streamed call interrupted while it runs may have
- * written the ranges finished before -- the reference's loop writes its
+ * host memory:
+ *   - page-locked buffers (cudaHostAlloc, cudaHostRegister; every array of
+ *     every tile) are read and written in place by the kernels, as the
+ *     reference's loop writes its arrays: fields a kernel does not produce,
+ *     and pixels a budget leaves unrun, keep the caller's values;
+ *   - pageable buffers are staged on the device: fields the kernels do not
+ *     produce come back as zeros and unrun pixels with stop_reason -1; a
+ *     perturbation call of at least 2^21 pixels runs as up to four launches
+ *     over consecutive pixel ranges, each range's outputs copied back while
+ *     the next computes (outputs identical to one launch).
+ * Returns FSG_OK, FSG_BUDGET (fsg_calc.iter_budget reached), FSG_INTERRUPTED
+ * (fsg_cancel: host buffers are left as they were when the cancel came before
+ * the call; one that comes while the call runs may leave written the pixels,
+ * or the staged ranges, finished before it -- the reference's loop writes its
  * arrays in place too, and discards an interrupted tile), or an error. */
 int fsg_std_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles,
                   int32_t ntiles, int32_t where);

@@ -301,3 +301,68 @@ def test_streamed_host_call_equals_device_call(ctx, mode):
             assert np.array_equal(a, want[k]), k
     assert done.sum() > 0
     ref.free()
+
+
+@pytest.mark.parametrize("kind", ["std", "fe32", "fp64"])
+def test_pinned_host_buffers_written_in_place(ctx, kind):
+    """Page-locked host buffers are read and written in place by the kernels
+    (no staging, no copy-back): the outputs equal the staged (pageable) call's
+    bit for bit, and a Z row the kernel does not produce keeps the caller's
+    values, where the staged call returns zeros."""
+    import torch
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import synthetic as syn
+    w = syn.seahorse_workload(nx=256, max_iter=1500)
+    n = w.nx * w.ny
+    ref = None
+    if kind == "std":
+        calc = nat.make_calc(max_iter=1000, M_divergence=1000., epsilon_stationnary=0.01)
+        kw = dict(center=-0.5 + 0j, dx=3.0)
+        nZ, run, spare = 3, ctx.std_tiles, None
+    else:
+        ref = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order, calc_dzndc=True,
+                            scale_m=w.dx_m, scale_e=w.dx_e, bla=True, kc=w.kc, bla_eps=1e-6)
+        calc = nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=kind, calc_dzndc=True,
+                             bla=True)
+        kw = dict(ref=ref, dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e,
+                  i_dzndc=1)
+        nZ, run, spare = 3, ctx.perturb_tiles, 2          # row 2: no code writes it
+
+    def arrays(pin):
+        def mk(shape, dtype, fill):
+            if pin:
+                a = torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+            else:
+                a = np.empty(shape, dtype=torch.empty(0, dtype=dtype).numpy().dtype)
+            a[...] = fill
+            return a
+        Zf = mk((nZ, n, 2), torch.float64, 7.0)
+        d = {"Z": Zf.view(np.complex128).reshape(nZ, n),
+             "sr": mk(n, torch.int8, -1), "si": mk(n, torch.int32, 0),
+             "xs": mk(w.nx, torch.float64, 0.), "ys": mk(w.ny, torch.float64, 0.)}
+        d["xs"][:] = w.xs
+        d["ys"][:] = w.ys
+        if kind != "std":
+            d["pot"] = mk(n, torch.float64, 0.)
+            d["dem"] = mk(n, torch.float64, 0.)
+        return d
+
+    out = {}
+    for pin in (False, True):
+        d = arrays(pin)
+        extra = {} if kind == "std" else dict(potential=d["pot"], dem=d["dem"])
+        t = nat.make_tile(xs=d["xs"], ys=d["ys"], lin_mat=LIN, Z=d["Z"], stop_reason=d["sr"],
+                          stop_iter=d["si"], **kw, **extra)
+        assert run(calc, [t], nat.HOST) == nat.FSG_OK
+        out[pin] = d
+    a, b = out[False], out[True]
+    rows = [r for r in range(nZ) if r != spare]
+    assert np.array_equal(a["Z"][rows].view(np.uint64), b["Z"][rows].view(np.uint64))
+    for k in ("sr", "si", "pot", "dem"):
+        if k in a:
+            assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
+    if spare is not None:
+        assert np.all(a["Z"][spare] == 0)                 # staged: zeros
+        assert np.all(b["Z"][spare] == 7.0 + 7.0j)        # in place: the caller's values
+    if ref is not None:
+        ref.free()
