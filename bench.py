@@ -97,8 +97,9 @@ def serving_leg(n_requests, device):
     """The serving stream: Poisson arrivals at 200/s, tiles of 256..2048
     squared, widths log-uniform in [1e-1000, 1e-10] around 8 seeded period-p
     nuclei (1100 digits), max_iter 2e5, FP32+exp deltas, 120 GB HBM budget --
-    served in arrival order and shortest-expected-work first; then the first
-    300 requests under a 1 GB budget, where admission by HBM binds."""
+    served in arrival order, shortest-expected-work first and by highest
+    response ratio (shortest first, aged by waiting time); then the first 300
+    requests under a 1 GB budget, where admission by HBM binds."""
     from fractalshades_gb300 import serving as srv
     rng = np.random.default_rng(5)
     periods = [int(p) for p in rng.integers(300, 3001, 8)]
@@ -109,7 +110,7 @@ def serving_leg(n_requests, device):
            "sides": [256, 512, 1024, 2048], "widths": "1e-1000 .. 1e-10 log-uniform",
            "slots_rule": "as many as the budget holds 8 Mpixel batches, at most 4 (one "
                          "persistent launch fills the GPU)"}
-    for order in ("fifo", "shortest"):
+    for order in ("fifo", "shortest", "hrrn"):
         reqs = srv.request_stream(centers, n_requests, rate=200.0, seed=5)
         out[order] = _serve_once(srv, centers, reqs, 120 * 2 ** 30, order, device)
     reqs = srv.request_stream(centers, min(300, n_requests), rate=200.0, seed=5)

@@ -110,6 +110,7 @@ SYMBOLS = [
 
 FSG_SERVE_FIFO = 0
 FSG_SERVE_SHORTEST = 1
+FSG_SERVE_HRRN = 2
 FSG_PENDING = 3
 
 
@@ -236,7 +237,7 @@ class Context:
     # ------------------------------------------------------------------
     # serving queue (fsg_serve_open / fsg_submit / fsg_poll)
     def serve_open(self, hbm_budget, slots, order="fifo"):
-        o = {"fifo": FSG_SERVE_FIFO, "shortest": FSG_SERVE_SHORTEST}[order]
+        o = {"fifo": FSG_SERVE_FIFO, "shortest": FSG_SERVE_SHORTEST, "hrrn": FSG_SERVE_HRRN}[order]
         self._serve_keep = {}
         self.check(self.L.fsg_serve_open(self.h, int(hbm_budget), int(slots), o),
                    "fsg_serve_open")

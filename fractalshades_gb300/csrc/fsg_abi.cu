@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <chrono>
 #include <mutex>
 #include <new>
 #include <string>
@@ -1235,6 +1236,7 @@ struct ServeReq {
     std::vector<TileDev> td;
     bool perturb = false;
     double work = 0.;
+    double submitted = 0., started = 0.;   // steady-clock seconds
     size_t bytes = 0;
     int state = 0;                         // 0 queued, 1 running, 2 done
     int rc = FSG_OK;
@@ -1251,7 +1253,13 @@ struct ServeState {
     int64_t next = 1;
     int64_t reserved = 0, peak = 0;
     int64_t queued = 0, running = 0;
+    double rate = 0.;                      // expected work per second of a slot
 };
+
+double steady_seconds() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
 
 namespace {
 
@@ -1275,6 +1283,7 @@ void serve_free_slots(ServeState *S) {
 void serve_start(fsg_ctx *ctx, ServeState *S, int k, int64_t ticket, ServeReq &R) {
     ServeSlot &sl = S->slots[k];
     R.state = 1; R.slot = k; sl.ticket = ticket;
+    R.started = steady_seconds();
     S->queued--; S->running++;
     S->reserved += (int64_t)R.bytes;
     if (S->reserved > S->peak) S->peak = S->reserved;
@@ -1342,6 +1351,9 @@ void serve_retire(fsg_ctx *ctx, ServeState *S) {
         R.state = 2;
         R.rc = rc == FSG_OK ? launch_rc : rc;
         sl.ticket = -1;
+        // the work rate of one slot, averaged over the finished requests
+        const double dt = steady_seconds() - R.started;
+        if (dt > 0.) S->rate = S->rate == 0. ? R.work / dt : 0.8 * S->rate + 0.2 * R.work / dt;
     }
 }
 
@@ -1353,11 +1365,26 @@ void serve_admit(fsg_ctx *ctx, ServeState *S) {
         for (int i = 0; i < (int)S->slots.size(); i++)
             if (S->slots[i].ticket < 0) { k = i; break; }
         if (k < 0) return;
+        // FIFO: the oldest ticket; SHORTEST: the least expected work; HRRN:
+        // the highest response ratio (wait + S) / S, S = work / rate (the
+        // least work while no request has finished yet)
         int64_t best = -1;
+        double best_key = 0.;
+        const bool hrrn = S->order == FSG_SERVE_HRRN && S->rate > 0.;
+        const double now = hrrn ? steady_seconds() : 0.;
         for (auto &kv : S->reqs) {
             if (kv.second.state != 0) continue;
-            if (best < 0) { best = kv.first; if (S->order == FSG_SERVE_FIFO) break; continue; }
-            if (kv.second.work < S->reqs[best].work) best = kv.first;
+            double key = kv.second.work;
+            if (hrrn) {
+                const double sv = kv.second.work / S->rate;
+                key = -(now - kv.second.submitted + sv) / sv;
+            }
+            if (best < 0) {
+                best = kv.first; best_key = key;
+                if (S->order == FSG_SERVE_FIFO) break;
+                continue;
+            }
+            if (key < best_key) { best = kv.first; best_key = key; }
         }
         if (best < 0) return;
         ServeReq &R = S->reqs[best];
@@ -1375,8 +1402,9 @@ int fsg_serve_open(fsg_ctx *ctx, int64_t hbm_budget_bytes, int32_t slots, int32_
     if (ctx->serve) return set_err(ctx, FSG_ERR_ARG, "the serving queue is already open");
     if (hbm_budget_bytes <= 0 || slots <= 0 || slots > 64)
         return set_err(ctx, FSG_ERR_ARG, "serving: budget > 0 and 1 .. 64 slots");
-    if (order != FSG_SERVE_FIFO && order != FSG_SERVE_SHORTEST)
-        return set_err(ctx, FSG_ERR_ARG, "serving: order FSG_SERVE_FIFO or FSG_SERVE_SHORTEST");
+    if (order != FSG_SERVE_FIFO && order != FSG_SERVE_SHORTEST && order != FSG_SERVE_HRRN)
+        return set_err(ctx, FSG_ERR_ARG,
+                       "serving: order FSG_SERVE_FIFO, FSG_SERVE_SHORTEST or FSG_SERVE_HRRN");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     ServeState *S = new (std::nothrow) ServeState();
     if (!S) return set_err(ctx, FSG_ERR_NOMEM, "out of host memory");
@@ -1430,6 +1458,7 @@ int fsg_submit(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_
     long long px = 0;
     for (int32_t i = 0; i < ntiles; i++) px += (long long)tiles[i].nx * tiles[i].ny;
     R.work = expected_work > 0. ? expected_work : (double)px;
+    R.submitted = steady_seconds();
     R.bytes = bytes;
     S->queued++;
     serve_retire(ctx, S);

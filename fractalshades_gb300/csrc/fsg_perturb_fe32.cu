@@ -439,6 +439,23 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
             if (stat) { stop = 2; break; }
             if (esc) { stop = 1; break; }
             if (w >= order) w = 0;
+        } else if ((Zc.w & 1) && !dzndz_on && dyn && 2 * md0 + 4 < Ec - 26) {
+            // Z_w = 0 (the critical point, once per period of a cycle) with
+            // |dz|^2 < 2^-27 |dc| and the reference derivative nullified
+            // (dyn, after the rebase there): dz' = dz^2 + dc is dc to within
+            // 2^-27 of its modulus (below the FP32 rounding of the value),
+            // and dzndc' = 2 dz dzndc is one FP32 complex product on the
+            // exponents' sum -- the fe step below, in FP32
+            n += 1;
+            nfull++;
+            if (dzndc_on && s.F != FE_ZERO_E) {
+                const float vx = s.ux * s.vx - s.uy * s.vy, vy = s.ux * s.vy + s.uy * s.vx;
+                s.vx = vx; s.vy = vy; s.F = s.F + s.E + 1;
+                renorm_v(s.vx, s.vy, s.F);
+            }
+            s.ux = cmx; s.uy = cmy; s.E = Ec;
+            w += 1;
+            if (w >= order) w = 0;
         } else {
             n += 1;
             nfull++;

@@ -495,7 +495,10 @@ __global__ void k_fe_bla(const double2 *M, const double *r, int n, int4 *F) {
 // index it = w / 8: 3 + ctz(it) capped at stages - 1 (stages - 1 for it = 0),
 // lowered to the largest stage whose step is below first_invalid - w; its
 // bla_f record is copied beside it so that the kernel's first test needs one
-// load
+// load.  Where stage 3 has radius 0 no stage of the index admits any dz
+// (radii never grow with the stage, :2023-2024; 0 < r is strict): step 0, no
+// lookup -- at the orbit's critical point Z_0 = 0 (A = 2 Z_0 = 0, r = 0) the
+// search failed once per period
 __global__ void k_fe_bla_first(const RefDev *Rp, const int4 *F, int nit, int4 *FF, int *FS) {
     const RefDev &R = *Rp;
     int it = blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,7 +510,7 @@ __global__ void k_fe_bla_first(const RefDev *Rp, const int4 *F, int nit, int4 *F
         int top = R.stages - 1;
         if (it != 0) top = min(top, 3 + __ffs(it) - 1);
         top = min(top, 31 - __clz(inv - 1));
-        if (top >= 3) {
+        if (top >= 3 && 2 * it < R.bla_len && F[2 * (2 * it)].x != 0) {
             const int idx = 2 * it + (1 << (top - 3)) - 1;
             if (idx < R.bla_len) { h = F[2 * idx]; p = F[2 * idx + 1]; step = 1 << top; }
         }

@@ -102,7 +102,10 @@ class TileServer:
         max_batch_pixels, at most max_slots (one persistent launch already
         fills the GPU; more concurrent launches only fill the tails).
         order "fifo" admits by arrival, "shortest" the smallest expected work
-        first (``expected_work``)."""
+        first (``expected_work``), "hrrn" the highest response ratio
+        (wait + S) / S first, S the expected service time (expected work over
+        the work rate measured on finished batches): short requests first,
+        and a long one once it has waited about its own service time."""
         import torch
         self.torch = torch
         self.device = torch.device("cuda", device)
@@ -116,9 +119,10 @@ class TileServer:
         if n_slots is None:
             n_slots = max(1, min(int(max_slots),
                                  self.hbm_budget // (self.max_batch_pixels * BYTES_PER_PIXEL)))
-        if order not in ("fifo", "shortest"):
-            raise ValueError("order: 'fifo' or 'shortest'")
+        if order not in ("fifo", "shortest", "hrrn"):
+            raise ValueError("order: 'fifo', 'shortest' or 'hrrn'")
         self.order = order
+        self.work_rate = 0.0        # expected work per second of a batch, measured
         self.slots = [_Slot(torch, self.device, i) for i in range(n_slots)]
         # reference builds on a high-priority stream of their own: their
         # kernels are scheduled first as SMs free up, and launches wait for
@@ -256,6 +260,12 @@ class TileServer:
 
     def _finish(self, slot):
         now = time.perf_counter()
+        # the work rate of one slot, an average over the finished batches
+        work = sum(self.expected_work(r) for r in slot.batch)
+        dt = now - min(r.admitted for r in slot.batch)
+        if dt > 0:
+            rate = work / dt
+            self.work_rate = rate if self.work_rate == 0 else 0.8 * self.work_rate + 0.2 * rate
         for req in slot.batch:
             h = req._host
             si = h["si"].numpy()
@@ -279,9 +289,18 @@ class TileServer:
         p = max(self.centers[req.center].p, 2)
         return req.side * req.side * (req.max_iter / p) * (math.log2(p) + 10.)
 
+    def priority(self, req, now):
+        """Sort key of the admission order (smallest first)."""
+        if self.order == "hrrn" and self.work_rate > 0:
+            service = self.expected_work(req) / self.work_rate
+            return -(now - req.arrival + service) / service
+        return self.expected_work(req)
+
     def _admit(self, slot):
-        if self.order == "shortest" and len(self.pending) > 1:
-            self.pending = collections.deque(sorted(self.pending, key=self.expected_work))
+        if self.order in ("shortest", "hrrn") and len(self.pending) > 1:
+            now = time.perf_counter()
+            self.pending = collections.deque(
+                sorted(self.pending, key=lambda r: self.priority(r, now)))
         batch = []
         pixels = 0
         while self.pending:

@@ -327,7 +327,12 @@ int fsg_clear_cancel(fsg_ctx *ctx);
  *     free and its staged bytes fit in what the budget has left; the next one
  *     in `order` waits for that (FSG_SERVE_FIFO: arrival order;
  *     FSG_SERVE_SHORTEST: smallest expected_work first, the caller's estimate,
- *     e.g. pixels x expected iterations; <= 0 means the pixel count);
+ *     e.g. pixels x expected iterations; <= 0 means the pixel count;
+ *     FSG_SERVE_HRRN: highest response ratio (wait + S) / S first, S =
+ *     expected_work over the work rate of a slot measured on the finished
+ *     requests -- short requests first, a long one once it has waited about
+ *     its own service time; smallest expected_work first until a request
+ *     has finished);
  *     FSG_ERR_LIMIT for a request larger than the whole budget;
  *   fsg_poll: FSG_PENDING while queued or running; once finished, the
  *     request's outcome (FSG_OK, FSG_BUDGET, FSG_INTERRUPTED with the
@@ -339,6 +344,7 @@ int fsg_clear_cancel(fsg_ctx *ctx);
  * fsg_cancel interrupts running and later-admitted requests alike. */
 #define FSG_SERVE_FIFO 0
 #define FSG_SERVE_SHORTEST 1
+#define FSG_SERVE_HRRN 2
 #define FSG_PENDING 3          /* fsg_poll: the request is not finished yet    */
 typedef struct {
     int64_t queued, running;

@@ -4,7 +4,8 @@ the GPU: requests of host-buffer tiles overlap on several slots and each
 result equals the synchronous call's on the same tiles, bit for bit; the HBM
 budget bounds what is staged at once and refuses a request larger than
 itself; shortest-expected-work-first admission lets small requests overtake a
-large queued one; an interruption leaves the caller's arrays untouched.
+large queued one, and the response-ratio order lets a long-waiting one go
+first; an interruption leaves the caller's arrays untouched.
 """
 import time
 
@@ -172,6 +173,43 @@ def test_queue_shortest_first_overtakes(ctx, seahorse):
         assert order[0] == tickets[0]
         assert order.index(tickets[2]) < order.index(tickets[1])
         assert order.index(tickets[3]) < order.index(tickets[1])
+    finally:
+        ctx.serve_close()
+
+
+def test_queue_hrrn_ages_a_long_wait(ctx, seahorse):
+    """FSG_SERVE_HRRN: a queued request that has waited long against its own
+    expected service time goes before a shorter one that arrived late (the
+    shortest-first order would take the short one)."""
+    from fractalshades_gb300 import _native as nat
+    w, ref = seahorse
+    c = nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode="fp64", calc_dzndc=True,
+                      bla=True)
+    # the blocker's duration, from a synchronous call
+    tb, outb = _perturb_tile(nat, w, ref, 1024, (0., 0.))
+    t0 = time.perf_counter()
+    ctx.perturb_tiles(c, [tb])
+    dur = time.perf_counter() - t0
+    ctx.serve_open(1 << 32, slots=1, order="hrrn")
+    try:
+        keep = []
+        # a first request measures the work rate
+        t, out = _perturb_tile(nat, w, ref, 32, (0., 0.))
+        keep.append(out)
+        first = ctx.submit(c, [t], expected_work=1.0, keep=out)
+        _wait(ctx, [first])
+        tb, outb = _perturb_tile(nat, w, ref, 1024, (0., 0.))
+        tl, outl = _perturb_tile(nat, w, ref, 32, (0.5, 0.))
+        ts, outs = _perturb_tile(nat, w, ref, 32, (0., 0.5))
+        keep += [outb, outl, outs]
+        blocker = ctx.submit(c, [tb], expected_work=1.0, keep=outb)
+        long_ = ctx.submit(c, [tl], expected_work=2e-3, keep=outl)
+        time.sleep(0.75 * dur)
+        short = ctx.submit(c, [ts], expected_work=1e-3, keep=outs)
+        _, order = _wait(ctx, [blocker, long_, short])
+        # when the blocker retires, the long request has waited ~dur against
+        # twice the short one's service time, the short one ~dur / 4
+        assert order.index(long_) < order.index(short)
     finally:
         ctx.serve_close()
 
