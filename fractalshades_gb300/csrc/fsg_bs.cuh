@@ -13,6 +13,16 @@
 #pragma once
 #include "fsg_internal.cuh"
 
+// Whether ref_BLA_get can admit any dz at start index w >> 3: radii never
+// grow with the stage (combine_BLA, combine_BLA_BS: r <= r of the first child,
+// perturbation.py:2023-2024, 2104-2105) and 0 < r is strict, so a stage-3
+// radius of 0 -- at the orbit's critical point, where A = 2 Z = 0 -- rules
+// every stage out, and |dz| need not be computed for the search.
+__device__ __forceinline__ bool bla_possible(const RefDev &R, int w) {
+    const int i3 = 2 * (w >> FSG_STG_COMPRESSED);
+    return i3 < R.bla_len && __ldg(&R.rbla[i3]) > 0.;
+}
+
 // perturbation.py:2116-2170 ref_BLA_get: returns the step (0 if none) and the
 // table index of the accepted entry.
 __device__ __forceinline__ int bla_lookup(const RefDev &R, double abs_zn, int w, int &ib) {
@@ -210,11 +220,12 @@ FSG_DEV bool fr_below(const fr_mod &a, fr xn, fr yn, float rm, int re, double r)
 template <class T> struct BLAGet;
 template <> struct BLAGet<double> {
     static FSG_DEV int get(const RefDev &R, double xn, double yn, int w, int &ib) {
-        return bla_lookup(R, hypot(xn, yn), w, ib);
+        return bla_possible(R, w) ? bla_lookup(R, hypot(xn, yn), w, ib) : 0;
     }
 };
 template <> struct BLAGet<fr> {
     static FSG_DEV int get(const RefDev &R, fr xn, fr yn, int w, int &ib) {
+        if (!bla_possible(R, w)) return 0;
         int it = w >> FSG_STG_COMPRESSED;
         int stages = FSG_STG_COMPRESSED;
         for (int s = FSG_STG_COMPRESSED; s < R.stages; s++) {
@@ -247,7 +258,8 @@ FSG_DEV xf scale2(xf v, int k) { v.e += k; return v; }
 // below the double range, perturbation.py:1520-1527)
 template <> struct BLAGet<xf> {
     static FSG_DEV int get(const RefDev &R, xf xn, xf yn, int w, int &ib) {
-        return bla_lookup(R, hypot(xf_to_std(xn), xf_to_std(yn)), w, ib);
+        return bla_possible(R, w) ? bla_lookup(R, hypot(xf_to_std(xn), xf_to_std(yn)), w, ib)
+                                  : 0;
     }
 };
 
@@ -810,7 +822,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                 int4 fz = __ldg(&R.bs_fz[w]);
                 for (;;) {
                     if (C.bla && R.bla_len > 0 && (w & 7) == 0 &&
-                        (1 << FSG_STG_COMPRESSED) < R.first_invalid - w) {
+                        (1 << FSG_STG_COMPRESSED) < R.first_invalid - w && bla_possible(R, w)) {
                         int ib;
                         const int step = BLAGet<T>::get(R, fr_norm(Fm.ux, Fm.E),
                                                         fr_norm(Fm.uy, Fm.E), w, ib);
