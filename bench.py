@@ -369,11 +369,14 @@ def view_leg(ctx, nat, torch, dev, timed, we, wx, parity_pixels, seed, workload)
     idx_dev = torch.from_numpy(idx).to(dev)
     out = {"workload": workload, "pixels": n}
     samples = {}
-    forms = [("fe32", "std", we), ("fp64", "std", we)]
+    # fe32_longest: the same FE32 launch claiming its pixels longest first
+    # (fsg_calc.claim_order), timed beside the default order
+    forms = [("fe32", "std", we), ("fe32_longest", "std", we), ("fp64", "std", we)]
     if wx is not None:
         forms.append(("xr64", "xr", wx))
     for form, key, wk in forms:
-        mode = form if not (form == "fp64" and wk.xr_mode) else "xr64"
+        mode = "fe32" if form.startswith("fe32") else form
+        mode = mode if not (mode == "fp64" and wk.xr_mode) else "xr64"
         t = nat.make_tile_ptrs(nx=wk.nx, ny=wk.ny, xs_ptr=xs.data_ptr(), ys_ptr=ys.data_ptr(),
                                lin_mat=LIN, Z_ptr=Z.data_ptr(), nZ=2,
                                stop_reason_ptr=sr.data_ptr(), stop_iter_ptr=si.data_ptr(),
@@ -381,16 +384,24 @@ def view_leg(ctx, nat, torch, dev, timed, we, wx, parity_pixels, seed, workload)
                                drift_m=wk.drift_m, drift_e=wk.drift_e, i_dzndc=1,
                                potential_ptr=pot.data_ptr(), dem_ptr=dem.data_ptr())
         c = nat.make_calc(max_iter=wk.max_iter, M_divergence=wk.M, mode=mode, calc_dzndc=True,
-                          interior=False, bla=True, xr_semantics=bool(wk.xr_mode))
-        warm = 1 if form == "fe32" else 0
-        kms, st = timed(lambda: ctx.perturb_tiles(c, [t], nat.DEVICE), 3 if form == "fe32" else 1,
-                        warm)
-        samples[form] = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
+                          interior=False, bla=True, xr_semantics=bool(wk.xr_mode),
+                          claim_order="longest" if form == "fe32_longest" else "pixels")
+        fast = form.startswith("fe32")
+        kms, st = timed(lambda: ctx.perturb_tiles(c, [t], nat.DEVICE), 3 if fast else 1,
+                        1 if fast else 0)
+        g = gather_outputs(idx_dev, Z, si, sr, 1, pot, dem)
+        if form == "fe32_longest":
+            same = all(np.array_equal(np.asarray(g[k]).view(np.uint8),
+                                      np.asarray(samples["fe32"][k]).view(np.uint8)) for k in g)
+        else:
+            samples[form] = g
         srn = sr.cpu().numpy()
         out[form] = {"kernel_ms": kms, "value": st["pixel_iters"] / (kms * 1e-3),
                      "pixel_iters": int(st["pixel_iters"]), "full_steps": int(st["full_steps"]),
                      "bla_steps": int(st["bla_steps"]), "rebases": int(st["rebases"]),
                      "escaped_frac": float(np.mean(srn == 1))}
+        if form == "fe32_longest":
+            out[form]["outputs_equal_fe32_on_sample"] = bool(same)
     out["speedup_fe32_vs_fp64"] = out["fe32"]["value"] / out["fp64"]["value"]
     if "xr64" in out:
         out["speedup_fe32_vs_xr64"] = out["fe32"]["value"] / out["xr64"]["value"]

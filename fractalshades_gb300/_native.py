@@ -55,7 +55,7 @@ class Calc(ct.Structure):
         ("mode", I32), ("calc_dzndc", I32), ("interior", I32), ("bla", I32),
         ("flavor", I32), ("xr_semantics", I32), ("nexp", I32),
         ("backshift", I32), ("calc_d2zndc2", I32), ("block", I32), ("ctas_per_sm", I32),
-        ("iter_budget", I64),
+        ("iter_budget", I64), ("claim_order", I32),
     ]
 
 
@@ -111,6 +111,8 @@ SYMBOLS = [
 FSG_SERVE_FIFO = 0
 FSG_SERVE_SHORTEST = 1
 FSG_SERVE_HRRN = 2
+FSG_ORDER_PIXELS = 0
+FSG_ORDER_LONGEST = 1
 FSG_PENDING = 3
 
 
@@ -494,7 +496,7 @@ def make_tile_ptrs(*, nx, ny, xs_ptr, ys_ptr, lin_mat, Z_ptr, nZ, stop_reason_pt
 def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
               calc_dzndc=True, interior=False, bla=True, flavor=0, xr_semantics=False,
               nexp=0, backshift=0, calc_d2zndc2=False, block=0, ctas_per_sm=0,
-              iter_budget=0):
+              iter_budget=0, claim_order="pixels"):
     c = Calc()
     c.max_iter = int(max_iter)
     c.M_divergence = float(M_divergence)
@@ -511,4 +513,6 @@ def make_calc(*, max_iter, M_divergence, epsilon_stationnary=0.0, mode="fp64",
     c.block = int(block)
     c.ctas_per_sm = int(ctas_per_sm)
     c.iter_budget = int(iter_budget)
+    c.claim_order = {"pixels": FSG_ORDER_PIXELS, "longest": FSG_ORDER_LONGEST}[claim_order] \
+        if isinstance(claim_order, str) else int(claim_order)
     return c

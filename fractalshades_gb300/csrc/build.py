@@ -39,6 +39,7 @@ SOURCES = {
     "fsg_perturb_bs32.cu": [],
     "fsg_peak.cu": [],
     "fsg_noalloc.cu": [],
+    "fsg_lpt.cu": [],
     "fsg_postproc.cu": ["-fmad=false"],
     "fsg_abi.cu": [],
 }

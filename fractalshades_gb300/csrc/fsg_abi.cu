@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <algorithm>
 #include <chrono>
 #include <mutex>
 #include <new>
@@ -50,10 +51,21 @@ void fsg_build_bs_fr_bla(const double *Mbs, const double *rbla, int bla_len, int
 
 double fsg_launch_fma_peak(int fp64, int sm_count, void *out, cudaStream_t s);
 
+// launchers of fsg_lpt.cu (claim order, longest pixels first)
+int fsg_lpt_blocks_count(const int *nx, const int *ny, int ntiles);
+void fsg_lpt_prepare(const TileDev *tiles, const long long *start, int ntiles, int nblk,
+                     int *blk_start, unsigned *hist, unsigned *rep, cudaStream_t s);
+void fsg_lpt_order(const TileDev *tiles, const long long *start, int ntiles, int nblk,
+                   const int *blk_start, unsigned *hist, const unsigned *rep,
+                   unsigned char *bucket, unsigned *order, cudaStream_t s);
+
 // Streamed copy-back of host-buffer calls (run_tiles): at most this many
 // launch segments, each of at least this many pixels
 #define FSG_COPY_SEGMENTS 4
 #define FSG_COPY_SEGMENT_PIXELS (1LL << 20)
+// Claim order longest pixels first (fsg_lpt.cu) for perturbation launches of
+// at least this many pixels (and below 2^31: 32-bit pixel indices)
+#define FSG_LPT_MIN_PIXELS (1LL << 18)
 
 struct ServeState;   // the serving queue (fsg_serve_open), below
 
@@ -82,6 +94,8 @@ struct fsg_ctx {
     TileDev *tiles_dev = nullptr; long long *start_dev = nullptr;
     // grow-only device scratch for host-buffer calls
     char *scratch = nullptr; size_t scratch_size = 0;
+    // grow-only device scratch of the longest-first claim order
+    char *lpt = nullptr; size_t lpt_size = 0;
 };
 
 struct fsg_ref {
@@ -261,6 +275,9 @@ TileDev make_tile(const fsg_tile &t) {
 struct Segment {
     long long base, end;
     bool first, last;
+    bool uploaded;             // the caller uploaded the descriptors already
+    const unsigned *order;     // claim order (device), nullptr: pixel order
+    bool keep_time;            // first: reset the statistics but not the timing
 };
 
 // The launch resources of one stream: the context's own, or a serving slot's
@@ -282,25 +299,35 @@ long long tiles_pixels(const TileDev *tiles, int ntiles) {
 
 // Launch the iteration kernel over the pixels [seg.base, seg.end) of ntiles
 // device-resident tiles on L.stream.
+// Upload the tile descriptors and their pixel offsets to L's device copies.
+int upload_descriptors(fsg_ctx *ctx, const LaunchRes &L, const TileDev *tiles, int ntiles) {
+    cudaStream_t s = L.stream;
+    // the descriptor staging buffer is reused: wait for the previous upload
+    if (L.ev_desc)
+        CK(cudaEventSynchronize(L.ev_desc), "cudaEventSynchronize(descriptor upload)");
+    long long total = 0;
+    L.start_host[0] = 0;
+    for (int i = 0; i < ntiles; i++) {
+        L.tiles_host[i] = tiles[i];
+        total += (long long)tiles[i].nx * tiles[i].ny;
+        L.start_host[i + 1] = total;
+    }
+    CK(cudaMemcpyAsync(L.tiles_dev, L.tiles_host, sizeof(TileDev) * ntiles,
+                       cudaMemcpyHostToDevice, s), "copy tile descriptors");
+    CK(cudaMemcpyAsync(L.start_dev, L.start_host, sizeof(long long) * (ntiles + 1),
+                       cudaMemcpyHostToDevice, s), "copy tile offsets");
+    if (L.ev_desc) CK(cudaEventRecord(L.ev_desc, s), "cudaEventRecord");
+    return FSG_OK;
+}
+
 int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const TileDev *tiles,
               int ntiles, bool perturb, const Segment &seg) {
     cudaStream_t s = L.stream;
     if (seg.first) {
-        // the descriptor staging buffer is reused: wait for the previous upload
-        if (L.ev_desc)
-            CK(cudaEventSynchronize(L.ev_desc), "cudaEventSynchronize(descriptor upload)");
-        long long total = 0;
-        L.start_host[0] = 0;
-        for (int i = 0; i < ntiles; i++) {
-            L.tiles_host[i] = tiles[i];
-            total += (long long)tiles[i].nx * tiles[i].ny;
-            L.start_host[i + 1] = total;
+        if (!seg.uploaded) {
+            int rc = upload_descriptors(ctx, L, tiles, ntiles);
+            if (rc != FSG_OK) return rc;
         }
-        CK(cudaMemcpyAsync(L.tiles_dev, L.tiles_host, sizeof(TileDev) * ntiles,
-                           cudaMemcpyHostToDevice, s), "copy tile descriptors");
-        CK(cudaMemcpyAsync(L.start_dev, L.start_host, sizeof(long long) * (ntiles + 1),
-                           cudaMemcpyHostToDevice, s), "copy tile offsets");
-        if (L.ev_desc) CK(cudaEventRecord(L.ev_desc, s), "cudaEventRecord");
         CK(cudaMemsetAsync(L.stats_dev, 0, 4 * sizeof(unsigned long long), s), "reset stats");
         CK(cudaMemsetAsync(L.status_dev, 0, sizeof(int), s), "reset status");
         CK(cudaMemsetAsync(L.used_dev, 0, sizeof(unsigned long long), s), "reset budget");
@@ -308,7 +335,7 @@ int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const Tile
     CK(cudaMemsetAsync(L.counter_dev, 0, sizeof(unsigned long long), s), "reset counter");
     WorkDev W;
     W.tiles = L.tiles_dev; W.start = L.start_dev; W.ntiles = ntiles;
-    W.base = seg.base; W.total = seg.end;
+    W.base = seg.base; W.total = seg.end; W.order = seg.order;
     W.counter = L.counter_dev; W.stats = L.stats_dev;
     W.cancel = ctx->cancel_dev; W.status = L.status_dev;
     W.budget = (unsigned long long)calc->iter_budget; W.used = L.used_dev;
@@ -316,7 +343,7 @@ int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const Tile
     // one persistent wave at the kernel's occupancy limit, or the tuned shape
     const int block = calc->block > 0 ? calc->block : default_block(calc, perturb);
     const int grid = calc->ctas_per_sm > 0 ? -calc->ctas_per_sm : 0;
-    if (L.ev0 && seg.first) CK(cudaEventRecord(L.ev0, s), "cudaEventRecord");
+    if (L.ev0 && seg.first && !seg.keep_time) CK(cudaEventRecord(L.ev0, s), "cudaEventRecord");
     if (!perturb) fsg_launch_std(W, C, grid, block, s);
     else if (calc->flavor == 0 && calc->mode == FSG_MODE_FE32) fsg_launch_perturb_fe32(W, C, grid, block, s);
     else if (calc->mode == FSG_MODE_FE32) fsg_launch_perturb_bs_fe32(W, C, grid, block, s);
@@ -329,7 +356,7 @@ int launch_on(fsg_ctx *ctx, const LaunchRes &L, const fsg_calc *calc, const Tile
 // Launch on the context's own stream, timed (one segment: the whole launch
 // by default).
 int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int ntiles,
-                 bool perturb, const Segment *segp = nullptr) {
+                 bool perturb, const Segment *segp = nullptr, bool allow_lpt = true) {
     LaunchRes L;
     L.stream = ctx->stream;
     L.tiles_host = ctx->tiles_host; L.start_host = ctx->start_host;
@@ -338,8 +365,57 @@ int launch_tiles(fsg_ctx *ctx, const fsg_calc *calc, const TileDev *tiles, int n
     L.status_dev = ctx->status_dev;
     L.ev_desc = ctx->ev_desc; L.ev0 = ctx->ev0; L.ev1 = ctx->ev1;
     const long long total = tiles_pixels(tiles, ntiles);
-    const Segment whole = {0, total, true, true};
-    int rc = launch_on(ctx, L, calc, tiles, ntiles, perturb, segp ? *segp : whole);
+    int rc;
+    // (not with an iteration budget: its claims stop in claim order, and the
+    // pixels left are the caller's to submit again; not for buffers written
+    // in place, which keep the caller's values wherever no pixel finished)
+    if (allow_lpt && !segp && perturb && calc->claim_order == FSG_ORDER_LONGEST
+        && calc->iter_budget == 0 && total >= FSG_LPT_MIN_PIXELS && total < (1LL << 31)) {
+        // longest pixels first: a pre-pass over one pixel per 8 x 8 block
+        // with max_iter capped at max_iter / 8 (256 .. 4096 iterations), then
+        // every pixel in decreasing order of its block's count; the pre-pass
+        // counts in no statistic and no budget (the main pass resets them)
+        std::vector<int> nx(ntiles), ny(ntiles);
+        for (int i = 0; i < ntiles; i++) { nx[i] = tiles[i].nx; ny[i] = tiles[i].ny; }
+        const int nblk = fsg_lpt_blocks_count(nx.data(), ny.data(), ntiles);
+        const size_t need = align_up(sizeof(int) * (ntiles + 1)) + align_up(4 * 32)
+                            + align_up(4 * (size_t)nblk) + align_up((size_t)nblk)
+                            + align_up(4 * (size_t)total);
+        if (need > ctx->lpt_size) {
+            if (ctx->lpt) { cudaStreamSynchronize(ctx->stream); cudaFree(ctx->lpt); }
+            ctx->lpt = nullptr; ctx->lpt_size = 0;
+            if (cudaMalloc((void **)&ctx->lpt, need) != cudaSuccess) {
+                (void)cudaGetLastError();
+                return set_err(ctx, FSG_ERR_NOMEM, "claim-order scratch");
+            }
+            ctx->lpt_size = need;
+        }
+        char *p = ctx->lpt;
+        int *blk_start = (int *)p; p += align_up(sizeof(int) * (ntiles + 1));
+        unsigned *hist = (unsigned *)p; p += align_up(4 * 32);
+        unsigned *rep = (unsigned *)p; p += align_up(4 * (size_t)nblk);
+        unsigned char *bucket = (unsigned char *)p; p += align_up((size_t)nblk);
+        unsigned *order = (unsigned *)p;
+        rc = upload_descriptors(ctx, L, tiles, ntiles);
+        if (rc != FSG_OK) return rc;
+        fsg_lpt_prepare(L.tiles_dev, L.start_dev, ntiles, nblk, blk_start, hist, rep, L.stream);
+        CK(cudaGetLastError(), "claim order (representatives)");
+        fsg_calc pc = *calc;
+        pc.max_iter = std::min<int64_t>(calc->max_iter,
+                                        std::max<int64_t>(256, std::min<int64_t>(4096, calc->max_iter / 8)));
+        pc.iter_budget = 0;
+        const Segment pre = {0, nblk, true, false, true, rep, false};
+        rc = launch_on(ctx, L, &pc, tiles, ntiles, perturb, pre);
+        if (rc != FSG_OK) return rc;
+        fsg_lpt_order(L.tiles_dev, L.start_dev, ntiles, nblk, blk_start, hist, rep, bucket,
+                      order, L.stream);
+        CK(cudaGetLastError(), "claim order");
+        const Segment main = {0, total, true, true, true, order, true};
+        rc = launch_on(ctx, L, calc, tiles, ntiles, perturb, main);
+    } else {
+        const Segment whole = {0, total, true, true, false, nullptr};
+        rc = launch_on(ctx, L, calc, tiles, ntiles, perturb, segp ? *segp : whole);
+    }
     if (rc != FSG_OK) return rc;
     ctx->timed = true;
     ctx->last_pixels = total;
@@ -361,6 +437,8 @@ int check_calc_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, 
         return set_err(ctx, FSG_ERR_ARG, "the power-n model runs in FSG_MODE_FP64 or FSG_MODE_XR64");
     if (calc->backshift < 0) return set_err(ctx, FSG_ERR_ARG, "backshift must be >= 0");
     if (calc->iter_budget < 0) return set_err(ctx, FSG_ERR_ARG, "iter_budget must be >= 0");
+    if (calc->claim_order != FSG_ORDER_PIXELS && calc->claim_order != FSG_ORDER_LONGEST)
+        return set_err(ctx, FSG_ERR_ARG, "claim_order: FSG_ORDER_PIXELS or FSG_ORDER_LONGEST");
     if (calc->backshift > 0 && perturb && calc->mode == FSG_MODE_FE32)
         return set_err(ctx, FSG_ERR_ARG, "calc_orbit runs in FSG_MODE_FP64 or FSG_MODE_XR64");
     if (calc->calc_d2zndc2 && (perturb || calc->flavor != 0))
@@ -573,7 +651,7 @@ int run_tiles(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_t
     if (pinned_tiles(tiles, ntiles, td.data())) {
         // page-locked host buffers, written in place
         if (*ctx->cancel_host) return FSG_INTERRUPTED;
-        rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb);
+        rc = launch_tiles(ctx, calc, td.data(), ntiles, perturb, nullptr, false);
         if (rc != FSG_OK) return rc;
         return fsg_sync(ctx);
     }
@@ -696,6 +774,7 @@ int fsg_ctx_destroy(fsg_ctx *ctx) {
     if (ctx->serve) fsg_serve_close(ctx);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->lpt) cudaFree(ctx->lpt);
     if (ctx->status_dev) cudaFree(ctx->status_dev);
     if (ctx->used_dev) cudaFree(ctx->used_dev);
     if (ctx->counter_dev) cudaFree(ctx->counter_dev);

@@ -132,8 +132,9 @@ struct WorkDev {
     const TileDev *tiles;
     const long long *start;          // [ntiles + 1] prefix sums of pixel counts
     int ntiles;
-    long long base;                  // pixels [base, total) of the concatenated tiles:
-    long long total;                 // one launch, or one segment of a streamed call
+    long long base;                  // claims [base, total): the pixels of the concatenated
+    long long total;                 // tiles (one launch, or one segment of a streamed call),
+    const unsigned *order;           // or, with order, the pixels order[base .. total)
     unsigned long long *counter;
     unsigned long long *stats;       // [4]: pixel_iters, full_steps, bla_steps, rebases
     volatile int *cancel;            // mapped host flag
@@ -152,8 +153,9 @@ __device__ __forceinline__ bool fsg_claim(const WorkDev &W, const long long *s_s
         *W.status = 2;
         return false;
     }
-    const long long g = W.base + (long long)atomicAdd(W.counter, 1ULL);
+    long long g = W.base + (long long)atomicAdd(W.counter, 1ULL);
     if (g >= W.total) return false;
+    if (W.order) g = (long long)W.order[g];
     int lo = 0, hi = W.ntiles - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;

@@ -143,6 +143,7 @@ extern "C" int fsg_std_tiles_noalloc(const fsg_calc *calc, const fsg_tile *tiles
     if (cudaGetLastError() != cudaSuccess) return FSG_ERR_CUDA;
     WorkDev W;
     W.tiles = S->tiles; W.start = S->start; W.ntiles = ntiles; W.base = 0; W.total = total;
+    W.order = nullptr;
     W.counter = &S->counter; W.stats = S->stats;
     W.cancel = &S->cancel; W.status = &S->status;
     W.budget = 0ULL; W.used = nullptr;

@@ -142,7 +142,19 @@ typedef struct {
                                  call returns FSG_BUDGET -- submit those pixels
                                  again to finish.  No counterpart in the
                                  reference (it runs a tile to its end)         */
+    int32_t claim_order;      /* FSG_ORDER_PIXELS (0): pixels claimed in order;
+                                 FSG_ORDER_LONGEST (1): a perturbation launch of
+                                 2^18 pixels or more claims them longest first
+                                 (see fsg_perturb_tiles).  Outputs are the same;
+                                 longest first shortens the tail of views whose
+                                 iteration counts spread over decades (a view
+                                 straddling a minibrot's boundary: -10 %) and
+                                 costs its pre-pass on uniform ones (+1.5 % on
+                                 an all-interior one)                          */
 } fsg_calc;
+
+#define FSG_ORDER_PIXELS 0
+#define FSG_ORDER_LONGEST 1
 
 /* One tile: a rectangle of pixels with its own view and outputs. */
 typedef struct {
@@ -280,8 +292,13 @@ int fsg_ref_download(fsg_ctx *ctx, const fsg_ref *ref, int which, void *out0,
                      void *out1);
 
 /* The iteration over the tiles (one launch of up to FSG_MAX_TILES_PER_LAUNCH
- * tiles).  With FSG_HOST buffers the call returns once the outputs are in
- * host memory:
+ * tiles).  With fsg_calc.claim_order = FSG_ORDER_LONGEST, a perturbation
+ * launch of 2^18 pixels or more (without an iteration budget, buffers not
+ * written in place) claims its pixels longest first: a pre-pass iterates one
+ * pixel per 8 x 8 block with max_iter capped at max_iter / 8 (256 .. 4096),
+ * then every pixel is claimed in decreasing order of its block's count;
+ * outputs do not depend on the order.  With FSG_HOST buffers the call
+ * returns once the outputs are in host memory:
  *   - page-locked buffers (cudaHostAlloc, cudaHostRegister; every array of
  *     every tile) are read and written in place by the kernels, as the
  *     reference's loop writes its arrays: fields a kernel does not produce,

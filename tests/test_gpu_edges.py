@@ -366,3 +366,42 @@ def test_pinned_host_buffers_written_in_place(ctx, kind):
         assert np.all(b["Z"][spare] == 7.0 + 7.0j)        # in place: the caller's values
     if ref is not None:
         ref.free()
+
+
+@pytest.mark.parametrize("mode", ["fe32", "fp64"])
+def test_longest_first_claim_order(ctx, mode):
+    """With claim_order "longest", a perturbation launch of 2^18 pixels or
+    more claims its pixels longest first (a capped pre-pass over one pixel per
+    8 x 8 block, then every pixel by its block's count): the outputs equal,
+    bit for bit, those of the same image launched as row bands below that size
+    (claimed in pixel order), and the statistics count the image's iterations
+    once."""
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import synthetic as syn
+    w = syn.seahorse_workload(nx=640, max_iter=3000)
+    ny = 480
+    ys_all = np.ascontiguousarray(w.ys[(w.ny - ny) // 2:(w.ny - ny) // 2 + ny])
+    ref = nat.Reference(ctx, w.Zn, div_iter=w.div_iter, order=w.order, calc_dzndc=True,
+                        scale_m=w.dx_m, scale_e=w.dx_e, bla=True, kc=w.kc, bla_eps=1e-6)
+    calc = nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode=mode, calc_dzndc=True,
+                         bla=True, claim_order="longest")
+    kw = dict(ref=ref, dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m, drift_e=w.drift_e,
+              i_dzndc=1)
+
+    def run(ys):
+        n = w.nx * ys.size
+        o = {"Z": np.zeros((2, n), dtype=np.complex128), "sr": -np.ones(n, dtype=np.int8),
+             "si": np.zeros(n, dtype=np.int32), "pot": np.zeros(n), "dem": np.zeros(n)}
+        t = nat.make_tile(xs=w.xs, ys=ys, lin_mat=LIN, Z=o["Z"], stop_reason=o["sr"],
+                          stop_iter=o["si"], potential=o["pot"], dem=o["dem"], **kw)
+        assert ctx.perturb_tiles(calc, [t]) == nat.FSG_OK
+        return o, ctx.stats()
+
+    whole, st = run(ys_all)
+    assert w.nx * ny >= 2 ** 18
+    assert st["pixel_iters"] == int(whole["si"].astype(np.int64).sum())
+    bands = [run(np.ascontiguousarray(ys_all[k:k + 120]))[0] for k in range(0, ny, 120)]
+    for key in ("Z", "sr", "si", "pot", "dem"):
+        b = np.concatenate([o[key] for o in bands], axis=-1)
+        assert np.array_equal(whole[key].view(np.uint8), b.view(np.uint8)), key
+    ref.free()
