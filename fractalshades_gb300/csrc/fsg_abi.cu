@@ -1314,6 +1314,7 @@ struct ServeReq {
     std::vector<fsg_tile> tiles;
     std::vector<TileDev> td;
     bool perturb = false;
+    bool inplace = false;                  // page-locked buffers: no staging, no copy-back
     double work = 0.;
     double submitted = 0., started = 0.;   // steady-clock seconds
     size_t bytes = 0;
@@ -1367,10 +1368,13 @@ void serve_start(fsg_ctx *ctx, ServeState *S, int k, int64_t ticket, ServeReq &R
     S->reserved += (int64_t)R.bytes;
     if (S->reserved > S->peak) S->peak = S->reserved;
     int rc = FSG_OK;
-    cudaError_t e = cudaMallocAsync(&R.block, R.bytes, sl.stream);
-    if (e != cudaSuccess) rc = cuda_err(ctx, e, "cudaMallocAsync(request)");
+    cudaError_t e = cudaSuccess;
+    if (!R.inplace) {
+        e = cudaMallocAsync(&R.block, R.bytes, sl.stream);
+        if (e != cudaSuccess) rc = cuda_err(ctx, e, "cudaMallocAsync(request)");
+    }
     if (rc == FSG_OK) rc = wait_references(ctx, R.tiles.data(), (int32_t)R.tiles.size(), sl.stream);
-    if (rc == FSG_OK) {
+    if (rc == FSG_OK && !R.inplace) {
         R.td.resize(R.tiles.size());
         rc = stage_tiles(ctx, &R.calc, R.tiles.data(), (int32_t)R.tiles.size(), (char *)R.block,
                          sl.stream, R.td.data());
@@ -1415,7 +1419,7 @@ void serve_retire(fsg_ctx *ctx, ServeState *S) {
         if (e == cudaSuccess) e = cudaStreamSynchronize(sl.stream);
         if (e != cudaSuccess) rc = cuda_err(ctx, e, "read request status");
         const int launch_rc = st == 1 ? FSG_INTERRUPTED : (st == 2 ? FSG_BUDGET : FSG_OK);
-        if (rc == FSG_OK && launch_rc != FSG_INTERRUPTED) {
+        if (rc == FSG_OK && launch_rc != FSG_INTERRUPTED && !R.inplace) {
             rc = copy_back(ctx, &R.calc, R.tiles.data(), (int32_t)R.tiles.size(), R.td.data(),
                            sl.stream);
             if (rc == FSG_OK) {
@@ -1423,7 +1427,7 @@ void serve_retire(fsg_ctx *ctx, ServeState *S) {
                 if (e != cudaSuccess) rc = cuda_err(ctx, e, "copy request back");
             }
         }
-        cudaFreeAsync(R.block, sl.stream);
+        if (R.block) cudaFreeAsync(R.block, sl.stream);
         R.block = nullptr;
         S->reserved -= (int64_t)R.bytes;
         S->running--;
@@ -1525,7 +1529,10 @@ int fsg_submit(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_
             return set_err(ctx, FSG_ERR_ARG, "a request mixes perturbation and standard tiles");
     int rc = check_calc_tiles(ctx, calc, tiles, ntiles, perturb);
     if (rc != FSG_OK) return rc;
-    const size_t bytes = staged_bytes(calc, tiles, ntiles);
+    // page-locked buffers are written in place: nothing staged on the device
+    std::vector<TileDev> pinned_td(ntiles);
+    const bool inplace = pinned_tiles(tiles, ntiles, pinned_td.data());
+    const size_t bytes = inplace ? 0 : staged_bytes(calc, tiles, ntiles);
     std::lock_guard<std::mutex> lock(S->m);
     if ((int64_t)bytes > S->budget)
         return set_err(ctx, FSG_ERR_LIMIT, "request larger than the serving budget");
@@ -1539,6 +1546,8 @@ int fsg_submit(fsg_ctx *ctx, const fsg_calc *calc, const fsg_tile *tiles, int32_
     R.work = expected_work > 0. ? expected_work : (double)px;
     R.submitted = steady_seconds();
     R.bytes = bytes;
+    R.inplace = inplace;
+    if (inplace) R.td = std::move(pinned_td);
     S->queued++;
     serve_retire(ctx, S);
     serve_admit(ctx, S);

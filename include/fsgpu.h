@@ -341,7 +341,9 @@ int fsg_clear_cancel(fsg_ctx *ctx);
  *     all standard tiles) and returns its ticket at once.  The caller keeps
  *     every buffer of the tiles, and the references, alive until fsg_poll
  *     reports the request finished.  A request is admitted when a slot is
- *     free and its staged bytes fit in what the budget has left; the next one
+ *     free and its staged bytes fit in what the budget has left (a request
+ *     whose arrays are all page-locked stages nothing: the kernels read and
+ *     write them in place, as fsg_perturb_tiles does); the next one
  *     in `order` waits for that (FSG_SERVE_FIFO: arrival order;
  *     FSG_SERVE_SHORTEST: smallest expected_work first, the caller's estimate,
  *     e.g. pixels x expected iterations; <= 0 means the pixel count;
@@ -353,7 +355,8 @@ int fsg_clear_cancel(fsg_ctx *ctx);
  *     FSG_ERR_LIMIT for a request larger than the whole budget;
  *   fsg_poll: FSG_PENDING while queued or running; once finished, the
  *     request's outcome (FSG_OK, FSG_BUDGET, FSG_INTERRUPTED with the
- *     caller's arrays untouched, or an error code), its results in the
+ *     caller's arrays untouched -- for staged requests; one written in place
+ *     may hold the pixels finished before -- or an error code), its results in the
  *     caller's buffers, and the ticket released.  Polling also retires
  *     finished launches and admits queued requests: call it regularly;
  *   fsg_serve_close: waits for running requests, drops queued ones;

@@ -1055,6 +1055,22 @@ def bs_xr_cases():
         print(name + " done", flush=True)
 
 
+def bs_xr_flavor_cases():
+    """The Xrange branch (dx = 1e-305) for flavors 2, 3 and 4 (Perpendicular
+    burning ship, Shark fin, Celtic) at the centres of their FP64-branch
+    cases, whose references diverge after ~3000 iterations."""
+    mpmath.mp.dps = 340
+    for flav, x, y, name in (
+            ("Perpendicular burning ship", "-0.5710063401785717", "-0.6660741479166669",
+             "pert_bs_xr_2"),
+            ("Shark fin", "-0.6922635670582709", "-0.3510271929824563", "pert_bs_xr_3"),
+            ("Celtic", "-0.7584971274906015", "-0.8352377380482457", "pert_bs_xr_4")):
+        golden_perturb_bs(
+            os.path.join(HERE, name + ".npz"), x=x, y=y, dx="1.e-305",
+            nx=4, precision=340, max_iter=5000, flavor=flav)
+        print(name + " done", flush=True)
+
+
 def bs_xr_axis_case():
     """Burning Ship on the Xrange branch around a point of the real axis
     (-1.7548776662466927, the real map's superstable period 3): Y_n = 0 on
@@ -1073,6 +1089,8 @@ if __name__ == "__main__":
         bs_xr_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "bs_xr_axis":
         bs_xr_axis_case()
+    elif len(sys.argv) > 2 and sys.argv[2] == "bs_xr_flavors":
+        bs_xr_flavor_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "p2562":
         p2562_cases()
     elif len(sys.argv) > 2 and sys.argv[2] == "bs_flavors":

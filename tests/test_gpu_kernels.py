@@ -826,7 +826,8 @@ def test_long_orbit_paths_scan_vs_oracle(ctx, xr):
 # Burning Ship on the Xrange branch (dx = 1e-305, reference-generated): the
 # XR64 kernel against the reference's results, its Xrange Jacobian paths
 # against the oracle's; the FP32 + exponent form on the same cases
-BS_XR_CASES = ["pert_bs_xr_1", "pert_bs_xr_5", "pert_bs_xr_axis"]
+BS_XR_CASES = ["pert_bs_xr_1", "pert_bs_xr_2", "pert_bs_xr_3", "pert_bs_xr_4", "pert_bs_xr_5",
+               "pert_bs_xr_axis"]
 
 
 def _bs_xr_ref(ctx, d):

@@ -234,3 +234,46 @@ def test_queue_interruption_leaves_arrays_untouched(ctx, seahorse):
     finally:
         ctx.clear_cancel()
         ctx.serve_close()
+
+
+def test_queue_pinned_request_written_in_place(ctx, seahorse):
+    """A request whose arrays are all page-locked stages nothing on the
+    device (the kernels write it in place): its results equal the
+    synchronous call's bit for bit, and the budget reserves no bytes for it."""
+    import torch
+    from fractalshades_gb300 import _native as nat
+    from fractalshades_gb300 import synthetic as syn
+    w, ref = seahorse
+    c = nat.make_calc(max_iter=w.max_iter, M_divergence=w.M, mode="fe32", calc_dzndc=True,
+                      bla=True)
+    side = 96
+    n = side * side
+    xs, ys = syn.image_axes(side, side)
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0].copy()).dtype, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+    xs_p, ys_p = pinned(xs), pinned(ys)
+    Zf = torch.zeros((2, n, 2), dtype=torch.float64, pin_memory=True).numpy()
+    out = {"Z": Zf.view(np.complex128).reshape(2, n),
+           "sr": pinned(-np.ones(n, dtype=np.int8)), "si": pinned(np.zeros(n, dtype=np.int32)),
+           "pot": pinned(np.zeros(n)), "dem": pinned(np.zeros(n))}
+    t = nat.make_tile(xs=xs_p, ys=ys_p, lin_mat=LIN, Z=out["Z"], stop_reason=out["sr"],
+                      stop_iter=out["si"], ref=ref, dx_m=w.dx_m, dx_e=w.dx_e, drift_m=w.drift_m,
+                      drift_e=w.drift_e, i_dzndc=1, potential=out["pot"], dem=out["dem"],
+                      keep=[xs_p, ys_p])
+    ts, outs = _perturb_tile(nat, w, ref, side, (0., 0.))
+    assert ctx.perturb_tiles(c, [ts]) == nat.FSG_OK
+    ctx.serve_open(1 << 20, slots=1, order="fifo")
+    try:
+        ticket = ctx.submit(c, [t], keep=out)
+        assert ctx.serve_info()["reserved_bytes"] == 0
+        rcs, _ = _wait(ctx, [ticket])
+        assert rcs[ticket] == nat.FSG_OK
+        assert ctx.serve_info()["peak_reserved_bytes"] == 0
+    finally:
+        ctx.serve_close()
+    _same({k: v for k, v in outs.items() if not k.startswith("_")},
+          {"Z": out["Z"], "sr": out["sr"].reshape(1, n), "si": out["si"].reshape(1, n),
+           "pot": out["pot"], "dem": out["dem"]})

@@ -350,7 +350,8 @@ def test_perturb_expmap_oracle_matches_reference():
 # Burning Ship on the Xrange branch (dx = 1e-305): flavor 1 and 5 around
 # diverging references, flavor 1 on the real axis (every orbit point in the
 # side table)
-BS_XR_CASES = ["pert_bs_xr_1", "pert_bs_xr_5", "pert_bs_xr_axis"]
+BS_XR_CASES = ["pert_bs_xr_1", "pert_bs_xr_2", "pert_bs_xr_3", "pert_bs_xr_4", "pert_bs_xr_5",
+               "pert_bs_xr_axis"]
 
 
 def _xr_normal(m, e):
