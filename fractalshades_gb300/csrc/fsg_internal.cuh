@@ -257,14 +257,15 @@ __device__ __forceinline__ void fsg_epilogue(const TileDev &T, const CalcDev &C,
 // Persistent grid for a kernel: every SM filled to its occupancy limit,
 // capped by the number of blocks the work needs.  grid > 0 is kept as given.
 template <class K>
-inline int fsg_auto_grid(K kernel, int grid, int block, long long total) {
+inline int fsg_auto_grid(K kernel, int grid, int block, long long total, size_t smem = 0) {
     // grid > 0: as given; 0: one wave at the occupancy limit; -k: at most k
     // CTAs per SM
     if (grid > 0) return grid;
     int dev = 0, sms = 1, per = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess || per < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem) != cudaSuccess
+        || per < 1)
         per = 1;
     if (grid < 0 && -grid < per) per = -grid;
     long long need = (total + block - 1) / block;

@@ -612,12 +612,16 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
 // (80 registers)
 #define FE32_BLOCK 128
 template <bool INTERIOR>
+// Shared memory, sized at launch (the unified L1 keeps the rest for the orbit
+// and BLA tables): per-thread statistics (iterations, full steps, BLA steps,
+// rebases; 64-bit accumulators would hold 8 registers in the loop), then the
+// pixel offsets of the launch's tiles.
 __global__ void __launch_bounds__(FE32_BLOCK, INTERIOR ? 6 : 7) k_perturb_m2_fe32(WorkDev W, CalcDev C) {
-    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
-    // per-thread statistics (iterations, full steps, BLA steps, rebases) in
-    // shared memory: 64-bit accumulators would hold 8 registers in the loop
-    __shared__ unsigned long long s_acc[4][FE32_BLOCK];
-    for (int k = 0; k < 4; k++) s_acc[k][threadIdx.x] = 0ULL;
+    extern __shared__ unsigned long long fe32_smem[];
+    unsigned long long *acc = fe32_smem + threadIdx.x;         // acc[k * blockDim.x]
+    long long *s_start = (long long *)(fe32_smem + 4 * blockDim.x);
+    const int nb = blockDim.x;
+    for (int k = 0; k < 4; k++) acc[k * nb] = 0ULL;
     fsg_load_starts(W, s_start);
     int t; long long ip;
     while (true) {
@@ -626,22 +630,22 @@ __global__ void __launch_bounds__(FE32_BLOCK, INTERIOR ? 6 : 7) k_perturb_m2_fe3
         unsigned nfull = 0, nbla = 0, nreb = 0;
         const int n = pixel_fe32<INTERIOR>(W.tiles[t], C, ip, nfull, nbla, nreb);
         fsg_account(W, (unsigned long long)n);
-        s_acc[0][threadIdx.x] += (unsigned long long)n;
-        s_acc[1][threadIdx.x] += nfull;
-        s_acc[2][threadIdx.x] += nbla;
-        s_acc[3][threadIdx.x] += nreb;
+        acc[0] += (unsigned long long)n;
+        acc[nb] += nfull;
+        acc[2 * nb] += nbla;
+        acc[3 * nb] += nreb;
     }
-    fsg_flush_stats(W, s_acc[0][threadIdx.x], s_acc[1][threadIdx.x], s_acc[2][threadIdx.x],
-                    s_acc[3][threadIdx.x]);
+    fsg_flush_stats(W, acc[0], acc[nb], acc[2 * nb], acc[3 * nb]);
 }
 
 void fsg_launch_perturb_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
                              cudaStream_t s) {
     const int b = (block > 0 && block <= FE32_BLOCK) ? block : FE32_BLOCK;
+    const size_t smem = sizeof(unsigned long long) * (4 * (size_t)b + W.ntiles + 1);
     if (C.interior)
-        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, b, W.total - W.base), b, 0,
-                                  s>>>(W, C);
+        k_perturb_m2_fe32<true><<<fsg_auto_grid(k_perturb_m2_fe32<true>, grid, b,
+                                                W.total - W.base, smem), b, smem, s>>>(W, C);
     else
-        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, b, W.total - W.base), b, 0,
-                                   s>>>(W, C);
+        k_perturb_m2_fe32<false><<<fsg_auto_grid(k_perturb_m2_fe32<false>, grid, b,
+                                                 W.total - W.base, smem), b, smem, s>>>(W, C);
 }
