@@ -1041,7 +1041,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
 template <class T, int FL>
 __global__ void __launch_bounds__(256, IsFr<T>::value ? 3 : 1)
 k_perturb_bs(WorkDev W, CalcDev C) {
-    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    extern __shared__ long long s_start[];          // [W.ntiles + 1], sized at launch
     fsg_load_starts(W, s_start);
     unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
     int t; long long ip;

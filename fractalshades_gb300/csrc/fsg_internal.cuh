@@ -177,6 +177,9 @@ __device__ __forceinline__ bool fsg_cancelled(const WorkDev &W) {
     return false;
 }
 
+// shared memory of a kernel's tile offsets, sized at launch (dynamic)
+inline size_t fsg_starts_smem(const WorkDev &W) { return sizeof(long long) * (W.ntiles + 1); }
+
 __device__ __forceinline__ void fsg_load_starts(const WorkDev &W, long long *s_start) {
     for (int i = threadIdx.x; i <= W.ntiles; i += blockDim.x) s_start[i] = W.start[i];
     __syncthreads();

@@ -231,7 +231,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
 
 template <bool XR, bool MN, bool ORB>
 __global__ void __launch_bounds__(256) k_perturb_m2(WorkDev W, CalcDev C) {
-    __shared__ long long s_start[FSG_MAX_TILES_PER_LAUNCH + 1];
+    extern __shared__ long long s_start[];          // [W.ntiles + 1], sized at launch
     fsg_load_starts(W, s_start);
     unsigned long long nfull = 0, nbla = 0, nreb = 0, itsum = 0;
     int t; long long ip;
@@ -253,8 +253,9 @@ template __global__ void k_perturb_bs<xf, 0>(WorkDev W, CalcDev C);
 
 template <bool XR, bool MN, bool ORB>
 static void launch_m2(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    k_perturb_m2<XR, MN, ORB><<<fsg_auto_grid(k_perturb_m2<XR, MN, ORB>, grid, block, W.total - W.base),
-                                block, 0, s>>>(W, C);
+    const size_t sm = fsg_starts_smem(W);
+    k_perturb_m2<XR, MN, ORB><<<fsg_auto_grid(k_perturb_m2<XR, MN, ORB>, grid, block,
+                                              W.total - W.base, sm), block, sm, s>>>(W, C);
 }
 
 template <bool ORB>
@@ -267,12 +268,13 @@ static void launch_m2_orb(const WorkDev &W, const CalcDev &C, int grid, int bloc
 }
 
 void fsg_launch_perturb(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
+    const size_t sm = fsg_starts_smem(W);
     if (C.flavor != 0 && C.mode == 1)
-        k_perturb_bs<xf, 0><<<fsg_auto_grid(k_perturb_bs<xf, 0>, grid, block, W.total - W.base), block, 0,
-                           s>>>(W, C);
+        k_perturb_bs<xf, 0><<<fsg_auto_grid(k_perturb_bs<xf, 0>, grid, block, W.total - W.base, sm),
+                              block, sm, s>>>(W, C);
     else if (C.flavor != 0)
-        k_perturb_bs<double, 0><<<fsg_auto_grid(k_perturb_bs<double, 0>, grid, block, W.total - W.base), block, 0,
-                               s>>>(W, C);
+        k_perturb_bs<double, 0><<<fsg_auto_grid(k_perturb_bs<double, 0>, grid, block,
+                                                W.total - W.base, sm), block, sm, s>>>(W, C);
     else if (C.backshift > 0)
         launch_m2_orb<true>(W, C, grid, block, s);
     else

@@ -6,8 +6,9 @@
 
 template <int FL>
 static void launch_bs_fr(const WorkDev &W, const CalcDev &C, int grid, int block, cudaStream_t s) {
-    k_perturb_bs<fr, FL><<<fsg_auto_grid(k_perturb_bs<fr, FL>, grid, block, W.total - W.base), block, 0, s>>>(
-        W, C);
+    const size_t sm = fsg_starts_smem(W);
+    k_perturb_bs<fr, FL><<<fsg_auto_grid(k_perturb_bs<fr, FL>, grid, block, W.total - W.base, sm),
+                           block, sm, s>>>(W, C);
 }
 
 void fsg_launch_perturb_bs_fe32(const WorkDev &W, const CalcDev &C, int grid, int block,
