@@ -260,11 +260,12 @@ def supplementary(ctx, nat, syn, torch, dev, stream, flush, bs_max_iter,
             "M 1e3, Hessian, one launch")
     if "bs_edge" in legs:
         # the same centres, each tile four times its nucleus' size estimate
-        # wide (boundary-straddling: pixels escape), first 16 tiles, all forms
+        # wide (boundary-straddling: pixels escape), first 16 tiles; FP64 on
+        # a labelled subset of about a quarter of the pixels
         out["burning_ship_edge_16_tiles"] = bs_leg(
             ctx, nat, torch, dev, timed,
             syn.config4_workload(max_iter=bs_max_iter, n_tiles=16, edge=True),
-            bs_max_iter, 1.0,
+            bs_max_iter, 0.25,
             f"Burning Ship, {{n}} tiles of the 64-tile workload's first centres, each 4 x its "
             f"nucleus size estimate wide, max_iter {bs_max_iter}, M 1e3, Hessian, one launch")
     if "model_api" in legs:
