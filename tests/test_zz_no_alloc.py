@@ -178,3 +178,65 @@ def test_noalloc_rejects_too_many_tiles():
     n = nat.FSG_NOALLOC_MAX_TILES + 1
     tiles = (nat.Tile * n)()
     assert L.fsg_std_tiles_noalloc(ct.byref(calc), tiles, n, None) == nat.FSG_ERR_LIMIT
+
+
+def test_noalloc_captured_in_cuda_graph():
+    """A frame loop's use of the allocation-free call: captured once into a
+    CUDA graph (it allocates, copies and synchronises nothing: the upload
+    kernel carries the descriptors), then replayed.  Every replay equals the
+    eager call bit for bit, and a replay after the axes were rewritten in
+    place renders the new view (the graph reads the buffers, not a copy)."""
+    torch = pytest.importorskip("torch")
+    from fractalshades_gb300 import _native as nat
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    L = nat.load()
+    L.fsg_std_tiles_noalloc.argtypes = [ct.POINTER(nat.Calc), ct.POINTER(nat.Tile), ct.c_int32,
+                                        ct.c_void_p]
+    nx, ny = 256, 192
+    calc = nat.make_calc(max_iter=500, M_divergence=1000., epsilon_stationnary=0.01)
+    b, nZ = _device_case(torch, dev, nx, ny, 0)
+    tiles = (nat.Tile * 1)(_tile(nat, b, nx, ny, nZ, -0.75 + 0.1j, 0.5))
+    xs0, ys0 = b["xs"].clone(), b["ys"].clone()
+
+    def junk():
+        for k in ("Z", "pot", "dem"):
+            b[k].fill_(-7.0)
+        b["sr"].fill_(99)
+        b["si"].fill_(-1)
+
+    def eager():
+        junk()
+        s = torch.cuda.current_stream(dev)
+        rc = L.fsg_std_tiles_noalloc(ct.byref(calc), tiles, 1, ct.c_void_p(s.cuda_stream))
+        assert rc == nat.FSG_OK
+        torch.cuda.synchronize(dev)
+        return _snapshot(b)
+
+    # eager results of two views (the first call also does the set-up, before
+    # any capture); the second view is the first zoomed 4x, axes scaled in place
+    first = eager()
+    b["xs"].mul_(0.25)
+    b["ys"].mul_(0.25)
+    second = eager()
+    assert not np.array_equal(first["si"], second["si"])
+    b["xs"].copy_(xs0)
+    b["ys"].copy_(ys0)
+    torch.cuda.synchronize(dev)
+
+    g = torch.cuda.CUDAGraph()
+    rcs = []
+    with torch.cuda.graph(g):
+        s = torch.cuda.current_stream(dev)
+        rcs.append(L.fsg_std_tiles_noalloc(ct.byref(calc), tiles, 1, ct.c_void_p(s.cuda_stream)))
+    assert rcs == [nat.FSG_OK]
+
+    for expected, scale in ((first, 1.0), (first, 1.0), (second, 0.25)):
+        b["xs"].copy_(xs0 * scale)
+        b["ys"].copy_(ys0 * scale)
+        junk()
+        g.replay()
+        torch.cuda.synchronize(dev)
+        got = _snapshot(b)
+        for k in expected:
+            assert np.array_equal(got[k].view(np.uint8), expected[k].view(np.uint8)), (scale, k)
