@@ -19,6 +19,39 @@
 #define FSG_DEV __device__ __forceinline__
 
 // ---------------------------------------------------------------------------
+// double tests on the bit patterns.  GB300 issues a double compare to the
+// FP64 pipe, where it costs what a multiply costs (a warp instruction holds
+// the pipe for about 64 cycles); the forms below read the bits on the
+// integer pipes and decide exactly as the double compare does, NaN included.
+// ---------------------------------------------------------------------------
+#define FSG_D_INF_BITS 0x7ff0000000000000ULL
+FSG_DEV unsigned long long dbits(double m) { return (unsigned long long)__double_as_longlong(m); }
+// m == 0. (+0 or -0)
+FSG_DEV bool d_is0(double m) { return (dbits(m) << 1) == 0ULL; }
+// inf or NaN
+FSG_DEV bool d_nonfinite(double m) { return (dbits(m) & FSG_D_INF_BITS) == FSG_D_INF_BITS; }
+// |a| <= |b| (false when either is NaN)
+FSG_DEV bool d_abs_le(double a, double b) {
+    const unsigned long long x = dbits(a) << 1, y = dbits(b) << 1;
+    return x <= y && y <= (FSG_D_INF_BITS << 1);
+}
+// s > t and s < t for s >= +0 or NaN (a sum of squares, never -0) and t a
+// square (never -0): non-negative doubles order as their bit patterns read as
+// signed integers, and a NaN on either side (of either sign) decides false
+FSG_DEV bool d_sq_gt(double s, double t) {
+    const long long a = __double_as_longlong(s), b = __double_as_longlong(t);
+    return a > b && (unsigned long long)a <= FSG_D_INF_BITS
+           && (dbits(t) << 1) <= (FSG_D_INF_BITS << 1);
+}
+FSG_DEV bool d_sq_lt(double s, double t) {
+    const long long a = __double_as_longlong(s), b = __double_as_longlong(t);
+    return a < b && (unsigned long long)a <= FSG_D_INF_BITS
+           && (dbits(t) << 1) <= (FSG_D_INF_BITS << 1);
+}
+// a zero of the given sign
+FSG_DEV double d_zero(bool neg) { return __longlong_as_double(neg ? (long long)0x8000000000000000ULL : 0LL); }
+
+// ---------------------------------------------------------------------------
 // complex128
 // ---------------------------------------------------------------------------
 FSG_DEV double2 cx(double re, double im) { return make_double2(re, im); }
@@ -26,8 +59,21 @@ FSG_DEV double2 cadd(double2 a, double2 b) { return cx(a.x + b.x, a.y + b.y); }
 FSG_DEV double2 cmul(double2 a, double2 b) {
     return cx(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-// float * complex: promote the float to complex(x, 0.) first
-FSG_DEV double2 rmul(double s, double2 b) { return cmul(cx(s, 0.), b); }
+// float * complex: the float promoted to complex(s, 0.) first, so the product
+// is (s x - 0 y) + (s y + 0 x) i.  For finite s, x, y the products with 0 are
+// zeros whose only effect is the sign of a zero result (-0 - +0 = -0,
+// -0 + -0 = -0, any other sum of two zeros +0): two multiplies and the sign
+// rule give the same bits as the four multiplies and two additions.  Inf or
+// NaN operands take the full product, out of line: inlined, the compiler
+// evaluates both forms and selects, and the FP64 pipe pays for both.
+static __device__ __noinline__ double2 rmul_full(double s, double2 b) { return cmul(cx(s, 0.), b); }
+FSG_DEV double2 rmul(double s, double2 b) {
+    if (d_nonfinite(s) || d_nonfinite(b.x) || d_nonfinite(b.y)) return rmul_full(s, b);
+    double re = s * b.x, im = s * b.y;
+    if (d_is0(re)) re = d_zero((dbits(re) >> 63) && !(dbits(b.y) >> 63));
+    if (d_is0(im)) im = d_zero((dbits(im) >> 63) && (dbits(b.x) >> 63));
+    return cx(re, im);
+}
 FSG_DEV double2 caddr(double2 a, double s) { return cx(a.x + s, a.y + 0.); }
 
 // ---------------------------------------------------------------------------
@@ -47,7 +93,7 @@ FSG_DEV double xr_frexp(double m, int &e) {
                                             + (b & 0xfffffffffffffULL)));
 }
 FSG_DEV double xr_norm_real(double m, int exp, int &eo) {
-    if (m == 0.) { eo = 0; return m; }
+    if (d_is0(m)) { eo = 0; return m; }
     int ne; double nm = xr_frexp(m, ne);
     eo = exp + ne; return nm;
 }
@@ -68,8 +114,8 @@ FSG_DEV bool xr_need_renorm_c(double2 m) { return xr_need_renorm_r(m.x) || xr_ne
 
 FSG_DEV void xr_coexp_r(double m0, int e0, double m1, int e1, double &o0, double &o1, int &eo) {
     long long d = (long long)e0 - (long long)e1;
-    if (m0 == 0.) { eo = e1; }
-    else if (m1 == 0.) { eo = e0; }
+    if (d_is0(m0)) { eo = e1; }
+    else if (d_is0(m1)) { eo = e0; }
     else if (e1 > e0) { m0 = xr_exp2_shift(m0, d); eo = e1; }
     else if (e0 > e1) { m1 = xr_exp2_shift(m1, -d); eo = e0; }
     else { eo = e0; }
@@ -77,8 +123,8 @@ FSG_DEV void xr_coexp_r(double m0, int e0, double m1, int e1, double &o0, double
 }
 FSG_DEV void xr_coexp_c(double2 m0, int e0, double2 m1, int e1, double2 &o0, double2 &o1, int &eo) {
     long long d = (long long)e0 - (long long)e1;
-    if (m0.x == 0. && m0.y == 0.) { eo = e1; }
-    else if (m1.x == 0. && m1.y == 0.) { eo = e0; }
+    if (d_is0(m0.x) && d_is0(m0.y)) { eo = e1; }
+    else if (d_is0(m1.x) && d_is0(m1.y)) { eo = e0; }
     else if (e1 > e0) { m0 = cx(xr_exp2_shift(m0.x, d), xr_exp2_shift(m0.y, d)); eo = e1; }
     else if (e0 > e1) { m1 = cx(xr_exp2_shift(m1.x, -d), xr_exp2_shift(m1.y, -d)); eo = e0; }
     else { eo = e0; }
@@ -129,6 +175,17 @@ FSG_DEV xf xr_abs2(xc a) {
 }
 FSG_DEV bool xf_lt_s(xf a, double x) {
     double o0, o1; int e; xr_coexp_r(a.m, a.e, x, 0, o0, o1, e); return o0 < o1;
+}
+// xf_lt_s for a the Xrange sum of squares and x a square: the co-exponent
+// mantissas are >= +0 and finite there and compare on their bits; any other
+// pair (a NaN or infinite mantissa shifted into a finite one) takes the
+// double compare, out of line
+static __device__ __noinline__ bool d_lt_full(double a, double b) { return a < b; }
+FSG_DEV bool xf_sq_lt_s(xf a, double x) {
+    double o0, o1; int e; xr_coexp_r(a.m, a.e, x, 0, o0, o1, e);
+    if (dbits(o0) < FSG_D_INF_BITS && dbits(o1) < FSG_D_INF_BITS)
+        return (long long)dbits(o0) < (long long)dbits(o1);
+    return d_lt_full(o0, o1);
 }
 FSG_DEV bool xf_le(xf a, xf b) {
     double o0, o1; int e; xr_coexp_r(a.m, a.e, b.m, b.e, o0, o1, e); return o0 <= o1;
@@ -182,7 +239,7 @@ FSG_DEV double2 xr_to_std(xc a) {
 }
 // to_standard of a real Xrange record
 FSG_DEV double ldexp_d(double m, int e);
-FSG_DEV double xf_to_std(xf a) { return a.m == 0. ? 0. * a.m : ldexp_d(a.m, a.e); }
+FSG_DEV double xf_to_std(xf a) { return d_is0(a.m) ? 0. * a.m : ldexp_d(a.m, a.e); }
 
 // ldexp(m, e) with one rounding (m is in [1, 2) or a small normal number)
 FSG_DEV double ldexp_d(double m, int e) {

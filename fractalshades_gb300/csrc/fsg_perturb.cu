@@ -124,10 +124,10 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
             bool stat;
             if (XR) {
                 xc ZdZ = xr_add(xdzndz, ldx(R.dZndz_xm, R.dZndz_xe, k));
-                stat = xf_lt_s(xr_abs2(ZdZ), C.eps2);
+                stat = xf_sq_lt_s(xr_abs2(ZdZ), C.eps2);
             } else {
                 double2 ZdZ = cadd(dzndz, __ldg(&R.dZndz[k]));
-                stat = ZdZ.x * ZdZ.x + ZdZ.y * ZdZ.y < C.eps2;
+                stat = d_sq_lt(ZdZ.x * ZdZ.x + ZdZ.y * ZdZ.y, C.eps2);
             }
             if (stat) { stop = 2; break; }
         }
@@ -135,7 +135,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         double2 ref_next = __ldg(&R.Zn[w]);
         double2 ZZ = cadd(zn, ref_next);
         if (ORB) S.take(n, bs, ZZ);                                   // :1265-1273
-        if (ZZ.x * ZZ.x + ZZ.y * ZZ.y > C.M2) { stop = 1; break; }
+        if (d_sq_gt(ZZ.x * ZZ.x + ZZ.y * ZZ.y, C.M2)) { stop = 1; break; }
         // rebase when the reference diverges :1283-1313
         if (w >= div_iter - 1) {
             zn = ZZ;
@@ -160,7 +160,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
             continue;
         }
         // dynamic rebase :1317-1372, componentwise test
-        dyn = (fabs(ZZ.x) <= fabs(zn.x)) && (fabs(ZZ.y) <= fabs(zn.y));
+        dyn = d_abs_le(ZZ.x, zn.x) && d_abs_le(ZZ.y, zn.y);
         if (dyn) {
             if (XR) {
                 int slot = R.n_xr ? __ldg(&R.xr_slot[w]) : -1;

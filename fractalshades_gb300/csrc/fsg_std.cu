@@ -65,8 +65,8 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
                 dzndz = cmul(rmul(2., dzndz), zn);
                 zn = cadd(cmul(zn, zn), c);
                 if (n == 1) dzndz = cx(1., 0.);
-                if (zn.x * zn.x + zn.y * zn.y > C.M2) reason = 1;
-                else if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) reason = 2;
+                if (d_sq_gt(zn.x * zn.x + zn.y * zn.y, C.M2)) reason = 1;
+                else if (d_sq_lt(dzndz.x * dzndz.x + dzndz.y * dzndz.y, C.eps2)) reason = 2;
                 else stop = false;
             }
             if (OPT && bs > 0) S.take(n, bs, zn);
@@ -187,8 +187,8 @@ __global__ void __launch_bounds__(256) k_std_mn(WorkDev W, CalcDev C) {
                 dzndz = cmul(rmul(deg, dzndz), zm1);
                 zn = cadd(zm, c);
                 if (n == 1) dzndz = cx(1., 0.);
-                if (zn.x * zn.x + zn.y * zn.y > C.M2) reason = 1;
-                else if (dzndz.x * dzndz.x + dzndz.y * dzndz.y < C.eps2) reason = 2;
+                if (d_sq_gt(zn.x * zn.x + zn.y * zn.y, C.M2)) reason = 1;
+                else if (d_sq_lt(dzndz.x * dzndz.x + dzndz.y * dzndz.y, C.eps2)) reason = 2;
                 else stop = false;
             }
             if (OPT && bs > 0) S.take(n, bs, zn);
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(256) k_std_bs(WorkDev W, CalcDev C) {
                     nYb = 2. * (fabs(X) * sgn(Y) * dYdB + sgn(X) * dXdB * fabs(Y)) - 1.;
                 }
                 X = nX; Y = nY; dXdA = nXa; dXdB = nXb; dYdA = nYa; dYdB = nYb;
-                bool esc = X * X + Y * Y > C.M2;
+                bool esc = d_sq_gt(X * X + Y * Y, C.M2);
                 if (OPT && bs > 0) S.take(n, bs, cx(X, Y));
                 if (esc) reason = 1;
                 else stop = false;
