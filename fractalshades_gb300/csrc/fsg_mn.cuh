@@ -35,13 +35,13 @@ FSG_DEV double2 mn_ipow(double2 a, int n) {
 // df/dz: n z^(n-1) as z * z * ... * z times n (mandelbrot_Mn.py:645-652);
 // the power-2 model's 2 z when nexp = 0
 FSG_DEV double2 mn_dfdz(int nexp, double2 z) {
-    if (nexp == 0) return rmul(2., z);
+    if (nexp == 0) return rmul2(z);
     double2 t = z;
     for (int k = 2; k < nexp; k++) t = cmul(t, z);
     return rmul((double)nexp, t);
 }
 FSG_DEV xc mn_dfdz_x(int nexp, xc z) {
-    if (nexp == 0) return xr_mul_r(2., z);
+    if (nexp == 0) return xr_mul_2(z);
     xc t = z;
     for (int k = 2; k < nexp; k++) t = xr_mul(t, z);
     return xr_mul_r((double)nexp, t);

@@ -74,6 +74,26 @@ FSG_DEV double2 rmul(double s, double2 b) {
     if (d_is0(im)) im = d_zero((dbits(im) >> 63) && (dbits(b.x) >> 63));
     return cx(re, im);
 }
+// 2 x, exact, on the bits: one more in the exponent field of a normal x, the
+// magnitude shifted up for a zero or subnormal x (a carry into the exponent
+// field gives the normal result); x * 2. out of line where 2 x overflows, and
+// for inf and NaN
+static __device__ __noinline__ double d_twice_full(double x) { return x * 2.; }
+FSG_DEV double d_twice(double x) {
+    const unsigned long long b = dbits(x), e = b & FSG_D_INF_BITS;
+    const unsigned long long sign = b & 0x8000000000000000ULL;
+    if (e == 0ULL) return __longlong_as_double((long long)(sign | ((b ^ sign) << 1)));
+    if (e < (2046ULL << 52)) return __longlong_as_double((long long)(b + (1ULL << 52)));
+    return d_twice_full(x);
+}
+// rmul(2., b): the same bits, the two products taken by d_twice
+FSG_DEV double2 rmul2(double2 b) {
+    if (d_nonfinite(b.x) || d_nonfinite(b.y)) return rmul_full(2., b);
+    double re = d_twice(b.x), im = d_twice(b.y);
+    if (d_is0(re)) re = d_zero((dbits(re) >> 63) && !(dbits(b.y) >> 63));
+    if (d_is0(im)) im = d_zero((dbits(im) >> 63) && (dbits(b.x) >> 63));
+    return cx(re, im);
+}
 FSG_DEV double2 caddr(double2 a, double s) { return cx(a.x + s, a.y + 0.); }
 
 // ---------------------------------------------------------------------------
@@ -162,6 +182,12 @@ FSG_DEV xc xr_mul_s(double2 s, xc b) {
 }
 FSG_DEV xc xr_mul_r(double s, xc b) {
     double2 m = rmul(s, xm(b));
+    if (xr_need_renorm_c(m)) return xr_normalize_c(m, b.e);
+    return xc_make(m.x, m.y, b.e);
+}
+// xr_mul_r(2., b)
+FSG_DEV xc xr_mul_2(xc b) {
+    double2 m = rmul2(xm(b));
     if (xr_need_renorm_c(m)) return xr_normalize_c(m, b.e);
     return xc_make(m.x, m.y, b.e);
 }

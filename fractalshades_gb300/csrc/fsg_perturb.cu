@@ -88,11 +88,11 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
             if (XR) {
                 xc rd = dyn ? xzero : ldx(R.dZndc_xm, R.dZndc_xe, w);
                 xdzndc = MN ? mn_p_deriv_x(nexp, Cb, xzn, xdzndc, ref_zn_xr, rd)
-                            : xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndc), xr_mul(rd, xzn)));
+                            : xr_mul_2(xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndc), xr_mul(rd, xzn)));
             } else {
                 double2 rd = dyn ? cx(0., 0.) : __ldg(&R.dZndc[w]);
                 dzndc = MN ? mn_p_deriv(nexp, Cb, zn, dzndc, ref_zn, rd)
-                           : rmul(2., cadd(cmul(cadd(ref_zn, zn), dzndc), cmul(rd, zn)));
+                           : rmul2(cadd(cmul(cadd(ref_zn, zn), dzndc), cmul(rd, zn)));
             }
         }
         if (dzndz_on) {
@@ -100,19 +100,19 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
             if (XR) {
                 xc rd = ldx(R.dZndz_xm, R.dZndz_xe, k);
                 xdzndz = MN ? mn_p_deriv_x(nexp, Cb, xzn, xdzndz, ref_zn_xr, rd)
-                            : xr_mul_r(2., xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndz), xr_mul(rd, xzn)));
+                            : xr_mul_2(xr_add(xr_mul(xr_add(ref_zn_xr, xzn), xdzndz), xr_mul(rd, xzn)));
             } else {
                 double2 rd = __ldg(&R.dZndz[k]);
                 dzndz = MN ? mn_p_deriv(nexp, Cb, zn, dzndz, ref_zn, rd)
-                           : rmul(2., cadd(cmul(cadd(ref_zn, zn), dzndz), cmul(rd, zn)));
+                           : rmul2(cadd(cmul(cadd(ref_zn, zn), dzndz), cmul(rd, zn)));
             }
         }
         if (XR) {
             xzn = MN ? mn_p_zn_x(nexp, Cb, xzn, ref_zn_xr, c_xr)
-                     : xr_add(xr_mul(xzn, xr_add(xzn, xr_mul_r(2., ref_zn_xr))), c_xr);
+                     : xr_add(xr_mul(xzn, xr_add(xzn, xr_mul_2(ref_zn_xr))), c_xr);
             zn = xr_to_std(xzn);
         } else {
-            zn = MN ? mn_p_zn(nexp, Cb, zn, ref_zn, c) : cadd(cmul(zn, cadd(zn, rmul(2., ref_zn))), c);
+            zn = MN ? mn_p_zn(nexp, Cb, zn, ref_zn, c) : cadd(cmul(zn, cadd(zn, rmul2(ref_zn))), c);
         }
         w += 1;
         if (w >= order) w = w % order;

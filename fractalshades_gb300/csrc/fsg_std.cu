@@ -60,9 +60,9 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
             if (n >= C.max_iter) {
                 reason = 0;
             } else {
-                if (d2_on) d2 = rmul(2., cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
-                dzndc = caddr(cmul(rmul(2., dzndc), zn), 1.);
-                dzndz = cmul(rmul(2., dzndz), zn);
+                if (d2_on) d2 = rmul2(cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
+                dzndc = caddr(cmul(rmul2(dzndc), zn), 1.);
+                dzndz = cmul(rmul2(dzndz), zn);
                 zn = cadd(cmul(zn, zn), c);
                 if (n == 1) dzndz = cx(1., 0.);
                 if (d_sq_gt(zn.x * zn.x + zn.y * zn.y, C.M2)) reason = 1;

@@ -35,6 +35,7 @@ int main(int argc, char **argv) {
     const long cases = argc > 1 ? atol(argv[1]) : 2000000;
     const std::vector<double> special = {
         0., -0., 1., -1., 2., -2., 0.5, 3., -3., 1e-300, -1e-300, 1e-310, -1e-310,
+        2.225073858507201e-308, -2.225073858507201e-308, 8.98846567431158e307, -8.98846567431158e307,
         4.9e-324, -4.9e-324, 2.2250738585072014e-308, 1e308, -1e308, 1.7976931348623157e308,
         INFINITY, -INFINITY, NAN, -NAN};
     std::mt19937_64 g(7);
@@ -49,6 +50,12 @@ int main(int argc, char **argv) {
         const double2 f = rmul(s, make_double2(x, y)), r = promoted_product(s, make_double2(x, y));
         if (!same(f.x, r.x) || !same(f.y, r.y)) {
             if (bad++ < 5) printf("rmul(%a, %a, %a)\n", s, x, y);
+        }
+        volatile double two_x = x * 2.;
+        if (!same(d_twice(x), two_x)) { if (bad++ < 5) printf("d_twice(%a)\n", x); }
+        const double2 f2 = rmul2(make_double2(x, y)), r2 = promoted_product(2., make_double2(x, y));
+        if (!same(f2.x, r2.x) || !same(f2.y, r2.y)) {
+            if (bad++ < 5) printf("rmul2(%a, %a)\n", x, y);
         }
         if (d_is0(x) != (x == 0.)) { if (bad++ < 5) printf("d_is0(%a)\n", x); }
         if (d_nonfinite(x) != !std::isfinite(x)) { if (bad++ < 5) printf("d_nonfinite(%a)\n", x); }
