@@ -19,15 +19,15 @@
 // products, else binary powering from 1).
 FSG_DEV double2 mn_ipow(double2 a, int n) {
     if (n == 1) return a;
-    if (n == 2) return cmul(a, a);
-    if (n == 3) return cmul(a, cmul(a, a));
+    if (n == 2) return csq(a);
+    if (n == 3) return cmul(a, csq(a));
     double2 acc = cx(1., 0.), p = a;
     int mask = 1;
     for (;;) {
         if (n & mask) acc = cmul(acc, p);
         mask <<= 1;
         if (n < mask) break;
-        p = cmul(p, p);
+        p = csq(p);
     }
     return acc;
 }

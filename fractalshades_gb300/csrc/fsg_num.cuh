@@ -95,6 +95,10 @@ FSG_DEV double2 rmul2(double2 b) {
     return cx(re, im);
 }
 FSG_DEV double2 caddr(double2 a, double s) { return cx(a.x + s, a.y + 0.); }
+// cmul(a, a) without contraction (the translation units built with
+// -fmad=false): a.x a.y + a.y a.x adds one rounded product to itself, which
+// is twice that product exactly
+FSG_DEV double2 csq(double2 a) { return cx(a.x * a.x - a.y * a.y, d_twice(a.x * a.y)); }
 
 // ---------------------------------------------------------------------------
 // Xrange complex (reference semantics, numba_xr.py)
@@ -256,12 +260,26 @@ FSG_DEV double pow2d(int e) {
     if (e >= -1074) return __longlong_as_double(1LL << (e + 1074));
     return 0.;
 }
+// rmul(pow2d(k), b): where both parts are normal and stay normal the
+// product is exact and only moves the exponent fields; anything else (a zero
+// or subnormal part, a rounded or overflowing result, an inf or NaN, k out of
+// the normal powers) takes the full product, out of line
+FSG_DEV double2 rmul_p2(int k, double2 b) {
+    const unsigned long long bx = dbits(b.x), by = dbits(b.y);
+    const int ex = (int)((bx >> 52) & 0x7ff), ey = (int)((by >> 52) & 0x7ff);
+    if (k >= -1022 && k <= 1023 && ex >= 1 && ex <= 2046 && ey >= 1 && ey <= 2046
+        && ex + k >= 1 && ex + k <= 2046 && ey + k >= 1 && ey + k <= 2046) {
+        const unsigned long long sh = (unsigned long long)(long long)k << 52;
+        return cx(__longlong_as_double((long long)(bx + sh)), __longlong_as_double((long long)(by + sh)));
+    }
+    return rmul_full(pow2d(k), b);
+}
 FSG_DEV double2 xr_to_std(xc a) {
     int ere, eim;
     double nre = xr_norm_real(a.re, a.e, ere), nim = xr_norm_real(a.im, a.e, eim);
     double cr, ci; int ce;
     xr_coexp_r(nre, ere, nim, eim, cr, ci, ce);
-    return rmul(pow2d(ce), cx(cr, ci));
+    return rmul_p2(ce, cx(cr, ci));
 }
 // to_standard of a real Xrange record
 FSG_DEV double ldexp_d(double m, int e);

@@ -214,7 +214,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         double2 CC = cadd(c, __ldg(&R.Zn[1]));
         double2 zo = S.z2;
         for (int i2 = S.i2; i2 < n - bs; i2++)
-            zo = MN ? cadd(mn_ipow(zo, nexp), CC) : cadd(cmul(zo, zo), CC);
+            zo = MN ? cadd(mn_ipow(zo, nexp), CC) : cadd(csq(zo), CC);
         Z[(long long)T.i_orb * np + ip] = zo;
     }
     Z[ip] = zn;

@@ -26,7 +26,7 @@ __device__ __forceinline__ double cm_h3(double x) { return 0.5 * x * (-1. + 2. *
 // (mandelbrot_Mn.py:13-17, numpy's integer power), BS_iterate
 // (burning_ship.py:82-123)
 __device__ __forceinline__ double2 fl_map(int model, double2 z, double2 c) {
-    if (model == 0) return cadd(cmul(z, z), c);
+    if (model == 0) return cadd(csq(z), c);
     if (model > 0) return cadd(mn_ipow(z, model), c);
     double nx, ny;
     bs_map(-model, z.x, z.y, c.x, c.y, nx, ny);
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_normal(NormalDev A) {
         } else if (A.kind == 1) {
             const double2 dc = A.dzndc[j], d2 = A.d2[j];
             const double lo = log(hypot(zn.x, zn.y));
-            const double2 t1 = rmul(1. + lo, conj_(cmul(dc, dc)));
+            const double2 t1 = rmul(1. + lo, conj_(csq(dc)));
             const double2 t2 = rmul(lo, conj_(cmul(zn, d2)));
             nv = cmul(cmul(zn, dc), cx(t1.x - t2.x, t1.y - t2.y));
         } else {

@@ -60,10 +60,10 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
             if (n >= C.max_iter) {
                 reason = 0;
             } else {
-                if (d2_on) d2 = rmul2(cadd(cmul(d2, zn), cmul(dzndc, dzndc)));
+                if (d2_on) d2 = rmul2(cadd(cmul(d2, zn), csq(dzndc)));
                 dzndc = caddr(cmul(rmul2(dzndc), zn), 1.);
                 dzndz = cmul(rmul2(dzndz), zn);
-                zn = cadd(cmul(zn, zn), c);
+                zn = cadd(csq(zn), c);
                 if (n == 1) dzndz = cx(1., 0.);
                 if (d_sq_gt(zn.x * zn.x + zn.y * zn.y, C.M2)) reason = 1;
                 else if (d_sq_lt(dzndz.x * dzndz.x + dzndz.y * dzndz.y, C.eps2)) reason = 2;
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(256) k_std_m2(WorkDev W, CalcDev C) {
                 if (d2_on) Z[3 * np + ip] = d2;
                 if (OPT && bs > 0) {
                     double2 zo = S.z2;
-                    for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(cmul(zo, zo), c);   // M2_iterate
+                    for (int i2 = S.i2; i2 < n - bs; i2++) zo = cadd(csq(zo), c);   // M2_iterate
                     Z[(long long)T.i_orb * np + ip] = zo;
                 }
                 T.stop_iter[ip] = n; T.stop_reason[ip] = reason;

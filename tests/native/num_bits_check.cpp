@@ -57,6 +57,13 @@ int main(int argc, char **argv) {
         if (!same(f2.x, r2.x) || !same(f2.y, r2.y)) {
             if (bad++ < 5) printf("rmul2(%a, %a)\n", x, y);
         }
+        volatile double xx = x * x, yy = y * y, xy = x * y, yx = y * x;
+        const double2 sq2 = csq(make_double2(x, y));
+        if (!same(sq2.x, xx - yy) || !same(sq2.y, xy + yx)) { if (bad++ < 5) printf("csq(%a, %a)\n", x, y); }
+        const int k = (int)(g() % 2300) - 1150;
+        volatile double pk = pow2d(k);
+        const double2 fp = rmul_p2(k, make_double2(x, y)), rp = promoted_product(pk, make_double2(x, y));
+        if (!same(fp.x, rp.x) || !same(fp.y, rp.y)) { if (bad++ < 5) printf("rmul_p2(%d, %a, %a)\n", k, x, y); }
         if (d_is0(x) != (x == 0.)) { if (bad++ < 5) printf("d_is0(%a)\n", x); }
         if (d_nonfinite(x) != !std::isfinite(x)) { if (bad++ < 5) printf("d_nonfinite(%a)\n", x); }
         if (d_abs_le(x, y) != (std::fabs(x) <= std::fabs(y))) {
