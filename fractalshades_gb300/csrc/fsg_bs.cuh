@@ -20,25 +20,37 @@
 // every stage out, and |dz| need not be computed for the search.
 __device__ __forceinline__ bool bla_possible(const RefDev &R, int w) {
     const int i3 = 2 * (w >> FSG_STG_COMPRESSED);
-    return i3 < R.bla_len && __ldg(&R.rbla[i3]) > 0.;
+    return i3 < R.bla_len && d_sq_gt(__ldg(&R.rbla[i3]), 0.);
 }
 
-// perturbation.py:2116-2170 ref_BLA_get: returns the step (0 if none) and the
-// table index of the accepted entry.
-__device__ __forceinline__ int bla_lookup(const RefDev &R, double abs_zn, int w, int &ib) {
+// perturbation.py:2116-2170 ref_BLA_get on dz itself: returns the step (0 if
+// none) and the table index of the accepted entry.  The reference tests
+// abs(dz) < r, a hypot, against each candidate radius; abs_cmp (fsg_num.cuh)
+// gives the same answers from |dz|^2 on dz's own scale, and hypot(dz) is
+// computed (out of line) only where that leaves one open.
+static __device__ __noinline__ double bla_hypot(double x, double y) { return hypot(x, y); }
+__device__ __forceinline__ int bla_lookup_z(const RefDev &R, double2 z, int w, int &ib) {
+    const AbsScaled a = abs_scaled(z);
+    double h = -1.;              // hypot(z), once needed
     int it = w >> FSG_STG_COMPRESSED;
     int stages = FSG_STG_COMPRESSED;
-    for (int s = FSG_STG_COMPRESSED; s < R.stages; s++) {
-        stages = s;
+    for (int st = FSG_STG_COMPRESSED; st < R.stages; st++) {
+        stages = st;
         if (it & 1) break;
         it >>= 1;
     }
-    int invalid_step = R.first_invalid - w;
+    const int invalid_step = R.first_invalid - w;
     for (int stg = stages; stg >= FSG_STG_COMPRESSED; stg--) {
-        int step = 1 << stg;
+        const int step = 1 << stg;
         if (step >= invalid_step) continue;
-        int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
-        if (abs_zn < __ldg(&R.rbla[idx])) { ib = idx; return step; }
+        const int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
+        const double r = __ldg(&R.rbla[idx]);
+        int lt = abs_cmp(a, r);
+        if (lt < 0) {
+            if (h < 0.) h = bla_hypot(z.x, z.y);
+            lt = h < r;
+        }
+        if (lt) { ib = idx; return step; }
     }
     return 0;
 }
@@ -220,7 +232,7 @@ FSG_DEV bool fr_below(const fr_mod &a, fr xn, fr yn, float rm, int re, double r)
 template <class T> struct BLAGet;
 template <> struct BLAGet<double> {
     static FSG_DEV int get(const RefDev &R, double xn, double yn, int w, int &ib) {
-        return bla_possible(R, w) ? bla_lookup(R, hypot(xn, yn), w, ib) : 0;
+        return bla_possible(R, w) ? bla_lookup_z(R, cx(xn, yn), w, ib) : 0;
     }
 };
 template <> struct BLAGet<fr> {
@@ -258,7 +270,7 @@ FSG_DEV xf scale2(xf v, int k) { v.e += k; return v; }
 // below the double range, perturbation.py:1520-1527)
 template <> struct BLAGet<xf> {
     static FSG_DEV int get(const RefDev &R, xf xn, xf yn, int w, int &ib) {
-        return bla_possible(R, w) ? bla_lookup(R, hypot(xf_to_std(xn), xf_to_std(yn)), w, ib)
+        return bla_possible(R, w) ? bla_lookup_z(R, cx(xf_to_std(xn), xf_to_std(yn)), w, ib)
                                   : 0;
     }
 };

@@ -51,6 +51,54 @@ FSG_DEV bool d_sq_lt(double s, double t) {
 // a zero of the given sign
 FSG_DEV double d_zero(bool neg) { return __longlong_as_double(neg ? (long long)0x8000000000000000ULL : 0LL); }
 
+// |z| < r as hypot(z.x, z.y) < r decides it, without the hypot.  abs_scaled
+// takes |z|^2 on z's own power of two: the larger part scaled into [1, 2) on
+// its exponent bits, the other alike (dropped below 2^-1022 of it), s =
+// a^2 + b^2 in [1, 8) within 2^-51 of the true value.  abs_cmp scales r the
+// same way and compares r^2 with s: outside a margin of 256 units in the last
+// place (at least 2^-45 of the value, far beyond the roundings of s, of r^2
+// and of any hypot within a few units in the last place) the answer is
+// hypot's; inside it, and for zero, subnormal, infinite or NaN parts of z or
+// r, abs_cmp returns -1 and the caller computes hypot.
+struct AbsScaled { double s; int k; bool ok, zero; };
+FSG_DEV AbsScaled abs_scaled(double2 z) {
+    const unsigned long long MAG = 0x7fffffffffffffffULL, FRAC = 0x000fffffffffffffULL;
+    const unsigned long long ux = dbits(z.x) & MAG, uy = dbits(z.y) & MAG;
+    const unsigned long long um = ux > uy ? ux : uy, un = ux > uy ? uy : ux;
+    const int em = (int)(um >> 52), en = (int)(un >> 52);
+    AbsScaled r;
+    r.zero = um == 0ULL;
+    r.ok = em >= 1 && em <= 2046 && (un == 0ULL || (en >= 1 && en <= 2046));
+    r.s = 0.;
+    r.k = 0;
+    if (r.ok) {
+        r.k = em - 1023;
+        const double a = __longlong_as_double((long long)((um & FRAC) | (1023ULL << 52)));
+        const int eb = en - r.k;
+        const double b = (un == 0ULL || eb < 1)
+            ? 0. : __longlong_as_double((long long)((un & FRAC) | ((unsigned long long)eb << 52)));
+        r.s = a * a + b * b;
+    }
+    return r;
+}
+// 1: hypot(z) < r, 0: not, -1: open (compute hypot)
+FSG_DEV int abs_cmp(const AbsScaled &a, double r) {
+    const unsigned long long FRAC = 0x000fffffffffffffULL;
+    const unsigned long long ur = dbits(r);
+    const int er = (int)(ur >> 52) & 0x7ff;
+    if ((ur << 1) == 0ULL) return 0;                      // hypot < 0: never
+    if (a.zero) return d_sq_gt(r, 0.) ? 1 : 0;            // hypot(0) = 0 < r
+    if (!a.ok || (ur >> 63) != 0ULL || er < 1 || er > 2046) return -1;
+    const int e2 = er - a.k;
+    if (e2 < 1) return 0;                                 // r below 2^-1022 |z|
+    if (e2 > 2046) return 1;                              // r above 2^1023 |z|
+    const double rs = __longlong_as_double((long long)((ur & FRAC) | ((unsigned long long)e2 << 52)));
+    const unsigned long long sb = dbits(a.s), rb = dbits(rs * rs);
+    if (sb + 256ULL < rb) return 1;
+    if (sb > rb + 256ULL) return 0;
+    return -1;
+}
+
 // ---------------------------------------------------------------------------
 // complex128
 // ---------------------------------------------------------------------------

@@ -56,7 +56,7 @@ __device__ __forceinline__ void pixel_m2(const TileDev &T, const CalcDev &C, lon
         // BLA step :1121-1154
         if (C.bla && R.bla_len > 0 && (w & 7) == 0) {
             int ib;
-            const int step = bla_possible(R, w) ? bla_lookup(R, hypot(zn.x, zn.y), w, ib) : 0;
+            const int step = bla_possible(R, w) ? bla_lookup_z(R, zn, w, ib) : 0;
             if (step != 0) {
                 double2 A = __ldg(&R.Mbla[2 * ib]), B = __ldg(&R.Mbla[2 * ib + 1]);
                 n += step;

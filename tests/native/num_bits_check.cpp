@@ -64,6 +64,19 @@ int main(int argc, char **argv) {
         volatile double pk = pow2d(k);
         const double2 fp = rmul_p2(k, make_double2(x, y)), rp = promoted_product(pk, make_double2(x, y));
         if (!same(fp.x, rp.x) || !same(fp.y, rp.y)) { if (bad++ < 5) printf("rmul_p2(%d, %a, %a)\n", k, x, y); }
+        // |z| < r without the hypot: where abs_cmp decides, hypot's answer
+        // (radii drawn at random and within a few units of |z|)
+        {
+            const double h = std::hypot(x, y);
+            const AbsScaled as = abs_scaled(make_double2(x, y));
+            const double near = std::isfinite(h) ? h * (1. + std::ldexp((double)((long)(g() % 2001) - 1000), -52 + (int)(g() % 12))) : t;
+            for (double r : {t, std::fabs(t), near, std::nextafter(h, INFINITY), std::nextafter(h, 0.), h}) {
+                const int c = abs_cmp(as, r);
+                if (c >= 0 && c != (h < r ? 1 : 0)) {
+                    if (bad++ < 5) printf("abs_cmp(%a, %a; %a) = %d\n", x, y, r, c);
+                }
+            }
+        }
         if (d_is0(x) != (x == 0.)) { if (bad++ < 5) printf("d_is0(%a)\n", x); }
         if (d_nonfinite(x) != !std::isfinite(x)) { if (bad++ < 5) printf("d_nonfinite(%a)\n", x); }
         if (d_abs_le(x, y) != (std::fabs(x) <= std::fabs(y))) {
