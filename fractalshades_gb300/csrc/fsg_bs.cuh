@@ -152,21 +152,21 @@ template <> FSG_DEV fr from_me<fr>(double m, int e) {
     return r;
 }
 template <> FSG_DEV xf from_me<xf>(double m, int e) { return xf_make(m, e); }
-FSG_DEV bool ge0(double x) { return x >= 0.; }
+FSG_DEV bool ge0(double x) { return d_ge0(x); }
 FSG_DEV bool ge0(fr x) { return x.m >= 0.f; }
 FSG_DEV bool ge0(xf x) { return xf_ge_s(x, 0.); }
-FSG_DEV bool le0(double x) { return x <= 0.; }
+FSG_DEV bool le0(double x) { return d_le0(x); }
 FSG_DEV bool le0(fr x) { return x.m <= 0.f; }
 FSG_DEV bool le0(xf x) { return xf_le_s(x, 0.); }
-FSG_DEV double absT(double x) { return fabs(x); }
+FSG_DEV double absT(double x) { return d_abs(x); }
 FSG_DEV fr absT(fr x) { x.m = fabsf(x.m); return x; }
 FSG_DEV xf absT(xf x) { x.m = fabs(x.m); return x; }
 // sgn with 0 mapped to +1 (burning_ship.py:12-17)
-FSG_DEV double sgnT(double x) { return x < 0. ? -1. : 1.; }
+FSG_DEV double sgnT(double x) { return d_lt0(x) ? -1. : 1.; }
 FSG_DEV fr sgnT(fr x) { fr r; r.m = x.m < 0.f ? -1.f : 1.f; r.e = 0; return r; }
 FSG_DEV xf sgnT(xf x) { return xf_make(xf_lt_s(x, 0.) ? -1. : 1., 0); }
 // |a| <= |b|
-FSG_DEV bool abs_le(double a, double b) { return fabs(a) <= fabs(b); }
+FSG_DEV bool abs_le(double a, double b) { return d_abs_le(a, b); }
 FSG_DEV bool abs_le(xf a, xf b) { a.m = fabs(a.m); b.m = fabs(b.m); return xf_le(a, b); }
 FSG_DEV bool abs_le(fr a, fr b) {
     if (a.m == 0.f) return true;
@@ -342,9 +342,19 @@ template <> struct BSRef<xf> {
 };
 
 // burning_ship.py:19-60 diffabs(X, x) = |X + x| - |X| and its derivatives
+// 2. * x and 1. * x of the closures in their real type: for a double, the
+// doubling on the exponent bits and x itself (a NaN or inf takes the
+// product, out of line) -- the same bits with no FP64 instruction
+FSG_DEV double twice_t(double x) { return d_twice(x); }
+FSG_DEV fr twice_t(fr x) { return 2. * x; }
+FSG_DEV xf twice_t(xf x) { return 2. * x; }
+static __device__ __noinline__ double d_one_full(double x) { return 1. * x; }
+FSG_DEV double one_t(double x) { return d_nonfinite(x) ? d_one_full(x) : x; }
+FSG_DEV fr one_t(fr x) { return 1. * x; }
+FSG_DEV xf one_t(xf x) { return 1. * x; }
 template <class T> FSG_DEV T diffabs(T X, T x) {
-    if (ge0(X)) { if (ge0(X + x)) return 1. * x; else return -(2. * X + x); }
-    else { if (le0(X + x)) return -x; else return (2. * X + x); }
+    if (ge0(X)) { if (ge0(X + x)) return one_t(x); else return -(twice_t(X) + x); }
+    else { if (le0(X + x)) return -x; else return (twice_t(X) + x); }
 }
 template <class T> FSG_DEV T ddiffabsdX(T X, T x) {
     if (ge0(X)) { if (ge0(X + x)) return cst<T>(0.f); else return cst<T>(-2.f); }
@@ -361,22 +371,22 @@ FSG_DEV void bs_zn(int flavor, T &xn, T &yn, T X, T Y, T a, T b) {
     T nx, ny;
     if (flavor == 1) {
         T ref_xyn = X * Y;
-        nx = xn * (xn + 2. * X) - yn * (yn + 2. * Y) + a;
-        ny = 2. * diffabs(ref_xyn, xn * yn + xn * Y + yn * X) - b;
+        nx = xn * (xn + twice_t(X)) - yn * (yn + twice_t(Y)) + a;
+        ny = twice_t(diffabs(ref_xyn, xn * yn + xn * Y + yn * X)) - b;
     } else if (flavor == 2) {
-        nx = xn * (xn + 2. * X) - yn * (yn + 2. * Y) + a;
-        ny = 2. * (X * diffabs(Y, yn) + xn * absT(Y + yn)) - b;
+        nx = xn * (xn + twice_t(X)) - yn * (yn + twice_t(Y)) + a;
+        ny = twice_t(X * diffabs(Y, yn) + xn * absT(Y + yn)) - b;
     } else if (flavor == 3) {
-        nx = xn * (xn + 2. * X) - Y * diffabs(Y, yn) - yn * absT(Y + yn) + a;
-        ny = 2. * (X * yn + Y * xn + xn * yn) - b;
+        nx = xn * (xn + twice_t(X)) - Y * diffabs(Y, yn) - yn * absT(Y + yn) + a;
+        ny = twice_t(X * yn + Y * xn + xn * yn) - b;
     } else if (flavor == 4) {
         T q = X * X - Y * Y;
-        nx = diffabs(q, xn * (xn + 2. * X) - yn * (yn + 2. * Y)) + a;
-        ny = 2. * (X * yn + Y * xn + xn * yn) - b;
+        nx = diffabs(q, xn * (xn + twice_t(X)) - yn * (yn + twice_t(Y))) + a;
+        ny = twice_t(X * yn + Y * xn + xn * yn) - b;
     } else {
         T ref_xyn = X * Y, q = X * X - Y * Y;
-        nx = diffabs(q, xn * (xn + 2. * X) - yn * (yn + 2. * Y)) + a;
-        ny = 2. * diffabs(ref_xyn, xn * yn + xn * Y + yn * X) - b;
+        nx = diffabs(q, xn * (xn + twice_t(X)) - yn * (yn + twice_t(Y))) + a;
+        ny = twice_t(diffabs(ref_xyn, xn * yn + xn * Y + yn * X)) - b;
     }
     xn = nx; yn = ny;
 }
@@ -393,17 +403,17 @@ FSG_DEV void bs_hess(int flavor, T h[4], T xn, T yn, T X, T Y, T Xa, T Xb, T Ya,
         T dxa = xa * yn + xn * ya + xa * Y + xn * Ya + ya * X + yn * Xa;
         T dxb = xb * yn + xn * yb + xb * Y + xn * Yb + yb * X + yn * Xb;
         T dX = ddiffabsdX(opX, opx), dx = ddiffabsdx(opX, opx);
-        nya = 2. * (dX * dXa + dx * dxa);
-        nyb = 2. * (dX * dXb + dx * dxb);
+        nya = twice_t(dX * dXa + dx * dxa);
+        nyb = twice_t(dX * dXb + dx * dxb);
         if (flavor == 1) {
-            nxa = 2. * ((X + xn) * xa + Xa * xn) - 2. * ((Y + yn) * ya + Ya * yn);
-            nxb = 2. * ((X + xn) * xb + Xb * xn) - 2. * ((Y + yn) * yb + Yb * yn);
+            nxa = twice_t((X + xn) * xa + Xa * xn) - twice_t((Y + yn) * ya + Ya * yn);
+            nxb = twice_t((X + xn) * xb + Xb * xn) - twice_t((Y + yn) * yb + Yb * yn);
         } else {
             T opX2 = X * X - Y * Y;
-            T dXa2 = 2. * (X * Xa - Y * Ya), dXb2 = 2. * (X * Xb - Y * Yb);
-            T opx2 = xn * (xn + 2. * X) - yn * (yn + 2. * Y);
-            T dxa2 = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - ya * (yn + 2. * Y) - yn * (ya + 2. * Ya);
-            T dxb2 = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - yb * (yn + 2. * Y) - yn * (yb + 2. * Yb);
+            T dXa2 = twice_t(X * Xa - Y * Ya), dXb2 = twice_t(X * Xb - Y * Yb);
+            T opx2 = xn * (xn + twice_t(X)) - yn * (yn + twice_t(Y));
+            T dxa2 = xa * (xn + twice_t(X)) + xn * (xa + twice_t(Xa)) - ya * (yn + twice_t(Y)) - yn * (ya + twice_t(Ya));
+            T dxb2 = xb * (xn + twice_t(X)) + xn * (xb + twice_t(Xb)) - yb * (yn + twice_t(Y)) - yn * (yb + twice_t(Yb));
             T dX2 = ddiffabsdX(opX2, opx2), dx2 = ddiffabsdx(opX2, opx2);
             nxa = dX2 * dXa2 + dx2 * dxa2;
             nxb = dX2 * dXb2 + dx2 * dxb2;
@@ -411,30 +421,30 @@ FSG_DEV void bs_hess(int flavor, T h[4], T xn, T yn, T X, T Y, T Xa, T Xb, T Ya,
     } else if (flavor == 2) {
         T da = diffabs(Y, yn), dX = ddiffabsdX(Y, yn), dx = ddiffabsdx(Y, yn);
         T Yy = Y + yn, ab = absT(Yy), sg = sgnT(Yy);
-        nxa = 2. * (((X + xn) * xa + Xa * xn) - ((Y + yn) * ya + Ya * yn));
-        nxb = 2. * (((X + xn) * xb + Xb * xn) - ((Y + yn) * yb + Yb * yn));
-        nya = 2. * (Xa * da + X * (dX * Ya + dx * ya) + xa * ab + xn * sg * (Ya + ya));
-        nyb = 2. * (Xb * da + X * (dX * Yb + dx * yb) + xb * ab + xn * sg * (Yb + yb));
+        nxa = twice_t(((X + xn) * xa + Xa * xn) - ((Y + yn) * ya + Ya * yn));
+        nxb = twice_t(((X + xn) * xb + Xb * xn) - ((Y + yn) * yb + Yb * yn));
+        nya = twice_t(Xa * da + X * (dX * Ya + dx * ya) + xa * ab + xn * sg * (Ya + ya));
+        nyb = twice_t(Xb * da + X * (dX * Yb + dx * yb) + xb * ab + xn * sg * (Yb + yb));
     } else if (flavor == 3) {
         T da = diffabs(Y, yn), dX = ddiffabsdX(Y, yn), dx = ddiffabsdx(Y, yn);
         T Yy = Y + yn, ab = absT(Yy), sg = sgnT(Yy);
-        nxa = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - Ya * da - Y * (Ya * dX + ya * dx)
+        nxa = xa * (xn + twice_t(X)) + xn * (xa + twice_t(Xa)) - Ya * da - Y * (Ya * dX + ya * dx)
               - ya * ab - yn * sg * (Ya + ya);
-        nxb = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - Yb * da - Y * (Yb * dX + yb * dx)
+        nxb = xb * (xn + twice_t(X)) + xn * (xb + twice_t(Xb)) - Yb * da - Y * (Yb * dX + yb * dx)
               - yb * ab - yn * sg * (Yb + yb);
-        nya = 2. * (Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
-        nyb = 2. * (Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
+        nya = twice_t(Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
+        nyb = twice_t(Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
     } else {
         T opX = X * X - Y * Y;
-        T dXa = 2. * (X * Xa - Y * Ya), dXb = 2. * (X * Xb - Y * Yb);
-        T opx = xn * (xn + 2. * X) - yn * (yn + 2. * Y);
-        T dxa = xa * (xn + 2. * X) + xn * (xa + 2. * Xa) - ya * (yn + 2. * Y) - yn * (ya + 2. * Ya);
-        T dxb = xb * (xn + 2. * X) + xn * (xb + 2. * Xb) - yb * (yn + 2. * Y) - yn * (yb + 2. * Yb);
+        T dXa = twice_t(X * Xa - Y * Ya), dXb = twice_t(X * Xb - Y * Yb);
+        T opx = xn * (xn + twice_t(X)) - yn * (yn + twice_t(Y));
+        T dxa = xa * (xn + twice_t(X)) + xn * (xa + twice_t(Xa)) - ya * (yn + twice_t(Y)) - yn * (ya + twice_t(Ya));
+        T dxb = xb * (xn + twice_t(X)) + xn * (xb + twice_t(Xb)) - yb * (yn + twice_t(Y)) - yn * (yb + twice_t(Yb));
         T dX = ddiffabsdX(opX, opx), dx = ddiffabsdx(opX, opx);
         nxa = dX * dXa + dx * dxa;
         nxb = dX * dXb + dx * dxb;
-        nya = 2. * (Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
-        nyb = 2. * (Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
+        nya = twice_t(Xa * yn + X * ya + Ya * xn + Y * xa + xa * yn + xn * ya);
+        nyb = twice_t(Xb * yn + X * yb + Yb * xn + Y * xb + xb * yn + xn * yb);
     }
     h[0] = nxa; h[1] = nxb; h[2] = nya; h[3] = nyb;
 }
@@ -934,7 +944,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
             const double xs = to_d(xn), ys = to_d(yn);
             const double XXd = xs + Zs.x, YYd = ys + Zs.y;
             if (bs > 0) S.take(n, bs, cx(XXd, YYd));
-            if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
+            if (d_sq_gt(XXd * XXd + YYd * YYd, C.M2)) { stop = 1; break; }
             if (w >= div_iter - 1) {
                 xn = from_d<T>(XXd); yn = from_d<T>(YYd);
                 if (hess) {
@@ -944,7 +954,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
                 }
                 w = 0; nreb++; continue;
             }
-            dyn = (fabs(XXd) <= fabs(xs)) && (fabs(YYd) <= fabs(ys));
+            dyn = d_abs_le(XXd, xs) && d_abs_le(YYd, ys);
             if (dyn) {
                 T Xt, Yt;
                 const bool tab = BSRef<T>::table(R, w, Xt, Yt);
@@ -968,7 +978,7 @@ FSG_DEV void pixel_bs(const TileDev &T_, const CalcDev &C, long long ip,
         if constexpr (ORB_FORM) {
             const double XXd = to_d(XX), YYd = to_d(YY);
             if (bs > 0) S.take(n, bs, cx(XXd, YYd));             // :1641-1651
-            if (XXd * XXd + YYd * YYd > C.M2) { stop = 1; break; }
+            if (d_sq_gt(XXd * XXd + YYd * YYd, C.M2)) { stop = 1; break; }
         } else {
             if (fr_escaped(XX, YY, M2f, C.M2)) { stop = 1; break; }
         }

@@ -48,6 +48,17 @@ FSG_DEV bool d_sq_lt(double s, double t) {
     return a < b && (unsigned long long)a <= FSG_D_INF_BITS
            && (dbits(t) << 1) <= (FSG_D_INF_BITS << 1);
 }
+// x >= 0., x <= 0., x < 0. and fabs(x) on the bits (either zero is >= 0
+// and <= 0, a NaN is neither)
+FSG_DEV bool d_ge0(double x) { return dbits(x) <= FSG_D_INF_BITS || dbits(x) == 0x8000000000000000ULL; }
+FSG_DEV bool d_le0(double x) {
+    return dbits(x) == 0ULL || ((dbits(x) >> 63) && (dbits(x) << 1) <= (FSG_D_INF_BITS << 1));
+}
+FSG_DEV bool d_lt0(double x) {
+    const unsigned long long b = dbits(x);
+    return (b >> 63) && (b << 1) != 0ULL && (b << 1) <= (FSG_D_INF_BITS << 1);
+}
+FSG_DEV double d_abs(double x) { return __longlong_as_double((long long)(dbits(x) & 0x7fffffffffffffffULL)); }
 // a zero of the given sign
 FSG_DEV double d_zero(bool neg) { return __longlong_as_double(neg ? (long long)0x8000000000000000ULL : 0LL); }
 

@@ -77,6 +77,10 @@ int main(int argc, char **argv) {
                 }
             }
         }
+        if (d_ge0(x) != (x >= 0.) || d_le0(x) != (x <= 0.) || d_lt0(x) != (x < 0.)) {
+            if (bad++ < 5) printf("sign tests(%a)\n", x);
+        }
+        if (!same(d_abs(x), std::fabs(x))) { if (bad++ < 5) printf("d_abs(%a)\n", x); }
         if (d_is0(x) != (x == 0.)) { if (bad++ < 5) printf("d_is0(%a)\n", x); }
         if (d_nonfinite(x) != !std::isfinite(x)) { if (bad++ < 5) printf("d_nonfinite(%a)\n", x); }
         if (d_abs_le(x, y) != (std::fabs(x) <= std::fabs(y))) {
