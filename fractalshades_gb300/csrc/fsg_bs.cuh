@@ -28,7 +28,12 @@ __device__ __forceinline__ bool bla_possible(const RefDev &R, int w) {
 // abs(dz) < r, a hypot, against each candidate radius; abs_cmp (fsg_num.cuh)
 // gives the same answers from |dz|^2 on dz's own scale, and hypot(dz) is
 // computed (out of line) only where that leaves one open.
-static __device__ __noinline__ double bla_hypot(double x, double y) { return hypot(x, y); }
+// hypot(z) < r, with hypot(z) computed once per lookup (h < 0: not yet);
+// out of line, compare included (inlined, the FP64 form ran 1.4 % slower)
+static __device__ __noinline__ int bla_hypot_lt(double2 z, double r, double &h) {
+    if (h < 0.) h = hypot(z.x, z.y);
+    return h < r;
+}
 __device__ __forceinline__ int bla_lookup_z(const RefDev &R, double2 z, int w, int &ib) {
     const AbsScaled a = abs_scaled(z);
     double h = -1.;              // hypot(z), once needed
@@ -46,10 +51,7 @@ __device__ __forceinline__ int bla_lookup_z(const RefDev &R, double2 z, int w, i
         const int idx = 2 * (w >> FSG_STG_COMPRESSED) + ((1 << (stg - FSG_STG_COMPRESSED)) - 1);
         const double r = __ldg(&R.rbla[idx]);
         int lt = abs_cmp(a, r);
-        if (lt < 0) {
-            if (h < 0.) h = bla_hypot(z.x, z.y);
-            lt = h < r;
-        }
+        if (lt < 0) lt = bla_hypot_lt(z, r, h);
         if (lt) { ib = idx; return step; }
     }
     return 0;
