@@ -32,6 +32,8 @@ void fsg_build_paths_bs_xr(const RefDev *Rd, int len, double *pm, int *pe, doubl
 void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *Mbs, double *r,
                    int stages, double kc, double eps, cudaStream_t s);
 void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, cudaStream_t s);
+void fsg_build_fe_runs(const RefDev *Rd, int len, const int4 *Zp, const int4 *Df, int4 *runs,
+                       cudaStream_t s);
 void fsg_build_fe_tables(const RefDev *Rd, int len, int4 *Zf, const double2 *dzndc,
                          const double2 *dzndc_xm, const int *dzndc_xe, int4 *dzndc_f,
                          const double2 *dzndz, const double2 *dzndz_xm, const int *dzndz_xe,
@@ -934,7 +936,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     R.Mbla = Mbla; R.Mbla_bs = Mbs; R.rbla = rbla; R.stages = stages;
     // fe tables (M2)
     int4 *Zf = nullptr, *Zp = nullptr, *dzndc_f = nullptr, *dzndz_f = nullptr, *bla_f = nullptr,
-         *bla_first = nullptr, *bla_chain = nullptr;
+         *bla_first = nullptr, *bla_chain = nullptr, *fe_runs = nullptr;
     int *bla_first_step = nullptr;
     int2 *bla_chain_step = nullptr;
     const int bla_nit = (len >> 3) + 1;
@@ -942,6 +944,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     if (fe_tables) {
         RA(Zf, len + 1);
         RA(Zp, len + 1);
+        RA(fe_runs, 5 * (size_t)(len + 1));
         if (d->calc_dzndc) RA(dzndc_f, len + 1);
         if (d->calc_dzndz) RA(dzndz_f, len + 2);
         if (R.bla_len > 0) {
@@ -955,6 +958,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
     R.Zf = Zf; R.Zp = Zp; R.dZndc_f = dzndc_f; R.dZndz_f = dzndz_f; R.bla_f = bla_f;
     R.bla_first = bla_first; R.bla_first_step = bla_first_step; R.bla_nit = bla_nit;
     R.bla_chain = bla_chain; R.bla_chain_step = bla_chain_step;
+    R.fe_runs = fe_runs;
     // FP32+exp tables (Burning Ship)
     int4 *bs_Zf = nullptr, *bs_hf = nullptr, *bs_blaf = nullptr;
     int2 *bs_rf = nullptr;
@@ -997,6 +1001,7 @@ int fsg_ref_create(fsg_ctx *ctx, const fsg_ref_desc *d, fsg_ref **out) {
                             dzndz_xe, dzndz_f, Mbla, rbla, R.bla_len, bla_f, bla_nit, bla_first,
                             bla_first_step, d->kc, bla_chain, bla_chain_step, s);
         fsg_build_plain_orbit(r->dev, len, Zf, Zp, s);
+        fsg_build_fe_runs(r->dev, len, Zp, dzndc_f, fe_runs, s);
     }
     RCK(cudaGetLastError(), "reference table kernels");
     RCK(cudaStreamSynchronize(s), "reference table build");

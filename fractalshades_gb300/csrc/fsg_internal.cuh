@@ -56,6 +56,12 @@ struct RefDev {
     const int2 *bla_chain_step; // [bla_nit] {iterations of that run, its BLA steps}, {0, 0}
                                 // when none is stored
     int bla_nit;                // (len >> 3) + 1
+    const int4 *fe_runs;        // [5 (len + 1)] per position w, the composed map of the
+                                // fast steps from w to the next multiple of 8 (fsg_ref.cu,
+                                // k_fe_runs): {P.x, P.y, P exponent, Q exponent},
+                                // {Q.x, Q.y, R.x, R.y}, {R exponent, S exponent, S.x, S.y},
+                                // {a mantissa, a exponent, b mantissa, b exponent},
+                                // {max |2 Z|^2 bits, steps or 0 when not composable, 0, 0}
     // Burning Ship FP32+exp tables: reals as {mantissa bits, exponent} pairs
     const int4 *bs_Zf;          // [len + 1] {X, Y} (Xrange side-table values where present)
     const int4 *bs_hf;          // [2 (len + 1)] {dXa, dXb}, {dYa, dYb}

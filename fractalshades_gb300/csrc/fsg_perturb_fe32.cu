@@ -267,6 +267,7 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
     const int4 *__restrict__ bla_f = R.bla_f;
     const int4 *__restrict__ bla_first = R.bla_first;
     const int *__restrict__ bla_first_step = R.bla_first_step;
+    const int4 *__restrict__ fe_runs = R.fe_runs;
     const int4 *__restrict__ bla_chain = R.bla_chain;
     const int2 *__restrict__ bla_chain_step = R.bla_chain_step;
     // c from the pixel (perturbation.py:2214-2230) in Xrange, then fe
@@ -350,7 +351,72 @@ __device__ __forceinline__ int pixel_fe32(const TileDev &T, const CalcDev &C, lo
         // (u = 0 counts as 2^(E - 127).)  Below E = -126 the plain value of
         // dz flushes to 0, which is exact only in the |dz| < 2^-26 |Z| regime.
         const int md0 = s.E + mag_b(s) - 127;     // exponent of |dz|inf
-        if (Zc.z != FE_ZERO_E && md0 <= 100 && (Zc.z >= md0 || s.E >= -126)) {
+        const int4 *Rr = fe_runs + 5 * (size_t)w;
+        int4 T4 = make_int4(0, 0, 0, 0), T3 = T4;
+        // (the table is read only where its bound can hold: |dz| below the
+        // fast-step limit at w already)
+        if (!INTERIOR && fe_runs != nullptr && !dyn && (w & 7) != 0 && Zc.z != FE_ZERO_E
+            && Zc.z > md0) {
+            T4 = __ldg(&Rr[4]);
+            T3 = __ldg(&Rr[3]);
+        }
+        // A composed run (fsg_ref.cu, k_fe_runs): the fast steps from w to the
+        // next multiple of 8 in one, where the table's bound shows that every
+        // one of them is in the |dz| < 2^-26 |Z| regime (|U0| a + |c| b < 1/2,
+        // each term bounded by 2 max(|x|, |y|) 2^e < 2^-2), so that no rebase
+        // test could fire, and the orbit's |2 Z|^2 stays below 4 M^2 (the run's
+        // escape tests); the run must also fit before the orbit's end, the
+        // reference's divergence and max_iter, as a stepwise run would.  Only
+        // runs that start between BLA attempt points are composed (the run
+        // after the orbit's critical point); on escape-dominated views most
+        // runs start at a declined attempt, and lanes of one warp split between
+        // the two forms would run both.  The choice depends on the pixel alone.
+        if (T4.y != 0 && w + T4.y <= order && w + T4.y <= div_iter - 1 && n + T4.y <= max_iter
+            && __int_as_float(T4.x) <= M2f4 * (1.f - 0x1p-20f)
+            && fexp(__int_as_float(T3.x) * fmaxf(fabsf(s.ux), fabsf(s.uy))) + T3.y + s.E <= -3
+            && fexp(__int_as_float(T3.z) * fmaxf(fabsf(cmx), fabsf(cmy))) + T3.w + Ec <= -3) {
+            const int kt = T4.y;
+            const int4 T0 = __ldg(&Rr[0]), T1 = __ldg(&Rr[1]);
+            const float Px = __int_as_float(T0.x), Py = __int_as_float(T0.y);
+            const float Qx = __int_as_float(T1.x), Qy = __int_as_float(T1.y);
+            if (dzndc_on) {
+                // V = P V0 + R U0 + S c on the largest term's exponent (the
+                // others scaled by at most 1; below 2^-127 of it they vanish)
+                const int4 T2 = __ldg(&Rr[2]);
+                const float Rx = __int_as_float(T1.z), Ry = __int_as_float(T1.w);
+                const float Sx = __int_as_float(T2.z), Sy = __int_as_float(T2.w);
+                const int e1 = (s.F == FE_ZERO_E) ? FE_ZERO_E : s.F + T0.z;
+                const int e2 = (T2.x == FE_ZERO_E) ? FE_ZERO_E : s.E + T2.x;
+                const int e3 = (T2.y == FE_ZERO_E || dc_zero) ? FE_ZERO_E : Ec + T2.y;
+                const int Fn = max(max(e1, e2), e3);
+                if (Fn > FE_ZERO_E / 2) {
+                    const float s1 = p2f(max(e1 - Fn, -127)), s2 = p2f(max(e2 - Fn, -127));
+                    const float s3 = p2f(max(e3 - Fn, -127));
+                    const float ax = (Px * s.vx - Py * s.vy) * s1, ay = (Px * s.vy + Py * s.vx) * s1;
+                    const float bx = (Rx * s.ux - Ry * s.uy) * s2, by = (Rx * s.uy + Ry * s.ux) * s2;
+                    const float cx_ = (Sx * cmx - Sy * cmy) * s3, cy_ = (Sx * cmy + Sy * cmx) * s3;
+                    s.vx = ax + bx + cx_;
+                    s.vy = ay + by + cy_;
+                    s.F = Fn;
+                    renorm_v(s.vx, s.vy, s.F);
+                }
+            }
+            // U = P U0 + Q c, as a BLA step applies A dz + B dc
+            const int Ea = s.E + T0.z, Eb = Ec + T0.w;
+            const int En = max(max(Ea, Eb - 60), Ec - 100);
+            const float sa = __int_as_float((max(Ea - En, -127) + 127) << 23);
+            const float sb = __int_as_float((max(Eb - En, -127) + 127) << 23);
+            const float bx = (Qx * cmx - Qy * cmy) * sb, by = (Qx * cmy + Qy * cmx) * sb;
+            const float nx = fmaf(Px * s.ux - Py * s.uy, sa, bx);
+            const float ny = fmaf(Px * s.uy + Py * s.ux, sa, by);
+            s.ux = nx; s.uy = ny; s.E = En;
+            if ((unsigned)(mag_b(s) - 97) > 60u) renorm_u(s, cmx, cmy, Ec);
+            n += kt;
+            nbla++;
+            w += kt;
+            if (w >= order) w = 0;
+            dyn = false;
+        } else if (Zc.z != FE_ZERO_E && md0 <= 100 && (Zc.z >= md0 || s.E >= -126)) {
             // the run lasts up to the next event that needs the general
             // tests -- a BLA attempt (w % 8 == 0), max_iter, the reference's
             // divergence rebase, the orbit's wrap -- or until a step's tests

@@ -461,6 +461,94 @@ __global__ void k_plain_orbit(const RefDev *Rp, const int4 *Zf, int4 *Zp) {
     Zp[i] = make_int4(__float_as_int(x), __float_as_int(y), f.z - 26, 0);
 }
 
+// Composed runs of fast steps.  While |dz| < 2^-26 |Z| a fast step is affine
+// (perturbation.py:1158-1214 with the dz^2 term below FP32 resolution):
+// u' = 2Z u + c and v' = 2Z v + 2 D u (D the reference dZndc), so the k steps
+// from w to the next multiple of 8 (a BLA attempt point) compose to
+// U = P U0 + Q c and V = P V0 + R U0 + S c.  The entry also bounds the run:
+// every intermediate U_j = P_j U0 + Q_j c stays below 2^(Zp.z) (the fast-step
+// limit at w + j) when a |U0| + b |c| < 1/2, with a = max_j |P_j| 2^-Zp.z and
+// b = max_j |Q_j| 2^-Zp.z; and the largest |2 Z|^2 the run's escape tests read.
+// Products in double from the float 2Z of Zp and the fe values of dZndc (an
+// exponent kept beside the R and S mantissas).  Not composable: runs of one
+// step, past len, or through an orbit value outside the float range.
+__device__ __forceinline__ void runs_acc(double2 &m, int &e, double2 t, int te) {
+    // m 2^e += t 2^te
+    if (t.x == 0. && t.y == 0.) return;
+    if (m.x == 0. && m.y == 0.) { m = t; e = te; return; }
+    if (te > e) { m = cx(ldexp(m.x, e - te), ldexp(m.y, e - te)); e = te; }
+    else t = cx(ldexp(t.x, te - e), ldexp(t.y, te - e));
+    m = cadd(m, t);
+}
+__device__ __forceinline__ void runs_norm(double2 &m, int &e) {
+    const double a = fmax(fabs(m.x), fabs(m.y));
+    if (a == 0.) { e = FE_ZERO_E; return; }
+    int k;
+    frexp(a, &k);
+    m = cx(ldexp(m.x, -k), ldexp(m.y, -k));
+    e += k;
+}
+__device__ __forceinline__ int4 runs_pack2(double2 m, int e, int e2) {
+    return make_int4(__float_as_int((float)m.x), __float_as_int((float)m.y), e, e2);
+}
+__global__ void k_fe_runs(const RefDev *Rp, const int4 *Zp, const int4 *Df, int len, int4 *out) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w > len) return;
+    int4 *o = out + 5 * (size_t)w;
+    const int k = 8 - (w & 7);
+    bool ok = k >= 2 && w + k <= len;
+    double2 P = cx(1., 0.), Q = cx(0., 0.), Rm = cx(0., 0.), Sm = cx(0., 0.);
+    int eR = 0, eS = 0;
+    double amax = 0., bmax = 0., z2max = 0.;
+    for (int j = 0; j < k && ok; j++) {
+        const int4 z = Zp[w + j];
+        if (z.z == FE_ZERO_E) { ok = false; break; }
+        const double sc = ldexp(1., -z.z);
+        amax = fmax(amax, hypot(P.x, P.y) * sc);
+        bmax = fmax(bmax, hypot(Q.x, Q.y) * sc);
+        const double2 T = cx((double)__int_as_float(z.x), (double)__int_as_float(z.y));
+        if (j >= 1) z2max = fmax(z2max, T.x * T.x + T.y * T.y);
+        if (Df) {
+            const int4 d = Df[w + j];
+            if (d.z != FE_ZERO_E) {
+                const double2 D2 = cx(2. * (double)__int_as_float(d.x), 2. * (double)__int_as_float(d.y));
+                Rm = cmul(T, Rm);
+                Sm = cmul(T, Sm);
+                runs_acc(Rm, eR, cmul(D2, P), d.z);
+                runs_acc(Sm, eS, cmul(D2, Q), d.z);
+            } else {
+                Rm = cmul(T, Rm);
+                Sm = cmul(T, Sm);
+            }
+            runs_norm(Rm, eR);
+            if (eR == FE_ZERO_E) eR = 0;
+            runs_norm(Sm, eS);
+            if (eS == FE_ZERO_E) eS = 0;
+        }
+        P = cmul(T, P);
+        Q = cadd(cmul(T, Q), cx(1., 0.));
+    }
+    if (!ok) {
+        o[4] = make_int4(0, 0, 0, 0);
+        return;
+    }
+    int eP = 0, eQ = 0;
+    runs_norm(P, eP);
+    runs_norm(Q, eQ);
+    const bool r0 = Rm.x == 0. && Rm.y == 0., s0 = Sm.x == 0. && Sm.y == 0.;
+    o[0] = runs_pack2(P, eP, eQ);
+    o[1] = make_int4(__float_as_int((float)Q.x), __float_as_int((float)Q.y),
+                     __float_as_int((float)Rm.x), __float_as_int((float)Rm.y));
+    o[2] = make_int4(r0 ? FE_ZERO_E : eR, s0 ? FE_ZERO_E : eS,
+                     __float_as_int((float)Sm.x), __float_as_int((float)Sm.y));
+    int ea = 0, eb = 0;
+    const double ma = frexp(amax, &ea), mb = frexp(bmax, &eb);
+    // the mantissas rounded up to float: the bound stays an upper bound
+    o[3] = make_int4(__float_as_int(__double2float_ru(ma)), ea,
+                     __float_as_int(__double2float_ru(mb)), eb);
+    o[4] = make_int4(__float_as_int(__double2float_ru(z2max)), k, 0, 0);
+}
+
 __global__ void k_fe_path(const double2 *std_p, const double2 *xm, const int *xe, int n,
                           int4 *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -810,6 +898,11 @@ void fsg_build_bla(const RefDev *Rd, int flavor, int len, double2 *M2, double *M
     }
 }
 
+void fsg_build_fe_runs(const RefDev *Rd, int len, const int4 *Zp, const int4 *Df, int4 *runs,
+                       cudaStream_t s) {
+    const int tb = 128;
+    k_fe_runs<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zp, Df, len, runs);
+}
 void fsg_build_plain_orbit(const RefDev *Rd, int len, const int4 *Zf, int4 *Zp, cudaStream_t s) {
     int tb = 256;
     k_plain_orbit<<<(len + 1 + tb - 1) / tb, tb, 0, s>>>(Rd, Zf, Zp);
