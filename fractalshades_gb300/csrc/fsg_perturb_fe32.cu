@@ -27,10 +27,13 @@
 // The BLA validity test |dz| < r is |u|^2 < r^2 2^(-2E) in FP32 with the
 // exponent gap clamped (to_standard(dz), which the reference compares, is 0
 // only below every r > 0), against the FP64 radius rounded down with a
-// margin that covers the test's rounding: never a step beyond the radius.  Runs of consecutive BLA steps (each on the largest admissible
-// stage) are applied as one composite step where the composite's radius
-// admits dz (fsg_ref.cu, k_fe_bla_chain): the same iterations, the same
-// decisions, one step.
+// margin that covers the test's rounding: never a step beyond the radius.
+// Runs of consecutive BLA steps (each on the largest admissible stage) are
+// applied as one composite step where the composite's radius admits dz
+// (fsg_ref.cu, k_fe_bla_chain), and so are runs of FP32 steps between BLA
+// attempt points in the |dz| < 2^-26 |Z| regime, where a tabulated bound
+// shows that every step of the run stays there (fsg_ref.cu, k_fe_runs): the
+// same iterations, the same decisions, one step.
 #include "fsg_internal.cuh"
 
 // 2^k as a float for k in [-126, 127]; 0 below; k > 127 is clamped (callers
